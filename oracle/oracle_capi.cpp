@@ -1,0 +1,420 @@
+// CPU ORACLE — TEST INFRASTRUCTURE ONLY (see oracle_core.hpp).
+//
+// C entry points of the oracle library (oracle/_build/liboracle.so), called
+// through ctypes by the tests, by __graft_entry__.smoke() and by the CPU
+// baseline leg of bench.py.  Never linked into the product.
+#include "oracle_problems.hpp"
+
+#include <chrono>
+
+using namespace orc;
+
+extern "C"
+{
+  struct or_mesh_t
+  {
+    int      dim, degree, n_q, n_ref;
+    int      rep[3];
+    double   lo[3], hi[3];
+    int      boundary_id[6];
+    int      n_dirichlet;
+    int      dirichlet_id[8];
+    unsigned dirichlet_mask[8];
+  };
+
+  struct or_material_t
+  {
+    double mu, nu, rho, alpha_1;
+    int    formulation;
+  };
+
+  static MeshSpec
+  to_spec(const or_mesh_t *m)
+  {
+    MeshSpec s;
+    s.dim    = m->dim;
+    s.degree = m->degree;
+    s.n_q    = m->n_q;
+    s.n_ref  = m->n_ref;
+    for (int d = 0; d < 3; ++d)
+      {
+        s.rep[d] = m->rep[d];
+        s.lo[d]  = m->lo[d];
+        s.hi[d]  = m->hi[d];
+      }
+    for (int f = 0; f < 6; ++f)
+      s.boundary_id[f] = m->boundary_id[f];
+    s.n_dirichlet = m->n_dirichlet;
+    for (int i = 0; i < 8; ++i)
+      {
+        s.dirichlet_id[i]   = m->dirichlet_id[i];
+        s.dirichlet_mask[i] = m->dirichlet_mask[i];
+      }
+    return s;
+  }
+
+  static Material
+  to_mat(const or_material_t *m)
+  {
+    Material r;
+    r.mu          = m->mu;
+    r.nu          = m->nu;
+    r.rho         = m->rho;
+    r.alpha_1     = m->alpha_1;
+    r.formulation = m->formulation;
+    return r;
+  }
+
+  int
+  or_set_threads(int n)
+  {
+#ifdef _OPENMP
+    if (n > 0)
+      omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+  }
+
+  long
+  or_n_nodes(const or_mesh_t *m, int level)
+  {
+    return long(to_spec(m).box(level).n_nodes);
+  }
+
+  // basis matrices (for tests of the 1D machinery): S, G of size Q x N,
+  // nodes (N), points (Q), weights (Q)
+  int
+  or_basis(int degree, int nq, double *S, double *G, double *nodes,
+           double *xq, double *wq)
+  {
+    Basis1D b(degree, nq);
+    std::copy(b.S.begin(), b.S.end(), S);
+    std::copy(b.G.begin(), b.G.end(), G);
+    std::copy(b.nodes.begin(), b.nodes.end(), nodes);
+    std::copy(b.xq.begin(), b.xq.end(), xq);
+    std::copy(b.wq.begin(), b.wq.end(), wq);
+    return 0;
+  }
+
+  extern "C++"
+  {
+  template <typename T>
+  static int
+  heat_vmult_t(const or_mesh_t *m, int level, double k_dt, int constrained,
+               const T *src, T *dst)
+  {
+    MeshSpec   s = to_spec(m);
+    Basis1D    b(s.degree, s.n_q);
+    LevelOp<T> op;
+    op.box         = s.box(level);
+    op.basis       = &b;
+    op.nc          = 1;
+    op.kind        = op_heat;
+    op.k_dt        = k_dt;
+    op.constrained = constrained != 0;
+    op.vmult(dst, src);
+    return 0;
+  }
+  }
+
+  int
+  or_heat_vmult(const or_mesh_t *m, int level, double k_dt, int constrained,
+                int precision, const void *src, void *dst)
+  {
+    if (precision == 32)
+      return heat_vmult_t(m, level, k_dt, constrained, (const float *)src,
+                          (float *)dst);
+    return heat_vmult_t(m, level, k_dt, constrained, (const double *)src,
+                        (double *)dst);
+  }
+
+  extern "C++"
+  {
+  template <typename T>
+  static int
+  heat_invdiag_t(const or_mesh_t *m, int level, double k_dt, T *out)
+  {
+    MeshSpec   s = to_spec(m);
+    Basis1D    b(s.degree, s.n_q);
+    LevelOp<T> op;
+    op.box   = s.box(level);
+    op.basis = &b;
+    op.nc    = 1;
+    op.kind  = op_heat;
+    op.k_dt  = k_dt;
+    op.compute_diagonal();
+    std::copy(op.inv_diag.begin(), op.inv_diag.end(), out);
+    return 0;
+  }
+  }
+
+  int
+  or_heat_inv_diagonal(const or_mesh_t *m, int level, double k_dt,
+                       int precision, void *out)
+  {
+    if (precision == 32)
+      return heat_invdiag_t(m, level, k_dt, (float *)out);
+    return heat_invdiag_t(m, level, k_dt, (double *)out);
+  }
+
+  // mode: 0 vmult, 1 inverse diagonal (src ignored)
+  extern "C++"
+  {
+  template <typename T>
+  static int
+  nh_apply_t(const or_mesh_t *m, int level, const or_material_t *mat,
+             int caching, const T *u, const T *src, T *dst, int mode)
+  {
+    MeshSpec   s = to_spec(m);
+    Basis1D    b(s.degree, s.n_q);
+    LevelOp<T> op;
+    op.box        = s.box(level);
+    op.basis      = &b;
+    op.nc         = s.dim;
+    op.kind       = op_nh;
+    op.nh.mat     = to_mat(mat);
+    op.nh.caching = Caching(caching);
+    try
+      {
+        nh_cache(op.nh, op.box, b, u);
+      }
+    catch (...)
+      {
+        return -2;
+      }
+    if (!op.nh.positive_J)
+      return -3;
+    if (mode == 0)
+      op.vmult(dst, src);
+    else
+      {
+        op.compute_diagonal();
+        std::copy(op.inv_diag.begin(), op.inv_diag.end(), dst);
+      }
+    return 0;
+  }
+  }
+
+  int
+  or_nh_vmult(const or_mesh_t *m, int level, const or_material_t *mat,
+              int caching, int precision, const void *u, const void *src,
+              void *dst)
+  {
+    if (precision == 32)
+      return nh_apply_t(m, level, mat, caching, (const float *)u,
+                        (const float *)src, (float *)dst, 0);
+    return nh_apply_t(m, level, mat, caching, (const double *)u,
+                      (const double *)src, (double *)dst, 0);
+  }
+
+  int
+  or_nh_inv_diagonal(const or_mesh_t *m, int level, const or_material_t *mat,
+                     int caching, int precision, const void *u, void *out)
+  {
+    if (precision == 32)
+      return nh_apply_t(m, level, mat, caching, (const float *)u,
+                        (const float *)nullptr, (float *)out, 1);
+    return nh_apply_t(m, level, mat, caching, (const double *)u,
+                      (const double *)nullptr, (double *)out, 1);
+  }
+
+  // transfer between level (coarse) and level+1; op: 0 prolongate
+  // (fine = P coarse), 1 restrict (coarse += P^T fine), 2 interpolate
+  // (coarse = fine at coarse nodes)
+  int
+  or_transfer(const or_mesh_t *m, int coarse_level, int nc, int op,
+              double *coarse, double *fine)
+  {
+    MeshSpec              s = to_spec(m);
+    Basis1D               b(s.degree, s.n_q);
+    Box                   bc = s.box(coarse_level), bf = s.box(coarse_level + 1);
+    LevelTransfer<double> t(b, bc, bf, nc);
+    if (op == 0)
+      t.prolongate(fine, coarse);
+    else if (op == 1)
+      t.restrict_add(coarse, fine);
+    else
+      t.interpolate(coarse, fine);
+    return 0;
+  }
+
+  struct or_solid_params_t
+  {
+    or_mesh_t     mesh;
+    or_material_t mat;
+    int           caching, precond;
+    double        relaxation, tol_lin;
+    int           max_it_mult, max_newton;
+    double        tol_f, tol_f_abs, tol_u, tol_u_abs;
+    double        dt;
+    int           n_steps;
+    double        body_force[3];
+    int           traction_id;
+    double        traction[3];
+    double        watch[3];
+    int           cheb_degree;
+    double        cheb_range;
+    int           cheb_eig_its, coarse_accurate, mg_float;
+  };
+
+  struct or_solid_result_t
+  {
+    int    newton_its[64];
+    double watch_disp[64][3];
+    long   total_cg;
+    int    n_solves, n_steps, ok;
+    double seconds;
+  };
+
+  int
+  or_solid_run(const or_solid_params_t *p, or_solid_result_t *r,
+               double *u_out)
+  {
+    SolidParams P;
+    P.mesh            = to_spec(&p->mesh);
+    P.mat             = to_mat(&p->mat);
+    P.caching         = p->caching;
+    P.precond         = p->precond;
+    P.relaxation      = p->relaxation;
+    P.tol_lin         = p->tol_lin;
+    P.max_it_mult     = p->max_it_mult;
+    P.max_newton      = p->max_newton;
+    P.tol_f           = p->tol_f;
+    P.tol_f_abs       = p->tol_f_abs;
+    P.tol_u           = p->tol_u;
+    P.tol_u_abs       = p->tol_u_abs;
+    P.dt              = p->dt;
+    P.n_steps         = p->n_steps;
+    P.traction_id     = p->traction_id;
+    P.cheb_degree     = p->cheb_degree;
+    P.cheb_range      = p->cheb_range;
+    P.cheb_eig_its    = p->cheb_eig_its;
+    P.coarse_accurate = p->coarse_accurate;
+    P.mg_float        = p->mg_float;
+    for (int d = 0; d < 3; ++d)
+      {
+        P.body_force[d] = p->body_force[d];
+        P.traction[d]   = p->traction[d];
+        P.watch[d]      = p->watch[d];
+      }
+    SolidResult R;
+    auto        t0 = std::chrono::steady_clock::now();
+    try
+      {
+        if (P.mg_float)
+          {
+            SolidDriver<float> drv(P);
+            drv.run(R);
+            if (u_out)
+              std::copy(drv.last_u.begin(), drv.last_u.end(), u_out);
+          }
+        else
+          {
+            SolidDriver<double> drv(P);
+            drv.run(R);
+            if (u_out)
+              std::copy(drv.last_u.begin(), drv.last_u.end(), u_out);
+          }
+      }
+    catch (...)
+      {
+        return -1;
+      }
+    auto t1 = std::chrono::steady_clock::now();
+    std::memset(r, 0, sizeof(*r));
+    for (int i = 0; i < 64; ++i)
+      {
+        r->newton_its[i] = R.newton_its[i];
+        for (int d = 0; d < 3; ++d)
+          r->watch_disp[i][d] = R.watch_disp[i][d];
+      }
+    r->total_cg = R.total_cg;
+    r->n_solves = R.n_solves;
+    r->n_steps  = R.n_steps;
+    r->ok       = R.ok;
+    r->seconds  = std::chrono::duration<double>(t1 - t0).count();
+    return R.ok ? 0 : -3;
+  }
+
+  struct or_heat_params_t
+  {
+    or_mesh_t mesh;
+    double    dt;
+    int       n_steps;
+    double    tol_rel;
+    int       precond, analytic;
+    double    alpha, beta;
+    int       n_gauss;
+    double    g_center[8][3];
+    double    g_width[8];
+    double    g_amp[8];
+    int       mg_float;
+  };
+
+  struct or_heat_result_t
+  {
+    double l2_error[64];
+    int    cg_its[64];
+    int    n_steps;
+    double seconds;
+  };
+
+  int
+  or_heat_run(const or_heat_params_t *p, or_heat_result_t *r, double *u_out)
+  {
+    HeatParams P;
+    P.mesh     = to_spec(&p->mesh);
+    P.dt       = p->dt;
+    P.n_steps  = p->n_steps;
+    P.tol_rel  = p->tol_rel;
+    P.precond  = p->precond;
+    P.analytic = p->analytic;
+    P.alpha    = p->alpha;
+    P.beta     = p->beta;
+    P.n_gauss  = p->n_gauss;
+    P.mg_float = p->mg_float;
+    for (int i = 0; i < 8; ++i)
+      {
+        for (int d = 0; d < 3; ++d)
+          P.g_center[i][d] = p->g_center[i][d];
+        P.g_width[i] = p->g_width[i];
+        P.g_amp[i]   = p->g_amp[i];
+      }
+    HeatResult R;
+    auto       t0 = std::chrono::steady_clock::now();
+    try
+      {
+        if (P.mg_float)
+          {
+            HeatDriver<float> drv(P);
+            drv.run(R);
+            if (u_out)
+              std::copy(drv.solution.begin(), drv.solution.end(), u_out);
+          }
+        else
+          {
+            HeatDriver<double> drv(P);
+            drv.run(R);
+            if (u_out)
+              std::copy(drv.solution.begin(), drv.solution.end(), u_out);
+          }
+      }
+    catch (...)
+      {
+        return -1;
+      }
+    auto t1 = std::chrono::steady_clock::now();
+    std::memset(r, 0, sizeof(*r));
+    for (int i = 0; i < 64; ++i)
+      {
+        r->l2_error[i] = R.l2_error[i];
+        r->cg_its[i]   = R.cg_its[i];
+      }
+    r->n_steps = R.n_steps;
+    r->seconds = std::chrono::duration<double>(t1 - t0).count();
+    return 0;
+  }
+}
