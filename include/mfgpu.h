@@ -1,0 +1,273 @@
+/*
+ * mfgpu.h — C-ABI of the GB300 matrix-free library (libmfgpu.so).
+ *
+ * A drop-in for the reference's CPU MatrixFree path
+ * (davidscn/matrix-free-dealii-precice): the neo-Hookean tangent operator
+ * (NeoHookOperator, include/solid_mechanics/mf_nh_operator.h:103-173), the
+ * backward-Euler heat operator (LaplaceOperator,
+ * include/heat_transfer/heat_transfer.h:81-127), the Chebyshev-smoothed
+ * geometric multigrid V-cycle with its transfers, the CG solver and the
+ * Newton-Newmark / backward-Euler drivers.
+ *
+ * Conventions
+ *   - Every function returns an int status: MFGPU_OK (0) or an error code;
+ *     mfgpu_last_error() returns a message for the calling thread.
+ *   - Vectors are device pointers (double* for precision 64, float* for 32)
+ *     of length m() = n_components * n_nodes, component-blocked:
+ *     dof = component * n_nodes + node, nodes numbered lexicographically
+ *     (x fastest) on the Q_p Gauss-Lobatto node grid of the level.
+ *   - Meshes are boxes [lower, upper] with repetitions[d] coarse cells per
+ *     direction, refined n_refinements times (subdivided_hyper_rectangle +
+ *     refine_global, as the reference's cases build them); level L has
+ *     repetitions[d] * 2^L cells per direction; level -1 means the finest.
+ *   - Box faces are numbered x-, x+, y-, y+, z-, z+ (deal.II colorize
+ *     numbering); boundary_id[f] gives each face's boundary id and the
+ *     Dirichlet list maps boundary ids to component masks.
+ *   - Objects are bound to the CUDA stream of their context; they are
+ *     thread-compatible (one thread per object at a time).
+ */
+#ifndef MFGPU_H
+#define MFGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MFGPU_OK 0
+#define MFGPU_ERR_ARG 1
+#define MFGPU_ERR_CUDA 2
+#define MFGPU_ERR_OOM 3
+#define MFGPU_ERR_NONFINITE 4
+#define MFGPU_ERR_NOT_CONVERGED 5
+#define MFGPU_ERR_STATE 6
+#define MFGPU_ERR_DET_F 7
+#define MFGPU_ERR_UNSUPPORTED 8
+#define MFGPU_ERR_TIMEOUT 9
+
+typedef struct mfgpu_context mfgpu_context;
+typedef struct mfgpu_operator mfgpu_operator;
+typedef struct mfgpu_mg mfgpu_mg;
+typedef struct mfgpu_solid mfgpu_solid;
+typedef struct mfgpu_heat mfgpu_heat;
+
+typedef struct mfgpu_mesh
+{
+  int      degree;         /* FE_Q degree p, 1..6                    */
+  int      n_q_1d;         /* Gauss points per direction (== p + 1)  */
+  int      n_refinements;  /* global refinements of the coarse box   */
+  int      repetitions[3]; /* coarse cells per direction             */
+  double   lower[3];
+  double   upper[3];
+  int      boundary_id[6];    /* per box face x-,x+,y-,y+,z-,z+      */
+  int      n_dirichlet;       /* entries used in the two lists below */
+  int      dirichlet_id[8];   /* boundary ids with Dirichlet data     */
+  unsigned dirichlet_mask[8]; /* component mask per boundary id       */
+} mfgpu_mesh;
+
+/* Material_Compressible_Neo_Hook_One_Field(mu, nu, rho, alpha_1,
+ * formulation), include/solid_mechanics/material.h:78-94 */
+typedef struct mfgpu_material
+{
+  double mu;
+  double nu;
+  double rho;
+  double alpha_1; /* 1 / (beta dt^2) of the Newmark scheme */
+  int    formulation;
+} mfgpu_material;
+
+/* ---------------------------------------------------------------- */
+/* library / context                                                 */
+/* ---------------------------------------------------------------- */
+const char *mfgpu_last_error(void);
+int         mfgpu_version(void);
+/* number of kernel launches issued by this process so far */
+long long mfgpu_launch_count(void);
+
+/* context: one CUDA device + one stream + reduction scratch */
+int mfgpu_context_create(int device, mfgpu_context **ctx);
+int mfgpu_context_destroy(mfgpu_context *ctx);
+int mfgpu_context_synchronize(mfgpu_context *ctx);
+/* the cudaStream_t of the context, as void* */
+int mfgpu_context_stream(mfgpu_context *ctx, void **stream);
+
+/* copy bytes between any two host/device buffers on the context's stream
+ * (unified addressing), then synchronize the stream */
+int mfgpu_copy(mfgpu_context *ctx, void *dst, const void *src, size_t bytes);
+
+/* number of nodes of a level (dofs = n_components * nodes) */
+int mfgpu_mesh_n_nodes(const mfgpu_mesh *mesh, int level, size_t *n_nodes);
+
+/* ---------------------------------------------------------------- */
+/* operators                                                         */
+/* ---------------------------------------------------------------- */
+
+/* LaplaceOperator<3,number>: MatrixFreeOperators::Base API
+ * (heat_transfer.h:81-127).  constrained = 0 builds the operator without
+ * constraints (the reference's inhomogeneous_operator, heat_transfer.h:484-495). */
+int mfgpu_heat_operator_create(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                               int level, int precision, int constrained,
+                               mfgpu_operator **op);
+/* LaplaceOperator::set_delta_t (heat_transfer.h:101-105) */
+int mfgpu_heat_operator_set_delta_t(mfgpu_operator *op, double delta_t);
+/* LaplaceOperator::evaluate_coefficient (heat_transfer.h:150-166) with the
+ * reference's constant Coefficient (heat_transfer.h:63-71) */
+int mfgpu_heat_operator_evaluate_coefficient(mfgpu_operator *op,
+                                             double coefficient);
+
+/* NeoHookOperator<3,Number> (mf_nh_operator.h:103-173).  caching is one of
+ * "scalar_referential", "tensor2", "tensor4", "tensor4_ns" (the reference's
+ * MF caching options, parameter_handling.h:231-235) or "referential_qp",
+ * a referential cache of F^{-T} and mu - 2 lambda ln J per quadrature point. */
+int mfgpu_nh_operator_create(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                             int level, int precision, const char *caching,
+                             mfgpu_operator **op);
+/* NeoHookOperator::set_material (mf_nh_operator.h:529-539); the inclusion
+ * material may be NULL (all cells carry material id 0) */
+int mfgpu_nh_operator_set_material(mfgpu_operator *op,
+                                   const mfgpu_material *material,
+                                   const mfgpu_material *inclusion);
+/* NeoHookOperator::initialize (mf_nh_operator.h:333-388): registers the
+ * linearisation displacement (device pointer of the operator's precision,
+ * NOT owned; keep it alive while the operator is used) */
+int mfgpu_nh_operator_initialize(mfgpu_operator *op, const void *displacement);
+/* NeoHookOperator::cache (mf_nh_operator.h:394-523); MFGPU_ERR_DET_F if
+ * det F <= 0 at a quadrature point */
+int mfgpu_nh_operator_cache(mfgpu_operator *op);
+
+/* vmult / vmult_add / Tvmult / Tvmult_add (mf_nh_operator.h:545-625 and
+ * MatrixFreeOperators::Base::vmult): dst = A src with constrained rows
+ * dst = src */
+int mfgpu_operator_vmult(mfgpu_operator *op, void *dst, const void *src);
+int mfgpu_operator_vmult_add(mfgpu_operator *op, void *dst, const void *src);
+int mfgpu_operator_Tvmult(mfgpu_operator *op, void *dst, const void *src);
+int mfgpu_operator_Tvmult_add(mfgpu_operator *op, void *dst, const void *src);
+/* vmult with HOST buffers: copies src in, applies, copies dst out */
+int mfgpu_operator_vmult_host(mfgpu_operator *op, void *dst_host,
+                              const void *src_host);
+/* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
+int mfgpu_operator_compute_diagonal(mfgpu_operator *op);
+/* get_matrix_diagonal_inverse: device pointer owned by the operator */
+int mfgpu_operator_get_matrix_diagonal_inverse(mfgpu_operator *op,
+                                               const void **inv_diag);
+/* el(row, col): diagonal entries only (mf_nh_operator.h:1066-1073) */
+int mfgpu_operator_el(mfgpu_operator *op, size_t row, size_t col,
+                      double *value);
+/* precondition_Jacobi (mf_nh_operator.h:283-291): dst = omega D^{-1} src */
+int mfgpu_operator_precondition_jacobi(mfgpu_operator *op, void *dst,
+                                       const void *src, double omega);
+/* m(), n() */
+int mfgpu_operator_m(mfgpu_operator *op, size_t *m);
+/* memory_consumption (mf_nh_operator.h:243-260): cache bytes */
+int mfgpu_operator_memory_consumption(mfgpu_operator *op, size_t *bytes);
+/* clear (mf_nh_operator.h:315-327) */
+int mfgpu_operator_clear(mfgpu_operator *op);
+int mfgpu_operator_destroy(mfgpu_operator *op);
+
+/* ---------------------------------------------------------------- */
+/* multigrid transfer between level and level+1 (MGTransferMatrixFree) */
+/* ---------------------------------------------------------------- */
+/* fine = P coarse */
+int mfgpu_transfer_prolongate(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                              int coarse_level, int n_components,
+                              int precision, const void *coarse, void *fine);
+/* coarse += P^T fine */
+int mfgpu_transfer_restrict_add(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                                int coarse_level, int n_components,
+                                int precision, void *coarse, const void *fine);
+/* coarse = fine field evaluated at the coarse nodes (interpolate_to_mg) */
+int mfgpu_transfer_interpolate(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                               int coarse_level, int n_components,
+                               int precision, void *coarse, const void *fine);
+
+/* ---------------------------------------------------------------- */
+/* drivers                                                           */
+/* ---------------------------------------------------------------- */
+typedef struct mfgpu_solver_params
+{
+  int    preconditioner;  /* 0 none, 1 jacobi, 2 gmg                        */
+  double relaxation;      /* Jacobi relaxation                              */
+  double tol;             /* relative CG tolerance                          */
+  int    max_it_mult;     /* max CG iterations = n_dofs * multiplier        */
+  int    cheb_degree;     /* Chebyshev degree on levels > 0                 */
+  double cheb_range;      /* smoothing range on levels > 0                  */
+  int    cheb_eig_its;    /* CG iterations for the eigenvalue estimate      */
+  int    coarse_accurate; /* level 0: eigenvalue CG iterations = m()        */
+  int    mg_precision;    /* 32: FP32 level operators, 64: all-FP64 V-cycle */
+  int    coarse_fp64;     /* level-0 Chebyshev solve in FP64                */
+} mfgpu_solver_params;
+
+typedef struct mfgpu_solid_params
+{
+  mfgpu_mesh          mesh;
+  mfgpu_material      material; /* alpha_1 is set from dt */
+  const char         *caching;
+  mfgpu_solver_params solver;
+  int                 max_newton;
+  double              tol_f, tol_f_abs, tol_u, tol_u_abs;
+  double              dt;
+  int                 n_steps;
+  double              body_force[3];
+  int                 traction_id;
+  double              traction[3];
+  double              watch[3];
+} mfgpu_solid_params;
+
+typedef struct mfgpu_solid_result
+{
+  int    newton_its[64];
+  double watch_disp[64][3];
+  long   total_cg;
+  int    n_solves;
+  int    n_steps;
+  double seconds;
+} mfgpu_solid_result;
+
+/* Solid<3,double>::run with the coupling replaced by a constant traction */
+int mfgpu_solid_create(mfgpu_context *ctx, const mfgpu_solid_params *p,
+                       mfgpu_solid **s);
+int mfgpu_solid_run(mfgpu_solid *s, mfgpu_solid_result *r);
+/* final displacement (device pointer owned by the solver) */
+int mfgpu_solid_displacement(mfgpu_solid *s, const double **u);
+/* one linear system of the Newton loop: linearise at u (device), solve
+ * K du = rhs (device) to tol * |rhs|; returns the CG iteration count */
+int mfgpu_solid_linear_solve(mfgpu_solid *s, const double *u,
+                             const double *rhs, double *du, int *iterations,
+                             double *seconds);
+int mfgpu_solid_destroy(mfgpu_solid *s);
+
+typedef struct mfgpu_heat_params
+{
+  mfgpu_mesh          mesh;
+  double              dt;
+  int                 n_steps;
+  mfgpu_solver_params solver;
+  int                 analytic; /* 1: u = 1 + x^2 + alpha y^2 + beta t */
+  double              alpha, beta;
+  int                 n_gauss; /* source = sum of Gaussians */
+  double              g_center[8][3];
+  double              g_width[8];
+  double              g_amp[8];
+} mfgpu_heat_params;
+
+typedef struct mfgpu_heat_result
+{
+  int    cg_its[64];
+  int    n_steps;
+  double seconds;
+} mfgpu_heat_result;
+
+/* LaplaceProblem<3>::run with the coupling replaced by Dirichlet data */
+int mfgpu_heat_create(mfgpu_context *ctx, const mfgpu_heat_params *p,
+                      mfgpu_heat **h);
+int mfgpu_heat_run(mfgpu_heat *h, mfgpu_heat_result *r);
+int mfgpu_heat_solution(mfgpu_heat *h, const double **u);
+int mfgpu_heat_destroy(mfgpu_heat *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MFGPU_H */

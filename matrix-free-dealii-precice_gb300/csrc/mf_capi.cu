@@ -1,0 +1,601 @@
+// extern "C" entry points of libmfgpu.so (declared in include/mfgpu.h).
+// Every entry point converts exceptions into a status code and a
+// per-thread error message.
+#include <chrono>
+#include <cstring>
+#include <string>
+
+#include "../../include/mfgpu.h"
+#include "mf_drivers.h"
+
+using namespace mfgpu;
+
+struct mfgpu_context
+{
+  std::unique_ptr<Context> c;
+};
+
+struct mfgpu_operator
+{
+  std::unique_ptr<Operator> op;
+  mfgpu_context            *ctx;
+  DevBuf                    hsrc, hdst; // device staging for the host-buffer vmult
+};
+
+struct mfgpu_solid
+{
+  std::unique_ptr<SolidDriver> d;
+};
+
+struct mfgpu_heat
+{
+  std::unique_ptr<HeatDriver> d;
+};
+
+static thread_local std::string g_last_error;
+
+template <typename F>
+static int
+guarded(F &&f)
+{
+  try
+    {
+      f();
+      return MFGPU_OK;
+    }
+  catch (const Error &e)
+    {
+      g_last_error = e.what();
+      return e.code;
+    }
+  catch (const std::exception &e)
+    {
+      g_last_error = e.what();
+      return MFGPU_ERR_ARG;
+    }
+  catch (...)
+    {
+      g_last_error = "unknown exception";
+      return MFGPU_ERR_ARG;
+    }
+}
+
+static void
+need(const void *p, const char *what)
+{
+  if (!p)
+    throw Error(ERR_ARG, std::string("null argument: ") + what);
+}
+
+extern "C"
+{
+  const char *
+  mfgpu_last_error(void)
+  {
+    return g_last_error.c_str();
+  }
+
+  int
+  mfgpu_version(void)
+  {
+    return 100;
+  }
+
+  long long
+  mfgpu_launch_count(void)
+  {
+    return launch_count();
+  }
+
+  int
+  mfgpu_context_create(int device, mfgpu_context **ctx)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      auto *c = new mfgpu_context();
+      try
+        {
+          c->c.reset(new Context(device));
+        }
+      catch (...)
+        {
+          delete c;
+          throw;
+        }
+      *ctx = c;
+    });
+  }
+
+  int
+  mfgpu_context_destroy(mfgpu_context *ctx)
+  {
+    return guarded([&] { delete ctx; });
+  }
+
+  int
+  mfgpu_context_synchronize(mfgpu_context *ctx)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      ctx->c->sync();
+    });
+  }
+
+  int
+  mfgpu_context_stream(mfgpu_context *ctx, void **stream)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(stream, "stream");
+      *stream = (void *)ctx->c->stream;
+    });
+  }
+
+  int
+  mfgpu_copy(mfgpu_context *ctx, void *dst, const void *src, size_t bytes)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      if (bytes == 0)
+        return;
+      need(dst, "dst");
+      need(src, "src");
+      MF_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, ctx->c->stream));
+      ctx->c->sync();
+    });
+  }
+
+  int
+  mfgpu_mesh_n_nodes(const mfgpu_mesh *mesh, int level, size_t *n_nodes)
+  {
+    return guarded([&] {
+      need(mesh, "mesh");
+      need(n_nodes, "n_nodes");
+      *n_nodes = to_mesh(*mesh).level(level).n_nodes;
+    });
+  }
+
+  int
+  mfgpu_heat_operator_create(mfgpu_context *ctx, const mfgpu_mesh *mesh, int level,
+                             int precision, int constrained, mfgpu_operator **op)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(mesh, "mesh");
+      need(op, "op");
+      auto *o = new mfgpu_operator();
+      try
+        {
+          o->op  = make_heat(ctx->c.get(), to_mesh(*mesh), level, precision, constrained != 0);
+          o->ctx = ctx;
+        }
+      catch (...)
+        {
+          delete o;
+          throw;
+        }
+      *op = o;
+    });
+  }
+
+  static HeatOperator *
+  as_heat(mfgpu_operator *op)
+  {
+    need(op, "op");
+    auto *h = dynamic_cast<HeatOperator *>(op->op.get());
+    if (!h)
+      throw Error(ERR_ARG, "not a heat operator");
+    return h;
+  }
+
+  static NHOperator *
+  as_nh(mfgpu_operator *op)
+  {
+    need(op, "op");
+    auto *h = dynamic_cast<NHOperator *>(op->op.get());
+    if (!h)
+      throw Error(ERR_ARG, "not a neo-Hookean operator");
+    return h;
+  }
+
+  int
+  mfgpu_heat_operator_set_delta_t(mfgpu_operator *op, double delta_t)
+  {
+    return guarded([&] {
+      if (!(delta_t > 0))
+        throw Error(ERR_ARG, "delta_t must be positive");
+      as_heat(op)->delta_t = delta_t;
+    });
+  }
+
+  int
+  mfgpu_heat_operator_evaluate_coefficient(mfgpu_operator *op, double coefficient)
+  {
+    return guarded([&] { as_heat(op)->coefficient = coefficient; });
+  }
+
+  int
+  mfgpu_nh_operator_create(mfgpu_context *ctx, const mfgpu_mesh *mesh, int level,
+                           int precision, const char *caching, mfgpu_operator **op)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(mesh, "mesh");
+      need(op, "op");
+      const int var = parse_caching(caching);
+      auto     *o   = new mfgpu_operator();
+      try
+        {
+          o->op  = make_nh(ctx->c.get(), to_mesh(*mesh), level, precision, var);
+          o->ctx = ctx;
+        }
+      catch (...)
+        {
+          delete o;
+          throw;
+        }
+      *op = o;
+    });
+  }
+
+  int
+  mfgpu_nh_operator_set_material(mfgpu_operator *op, const mfgpu_material *material,
+                                 const mfgpu_material *inclusion)
+  {
+    return guarded([&] {
+      need(material, "material");
+      (void)inclusion; // every cell carries material id 0 on box meshes
+      NHOperator *h    = as_nh(op);
+      h->mat           = make_material(material->mu, material->nu, material->rho, material->alpha_1);
+      h->formulation   = material->formulation;
+      if (h->formulation != 0 && h->formulation != 1)
+        throw Error(ERR_ARG, "Unknown material formulation");
+      h->have_material = true;
+      h->cached        = false;
+    });
+  }
+
+  int
+  mfgpu_nh_operator_initialize(mfgpu_operator *op, const void *displacement)
+  {
+    return guarded([&] {
+      need(displacement, "displacement");
+      NHOperator *h = as_nh(op);
+      h->u          = displacement;
+      h->cached     = false;
+    });
+  }
+
+  int
+  mfgpu_nh_operator_cache(mfgpu_operator *op)
+  {
+    return guarded([&] { as_nh(op)->do_cache(); });
+  }
+
+  int
+  mfgpu_operator_vmult(mfgpu_operator *op, void *dst, const void *src)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(dst, "dst");
+      need(src, "src");
+      op->op->vmult(dst, src);
+    });
+  }
+
+  int
+  mfgpu_operator_vmult_add(mfgpu_operator *op, void *dst, const void *src)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(dst, "dst");
+      need(src, "src");
+      op->op->vmult_add(dst, src);
+    });
+  }
+
+  int
+  mfgpu_operator_Tvmult(mfgpu_operator *op, void *dst, const void *src)
+  {
+    return mfgpu_operator_vmult(op, dst, src);
+  }
+
+  int
+  mfgpu_operator_Tvmult_add(mfgpu_operator *op, void *dst, const void *src)
+  {
+    return mfgpu_operator_vmult_add(op, dst, src);
+  }
+
+  int
+  mfgpu_operator_vmult_host(mfgpu_operator *op, void *dst_host, const void *src_host)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(dst_host, "dst");
+      need(src_host, "src");
+      Operator    *o     = op->op.get();
+      const size_t bytes = o->m() * o->elem_size();
+      if (op->hsrc.bytes != bytes)
+        {
+          op->hsrc.alloc(bytes);
+          op->hdst.alloc(bytes);
+        }
+      cudaStream_t s = o->ctx->stream;
+      MF_CK(cudaMemcpyAsync(op->hsrc.ptr, src_host, bytes, cudaMemcpyHostToDevice, s));
+      o->vmult(op->hdst.ptr, op->hsrc.ptr);
+      MF_CK(cudaMemcpyAsync(dst_host, op->hdst.ptr, bytes, cudaMemcpyDeviceToHost, s));
+      MF_CK(cudaStreamSynchronize(s));
+    });
+  }
+
+  int
+  mfgpu_operator_compute_diagonal(mfgpu_operator *op)
+  {
+    return guarded([&] {
+      need(op, "op");
+      op->op->compute_diagonal();
+    });
+  }
+
+  int
+  mfgpu_operator_get_matrix_diagonal_inverse(mfgpu_operator *op, const void **inv_diag)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(inv_diag, "inv_diag");
+      if (!op->op->diag_ready)
+        throw Error(ERR_STATE, "compute_diagonal() first");
+      *inv_diag = op->op->inv_diag.ptr;
+    });
+  }
+
+  int
+  mfgpu_operator_el(mfgpu_operator *op, size_t row, size_t col, double *value)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(value, "value");
+      if (row != col)
+        throw Error(ERR_UNSUPPORTED, "el(): only diagonal entries are available");
+      Operator *o = op->op.get();
+      if (!o->diag_ready)
+        throw Error(ERR_STATE, "compute_diagonal() first");
+      if (row >= o->m())
+        throw Error(ERR_ARG, "row out of range");
+      if (o->precision == 32)
+        {
+          float v;
+          MF_CK(cudaMemcpyAsync(&v, o->diag.as<float>() + row, 4, cudaMemcpyDeviceToHost, o->ctx->stream));
+          o->ctx->sync();
+          *value = v;
+        }
+      else
+        {
+          MF_CK(cudaMemcpyAsync(value, o->diag.as<double>() + row, 8, cudaMemcpyDeviceToHost, o->ctx->stream));
+          o->ctx->sync();
+        }
+    });
+  }
+
+  int
+  mfgpu_operator_precondition_jacobi(mfgpu_operator *op, void *dst, const void *src, double omega)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(dst, "dst");
+      need(src, "src");
+      Operator *o = op->op.get();
+      if (!o->diag_ready)
+        throw Error(ERR_STATE, "compute_diagonal() first");
+      if (o->precision == 32)
+        vec_scale<float>(*o->ctx, o->m(), float(omega), o->inv_diag.as<float>(), (const float *)src, (float *)dst);
+      else
+        vec_scale<double>(*o->ctx, o->m(), omega, o->inv_diag.as<double>(), (const double *)src, (double *)dst);
+    });
+  }
+
+  int
+  mfgpu_operator_m(mfgpu_operator *op, size_t *m)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(m, "m");
+      *m = op->op->m();
+    });
+  }
+
+  int
+  mfgpu_operator_memory_consumption(mfgpu_operator *op, size_t *bytes)
+  {
+    return guarded([&] {
+      need(op, "op");
+      need(bytes, "bytes");
+      *bytes = op->op->memory_consumption();
+    });
+  }
+
+  int
+  mfgpu_operator_clear(mfgpu_operator *op)
+  {
+    return guarded([&] {
+      need(op, "op");
+      op->op->clear();
+    });
+  }
+
+  int
+  mfgpu_operator_destroy(mfgpu_operator *op)
+  {
+    return guarded([&] {
+      if (op && op->op)
+        op->op->ctx->sync();
+      delete op;
+    });
+  }
+
+  static int
+  transfer_call(mfgpu_context *ctx, const mfgpu_mesh *mesh, int coarse_level, int nc,
+                int precision, const void *in, void *out, int mode)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(mesh, "mesh");
+      need(in, "input");
+      need(out, "output");
+      const Mesh m = to_mesh(*mesh);
+      if (coarse_level < 0 || coarse_level + 1 > m.n_ref)
+        throw Error(ERR_ARG, "coarse_level must be in [0, n_refinements)");
+      if (precision != 32 && precision != 64)
+        throw Error(ERR_ARG, "precision must be 32 or 64");
+      HostBasis b;
+      make_host_basis(m.degree, b);
+      Transfer t(ctx->c.get(), b, m.level(coarse_level), m.level(coarse_level + 1), nc, precision);
+      if (mode == 0)
+        t.prolongate(out, in);
+      else if (mode == 1)
+        t.restrict_add(out, in);
+      else
+        t.interpolate(out, in);
+      ctx->c->sync();
+    });
+  }
+
+  int
+  mfgpu_transfer_prolongate(mfgpu_context *ctx, const mfgpu_mesh *mesh, int coarse_level,
+                            int n_components, int precision, const void *coarse, void *fine)
+  {
+    return transfer_call(ctx, mesh, coarse_level, n_components, precision, coarse, fine, 0);
+  }
+
+  int
+  mfgpu_transfer_restrict_add(mfgpu_context *ctx, const mfgpu_mesh *mesh, int coarse_level,
+                              int n_components, int precision, void *coarse, const void *fine)
+  {
+    return transfer_call(ctx, mesh, coarse_level, n_components, precision, fine, coarse, 1);
+  }
+
+  int
+  mfgpu_transfer_interpolate(mfgpu_context *ctx, const mfgpu_mesh *mesh, int coarse_level,
+                             int n_components, int precision, void *coarse, const void *fine)
+  {
+    return transfer_call(ctx, mesh, coarse_level, n_components, precision, fine, coarse, 2);
+  }
+
+  int
+  mfgpu_solid_create(mfgpu_context *ctx, const mfgpu_solid_params *p, mfgpu_solid **s)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(p, "params");
+      need(s, "solid");
+      auto *o = new mfgpu_solid();
+      try
+        {
+          o->d.reset(new SolidDriver(ctx->c.get(), *p));
+        }
+      catch (...)
+        {
+          delete o;
+          throw;
+        }
+      *s = o;
+    });
+  }
+
+  int
+  mfgpu_solid_run(mfgpu_solid *s, mfgpu_solid_result *r)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(r, "result");
+      s->d->run(*r);
+    });
+  }
+
+  int
+  mfgpu_solid_displacement(mfgpu_solid *s, const double **u)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(u, "u");
+      *u = s->d->u.as<double>();
+    });
+  }
+
+  int
+  mfgpu_solid_linear_solve(mfgpu_solid *s, const double *u, const double *rhs, double *du,
+                           int *iterations, double *seconds)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(u, "u");
+      need(rhs, "rhs");
+      need(du, "du");
+      SolidDriver *d = s->d.get();
+      d->update_operators(u);
+      const size_t n  = d->fine->m();
+      const double nb = std::sqrt(vec_dot<double>(*d->ctx, n, rhs, rhs));
+      d->ctx->sync();
+      auto      t0  = std::chrono::steady_clock::now();
+      const int its = d->solve_linear(rhs, du, d->P.solver.tol * nb);
+      d->ctx->sync();
+      if (iterations)
+        *iterations = its;
+      if (seconds)
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+  }
+
+  int
+  mfgpu_solid_destroy(mfgpu_solid *s)
+  {
+    return guarded([&] { delete s; });
+  }
+
+  int
+  mfgpu_heat_create(mfgpu_context *ctx, const mfgpu_heat_params *p, mfgpu_heat **h)
+  {
+    return guarded([&] {
+      need(ctx, "ctx");
+      need(p, "params");
+      need(h, "heat");
+      auto *o = new mfgpu_heat();
+      try
+        {
+          o->d.reset(new HeatDriver(ctx->c.get(), *p));
+        }
+      catch (...)
+        {
+          delete o;
+          throw;
+        }
+      *h = o;
+    });
+  }
+
+  int
+  mfgpu_heat_run(mfgpu_heat *h, mfgpu_heat_result *r)
+  {
+    return guarded([&] {
+      need(h, "heat");
+      need(r, "result");
+      h->d->run(*r);
+    });
+  }
+
+  int
+  mfgpu_heat_solution(mfgpu_heat *h, const double **u)
+  {
+    return guarded([&] {
+      need(h, "heat");
+      need(u, "u");
+      *u = h->d->sol.as<double>();
+    });
+  }
+
+  int
+  mfgpu_heat_destroy(mfgpu_heat *h)
+  {
+    return guarded([&] { delete h; });
+  }
+}

@@ -1,0 +1,796 @@
+// Sum-factorization cell kernels for sm_103a.
+//
+// One thread block takes CPB cells; every cell gets N*N threads (N = p+1).
+// Thread (a,b) of a cell owns one line of N points in each 1D sweep: x-lines
+// at (y=a,z=b), y-lines at (x=a,z=b), z-lines at (x=a,y=b).  A sweep loads its
+// line from shared memory (or registers), applies an N x N matrix with the
+// matrix entries read from the kernel's constant parameter bank (uniform
+// across the warp), and stores the line.  The gather reads z-columns straight
+// from global memory into registers (the first sweep runs in registers), and
+// the scatter adds z-columns from registers with atomics.
+//
+// Evaluation uses deal.II's collocation scheme: interpolate the Gauss-Lobatto
+// nodal values to the Gauss points with S (3 sweeps), then differentiate on
+// the Gauss points with the collocation matrix D (3 sweeps); integration is
+// the transpose.  This is what FEEvaluation::evaluate / integrate compute for
+// n_q = p+1 (call sites include/solid_mechanics/mf_nh_operator.h:697,1018 and
+// include/heat_transfer/heat_transfer.h:241,249).
+#pragma once
+
+#include "mf_common.cuh"
+
+namespace mfgpu
+{
+  template <typename T>
+  __device__ __forceinline__ T
+  fma_(T a, T b, T c)
+  {
+    return fma(a, b, c);
+  }
+
+  // out[r] = sum_k M[r][k] in[k]
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  mat_apply(const T *__restrict__ M, const T (&in)[N], T (&out)[N])
+  {
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      {
+        T s = M[r * N] * in[0];
+#pragma unroll
+        for (int k = 1; k < N; ++k)
+          s = fma_(M[r * N + k], in[k], s);
+        out[r] = s;
+      }
+  }
+
+  // out[k] = sum_r M[r][k] in[r]
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  mat_apply_t(const T *__restrict__ M, const T (&in)[N], T (&out)[N])
+  {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      {
+        T s = M[k] * in[0];
+#pragma unroll
+        for (int r = 1; r < N; ++r)
+          s = fma_(M[r * N + k], in[r], s);
+        out[k] = s;
+      }
+  }
+
+  // out[k] += sum_r M[r][k] in[r]
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  mat_apply_t_add(const T *__restrict__ M, const T (&in)[N], T (&out)[N])
+  {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      {
+        T s = out[k];
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+          s = fma_(M[r * N + k], in[r], s);
+        out[k] = s;
+      }
+  }
+
+  template <int N>
+  __device__ __forceinline__ int
+  line_base(int dir, int a, int b)
+  {
+    return dir == 0 ? (a * N + b * N * N) : (dir == 1 ? (a + b * N * N) : (a + b * N));
+  }
+
+  template <int N>
+  __host__ __device__ constexpr int
+  line_stride(int dir)
+  {
+    return dir == 0 ? 1 : (dir == 1 ? N : N * N);
+  }
+
+  template <int N, typename T, int DIR>
+  __device__ __forceinline__ void
+  load_line(const T *buf, int a, int b, T (&x)[N])
+  {
+    const int base = line_base<N>(DIR, a, b);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      x[i] = buf[base + i * line_stride<N>(DIR)];
+  }
+
+  template <int N, typename T, int DIR>
+  __device__ __forceinline__ void
+  store_line(T *buf, int a, int b, const T (&x)[N])
+  {
+    const int base = line_base<N>(DIR, a, b);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      buf[base + i * line_stride<N>(DIR)] = x[i];
+  }
+
+  // Cells per block for a degree / number of components / precision: aim
+  // at 100-256 threads and <= ~100 KB of shared memory.
+  template <int N, int NC, typename T>
+  __host__ __device__ constexpr int
+  cells_per_block()
+  {
+    return N == 2 ? 32 :
+           N == 3 ? 16 :
+           N == 4 ? 8 :
+           N == 5 ? (NC == 1 ? 8 : (sizeof(T) == 8 ? 4 : 8)) :
+           N == 6 ? (NC == 1 ? 4 : (sizeof(T) == 8 ? 2 : 4)) :
+                    (NC == 1 ? 4 : 2);
+  }
+
+  // shared memory per cell (in elements of T): NC*(value + 3 gradients)
+  // + 2 scratch arrays + (optional) 3*NC gradients of the linearisation
+  template <int N, int NC, bool EVAL_U>
+  __host__ __device__ constexpr int
+  smem_per_cell()
+  {
+    return (NC * 4 + 2 + (EVAL_U ? 3 * NC : 0)) * N * N * N;
+  }
+
+  // ---------------------------------------------------------------------
+  // Evaluate values and reference gradients (at the Gauss points) of one
+  // scalar field whose z-columns are in registers.  Writes V, G0, G1, G2.
+  // Requires a __syncthreads() before V/G are read by other threads.
+  // ---------------------------------------------------------------------
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  evaluate_field(const Shape<N, T> &sh, const T (&col)[N], T *V, T *G0, T *G1,
+                 T *G2, T *T0, T *T1, int a, int b, bool want_values)
+  {
+    T x[N], y[N];
+    // z interpolation in registers, store z-line (x=a, y=b)
+    mat_apply<N>(sh.S, col, y);
+    store_line<N, T, 2>(T0, a, b, y);
+    __syncthreads();
+    // y interpolation: line (x=a, z=b)
+    load_line<N, T, 1>(T0, a, b, x);
+    mat_apply<N>(sh.S, x, y);
+    store_line<N, T, 1>(T1, a, b, y);
+    __syncthreads();
+    // x interpolation: line (y=a, z=b) -> values; x-derivative from registers
+    load_line<N, T, 0>(T1, a, b, x);
+    mat_apply<N>(sh.S, x, y);
+    if (want_values)
+      store_line<N, T, 0>(V, a, b, y);
+    mat_apply<N>(sh.D, y, x);
+    store_line<N, T, 0>(G0, a, b, x);
+    if (!want_values)
+      store_line<N, T, 0>(V, a, b, y); // V needed for the y/z derivatives
+    __syncthreads();
+    // y and z derivatives of the values
+    load_line<N, T, 1>(V, a, b, x);
+    mat_apply<N>(sh.D, x, y);
+    store_line<N, T, 1>(G1, a, b, y);
+    load_line<N, T, 2>(V, a, b, x);
+    mat_apply<N>(sh.D, x, y);
+    store_line<N, T, 2>(G2, a, b, y);
+  }
+
+  // ---------------------------------------------------------------------
+  // Integrate: nodal result = S^T (V + D^T G) in 3D, returned as the
+  // z-column (x=a, y=b) in registers.  V is overwritten.  Starts with a
+  // __syncthreads() so that the submitted values of all threads are visible.
+  // ---------------------------------------------------------------------
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  integrate_field(const Shape<N, T> &sh, T *V, const T *G0, const T *G1,
+                  const T *G2, T *T0, T *T1, int a, int b, bool has_values,
+                  bool has_gradients, T (&col)[N])
+  {
+    T x[N], y[N];
+    __syncthreads();
+    if (has_gradients)
+      {
+        // z: V += D^T G2 on z-line (x=a,y=b)
+        load_line<N, T, 2>(G2, a, b, x);
+        if (has_values)
+          load_line<N, T, 2>(V, a, b, y);
+        else
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            y[i] = T(0);
+        mat_apply_t_add<N>(sh.D, x, y);
+        store_line<N, T, 2>(V, a, b, y);
+        __syncthreads();
+        // y: V += D^T G1 on y-line (x=a,z=b)
+        load_line<N, T, 1>(G1, a, b, x);
+        load_line<N, T, 1>(V, a, b, y);
+        mat_apply_t_add<N>(sh.D, x, y);
+        store_line<N, T, 1>(V, a, b, y);
+        __syncthreads();
+        // x: t = V + D^T G0 on x-line (y=a,z=b); then S^T
+        load_line<N, T, 0>(G0, a, b, x);
+        load_line<N, T, 0>(V, a, b, y);
+        mat_apply_t_add<N>(sh.D, x, y);
+      }
+    else
+      load_line<N, T, 0>(V, a, b, y);
+    mat_apply_t<N>(sh.S, y, x);
+    store_line<N, T, 0>(T0, a, b, x);
+    __syncthreads();
+    load_line<N, T, 1>(T0, a, b, x);
+    mat_apply_t<N>(sh.S, x, y);
+    store_line<N, T, 1>(T1, a, b, y);
+    __syncthreads();
+    load_line<N, T, 2>(T1, a, b, x);
+    mat_apply_t<N>(sh.S, x, col);
+  }
+
+  // node index of local node (a, b, k) of cell (cx,cy,cz)
+  template <typename T>
+  __device__ __forceinline__ size_t
+  node_index(const CellGeom<T> &g, int cx, int cy, int cz, int a, int b, int k)
+  {
+    return size_t(cx * g.p + a) +
+           size_t(g.Nn[0]) * (size_t(cy * g.p + b) + size_t(g.Nn[1]) * size_t(cz * g.p + k));
+  }
+
+  template <typename T>
+  __device__ __forceinline__ unsigned
+  node_mask_g(const CellGeom<T> &g, int ix, int iy, int iz)
+  {
+    return node_mask(g.face_mask, g.Nn, ix, iy, iz);
+  }
+
+  // ---------------------------------------------------------------------
+  // Generic operator application kernel:
+  //   dst += sum_cells  integrate( QOp( evaluate( gather(src) ) ) )
+  // with homogeneous constraints applied on gather/scatter when CONSTRAINED.
+  //
+  // QOp interface:
+  //   static constexpr bool eval_u;        // evaluate gradients of cached u
+  //   const T* ucell;                       // cell-local u values if eval_u
+  //   __device__ void operator()(unsigned cell, int q, T (&v)[NC],
+  //                              T (&H)[NC][3], const T (*Hu)[3]) const;
+  // v and H arrive as the values and REAL gradients at quadrature point q and
+  // leave as the submitted value and flux (before JxW).
+  // ---------------------------------------------------------------------
+  template <int N, typename T, int NC, class QOp, bool CONSTRAINED>
+  __global__ void __launch_bounds__(cells_per_block<N, NC, T>() * N * N)
+  cell_apply_kernel(const __grid_constant__ Shape<N, T> sh,
+                    const __grid_constant__ CellGeom<T> g, const QOp op,
+                    const T *__restrict__ src, T *__restrict__ dst)
+  {
+    constexpr int N2  = N * N;
+    constexpr int N3  = N * N * N;
+    constexpr int CPB = cells_per_block<N, NC, T>();
+    constexpr int SPC = smem_per_cell<N, NC, QOp::eval_u>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+
+    const int      lc     = threadIdx.x / N2;
+    const int      l      = threadIdx.x - lc * N2;
+    const int      a      = l % N;
+    const int      b      = l / N;
+    const unsigned cell   = blockIdx.x * CPB + lc;
+    const bool     active = cell < g.n_cells;
+    T             *cb     = sm + lc * SPC;
+    T             *T0     = cb + NC * 4 * N3;
+    T             *T1     = T0 + N3;
+    T             *GU     = T1 + N3; // 3*NC*N3 if eval_u
+
+    const unsigned cc  = active ? cell : 0u;
+    const int      cx  = int(cc % unsigned(g.C[0]));
+    const int      cyz = int(cc / unsigned(g.C[0]));
+    const int      cy  = cyz % g.C[1];
+    const int      cz  = cyz / g.C[1];
+
+    // -------- gather + evaluate ------------------------------------------
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c)
+      {
+        T col[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          {
+            T val = T(0);
+            if (active)
+              {
+                const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
+                const size_t node =
+                  size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+                bool skip = false;
+                if (CONSTRAINED)
+                  skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
+                if (!skip)
+                  val = __ldg(src + size_t(c) * g.n_nodes + node);
+              }
+            col[k] = val;
+          }
+        T *V = cb + c * 4 * N3;
+        evaluate_field<N>(sh, col, V, V + N3, V + 2 * N3, V + 3 * N3, T0, T1, a,
+                          b, true);
+      }
+    if constexpr (QOp::eval_u)
+      {
+        // gradients of the cached linearisation values (cell-local layout)
+#pragma unroll 1
+        for (int c = 0; c < NC; ++c)
+          {
+            T col[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              col[k] = active ? op.ucell[(size_t(cc) * NC + c) * N3 + a + b * N + k * N2] : T(0);
+            // reuse the value slot of T1 as V scratch: write values to a
+            // scratch area (GU + c*3*N3 holds the 3 gradients)
+            T *Gc = GU + c * 3 * N3;
+            __syncthreads();
+            evaluate_field<N>(sh, col, T1, Gc, Gc + N3, Gc + 2 * N3, T0, T1, a,
+                              b, false);
+          }
+      }
+    __syncthreads();
+
+    // -------- quadrature-point operation ---------------------------------
+    if (active)
+      {
+        const T wab = sh.w[a] * sh.w[b] * g.vol;
+#pragma unroll 1
+        for (int k = 0; k < N; ++k)
+          {
+            const int q = a + b * N + k * N2;
+            T         v[NC];
+            T         H[NC][3];
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+              {
+                const T *V = cb + c * 4 * N3;
+                v[c]       = V[q];
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                  H[c][d] = V[(d + 1) * N3 + q] * g.inv_h[d];
+              }
+            T Hu[NC][3];
+            if constexpr (QOp::eval_u)
+              {
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+#pragma unroll
+                  for (int d = 0; d < 3; ++d)
+                    Hu[c][d] = GU[(c * 3 + d) * N3 + q] * g.inv_h[d];
+              }
+            op(cell, q, v, H, Hu);
+            const T jxw = wab * sh.w[k];
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+              {
+                T *V = cb + c * 4 * N3;
+                V[q] = v[c] * jxw;
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                  V[(d + 1) * N3 + q] = H[c][d] * (jxw * g.inv_h[d]);
+              }
+          }
+      }
+
+    // -------- integrate + scatter ----------------------------------------
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c)
+      {
+        T *V = cb + c * 4 * N3;
+        T  col[N];
+        integrate_field<N>(sh, V, V + N3, V + 2 * N3, V + 3 * N3, T0, T1, a, b,
+                           true, true, col);
+        if (active)
+          {
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              {
+                const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
+                if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
+                  continue;
+                const size_t node =
+                  size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+                atomicAdd(dst + size_t(c) * g.n_nodes + node, col[k]);
+              }
+          }
+      }
+  }
+
+  // ---------------------------------------------------------------------
+  // quadrature-point operations
+  // ---------------------------------------------------------------------
+
+  // heat: mass + dt*k*Laplace (heat_transfer.h:242-248)
+  template <typename T>
+  struct HeatQOp
+  {
+    static constexpr bool eval_u = false;
+    const T              *ucell  = nullptr;
+    T                     kdt;
+    __device__ __forceinline__ void
+    operator()(unsigned, int, T (&)[1], T (&H)[1][3], const T (*)[3]) const
+    {
+      H[0][0] *= kdt;
+      H[0][1] *= kdt;
+      H[0][2] *= kdt;
+    }
+  };
+
+  // neo-Hookean material constants (material.h:78-94)
+  template <typename T>
+  struct NHMat
+  {
+    T mu, lambda, rho_alpha, kappa, c_1;
+  };
+
+  // scalar_referential (mf_nh_operator.h:848-943): F from the gradient of the
+  // cached cell-local displacement, c = mu - 2 lambda ln J cached per qp.
+  template <typename T>
+  struct NHScalarRefQOp
+  {
+    static constexpr bool eval_u = true;
+    const T              *ucell;  // [cell][3][N^3]
+    const T              *scalar; // [cell][N^3]
+    NHMat<T>              m;
+    int                   n3;
+    __device__ __forceinline__ void
+    operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
+               const T (*Hu)[3]) const
+    {
+      T F[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          F[i][j] = Hu[i][j] + (i == j ? T(1) : T(0));
+      const T c = scalar[size_t(cell) * n3 + q];
+      // tau = mu F F^T - c I
+      T tau[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            T s = F[i][0] * F[j][0];
+            s   = fma_(F[i][1], F[j][1], s);
+            s   = fma_(F[i][2], F[j][2], s);
+            tau[i][j] = m.mu * s - (i == j ? c : T(0));
+          }
+      // F^{-1}
+      const T c00 = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+      const T c01 = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+      const T c02 = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+      const T det = F[0][0] * c00 + F[0][1] * c01 + F[0][2] * c02;
+      const T id  = T(1) / det;
+      T       Fi[3][3];
+      Fi[0][0] = c00 * id;
+      Fi[1][0] = c01 * id;
+      Fi[2][0] = c02 * id;
+      Fi[0][1] = (F[0][2] * F[2][1] - F[0][1] * F[2][2]) * id;
+      Fi[1][1] = (F[0][0] * F[2][2] - F[0][2] * F[2][0]) * id;
+      Fi[2][1] = (F[0][1] * F[2][0] - F[0][0] * F[2][1]) * id;
+      Fi[0][2] = (F[0][1] * F[1][2] - F[0][2] * F[1][1]) * id;
+      Fi[1][2] = (F[0][2] * F[1][0] - F[0][0] * F[1][2]) * id;
+      Fi[2][2] = (F[0][0] * F[1][1] - F[0][1] * F[1][0]) * id;
+      // g = H F^{-1}
+      T gg[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            T s = H[i][0] * Fi[0][j];
+            s   = fma_(H[i][1], Fi[1][j], s);
+            s   = fma_(H[i][2], Fi[2][j], s);
+            gg[i][j] = s;
+          }
+      const T tr = gg[0][0] + gg[1][1] + gg[2][2];
+      T       qd[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            T s = gg[i][0] * tau[0][j];
+            s   = fma_(gg[i][1], tau[1][j], s);
+            s   = fma_(gg[i][2], tau[2][j], s);
+            qd[i][j] = c * (gg[i][j] + gg[j][i]) + (i == j ? T(2) * m.lambda * tr : T(0)) + s;
+          }
+      // P = qd F^{-T}
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            T s = qd[i][0] * Fi[j][0];
+            s   = fma_(qd[i][1], Fi[j][1], s);
+            s   = fma_(qd[i][2], Fi[j][2], s);
+            H[i][j] = s;
+          }
+#pragma unroll
+      for (int c2 = 0; c2 < 3; ++c2)
+        v[c2] *= m.rho_alpha;
+    }
+  };
+
+  // Referential tangent from 10 cached values per qp: M = F^{-T} (9) and
+  // c = mu - 2 lambda ln J.  The scalar_referential flux
+  //   [2c sym(g) + 2 lambda tr(g) I + g tau] F^{-T},  g = H F^{-1},
+  //   tau = mu F F^T - c I
+  // equals  mu H + c M H^T M + 2 lambda (M:H) M  identically, which needs no
+  // gradient of the linearisation during the vmult.
+  template <typename T>
+  struct NHQp10QOp
+  {
+    static constexpr bool eval_u = false;
+    const T              *ucell  = nullptr;
+    const T              *cache; // [cell][10][N^3]
+    NHMat<T>              m;
+    int                   n3;
+    __device__ __forceinline__ void
+    operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
+               const T (*)[3]) const
+    {
+      const T *cp = cache + size_t(cell) * 10 * n3 + q;
+      T        M[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          M[i][j] = __ldg(cp + (i * 3 + j) * n3);
+      const T c = __ldg(cp + 9 * n3);
+      // t = M : H
+      T t = M[0][0] * H[0][0];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          if (i + j > 0)
+            t = fma_(M[i][j], H[i][j], t);
+      // K = M H^T  (K_ik = sum_j M_ij H_kj)
+      T K[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          {
+            T s = M[i][0] * H[k][0];
+            s   = fma_(M[i][1], H[k][1], s);
+            s   = fma_(M[i][2], H[k][2], s);
+            K[i][k] = s;
+          }
+      const T tl = T(2) * m.lambda * t;
+      T       P[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            T s = K[i][0] * M[0][j];
+            s   = fma_(K[i][1], M[1][j], s);
+            s   = fma_(K[i][2], M[2][j], s);
+            P[i][j] = fma_(m.mu, H[i][j], fma_(c, s, tl * M[i][j]));
+          }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          H[i][j] = P[i][j];
+#pragma unroll
+      for (int c2 = 0; c2 < 3; ++c2)
+        v[c2] *= m.rho_alpha;
+    }
+  };
+
+  // Deformed-frame variants (mf_nh_operator.h:945-994, 701-840) and the
+  // referential dP/dF variant (996-1010).  Eulerian geometry per qp: F^{-1}
+  // (9) and det F (1) = the inverse Jacobian and JxW ratio of
+  // MappingQEulerian; the current-frame flux Pc integrates as det F Pc F^{-T}.
+  // cache layout [cell][field][N^3]:
+  //   tensor2:    0-8 Finv, 9 J, 10 c2=2c/J, 11 s2=1/J, 12-17 tau/J (xx,yy,zz,xy,xz,yz)
+  //   tensor4:    0-8 Finv, 9 J, 10 s2, 11-16 tau/J, 17-52 C4 (6x6, Voigt with
+  //               sym(g) off-diagonals entered once: C4 : sym(g))
+  //   tensor4_ns: 0-80 A_ijkl
+  //   form0:      0-8 Finv, 9 J, 10-18 F, 19 J^{-1/3}
+  __device__ __forceinline__ int
+  voigt(int i, int j)
+  {
+    // xx,yy,zz,xy,xz,yz
+    return i == j ? i : (i + j == 1 ? 3 : (i + j == 2 ? 4 : 5));
+  }
+
+  // Formulation-0 current-frame flux (mf_nh_operator.h:707-839)
+  template <typename T>
+  __device__ __forceinline__ void
+  form0_flux_dev(const NHMat<T> &m, const T (&F)[3][3], T js, const T (&gg)[3][3],
+                 T (&Pc)[3][3])
+  {
+    T Fb[3][3], bb[3][3], sg[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        Fb[i][j] = F[i][j] * js;
+    const T J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) -
+                F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
+                F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        {
+          bb[i][j] = Fb[i][0] * Fb[j][0] + Fb[i][1] * Fb[j][1] + Fb[i][2] * Fb[j][2];
+          sg[i][j] = T(0.5) * (gg[i][j] + gg[j][i]);
+        }
+    const T inv_dim = T(1.0 / 3.0), two_over_dim = T(2.0 / 3.0);
+    T       tau_bar[3][3];
+    T       tr_tb = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        tau_bar[i][j] = bb[i][j] * (T(2.0) * m.c_1);
+    tr_tb               = tau_bar[0][0] + tau_bar[1][1] + tau_bar[2][2];
+    const T tr_tb_dim   = tr_tb * inv_dim;
+    const T dPsi        = (m.kappa / T(2.0)) * (J - T(1.0) / J);
+    const T dPsi_J      = dPsi * J;
+    const T d2Psi       = (m.kappa / T(2.0)) * (T(1.0) + T(1.0) / (J * J));
+    const T tr          = sg[0][0] + sg[1][1] + sg[2][2];
+    T       tau_iso_src = T(0);
+    T       jc[3][3], tau[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        {
+          const T dev     = sg[i][j] - (i == j ? tr * inv_dim : T(0));
+          const T tau_iso = tau_bar[i][j] - (i == j ? tr_tb_dim : T(0));
+          tau[i][j]       = tau_bar[i][j] + (i == j ? dPsi_J - tr_tb_dim : T(0));
+          jc[i][j] = sg[i][j] * (-dPsi_J * T(2.0)) +
+                     (i == j ? J * (dPsi + J * d2Psi) * tr : T(0)) +
+                     (two_over_dim * tr_tb) * dev - (two_over_dim * tr) * tau_iso;
+          tau_iso_src += tau_iso * sg[i][j];
+        }
+    const T inv_J = T(1.0) / J;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        {
+          const T geo = gg[i][0] * tau[0][j] + gg[i][1] * tau[1][j] + gg[i][2] * tau[2][j];
+          Pc[i][j] = (jc[i][j] - (i == j ? two_over_dim * tau_iso_src : T(0)) + geo) * inv_J;
+        }
+  }
+
+  template <typename T, int VAR>
+  struct NHCachedQOp
+  {
+    static constexpr bool eval_u = false;
+    const T              *ucell  = nullptr;
+    const T              *cache;
+    NHMat<T>              m;
+    int                   n3;
+    __device__ __forceinline__ void
+    operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
+               const T (*)[3]) const
+    {
+      constexpr int NF = nh_cache_fields(VAR);
+      const T      *cp = cache + size_t(cell) * NF * n3 + q;
+      if constexpr (VAR == V_TENSOR4_NS)
+        {
+          T P[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              {
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                  for (int l = 0; l < 3; ++l)
+                    s = fma_(__ldg(cp + (((i * 3 + j) * 3 + k) * 3 + l) * n3), H[k][l], s);
+                P[i][j] = s;
+              }
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              H[i][j] = P[i][j];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            v[c] *= m.rho_alpha;
+          return;
+        }
+      else
+        {
+          T Fi[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              Fi[i][j] = __ldg(cp + (i * 3 + j) * n3);
+          const T J = __ldg(cp + 9 * n3);
+          T       gg[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              gg[i][j] = H[i][0] * Fi[0][j] + H[i][1] * Fi[1][j] + H[i][2] * Fi[2][j];
+          T Pc[3][3];
+          T vscale;
+          if constexpr (VAR == V_TENSOR2)
+            {
+              const T c2 = __ldg(cp + 10 * n3);
+              const T s2 = __ldg(cp + 11 * n3);
+              T       Tt[3][3];
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  Tt[i][j] = __ldg(cp + (12 + voigt(i, j)) * n3);
+              const T tmp = T(2) * m.lambda * s2 * (gg[0][0] + gg[1][1] + gg[2][2]);
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  Pc[i][j] = c2 * T(0.5) * (gg[i][j] + gg[j][i]) + (i == j ? tmp : T(0)) +
+                             gg[i][0] * Tt[0][j] + gg[i][1] * Tt[1][j] + gg[i][2] * Tt[2][j];
+              vscale = m.rho_alpha * s2 * J;
+            }
+          else if constexpr (VAR == V_TENSOR4)
+            {
+              const T s2 = __ldg(cp + 10 * n3);
+              T       Tt[3][3];
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  Tt[i][j] = __ldg(cp + (11 + voigt(i, j)) * n3);
+              T sgv[6];
+              sgv[0] = gg[0][0];
+              sgv[1] = gg[1][1];
+              sgv[2] = gg[2][2];
+              sgv[3] = gg[0][1] + gg[1][0];
+              sgv[4] = gg[0][2] + gg[2][0];
+              sgv[5] = gg[1][2] + gg[2][1];
+              T cs[6];
+#pragma unroll
+              for (int r = 0; r < 6; ++r)
+                {
+                  T s = T(0);
+#pragma unroll
+                  for (int k = 0; k < 6; ++k)
+                    s = fma_(__ldg(cp + (17 + r * 6 + k) * n3), sgv[k], s);
+                  cs[r] = s;
+                }
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  Pc[i][j] = gg[i][0] * Tt[0][j] + gg[i][1] * Tt[1][j] + gg[i][2] * Tt[2][j] +
+                             cs[voigt(i, j)];
+              vscale = m.rho_alpha * s2 * J;
+            }
+          else // V_FORM0
+            {
+              T F[3][3];
+#pragma unroll
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                  F[i][j] = __ldg(cp + (10 + i * 3 + j) * n3);
+              const T js = __ldg(cp + 19 * n3);
+              form0_flux_dev(m, F, js, gg, Pc);
+              vscale = m.rho_alpha;
+            }
+          // P = J Pc F^{-T}
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              H[i][j] = J * (Pc[i][0] * Fi[j][0] + Pc[i][1] * Fi[j][1] + Pc[i][2] * Fi[j][2]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            v[c] *= vscale;
+        }
+    }
+  };
+} // namespace mfgpu

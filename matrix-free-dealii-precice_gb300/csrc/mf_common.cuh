@@ -1,0 +1,132 @@
+// Shared definitions of the GB300 matrix-free library: level geometry,
+// 1D shape matrices, error reporting.
+//
+// Data layout in HBM (one multigrid level):
+//   * structured box of C[0] x C[1] x C[2] hexahedral cells with uniform cell
+//     size h[d] (subdivided_hyper_rectangle + refine_global, the meshes of the
+//     reference's cases, include/cases/elasticity/turek_hron.h:23-45);
+//   * continuous Q_p nodes on Gauss-Lobatto points (FE_Q(p)), numbered
+//     lexicographically on the global node grid Nn[d] = C[d]*p + 1 (x fastest);
+//   * vector fields component-blocked: dof = comp * n_nodes + node;
+//   * homogeneous Dirichlet constraints given per box face (x-,x+,y-,y+,z-,z+)
+//     as a component bitmask, so no constraint index lists are stored.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace mfgpu
+{
+  constexpr int MAX_N = 7; // degree 6
+
+  struct LevelGeom
+  {
+    int      C[3];
+    int      Nn[3];
+    int      p;
+    size_t   n_nodes;
+    size_t   n_cells;
+    double   h[3];
+    double   lo[3];
+    unsigned face_mask[6];
+  };
+
+  // 1D matrices for a degree, in the compute precision T:
+  //   S[q][i]  Gauss-Lobatto Lagrange basis at Gauss point q   (N x N)
+  //   D[q][r]  collocation derivative on the Gauss points      (N x N)
+  //   w[q]     Gauss weights on [0,1]
+  template <int N, typename T>
+  struct Shape
+  {
+    T S[N * N];
+    T D[N * N];
+    T w[N];
+  };
+
+  // geometry of a level as seen by a cell kernel, in precision T
+  template <typename T>
+  struct CellGeom
+  {
+    int      C[3];
+    int      Nn[3];
+    int      p;
+    unsigned n_cells;
+    size_t   n_nodes;
+    T        inv_h[3];
+    T        vol; // h0*h1*h2
+    unsigned face_mask[6];
+  };
+
+  template <typename T>
+  inline CellGeom<T>
+  make_cell_geom(const LevelGeom &g)
+  {
+    CellGeom<T> c;
+    for (int d = 0; d < 3; ++d)
+      {
+        c.C[d]     = g.C[d];
+        c.Nn[d]    = g.Nn[d];
+        c.inv_h[d] = T(1.0 / g.h[d]);
+      }
+    c.p       = g.p;
+    c.n_cells = unsigned(g.n_cells);
+    c.n_nodes = g.n_nodes;
+    c.vol     = T(g.h[0] * g.h[1] * g.h[2]);
+    for (int f = 0; f < 6; ++f)
+      c.face_mask[f] = g.face_mask[f];
+    return c;
+  }
+
+  // component mask of the Dirichlet constraints on node (ix,iy,iz)
+  __host__ __device__ inline unsigned
+  node_mask(const unsigned *fm, const int *Nn, int ix, int iy, int iz)
+  {
+    unsigned m = 0;
+    m |= (ix == 0) ? fm[0] : 0u;
+    m |= (ix == Nn[0] - 1) ? fm[1] : 0u;
+    m |= (iy == 0) ? fm[2] : 0u;
+    m |= (iy == Nn[1] - 1) ? fm[3] : 0u;
+    m |= (iz == 0) ? fm[4] : 0u;
+    m |= (iz == Nn[2] - 1) ? fm[5] : 0u;
+    return m;
+  }
+
+  // status codes of the C-ABI
+  enum Status
+  {
+    OK               = 0,
+    ERR_ARG          = 1,
+    ERR_CUDA         = 2,
+    ERR_OOM          = 3,
+    ERR_NONFINITE    = 4,
+    ERR_NOT_CONVERGED = 5,
+    ERR_STATE        = 6,
+    ERR_DET_F        = 7,
+    ERR_UNSUPPORTED  = 8,
+    ERR_TIMEOUT      = 9
+  };
+  // neo-Hookean caching variants and the cached fields per quadrature point
+  enum NHVariant
+  {
+    V_SCALAR_REF = 0,
+    V_TENSOR2    = 1,
+    V_TENSOR4    = 2,
+    V_TENSOR4_NS = 3,
+    V_QP10       = 4,
+    V_FORM0      = 5
+  };
+
+  __host__ __device__ constexpr int
+  nh_cache_fields(int v)
+  {
+    return v == V_SCALAR_REF ? 1 :
+           v == V_TENSOR2    ? 18 :
+           v == V_TENSOR4    ? 53 :
+           v == V_TENSOR4_NS ? 81 :
+           v == V_QP10       ? 10 :
+                               20;
+  }
+
+} // namespace mfgpu

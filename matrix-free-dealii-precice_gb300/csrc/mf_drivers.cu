@@ -1,0 +1,595 @@
+// Solid (Newton-Newmark) and heat (backward Euler) drivers on the device,
+// restating Solid::solve_nonlinear_timestep / assemble_residual /
+// solve_linear_system (include/solid_mechanics/mf_elasticity.h:1402-1491,
+// 1649-1908, 1983-2070) and LaplaceProblem::assemble_rhs / solve
+// (include/heat_transfer/heat_transfer.h:579-655, 715-812), with preCICE
+// replaced by a constant boundary traction / analytic Dirichlet data.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "../../include/mfgpu.h"
+#include "mf_drivers.h"
+#include "mf_vec.cuh"
+
+namespace mfgpu
+{
+  static cudaError_t
+  dispatch_residual(int N, const HostBasis &b, const LevelGeom &g, int form, const NHMatD &m,
+                    double rho, const double *body, const double *u, const double *acc,
+                    double *rhs, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_residual<2>(b, g, form, m, rho, body, u, acc, rhs, s);
+        case 3: return launch_residual<3>(b, g, form, m, rho, body, u, acc, rhs, s);
+        case 4: return launch_residual<4>(b, g, form, m, rho, body, u, acc, rhs, s);
+        case 5: return launch_residual<5>(b, g, form, m, rho, body, u, acc, rhs, s);
+        case 6: return launch_residual<6>(b, g, form, m, rho, body, u, acc, rhs, s);
+        case 7: return launch_residual<7>(b, g, form, m, rho, body, u, acc, rhs, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  static cudaError_t
+  dispatch_heat_rhs(int N, const HostBasis &b, const LevelGeom &g, double dt,
+                    const SourceDesc &f, const double *u_old, double *rhs, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_heat_rhs<2>(b, g, dt, f, u_old, rhs, s);
+        case 3: return launch_heat_rhs<3>(b, g, dt, f, u_old, rhs, s);
+        case 4: return launch_heat_rhs<4>(b, g, dt, f, u_old, rhs, s);
+        case 5: return launch_heat_rhs<5>(b, g, dt, f, u_old, rhs, s);
+        case 6: return launch_heat_rhs<6>(b, g, dt, f, u_old, rhs, s);
+        case 7: return launch_heat_rhs<7>(b, g, dt, f, u_old, rhs, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  Mesh
+  to_mesh(const mfgpu_mesh &m)
+  {
+    Mesh r;
+    r.degree = m.degree;
+    r.n_q    = m.n_q_1d;
+    r.n_ref  = m.n_refinements;
+    for (int d = 0; d < 3; ++d)
+      {
+        r.rep[d] = m.repetitions[d];
+        r.lo[d]  = m.lower[d];
+        r.hi[d]  = m.upper[d];
+        if (m.repetitions[d] < 1 || !(m.upper[d] > m.lower[d]))
+          throw Error(ERR_ARG, "mesh: repetitions must be >= 1 and upper > lower");
+      }
+    if (m.degree < 1 || m.degree > 6)
+      throw Error(ERR_UNSUPPORTED, "mesh: degree must be 1..6");
+    if (m.n_refinements < 0 || m.n_refinements > 12)
+      throw Error(ERR_ARG, "mesh: n_refinements out of range");
+    if (m.n_dirichlet < 0 || m.n_dirichlet > 8)
+      throw Error(ERR_ARG, "mesh: n_dirichlet out of range");
+    for (int f = 0; f < 6; ++f)
+      r.boundary_id[f] = m.boundary_id[f];
+    r.n_dirichlet = m.n_dirichlet;
+    for (int i = 0; i < 8; ++i)
+      {
+        r.dirichlet_id[i]   = m.dirichlet_id[i];
+        r.dirichlet_mask[i] = m.dirichlet_mask[i];
+      }
+    return r;
+  }
+
+  // ---------------------------------------------------------------------
+  // preconditioner wrappers
+  // ---------------------------------------------------------------------
+  struct IdentityPre : Precond<double>
+  {
+    Context *ctx;
+    size_t   n;
+    void vmult(double *d, const double *s) override { vec_copy<double>(*ctx, n, s, d); }
+  };
+
+  struct JacobiPre64 : Precond<double>
+  {
+    Context  *ctx;
+    Operator *A;
+    double    omega;
+    void
+    vmult(double *d, const double *s) override
+    {
+      vec_scale<double>(*ctx, A->m(), omega, A->inv_diag.as<double>(), s, d);
+    }
+  };
+
+  // ---------------------------------------------------------------------
+  // solid
+  // ---------------------------------------------------------------------
+  SolidDriver::SolidDriver(Context *c, const mfgpu_solid_params &p)
+    : ctx(c)
+    , P(p)
+  {
+    mesh = to_mesh(P.mesh);
+    L    = mesh.n_ref;
+    make_host_basis(mesh.degree, basis);
+    const double beta = 0.25;
+    const double a1   = 1. / (beta * P.dt * P.dt);
+    P.material.alpha_1 = a1;
+    mat      = make_material(P.material.mu, P.material.nu, P.material.rho, a1);
+    variant  = parse_caching(P.caching);
+    if (P.material.formulation != 0 && P.material.formulation != 1)
+      throw Error(ERR_ARG, "formulation must be 0 or 1");
+    fine                = make_nh(ctx, mesh, -1, 64, variant);
+    fine->mat           = mat;
+    fine->formulation   = P.material.formulation;
+    fine->have_material = true;
+    const size_t n      = fine->m();
+    for (DevBuf *b : {&u, &delta, &v_old, &a_old, &acc, &rhs, &du})
+      {
+        b->alloc(n * sizeof(double));
+        MF_CK(cudaMemsetAsync(b->ptr, 0, n * sizeof(double), ctx->stream));
+      }
+    if (P.solver.preconditioner == 2)
+      {
+        lprec = P.solver.mg_precision == 64 ? 64 : 32;
+        for (int l = 0; l <= L; ++l)
+          {
+            auto op           = make_nh(ctx, mesh, l, lprec, variant);
+            op->mat           = mat;
+            op->formulation   = P.material.formulation;
+            op->have_material = true;
+            lops.push_back(std::move(op));
+            u_levels.emplace_back(lops.back()->m() * (lprec == 32 ? 4 : 8));
+          }
+        if (P.solver.coarse_fp64 && lprec == 32)
+          {
+            coarse64                = make_nh(ctx, mesh, 0, 64, variant);
+            coarse64->mat           = mat;
+            coarse64->formulation   = P.material.formulation;
+            coarse64->have_material = true;
+            u0_64.alloc(coarse64->m() * sizeof(double));
+          }
+        auto fill = [&](auto &mg) {
+          mg.ctx = ctx;
+          for (int l = 0; l <= L; ++l)
+            {
+              mg.ops.push_back(lops[l].get());
+              if (l == 0)
+                mg.transfers.emplace_back(nullptr);
+              else
+                mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
+                                                       lops[l]->geom, 3, lprec));
+            }
+          mg.coarse64 = coarse64.get();
+        };
+        if (lprec == 32)
+          {
+            mgf.reset(new Multigrid<float>());
+            fill(*mgf);
+          }
+        else
+          {
+            mgd.reset(new Multigrid<double>());
+            fill(*mgd);
+          }
+      }
+  }
+
+  void
+  SolidDriver::update_operators(const double *ulin)
+  {
+    fine->u = ulin;
+    fine->do_cache();
+    if (P.solver.preconditioner == 1)
+      fine->compute_diagonal();
+    if (P.solver.preconditioner != 2)
+      return;
+    const size_t nf = lops[L]->m();
+    if (lprec == 32)
+      vec_convert<float, double>(*ctx, nf, ulin, u_levels[L].as<float>());
+    else
+      vec_copy<double>(*ctx, nf, ulin, u_levels[L].as<double>());
+    for (int l = L; l > 0; --l)
+      {
+        Transfer *t = lprec == 32 ? mgf->transfers[l].get() : mgd->transfers[l].get();
+        t->interpolate(u_levels[l - 1].ptr, u_levels[l].ptr);
+      }
+    for (int l = 0; l <= L; ++l)
+      {
+        lops[l]->u = u_levels[l].ptr;
+        lops[l]->do_cache();
+        lops[l]->compute_diagonal();
+      }
+    if (coarse64)
+      {
+        vec_convert<double, float>(*ctx, coarse64->m(), u_levels[0].as<float>(), u0_64.as<double>());
+        coarse64->u = u0_64.ptr;
+        coarse64->do_cache();
+        coarse64->compute_diagonal();
+      }
+    const int coarse_its = P.solver.coarse_accurate ? int(lops[0]->m()) : P.solver.cheb_eig_its;
+    if (lprec == 32)
+      mgf->setup(P.solver.cheb_range, P.solver.cheb_degree, P.solver.cheb_eig_its, coarse_its);
+    else
+      mgd->setup(P.solver.cheb_range, P.solver.cheb_degree, P.solver.cheb_eig_its, coarse_its);
+  }
+
+  double
+  SolidDriver::assemble_residual()
+  {
+    const size_t n = fine->m();
+    MF_CK(cudaMemsetAsync(rhs.ptr, 0, n * sizeof(double), ctx->stream));
+    MF_CK(dispatch_residual(basis.N, basis, fine->geom, P.material.formulation, mat, P.material.rho,
+                            P.body_force, u.as<double>(), acc.as<double>(), rhs.as<double>(),
+                            ctx->stream));
+    count_launch();
+    // traction faces
+    for (int f = 0; f < 6; ++f)
+      {
+        if (mesh.boundary_id[f] != P.traction_id)
+          continue;
+        TractionArgs A;
+        std::memset(&A, 0, sizeof(A));
+        const LevelGeom &g = fine->geom;
+        for (int d = 0; d < 3; ++d)
+          {
+            A.C[d]  = g.C[d];
+            A.Nn[d] = g.Nn[d];
+            A.h[d]  = g.h[d];
+            A.t[d]  = P.traction[d];
+          }
+        A.p       = g.p;
+        A.N       = basis.N;
+        A.n_nodes = g.n_nodes;
+        A.face    = f;
+        for (int i = 0; i < basis.N * basis.N; ++i)
+          {
+            A.S[i] = basis.S[i];
+            A.G[i] = basis.G[i];
+          }
+        for (int i = 0; i < basis.N; ++i)
+          {
+            A.Ge[0][i] = basis.Ge[0][i];
+            A.Ge[1][i] = basis.Ge[1][i];
+            A.w[i]     = basis.w[i];
+          }
+        const int nd = f / 2, d1 = nd == 0 ? 1 : 0, d2 = nd == 2 ? 1 : 2;
+        const unsigned nfaces = unsigned(g.C[d1] * g.C[d2]);
+        k_traction<<<nfaces, 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
+        count_launch();
+        MF_CK(cudaGetLastError());
+      }
+    constrained_op<double>(*ctx, fine->geom, 3, 2, nullptr, rhs.as<double>());
+    return std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+  }
+
+  struct FineOp : LinOp<double>
+  {
+    Operator *op;
+    size_t size() const override { return op->m(); }
+    void   vmult(double *d, const double *s) override { op->vmult(d, s); }
+  };
+
+  int
+  SolidDriver::solve_linear(const double *b, double *x, double tol)
+  {
+    const size_t n = fine->m();
+    MF_CK(cudaMemsetAsync(x, 0, n * sizeof(double), ctx->stream));
+    FineOp A;
+    A.op            = fine.get();
+    const int maxit = int(std::min<size_t>(n * size_t(std::max(P.solver.max_it_mult, 1)), 1000000000));
+    CGStats   st;
+    if (P.solver.preconditioner == 1)
+      {
+        JacobiPre64 J;
+        J.ctx   = ctx;
+        J.A     = fine.get();
+        J.omega = P.solver.relaxation;
+        st      = cg_solve<double>(*ctx, A, &J, x, b, tol, maxit);
+      }
+    else if (P.solver.preconditioner == 2)
+      {
+        Precond<double> *M = lprec == 32 ? static_cast<Precond<double> *>(mgf.get()) :
+                                           static_cast<Precond<double> *>(mgd.get());
+        st = cg_solve<double>(*ctx, A, M, x, b, tol, maxit);
+      }
+    else
+      st = cg_solve<double>(*ctx, A, nullptr, x, b, tol, maxit);
+    constrained_op<double>(*ctx, fine->geom, 3, 2, nullptr, x);
+    if (!st.converged)
+      throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+    return st.its;
+  }
+
+  std::vector<double>
+  SolidDriver::point_value(const double *x)
+  {
+    const LevelGeom &g = fine->geom;
+    std::vector<double> h(fine->m());
+    MF_CK(cudaMemcpyAsync(h.data(), u.ptr, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    int    cc[3];
+    double xi[3];
+    for (int d = 0; d < 3; ++d)
+      {
+        const double t = (x[d] - g.lo[d]) / g.h[d];
+        int          c = int(std::floor(t));
+        c              = std::min(std::max(c, 0), g.C[d] - 1);
+        cc[d]          = c;
+        xi[d]          = t - c;
+      }
+    auto lag = [&](int i, double t) {
+      double v = 1;
+      for (int j = 0; j < basis.N; ++j)
+        if (j != i)
+          v *= (t - basis.nodes[j]) / (basis.nodes[i] - basis.nodes[j]);
+      return v;
+    };
+    std::vector<double> r(3, 0.0);
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < basis.N; ++k)
+        for (int j = 0; j < basis.N; ++j)
+          for (int i = 0; i < basis.N; ++i)
+            {
+              const size_t node = size_t(cc[0] * g.p + i) +
+                                  size_t(g.Nn[0]) * (size_t(cc[1] * g.p + j) + size_t(g.Nn[1]) * (cc[2] * g.p + k));
+              r[c] += lag(i, xi[0]) * lag(j, xi[1]) * lag(k, xi[2]) * h[size_t(c) * g.n_nodes + node];
+            }
+    return r;
+  }
+
+  void
+  SolidDriver::run(mfgpu_solid_result &res)
+  {
+    auto         t0 = std::chrono::steady_clock::now();
+    const size_t n  = fine->m();
+    const double dt = P.dt, beta = 0.25, gamma = 0.5;
+    const double a1 = 1. / (beta * dt * dt), a2 = 1. / (beta * dt), a3 = (1 - 2 * beta) / (2 * beta),
+                 a4 = gamma / (beta * dt), a5 = 1 - gamma / beta, a6 = (1 - gamma / (2 * beta)) * dt;
+    std::memset(&res, 0, sizeof(res));
+    if (P.n_steps > 64)
+      throw Error(ERR_ARG, "at most 64 time steps per run");
+    res.n_steps = P.n_steps;
+    double *U = u.as<double>(), *Dl = delta.as<double>(), *V = v_old.as<double>(),
+           *Ao = a_old.as<double>(), *Ac = acc.as<double>(), *R = rhs.as<double>(), *DU = du.as<double>();
+    for (int step = 0; step < P.n_steps; ++step)
+      {
+        MF_CK(cudaMemsetAsync(Dl, 0, n * sizeof(double), ctx->stream));
+        double err_res0 = 0, err_upd = 0, err_upd0 = 0, err_upd_norm = 0;
+        int    it       = 0;
+        for (; it < P.max_newton; ++it)
+          {
+            // update_acceleration (mf_elasticity.h:1616-1620)
+            vec_axpbyz<double>(*ctx, n, a1, Dl, -a2, V, Ac);
+            vec_axpby<double>(*ctx, n, -a3, Ao, 1.0, Ac);
+            const double err_res = assemble_residual();
+            if (!std::isfinite(err_res))
+              throw Error(ERR_NONFINITE, "non-finite residual");
+            if (it == 0)
+              err_res0 = err_res;
+            const double err_res_norm = err_res0 != 0 ? err_res / err_res0 : err_res;
+            if (it > 2)
+              {
+                bool conv = (err_res <= P.tol_f_abs || err_upd <= P.tol_u_abs);
+                if (err_res_norm <= P.tol_f && err_upd_norm <= P.tol_u)
+                  conv = true;
+                if (conv)
+                  break;
+              }
+            update_operators(U);
+            const int its = solve_linear(R, DU, P.solver.tol * err_res);
+            res.total_cg += its;
+            res.n_solves++;
+            err_upd = std::sqrt(vec_dot<double>(*ctx, n, DU, DU));
+            if (it == 0)
+              err_upd0 = err_upd;
+            err_upd_norm = err_upd0 != 0 ? err_upd / err_upd0 : err_upd;
+            vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, Dl);
+            vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, U);
+          }
+        if (it >= P.max_newton)
+          throw Error(ERR_NOT_CONVERGED, "no convergence in nonlinear solver");
+        res.newton_its[step] = it;
+        // update_velocity (mf_elasticity.h:1602-1610): v = a4 delta + a5 v_old + a6 a_old
+        vec_axpby<double>(*ctx, n, a6, Ao, a5, V);
+        vec_axpby<double>(*ctx, n, a4, Dl, 1.0, V);
+        vec_copy<double>(*ctx, n, Ac, Ao);
+        const std::vector<double> w = point_value(P.watch);
+        for (int d = 0; d < 3; ++d)
+          res.watch_disp[step][d] = w[d];
+      }
+    ctx->sync();
+    res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  // ---------------------------------------------------------------------
+  // heat
+  // ---------------------------------------------------------------------
+  HeatDriver::HeatDriver(Context *c, const mfgpu_heat_params &p)
+    : ctx(c)
+    , P(p)
+  {
+    mesh = to_mesh(P.mesh);
+    L    = mesh.n_ref;
+    make_host_basis(mesh.degree, basis);
+    op          = make_heat(ctx, mesh, -1, 64, true);
+    op->delta_t = P.dt;
+    op_u        = make_heat(ctx, mesh, -1, 64, false);
+    op_u->delta_t = P.dt;
+    const size_t n = op->m();
+    for (DevBuf *b : {&sol, &sol_old, &rhs, &du, &uD})
+      {
+        b->alloc(n * sizeof(double));
+        MF_CK(cudaMemsetAsync(b->ptr, 0, n * sizeof(double), ctx->stream));
+      }
+    if (P.solver.preconditioner == 2)
+      {
+        lprec = P.solver.mg_precision == 64 ? 64 : 32;
+        for (int l = 0; l <= L; ++l)
+          {
+            auto lo     = make_heat(ctx, mesh, l, lprec, true);
+            lo->delta_t = P.dt;
+            lops.push_back(std::move(lo));
+          }
+        if (P.solver.coarse_fp64 && lprec == 32)
+          {
+            coarse64          = make_heat(ctx, mesh, 0, 64, true);
+            coarse64->delta_t = P.dt;
+          }
+        auto fill = [&](auto &mg) {
+          mg.ctx = ctx;
+          for (int l = 0; l <= L; ++l)
+            {
+              mg.ops.push_back(lops[l].get());
+              if (l == 0)
+                mg.transfers.emplace_back(nullptr);
+              else
+                mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
+                                                       lops[l]->geom, 1, lprec));
+            }
+          mg.coarse64 = coarse64.get();
+        };
+        if (lprec == 32)
+          {
+            mgf.reset(new Multigrid<float>());
+            fill(*mgf);
+          }
+        else
+          {
+            mgd.reset(new Multigrid<double>());
+            fill(*mgd);
+          }
+      }
+  }
+
+  void
+  HeatDriver::node_x(size_t g, double *x) const
+  {
+    const LevelGeom &G = op->geom;
+    int              ii[3];
+    ii[0] = int(g % G.Nn[0]);
+    g /= G.Nn[0];
+    ii[1] = int(g % G.Nn[1]);
+    ii[2] = int(g / G.Nn[1]);
+    for (int d = 0; d < 3; ++d)
+      {
+        const int c  = std::min(ii[d] / G.p, G.C[d] - 1);
+        const int li = ii[d] - c * G.p;
+        x[d]         = G.lo[d] + (c + basis.nodes[li]) * G.h[d];
+      }
+  }
+
+  void
+  HeatDriver::run(mfgpu_heat_result &res)
+  {
+    auto         t0 = std::chrono::steady_clock::now();
+    const size_t n  = op->m();
+    std::memset(&res, 0, sizeof(res));
+    if (P.n_steps > 64)
+      throw Error(ERR_ARG, "at most 64 time steps per run");
+    res.n_steps = P.n_steps;
+    const LevelGeom &G = op->geom;
+    std::vector<double> h;
+    if (P.analytic)
+      {
+        h.resize(n);
+        for (size_t g = 0; g < n; ++g)
+          {
+            double x[3];
+            node_x(g, x);
+            h[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1];
+          }
+        MF_CK(cudaMemcpyAsync(sol.ptr, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->sync();
+      }
+    vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
+    if (P.solver.preconditioner == 2)
+      {
+        for (auto &lo : lops)
+          lo->compute_diagonal();
+        if (coarse64)
+          coarse64->compute_diagonal();
+      }
+    if (P.solver.preconditioner == 1)
+      op->compute_diagonal();
+    SourceDesc src;
+    std::memset(&src, 0, sizeof(src));
+    src.constant = P.analytic ? P.beta - 2 - 2 * P.alpha : 0.0;
+    src.n_gauss  = P.analytic ? 0 : P.n_gauss;
+    for (int i = 0; i < 8; ++i)
+      {
+        for (int d = 0; d < 3; ++d)
+          src.center[i][d] = P.g_center[i][d];
+        src.width[i] = P.g_width[i];
+        src.amp[i]   = P.g_amp[i];
+      }
+    double t = 0;
+    for (int step = 0; step < P.n_steps; ++step)
+      {
+        t += P.dt;
+        // inhomogeneous Dirichlet values on the constrained nodes at time t
+        MF_CK(cudaMemsetAsync(uD.ptr, 0, n * sizeof(double), ctx->stream));
+        if (P.analytic)
+          {
+            std::vector<double> hd(n, 0.0);
+            for (size_t g = 0; g < n; ++g)
+              {
+                int ii[3];
+                size_t gg = g;
+                ii[0] = int(gg % G.Nn[0]);
+                gg /= G.Nn[0];
+                ii[1] = int(gg % G.Nn[1]);
+                ii[2] = int(gg / G.Nn[1]);
+                if (node_mask(G.face_mask, G.Nn, ii[0], ii[1], ii[2]) & 1u)
+                  {
+                    double x[3];
+                    node_x(g, x);
+                    hd[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1] + P.beta * t;
+                  }
+              }
+            MF_CK(cudaMemcpyAsync(uD.ptr, hd.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+            ctx->sync();
+          }
+        // rhs = -A_unconstrained uD + int (u_old + dt f) v
+        op_u->vmult(rhs.ptr, uD.ptr);
+        vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
+        MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
+                                ctx->stream));
+        count_launch();
+        const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+        FineOp A;
+        A.op = op.get();
+        CGStats st;
+        if (P.solver.preconditioner == 2)
+          {
+            if (lprec == 32)
+              {
+                mgf->setup(15., 5, 10, int(lops[0]->m()));
+                st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+              }
+            else
+              {
+                mgd->setup(15., 5, 10, int(lops[0]->m()));
+                st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+              }
+          }
+        else if (P.solver.preconditioner == 1)
+          {
+            JacobiPre64 J;
+            J.ctx   = ctx;
+            J.A     = op.get();
+            J.omega = 0.7;
+            st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n));
+          }
+        else
+          st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
+        if (!st.converged)
+          throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+        res.cg_its[step] = st.its;
+        constrained_op<double>(*ctx, G, 1, 2, nullptr, du.as<double>());
+        vec_axpbyz<double>(*ctx, n, 1.0, uD.as<double>(), 1.0, du.as<double>(), sol.as<double>());
+        vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
+      }
+    ctx->sync();
+    res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+} // namespace mfgpu

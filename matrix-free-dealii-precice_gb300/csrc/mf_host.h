@@ -1,0 +1,211 @@
+// Internal host-side classes of the library (behind the C-ABI of mfgpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mf_launch.h"
+
+namespace mfgpu
+{
+  // exception carrying a C-ABI status
+  struct Error : std::runtime_error
+  {
+    int code;
+    Error(int c, const std::string &m)
+      : std::runtime_error(m)
+      , code(c)
+    {}
+  };
+
+  void check_cuda(cudaError_t e, const char *what);
+#define MF_CK(x) ::mfgpu::check_cuda((x), #x)
+
+  void count_launch(int n = 1);
+  long long launch_count();
+
+  // owning device buffer
+  struct DevBuf
+  {
+    void  *ptr   = nullptr;
+    size_t bytes = 0;
+    DevBuf()     = default;
+    explicit DevBuf(size_t b) { alloc(b); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept
+      : ptr(o.ptr)
+      , bytes(o.bytes)
+    {
+      o.ptr   = nullptr;
+      o.bytes = 0;
+    }
+    DevBuf &
+    operator=(DevBuf &&o) noexcept
+    {
+      release();
+      ptr     = o.ptr;
+      bytes   = o.bytes;
+      o.ptr   = nullptr;
+      o.bytes = 0;
+      return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t b);
+    void release();
+    template <typename T>
+    T *
+    as() const
+    {
+      return static_cast<T *>(ptr);
+    }
+  };
+
+  struct Context
+  {
+    int          device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf       err;      // int error flags
+    DevBuf       partial;  // reduction partials
+    DevBuf       scalars;  // device scalars (double[32])
+    double      *host_scalars = nullptr; // pinned
+    explicit Context(int dev);
+    ~Context();
+    // error flags set by kernels since the last call (and reset)
+    int  take_error_flags();
+    void sync();
+  };
+
+  // geometry of one level of the box hierarchy
+  struct Mesh
+  {
+    int      degree, n_q, n_ref;
+    int      rep[3];
+    double   lo[3], hi[3];
+    int      boundary_id[6];
+    int      n_dirichlet;
+    int      dirichlet_id[8];
+    unsigned dirichlet_mask[8];
+    LevelGeom level(int l) const; // l < 0: finest
+    int       finest() const { return n_ref; }
+  };
+
+  // ---------------------------------------------------------------------
+  // vector kernels (instantiated for float and double)
+  // ---------------------------------------------------------------------
+  template <typename T> void vec_fill(Context &c, size_t n, T v, T *x);
+  template <typename T> void vec_axpby(Context &c, size_t n, T a, const T *x, T b, T *y);
+  template <typename T> void vec_axpbyz(Context &c, size_t n, T a, const T *x, T b, const T *y, T *z);
+  template <typename T> void vec_copy(Context &c, size_t n, const T *x, T *y);
+  template <typename TD, typename TS> void vec_convert(Context &c, size_t n, const TS *s, TD *d);
+  template <typename T> void vec_scale(Context &c, size_t n, T omega, const T *d, const T *x, T *y);
+  template <typename T> void vec_invert(Context &c, size_t n, T *x);
+  // dot product into device scalar slot (deterministic)
+  template <typename T> void vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot);
+  template <typename T> double vec_dot(Context &c, size_t n, const T *x, const T *y);
+  template <typename T> void cg_update(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q, int rr_slot);
+  template <typename T> void cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p);
+  template <typename T> void cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold);
+  template <typename T> void cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b, const T *Ax, const T *dinv, T *x, T *xold);
+  // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1
+  template <typename T> void constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst);
+  double *scalar_slots(Context &c); // device pointer to the scalars
+  void    read_scalars(Context &c, int n); // D2H of the first n slots (sync)
+
+  // ---------------------------------------------------------------------
+  // operators
+  // ---------------------------------------------------------------------
+  struct Operator
+  {
+    Context  *ctx = nullptr;
+    Mesh      mesh;
+    int       level = -1;
+    LevelGeom geom;
+    HostBasis basis;
+    int       precision   = 64;
+    int       nc          = 1;
+    bool      constrained = true;
+    DevBuf    inv_diag;
+    DevBuf    diag;
+    bool      diag_ready = false;
+    virtual ~Operator() = default;
+    size_t
+    m() const
+    {
+      return size_t(nc) * geom.n_nodes;
+    }
+    size_t
+    elem_size() const
+    {
+      return precision == 32 ? 4 : 8;
+    }
+    // dst += A src (cell part, constrained rows untouched)
+    virtual void apply_cells(void *dst, const void *src) = 0;
+    virtual void compute_diagonal() = 0;
+    virtual size_t memory_consumption() const { return 0; }
+    virtual void clear() {}
+    void vmult(void *dst, const void *src);
+    void vmult_add(void *dst, const void *src);
+    void finish_diagonal(); // constrained -> 1, invert
+  };
+
+  struct HeatOperator : Operator
+  {
+    double delta_t     = 0;
+    double coefficient = 1;
+    void   apply_cells(void *dst, const void *src) override;
+    void   compute_diagonal() override;
+  };
+
+  struct NHOperator : Operator
+  {
+    int        variant = 0; // NHVariant
+    NHMatD     mat{};
+    int        formulation = 1;
+    bool       have_material = false;
+    const void *u      = nullptr; // linearisation (not owned)
+    DevBuf      cache;
+    DevBuf      ucell;
+    bool        cached = false;
+    void   apply_cells(void *dst, const void *src) override;
+    void   compute_diagonal() override;
+    void   do_cache();
+    size_t memory_consumption() const override { return cache.bytes + ucell.bytes; }
+    void   clear() override;
+  };
+
+  int  parse_caching(const char *s);
+  NHMatD make_material(double mu, double nu, double rho, double alpha_1);
+  std::unique_ptr<HeatOperator> make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained);
+  std::unique_ptr<NHOperator>   make_nh(Context *c, const Mesh &m, int level, int precision, int variant);
+
+  // ---------------------------------------------------------------------
+  // transfer between level l and l+1 (tensor product of 1D operators)
+  // ---------------------------------------------------------------------
+  struct Transfer
+  {
+    Context  *ctx = nullptr;
+    LevelGeom coarse, fine;
+    int       nc = 1, precision = 64;
+    // per direction: prolongation (fine rows), restriction = P^T (coarse
+    // rows), interpolation (coarse rows); banded gather lists
+    struct Band
+    {
+      DevBuf col, val;
+      int    rows = 0, width = 0;
+    };
+    Band   P[3], R[3], I[3];
+    DevBuf tmp0, tmp1;
+    Transfer(Context *c, const HostBasis &b, const LevelGeom &cg, const LevelGeom &fg, int nc, int precision);
+    void prolongate(void *fine_v, const void *coarse_v);        // fine = P coarse
+    void prolongate_add(void *fine_v, const void *coarse_v);    // fine += P coarse
+    void restrict_add(void *coarse_v, const void *fine_v);      // coarse += P^T fine
+    void interpolate(void *coarse_v, const void *fine_v);       // coarse = I fine
+  private:
+    void passes(const Band *B, const LevelGeom &from, const LevelGeom &to, const void *in, void *out);
+  };
+} // namespace mfgpu

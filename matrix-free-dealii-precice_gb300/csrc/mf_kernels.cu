@@ -1,0 +1,316 @@
+// Instantiation of the cell kernels for one degree.  Compiled once per
+// N = p+1 in {2..7} with -DMF_N=<N>, so the per-degree builds run in
+// parallel.
+#include <cmath>
+#include <cstring>
+
+#include "mf_launch.h"
+#include "mf_setup.cuh"
+
+#ifndef MF_N
+#error "MF_N must be defined (2..7)"
+#endif
+
+namespace mfgpu
+{
+  namespace
+  {
+    template <int N, typename T>
+    Shape<N, T>
+    make_shape(const HostBasis &b)
+    {
+      Shape<N, T> s;
+      for (int i = 0; i < N * N; ++i)
+        {
+          s.S[i] = T(b.S[i]);
+          s.D[i] = T(b.D[i]);
+        }
+      for (int i = 0; i < N; ++i)
+        s.w[i] = T(b.w[i]);
+      return s;
+    }
+
+    template <typename T>
+    NHMat<T>
+    to_mat(const NHMatD &m)
+    {
+      NHMat<T> r;
+      r.mu        = T(m.mu);
+      r.lambda    = T(m.lambda);
+      r.rho_alpha = T(m.rho_alpha);
+      r.kappa     = T(m.kappa);
+      r.c_1       = T(m.c_1);
+      return r;
+    }
+
+    template <typename K>
+    cudaError_t
+    prepare(K kernel, size_t smem)
+    {
+      if (smem > 48 * 1024)
+        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem));
+      return cudaSuccess;
+    }
+
+    template <int N, typename T, int NC, class Op, bool CON>
+    cudaError_t
+    run_apply(const Shape<N, T> &sh, const CellGeom<T> &cg, const Op &op,
+              const T *src, T *dst, cudaStream_t s)
+    {
+      constexpr int CPB  = cells_per_block<N, NC, T>();
+      const size_t  smem = size_t(CPB) * smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
+      auto          k    = cell_apply_kernel<N, T, NC, Op, CON>;
+      cudaError_t   e    = prepare(k, smem);
+      if (e != cudaSuccess)
+        return e;
+      const unsigned grid = (cg.n_cells + CPB - 1) / CPB;
+      k<<<grid, CPB * N * N, smem, s>>>(sh, cg, op, src, dst);
+      return cudaGetLastError();
+    }
+
+    template <int N, typename T, int NC, class Op>
+    cudaError_t
+    run_apply_c(bool con, const Shape<N, T> &sh, const CellGeom<T> &cg,
+                const Op &op, const T *src, T *dst, cudaStream_t s)
+    {
+      return con ? run_apply<N, T, NC, Op, true>(sh, cg, op, src, dst, s) :
+                   run_apply<N, T, NC, Op, false>(sh, cg, op, src, dst, s);
+    }
+  } // namespace
+
+  template <int N, typename T>
+  cudaError_t
+  launch_apply(const HostBasis &b, const LevelGeom &g, const ApplyArgs &a,
+               cudaStream_t s)
+  {
+    const Shape<N, T>    sh  = make_shape<N, T>(b);
+    const CellGeom<T>    cg  = make_cell_geom<T>(g);
+    const T             *src = static_cast<const T *>(a.src);
+    T                   *dst = static_cast<T *>(a.dst);
+    constexpr int        N3  = N * N * N;
+    if (a.kind == 0)
+      {
+        HeatQOp<T> op;
+        op.kdt = T(a.kdt);
+        return run_apply_c<N, T, 1>(a.constrained, sh, cg, op, src, dst, s);
+      }
+    const NHMat<T> m     = to_mat<T>(a.mat);
+    const T       *cache = static_cast<const T *>(a.cache);
+    switch (a.var)
+      {
+        case V_SCALAR_REF:
+          {
+            NHScalarRefQOp<T> op;
+            op.ucell  = static_cast<const T *>(a.ucell);
+            op.scalar = cache;
+            op.m      = m;
+            op.n3     = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+        case V_QP10:
+          {
+            NHQp10QOp<T> op;
+            op.cache = cache;
+            op.m     = m;
+            op.n3    = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+        case V_TENSOR2:
+          {
+            NHCachedQOp<T, V_TENSOR2> op;
+            op.cache = cache;
+            op.m     = m;
+            op.n3    = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+        case V_TENSOR4:
+          {
+            NHCachedQOp<T, V_TENSOR4> op;
+            op.cache = cache;
+            op.m     = m;
+            op.n3    = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+        case V_TENSOR4_NS:
+          {
+            NHCachedQOp<T, V_TENSOR4_NS> op;
+            op.cache = cache;
+            op.m     = m;
+            op.n3    = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+        case V_FORM0:
+          {
+            NHCachedQOp<T, V_FORM0> op;
+            op.cache = cache;
+            op.m     = m;
+            op.n3    = N3;
+            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+          }
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  template <int N, typename T>
+  cudaError_t
+  launch_nh_cache(const HostBasis &b, const LevelGeom &g, int var,
+                  const NHMatD &md, const void *u, void *cache, void *ucell,
+                  int *err, cudaStream_t s)
+  {
+    const Shape<N, T>  sh   = make_shape<N, T>(b);
+    const CellGeom<T>  cg   = make_cell_geom<T>(g);
+    const NHMat<T>     m    = to_mat<T>(md);
+    constexpr int      CPB  = cells_per_block<N, 3, T>();
+    const size_t       smem = size_t(CPB) * smem_per_cell<N, 3, false>() * sizeof(T);
+    const unsigned     grid = (cg.n_cells + CPB - 1) / CPB;
+    const T           *uu   = static_cast<const T *>(u);
+    T                 *cp   = static_cast<T *>(cache);
+    T                 *uc   = static_cast<T *>(ucell);
+    cudaError_t        e    = cudaSuccess;
+#define MF_CACHE_CASE(V)                                                      \
+  case V:                                                                     \
+    {                                                                         \
+      auto k = nh_cache_kernel<N, T, V>;                                      \
+      if ((e = prepare(k, smem)) != cudaSuccess)                              \
+        return e;                                                             \
+      k<<<grid, CPB * N * N, smem, s>>>(sh, cg, m, uu, cp, uc, err);          \
+      return cudaGetLastError();                                              \
+    }
+    switch (var)
+      {
+        MF_CACHE_CASE(V_SCALAR_REF)
+        MF_CACHE_CASE(V_TENSOR2)
+        MF_CACHE_CASE(V_TENSOR4)
+        MF_CACHE_CASE(V_TENSOR4_NS)
+        MF_CACHE_CASE(V_QP10)
+        MF_CACHE_CASE(V_FORM0)
+      }
+#undef MF_CACHE_CASE
+    return cudaErrorInvalidValue;
+  }
+
+  template <int N, typename T>
+  cudaError_t
+  launch_diag(const HostBasis &b, const LevelGeom &g, int kind,
+              const NHMatD &md, double kdt, const void *u, void *diag,
+              cudaStream_t s)
+  {
+    const Shape<N, T>  sh = make_shape<N, T>(b);
+    DiagShape<N, T>    ds;
+    for (int q = 0; q < N; ++q)
+      for (int i = 0; i < N; ++i)
+        {
+          const double sv = b.S[q * N + i], gv = b.G[q * N + i];
+          ds.SS[q * N + i] = T(sv * sv);
+          ds.SG[q * N + i] = T(sv * gv);
+          ds.GG[q * N + i] = T(gv * gv);
+        }
+    for (int i = 0; i < N; ++i)
+      ds.w[i] = T(b.w[i]);
+    const CellGeom<T> cg   = make_cell_geom<T>(g);
+    const NHMat<T>    m    = to_mat<T>(md);
+    constexpr int     CPB  = cells_per_block<N, 3, T>();
+    constexpr int     N3   = N * N * N;
+    const unsigned    grid = (cg.n_cells + CPB - 1) / CPB;
+    const T          *uu   = static_cast<const T *>(u);
+    T                *dg   = static_cast<T *>(diag);
+    cudaError_t       e;
+#define MF_DIAG_CASE(K)                                                       \
+  case K:                                                                     \
+    {                                                                         \
+      const size_t smem = size_t(CPB) * ((K == 0 ? 0 : 12 * N3) + 9 * N3) * sizeof(T); \
+      auto         k    = diag_kernel<N, T, K>;                               \
+      if ((e = prepare(k, smem)) != cudaSuccess)                              \
+        return e;                                                             \
+      k<<<grid, CPB * N * N, smem, s>>>(sh, ds, cg, m, T(kdt), uu, dg);      \
+      return cudaGetLastError();                                              \
+    }
+    switch (kind)
+      {
+        MF_DIAG_CASE(0)
+        MF_DIAG_CASE(1)
+        MF_DIAG_CASE(2)
+      }
+#undef MF_DIAG_CASE
+    return cudaErrorInvalidValue;
+  }
+
+  template <int N>
+  cudaError_t
+  launch_residual(const HostBasis &b, const LevelGeom &g, int form,
+                  const NHMatD &md, double rho, const double *body,
+                  const double *u, const double *acc, double *rhs,
+                  cudaStream_t s)
+  {
+    const Shape<N, double>    sh   = make_shape<N, double>(b);
+    const CellGeom<double>    cg   = make_cell_geom<double>(g);
+    const NHMat<double>       m    = to_mat<double>(md);
+    constexpr int             CPB  = cells_per_block<N, 3, double>();
+    constexpr int             N3   = N * N * N;
+    const size_t              smem = size_t(CPB) * (smem_per_cell<N, 3, false>() + 3 * N3) * sizeof(double);
+    const unsigned            grid = (cg.n_cells + CPB - 1) / CPB;
+    cudaError_t               e;
+    if (form == 1)
+      {
+        auto k = residual_kernel<N, double, 1>;
+        if ((e = prepare(k, smem)) != cudaSuccess)
+          return e;
+        k<<<grid, CPB * N * N, smem, s>>>(sh, cg, m, rho, body[0], body[1], body[2], u, acc, rhs);
+      }
+    else
+      {
+        auto k = residual_kernel<N, double, 0>;
+        if ((e = prepare(k, smem)) != cudaSuccess)
+          return e;
+        k<<<grid, CPB * N * N, smem, s>>>(sh, cg, m, rho, body[0], body[1], body[2], u, acc, rhs);
+      }
+    return cudaGetLastError();
+  }
+
+  template <int N>
+  cudaError_t
+  launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
+                  const SourceDesc &f, const double *u_old, double *rhs,
+                  cudaStream_t s)
+  {
+    const Shape<N, double>  sh = make_shape<N, double>(b);
+    const CellGeom<double>  cg = make_cell_geom<double>(g);
+    SourceDev               sd;
+    std::memset(&sd, 0, sizeof(sd));
+    sd.constant = f.constant;
+    sd.n_gauss  = f.n_gauss;
+    for (int i = 0; i < 8; ++i)
+      {
+        for (int d = 0; d < 3; ++d)
+          sd.center[i][d] = f.center[i][d];
+        sd.width[i] = f.width[i];
+        sd.amp[i]   = f.amp[i];
+      }
+    for (int d = 0; d < 3; ++d)
+      {
+        sd.lo[d] = g.lo[d];
+        sd.h[d]  = g.h[d];
+      }
+    for (int i = 0; i < N; ++i)
+      sd.xq[i] = b.xq[i];
+    constexpr int  CPB  = cells_per_block<N, 1, double>();
+    const size_t   smem = size_t(CPB) * smem_per_cell<N, 1, false>() * sizeof(double);
+    const unsigned grid = (cg.n_cells + CPB - 1) / CPB;
+    auto           k    = heat_rhs_kernel<N>;
+    cudaError_t    e    = prepare(k, smem);
+    if (e != cudaSuccess)
+      return e;
+    k<<<grid, CPB * N * N, smem, s>>>(sh, cg, sd, dt, u_old, rhs);
+    return cudaGetLastError();
+  }
+
+  template cudaError_t launch_apply<MF_N, double>(const HostBasis &, const LevelGeom &, const ApplyArgs &, cudaStream_t);
+  template cudaError_t launch_apply<MF_N, float>(const HostBasis &, const LevelGeom &, const ApplyArgs &, cudaStream_t);
+  template cudaError_t launch_nh_cache<MF_N, double>(const HostBasis &, const LevelGeom &, int, const NHMatD &, const void *, void *, void *, int *, cudaStream_t);
+  template cudaError_t launch_nh_cache<MF_N, float>(const HostBasis &, const LevelGeom &, int, const NHMatD &, const void *, void *, void *, int *, cudaStream_t);
+  template cudaError_t launch_diag<MF_N, double>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const void *, void *, cudaStream_t);
+  template cudaError_t launch_diag<MF_N, float>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const void *, void *, cudaStream_t);
+  template cudaError_t launch_residual<MF_N>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const double *, const double *, const double *, double *, cudaStream_t);
+  template cudaError_t launch_heat_rhs<MF_N>(const HostBasis &, const LevelGeom &, double, const SourceDesc &, const double *, double *, cudaStream_t);
+} // namespace mfgpu

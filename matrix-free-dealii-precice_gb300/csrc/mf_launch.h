@@ -1,0 +1,85 @@
+// Host-side launch interface of the cell kernels (instantiated per degree
+// in mf_kernels.cu, one translation unit per N = p+1).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mf_common.cuh"
+
+namespace mfgpu
+{
+  // 1D data of one degree on the host, double precision
+  struct HostBasis
+  {
+    int    N = 0;
+    double nodes[MAX_N];      // Gauss-Lobatto support points on [0,1]
+    double xq[MAX_N];         // Gauss points on [0,1]
+    double w[MAX_N];          // Gauss weights
+    double S[MAX_N * MAX_N];  // [q][i] nodal basis at Gauss points
+    double D[MAX_N * MAX_N];  // [q][r] collocation derivative on Gauss points
+    double G[MAX_N * MAX_N];  // [q][i] derivative of nodal basis at Gauss points
+    double Ge[2][MAX_N];      // derivative of nodal basis at 0 and 1
+  };
+
+  void make_host_basis(int degree, HostBasis &b);
+
+  struct NHMatD
+  {
+    double mu, lambda, rho_alpha, kappa, c_1;
+  };
+
+  // operator application: dst += A src (cell part only)
+  //   kind 0: heat (param kdt); kind 1: neo-Hookean with variant var
+  struct ApplyArgs
+  {
+    int         kind;
+    int         var;
+    bool        constrained;
+    double      kdt;
+    NHMatD      mat;
+    const void *cache;
+    const void *ucell;
+    const void *src;
+    void       *dst;
+  };
+
+  template <int N, typename T>
+  cudaError_t launch_apply(const HostBasis &b, const LevelGeom &g,
+                           const ApplyArgs &a, cudaStream_t s);
+
+  template <int N, typename T>
+  cudaError_t launch_nh_cache(const HostBasis &b, const LevelGeom &g, int var,
+                              const NHMatD &m, const void *u, void *cache,
+                              void *ucell, int *err, cudaStream_t s);
+
+  // kind 0 heat, 1 NH formulation 1, 2 NH formulation 0; diag += local diags
+  template <int N, typename T>
+  cudaError_t launch_diag(const HostBasis &b, const LevelGeom &g, int kind,
+                          const NHMatD &m, double kdt, const void *u,
+                          void *diag, cudaStream_t s);
+
+  template <int N>
+  cudaError_t launch_residual(const HostBasis &b, const LevelGeom &g, int form,
+                              const NHMatD &m, double rho, const double *body,
+                              const double *u, const double *acc, double *rhs,
+                              cudaStream_t s);
+
+  // heat right-hand side: rhs += int (u_old + dt f) v, f = constant +
+  // sum of Gaussians
+  struct SourceDesc
+  {
+    double constant;
+    int    n_gauss;
+    double center[8][3];
+    double width[8];
+    double amp[8];
+  };
+
+  template <int N>
+  cudaError_t launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
+                              const SourceDesc &f, const double *u_old,
+                              double *rhs, cudaStream_t s);
+
+  // number of cells per block / dynamic shared memory (for reporting)
+  int apply_cells_per_block(int N, int nc, int tsize);
+} // namespace mfgpu

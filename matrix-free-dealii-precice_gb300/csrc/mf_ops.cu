@@ -1,0 +1,1007 @@
+// Host side of the operators: basis data, context, vector kernels, the
+// heat and neo-Hookean operators (vmult, compute_diagonal, cache) and the
+// multigrid transfer.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "mf_host.h"
+#include "mf_vec.cuh"
+
+namespace mfgpu
+{
+  // ---------------------------------------------------------------------
+  // errors, launch counting
+  // ---------------------------------------------------------------------
+  static std::atomic<long long> g_launches{0};
+  void
+  count_launch(int n)
+  {
+    g_launches += n;
+  }
+  long long
+  launch_count()
+  {
+    return g_launches.load();
+  }
+
+  void
+  check_cuda(cudaError_t e, const char *what)
+  {
+    if (e == cudaSuccess)
+      return;
+    if (e == cudaErrorMemoryAllocation)
+      throw Error(ERR_OOM, std::string("out of device memory: ") + what);
+    throw Error(ERR_CUDA, std::string(cudaGetErrorString(e)) + " in " + what);
+  }
+
+  void
+  DevBuf::alloc(size_t b)
+  {
+    release();
+    if (b == 0)
+      return;
+    cudaError_t e = cudaMalloc(&ptr, b);
+    if (e != cudaSuccess)
+      {
+        ptr = nullptr;
+        (void)cudaGetLastError();
+        throw Error(ERR_OOM, "cudaMalloc of " + std::to_string(b) + " bytes failed");
+      }
+    bytes = b;
+  }
+
+  void
+  DevBuf::release()
+  {
+    if (ptr)
+      cudaFree(ptr);
+    ptr   = nullptr;
+    bytes = 0;
+  }
+
+  // ---------------------------------------------------------------------
+  // 1D basis: FE_Q(p) on Gauss-Lobatto points, QGauss(p+1), collocation
+  // derivative on the Gauss points
+  // ---------------------------------------------------------------------
+  namespace
+  {
+    void
+    legendre_ld(int n, long double x, long double &p, long double &dp)
+    {
+      long double p0 = 1, p1 = x;
+      if (n == 0)
+        {
+          p  = 1;
+          dp = 0;
+          return;
+        }
+      for (int k = 2; k <= n; ++k)
+        {
+          const long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+          p0                   = p1;
+          p1                   = p2;
+        }
+      p  = p1;
+      dp = n * (x * p1 - p0) / (x * x - 1);
+    }
+
+    long double
+    lagr(const long double *x, int n, int i, long double t)
+    {
+      long double v = 1;
+      for (int j = 0; j < n; ++j)
+        if (j != i)
+          v *= (t - x[j]) / (x[i] - x[j]);
+      return v;
+    }
+
+    long double
+    lagr_d(const long double *x, int n, int i, long double t)
+    {
+      long double s = 0;
+      for (int k = 0; k < n; ++k)
+        {
+          if (k == i)
+            continue;
+          long double v = 1 / (x[i] - x[k]);
+          for (int j = 0; j < n; ++j)
+            if (j != i && j != k)
+              v *= (t - x[j]) / (x[i] - x[j]);
+          s += v;
+        }
+      return s;
+    }
+  } // namespace
+
+  void
+  make_host_basis(int degree, HostBasis &b)
+  {
+    if (degree < 1 || degree > MAX_N - 1)
+      throw Error(ERR_UNSUPPORTED, "degree must be 1..6");
+    const int   N  = degree + 1;
+    const long double pi = 3.14159265358979323846264338327950288L;
+    long double gl[MAX_N], gq[MAX_N], wq[MAX_N];
+    b.N   = N;
+    gl[0] = 0;
+    gl[degree] = 1;
+    for (int i = 1; i < degree; ++i)
+      {
+        long double z = -std::cos(pi * i / degree);
+        for (int it = 0; it < 100; ++it)
+          {
+            long double p, dp;
+            legendre_ld(degree, z, p, dp);
+            const long double d2 = (2 * z * dp - degree * (degree + 1) * p) / (1 - z * z);
+            const long double dz = dp / d2;
+            z -= dz;
+            if (std::fabs(double(dz)) < 1e-19)
+              break;
+          }
+        gl[i] = (1 + z) / 2;
+      }
+    for (int i = 0; i < N; ++i)
+      {
+        long double z = std::cos(pi * (i + 0.75L) / (N + 0.5L));
+        long double p, dp;
+        for (int it = 0; it < 100; ++it)
+          {
+            legendre_ld(N, z, p, dp);
+            const long double dz = p / dp;
+            z -= dz;
+            if (std::fabs(double(dz)) < 1e-19)
+              break;
+          }
+        legendre_ld(N, z, p, dp);
+        gq[N - 1 - i] = (1 + z) / 2;
+        wq[N - 1 - i] = 1 / ((1 - z * z) * dp * dp);
+      }
+    for (int i = 0; i < N; ++i)
+      {
+        b.nodes[i] = double(gl[i]);
+        b.xq[i]    = double(gq[i]);
+        b.w[i]     = double(wq[i]);
+      }
+    for (int q = 0; q < N; ++q)
+      for (int i = 0; i < N; ++i)
+        {
+          b.S[q * N + i] = double(lagr(gl, N, i, gq[q]));
+          b.G[q * N + i] = double(lagr_d(gl, N, i, gq[q]));
+          b.D[q * N + i] = double(lagr_d(gq, N, i, gq[q]));
+        }
+    for (int i = 0; i < N; ++i)
+      {
+        b.Ge[0][i] = double(lagr_d(gl, N, i, 0.0L));
+        b.Ge[1][i] = double(lagr_d(gl, N, i, 1.0L));
+      }
+  }
+
+  LevelGeom
+  Mesh::level(int l) const
+  {
+    if (l < 0)
+      l = n_ref;
+    if (l > n_ref)
+      throw Error(ERR_ARG, "level beyond the number of refinements");
+    LevelGeom g;
+    g.p       = degree;
+    g.n_nodes = 1;
+    g.n_cells = 1;
+    for (int d = 0; d < 3; ++d)
+      {
+        g.C[d]  = rep[d] << l;
+        g.Nn[d] = g.C[d] * degree + 1;
+        g.lo[d] = lo[d];
+        g.h[d]  = (hi[d] - lo[d]) / g.C[d];
+        g.n_nodes *= size_t(g.Nn[d]);
+        g.n_cells *= size_t(g.C[d]);
+      }
+    for (int f = 0; f < 6; ++f)
+      {
+        g.face_mask[f] = 0;
+        for (int i = 0; i < n_dirichlet; ++i)
+          if (boundary_id[f] == dirichlet_id[i])
+            g.face_mask[f] |= dirichlet_mask[i];
+      }
+    return g;
+  }
+
+  // ---------------------------------------------------------------------
+  // context
+  // ---------------------------------------------------------------------
+  Context::Context(int dev)
+    : device(dev)
+  {
+    MF_CK(cudaSetDevice(dev));
+    MF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    err.alloc(sizeof(int) * 4);
+    partial.alloc(sizeof(double) * RED_BLOCKS);
+    scalars.alloc(sizeof(double) * 32);
+    MF_CK(cudaMemsetAsync(err.ptr, 0, err.bytes, stream));
+    MF_CK(cudaMemsetAsync(scalars.ptr, 0, scalars.bytes, stream));
+    MF_CK(cudaMallocHost(&host_scalars, sizeof(double) * 32));
+    MF_CK(cudaStreamSynchronize(stream));
+  }
+
+  Context::~Context()
+  {
+    if (stream)
+      cudaStreamSynchronize(stream);
+    if (host_scalars)
+      cudaFreeHost(host_scalars);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+
+  int
+  Context::take_error_flags()
+  {
+    int h = 0;
+    MF_CK(cudaMemcpyAsync(&h, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    MF_CK(cudaStreamSynchronize(stream));
+    if (h)
+      MF_CK(cudaMemsetAsync(err.ptr, 0, sizeof(int), stream));
+    return h;
+  }
+
+  void
+  Context::sync()
+  {
+    MF_CK(cudaStreamSynchronize(stream));
+  }
+
+  double *
+  scalar_slots(Context &c)
+  {
+    return c.scalars.as<double>();
+  }
+
+  void
+  read_scalars(Context &c, int n)
+  {
+    MF_CK(cudaMemcpyAsync(c.host_scalars, c.scalars.ptr, sizeof(double) * n,
+                          cudaMemcpyDeviceToHost, c.stream));
+    MF_CK(cudaStreamSynchronize(c.stream));
+  }
+
+  // ---------------------------------------------------------------------
+  // vector kernels
+  // ---------------------------------------------------------------------
+  static inline unsigned
+  grid_for(size_t n, int threads = 256)
+  {
+    const size_t g = (n + threads - 1) / threads;
+    return unsigned(std::min<size_t>(std::max<size_t>(g, 1), 152 * 16));
+  }
+
+  template <typename T>
+  void
+  vec_fill(Context &c, size_t n, T v, T *x)
+  {
+    k_fill<<<grid_for(n), 256, 0, c.stream>>>(n, v, x);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_axpby(Context &c, size_t n, T a, const T *x, T b, T *y)
+  {
+    k_axpby<<<grid_for(n), 256, 0, c.stream>>>(n, a, x, b, y);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_axpbyz(Context &c, size_t n, T a, const T *x, T b, const T *y, T *z)
+  {
+    k_axpbyz<<<grid_for(n), 256, 0, c.stream>>>(n, a, x, b, y, z);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_copy(Context &c, size_t n, const T *x, T *y)
+  {
+    MF_CK(cudaMemcpyAsync(y, x, n * sizeof(T), cudaMemcpyDeviceToDevice, c.stream));
+  }
+  template <typename TD, typename TS>
+  void
+  vec_convert(Context &c, size_t n, const TS *s, TD *d)
+  {
+    k_convert<TD, TS><<<grid_for(n), 256, 0, c.stream>>>(n, s, d);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_scale(Context &c, size_t n, T omega, const T *d, const T *x, T *y)
+  {
+    k_scale<<<grid_for(n), 256, 0, c.stream>>>(n, omega, d, x, y);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_invert(Context &c, size_t n, T *x)
+  {
+    k_invert<<<grid_for(n), 256, 0, c.stream>>>(n, x, c.err.as<int>());
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot)
+  {
+    k_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>());
+    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, c.partial.as<double>(),
+                                                    scalar_slots(c) + slot);
+    count_launch(2);
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  double
+  vec_dot(Context &c, size_t n, const T *x, const T *y)
+  {
+    vec_dot_dev(c, n, x, y, 31);
+    double h;
+    MF_CK(cudaMemcpyAsync(&h, scalar_slots(c) + 31, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MF_CK(cudaStreamSynchronize(c.stream));
+    return h;
+  }
+  template <typename T>
+  void
+  cg_update(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p,
+            T *r, const T *q, int rr_slot)
+  {
+    double *s = scalar_slots(c);
+    k_cg_update<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+                                                          c.partial.as<double>());
+    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, c.partial.as<double>(), s + rr_slot);
+    count_launch(2);
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p)
+  {
+    double *s = scalar_slots(c);
+    k_cg_direction<<<grid_for(n), 256, 0, c.stream>>>(n, s + num_slot, s + den_slot, z, p);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold)
+  {
+    k_cheby_start<<<grid_for(n), 256, 0, c.stream>>>(n, f, b, dinv, x, xold);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b,
+               const T *Ax, const T *dinv, T *x, T *xold)
+  {
+    k_cheby_update<<<grid_for(n), 256, 0, c.stream>>>(n, f1, f2, int(first), b, Ax, dinv, x, xold);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst)
+  {
+    bool any = false;
+    for (int f = 0; f < 6; ++f)
+      any |= g.face_mask[f] != 0;
+    if (!any)
+      return;
+    FaceInfo fi;
+    for (int d = 0; d < 3; ++d)
+      fi.Nn[d] = g.Nn[d];
+    fi.n_nodes = g.n_nodes;
+    for (int f = 0; f < 6; ++f)
+      fi.face_mask[f] = g.face_mask[f];
+    fi.nc = nc;
+    size_t maxface = 0;
+    for (int d = 0; d < 3; ++d)
+      maxface = std::max(maxface, g.n_nodes / size_t(g.Nn[d]));
+    dim3 grid(unsigned(std::min<size_t>((maxface + 255) / 256, 1024)), 6);
+    k_constrained<<<grid, 256, 0, c.stream>>>(fi, op, src, dst);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+
+#define MF_INST_VEC(T)                                                                      \
+  template void vec_fill<T>(Context &, size_t, T, T *);                                     \
+  template void vec_axpby<T>(Context &, size_t, T, const T *, T, T *);                      \
+  template void vec_axpbyz<T>(Context &, size_t, T, const T *, T, const T *, T *);          \
+  template void vec_copy<T>(Context &, size_t, const T *, T *);                             \
+  template void vec_scale<T>(Context &, size_t, T, const T *, const T *, T *);              \
+  template void vec_invert<T>(Context &, size_t, T *);                                      \
+  template void vec_dot_dev<T>(Context &, size_t, const T *, const T *, int);               \
+  template double vec_dot<T>(Context &, size_t, const T *, const T *);                      \
+  template void cg_update<T>(Context &, size_t, int, int, T *, const T *, T *, const T *, int); \
+  template void cg_direction<T>(Context &, size_t, int, int, const T *, T *);               \
+  template void cheby_start<T>(Context &, size_t, T, const T *, const T *, T *, T *);       \
+  template void cheby_update<T>(Context &, size_t, T, T, bool, const T *, const T *, const T *, T *, T *); \
+  template void constrained_op<T>(Context &, const LevelGeom &, int, int, const T *, T *);
+  MF_INST_VEC(float)
+  MF_INST_VEC(double)
+  template void vec_convert<float, double>(Context &, size_t, const double *, float *);
+  template void vec_convert<double, float>(Context &, size_t, const float *, double *);
+  template void vec_convert<double, double>(Context &, size_t, const double *, double *);
+  template void vec_convert<float, float>(Context &, size_t, const float *, float *);
+
+  // ---------------------------------------------------------------------
+  // dispatch over the degree
+  // ---------------------------------------------------------------------
+  template <typename T>
+  static cudaError_t
+  dispatch_apply(int N, const HostBasis &b, const LevelGeom &g, const ApplyArgs &a, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_apply<2, T>(b, g, a, s);
+        case 3: return launch_apply<3, T>(b, g, a, s);
+        case 4: return launch_apply<4, T>(b, g, a, s);
+        case 5: return launch_apply<5, T>(b, g, a, s);
+        case 6: return launch_apply<6, T>(b, g, a, s);
+        case 7: return launch_apply<7, T>(b, g, a, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  template <typename T>
+  static cudaError_t
+  dispatch_cache(int N, const HostBasis &b, const LevelGeom &g, int var, const NHMatD &m,
+                 const void *u, void *cache, void *ucell, int *err, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_nh_cache<2, T>(b, g, var, m, u, cache, ucell, err, s);
+        case 3: return launch_nh_cache<3, T>(b, g, var, m, u, cache, ucell, err, s);
+        case 4: return launch_nh_cache<4, T>(b, g, var, m, u, cache, ucell, err, s);
+        case 5: return launch_nh_cache<5, T>(b, g, var, m, u, cache, ucell, err, s);
+        case 6: return launch_nh_cache<6, T>(b, g, var, m, u, cache, ucell, err, s);
+        case 7: return launch_nh_cache<7, T>(b, g, var, m, u, cache, ucell, err, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  template <typename T>
+  static cudaError_t
+  dispatch_diag(int N, const HostBasis &b, const LevelGeom &g, int kind, const NHMatD &m,
+                double kdt, const void *u, void *diag, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_diag<2, T>(b, g, kind, m, kdt, u, diag, s);
+        case 3: return launch_diag<3, T>(b, g, kind, m, kdt, u, diag, s);
+        case 4: return launch_diag<4, T>(b, g, kind, m, kdt, u, diag, s);
+        case 5: return launch_diag<5, T>(b, g, kind, m, kdt, u, diag, s);
+        case 6: return launch_diag<6, T>(b, g, kind, m, kdt, u, diag, s);
+        case 7: return launch_diag<7, T>(b, g, kind, m, kdt, u, diag, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  // ---------------------------------------------------------------------
+  // operators
+  // ---------------------------------------------------------------------
+  void
+  Operator::vmult(void *dst, const void *src)
+  {
+    // dst = 0 except constrained rows dst = src, then dst += A src
+    MF_CK(cudaMemsetAsync(dst, 0, m() * elem_size(), ctx->stream));
+    if (constrained)
+      {
+        if (precision == 32)
+          constrained_op<float>(*ctx, geom, nc, 0, (const float *)src, (float *)dst);
+        else
+          constrained_op<double>(*ctx, geom, nc, 0, (const double *)src, (double *)dst);
+      }
+    apply_cells(dst, src);
+  }
+
+  void
+  Operator::vmult_add(void *dst, const void *src)
+  {
+    apply_cells(dst, src);
+    if (constrained)
+      {
+        if (precision == 32)
+          constrained_op<float>(*ctx, geom, nc, 1, (const float *)src, (float *)dst);
+        else
+          constrained_op<double>(*ctx, geom, nc, 1, (const double *)src, (double *)dst);
+      }
+  }
+
+  void
+  Operator::finish_diagonal()
+  {
+    // set_constrained_entries_to_one, keep a copy of the diagonal, invert
+    if (precision == 32)
+      {
+        constrained_op<float>(*ctx, geom, nc, 3, nullptr, inv_diag.as<float>());
+        vec_copy<float>(*ctx, m(), inv_diag.as<float>(), diag.as<float>());
+        vec_invert<float>(*ctx, m(), inv_diag.as<float>());
+      }
+    else
+      {
+        constrained_op<double>(*ctx, geom, nc, 3, nullptr, inv_diag.as<double>());
+        vec_copy<double>(*ctx, m(), inv_diag.as<double>(), diag.as<double>());
+        vec_invert<double>(*ctx, m(), inv_diag.as<double>());
+      }
+    const int f = ctx->take_error_flags();
+    diag_ready  = true;
+    if (f & 2)
+      throw Error(ERR_NONFINITE, "non-positive diagonal entry in a positive definite operator");
+  }
+
+  void
+  HeatOperator::apply_cells(void *dst, const void *src)
+  {
+    if (delta_t <= 0)
+      throw Error(ERR_STATE, "delta_t not set (set_delta_t)");
+    ApplyArgs a{};
+    a.kind        = 0;
+    a.constrained = constrained;
+    a.kdt         = coefficient * delta_t;
+    a.src         = src;
+    a.dst         = dst;
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
+    count_launch();
+    MF_CK(e);
+  }
+
+  void
+  HeatOperator::compute_diagonal()
+  {
+    if (delta_t <= 0)
+      throw Error(ERR_STATE, "delta_t not set (set_delta_t)");
+    inv_diag.alloc(m() * elem_size());
+    diag.alloc(m() * elem_size());
+    MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
+    NHMatD      md{};
+    cudaError_t e = precision == 32 ?
+                      dispatch_diag<float>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream) :
+                      dispatch_diag<double>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream);
+    count_launch();
+    MF_CK(e);
+    finish_diagonal();
+  }
+
+  int
+  parse_caching(const char *s)
+  {
+    const std::string c = s ? s : "scalar_referential";
+    if (c == "scalar_referential")
+      return V_SCALAR_REF;
+    if (c == "tensor2")
+      return V_TENSOR2;
+    if (c == "tensor4")
+      return V_TENSOR4;
+    if (c == "tensor4_ns")
+      return V_TENSOR4_NS;
+    if (c == "referential_qp")
+      return V_QP10;
+    throw Error(ERR_ARG, "unknown caching '" + c + "'");
+  }
+
+  NHMatD
+  make_material(double mu, double nu, double rho, double alpha_1)
+  {
+    // material.h:78-94
+    NHMatD m;
+    m.kappa     = (2.0 * mu * (1.0 + nu)) / (3.0 * (1.0 - 2.0 * nu));
+    m.c_1       = mu / 2.0;
+    m.mu        = mu;
+    m.rho_alpha = rho * alpha_1;
+    m.lambda    = (2.0 * mu * nu) / (1.0 - 2.0 * nu);
+    if (!(m.kappa > 0))
+      throw Error(ERR_ARG, "material: kappa must be positive");
+    return m;
+  }
+
+  void
+  NHOperator::do_cache()
+  {
+    if (!u)
+      throw Error(ERR_STATE, "NeoHookOperator: initialize() with a displacement first");
+    if (!have_material)
+      throw Error(ERR_STATE, "NeoHookOperator: set_material() first");
+    int var = variant;
+    if (formulation == 0)
+      {
+        if (variant != V_TENSOR2)
+          throw Error(ERR_UNSUPPORTED, "formulation 0 requires tensor2 caching");
+        var = V_FORM0;
+      }
+    const int    N3 = basis.N * basis.N * basis.N;
+    const size_t nq = geom.n_cells * size_t(N3);
+    const size_t want = nq * nh_cache_fields(var) * elem_size();
+    if (cache.bytes != want)
+      cache.alloc(want);
+    if (var == V_SCALAR_REF)
+      {
+        const size_t wu = nq * 3 * elem_size();
+        if (ucell.bytes != wu)
+          ucell.alloc(wu);
+      }
+    else
+      ucell.release();
+    cudaError_t e = precision == 32 ?
+                      dispatch_cache<float>(basis.N, basis, geom, var, mat, u, cache.ptr, ucell.ptr, ctx->err.as<int>(), ctx->stream) :
+                      dispatch_cache<double>(basis.N, basis, geom, var, mat, u, cache.ptr, ucell.ptr, ctx->err.as<int>(), ctx->stream);
+    count_launch();
+    MF_CK(e);
+    const int f = ctx->take_error_flags();
+    if (f & 1)
+      {
+        cached = false;
+        throw Error(ERR_DET_F, "det_F is not positive");
+      }
+    cached = true;
+  }
+
+  void
+  NHOperator::apply_cells(void *dst, const void *src)
+  {
+    if (!cached)
+      throw Error(ERR_STATE, "NeoHookOperator: cache() before vmult");
+    ApplyArgs a{};
+    a.kind        = 1;
+    a.var         = formulation == 0 ? int(V_FORM0) : variant;
+    a.constrained = constrained;
+    a.mat         = mat;
+    a.cache       = cache.ptr;
+    a.ucell       = ucell.ptr;
+    a.src         = src;
+    a.dst         = dst;
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
+    count_launch();
+    MF_CK(e);
+  }
+
+  void
+  NHOperator::compute_diagonal()
+  {
+    if (!u || !have_material)
+      throw Error(ERR_STATE, "NeoHookOperator: initialize() and set_material() first");
+    inv_diag.alloc(m() * elem_size());
+    diag.alloc(m() * elem_size());
+    MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
+    const int   kind = formulation == 0 ? 2 : 1;
+    cudaError_t e    = precision == 32 ?
+                         dispatch_diag<float>(basis.N, basis, geom, kind, mat, 0.0, u, inv_diag.ptr, ctx->stream) :
+                         dispatch_diag<double>(basis.N, basis, geom, kind, mat, 0.0, u, inv_diag.ptr, ctx->stream);
+    count_launch();
+    MF_CK(e);
+    finish_diagonal();
+  }
+
+  void
+  NHOperator::clear()
+  {
+    cache.release();
+    ucell.release();
+    inv_diag.release();
+    diag.release();
+    cached     = false;
+    diag_ready = false;
+    u          = nullptr;
+  }
+
+  static void
+  init_op(Operator &op, Context *c, const Mesh &m, int level, int precision)
+  {
+    if (precision != 32 && precision != 64)
+      throw Error(ERR_ARG, "precision must be 32 or 64");
+    if (m.n_q != m.degree + 1)
+      throw Error(ERR_UNSUPPORTED, "the device kernels need n_q_1d == degree + 1");
+    op.ctx       = c;
+    op.mesh      = m;
+    op.level     = level < 0 ? m.n_ref : level;
+    op.geom      = m.level(op.level);
+    op.precision = precision;
+    make_host_basis(m.degree, op.basis);
+    if (op.geom.n_cells >= (size_t(1) << 31))
+      throw Error(ERR_UNSUPPORTED, "too many cells");
+  }
+
+  std::unique_ptr<HeatOperator>
+  make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained)
+  {
+    std::unique_ptr<HeatOperator> op(new HeatOperator());
+    init_op(*op, c, m, level, precision);
+    op->nc          = 1;
+    op->constrained = constrained;
+    return op;
+  }
+
+  std::unique_ptr<NHOperator>
+  make_nh(Context *c, const Mesh &m, int level, int precision, int variant)
+  {
+    std::unique_ptr<NHOperator> op(new NHOperator());
+    init_op(*op, c, m, level, precision);
+    op->nc      = 3;
+    op->variant = variant;
+    return op;
+  }
+
+  // ---------------------------------------------------------------------
+  // transfer
+  // ---------------------------------------------------------------------
+  namespace
+  {
+    double
+    lagr_nodes(const double *x, int n, int i, double t)
+    {
+      double v = 1;
+      for (int j = 0; j < n; ++j)
+        if (j != i)
+          v *= (t - x[j]) / (x[i] - x[j]);
+      return v;
+    }
+  } // namespace
+
+  Transfer::Transfer(Context *c, const HostBasis &b, const LevelGeom &cg,
+                     const LevelGeom &fg, int nc_, int prec)
+    : ctx(c)
+    , coarse(cg)
+    , fine(fg)
+    , nc(nc_)
+    , precision(prec)
+  {
+    const int p = cg.p;
+    for (int d = 0; d < 3; ++d)
+      {
+        const int C = cg.C[d], nf = fg.Nn[d], ncn = cg.Nn[d];
+        // prolongation rows: fine node f -> (p+1) coarse entries
+        std::vector<int>    pc(size_t(nf) * (p + 1));
+        std::vector<double> pv(size_t(nf) * (p + 1));
+        for (int f = 0; f < nf; ++f)
+          {
+            const int    fc = std::min(f / p, 2 * C - 1);
+            const int    lf = f - fc * p;
+            const int    cc = fc / 2;
+            const double xi = 0.5 * (fc % 2) + 0.5 * b.nodes[lf];
+            for (int i = 0; i <= p; ++i)
+              {
+                pc[size_t(f) * (p + 1) + i] = cc * p + i;
+                pv[size_t(f) * (p + 1) + i] = lagr_nodes(b.nodes, p + 1, i, xi);
+              }
+          }
+        // restriction = transpose in gather form: coarse row -> fine entries
+        std::vector<std::vector<std::pair<int, double>>> rt(ncn);
+        for (int f = 0; f < nf; ++f)
+          for (int i = 0; i <= p; ++i)
+            {
+              const double v = pv[size_t(f) * (p + 1) + i];
+              if (v != 0.0)
+                rt[pc[size_t(f) * (p + 1) + i]].push_back({f, v});
+            }
+        int wr = 1;
+        for (auto &r : rt)
+          wr = std::max(wr, int(r.size()));
+        std::vector<int>    rc(size_t(ncn) * wr, -1);
+        std::vector<double> rv(size_t(ncn) * wr, 0.0);
+        for (int r = 0; r < ncn; ++r)
+          for (size_t t = 0; t < rt[r].size(); ++t)
+            {
+              rc[size_t(r) * wr + t] = rt[r][t].first;
+              rv[size_t(r) * wr + t] = rt[r][t].second;
+            }
+        // interpolation: coarse node -> fine field at that point
+        std::vector<int>    ic(size_t(ncn) * (p + 1));
+        std::vector<double> iv(size_t(ncn) * (p + 1));
+        for (int i = 0; i < ncn; ++i)
+          {
+            const int    cc    = std::min(i / p, C - 1);
+            const int    li    = i - cc * p;
+            const double xi    = b.nodes[li];
+            const int    child = xi < 0.5 ? 0 : 1;
+            const double xl    = child == 0 ? 2 * xi : 2 * xi - 1;
+            const int    fc    = 2 * cc + child;
+            for (int j = 0; j <= p; ++j)
+              {
+                ic[size_t(i) * (p + 1) + j] = fc * p + j;
+                iv[size_t(i) * (p + 1) + j] = lagr_nodes(b.nodes, p + 1, j, xl);
+              }
+          }
+        auto upload = [&](Band &B, const std::vector<int> &col, const std::vector<double> &val,
+                          int rows, int width) {
+          B.rows  = rows;
+          B.width = width;
+          B.col.alloc(col.size() * sizeof(int));
+          MF_CK(cudaMemcpy(B.col.ptr, col.data(), col.size() * sizeof(int), cudaMemcpyHostToDevice));
+          if (precision == 32)
+            {
+              std::vector<float> vf(val.begin(), val.end());
+              B.val.alloc(vf.size() * sizeof(float));
+              MF_CK(cudaMemcpy(B.val.ptr, vf.data(), vf.size() * sizeof(float), cudaMemcpyHostToDevice));
+            }
+          else
+            {
+              B.val.alloc(val.size() * sizeof(double));
+              MF_CK(cudaMemcpy(B.val.ptr, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
+            }
+        };
+        upload(P[d], pc, pv, nf, p + 1);
+        upload(R[d], rc, rv, ncn, wr);
+        upload(I[d], ic, iv, ncn, p + 1);
+      }
+    const size_t es = precision == 32 ? 4 : 8;
+    tmp0.alloc(fg.n_nodes * nc * es);
+    tmp1.alloc(fg.n_nodes * nc * es);
+  }
+
+  // apply the three 1D passes x, y, z: from grid `from` to grid `to`
+  void
+  Transfer::passes(const Band *B, const LevelGeom &from, const LevelGeom &to,
+                   const void *in, void *out)
+  {
+    int         ext[3] = {from.Nn[0], from.Nn[1], from.Nn[2]};
+    const void *cur    = in;
+    void       *bufs[2] = {tmp1.ptr, out};
+    for (int d = 0; d < 3; ++d)
+      {
+        PassDims pd;
+        for (int e = 0; e < 3; ++e)
+          {
+            pd.ext_in[e]  = ext[e];
+            pd.ext_out[e] = ext[e];
+          }
+        pd.ext_out[d] = to.Nn[d];
+        pd.nc         = nc;
+        pd.dir        = d;
+        pd.width      = B[d].width;
+        // pass 0 -> tmp1, pass 1 -> tmp0 (in == tmp0 for pass 0 is safe:
+        // tmp0 is only read there), pass 2 -> out
+        void *dst = d == 2 ? out : (d == 0 ? tmp1.ptr : tmp0.ptr);
+        (void)bufs;
+        const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
+        if (precision == 32)
+          k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, B[d].col.as<int>(), B[d].val.as<float>(), (const float *)cur, (float *)dst);
+        else
+          k_transfer_pass<double><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, B[d].col.as<int>(), B[d].val.as<double>(), (const double *)cur, (double *)dst);
+        count_launch();
+        MF_CK(cudaGetLastError());
+        cur    = dst;
+        ext[d] = to.Nn[d];
+      }
+  }
+
+  void
+  Transfer::prolongate(void *fine_v, const void *coarse_v)
+  {
+    const size_t es = precision == 32 ? 4 : 8;
+    MF_CK(cudaMemcpyAsync(tmp0.ptr, coarse_v, coarse.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (precision == 32)
+      constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp0.as<float>());
+    else
+      constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp0.as<double>());
+    passes(P, coarse, fine, tmp0.ptr, fine_v);
+    if (precision == 32)
+      constrained_op<float>(*ctx, fine, nc, 2, nullptr, (float *)fine_v);
+    else
+      constrained_op<double>(*ctx, fine, nc, 2, nullptr, (double *)fine_v);
+  }
+
+  void
+  Transfer::prolongate_add(void *fine_v, const void *coarse_v)
+  {
+    // result of the passes into tmp0 (last pass writes `out`)
+    const size_t es = precision == 32 ? 4 : 8;
+    DevBuf       &out = tmp0;
+    MF_CK(cudaMemcpyAsync(tmp1.ptr, coarse_v, coarse.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (precision == 32)
+      constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp1.as<float>());
+    else
+      constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp1.as<double>());
+    // passes() uses tmp1 and tmp0 as intermediates: run x into a third area
+    // by going through the fine vector itself is not allowed (we add), so
+    // use a dedicated order: x pass tmp1 -> tmp0, y pass tmp0 -> tmp1,
+    // z pass tmp1 -> tmp0
+    int         ext[3] = {coarse.Nn[0], coarse.Nn[1], coarse.Nn[2]};
+    const void *cur    = tmp1.ptr;
+    void       *seq[3] = {tmp0.ptr, tmp1.ptr, tmp0.ptr};
+    for (int d = 0; d < 3; ++d)
+      {
+        PassDims pd;
+        for (int e = 0; e < 3; ++e)
+          {
+            pd.ext_in[e]  = ext[e];
+            pd.ext_out[e] = ext[e];
+          }
+        pd.ext_out[d] = fine.Nn[d];
+        pd.nc         = nc;
+        pd.dir        = d;
+        pd.width      = P[d].width;
+        const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
+        if (precision == 32)
+          k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, P[d].col.as<int>(), P[d].val.as<float>(), (const float *)cur, (float *)seq[d]);
+        else
+          k_transfer_pass<double><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, P[d].col.as<int>(), P[d].val.as<double>(), (const double *)cur, (double *)seq[d]);
+        count_launch();
+        MF_CK(cudaGetLastError());
+        cur    = seq[d];
+        ext[d] = fine.Nn[d];
+      }
+    const size_t n = fine.n_nodes * nc;
+    if (precision == 32)
+      {
+        constrained_op<float>(*ctx, fine, nc, 2, nullptr, out.as<float>());
+        vec_axpby<float>(*ctx, n, 1.0f, out.as<float>(), 1.0f, (float *)fine_v);
+      }
+    else
+      {
+        constrained_op<double>(*ctx, fine, nc, 2, nullptr, out.as<double>());
+        vec_axpby<double>(*ctx, n, 1.0, out.as<double>(), 1.0, (double *)fine_v);
+      }
+  }
+
+  void
+  Transfer::restrict_add(void *coarse_v, const void *fine_v)
+  {
+    const size_t es = precision == 32 ? 4 : 8;
+    MF_CK(cudaMemcpyAsync(tmp0.ptr, fine_v, fine.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (precision == 32)
+      constrained_op<float>(*ctx, fine, nc, 2, nullptr, tmp0.as<float>());
+    else
+      constrained_op<double>(*ctx, fine, nc, 2, nullptr, tmp0.as<double>());
+    // x: tmp0 -> tmp1, y: tmp1 -> tmp0 ... the last pass must not overwrite
+    // the input of the add: write it to tmp1 region after tmp0 use
+    int         ext[3] = {fine.Nn[0], fine.Nn[1], fine.Nn[2]};
+    const void *cur    = tmp0.ptr;
+    void       *seq[3] = {tmp1.ptr, tmp0.ptr, tmp1.ptr};
+    for (int d = 0; d < 3; ++d)
+      {
+        PassDims pd;
+        for (int e = 0; e < 3; ++e)
+          {
+            pd.ext_in[e]  = ext[e];
+            pd.ext_out[e] = ext[e];
+          }
+        pd.ext_out[d] = coarse.Nn[d];
+        pd.nc         = nc;
+        pd.dir        = d;
+        pd.width      = R[d].width;
+        const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
+        if (precision == 32)
+          k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, R[d].col.as<int>(), R[d].val.as<float>(), (const float *)cur, (float *)seq[d]);
+        else
+          k_transfer_pass<double><<<grid_for(total), 256, 0, ctx->stream>>>(
+            pd, R[d].col.as<int>(), R[d].val.as<double>(), (const double *)cur, (double *)seq[d]);
+        count_launch();
+        MF_CK(cudaGetLastError());
+        cur    = seq[d];
+        ext[d] = coarse.Nn[d];
+      }
+    const size_t n = coarse.n_nodes * nc;
+    if (precision == 32)
+      {
+        constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp1.as<float>());
+        vec_axpby<float>(*ctx, n, 1.0f, tmp1.as<float>(), 1.0f, (float *)coarse_v);
+      }
+    else
+      {
+        constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp1.as<double>());
+        vec_axpby<double>(*ctx, n, 1.0, tmp1.as<double>(), 1.0, (double *)coarse_v);
+      }
+  }
+
+  void
+  Transfer::interpolate(void *coarse_v, const void *fine_v)
+  {
+    passes(I, fine, coarse, fine_v, coarse_v);
+  }
+} // namespace mfgpu

@@ -1,0 +1,343 @@
+// CG (SolverCG), Chebyshev smoother (PreconditionChebyshev) and the
+// multigrid V-cycle (Multigrid::level_v_step + PreconditionMG) on the
+// device.  The host only sequences kernel launches; vectors never leave
+// HBM.  Per CG iteration one 8-byte residual norm is read back for the
+// convergence test.
+#include <cmath>
+
+#include "mf_solvers.h"
+
+namespace mfgpu
+{
+  // ---------------------------------------------------------------------
+  // CG
+  // ---------------------------------------------------------------------
+  template <typename T>
+  CGStats
+  cg_solve(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol,
+           int maxit, bool record, bool fixed_iterations)
+  {
+    CGStats      st;
+    const size_t n = A.size();
+    DevBuf       rb(n * sizeof(T)), zb(n * sizeof(T)), pb(n * sizeof(T)), qb(n * sizeof(T));
+    T *r = rb.as<T>(), *z = zb.as<T>(), *p = pb.as<T>(), *q = qb.as<T>();
+    // r = b - A x
+    A.vmult(r, x);
+    vec_axpby<T>(c, n, T(1), b, T(-1), r);
+    vec_dot_dev<T>(c, n, r, r, S_RR);
+    read_scalars(c, S_RR + 1);
+    double res = std::sqrt(c.host_scalars[S_RR]);
+    st.res0    = res;
+    st.res     = res;
+    if (!std::isfinite(res))
+      throw Error(ERR_NONFINITE, "CG: non-finite residual");
+    if (res <= tol && !fixed_iterations)
+      {
+        st.converged = true;
+        return st;
+      }
+    if (P)
+      P->vmult(z, r);
+    else
+      vec_copy<T>(c, n, r, z);
+    vec_dot_dev<T>(c, n, r, z, S_RZ);
+    vec_copy<T>(c, n, z, p);
+    int rz = S_RZ, rzn = S_RZN;
+    for (int it = 1; it <= maxit; ++it)
+      {
+        A.vmult(q, p);
+        vec_dot_dev<T>(c, n, p, q, S_PQ);
+        cg_update<T>(c, n, rz, S_PQ, x, p, r, q, S_RR);
+        read_scalars(c, 5);
+        res    = std::sqrt(c.host_scalars[S_RR]);
+        st.its = it;
+        st.res = res;
+        if (record)
+          st.alpha.push_back(c.host_scalars[rz] / c.host_scalars[S_PQ]);
+        if (!std::isfinite(res))
+          throw Error(ERR_NONFINITE, "CG: non-finite residual");
+        if (res <= tol)
+          {
+            st.converged = true;
+            break;
+          }
+        if (P)
+          P->vmult(z, r);
+        else
+          vec_copy<T>(c, n, r, z);
+        vec_dot_dev<T>(c, n, r, z, rzn);
+        cg_direction<T>(c, n, rzn, rz, z, p);
+        if (record)
+          {
+            read_scalars(c, 5);
+            st.beta.push_back(c.host_scalars[rzn] / c.host_scalars[rz]);
+          }
+        std::swap(rz, rzn);
+      }
+    return st;
+  }
+
+  template CGStats cg_solve<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, bool, bool);
+  template CGStats cg_solve<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, bool, bool);
+
+  // ---------------------------------------------------------------------
+  // symmetric tridiagonal extreme eigenvalues (bisection, Sturm counts)
+  // ---------------------------------------------------------------------
+  static int
+  sturm(const std::vector<double> &d, const std::vector<double> &e, double x)
+  {
+    int    cnt = 0;
+    double q   = 1;
+    for (size_t i = 0; i < d.size(); ++i)
+      {
+        q = d[i] - x - (i ? e[i - 1] * e[i - 1] / q : 0.0);
+        if (q == 0)
+          q = 1e-300;
+        if (q < 0)
+          ++cnt;
+      }
+    return cnt;
+  }
+
+  static double
+  tridiag_eig(const std::vector<double> &d, const std::vector<double> &e, int k)
+  {
+    double lo = 1e300, hi = -1e300;
+    for (size_t i = 0; i < d.size(); ++i)
+      {
+        const double r = (i ? std::fabs(e[i - 1]) : 0.0) + (i + 1 < d.size() ? std::fabs(e[i]) : 0.0);
+        lo             = std::min(lo, d[i] - r);
+        hi             = std::max(hi, d[i] + r);
+      }
+    for (int it = 0; it < 200; ++it)
+      {
+        const double mid = 0.5 * (lo + hi);
+        if (sturm(d, e, mid) > k)
+          hi = mid;
+        else
+          lo = mid;
+      }
+    return 0.5 * (lo + hi);
+  }
+
+  // ---------------------------------------------------------------------
+  // Chebyshev
+  // ---------------------------------------------------------------------
+  template <typename T>
+  struct JacobiPre : Precond<T>
+  {
+    Context  *ctx;
+    Operator *A;
+    void
+    vmult(T *dst, const T *src) override
+    {
+      vec_scale<T>(*ctx, A->m(), T(1), A->inv_diag.as<T>(), src, dst);
+    }
+  };
+
+  template <typename T>
+  void
+  Chebyshev<T>::estimate()
+  {
+    const size_t n = A->m();
+    xold.alloc(n * sizeof(T));
+    t1.alloc(n * sizeof(T));
+    w0.alloc(n * sizeof(T));
+    w1.alloc(n * sizeof(T));
+    // initial guess with high-frequency content and the constant mode:
+    // entries 1 except every 11th, mean removed
+    std::vector<T> h(n);
+    double         mean = 0;
+    for (size_t i = 0; i < n; ++i)
+      {
+        h[i] = (i % 11 == 0) ? T(0) : T(1);
+        mean += double(h[i]);
+      }
+    mean /= double(n);
+    for (size_t i = 0; i < n; ++i)
+      h[i] -= T(mean);
+    MF_CK(cudaMemcpyAsync(w0.ptr, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    MF_CK(cudaMemsetAsync(w1.ptr, 0, n * sizeof(T), ctx->stream));
+    OpRef<T>     Aop(A);
+    JacobiPre<T> P;
+    P.ctx     = ctx;
+    P.A       = A;
+    CGStats st = cg_solve<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, true, false);
+    const size_t k = st.alpha.size();
+    if (k == 0)
+      lambda_min = lambda_max = 1.0;
+    else
+      {
+        std::vector<double> d(k), e(k > 0 ? k - 1 : 0);
+        for (size_t i = 0; i < k; ++i)
+          d[i] = 1. / st.alpha[i] + (i > 0 ? st.beta[i - 1] / st.alpha[i - 1] : 0.);
+        for (size_t i = 0; i + 1 < k; ++i)
+          e[i] = std::sqrt(st.beta[i]) / st.alpha[i];
+        lambda_min = tridiag_eig(d, e, 0);
+        lambda_max = 1.2 * tridiag_eig(d, e, int(k) - 1);
+      }
+    const double alpha = smoothing_range > 1. ? lambda_max / smoothing_range :
+                                                std::min(0.9 * lambda_max, lambda_min);
+    if (degree == 0)
+      {
+        const double actual_range = lambda_max / alpha;
+        const double sigma        = (1. - std::sqrt(1. / actual_range)) / (1. + std::sqrt(1. / actual_range));
+        const double eps          = smoothing_range;
+        degree = 1 + unsigned(std::log(1. / eps + std::sqrt(1. / eps / eps - 1.)) / std::log(1. / sigma));
+      }
+    delta       = (lambda_max - alpha) * 0.5;
+    theta       = (lambda_max + alpha) * 0.5;
+    initialized = true;
+  }
+
+  template <typename T>
+  void
+  Chebyshev<T>::vmult(T *x, const T *b)
+  {
+    if (!initialized)
+      estimate();
+    const size_t n    = A->m();
+    const T     *dinv = A->inv_diag.as<T>();
+    cheby_start<T>(*ctx, n, T(1. / theta), b, dinv, x, xold.as<T>());
+    if (degree < 2)
+      return;
+    double rhok = delta / theta, sigma = theta / delta;
+    for (unsigned k = 0; k + 1 < degree; ++k)
+      {
+        A->vmult(t1.ptr, x);
+        const double rhokp = 1. / (2. * sigma - rhok);
+        const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
+        rhok = rhokp;
+        cheby_update<T>(*ctx, n, T(f1), T(f2), k == 0, b, t1.as<T>(), dinv, x, xold.as<T>());
+      }
+  }
+
+  template <typename T>
+  void
+  Chebyshev<T>::step(T *x, const T *b)
+  {
+    if (!initialized)
+      estimate();
+    const size_t n    = A->m();
+    const T     *dinv = A->inv_diag.as<T>();
+    A->vmult(t1.ptr, x);
+    cheby_update<T>(*ctx, n, T(0), T(1. / theta), true, b, t1.as<T>(), dinv, x, xold.as<T>());
+    if (degree < 2)
+      return;
+    double rhok = delta / theta, sigma = theta / delta;
+    for (unsigned k = 0; k + 1 < degree; ++k)
+      {
+        A->vmult(t1.ptr, x);
+        const double rhokp = 1. / (2. * sigma - rhok);
+        const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
+        rhok = rhokp;
+        cheby_update<T>(*ctx, n, T(f1), T(f2), false, b, t1.as<T>(), dinv, x, xold.as<T>());
+      }
+  }
+
+  template struct Chebyshev<float>;
+  template struct Chebyshev<double>;
+
+  // ---------------------------------------------------------------------
+  // Multigrid
+  // ---------------------------------------------------------------------
+  template <typename T>
+  void
+  Multigrid<T>::setup(double range, unsigned degree, int eig_its, int coarse_eig_its)
+  {
+    const int L = int(ops.size());
+    smoothers.clear();
+    smoothers.resize(L);
+    sol.resize(L);
+    def.resize(L);
+    tmp.resize(L);
+    for (int l = 0; l < L; ++l)
+      {
+        Chebyshev<T> &s = smoothers[l];
+        s.ctx           = ctx;
+        s.A             = ops[l];
+        if (l == 0)
+          {
+            s.smoothing_range   = 1e-3;
+            s.degree            = 0;
+            s.eig_cg_iterations = coarse_eig_its;
+          }
+        else
+          {
+            s.smoothing_range   = range;
+            s.degree            = degree;
+            s.eig_cg_iterations = eig_its;
+          }
+        s.initialized = false;
+        const size_t bytes = ops[l]->m() * sizeof(T);
+        if (sol[l].bytes != bytes)
+          {
+            sol[l].alloc(bytes);
+            def[l].alloc(bytes);
+            tmp[l].alloc(bytes);
+          }
+      }
+    if (coarse64)
+      {
+        coarse_cheb64                   = Chebyshev<double>();
+        coarse_cheb64.ctx               = ctx;
+        coarse_cheb64.A                 = coarse64;
+        coarse_cheb64.smoothing_range   = 1e-3;
+        coarse_cheb64.degree            = 0;
+        coarse_cheb64.eig_cg_iterations = coarse_eig_its;
+        c64_sol.alloc(coarse64->m() * sizeof(double));
+        c64_def.alloc(coarse64->m() * sizeof(double));
+      }
+  }
+
+  template <typename T>
+  void
+  Multigrid<T>::level_v_step(int l)
+  {
+    const size_t n = ops[l]->m();
+    if (l == 0)
+      {
+        if (coarse64)
+          {
+            vec_convert<double, T>(*ctx, n, def[0].template as<T>(), c64_def.as<double>());
+            coarse_cheb64.vmult(c64_sol.as<double>(), c64_def.as<double>());
+            vec_convert<T, double>(*ctx, n, c64_sol.as<double>(), sol[0].template as<T>());
+          }
+        else
+          smoothers[0].vmult(sol[0].template as<T>(), def[0].template as<T>());
+        return;
+      }
+    T *s = sol[l].template as<T>(), *d = def[l].template as<T>(), *t = tmp[l].template as<T>();
+    smoothers[l].vmult(s, d);
+    ops[l]->vmult(t, s);
+    vec_axpby<T>(*ctx, n, T(1), d, T(-1), t); // t = d - A s
+    MF_CK(cudaMemsetAsync(def[l - 1].ptr, 0, def[l - 1].bytes, ctx->stream));
+    transfers[l]->restrict_add(def[l - 1].ptr, t);
+    MF_CK(cudaMemsetAsync(sol[l - 1].ptr, 0, sol[l - 1].bytes, ctx->stream));
+    level_v_step(l - 1);
+    transfers[l]->prolongate_add(s, sol[l - 1].ptr);
+    smoothers[l].step(s, d);
+  }
+
+  template <typename T>
+  void
+  Multigrid<T>::vmult(double *dst, const double *src)
+  {
+    const int    L = int(ops.size()) - 1;
+    const size_t n = ops[L]->m();
+    if constexpr (std::is_same<T, double>::value)
+      vec_copy<double>(*ctx, n, src, def[L].template as<double>());
+    else
+      vec_convert<T, double>(*ctx, n, src, def[L].template as<T>());
+    MF_CK(cudaMemsetAsync(sol[L].ptr, 0, sol[L].bytes, ctx->stream));
+    level_v_step(L);
+    if constexpr (std::is_same<T, double>::value)
+      vec_copy<double>(*ctx, n, sol[L].template as<double>(), dst);
+    else
+      vec_convert<double, T>(*ctx, n, sol[L].template as<T>(), dst);
+    ++vcycles;
+  }
+
+  template struct Multigrid<float>;
+  template struct Multigrid<double>;
+} // namespace mfgpu

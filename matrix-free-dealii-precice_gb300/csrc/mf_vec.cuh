@@ -1,0 +1,434 @@
+// Vector kernels: BLAS-1 updates, deterministic reductions, constrained-row
+// handling on the box faces, multigrid transfer passes and the boundary
+// traction term.  All are memory-bound streaming kernels: grid-stride loops,
+// grid size a multiple of the SM count.
+#pragma once
+
+#include "mf_common.cuh"
+
+namespace mfgpu
+{
+  constexpr int RED_BLOCKS  = 608; // 4 x 152 SMs
+  constexpr int RED_THREADS = 256;
+
+  template <typename T>
+  __global__ void
+  k_fill(size_t n, T v, T *__restrict__ x)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      x[i] = v;
+  }
+
+  // y = a*x + b*y
+  template <typename T>
+  __global__ void
+  k_axpby(size_t n, T a, const T *__restrict__ x, T b, T *__restrict__ y)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      y[i] = a * x[i] + b * y[i];
+  }
+
+  // z = a*x + b*y
+  template <typename T>
+  __global__ void
+  k_axpbyz(size_t n, T a, const T *__restrict__ x, T b, const T *__restrict__ y,
+           T *__restrict__ z)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      z[i] = a * x[i] + b * y[i];
+  }
+
+  template <typename TD, typename TS>
+  __global__ void
+  k_convert(size_t n, const TS *__restrict__ s, TD *__restrict__ d)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      d[i] = TD(s[i]);
+  }
+
+  // y = d .* x
+  template <typename T>
+  __global__ void
+  k_scale(size_t n, T omega, const T *__restrict__ d, const T *__restrict__ x,
+          T *__restrict__ y)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      y[i] = omega * d[i] * x[i];
+  }
+
+  template <typename T>
+  __global__ void
+  k_invert(size_t n, T *__restrict__ x, int *__restrict__ err)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        const T v = x[i];
+        if (!(v > T(0)))
+          atomicOr(err, 2);
+        x[i] = T(1) / v;
+      }
+  }
+
+  static __device__ __forceinline__ double
+  block_sum(double v)
+  {
+    __shared__ double ws[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+      ws[wid] = v;
+    __syncthreads();
+    v = 0;
+    if (wid == 0)
+      {
+        const int nw = (blockDim.x + 31) >> 5;
+        v            = lane < nw ? ws[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          v += __shfl_down_sync(0xffffffffu, v, o);
+      }
+    return v;
+  }
+
+  // partial[block] = sum x.y over the block's grid-stride share
+  template <typename T>
+  __global__ void __launch_bounds__(RED_THREADS)
+  k_dot_partial(size_t n, const T *__restrict__ x, const T *__restrict__ y,
+                double *__restrict__ partial)
+  {
+    double s = 0;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      s += double(x[i]) * double(y[i]);
+    s = block_sum(s);
+    if (threadIdx.x == 0)
+      partial[blockIdx.x] = s;
+  }
+
+  // out[slot] = sum of nparts partials (fixed order: deterministic)
+  static __global__ void __launch_bounds__(RED_THREADS)
+  k_reduce_final(int nparts, const double *__restrict__ partial,
+                 double *__restrict__ out)
+  {
+    double s = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+      s += partial[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0)
+      *out = s;
+  }
+
+  // CG update: x += alpha p ; r -= alpha q ; partial |r|^2
+  // alpha = num/den read from device scalars
+  template <typename T>
+  __global__ void __launch_bounds__(RED_THREADS)
+  k_cg_update(size_t n, const double *__restrict__ num,
+              const double *__restrict__ den, T *__restrict__ x,
+              const T *__restrict__ p, T *__restrict__ r,
+              const T *__restrict__ q, double *__restrict__ partial)
+  {
+    const T alpha = T(*num / *den);
+    double  s     = 0;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        x[i] += alpha * p[i];
+        const T rr = r[i] - alpha * q[i];
+        r[i]       = rr;
+        s += double(rr) * double(rr);
+      }
+    s = block_sum(s);
+    if (threadIdx.x == 0)
+      partial[blockIdx.x] = s;
+  }
+
+  // p = z + beta p,  beta = num/den
+  template <typename T>
+  __global__ void
+  k_cg_direction(size_t n, const double *__restrict__ num,
+                 const double *__restrict__ den, const T *__restrict__ z,
+                 T *__restrict__ p)
+  {
+    const T beta = T(*num / *den);
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      p[i] = z[i] + beta * p[i];
+  }
+
+  // Chebyshev step (PreconditionChebyshev vector updates):
+  //   t  = Dinv (b - Ax)
+  //   xn = first ? (1+f1) x + f2 t : x + f1 (x - xold) + f2 t ; xold = x ; x = xn
+  template <typename T>
+  __global__ void
+  k_cheby_update(size_t n, T f1, T f2, int first, const T *__restrict__ b,
+                 const T *__restrict__ Ax, const T *__restrict__ dinv,
+                 T *__restrict__ x, T *__restrict__ xold)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        const T t  = dinv[i] * (b[i] - Ax[i]);
+        const T xi = x[i];
+        const T xn = first ? (T(1) + f1) * xi + f2 * t : xi + f1 * (xi - xold[i]) + f2 * t;
+        xold[i]    = xi;
+        x[i]       = xn;
+      }
+  }
+
+  // x = f * dinv .* b ; xold = 0   (first Chebyshev iterate from zero)
+  template <typename T>
+  __global__ void
+  k_cheby_start(size_t n, T f, const T *__restrict__ b, const T *__restrict__ dinv,
+                T *__restrict__ x, T *__restrict__ xold)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        x[i]    = f * dinv[i] * b[i];
+        xold[i] = T(0);
+      }
+  }
+
+  // ---------------------------------------------------------------------
+  // Constrained rows (homogeneous Dirichlet on box faces).  Each (node,
+  // component) on a constrained face is visited exactly once: by the lowest
+  // numbered face that constrains that component at that node.
+  // op: 0 dst = src, 1 dst += src, 2 dst = 0, 3 dst = 1
+  // ---------------------------------------------------------------------
+  struct FaceInfo
+  {
+    int      Nn[3];
+    size_t   n_nodes;
+    unsigned face_mask[6];
+    int      nc;
+  };
+
+  template <typename T>
+  __global__ void
+  k_constrained(const FaceInfo fi, int op, const T *__restrict__ src,
+                T *__restrict__ dst)
+  {
+    const int f = blockIdx.y;
+    if (!fi.face_mask[f])
+      return;
+    const int nd = f / 2, side = f % 2;
+    const int d1 = nd == 0 ? 1 : 0, d2 = nd == 2 ? 1 : 2;
+    const int n1 = fi.Nn[d1], n2 = fi.Nn[d2];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n1 * n2;
+         t += gridDim.x * blockDim.x)
+      {
+        int ii[3];
+        ii[nd] = side ? fi.Nn[nd] - 1 : 0;
+        ii[d1] = t % n1;
+        ii[d2] = t / n1;
+        const size_t node = size_t(ii[0]) + size_t(fi.Nn[0]) * (size_t(ii[1]) + size_t(fi.Nn[1]) * ii[2]);
+        for (int c = 0; c < fi.nc; ++c)
+          {
+            if (!((fi.face_mask[f] >> c) & 1u))
+              continue;
+            // owner: lowest face constraining component c at this node
+            bool owner = true;
+            for (int f2 = 0; f2 < f; ++f2)
+              {
+                const int nd2 = f2 / 2, s2 = f2 % 2;
+                if (((fi.face_mask[f2] >> c) & 1u) && ii[nd2] == (s2 ? fi.Nn[nd2] - 1 : 0))
+                  owner = false;
+              }
+            if (!owner)
+              continue;
+            const size_t i = size_t(c) * fi.n_nodes + node;
+            if (op == 0)
+              dst[i] = src[i];
+            else if (op == 1)
+              dst[i] += src[i];
+            else if (op == 2)
+              dst[i] = T(0);
+            else
+              dst[i] = T(1);
+          }
+      }
+  }
+
+  // ---------------------------------------------------------------------
+  // One tensor-direction pass of a banded 1D operator (transfer):
+  //   out[.., r, ..] = sum_t val[r][t] * in[.., col[r][t], ..]
+  // along direction dir; the component index is the outermost dimension.
+  // ---------------------------------------------------------------------
+  struct PassDims
+  {
+    int ext_in[3];
+    int ext_out[3];
+    int nc;
+    int dir;
+    int width; // entries per row
+  };
+
+  template <typename T>
+  __global__ void
+  k_transfer_pass(const PassDims pd, const int *__restrict__ col,
+                  const T *__restrict__ val, const T *__restrict__ in,
+                  T *__restrict__ out)
+  {
+    const size_t per_c = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2];
+    const size_t total = per_c * pd.nc;
+    const size_t in_c  = size_t(pd.ext_in[0]) * pd.ext_in[1] * pd.ext_in[2];
+    size_t       stride_in = 1;
+    for (int d = 0; d < pd.dir; ++d)
+      stride_in *= pd.ext_in[d];
+    for (size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x; o < total;
+         o += size_t(gridDim.x) * blockDim.x)
+      {
+        const size_t c  = o / per_c;
+        size_t       rm = o - c * per_c;
+        int          idx[3];
+        idx[0] = int(rm % pd.ext_out[0]);
+        rm /= pd.ext_out[0];
+        idx[1] = int(rm % pd.ext_out[1]);
+        idx[2] = int(rm / pd.ext_out[1]);
+        const int r = idx[pd.dir];
+        idx[pd.dir] = 0;
+        const size_t base = c * in_c + size_t(idx[0]) +
+                            size_t(pd.ext_in[0]) * (size_t(idx[1]) + size_t(pd.ext_in[1]) * idx[2]);
+        T s = T(0);
+        for (int t = 0; t < pd.width; ++t)
+          {
+            const int cc = col[r * pd.width + t];
+            if (cc >= 0)
+              s += val[r * pd.width + t] * in[base + size_t(cc) * stride_in];
+          }
+        out[o] = s;
+      }
+  }
+
+  // ---------------------------------------------------------------------
+  // Boundary traction (mf_elasticity.h:1849-1897): for each cell face on
+  // the traction boundary, t0 = t |det F F^{-T} N| at the face Gauss points,
+  // integrated against the face shape functions.  One block per face,
+  // one thread per face quadrature point / face node.
+  // ---------------------------------------------------------------------
+  struct TractionArgs
+  {
+    int      C[3], Nn[3], p, N;
+    size_t   n_nodes;
+    double   h[3];
+    int      face; // box face 0..5
+    double   t[3];
+    double   S[MAX_N * MAX_N];   // [q][i]
+    double   G[MAX_N * MAX_N];   // [q][i] derivative at Gauss points
+    double   Ge[2][MAX_N];       // derivative at 0 and 1
+    double   w[MAX_N];
+  };
+
+  static __global__ void
+  k_traction(const __grid_constant__ TractionArgs A, const double *__restrict__ u,
+             double *__restrict__ rhs)
+  {
+    __shared__ double tq[3][MAX_N * MAX_N];
+    const int nd = A.face / 2, side = A.face % 2;
+    const int d1 = nd == 0 ? 1 : 0, d2 = nd == 2 ? 1 : 2;
+    const int N  = A.N;
+    // face cell (c1, c2) in the tangential directions
+    const int c1 = blockIdx.x % A.C[d1], c2 = blockIdx.x / A.C[d1];
+    int       cc[3];
+    cc[nd] = side ? A.C[nd] - 1 : 0;
+    cc[d1] = c1;
+    cc[d2] = c2;
+    const int ln = side ? N - 1 : 0; // local index of the face in nd
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x)
+      {
+        const int q1 = t % N, q2 = t / N;
+        double    F[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int k = 0; k < N; ++k)
+          for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i)
+              {
+                int li[3] = {i, j, k};
+                // basis factors per direction: value and derivative
+                double vv[3], dd[3];
+                for (int d = 0; d < 3; ++d)
+                  {
+                    if (d == nd)
+                      {
+                        vv[d] = li[d] == ln ? 1.0 : 0.0;
+                        dd[d] = A.Ge[side][li[d]];
+                      }
+                    else
+                      {
+                        const int q = d == d1 ? q1 : q2;
+                        vv[d]       = A.S[q * N + li[d]];
+                        dd[d]       = A.G[q * N + li[d]];
+                      }
+                  }
+                const double g0 = dd[0] * vv[1] * vv[2] / A.h[0];
+                const double g1 = vv[0] * dd[1] * vv[2] / A.h[1];
+                const double g2 = vv[0] * vv[1] * dd[2] / A.h[2];
+                const size_t node = size_t(cc[0] * A.p + i) +
+                                    size_t(A.Nn[0]) * (size_t(cc[1] * A.p + j) + size_t(A.Nn[1]) * (cc[2] * A.p + k));
+                for (int c = 0; c < 3; ++c)
+                  {
+                    const double uv = u[size_t(c) * A.n_nodes + node];
+                    F[c][0] += g0 * uv;
+                    F[c][1] += g1 * uv;
+                    F[c][2] += g2 * uv;
+                  }
+              }
+        for (int d = 0; d < 3; ++d)
+          F[d][d] += 1.0;
+        const double J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) -
+                         F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
+                         F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
+        // n* = J F^{-T} N = cofactor(F) N ; cofactor row nd
+        double cof[3][3];
+        cof[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+        cof[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+        cof[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+        cof[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+        cof[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+        cof[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+        cof[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+        cof[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+        cof[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+        (void)J;
+        const double sgn = side ? 1.0 : -1.0;
+        double       ns  = 0;
+        for (int i = 0; i < 3; ++i)
+          {
+            const double v = cof[i][nd] * sgn; // (J F^{-T})_{i nd} = cof(F)_{i nd}
+            ns += v * v;
+          }
+        ns              = sqrt(ns);
+        const double jw = A.w[q1] * A.h[d1] * A.w[q2] * A.h[d2];
+        for (int c = 0; c < 3; ++c)
+          tq[c][t] = A.t[c] * ns * jw;
+      }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x)
+      {
+        const int i1 = t % N, i2 = t / N;
+        int       li[3];
+        li[nd] = ln;
+        li[d1] = i1;
+        li[d2] = i2;
+        double r[3] = {0, 0, 0};
+        for (int q2 = 0; q2 < N; ++q2)
+          for (int q1 = 0; q1 < N; ++q1)
+            {
+              const double phi = A.S[q1 * N + i1] * A.S[q2 * N + i2];
+              for (int c = 0; c < 3; ++c)
+                r[c] += phi * tq[c][q1 + q2 * N];
+            }
+        const size_t node = size_t(cc[0] * A.p + li[0]) +
+                            size_t(A.Nn[0]) * (size_t(cc[1] * A.p + li[1]) + size_t(A.Nn[1]) * (cc[2] * A.p + li[2]));
+        for (int c = 0; c < 3; ++c)
+          atomicAdd(rhs + size_t(c) * A.n_nodes + node, r[c]);
+      }
+  }
+} // namespace mfgpu

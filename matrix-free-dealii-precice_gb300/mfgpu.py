@@ -1,0 +1,396 @@
+"""Python host binding of libmfgpu.so (ctypes over the C-ABI of include/mfgpu.h).
+
+Mirrors the reference's operator interface for the matrix-free path:
+``NeoHookOperator`` (include/solid_mechanics/mf_nh_operator.h:103-173) and
+``LaplaceOperator`` (include/heat_transfer/heat_transfer.h:81-127) with
+``vmult / vmult_add / Tvmult / compute_diagonal / get_matrix_diagonal_inverse
+/ el / m / precondition_Jacobi / memory_consumption``, the multigrid
+transfer, and the solid / heat drivers.  Vectors are CUDA tensors (torch is
+used only for device memory); every call goes through the C-ABI and raises
+``MfgpuError`` when the library returns a non-zero status.  There is no CPU
+fallback: without the built library or a GPU the calls fail.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmfgpu.so")
+
+OK = 0
+STATUS = {1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_OOM", 4: "ERR_NONFINITE",
+          5: "ERR_NOT_CONVERGED", 6: "ERR_STATE", 7: "ERR_DET_F",
+          8: "ERR_UNSUPPORTED", 9: "ERR_TIMEOUT"}
+
+
+class MfgpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Mesh(C.Structure):
+    _fields_ = [("degree", C.c_int), ("n_q_1d", C.c_int),
+                ("n_refinements", C.c_int), ("repetitions", C.c_int * 3),
+                ("lower", C.c_double * 3), ("upper", C.c_double * 3),
+                ("boundary_id", C.c_int * 6), ("n_dirichlet", C.c_int),
+                ("dirichlet_id", C.c_int * 8),
+                ("dirichlet_mask", C.c_uint * 8)]
+
+
+class Material(C.Structure):
+    _fields_ = [("mu", C.c_double), ("nu", C.c_double), ("rho", C.c_double),
+                ("alpha_1", C.c_double), ("formulation", C.c_int)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("preconditioner", C.c_int), ("relaxation", C.c_double),
+                ("tol", C.c_double), ("max_it_mult", C.c_int),
+                ("cheb_degree", C.c_int), ("cheb_range", C.c_double),
+                ("cheb_eig_its", C.c_int), ("coarse_accurate", C.c_int),
+                ("mg_precision", C.c_int), ("coarse_fp64", C.c_int)]
+
+
+class SolidParams(C.Structure):
+    _fields_ = [("mesh", Mesh), ("material", Material),
+                ("caching", C.c_char_p), ("solver", SolverParams),
+                ("max_newton", C.c_int), ("tol_f", C.c_double),
+                ("tol_f_abs", C.c_double), ("tol_u", C.c_double),
+                ("tol_u_abs", C.c_double), ("dt", C.c_double),
+                ("n_steps", C.c_int), ("body_force", C.c_double * 3),
+                ("traction_id", C.c_int), ("traction", C.c_double * 3),
+                ("watch", C.c_double * 3)]
+
+
+class SolidResult(C.Structure):
+    _fields_ = [("newton_its", C.c_int * 64),
+                ("watch_disp", (C.c_double * 3) * 64),
+                ("total_cg", C.c_long), ("n_solves", C.c_int),
+                ("n_steps", C.c_int), ("seconds", C.c_double)]
+
+
+class HeatParams(C.Structure):
+    _fields_ = [("mesh", Mesh), ("dt", C.c_double), ("n_steps", C.c_int),
+                ("solver", SolverParams), ("analytic", C.c_int),
+                ("alpha", C.c_double), ("beta", C.c_double),
+                ("n_gauss", C.c_int), ("g_center", (C.c_double * 3) * 8),
+                ("g_width", C.c_double * 8), ("g_amp", C.c_double * 8)]
+
+
+class HeatResult(C.Structure):
+    _fields_ = [("cg_its", C.c_int * 64), ("n_steps", C.c_int),
+                ("seconds", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libmfgpu.so (built by build.py); fails loudly when missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MfgpuError(-1, f"{LIB_PATH} not built (run build.py)")
+        _lib = C.CDLL(LIB_PATH)
+        _lib.mfgpu_last_error.restype = C.c_char_p
+        _lib.mfgpu_launch_count.restype = C.c_longlong
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        raise MfgpuError(rc, lib().mfgpu_last_error().decode())
+
+
+def launch_count():
+    return int(lib().mfgpu_launch_count())
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return C.c_void_p(t)
+    return C.c_void_p(t.data_ptr())
+
+
+def make_mesh(degree, n_refinements, repetitions, lower, upper,
+              boundary_id=(0, 0, 0, 0, 0, 0), dirichlet=(), n_q_1d=None):
+    """Box mesh; dirichlet: iterable of (boundary_id, component_mask)."""
+    m = Mesh()
+    m.degree = degree
+    m.n_q_1d = degree + 1 if n_q_1d is None else n_q_1d
+    m.n_refinements = n_refinements
+    for d in range(3):
+        m.repetitions[d] = repetitions[d]
+        m.lower[d] = lower[d]
+        m.upper[d] = upper[d]
+    for f in range(6):
+        m.boundary_id[f] = boundary_id[f]
+    m.n_dirichlet = len(dirichlet)
+    for i, (bid, mask) in enumerate(dirichlet):
+        m.dirichlet_id[i] = bid
+        m.dirichlet_mask[i] = mask
+    return m
+
+
+def n_nodes(mesh, level=-1):
+    n = C.c_size_t()
+    _check(lib().mfgpu_mesh_n_nodes(C.byref(mesh), level, C.byref(n)))
+    return n.value
+
+
+def material(mu=0.5e6, nu=0.4, rho=1000.0, dt=0.01, formulation=1, beta=0.25):
+    m = Material()
+    m.mu, m.nu, m.rho = mu, nu, rho
+    m.alpha_1 = 1.0 / (beta * dt * dt)
+    m.formulation = formulation
+    return m
+
+
+class Context:
+    """One CUDA device + stream (mfgpu_context)."""
+
+    def __init__(self, device=0):
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_context_create(device, C.byref(self.h)))
+
+    def synchronize(self):
+        _check(lib().mfgpu_context_synchronize(self.h))
+
+    def copy(self, dst, src, nbytes):
+        """Copy nbytes between device/host pointers or tensors."""
+        _check(lib().mfgpu_copy(self.h, _ptr(dst), _ptr(src), C.c_size_t(nbytes)))
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().mfgpu_context_stream(self.h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if self.h:
+            lib().mfgpu_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Operator:
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+
+    def m(self):
+        v = C.c_size_t()
+        _check(lib().mfgpu_operator_m(self.h, C.byref(v)))
+        return v.value
+
+    n = m
+
+    def vmult(self, dst, src):
+        _check(lib().mfgpu_operator_vmult(self.h, _ptr(dst), _ptr(src)))
+
+    def vmult_add(self, dst, src):
+        _check(lib().mfgpu_operator_vmult_add(self.h, _ptr(dst), _ptr(src)))
+
+    def Tvmult(self, dst, src):
+        _check(lib().mfgpu_operator_Tvmult(self.h, _ptr(dst), _ptr(src)))
+
+    def Tvmult_add(self, dst, src):
+        _check(lib().mfgpu_operator_Tvmult_add(self.h, _ptr(dst), _ptr(src)))
+
+    def vmult_host(self, dst_np, src_np):
+        """dst = A src with host numpy buffers (copies inside the call)."""
+        _check(lib().mfgpu_operator_vmult_host(
+            self.h, dst_np.ctypes.data_as(C.c_void_p),
+            src_np.ctypes.data_as(C.c_void_p)))
+
+    def compute_diagonal(self):
+        _check(lib().mfgpu_operator_compute_diagonal(self.h))
+
+    def get_matrix_diagonal_inverse(self):
+        p = C.c_void_p()
+        _check(lib().mfgpu_operator_get_matrix_diagonal_inverse(self.h, C.byref(p)))
+        return p.value
+
+    def el(self, row, col):
+        v = C.c_double()
+        _check(lib().mfgpu_operator_el(self.h, C.c_size_t(row), C.c_size_t(col),
+                                       C.byref(v)))
+        return v.value
+
+    def precondition_Jacobi(self, dst, src, omega):
+        _check(lib().mfgpu_operator_precondition_jacobi(
+            self.h, _ptr(dst), _ptr(src), C.c_double(omega)))
+
+    def memory_consumption(self):
+        v = C.c_size_t()
+        _check(lib().mfgpu_operator_memory_consumption(self.h, C.byref(v)))
+        return v.value
+
+    def clear(self):
+        _check(lib().mfgpu_operator_clear(self.h))
+
+    def close(self):
+        if self.h:
+            lib().mfgpu_operator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LaplaceOperator(_Operator):
+    """Heat operator M + dt k K on one level (heat_transfer.h:81-250)."""
+
+    def __init__(self, ctx, mesh, level=-1, precision=64, constrained=True,
+                 delta_t=None, coefficient=1.0):
+        super().__init__(ctx)
+        _check(lib().mfgpu_heat_operator_create(ctx.h, C.byref(mesh), level,
+                                                precision, int(constrained),
+                                                C.byref(self.h)))
+        if delta_t is not None:
+            self.set_delta_t(delta_t)
+        self.evaluate_coefficient(coefficient)
+
+    def set_delta_t(self, dt):
+        _check(lib().mfgpu_heat_operator_set_delta_t(self.h, C.c_double(dt)))
+
+    def evaluate_coefficient(self, k=1.0):
+        _check(lib().mfgpu_heat_operator_evaluate_coefficient(self.h, C.c_double(k)))
+
+
+class NeoHookOperator(_Operator):
+    """Linearised neo-Hookean tangent on one level (mf_nh_operator.h)."""
+
+    def __init__(self, ctx, mesh, level=-1, precision=64,
+                 caching="scalar_referential"):
+        super().__init__(ctx)
+        _check(lib().mfgpu_nh_operator_create(ctx.h, C.byref(mesh), level,
+                                              precision, caching.encode(),
+                                              C.byref(self.h)))
+        self._u = None
+
+    def set_material(self, mat, inclusion=None):
+        _check(lib().mfgpu_nh_operator_set_material(
+            self.h, C.byref(mat), C.byref(inclusion) if inclusion else None))
+
+    def initialize(self, displacement):
+        self._u = displacement  # keep the linearisation alive
+        _check(lib().mfgpu_nh_operator_initialize(self.h, _ptr(displacement)))
+
+    def cache(self):
+        _check(lib().mfgpu_nh_operator_cache(self.h))
+
+
+def _transfer(fn, ctx, mesh, coarse_level, nc, precision, a, b):
+    _check(getattr(lib(), fn)(ctx.h, C.byref(mesh), coarse_level, nc, precision,
+                              _ptr(a), _ptr(b)))
+
+
+def prolongate(ctx, mesh, coarse_level, nc, coarse, fine, precision=64):
+    _transfer("mfgpu_transfer_prolongate", ctx, mesh, coarse_level, nc, precision,
+              coarse, fine)
+
+
+def restrict_add(ctx, mesh, coarse_level, nc, coarse, fine, precision=64):
+    _transfer("mfgpu_transfer_restrict_add", ctx, mesh, coarse_level, nc, precision,
+              coarse, fine)
+
+
+def interpolate(ctx, mesh, coarse_level, nc, coarse, fine, precision=64):
+    _transfer("mfgpu_transfer_interpolate", ctx, mesh, coarse_level, nc, precision,
+              coarse, fine)
+
+
+def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
+                  cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
+                  coarse_accurate=True, mg_precision=32, coarse_fp64=False,
+                  max_it_mult=1):
+    s = SolverParams()
+    s.preconditioner = {"none": 0, "jacobi": 1, "gmg": 2}[preconditioner]
+    s.relaxation = relaxation
+    s.tol = tol
+    s.max_it_mult = max_it_mult
+    s.cheb_degree = cheb_degree
+    s.cheb_range = cheb_range
+    s.cheb_eig_its = cheb_eig_its
+    s.coarse_accurate = int(coarse_accurate)
+    s.mg_precision = mg_precision
+    s.coarse_fp64 = int(coarse_fp64)
+    return s
+
+
+class Solid:
+    """Newton-Newmark driver (mf_elasticity.h:555-628) on the device."""
+
+    def __init__(self, ctx, params):
+        self.ctx = ctx
+        self.params = params
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_solid_create(ctx.h, C.byref(params), C.byref(self.h)))
+
+    def run(self):
+        r = SolidResult()
+        _check(lib().mfgpu_solid_run(self.h, C.byref(r)))
+        return r
+
+    def displacement_ptr(self):
+        p = C.c_void_p()
+        _check(lib().mfgpu_solid_displacement(self.h, C.byref(p)))
+        return p.value
+
+    def linear_solve(self, u, rhs, du):
+        its = C.c_int()
+        secs = C.c_double()
+        _check(lib().mfgpu_solid_linear_solve(self.h, _ptr(u), _ptr(rhs), _ptr(du),
+                                              C.byref(its), C.byref(secs)))
+        return its.value, secs.value
+
+    def close(self):
+        if self.h:
+            lib().mfgpu_solid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Heat:
+    """Backward-Euler heat driver (heat_transfer.h:972-1037) on the device."""
+
+    def __init__(self, ctx, params):
+        self.ctx = ctx
+        self.params = params
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_heat_create(ctx.h, C.byref(params), C.byref(self.h)))
+
+    def run(self):
+        r = HeatResult()
+        _check(lib().mfgpu_heat_run(self.h, C.byref(r)))
+        return r
+
+    def solution_ptr(self):
+        p = C.c_void_p()
+        _check(lib().mfgpu_heat_solution(self.h, C.byref(p)))
+        return p.value
+
+    def close(self):
+        if self.h:
+            lib().mfgpu_heat_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

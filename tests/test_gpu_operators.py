@@ -1,0 +1,280 @@
+"""Device operators through the C-ABI against the CPU oracle.
+
+Tolerances: FP64 operator applications agree with the oracle within 1e-12
+relative l2 (the spec bar); FP32 within 2e-5 relative l2; FP64
+diagonals within 1e-11 (the device uses the tensor-product diagonal, the
+oracle applies the cell operator to local unit vectors).
+"""
+import numpy as np
+import pytest
+
+import mfgpu
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def small_heat(degree):
+    return W.unit_cube_heat(degree, 1, rep=(2, 1, 1))
+
+
+def small_cantilever(degree):
+    return W.cantilever(degree, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_heat_vmult(ctx, degree, precision):
+    spec = small_heat(degree)
+    dt = np.float64 if precision == 64 else np.float32
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 1)
+    src = W.uniform_vector(n, 1, dt)
+    ref = O.heat_vmult(om, 1, 0.1, src, precision=precision)
+    op = mfgpu.LaplaceOperator(ctx, m, -1, precision, True, delta_t=0.1)
+    d_src, d_dst = dev(src), dev(np.zeros_like(src))
+    op.vmult(d_dst, d_src)
+    assert rel(host(d_dst), ref) < (TOL64 if precision == 64 else TOL32)
+    # vmult_add adds; Tvmult == vmult (symmetric)
+    op.vmult_add(d_dst, d_src)
+    assert rel(host(d_dst), 2 * ref) < (TOL64 if precision == 64 else TOL32)
+    op.Tvmult(d_dst, d_src)
+    assert rel(host(d_dst), ref) < (TOL64 if precision == 64 else TOL32)
+
+
+@pytest.mark.parametrize("degree", [1, 2, 4])
+def test_heat_unconstrained_and_diagonal(ctx, degree):
+    spec = small_heat(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 1)
+    src = W.uniform_vector(n, 3)
+    ref = O.heat_vmult(om, 1, 0.1, src, constrained=False)
+    op = mfgpu.LaplaceOperator(ctx, m, -1, 64, False, delta_t=0.1)
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    assert rel(host(d_dst), ref) < TOL64
+    opc = mfgpu.LaplaceOperator(ctx, m, -1, 64, True, delta_t=0.1)
+    opc.compute_diagonal()
+    ptr = opc.get_matrix_diagonal_inverse()
+    d_inv = dev(np.zeros(n))
+    # copy through the Jacobi preconditioner: dst = 1.0 * Dinv * ones
+    opc.precondition_Jacobi(d_inv, dev(np.ones(n)), 1.0)
+    ref_inv = O.heat_inv_diagonal(om, 1, 0.1)
+    assert rel(host(d_inv), ref_inv) < 1e-11
+    assert ptr
+    # el(i,i) is the diagonal entry
+    i = n // 2
+    assert abs(opc.el(i, i) - 1.0 / ref_inv[i]) < 1e-10 * abs(1.0 / ref_inv[i])
+
+
+CACHINGS = ["scalar_referential", "tensor2", "tensor4", "tensor4_ns",
+            "referential_qp"]
+
+
+def nh_setup(degree, seed=2):
+    spec = small_cantilever(degree)
+    u = W.smooth_displacement(degree, spec["n_ref"], spec["rep"], spec["lo"],
+                              spec["hi"], seed=seed)
+    return spec, u
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("caching", CACHINGS)
+def test_nh_vmult_fp64(ctx, degree, caching):
+    spec, u = nh_setup(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 3)
+    mat_o = O.material(0.5e6, 0.4, 1000.0, 0.01)
+    mat_l = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+    src = W.uniform_vector(n, 3)
+    oracle_caching = "scalar_referential" if caching == "referential_qp" else caching
+    ref = O.nh_vmult(om, 1, mat_o, oracle_caching, u, src)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, 64, caching)
+    op.set_material(mat_l)
+    d_u = dev(u)
+    op.initialize(d_u)
+    op.cache()
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    assert rel(host(d_dst), ref) < TOL64, caching
+
+
+@pytest.mark.parametrize("degree", [1, 3, 5])
+def test_nh_vmult_fp32(ctx, degree):
+    spec, u = nh_setup(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 3)
+    src = W.uniform_vector(n, 3)
+    ref = O.nh_vmult(om, 1, O.material(dt=0.01), "scalar_referential", u, src)
+    for caching in ("scalar_referential", "referential_qp"):
+        op = mfgpu.NeoHookOperator(ctx, m, -1, 32, caching)
+        op.set_material(mfgpu.material(dt=0.01))
+        d_u = dev(u.astype(np.float32))
+        op.initialize(d_u)
+        op.cache()
+        d_dst = dev(np.zeros(n, np.float32))
+        op.vmult(d_dst, dev(src.astype(np.float32)))
+        assert rel(host(d_dst).astype(np.float64), ref) < 5e-5, caching
+
+
+@pytest.mark.parametrize("degree", [1, 2, 4])
+def test_nh_formulation0(ctx, degree):
+    spec, u = nh_setup(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 3)
+    src = W.uniform_vector(n, 5)
+    ref = O.nh_vmult(om, 1, O.material(dt=0.01, formulation=0), "tensor2", u, src)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, 64, "tensor2")
+    op.set_material(mfgpu.material(dt=0.01, formulation=0))
+    d_u = dev(u)
+    op.initialize(d_u)
+    op.cache()
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    assert rel(host(d_dst), ref) < TOL64
+    # the diagonal of formulation 0 (column-wise tangent blocks)
+    op.compute_diagonal()
+    d_inv = dev(np.zeros(n))
+    op.precondition_Jacobi(d_inv, dev(np.ones(n)), 1.0)
+    ref_inv = O.nh_inv_diagonal(om, 1, O.material(dt=0.01, formulation=0), "tensor2", u)
+    assert rel(host(d_inv), ref_inv) < 1e-11
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_nh_diagonal(ctx, degree, precision):
+    spec, u = nh_setup(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 3)
+    npdt = np.float64 if precision == 64 else np.float32
+    ref_inv = O.nh_inv_diagonal(om, 1, O.material(dt=0.01), "scalar_referential", u)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, precision, "scalar_referential")
+    op.set_material(mfgpu.material(dt=0.01))
+    d_u = dev(u.astype(npdt))
+    op.initialize(d_u)
+    op.cache()
+    op.compute_diagonal()
+    d_inv = dev(np.zeros(n, npdt))
+    op.precondition_Jacobi(d_inv, dev(np.ones(n, npdt)), 1.0)
+    tol = 1e-11 if precision == 64 else 5e-5
+    assert rel(host(d_inv).astype(np.float64), ref_inv) < tol
+
+
+def test_nh_det_f_error_status(ctx):
+    """A linearisation with det F <= 0 is reported as MFGPU_ERR_DET_F (the
+    kernel sets an error word; no device fault)."""
+    spec, u = nh_setup(2)
+    m = W.to_lib_mesh(mfgpu, spec)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, 64, "scalar_referential")
+    op.set_material(mfgpu.material(dt=0.01))
+    X, Y, Z = W.node_coords(2, spec["n_ref"], spec["rep"], spec["lo"], spec["hi"])
+    bad = np.concatenate([-2.0 * X, np.zeros_like(Y), np.zeros_like(Z)])  # F_xx = -1
+    d_u = dev(bad)
+    op.initialize(d_u)
+    with pytest.raises(mfgpu.MfgpuError) as e:
+        op.cache()
+    assert e.value.code == 7
+    # the context stays usable
+    op.initialize(dev(u))
+    op.cache()
+
+
+def test_state_errors(ctx):
+    spec, _ = nh_setup(1)
+    m = W.to_lib_mesh(mfgpu, spec)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, 64, "tensor2")
+    n = op.m()
+    with pytest.raises(mfgpu.MfgpuError) as e:
+        op.vmult(dev(np.zeros(n)), dev(np.zeros(n)))
+    assert e.value.code == 6
+    with pytest.raises(mfgpu.MfgpuError):
+        mfgpu.NeoHookOperator(ctx, m, -1, 64, "no_such_caching")
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 5])
+def test_vmult_host_buffers(ctx, degree):
+    spec, u = nh_setup(degree)
+    m = W.to_lib_mesh(mfgpu, spec)
+    n = W.n_dofs(spec, 3)
+    op = mfgpu.NeoHookOperator(ctx, m, -1, 64, "referential_qp")
+    op.set_material(mfgpu.material(dt=0.01))
+    d_u = dev(u)
+    op.initialize(d_u)
+    op.cache()
+    src = W.uniform_vector(n, 9)
+    out = np.zeros(n)
+    op.vmult_host(out, src)
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    # same operator, same inputs; the scatter's atomic adds may differ in
+    # the order of summation, so compare to round-off
+    assert rel(out, host(d_dst)) < 1e-14
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("nc", [1, 3])
+def test_transfer(ctx, degree, nc):
+    spec = W.cantilever(degree, 2, rep=(2, 1, 1), length=(2.0, 1.0, 1.0)) if nc == 3 \
+        else W.unit_cube_heat(degree, 2, rep=(2, 1, 1))
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    nco = mfgpu.n_nodes(m, 0) * nc
+    nf = mfgpu.n_nodes(m, 1) * nc
+    coarse = W.uniform_vector(nco, 11)
+    fine = W.uniform_vector(nf, 12)
+    # prolongate
+    ref_f = np.zeros(nf)
+    O.transfer(om, 0, nc, "prolongate", coarse.copy(), ref_f)
+    d_f = dev(np.zeros(nf))
+    mfgpu.prolongate(ctx, m, 0, nc, dev(coarse), d_f)
+    assert rel(host(d_f), ref_f) < 1e-13
+    # restrict (adds into coarse)
+    ref_c = coarse.copy()
+    O.transfer(om, 0, nc, "restrict", ref_c, fine.copy())
+    d_c = dev(coarse)
+    mfgpu.restrict_add(ctx, m, 0, nc, d_c, dev(fine))
+    assert rel(host(d_c), ref_c) < 1e-13
+    # interpolate
+    ref_i = np.zeros(nco)
+    O.transfer(om, 0, nc, "interpolate", ref_i, fine.copy())
+    d_i = dev(np.zeros(nco))
+    mfgpu.interpolate(ctx, m, 0, nc, d_i, dev(fine))
+    assert rel(host(d_i), ref_i) < 1e-13
+
+
+def test_prolongation_reproduces_polynomials(ctx):
+    """P interpolates: a polynomial of degree p is transferred exactly."""
+    spec = W.unit_cube_heat(3, 2, rep=(2, 1, 1))
+    spec["dirichlet"] = []
+    m = W.to_lib_mesh(mfgpu, spec)
+    f = lambda X, Y, Z: 1 + X ** 3 - 2 * X * Y ** 2 + Z ** 3 * Y ** 2
+    Xc, Yc, Zc = W.node_coords(3, 0, spec["rep"], spec["lo"], spec["hi"])
+    Xf, Yf, Zf = W.node_coords(3, 1, spec["rep"], spec["lo"], spec["hi"])
+    d_f = dev(np.zeros(len(Xf)))
+    mfgpu.prolongate(ctx, m, 0, 1, dev(f(Xc, Yc, Zc)), d_f)
+    assert np.max(np.abs(host(d_f) - f(Xf, Yf, Zf))) < 1e-12

@@ -1,0 +1,144 @@
+"""Device solvers (GMG-preconditioned CG, Newton-Newmark, backward Euler)
+through the C-ABI against the CPU oracle: Newton iteration counts equal,
+watchpoint displacement within 1e-8 relative, average CG counts within +-1,
+heat solutions within the solver tolerance."""
+import numpy as np
+import pytest
+
+import mfgpu
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def solid_pair(spec, caching="scalar_referential", precond="gmg", formulation=1,
+               dt=0.01, n_steps=2, traction=(0.0, -100.0, 0.0), mg_precision=32,
+               watch=None):
+    watch = watch or (spec["hi"][0], 0.5 * spec["hi"][1], 0.5 * spec["hi"][2])
+    # oracle
+    po = O.SolidParams()
+    po.mesh = W.to_oracle_mesh(O, spec)
+    po.mat = O.material(0.5e6, 0.4, 1000.0, dt, formulation)
+    po.caching = O.CACHING["scalar_referential" if caching == "referential_qp" else caching]
+    po.precond = {"none": 0, "jacobi": 1, "gmg": 2}[precond]
+    po.relaxation, po.tol_lin, po.max_it_mult, po.max_newton = 0.65, 1e-6, 1, 10
+    po.tol_f, po.tol_f_abs, po.tol_u, po.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+    po.dt, po.n_steps = dt, n_steps
+    po.body_force[:] = [0.0, 0.0, 0.0]
+    po.traction_id = W.TRACTION_ID
+    po.traction[:] = list(traction)
+    po.watch[:] = list(watch)
+    po.cheb_degree, po.cheb_range, po.cheb_eig_its, po.coarse_accurate = 5, 20.0, 30, 1
+    po.mg_float = 1 if mg_precision == 32 else 0
+    # library
+    pl = mfgpu.SolidParams()
+    pl.mesh = W.to_lib_mesh(mfgpu, spec)
+    pl.material = mfgpu.material(0.5e6, 0.4, 1000.0, dt, formulation)
+    pl.caching = caching.encode()
+    pl.solver = mfgpu.solver_params(precond, tol=1e-6, mg_precision=mg_precision)
+    pl.max_newton = 10
+    pl.tol_f, pl.tol_f_abs, pl.tol_u, pl.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+    pl.dt, pl.n_steps = dt, n_steps
+    pl.body_force[:] = [0.0, 0.0, 0.0]
+    pl.traction_id = W.TRACTION_ID
+    pl.traction[:] = list(traction)
+    pl.watch[:] = list(watch)
+    return po, pl
+
+
+@pytest.mark.parametrize("degree,caching,precond,form", [
+    (1, "scalar_referential", "gmg", 1),
+    (2, "scalar_referential", "gmg", 1),
+    (2, "tensor4", "gmg", 1),
+    (2, "referential_qp", "gmg", 1),
+    (3, "tensor2", "jacobi", 1),
+    (2, "tensor2", "gmg", 0),
+])
+def test_solid_newton_newmark(ctx, degree, caching, precond, form):
+    spec = W.cantilever(degree, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    po, pl = solid_pair(spec, caching, precond, form)
+    ro = O.solid_run(po)
+    s = mfgpu.Solid(ctx, pl)
+    rl = s.run()
+    n = po.n_steps
+    assert list(rl.newton_its[:n]) == list(ro.newton_its[:n])
+    for st in range(n):
+        wo = np.array(ro.watch_disp[st][:3])
+        wl = np.array(rl.watch_disp[st][:3])
+        assert np.linalg.norm(wl - wo) <= 1e-8 * np.linalg.norm(wo), (st, wl, wo)
+    avg_o = ro.total_cg / ro.n_solves
+    avg_l = rl.total_cg / rl.n_solves
+    assert abs(avg_l - avg_o) <= 1.0 + 0.01 * avg_o, (avg_l, avg_o)
+
+
+def test_solid_all_fp64_vcycle(ctx):
+    spec = W.cantilever(2, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    po, pl = solid_pair(spec, mg_precision=64)
+    ro = O.solid_run(po)
+    rl = mfgpu.Solid(ctx, pl).run()
+    assert list(rl.newton_its[:2]) == list(ro.newton_its[:2])
+    wo = np.array(ro.watch_disp[1][:3])
+    wl = np.array(rl.watch_disp[1][:3])
+    assert np.linalg.norm(wl - wo) <= 1e-8 * np.linalg.norm(wo)
+
+
+def heat_pair(spec, analytic=False, n_steps=1, tol=1e-10, mg_precision=32):
+    po = O.HeatParams()
+    po.mesh = W.to_oracle_mesh(O, spec)
+    po.dt, po.n_steps, po.tol_rel, po.precond = 0.1, n_steps, tol, 2
+    po.analytic, po.alpha, po.beta = int(analytic), 3.0, 1.3
+    po.mg_float = 1 if mg_precision == 32 else 0
+    pl = mfgpu.HeatParams()
+    pl.mesh = W.to_lib_mesh(mfgpu, spec)
+    pl.dt, pl.n_steps = 0.1, n_steps
+    pl.solver = mfgpu.solver_params("gmg", tol=tol, cheb_range=15.0, cheb_eig_its=10,
+                                    mg_precision=mg_precision)
+    pl.analytic, pl.alpha, pl.beta = int(analytic), 3.0, 1.3
+    if not analytic:
+        c, w, a = W.gaussian_source(0)
+        po.n_gauss = pl.n_gauss = 8
+        for i in range(8):
+            for d in range(3):
+                po.g_center[i][d] = pl.g_center[i][d] = c[i, d]
+            po.g_width[i] = pl.g_width[i] = w[i]
+            po.g_amp[i] = pl.g_amp[i] = a[i]
+    return po, pl
+
+
+def test_heat_analytic_solution(ctx):
+    """u = 1 + x^2 + 3 y^2 + 1.3 t is reproduced to round-off (the
+    reference's partitioned-heat golden, here on a single 3D domain with
+    Dirichlet data on all faces)."""
+    import torch
+    spec = W.unit_cube_heat(2, 2)
+    spec["boundary_id"] = (1, 1, 1, 1, 1, 1)
+    po, pl = heat_pair(spec, analytic=True, n_steps=5, tol=1e-12)
+    h = mfgpu.Heat(ctx, pl)
+    r = h.run()
+    n = W.n_dofs(spec, 1)
+    u = torch.empty(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.copy(u, h.solution_ptr(), n * 8)
+    X, Y, Z = W.node_coords(2, 2, spec["rep"], spec["lo"], spec["hi"])
+    exact = 1 + X ** 2 + 3 * Y ** 2 + 1.3 * 0.5
+    assert np.max(np.abs(u.cpu().numpy() - exact)) < 1e-11
+    ro = O.heat_run(po)
+    assert all(abs(a - b) <= 1 for a, b in zip(r.cg_its[:5], ro.cg_its[:5]))
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3])
+def test_heat_gaussian_step(ctx, degree):
+    import torch
+    spec = W.unit_cube_heat(degree, 2)
+    po, pl = heat_pair(spec, analytic=False, n_steps=1, tol=1e-10)
+    ro, uo = O.heat_run(po, return_u=True)
+    h = mfgpu.Heat(ctx, pl)
+    r = h.run()
+    n = W.n_dofs(spec, 1)
+    u = torch.empty(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.copy(u, h.solution_ptr(), n * 8)
+    ul = u.cpu().numpy()
+    assert np.linalg.norm(ul - uo) / np.linalg.norm(uo) < 1e-8
+    assert abs(r.cg_its[0] - ro.cg_its[0]) <= 1
