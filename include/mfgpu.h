@@ -182,6 +182,27 @@ int mfgpu_transfer_interpolate(mfgpu_context *ctx, const mfgpu_mesh *mesh,
                                int coarse_level, int n_components,
                                int precision, void *coarse, const void *fine);
 
+/* fine = P coarse without allocating any device memory: the same
+ * prolongation as mfgpu_transfer_prolongate, for callers that may not
+ * allocate device memory while they run.  Examples: a coupled solver whose
+ * partner code's pool already holds the GPU memory, a time loop that must
+ * not stall on cudaMalloc/cudaFree, a deployment that forbids allocation
+ * after start-up.  No counterpart in the reference (deal.II's transfer
+ * allocates its own vectors).  The two intermediate arrays live in a
+ * static 4 MiB device array that every GPU loading the library keeps until
+ * exit, so each intermediate (fine-x by coarse-y,z, then fine-x,y by
+ * coarse-z, times n_components) may hold at most 262,144 doubles or 524,288
+ * floats; larger levels return MFGPU_ERR_ARG.  Needs no context: it runs
+ * on `stream` (a cudaStream_t, NULL for the default stream) of the current
+ * device and returns without synchronising.  The first call on a device
+ * looks up the array's device address, so make it before any stream
+ * capture.  Every call shares the array and nothing in it has to start at
+ * zero; calls that overlap on the GPU race on it, so serialise them. */
+int mfgpu_transfer_prolongate_noalloc(const mfgpu_mesh *mesh, int coarse_level,
+                                      int n_components, int precision,
+                                      const void *coarse, void *fine,
+                                      void *stream);
+
 /* ---------------------------------------------------------------- */
 /* drivers                                                           */
 /* ---------------------------------------------------------------- */

@@ -34,6 +34,12 @@ struct mfgpu_heat
 
 static thread_local std::string g_last_error;
 
+void
+mfgpu::set_last_error(const char *msg)
+{
+  g_last_error = msg ? msg : "";
+}
+
 template <typename F>
 static int
 guarded(F &&f)

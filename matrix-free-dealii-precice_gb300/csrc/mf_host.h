@@ -25,6 +25,9 @@ namespace mfgpu
   void check_cuda(cudaError_t e, const char *what);
 #define MF_CK(x) ::mfgpu::check_cuda((x), #x)
 
+  // message returned by mfgpu_last_error() on the calling thread
+  void set_last_error(const char *msg);
+
   void count_launch(int n = 1);
   long long launch_count();
 

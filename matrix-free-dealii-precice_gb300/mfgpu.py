@@ -309,6 +309,15 @@ def interpolate(ctx, mesh, coarse_level, nc, coarse, fine, precision=64):
               coarse, fine)
 
 
+def prolongate_noalloc(mesh, coarse_level, nc, coarse, fine, precision=64,
+                       stream=None):
+    """fine = P coarse with no device allocation (static 4 MiB scratch);
+    asynchronous on `stream` (None: the default stream)."""
+    _check(lib().mfgpu_transfer_prolongate_noalloc(
+        C.byref(mesh), coarse_level, nc, precision, _ptr(coarse), _ptr(fine),
+        C.c_void_p(stream) if stream else None))
+
+
 def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
                   cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
                   coarse_accurate=True, mg_precision=32, coarse_fp64=False,
