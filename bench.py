@@ -42,6 +42,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--caching", default="referential_qp")
+    p.add_argument("--arith", default="native", choices=["native", "df64"],
+                   help="FP64 operator arithmetic: native FP64 or double-float on the FP32 pipe")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -237,6 +239,8 @@ def main():
     op = mfgpu.NeoHookOperator(ctx, mesh, -1, 64, args.caching)
     op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01))
     op.initialize(u)
+    if args.arith == "df64":
+        op.set_fp64_emulation(True)
     op.cache()
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 512 MB > L2
@@ -323,6 +327,8 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "nh_tangent_vmult_q4_cantilever_64x8x8", "n_dofs": n,
                    "n_cells": n_cells, "degree": 4, "n_q_1d": 5, "caching": args.caching,
+                   "arithmetic": "native FP64" if args.arith == "native" else
+                                 "double-float (FP32 pipe), parity 1e-12 vs FP64",
                    "l2": "flushed (512 MB write) before every timed application",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * n / e2e_s, "unit": UNIT,

@@ -137,6 +137,14 @@ int mfgpu_nh_operator_initialize(mfgpu_operator *op, const void *displacement);
  * det F <= 0 at a quadrature point */
 int mfgpu_nh_operator_cache(mfgpu_operator *op);
 
+/* Arithmetic of an FP64 operator: 0 native FP64 (default), 1 double-float
+ * (each FP64 value carried as an unevaluated sum of two floats on the FP32
+ * pipe, ~48 significant bits; the result agrees with native FP64 to ~1e-14
+ * relative).  Supported for heat operators and the referential_qp tangent
+ * (formulation 1); the neo-Hookean operator must be cache()d again after a
+ * change.  No counterpart in the reference (its path is native FP64). */
+int mfgpu_operator_set_fp64_emulation(mfgpu_operator *op, int enable);
+
 /* vmult / vmult_add / Tvmult / Tvmult_add (mf_nh_operator.h:545-625 and
  * MatrixFreeOperators::Base::vmult): dst = A src with constrained rows
  * dst = src */

@@ -279,6 +279,27 @@ extern "C"
   }
 
   int
+  mfgpu_operator_set_fp64_emulation(mfgpu_operator *op, int enable)
+  {
+    return guarded([&] {
+      need(op, "op");
+      Operator *o = op->op.get();
+      if (enable && o->precision != 64)
+        throw Error(ERR_UNSUPPORTED, "double-float arithmetic applies to FP64 operators");
+      if (enable)
+        {
+          auto *nh = dynamic_cast<NHOperator *>(o);
+          if (nh && (nh->variant != V_QP10 || nh->formulation != 1))
+            throw Error(ERR_UNSUPPORTED,
+                        "double-float arithmetic supports heat and referential_qp (formulation 1)");
+          if (nh)
+            nh->cached = false;
+        }
+      o->arith = enable ? 1 : 0;
+    });
+  }
+
+  int
   mfgpu_operator_vmult(mfgpu_operator *op, void *dst, const void *src)
   {
     return guarded([&] {

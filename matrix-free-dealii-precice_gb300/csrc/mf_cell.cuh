@@ -18,6 +18,7 @@
 #pragma once
 
 #include "mf_common.cuh"
+#include "mf_df64.cuh"
 
 namespace mfgpu
 {
@@ -74,6 +75,82 @@ namespace mfgpu
           s = fma_(M[r * N + k], in[r], s);
         out[k] = s;
       }
+  }
+
+  // df64 overloads of the 1D line operations: compensated dot products
+  template <int N>
+  __device__ __forceinline__ void
+  mat_apply(const df64 *__restrict__ M, const df64 (&in)[N], df64 (&out)[N])
+  {
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      {
+        DfAcc acc;
+        acc.init(M[r * N], in[0]);
+#pragma unroll
+        for (int k = 1; k < N; ++k)
+          acc.add(M[r * N + k], in[k]);
+        out[r] = acc.result();
+      }
+  }
+
+  template <int N>
+  __device__ __forceinline__ void
+  mat_apply_t(const df64 *__restrict__ M, const df64 (&in)[N], df64 (&out)[N])
+  {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      {
+        DfAcc acc;
+        acc.init(M[k], in[0]);
+#pragma unroll
+        for (int r = 1; r < N; ++r)
+          acc.add(M[r * N + k], in[r]);
+        out[k] = acc.result();
+      }
+  }
+
+  template <int N>
+  __device__ __forceinline__ void
+  mat_apply_t_add(const df64 *__restrict__ M, const df64 (&in)[N], df64 (&out)[N])
+  {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      {
+        DfAcc acc;
+        acc.init_add(out[k]);
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+          acc.add(M[r * N + k], in[r]);
+        out[k] = acc.result();
+      }
+  }
+
+  template <typename T>
+  __device__ __forceinline__ T
+  zero()
+  {
+    return T(0);
+  }
+  template <>
+  __device__ __forceinline__ df64
+  zero<df64>()
+  {
+    return df64{0.f, 0.f};
+  }
+
+  template <typename T>
+  __device__ __forceinline__ T
+  ldg_(const T *p)
+  {
+    return __ldg(p);
+  }
+  template <>
+  __device__ __forceinline__ df64
+  ldg_<df64>(const df64 *p)
+  {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return df64{v.x, v.y};
   }
 
   template <int N>
@@ -194,7 +271,7 @@ namespace mfgpu
         else
 #pragma unroll
           for (int i = 0; i < N; ++i)
-            y[i] = T(0);
+            y[i] = zero<T>();
         mat_apply_t_add<N>(sh.D, x, y);
         store_line<N, T, 2>(V, a, b, y);
         __syncthreads();
@@ -251,15 +328,15 @@ namespace mfgpu
   // v and H arrive as the values and REAL gradients at quadrature point q and
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
-  template <int N, typename T, int NC, class QOp, bool CONSTRAINED>
-  __global__ void __launch_bounds__(cells_per_block<N, NC, T>() * N * N)
+  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED>
+  __global__ void __launch_bounds__(cells_per_block<N, NC, TS>() * N * N)
   cell_apply_kernel(const __grid_constant__ Shape<N, T> sh,
                     const __grid_constant__ CellGeom<T> g, const QOp op,
-                    const T *__restrict__ src, T *__restrict__ dst)
+                    const TS *__restrict__ src, TS *__restrict__ dst)
   {
     constexpr int N2  = N * N;
     constexpr int N3  = N * N * N;
-    constexpr int CPB = cells_per_block<N, NC, T>();
+    constexpr int CPB = cells_per_block<N, NC, TS>();
     constexpr int SPC = smem_per_cell<N, NC, QOp::eval_u>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
@@ -289,7 +366,7 @@ namespace mfgpu
 #pragma unroll
         for (int k = 0; k < N; ++k)
           {
-            T val = T(0);
+            T val = zero<T>();
             if (active)
               {
                 const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
@@ -299,7 +376,7 @@ namespace mfgpu
                 if (CONSTRAINED)
                   skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
                 if (!skip)
-                  val = __ldg(src + size_t(c) * g.n_nodes + node);
+                  val = to_compute<T, TS>(__ldg(src + size_t(c) * g.n_nodes + node));
               }
             col[k] = val;
           }
@@ -316,9 +393,8 @@ namespace mfgpu
             T col[N];
 #pragma unroll
             for (int k = 0; k < N; ++k)
-              col[k] = active ? op.ucell[(size_t(cc) * NC + c) * N3 + a + b * N + k * N2] : T(0);
-            // reuse the value slot of T1 as V scratch: write values to a
-            // scratch area (GU + c*3*N3 holds the 3 gradients)
+              col[k] = active ? op.ucell[(size_t(cc) * NC + c) * N3 + a + b * N + k * N2] : zero<T>();
+            // the values go to T1 (scratch); GU + c*3*N3 holds the gradients
             T *Gc = GU + c * 3 * N3;
             __syncthreads();
             evaluate_field<N>(sh, col, T1, Gc, Gc + N3, Gc + 2 * N3, T0, T1, a,
@@ -387,7 +463,7 @@ namespace mfgpu
                   continue;
                 const size_t node =
                   size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
-                atomicAdd(dst + size_t(c) * g.n_nodes + node, col[k]);
+                atomicAdd(dst + size_t(c) * g.n_nodes + node, to_storage<TS, T>(col[k]));
               }
           }
       }
@@ -417,7 +493,7 @@ namespace mfgpu
   template <typename T>
   struct NHMat
   {
-    T mu, lambda, rho_alpha, kappa, c_1;
+    T mu, lambda, rho_alpha, kappa, c_1, two_lambda;
   };
 
   // scalar_referential (mf_nh_operator.h:848-943): F from the gradient of the
@@ -534,8 +610,8 @@ namespace mfgpu
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
-          M[i][j] = __ldg(cp + (i * 3 + j) * n3);
-      const T c = __ldg(cp + 9 * n3);
+          M[i][j] = ldg_(cp + (i * 3 + j) * n3);
+      const T c = ldg_(cp + 9 * n3);
       // t = M : H
       T t = M[0][0] * H[0][0];
 #pragma unroll
@@ -556,7 +632,7 @@ namespace mfgpu
             s   = fma_(M[i][2], H[k][2], s);
             K[i][k] = s;
           }
-      const T tl = T(2) * m.lambda * t;
+      const T tl = m.two_lambda * t;
       T       P[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -575,7 +651,7 @@ namespace mfgpu
           H[i][j] = P[i][j];
 #pragma unroll
       for (int c2 = 0; c2 < 3; ++c2)
-        v[c2] *= m.rho_alpha;
+        v[c2] = v[c2] * m.rho_alpha;
     }
   };
 

@@ -17,6 +17,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "mf_df64.cuh"
+
 namespace mfgpu
 {
   constexpr int MAX_N = 7; // degree 6
@@ -59,6 +61,20 @@ namespace mfgpu
     unsigned face_mask[6];
   };
 
+  // host-side conversion of a double constant to a compute type
+  template <typename T>
+  inline T
+  conv_host(double v)
+  {
+    return T(v);
+  }
+  template <>
+  inline df64
+  conv_host<df64>(double v)
+  {
+    return df_from_double_host(v);
+  }
+
   template <typename T>
   inline CellGeom<T>
   make_cell_geom(const LevelGeom &g)
@@ -68,12 +84,12 @@ namespace mfgpu
       {
         c.C[d]     = g.C[d];
         c.Nn[d]    = g.Nn[d];
-        c.inv_h[d] = T(1.0 / g.h[d]);
+        c.inv_h[d] = conv_host<T>(1.0 / g.h[d]);
       }
     c.p       = g.p;
     c.n_cells = unsigned(g.n_cells);
     c.n_nodes = g.n_nodes;
-    c.vol     = T(g.h[0] * g.h[1] * g.h[2]);
+    c.vol     = conv_host<T>(g.h[0] * g.h[1] * g.h[2]);
     for (int f = 0; f < 6; ++f)
       c.face_mask[f] = g.face_mask[f];
     return c;

@@ -132,6 +132,7 @@ namespace mfgpu
     int       precision   = 64;
     int       nc          = 1;
     bool      constrained = true;
+    int       arith       = 0; // 0 native, 1 double-float (FP64 operators only)
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;

@@ -22,11 +22,11 @@ namespace mfgpu
       Shape<N, T> s;
       for (int i = 0; i < N * N; ++i)
         {
-          s.S[i] = T(b.S[i]);
-          s.D[i] = T(b.D[i]);
+          s.S[i] = conv_host<T>(b.S[i]);
+          s.D[i] = conv_host<T>(b.D[i]);
         }
       for (int i = 0; i < N; ++i)
-        s.w[i] = T(b.w[i]);
+        s.w[i] = conv_host<T>(b.w[i]);
       return s;
     }
 
@@ -35,11 +35,12 @@ namespace mfgpu
     to_mat(const NHMatD &m)
     {
       NHMat<T> r;
-      r.mu        = T(m.mu);
-      r.lambda    = T(m.lambda);
-      r.rho_alpha = T(m.rho_alpha);
-      r.kappa     = T(m.kappa);
-      r.c_1       = T(m.c_1);
+      r.mu         = conv_host<T>(m.mu);
+      r.lambda     = conv_host<T>(m.lambda);
+      r.rho_alpha  = conv_host<T>(m.rho_alpha);
+      r.kappa      = conv_host<T>(m.kappa);
+      r.c_1        = conv_host<T>(m.c_1);
+      r.two_lambda = conv_host<T>(2.0 * m.lambda);
       return r;
     }
 
@@ -53,14 +54,14 @@ namespace mfgpu
       return cudaSuccess;
     }
 
-    template <int N, typename T, int NC, class Op, bool CON>
+    template <int N, typename TS, typename T, int NC, class Op, bool CON>
     cudaError_t
     run_apply(const Shape<N, T> &sh, const CellGeom<T> &cg, const Op &op,
-              const T *src, T *dst, cudaStream_t s)
+              const TS *src, TS *dst, cudaStream_t s)
     {
-      constexpr int CPB  = cells_per_block<N, NC, T>();
+      constexpr int CPB  = cells_per_block<N, NC, TS>();
       const size_t  smem = size_t(CPB) * smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
-      auto          k    = cell_apply_kernel<N, T, NC, Op, CON>;
+      auto          k    = cell_apply_kernel<N, TS, T, NC, Op, CON>;
       cudaError_t   e    = prepare(k, smem);
       if (e != cudaSuccess)
         return e;
@@ -69,13 +70,13 @@ namespace mfgpu
       return cudaGetLastError();
     }
 
-    template <int N, typename T, int NC, class Op>
+    template <int N, typename TS, typename T, int NC, class Op>
     cudaError_t
     run_apply_c(bool con, const Shape<N, T> &sh, const CellGeom<T> &cg,
-                const Op &op, const T *src, T *dst, cudaStream_t s)
+                const Op &op, const TS *src, TS *dst, cudaStream_t s)
     {
-      return con ? run_apply<N, T, NC, Op, true>(sh, cg, op, src, dst, s) :
-                   run_apply<N, T, NC, Op, false>(sh, cg, op, src, dst, s);
+      return con ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, s) :
+                   run_apply<N, TS, T, NC, Op, false>(sh, cg, op, src, dst, s);
     }
   } // namespace
 
@@ -93,7 +94,7 @@ namespace mfgpu
       {
         HeatQOp<T> op;
         op.kdt = T(a.kdt);
-        return run_apply_c<N, T, 1>(a.constrained, sh, cg, op, src, dst, s);
+        return run_apply_c<N, T, T, 1>(a.constrained, sh, cg, op, src, dst, s);
       }
     const NHMat<T> m     = to_mat<T>(a.mat);
     const T       *cache = static_cast<const T *>(a.cache);
@@ -106,7 +107,7 @@ namespace mfgpu
             op.scalar = cache;
             op.m      = m;
             op.n3     = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_QP10:
           {
@@ -114,7 +115,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_TENSOR2:
           {
@@ -122,7 +123,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_TENSOR4:
           {
@@ -130,7 +131,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_TENSOR4_NS:
           {
@@ -138,7 +139,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_FORM0:
           {
@@ -146,7 +147,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
       }
     return cudaErrorInvalidValue;
@@ -313,4 +314,50 @@ namespace mfgpu
   template cudaError_t launch_diag<MF_N, float>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const void *, void *, cudaStream_t);
   template cudaError_t launch_residual<MF_N>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const double *, const double *, const double *, double *, cudaStream_t);
   template cudaError_t launch_heat_rhs<MF_N>(const HostBasis &, const LevelGeom &, double, const SourceDesc &, const double *, double *, cudaStream_t);
+  template <int N>
+  cudaError_t
+  launch_apply_df(const HostBasis &b, const LevelGeom &g, const ApplyArgs &a,
+                  cudaStream_t s)
+  {
+    const Shape<N, df64>    sh  = make_shape<N, df64>(b);
+    const CellGeom<df64>    cg  = make_cell_geom<df64>(g);
+    const double           *src = static_cast<const double *>(a.src);
+    double                 *dst = static_cast<double *>(a.dst);
+    constexpr int           N3  = N * N * N;
+    if (a.kind == 0)
+      {
+        HeatQOp<df64> op;
+        op.kdt = conv_host<df64>(a.kdt);
+        return run_apply_c<N, double, df64, 1>(a.constrained, sh, cg, op, src, dst, s);
+      }
+    if (a.var != V_QP10)
+      return cudaErrorInvalidValue;
+    NHQp10QOp<df64> op;
+    op.cache = static_cast<const df64 *>(a.cache);
+    op.m     = to_mat<df64>(a.mat);
+    op.n3    = N3;
+    return run_apply_c<N, double, df64, 3>(a.constrained, sh, cg, op, src, dst, s);
+  }
+
+  template <int N>
+  cudaError_t
+  launch_nh_cache_df(const HostBasis &b, const LevelGeom &g, const NHMatD &md,
+                     const double *u, void *cache, int *err, cudaStream_t s)
+  {
+    const Shape<N, double>  sh   = make_shape<N, double>(b);
+    const CellGeom<double>  cg   = make_cell_geom<double>(g);
+    const NHMat<double>     m    = to_mat<double>(md);
+    constexpr int           CPB  = cells_per_block<N, 3, double>();
+    const size_t            smem = size_t(CPB) * smem_per_cell<N, 3, false>() * sizeof(double);
+    const unsigned          grid = (cg.n_cells + CPB - 1) / CPB;
+    auto                    k    = nh_cache_kernel<N, double, V_QP10, df64>;
+    cudaError_t             e    = prepare(k, smem);
+    if (e != cudaSuccess)
+      return e;
+    k<<<grid, CPB * N * N, smem, s>>>(sh, cg, m, u, static_cast<df64 *>(cache), nullptr, err);
+    return cudaGetLastError();
+  }
+
+  template cudaError_t launch_apply_df<MF_N>(const HostBasis &, const LevelGeom &, const ApplyArgs &, cudaStream_t);
+  template cudaError_t launch_nh_cache_df<MF_N>(const HostBasis &, const LevelGeom &, const NHMatD &, const double *, void *, int *, cudaStream_t);
 } // namespace mfgpu

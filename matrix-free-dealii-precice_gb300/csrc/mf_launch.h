@@ -47,6 +47,16 @@ namespace mfgpu
   cudaError_t launch_apply(const HostBasis &b, const LevelGeom &g,
                            const ApplyArgs &a, cudaStream_t s);
 
+  // FP64 storage, double-float (float pair) arithmetic: heat and the
+  // referential_qp tangent
+  template <int N>
+  cudaError_t launch_apply_df(const HostBasis &b, const LevelGeom &g,
+                              const ApplyArgs &a, cudaStream_t s);
+  template <int N>
+  cudaError_t launch_nh_cache_df(const HostBasis &b, const LevelGeom &g,
+                                 const NHMatD &m, const double *u, void *cache,
+                                 int *err, cudaStream_t s);
+
   template <int N, typename T>
   cudaError_t launch_nh_cache(const HostBasis &b, const LevelGeom &g, int var,
                               const NHMatD &m, const void *u, void *cache,

@@ -452,6 +452,37 @@ namespace mfgpu
     return cudaErrorInvalidValue;
   }
 
+  static cudaError_t
+  dispatch_apply_df(int N, const HostBasis &b, const LevelGeom &g, const ApplyArgs &a, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_apply_df<2>(b, g, a, s);
+        case 3: return launch_apply_df<3>(b, g, a, s);
+        case 4: return launch_apply_df<4>(b, g, a, s);
+        case 5: return launch_apply_df<5>(b, g, a, s);
+        case 6: return launch_apply_df<6>(b, g, a, s);
+        case 7: return launch_apply_df<7>(b, g, a, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
+  static cudaError_t
+  dispatch_cache_df(int N, const HostBasis &b, const LevelGeom &g, const NHMatD &m,
+                    const double *u, void *cache, int *err, cudaStream_t s)
+  {
+    switch (N)
+      {
+        case 2: return launch_nh_cache_df<2>(b, g, m, u, cache, err, s);
+        case 3: return launch_nh_cache_df<3>(b, g, m, u, cache, err, s);
+        case 4: return launch_nh_cache_df<4>(b, g, m, u, cache, err, s);
+        case 5: return launch_nh_cache_df<5>(b, g, m, u, cache, err, s);
+        case 6: return launch_nh_cache_df<6>(b, g, m, u, cache, err, s);
+        case 7: return launch_nh_cache_df<7>(b, g, m, u, cache, err, s);
+      }
+    return cudaErrorInvalidValue;
+  }
+
   template <typename T>
   static cudaError_t
   dispatch_cache(int N, const HostBasis &b, const LevelGeom &g, int var, const NHMatD &m,
@@ -551,6 +582,7 @@ namespace mfgpu
     a.src         = src;
     a.dst         = dst;
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
     count_launch();
     MF_CK(e);
@@ -632,7 +664,11 @@ namespace mfgpu
       }
     else
       ucell.release();
-    cudaError_t e = precision == 32 ?
+    if (arith == 1 && var != V_QP10)
+      throw Error(ERR_UNSUPPORTED, "double-float arithmetic supports the referential_qp caching");
+    cudaError_t e = arith == 1 ? dispatch_cache_df(basis.N, basis, geom, mat, (const double *)u, cache.ptr,
+                                                   ctx->err.as<int>(), ctx->stream) :
+                    precision == 32 ?
                       dispatch_cache<float>(basis.N, basis, geom, var, mat, u, cache.ptr, ucell.ptr, ctx->err.as<int>(), ctx->stream) :
                       dispatch_cache<double>(basis.N, basis, geom, var, mat, u, cache.ptr, ucell.ptr, ctx->err.as<int>(), ctx->stream);
     count_launch();
@@ -661,6 +697,7 @@ namespace mfgpu
     a.src         = src;
     a.dst         = dst;
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
     count_launch();
     MF_CK(e);

@@ -48,12 +48,12 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // NH cache: per quadrature point fields of the chosen variant
   // ---------------------------------------------------------------------
-  template <int N, typename T, int VAR>
+  template <int N, typename T, int VAR, typename TO = T>
   __global__ void __launch_bounds__(cells_per_block<N, 3, T>() * N * N)
   nh_cache_kernel(const __grid_constant__ Shape<N, T> sh,
                   const __grid_constant__ CellGeom<T> g, const NHMat<T> m,
-                  const T *__restrict__ u, T *__restrict__ cache,
-                  T *__restrict__ ucell, int *__restrict__ err)
+                  const T *__restrict__ u, TO *__restrict__ cache,
+                  TO *__restrict__ ucell, int *__restrict__ err)
   {
     constexpr int N2  = N * N;
     constexpr int N3  = N * N * N;
@@ -81,7 +81,7 @@ namespace mfgpu
         if (VAR == V_SCALAR_REF && active)
 #pragma unroll
           for (int k = 0; k < N; ++k)
-            ucell[(size_t(cc) * 3 + c) * N3 + a + b * N + k * N2] = col[k];
+            ucell[(size_t(cc) * 3 + c) * N3 + a + b * N + k * N2] = to_compute<TO, T>(col[k]);
         T *V = cb + c * 4 * N3;
         evaluate_field<N>(sh, col, V, V + N3, V + 2 * N3, V + 3 * N3, T0, T1, a, b, true);
       }
@@ -106,12 +106,13 @@ namespace mfgpu
           }
         T Fi[3][3];
         inv3(F, J, Fi);
-        T       *cp     = cache + size_t(cc) * NF * N3 + q;
+        TO      *cp     = cache + size_t(cc) * NF * N3 + q;
+        auto     st     = [&](int f, T v) { cp[size_t(f) * N3] = to_compute<TO, T>(v); };
         const T  lnJ    = log(J);
         const T  scalar = m.mu - T(2.0) * m.lambda * lnJ;
         if constexpr (VAR == V_SCALAR_REF)
           {
-            cp[0] = scalar;
+            st(0, scalar);
           }
         else if constexpr (VAR == V_QP10)
           {
@@ -119,8 +120,8 @@ namespace mfgpu
             for (int i = 0; i < 3; ++i)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
-                cp[(i * 3 + j) * N3] = Fi[j][i]; // M = F^{-T}
-            cp[9 * N3] = scalar;
+                st((i * 3 + j), Fi[j][i]); // M = F^{-T}
+            st(9, scalar);
           }
         else if constexpr (VAR == V_TENSOR4_NS)
           {
@@ -129,10 +130,9 @@ namespace mfgpu
               for (int j = 0; j < 3; ++j)
                 for (int k2 = 0; k2 < 3; ++k2)
                   for (int l2 = 0; l2 < 3; ++l2)
-                    cp[(((i * 3 + j) * 3 + k2) * 3 + l2) * N3] =
-                      T(2.) * m.lambda * Fi[j][i] * Fi[l2][k2] +
+                    st((((i * 3 + j) * 3 + k2) * 3 + l2), T(2.) * m.lambda * Fi[j][i] * Fi[l2][k2] +
                       scalar * Fi[l2][i] * Fi[j][k2] +
-                      (i == k2 && j == l2 ? m.mu : T(0));
+                      (i == k2 && j == l2 ? m.mu : T(0)));
           }
         else
           {
@@ -140,16 +140,16 @@ namespace mfgpu
             for (int i = 0; i < 3; ++i)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
-                cp[(i * 3 + j) * N3] = Fi[i][j];
-            cp[9 * N3] = J;
+                st((i * 3 + j), Fi[i][j]);
+            st(9, J);
             if constexpr (VAR == V_FORM0)
               {
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                   for (int j = 0; j < 3; ++j)
-                    cp[(10 + i * 3 + j) * N3] = F[i][j];
-                cp[19 * N3] = pow(J, T(-1.0 / 3.0));
+                    st((10 + i * 3 + j), F[i][j]);
+                st(19, pow(J, T(-1.0 / 3.0)));
               }
             else
               {
@@ -163,24 +163,24 @@ namespace mfgpu
                 const T iJ = T(1.) / J;
                 if constexpr (VAR == V_TENSOR2)
                   {
-                    cp[10 * N3] = scalar * T(2.) / J;
-                    cp[11 * N3] = iJ;
-                    cp[12 * N3] = tau[0][0] / J;
-                    cp[13 * N3] = tau[1][1] / J;
-                    cp[14 * N3] = tau[2][2] / J;
-                    cp[15 * N3] = tau[0][1] / J;
-                    cp[16 * N3] = tau[0][2] / J;
-                    cp[17 * N3] = tau[1][2] / J;
+                    st(10, scalar * T(2.) / J);
+                    st(11, iJ);
+                    st(12, tau[0][0] / J);
+                    st(13, tau[1][1] / J);
+                    st(14, tau[2][2] / J);
+                    st(15, tau[0][1] / J);
+                    st(16, tau[0][2] / J);
+                    st(17, tau[1][2] / J);
                   }
                 else // V_TENSOR4
                   {
-                    cp[10 * N3] = iJ;
-                    cp[11 * N3] = tau[0][0] / J;
-                    cp[12 * N3] = tau[1][1] / J;
-                    cp[13 * N3] = tau[2][2] / J;
-                    cp[14 * N3] = tau[0][1] / J;
-                    cp[15 * N3] = tau[0][2] / J;
-                    cp[16 * N3] = tau[1][2] / J;
+                    st(10, iJ);
+                    st(11, tau[0][0] / J);
+                    st(12, tau[1][1] / J);
+                    st(13, tau[2][2] / J);
+                    st(14, tau[0][1] / J);
+                    st(15, tau[0][2] / J);
+                    st(16, tau[1][2] / J);
                     const T aa = scalar * T(2.) / J;
                     const T bl = m.lambda * T(2.) / J;
                     // C4 : sym(g) in Voigt form with off-diagonal inputs g_kl + g_lk
@@ -193,7 +193,7 @@ namespace mfgpu
                           const int i = vi[r], j = vj[r], k2 = vi[s], l2 = vj[s];
                           const T   C = aa * T(0.5) * (T(i == k2 && j == l2) + T(i == l2 && j == k2)) +
                                       bl * T(i == j && k2 == l2);
-                          cp[(17 + r * 6 + s) * N3] = C;
+                          st((17 + r * 6 + s), C);
                         }
                   }
               }

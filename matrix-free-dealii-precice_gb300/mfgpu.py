@@ -208,6 +208,10 @@ class _Operator:
             self.h, dst_np.ctypes.data_as(C.c_void_p),
             src_np.ctypes.data_as(C.c_void_p)))
 
+    def set_fp64_emulation(self, enable=True):
+        """Double-float arithmetic on the FP32 pipe for an FP64 operator."""
+        _check(lib().mfgpu_operator_set_fp64_emulation(self.h, int(enable)))
+
     def compute_diagonal(self):
         _check(lib().mfgpu_operator_compute_diagonal(self.h))
 

@@ -278,3 +278,50 @@ def test_prolongation_reproduces_polynomials(ctx):
     d_f = dev(np.zeros(len(Xf)))
     mfgpu.prolongate(ctx, m, 0, 1, dev(f(Xc, Yc, Zc)), d_f)
     assert np.max(np.abs(host(d_f) - f(Xf, Yf, Zf))) < 1e-12
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+def test_fp64_emulation_parity(ctx, degree):
+    """Double-float arithmetic on the FP32 pipe keeps the FP64 operator
+    within the 1e-12 relative l2 bar against the oracle (heat and the
+    referential_qp tangent)."""
+    spec = small_heat(degree)
+    n = W.n_dofs(spec, 1)
+    src = W.uniform_vector(n, 1)
+    ref = O.heat_vmult(W.to_oracle_mesh(O, spec), 1, 0.1, src)
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    op.set_fp64_emulation(True)
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    assert rel(host(d_dst), ref) < TOL64
+
+    spec, u = nh_setup(degree)
+    n = W.n_dofs(spec, 3)
+    src = W.uniform_vector(n, 3)
+    ref = O.nh_vmult(W.to_oracle_mesh(O, spec), 1, O.material(dt=0.01),
+                     "scalar_referential", u, src)
+    op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, "referential_qp")
+    op.set_material(mfgpu.material(dt=0.01))
+    d_u = dev(u)
+    op.initialize(d_u)
+    op.set_fp64_emulation(True)
+    op.cache()
+    d_dst = dev(np.zeros(n))
+    op.vmult(d_dst, dev(src))
+    assert rel(host(d_dst), ref) < TOL64
+    # vmult_add on the same path
+    op.vmult_add(d_dst, dev(src))
+    assert rel(host(d_dst), 2 * ref) < TOL64
+
+
+def test_fp64_emulation_rejects_unsupported(ctx):
+    spec, _ = nh_setup(2)
+    op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, "tensor4")
+    op.set_material(mfgpu.material(dt=0.01))
+    with pytest.raises(mfgpu.MfgpuError) as e:
+        op.set_fp64_emulation(True)
+    assert e.value.code == 8
+    op32 = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, small_heat(2)), -1, 32, True,
+                                 delta_t=0.1)
+    with pytest.raises(mfgpu.MfgpuError):
+        op32.set_fp64_emulation(True)
