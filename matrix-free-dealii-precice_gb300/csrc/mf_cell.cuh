@@ -201,6 +201,21 @@ namespace mfgpu
                     (NC == 1 ? 4 : 2);
   }
 
+  // Cells per block of the operator-application kernels: blocks of
+  // CPB*N^2 threads that fill whole warps (or nearly), within the shared
+  // memory of one SM.
+  template <int N, int NC, typename TS, bool EVAL_U>
+  __host__ __device__ constexpr int
+  apply_cells_per_block()
+  {
+    return N == 2 ? 32 :
+           N == 3 ? 32 :
+           N == 4 ? 8 :
+           N == 5 ? 5 :
+           N == 6 ? (NC == 1 ? 8 : (EVAL_U ? 4 : 7)) :
+                    (NC == 1 ? 5 : (EVAL_U ? (sizeof(TS) == 8 ? 3 : 5) : 5));
+  }
+
   // shared memory per cell (in elements of T): NC*(value + 3 gradients)
   // + 2 scratch arrays + (optional) 3*NC gradients of the linearisation
   template <int N, int NC, bool EVAL_U>
@@ -217,36 +232,44 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   template <int N, typename T>
   __device__ __forceinline__ void
-  evaluate_field(const Shape<N, T> &sh, const T (&col)[N], T *V, T *G0, T *G1,
-                 T *G2, T *T0, T *T1, int a, int b, bool want_values)
+  evaluate_field(const T *S, const T *D0, const T *D1, const T *D2,
+                 const T (&col)[N], T *V, T *G0, T *G1, T *G2, T *T0, T *T1,
+                 int a, int b, bool want_values)
   {
     T x[N], y[N];
     // z interpolation in registers, store z-line (x=a, y=b)
-    mat_apply<N>(sh.S, col, y);
+    mat_apply<N>(S, col, y);
     store_line<N, T, 2>(T0, a, b, y);
     __syncthreads();
     // y interpolation: line (x=a, z=b)
     load_line<N, T, 1>(T0, a, b, x);
-    mat_apply<N>(sh.S, x, y);
+    mat_apply<N>(S, x, y);
     store_line<N, T, 1>(T1, a, b, y);
     __syncthreads();
     // x interpolation: line (y=a, z=b) -> values; x-derivative from registers
     load_line<N, T, 0>(T1, a, b, x);
-    mat_apply<N>(sh.S, x, y);
-    if (want_values)
-      store_line<N, T, 0>(V, a, b, y);
-    mat_apply<N>(sh.D, y, x);
+    mat_apply<N>(S, x, y);
+    store_line<N, T, 0>(V, a, b, y); // values (also needed for the y/z derivatives)
+    (void)want_values;
+    mat_apply<N>(D0, y, x);
     store_line<N, T, 0>(G0, a, b, x);
-    if (!want_values)
-      store_line<N, T, 0>(V, a, b, y); // V needed for the y/z derivatives
     __syncthreads();
     // y and z derivatives of the values
     load_line<N, T, 1>(V, a, b, x);
-    mat_apply<N>(sh.D, x, y);
+    mat_apply<N>(D1, x, y);
     store_line<N, T, 1>(G1, a, b, y);
     load_line<N, T, 2>(V, a, b, x);
-    mat_apply<N>(sh.D, x, y);
+    mat_apply<N>(D2, x, y);
     store_line<N, T, 2>(G2, a, b, y);
+  }
+
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  evaluate_field(const Shape<N, T> &sh, const T (&col)[N], T *V, T *G0, T *G1,
+                 T *G2, T *T0, T *T1, int a, int b, bool want_values)
+  {
+    evaluate_field<N>(sh.S, sh.D, sh.D, sh.D, col, V, G0, G1, G2, T0, T1, a, b,
+                      want_values);
   }
 
   // ---------------------------------------------------------------------
@@ -256,9 +279,9 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   template <int N, typename T>
   __device__ __forceinline__ void
-  integrate_field(const Shape<N, T> &sh, T *V, const T *G0, const T *G1,
-                  const T *G2, T *T0, T *T1, int a, int b, bool has_values,
-                  bool has_gradients, T (&col)[N])
+  integrate_field(const T *S, const T *D0, const T *D1, const T *D2, T *V,
+                  const T *G0, const T *G1, const T *G2, T *T0, T *T1, int a,
+                  int b, bool has_values, bool has_gradients, T (&col)[N])
   {
     T x[N], y[N];
     __syncthreads();
@@ -272,31 +295,41 @@ namespace mfgpu
 #pragma unroll
           for (int i = 0; i < N; ++i)
             y[i] = zero<T>();
-        mat_apply_t_add<N>(sh.D, x, y);
+        mat_apply_t_add<N>(D2, x, y);
         store_line<N, T, 2>(V, a, b, y);
         __syncthreads();
         // y: V += D^T G1 on y-line (x=a,z=b)
         load_line<N, T, 1>(G1, a, b, x);
         load_line<N, T, 1>(V, a, b, y);
-        mat_apply_t_add<N>(sh.D, x, y);
+        mat_apply_t_add<N>(D1, x, y);
         store_line<N, T, 1>(V, a, b, y);
         __syncthreads();
         // x: t = V + D^T G0 on x-line (y=a,z=b); then S^T
         load_line<N, T, 0>(G0, a, b, x);
         load_line<N, T, 0>(V, a, b, y);
-        mat_apply_t_add<N>(sh.D, x, y);
+        mat_apply_t_add<N>(D0, x, y);
       }
     else
       load_line<N, T, 0>(V, a, b, y);
-    mat_apply_t<N>(sh.S, y, x);
+    mat_apply_t<N>(S, y, x);
     store_line<N, T, 0>(T0, a, b, x);
     __syncthreads();
     load_line<N, T, 1>(T0, a, b, x);
-    mat_apply_t<N>(sh.S, x, y);
+    mat_apply_t<N>(S, x, y);
     store_line<N, T, 1>(T1, a, b, y);
     __syncthreads();
     load_line<N, T, 2>(T1, a, b, x);
-    mat_apply_t<N>(sh.S, x, col);
+    mat_apply_t<N>(S, x, col);
+  }
+
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  integrate_field(const Shape<N, T> &sh, T *V, const T *G0, const T *G1,
+                  const T *G2, T *T0, T *T1, int a, int b, bool has_values,
+                  bool has_gradients, T (&col)[N])
+  {
+    integrate_field<N>(sh.S, sh.D, sh.D, sh.D, V, G0, G1, G2, T0, T1, a, b,
+                       has_values, has_gradients, col);
   }
 
   // node index of local node (a, b, k) of cell (cx,cy,cz)
@@ -329,14 +362,14 @@ namespace mfgpu
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
   template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED>
-  __global__ void __launch_bounds__(cells_per_block<N, NC, TS>() * N * N)
-  cell_apply_kernel(const __grid_constant__ Shape<N, T> sh,
+  __global__ void __launch_bounds__(apply_cells_per_block<N, NC, TS, QOp::eval_u>() * N * N)
+  cell_apply_kernel(const __grid_constant__ ShapeA<N, T> sh,
                     const __grid_constant__ CellGeom<T> g, const QOp op,
                     const TS *__restrict__ src, TS *__restrict__ dst)
   {
     constexpr int N2  = N * N;
     constexpr int N3  = N * N * N;
-    constexpr int CPB = cells_per_block<N, NC, TS>();
+    constexpr int CPB = apply_cells_per_block<N, NC, TS, QOp::eval_u>();
     constexpr int SPC = smem_per_cell<N, NC, QOp::eval_u>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
@@ -381,8 +414,8 @@ namespace mfgpu
             col[k] = val;
           }
         T *V = cb + c * 4 * N3;
-        evaluate_field<N>(sh, col, V, V + N3, V + 2 * N3, V + 3 * N3, T0, T1, a,
-                          b, true);
+        evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
+                          V + 3 * N3, T0, T1, a, b, true);
       }
     if constexpr (QOp::eval_u)
       {
@@ -397,8 +430,8 @@ namespace mfgpu
             // the values go to T1 (scratch); GU + c*3*N3 holds the gradients
             T *Gc = GU + c * 3 * N3;
             __syncthreads();
-            evaluate_field<N>(sh, col, T1, Gc, Gc + N3, Gc + 2 * N3, T0, T1, a,
-                              b, false);
+            evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, T1, Gc, Gc + N3,
+                              Gc + 2 * N3, T0, T1, a, b, false);
           }
       }
     __syncthreads();
@@ -420,7 +453,7 @@ namespace mfgpu
                 v[c]       = V[q];
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
-                  H[c][d] = V[(d + 1) * N3 + q] * g.inv_h[d];
+                  H[c][d] = V[(d + 1) * N3 + q];
               }
             T Hu[NC][3];
             if constexpr (QOp::eval_u)
@@ -429,7 +462,7 @@ namespace mfgpu
                 for (int c = 0; c < NC; ++c)
 #pragma unroll
                   for (int d = 0; d < 3; ++d)
-                    Hu[c][d] = GU[(c * 3 + d) * N3 + q] * g.inv_h[d];
+                    Hu[c][d] = GU[(c * 3 + d) * N3 + q];
               }
             op(cell, q, v, H, Hu);
             const T jxw = wab * sh.w[k];
@@ -440,7 +473,7 @@ namespace mfgpu
                 V[q] = v[c] * jxw;
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
-                  V[(d + 1) * N3 + q] = H[c][d] * (jxw * g.inv_h[d]);
+                  V[(d + 1) * N3 + q] = H[c][d] * jxw;
               }
           }
       }
@@ -451,8 +484,8 @@ namespace mfgpu
       {
         T *V = cb + c * 4 * N3;
         T  col[N];
-        integrate_field<N>(sh, V, V + N3, V + 2 * N3, V + 3 * N3, T0, T1, a, b,
-                           true, true, col);
+        integrate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + N3, V + 2 * N3,
+                           V + 3 * N3, T0, T1, a, b, true, true, col);
         if (active)
           {
 #pragma unroll

@@ -47,6 +47,17 @@ namespace mfgpu
     T w[N];
   };
 
+  // shape data of the operator-application kernels: the collocation
+  // derivative per direction already divided by the cell size h_d, so the
+  // gradients come out in real coordinates
+  template <int N, typename T>
+  struct ShapeA
+  {
+    T S[N * N];
+    T D[3][N * N];
+    T w[N];
+  };
+
   // geometry of a level as seen by a cell kernel, in precision T
   template <typename T>
   struct CellGeom

@@ -57,6 +57,51 @@ namespace mfgpu
     e = __fsub_rn(b, __fsub_rn(s, a));
   }
 
+  // float -> double by exponent/mantissa re-encoding (integer pipe only);
+  // zeros, float subnormals, infinities and NaN take the ordinary path
+  __device__ __forceinline__ double
+  f2d_bits(float f)
+  {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 255u)
+      return double(f);
+    const unsigned long long bits =
+      (static_cast<unsigned long long>(u >> 31) << 63) |
+      (static_cast<unsigned long long>(e + 896u) << 52) |
+      (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
+    return __longlong_as_double(static_cast<long long>(bits));
+  }
+
+  // double -> df64 by splitting the mantissa: hi keeps the leading 24
+  // significant bits (exact float), lo = x - hi rounded to 24 bits.  Uses
+  // integer operations and one integer-to-float conversion; magnitudes
+  // outside [2^-74, 2^127] take the FP64 path.
+  __device__ __forceinline__ df64
+  df_from_double_bits(double x)
+  {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned           e = static_cast<unsigned>(b >> 52) & 0x7ffu;
+    if (e < 949u || e > 1150u)
+      return df_from_double(x);
+    const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+    const float    hi   = __uint_as_float(sign | ((e - 896u) << 23) |
+                                          (static_cast<unsigned>(b >> 29) & 0x7fffffu));
+    const unsigned r     = static_cast<unsigned>(b & 0x1fffffffu);
+    const float    scale = __uint_as_float((e - 948u) << 23); // 2^(e - 1075)
+    const float    lo    = __uint_as_float(sign | __float_as_uint(__fmul_rn(__uint2float_rn(r), scale)));
+    float          s, t;
+    quick_two_sum(hi, lo, s, t);
+    return {s, t};
+  }
+
+  // df64 -> double: exact float->double re-encodings and one FP64 add
+  __device__ __forceinline__ double
+  df_to_double_bits(df64 a)
+  {
+    return f2d_bits(a.hi) + f2d_bits(a.lo);
+  }
+
   __device__ __forceinline__ df64
   operator+(df64 a, df64 b)
   {
@@ -174,7 +219,7 @@ namespace mfgpu
   __device__ __forceinline__ df64
   to_compute<df64, double>(double x)
   {
-    return df_from_double(x);
+    return df_from_double_bits(x);
   }
   template <typename TS, typename TC>
   __device__ __forceinline__ TS
@@ -186,7 +231,7 @@ namespace mfgpu
   __device__ __forceinline__ double
   to_storage<double, df64>(df64 x)
   {
-    return df_to_double(x);
+    return df_to_double_bits(x);
   }
 
   // compile-time constant in the compute type

@@ -30,6 +30,22 @@ namespace mfgpu
       return s;
     }
 
+    template <int N, typename T>
+    ShapeA<N, T>
+    make_shape_apply(const HostBasis &b, const LevelGeom &g)
+    {
+      ShapeA<N, T> s;
+      for (int i = 0; i < N * N; ++i)
+        {
+          s.S[i] = conv_host<T>(b.S[i]);
+          for (int d = 0; d < 3; ++d)
+            s.D[d][i] = conv_host<T>(b.D[i] / g.h[d]);
+        }
+      for (int i = 0; i < N; ++i)
+        s.w[i] = conv_host<T>(b.w[i]);
+      return s;
+    }
+
     template <typename T>
     NHMat<T>
     to_mat(const NHMatD &m)
@@ -56,10 +72,10 @@ namespace mfgpu
 
     template <int N, typename TS, typename T, int NC, class Op, bool CON>
     cudaError_t
-    run_apply(const Shape<N, T> &sh, const CellGeom<T> &cg, const Op &op,
+    run_apply(const ShapeA<N, T> &sh, const CellGeom<T> &cg, const Op &op,
               const TS *src, TS *dst, cudaStream_t s)
     {
-      constexpr int CPB  = cells_per_block<N, NC, TS>();
+      constexpr int CPB  = apply_cells_per_block<N, NC, TS, Op::eval_u>();
       const size_t  smem = size_t(CPB) * smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
       auto          k    = cell_apply_kernel<N, TS, T, NC, Op, CON>;
       cudaError_t   e    = prepare(k, smem);
@@ -72,7 +88,7 @@ namespace mfgpu
 
     template <int N, typename TS, typename T, int NC, class Op>
     cudaError_t
-    run_apply_c(bool con, const Shape<N, T> &sh, const CellGeom<T> &cg,
+    run_apply_c(bool con, const ShapeA<N, T> &sh, const CellGeom<T> &cg,
                 const Op &op, const TS *src, TS *dst, cudaStream_t s)
     {
       return con ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, s) :
@@ -85,7 +101,7 @@ namespace mfgpu
   launch_apply(const HostBasis &b, const LevelGeom &g, const ApplyArgs &a,
                cudaStream_t s)
   {
-    const Shape<N, T>    sh  = make_shape<N, T>(b);
+    const ShapeA<N, T>   sh  = make_shape_apply<N, T>(b, g);
     const CellGeom<T>    cg  = make_cell_geom<T>(g);
     const T             *src = static_cast<const T *>(a.src);
     T                   *dst = static_cast<T *>(a.dst);
@@ -319,7 +335,7 @@ namespace mfgpu
   launch_apply_df(const HostBasis &b, const LevelGeom &g, const ApplyArgs &a,
                   cudaStream_t s)
   {
-    const Shape<N, df64>    sh  = make_shape<N, df64>(b);
+    const ShapeA<N, df64>   sh  = make_shape_apply<N, df64>(b, g);
     const CellGeom<df64>    cg  = make_cell_geom<df64>(g);
     const double           *src = static_cast<const double *>(a.src);
     double                 *dst = static_cast<double *>(a.dst);
