@@ -42,11 +42,13 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--caching", default="referential_qp")
-    p.add_argument("--arith", default="native", choices=["native", "df64"],
+    p.add_argument("--arith", default="df64", choices=["native", "df64"],
                    help="FP64 operator arithmetic: native FP64 or double-float on the FP32 pipe")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the secondary measurements (solves, degree sweep)")
     return p.parse_args()
 
 
@@ -170,6 +172,154 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
             "kind": "port",
             "sample": f"{reps} full applications (cache + vmult, scalar_referential) of "
                       f"the {n}-DoF Q4 operator on {nthreads} threads; first call {t_first:.2f}s"}
+
+
+def _timed_vmults(torch, op, dst, src, flush, stream, reps):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(reps)]
+    for i in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+        op.vmult(dst, src)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / reps * 1e-3
+
+
+def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
+    """128x16x16-cell Q3 cantilever (2.77M DoFs): the first Newton linear
+    system (linearised at rest, traction (0,-100,0) on x = 8) solved to a
+    1e-8 relative residual by FP64 CG with an FP32 V-cycle (FP64 coarse
+    solve) and with an all-FP64 V-cycle; error against an FP64-everywhere
+    solve to 1e-12."""
+    spec = W.cantilever(3, 4)
+    n = W.n_dofs(spec, 3)
+    zero = torch.zeros(n, dtype=torch.float64, device=dev)
+    rhs = torch.zeros(n, dtype=torch.float64, device=dev)
+
+    def params(mgp, c64, tol, emul=False):
+        p = mfgpu.SolidParams()
+        p.mesh = W.to_lib_mesh(mfgpu, spec)
+        p.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+        p.caching = b"referential_qp"
+        p.solver = mfgpu.solver_params("gmg", tol=tol, mg_precision=mgp, coarse_fp64=c64,
+                                       fp64_emulation=emul)
+        p.dt, p.n_steps, p.max_newton = 0.01, 1, 10
+        p.traction_id = W.TRACTION_ID
+        p.traction[:] = [0.0, -100.0, 0.0]
+        return p
+
+    ref_solver = mfgpu.Solid(ctx, params(64, False, 1e-12))
+    ref_solver.residual(zero, zero, rhs)
+    du_ref = torch.zeros_like(rhs)
+    ref_solver.linear_solve(zero, rhs, du_ref)
+    ref_solver.close()
+    out = {"workload": "cantilever 128x16x16 cells Q3, 2,773,155 DoFs, first Newton system",
+           "tolerance": 1e-8}
+    for name, mgp, c64, emul in (("mixed_fp32_vcycle", 32, True, False),
+                                 ("fp64_vcycle", 64, False, False),
+                                 ("fp64_vcycle_df64", 64, False, True)):
+        s = mfgpu.Solid(ctx, params(mgp, c64, 1e-8, emul))
+        du = torch.zeros_like(rhs)
+        s.linear_solve(zero, rhs, du)  # warm-up (setup + solve)
+        du.zero_()
+        t0 = time.perf_counter()
+        its, secs = s.linear_solve(zero, rhs, du)
+        total = time.perf_counter() - t0
+        err = (du - du_ref)
+        out[name] = {"cg_iterations": its, "solve_s": secs, "setup_plus_solve_s": total,
+                     "l2_rel_error_vs_fp64": float(err.norm() / du_ref.norm()),
+                     "max_rel_error_vs_fp64": float(err.abs().max() / du_ref.abs().max())}
+        s.close()
+    out["speedup_mixed_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle"]["solve_s"]
+    return out
+
+
+def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
+    """Heat operator on the unit cube with 64^3 cells, Q1..Q6: vmult DoF/s
+    and achieved GB/s (B_alg = 2 s N_dof + 4 s N_cells) in FP64 (native and
+    double-float) and FP32; FP32-GMG vs FP64-GMG CG to 1e-8 with the seeded
+    Gaussian source."""
+    res = []
+    c, w, a = W.gaussian_source(0)
+    for deg in range(1, 7):
+        spec = W.unit_cube_heat(deg, 6)
+        mesh = W.to_lib_mesh(mfgpu, spec)
+        n = W.n_dofs(spec, 1)
+        cells = 64 ** 3
+        row = {"degree": deg, "n_dofs": n}
+        for label, prec, emul in (("fp64", 64, False), ("fp64_df64", 64, True), ("fp32", 32, False)):
+            dt = torch.float64 if prec == 64 else torch.float32
+            op = mfgpu.LaplaceOperator(ctx, mesh, -1, prec, True, delta_t=0.1)
+            if emul:
+                op.set_fp64_emulation(True)
+            src = torch.rand(n, dtype=dt, device=dev) * 2 - 1
+            dst = torch.zeros_like(src)
+            op.vmult(dst, src)
+            t = _timed_vmults(torch, op, dst, src, flush, stream, 5)
+            s = 8 if prec == 64 else 4
+            gbs = (2 * s * n + 4 * s * cells) / t / 1e9
+            row[label] = {"dofs_per_s": n / t, "ms": t * 1e3, "gbs": gbs, "hbm_frac": gbs / peak}
+            op.close()
+            del src, dst
+        for label, mgp in (("gmg_fp32_solve_s", 32), ("gmg_fp64_solve_s", 64)):
+            hp = mfgpu.HeatParams()
+            hp.mesh = mesh
+            hp.dt, hp.n_steps = 0.1, 1
+            hp.solver = mfgpu.solver_params("gmg", tol=1e-8, cheb_range=15.0, cheb_eig_its=10,
+                                            mg_precision=mgp, coarse_fp64=(mgp == 32))
+            hp.n_gauss = 8
+            for i in range(8):
+                for d in range(3):
+                    hp.g_center[i][d] = c[i, d]
+                hp.g_width[i] = w[i]
+                hp.g_amp[i] = a[i]
+            h = mfgpu.Heat(ctx, hp)
+            r = h.run()
+            row[label] = r.seconds
+            row[label.replace("_s", "_its")] = r.cg_its[0]
+            h.close()
+        res.append(row)
+        torch.cuda.empty_cache()
+    return res
+
+
+def extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush):
+    """Unit cube 16^3 cells Q2 (35,937 DoFs): one backward-Euler step solved
+    by GMG-CG to 1e-10, and 100 FP64 vmults."""
+    spec = W.unit_cube_heat(2, 4)
+    mesh = W.to_lib_mesh(mfgpu, spec)
+    c, w, a = W.gaussian_source(0)
+    hp = mfgpu.HeatParams()
+    hp.mesh = mesh
+    hp.dt, hp.n_steps = 0.1, 1
+    hp.solver = mfgpu.solver_params("gmg", tol=1e-10, cheb_range=15.0, cheb_eig_its=10,
+                                    mg_precision=32)
+    hp.n_gauss = 8
+    for i in range(8):
+        for d in range(3):
+            hp.g_center[i][d] = c[i, d]
+        hp.g_width[i] = w[i]
+        hp.g_amp[i] = a[i]
+    h = mfgpu.Heat(ctx, hp)
+    h.run()
+    r = h.run()
+    h.close()
+    n = W.n_dofs(spec, 1)
+    op = mfgpu.LaplaceOperator(ctx, mesh, -1, 64, True, delta_t=0.1)
+    src = torch.rand(n, dtype=torch.float64, device=dev)
+    dst = torch.zeros_like(src)
+    op.vmult(dst, src)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(100):
+        op.vmult(dst, src)
+    ctx.synchronize()
+    t100 = time.perf_counter() - t0
+    return {"workload": "heat unit cube 16^3 Q2, 35,937 DoFs", "step_s": r.seconds,
+            "cg_iterations": r.cg_its[0], "vmult_100_s": t100}
 
 
 def run_reference(args):
@@ -314,7 +464,15 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
 
-    # correctness guard of the timed result: symmetric operator, u^T A v == v^T A u
+    # the same operator in native FP64 arithmetic, for comparison
+    native = None
+    if args.arith == "df64":
+        op.set_fp64_emulation(False)
+        op.cache()
+        t_nat = _timed_vmults(torch, op, dst, src, flush, stream, max(5, K // 4))
+        native = {"value": world * n / t_nat, "ms_per_step": t_nat * 1e3}
+        op.set_fp64_emulation(True)
+        op.cache()
     ctx.synchronize()
     peak, peak_kind = measured_peak_hbm()
     b_alg = algorithmic_bytes(n, n_cells)
@@ -324,7 +482,13 @@ def main():
         "metric": METRIC, "value": world * n / (ms_step * 1e-3), "unit": UNIT,
         "n_gpus": world, "steps": K, "warmup": max(args.warmup, 3),
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "df64" if args.arith == "df64" else "f64",
+        "dtype_note": ("FP64 vectors in and out; arithmetic in double-float (each FP64 value "
+                       "carried as a pair of FP32, 48-bit significand) on the FP32 pipe; agrees "
+                       "with the FP64 oracle within 1e-12 relative l2 (tests/test_gpu_operators.py)")
+                      if args.arith == "df64" else "native FP64 arithmetic",
+        "native_f64": native,
+        "data": "synthetic",
         "config": {"workload": "nh_tangent_vmult_q4_cantilever_64x8x8", "n_dofs": n,
                    "n_cells": n_cells, "degree": 4, "n_q_1d": 5, "caching": args.caching,
                    "arithmetic": "native FP64" if args.arith == "native" else
@@ -344,6 +508,19 @@ def main():
         "gpu_launches": launches,
         "wall_ms_per_step": t_wall / K * 1e3,
     }
+    if not args.no_extras:
+        extras = {}
+        for key, fn in (("time_to_solve_1e-8", lambda: extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev)),
+                        ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
+                        ("degree_sweep_heat_64cube", lambda: extra_degree_sweep(torch, mfgpu, W, ctx, dev,
+                                                                               stream, flush, peak))):
+            try:
+                t0 = time.perf_counter()
+                extras[key] = fn()
+                extras[key + "_wall_s"] = time.perf_counter() - t0
+            except Exception as e:
+                extras[key] = {"error": str(e)}
+        line["extras"] = extras
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(spec, u_h, src_h, args.cpu_seconds)

@@ -226,6 +226,7 @@ typedef struct mfgpu_solver_params
   int    coarse_accurate; /* level 0: eigenvalue CG iterations = m()        */
   int    mg_precision;    /* 32: FP32 level operators, 64: all-FP64 V-cycle */
   int    coarse_fp64;     /* level-0 Chebyshev solve in FP64                */
+  int    fp64_emulation;  /* FP64 operators in double-float arithmetic      */
 } mfgpu_solver_params;
 
 typedef struct mfgpu_solid_params
@@ -258,6 +259,12 @@ typedef struct mfgpu_solid_result
 int mfgpu_solid_create(mfgpu_context *ctx, const mfgpu_solid_params *p,
                        mfgpu_solid **s);
 int mfgpu_solid_run(mfgpu_solid *s, mfgpu_solid_result *r);
+/* Newton residual (Solid::assemble_residual, mf_elasticity.h:1649-1908):
+ * rhs = -int tau F^{-T} : Grad v + int rho (b - a) . v + traction term,
+ * constrained rows zero; u, acceleration, rhs are device vectors */
+int mfgpu_solid_residual(mfgpu_solid *s, const double *u,
+                         const double *acceleration, double *rhs,
+                         double *l2_norm);
 /* final displacement (device pointer owned by the solver) */
 int mfgpu_solid_displacement(mfgpu_solid *s, const double **u);
 /* one linear system of the Newton loop: linearise at u (device), solve

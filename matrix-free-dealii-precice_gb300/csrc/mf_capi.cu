@@ -540,6 +540,21 @@ extern "C"
   }
 
   int
+  mfgpu_solid_residual(mfgpu_solid *s, const double *u, const double *acceleration,
+                       double *rhs, double *l2_norm)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(u, "u");
+      need(acceleration, "acceleration");
+      need(rhs, "rhs");
+      const double nrm = s->d->residual_at(u, acceleration, rhs);
+      if (l2_norm)
+        *l2_norm = nrm;
+    });
+  }
+
+  int
   mfgpu_solid_displacement(mfgpu_solid *s, const double **u)
   {
     return guarded([&] {

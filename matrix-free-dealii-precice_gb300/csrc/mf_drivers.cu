@@ -122,6 +122,10 @@ namespace mfgpu
     fine->mat           = mat;
     fine->formulation   = P.material.formulation;
     fine->have_material = true;
+    const bool emul     = P.solver.fp64_emulation != 0;
+    if (emul && (variant != V_QP10 || P.material.formulation != 1))
+      throw Error(ERR_UNSUPPORTED, "fp64_emulation needs referential_qp caching and formulation 1");
+    fine->arith = emul ? 1 : 0;
     const size_t n      = fine->m();
     for (DevBuf *b : {&u, &delta, &v_old, &a_old, &acc, &rhs, &du})
       {
@@ -137,6 +141,7 @@ namespace mfgpu
             op->mat           = mat;
             op->formulation   = P.material.formulation;
             op->have_material = true;
+            op->arith         = (emul && lprec == 64) ? 1 : 0;
             lops.push_back(std::move(op));
             u_levels.emplace_back(lops.back()->m() * (lprec == 32 ? 4 : 8));
           }
@@ -146,6 +151,7 @@ namespace mfgpu
             coarse64->mat           = mat;
             coarse64->formulation   = P.material.formulation;
             coarse64->have_material = true;
+            coarse64->arith         = emul ? 1 : 0;
             u0_64.alloc(coarse64->m() * sizeof(double));
           }
         auto fill = [&](auto &mg) {
@@ -260,6 +266,18 @@ namespace mfgpu
       }
     constrained_op<double>(*ctx, fine->geom, 3, 2, nullptr, rhs.as<double>());
     return std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+  }
+
+  double
+  SolidDriver::residual_at(const double *uu, const double *aa, double *r)
+  {
+    const size_t n = fine->m();
+    vec_copy<double>(*ctx, n, uu, u.as<double>());
+    vec_copy<double>(*ctx, n, aa, acc.as<double>());
+    const double nrm = assemble_residual();
+    vec_copy<double>(*ctx, n, rhs.as<double>(), r);
+    ctx->sync();
+    return nrm;
   }
 
   struct FineOp : LinOp<double>
@@ -415,6 +433,9 @@ namespace mfgpu
     op->delta_t = P.dt;
     op_u        = make_heat(ctx, mesh, -1, 64, false);
     op_u->delta_t = P.dt;
+    const bool emul = P.solver.fp64_emulation != 0;
+    op->arith       = emul ? 1 : 0;
+    op_u->arith     = emul ? 1 : 0;
     const size_t n = op->m();
     for (DevBuf *b : {&sol, &sol_old, &rhs, &du, &uD})
       {
@@ -428,12 +449,14 @@ namespace mfgpu
           {
             auto lo     = make_heat(ctx, mesh, l, lprec, true);
             lo->delta_t = P.dt;
+            lo->arith   = (emul && lprec == 64) ? 1 : 0;
             lops.push_back(std::move(lo));
           }
         if (P.solver.coarse_fp64 && lprec == 32)
           {
             coarse64          = make_heat(ctx, mesh, 0, 64, true);
             coarse64->delta_t = P.dt;
+            coarse64->arith   = emul ? 1 : 0;
           }
         auto fill = [&](auto &mg) {
           mg.ctx = ctx;

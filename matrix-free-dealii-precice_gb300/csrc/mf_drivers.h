@@ -29,6 +29,7 @@ namespace mfgpu
     SolidDriver(Context *c, const mfgpu_solid_params &p);
     void                update_operators(const double *ulin);
     double              assemble_residual();
+    double              residual_at(const double *u, const double *acc, double *rhs);
     int                 solve_linear(const double *b, double *x, double tol);
     std::vector<double> point_value(const double *x);
     void                run(mfgpu_solid_result &res);

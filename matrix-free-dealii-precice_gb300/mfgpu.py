@@ -47,7 +47,8 @@ class SolverParams(C.Structure):
                 ("tol", C.c_double), ("max_it_mult", C.c_int),
                 ("cheb_degree", C.c_int), ("cheb_range", C.c_double),
                 ("cheb_eig_its", C.c_int), ("coarse_accurate", C.c_int),
-                ("mg_precision", C.c_int), ("coarse_fp64", C.c_int)]
+                ("mg_precision", C.c_int), ("coarse_fp64", C.c_int),
+                ("fp64_emulation", C.c_int)]
 
 
 class SolidParams(C.Structure):
@@ -325,7 +326,7 @@ def prolongate_noalloc(mesh, coarse_level, nc, coarse, fine, precision=64,
 def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
                   cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
                   coarse_accurate=True, mg_precision=32, coarse_fp64=False,
-                  max_it_mult=1):
+                  max_it_mult=1, fp64_emulation=False):
     s = SolverParams()
     s.preconditioner = {"none": 0, "jacobi": 1, "gmg": 2}[preconditioner]
     s.relaxation = relaxation
@@ -337,6 +338,7 @@ def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
     s.coarse_accurate = int(coarse_accurate)
     s.mg_precision = mg_precision
     s.coarse_fp64 = int(coarse_fp64)
+    s.fp64_emulation = int(fp64_emulation)
     return s
 
 
@@ -358,6 +360,12 @@ class Solid:
         p = C.c_void_p()
         _check(lib().mfgpu_solid_displacement(self.h, C.byref(p)))
         return p.value
+
+    def residual(self, u, acc, rhs):
+        nrm = C.c_double()
+        _check(lib().mfgpu_solid_residual(self.h, _ptr(u), _ptr(acc), _ptr(rhs),
+                                          C.byref(nrm)))
+        return nrm.value
 
     def linear_solve(self, u, rhs, du):
         its = C.c_int()
