@@ -322,6 +322,57 @@ def extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush):
             "cg_iterations": r.cg_its[0], "vmult_100_s": t100}
 
 
+def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
+    """300 independent requests (60 % heat on 8^3..64^3 cells, 40 %
+    neo-Hookean cantilevers 8k x k x k, k in {2,4,8}; degree U{1..4}; seeded
+    sources / tractions), Poisson arrivals at `load` times the server's
+    measured capacity, FP32-GMG preconditioned FP64 CG to 1e-8 served by
+    `workers` concurrent solves; against the same requests one at a time with
+    the plain FP64 solver (all-FP64 V-cycle)."""
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    reqs = W.serving_requests(mfgpu, n_requests, seed=seed, mg_precision=32)
+    # capacity: closed loop over the first 40 requests
+    srv = mfgpu.Server(0, workers, 0.8)
+    t0 = time.perf_counter()
+    ids = [srv.submit(r) for r in reqs[:40]]
+    for i in ids:
+        srv.wait(i)
+    capacity = 40 / (time.perf_counter() - t0)
+    rate = load * capacity
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    t0 = time.perf_counter()
+    ids = []
+    for r, ta in zip(reqs, arrivals):
+        dt = ta - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(r))
+    res = [srv.wait(i) for i in ids]
+    span = time.perf_counter() - t0
+    max_running, budget = srv.stats()
+    srv.close()
+    lat = np.array([r.latency_seconds for r in res])
+    errors = sum(1 for r in res if r.status != 0)
+    # baseline: one at a time, plain FP64 solver
+    base_reqs = W.serving_requests(mfgpu, n_requests, seed=seed, mg_precision=64)
+    srv = mfgpu.Server(0, 1, 0.8)
+    t0 = time.perf_counter()
+    ids = [srv.submit(r) for r in base_reqs]
+    bres = [srv.wait(i) for i in ids]
+    bspan = time.perf_counter() - t0
+    srv.close()
+    brun = np.array([r.run_seconds for r in bres])
+    return {"requests": n_requests, "workers": workers, "arrival_rate_per_s": rate,
+            "capacity_closed_loop_per_s": capacity,
+            "solves_per_s": n_requests / span, "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)), "max_concurrent": max_running,
+            "errors": errors,
+            "baseline_fp64_one_at_a_time": {"solves_per_s": n_requests / bspan,
+                                            "service_p50_s": float(np.percentile(brun, 50)),
+                                            "service_p99_s": float(np.percentile(brun, 99)),
+                                            "errors": sum(1 for r in bres if r.status != 0)}}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -513,7 +564,8 @@ def main():
         for key, fn in (("time_to_solve_1e-8", lambda: extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev)),
                         ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
                         ("degree_sweep_heat_64cube", lambda: extra_degree_sweep(torch, mfgpu, W, ctx, dev,
-                                                                               stream, flush, peak))):
+                                                                               stream, flush, peak)),
+                        ("serving_300_requests", lambda: extra_serving(mfgpu, W))):
             try:
                 t0 = time.perf_counter()
                 extras[key] = fn()

@@ -302,6 +302,53 @@ int mfgpu_heat_run(mfgpu_heat *h, mfgpu_heat_result *r);
 int mfgpu_heat_solution(mfgpu_heat *h, const double **u);
 int mfgpu_heat_destroy(mfgpu_heat *h);
 
+/* ---------------------------------------------------------------- */
+/* request server: independent solves served concurrently            */
+/* ---------------------------------------------------------------- */
+/* No counterpart in the reference (one problem per MPI job there).
+ * Requests queue FIFO; a request starts when a worker is free and its
+ * estimated device memory fits in the budget (memory_fraction of the free
+ * HBM at creation).  Each worker owns a CUDA stream, so admitted solves
+ * overlap on the device; a solve keeps its hierarchy resident until it
+ * finishes.  Results do not depend on what else runs (deterministic
+ * reductions; scatter round-off only). */
+typedef struct mfgpu_server mfgpu_server;
+
+typedef struct mfgpu_request
+{
+  int                kind; /* 0 heat (uses `heat`), 1 solid (uses `solid`) */
+  mfgpu_heat_params  heat;
+  mfgpu_solid_params solid;
+} mfgpu_request;
+
+typedef struct mfgpu_request_result
+{
+  int    status; /* MFGPU_OK or the error of the solve */
+  char   message[128];
+  int    cg_iterations;
+  int    newton_iterations;
+  double watch[3];
+  double solution_norm;
+  double n_dofs;
+  double queue_seconds;
+  double run_seconds;
+  double latency_seconds;
+} mfgpu_request_result;
+
+int mfgpu_server_create(int device, int max_concurrent, double memory_fraction,
+                        mfgpu_server **server);
+/* queue a request (copied); returns its id */
+int mfgpu_server_submit(mfgpu_server *server, const mfgpu_request *request,
+                        long long *id);
+/* block until request `id` finished; its record is released */
+int mfgpu_server_wait(mfgpu_server *server, long long id,
+                      mfgpu_request_result *result);
+/* highest number of solves that ran at the same time; memory budget */
+int mfgpu_server_stats(mfgpu_server *server, int *max_running,
+                       size_t *budget_bytes);
+/* finishes queued requests, then stops the workers */
+int mfgpu_server_destroy(mfgpu_server *server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,326 @@
+// Request server: independent heat and neo-Hookean solves on one GPU.
+//
+// Requests are queued FIFO.  A request is admitted when its estimated
+// device memory fits in the remaining budget (a fraction of the free HBM
+// at server start) and a worker is free.  Every worker owns a context with
+// its own CUDA stream, so admitted solves run concurrently and their
+// kernels overlap on the device.  A solve keeps its geometry, multigrid
+// hierarchy and vectors resident in HBM for its lifetime and releases
+// them (and its budget) when it finishes.  Latency = completion time -
+// submit time.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+
+#include "../../include/mfgpu.h"
+#include "mf_drivers.h"
+
+namespace mfgpu
+{
+  using clock_t_ = std::chrono::steady_clock;
+
+  struct ServerJob
+  {
+    long long            id;
+    mfgpu_request        req;
+    std::string          caching; // keeps req.solid.caching alive
+    size_t               bytes = 0;
+    clock_t_::time_point t_submit, t_start, t_end;
+    mfgpu_request_result res{};
+    bool                 done = false;
+  };
+
+  // device memory a request will hold (vectors, caches, level hierarchy),
+  // from the DoF and quadrature-point counts of its finest level
+  size_t
+  estimate_request_bytes(const mfgpu_request &r)
+  {
+    const mfgpu_mesh &mm = r.kind == 0 ? r.heat.mesh : r.solid.mesh;
+    const Mesh        m  = to_mesh(mm);
+    const LevelGeom   g  = m.level(-1);
+    const double      nq = double(g.n_cells) * (m.degree + 1) * (m.degree + 1) * (m.degree + 1);
+    const double      ml = 8.0 / 7.0; // geometric level hierarchy
+    if (r.kind == 0)
+      {
+        const double nd = double(g.n_nodes);
+        // 5 driver vectors + 2 operators' diagonals + CG (4) + MG (3 per level,
+        // FP32) + transfers (2 fine-sized temporaries)
+        return size_t(nd * 8 * 13 + nd * ml * 4 * 8 + (64 << 20));
+      }
+    const double nd = 3.0 * double(g.n_nodes);
+    // 7 driver vectors + CG (4) + diag (2) + cache (10 words per qp) + MG
+    return size_t(nd * 8 * 15 + nq * 80 * ml + nd * ml * 4 * 10 + (64 << 20));
+  }
+
+  struct Server
+  {
+    int                                   device;
+    size_t                                budget = 0, reserved = 0;
+    int                                   n_workers;
+    std::deque<ServerJob *>               queue;
+    std::map<long long, std::unique_ptr<ServerJob>> jobs;
+    std::mutex                            mu;
+    std::condition_variable               cv_work, cv_done;
+    std::vector<std::thread>              workers;
+    bool                                  stop = false;
+    long long                             next_id = 1;
+    int                                   running = 0, max_running = 0;
+
+    Server(int dev, int nw, double fraction)
+      : device(dev)
+      , n_workers(nw)
+    {
+      MF_CK(cudaSetDevice(dev));
+      size_t free_b = 0, total_b = 0;
+      MF_CK(cudaMemGetInfo(&free_b, &total_b));
+      budget = size_t(double(free_b) * fraction);
+      for (int i = 0; i < nw; ++i)
+        workers.emplace_back([this] { loop(); });
+    }
+
+    ~Server()
+    {
+      {
+        std::lock_guard<std::mutex> l(mu);
+        stop = true;
+      }
+      cv_work.notify_all();
+      for (auto &t : workers)
+        t.join();
+    }
+
+    void
+    loop()
+    {
+      cudaSetDevice(device);
+      std::unique_ptr<Context> ctx;
+      try
+        {
+          ctx.reset(new Context(device));
+        }
+      catch (...)
+        {
+          return;
+        }
+      for (;;)
+        {
+          ServerJob *job = nullptr;
+          {
+            std::unique_lock<std::mutex> l(mu);
+            cv_work.wait(l, [&] {
+              return stop || (!queue.empty() && reserved + queue.front()->bytes <= budget) ||
+                     (!queue.empty() && running == 0); // a job larger than the budget runs alone
+            });
+            if (stop && queue.empty())
+              return;
+            if (queue.empty())
+              continue;
+            job = queue.front();
+            queue.pop_front();
+            reserved += job->bytes;
+            ++running;
+            max_running = std::max(max_running, running);
+            job->t_start = clock_t_::now();
+          }
+          run(*ctx, *job);
+          {
+            std::lock_guard<std::mutex> l(mu);
+            job->t_end = clock_t_::now();
+            reserved -= job->bytes;
+            --running;
+            job->done                = true;
+            job->res.queue_seconds   = std::chrono::duration<double>(job->t_start - job->t_submit).count();
+            job->res.run_seconds     = std::chrono::duration<double>(job->t_end - job->t_start).count();
+            job->res.latency_seconds = std::chrono::duration<double>(job->t_end - job->t_submit).count();
+          }
+          cv_done.notify_all();
+          cv_work.notify_all();
+        }
+    }
+
+    void
+    run(Context &ctx, ServerJob &job)
+    {
+      mfgpu_request_result &r = job.res;
+      try
+        {
+          if (job.req.kind == 0)
+            {
+              HeatDriver        d(&ctx, job.req.heat);
+              mfgpu_heat_result hr;
+              d.run(hr);
+              int its = 0;
+              for (int s = 0; s < hr.n_steps; ++s)
+                its += hr.cg_its[s];
+              r.cg_iterations = its;
+              const size_t n  = d.op->m();
+              r.solution_norm = std::sqrt(vec_dot<double>(ctx, n, d.sol.as<double>(), d.sol.as<double>()));
+              r.n_dofs        = double(n);
+            }
+          else
+            {
+              mfgpu_solid_params p = job.req.solid;
+              p.caching            = job.caching.c_str();
+              SolidDriver         d(&ctx, p);
+              mfgpu_solid_result  sr;
+              d.run(sr);
+              r.cg_iterations     = int(sr.total_cg);
+              r.newton_iterations = 0;
+              for (int s = 0; s < sr.n_steps; ++s)
+                r.newton_iterations += sr.newton_its[s];
+              for (int k = 0; k < 3; ++k)
+                r.watch[k] = sr.watch_disp[sr.n_steps - 1][k];
+              const size_t n  = d.fine->m();
+              r.solution_norm = std::sqrt(vec_dot<double>(ctx, n, d.u.as<double>(), d.u.as<double>()));
+              r.n_dofs        = double(n);
+            }
+          r.status = MFGPU_OK;
+        }
+      catch (const Error &e)
+        {
+          r.status = e.code;
+          std::strncpy(r.message, e.what(), sizeof(r.message) - 1);
+        }
+      catch (const std::exception &e)
+        {
+          r.status = MFGPU_ERR_ARG;
+          std::strncpy(r.message, e.what(), sizeof(r.message) - 1);
+        }
+    }
+
+    long long
+    submit(const mfgpu_request &req)
+    {
+      std::unique_ptr<ServerJob> j(new ServerJob());
+      j->req = req;
+      if (req.kind == 1)
+        {
+          j->caching     = req.solid.caching ? req.solid.caching : "scalar_referential";
+          j->req.solid.caching = nullptr;
+        }
+      else if (req.kind != 0)
+        throw Error(ERR_ARG, "request kind must be 0 (heat) or 1 (solid)");
+      j->bytes    = estimate_request_bytes(req);
+      j->t_submit = clock_t_::now();
+      std::lock_guard<std::mutex> l(mu);
+      const long long id = next_id++;
+      j->id              = id;
+      queue.push_back(j.get());
+      jobs[id] = std::move(j);
+      cv_work.notify_one();
+      return id;
+    }
+
+    mfgpu_request_result
+    wait(long long id, bool remove)
+    {
+      std::unique_lock<std::mutex> l(mu);
+      auto                         it = jobs.find(id);
+      if (it == jobs.end())
+        throw Error(ERR_ARG, "unknown request id");
+      ServerJob *j = it->second.get();
+      cv_done.wait(l, [&] { return j->done; });
+      mfgpu_request_result r = j->res;
+      if (remove)
+        jobs.erase(it);
+      return r;
+    }
+  };
+} // namespace mfgpu
+
+using namespace mfgpu;
+
+struct mfgpu_server
+{
+  std::unique_ptr<Server> s;
+};
+
+extern "C"
+{
+  int
+  mfgpu_server_create(int device, int max_concurrent, double memory_fraction, mfgpu_server **server)
+  {
+    try
+      {
+        if (!server || max_concurrent < 1 || max_concurrent > 64 || !(memory_fraction > 0) ||
+            memory_fraction > 1)
+          throw Error(ERR_ARG, "server: invalid arguments");
+        auto *o = new mfgpu_server();
+        try
+          {
+            o->s.reset(new Server(device, max_concurrent, memory_fraction));
+          }
+        catch (...)
+          {
+            delete o;
+            throw;
+          }
+        *server = o;
+        return MFGPU_OK;
+      }
+    catch (const Error &e)
+      {
+        set_last_error(e.what());
+        return e.code;
+      }
+  }
+
+  int
+  mfgpu_server_submit(mfgpu_server *server, const mfgpu_request *request, long long *id)
+  {
+    try
+      {
+        if (!server || !request || !id)
+          throw Error(ERR_ARG, "server_submit: null argument");
+        *id = server->s->submit(*request);
+        return MFGPU_OK;
+      }
+    catch (const Error &e)
+      {
+        set_last_error(e.what());
+        return e.code;
+      }
+  }
+
+  int
+  mfgpu_server_wait(mfgpu_server *server, long long id, mfgpu_request_result *result)
+  {
+    try
+      {
+        if (!server || !result)
+          throw Error(ERR_ARG, "server_wait: null argument");
+        *result = server->s->wait(id, true);
+        return MFGPU_OK;
+      }
+    catch (const Error &e)
+      {
+        set_last_error(e.what());
+        return e.code;
+      }
+  }
+
+  int
+  mfgpu_server_stats(mfgpu_server *server, int *max_running, size_t *budget_bytes)
+  {
+    if (!server)
+      return MFGPU_ERR_ARG;
+    std::lock_guard<std::mutex> l(server->s->mu);
+    if (max_running)
+      *max_running = server->s->max_running;
+    if (budget_bytes)
+      *budget_bytes = server->s->budget;
+    return MFGPU_OK;
+  }
+
+  int
+  mfgpu_server_destroy(mfgpu_server *server)
+  {
+    delete server;
+    return MFGPU_OK;
+  }
+}

@@ -82,6 +82,18 @@ class HeatResult(C.Structure):
                 ("seconds", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("heat", HeatParams), ("solid", SolidParams)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("message", C.c_char * 128),
+                ("cg_iterations", C.c_int), ("newton_iterations", C.c_int),
+                ("watch", C.c_double * 3), ("solution_norm", C.c_double),
+                ("n_dofs", C.c_double), ("queue_seconds", C.c_double),
+                ("run_seconds", C.c_double), ("latency_seconds", C.c_double)]
+
+
 _lib = None
 
 
@@ -408,6 +420,46 @@ class Heat:
     def close(self):
         if self.h:
             lib().mfgpu_heat_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Concurrent solve server (mfgpu_server): submit heat / solid requests,
+    wait for their results."""
+
+    def __init__(self, device=0, max_concurrent=4, memory_fraction=0.8):
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_server_create(device, max_concurrent,
+                                         C.c_double(memory_fraction), C.byref(self.h)))
+        self._keep = {}
+
+    def submit(self, request):
+        rid = C.c_longlong()
+        _check(lib().mfgpu_server_submit(self.h, C.byref(request), C.byref(rid)))
+        self._keep[rid.value] = request
+        return rid.value
+
+    def wait(self, rid):
+        r = RequestResult()
+        _check(lib().mfgpu_server_wait(self.h, C.c_longlong(rid), C.byref(r)))
+        self._keep.pop(rid, None)
+        return r
+
+    def stats(self):
+        mr = C.c_int()
+        b = C.c_size_t()
+        _check(lib().mfgpu_server_stats(self.h, C.byref(mr), C.byref(b)))
+        return mr.value, b.value
+
+    def close(self):
+        if self.h:
+            lib().mfgpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -127,3 +127,55 @@ def n_dofs(spec, n_components):
     for d in range(3):
         n *= (spec["rep"][d] << spec["n_ref"]) * spec["degree"] + 1
     return n * n_components
+
+
+def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degrees=(1, 2, 3, 4),
+                     mg_precision=32, tol=1e-8):
+    """The serving mix: 60 % heat / 40 % neo-Hookean requests.  Heat: unit
+    cube with 8^3..(2^max_heat_ref)^3 cells (uniform random refinement 3..),
+    zero Dirichlet on x = 0, a seeded Gaussian source, one backward-Euler
+    step.  Solid: cantilever 8k x k x k cells, k in solid_k, clamped at x = 0,
+    a seeded traction of magnitude U(50, 150) on x = 8, one Newton-Newmark
+    step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG
+    (mg_precision=32) or the plain FP64 solver (mg_precision=64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    reqs = []
+    for i in range(n):
+        r = mfgpu.Request()
+        deg = int(rng.choice(degrees))
+        if rng.uniform() < 0.6:
+            r.kind = 0
+            nref = int(rng.integers(3, max_heat_ref + 1))
+            spec = unit_cube_heat(deg, nref)
+            hp = r.heat
+            hp.mesh = to_lib_mesh(mfgpu, spec)
+            hp.dt, hp.n_steps = 0.1, 1
+            hp.solver = mfgpu.solver_params("gmg", tol=tol, cheb_range=15.0, cheb_eig_its=10,
+                                            mg_precision=mg_precision,
+                                            coarse_fp64=(mg_precision == 32))
+            c, w, a = gaussian_source(int(rng.integers(1 << 30)))
+            hp.n_gauss = 8
+            for j in range(8):
+                for d in range(3):
+                    hp.g_center[j][d] = c[j, d]
+                hp.g_width[j] = w[j]
+                hp.g_amp[j] = a[j]
+        else:
+            r.kind = 1
+            k = int(rng.choice(solid_k))
+            nref = {2: 1, 4: 2, 8: 3, 16: 4}[k]
+            spec = cantilever(deg, nref)
+            sp = r.solid
+            sp.mesh = to_lib_mesh(mfgpu, spec)
+            sp.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+            sp.caching = b"referential_qp"
+            sp.solver = mfgpu.solver_params("gmg", tol=tol, mg_precision=mg_precision,
+                                            coarse_fp64=(mg_precision == 32))
+            sp.max_newton = 10
+            sp.tol_f, sp.tol_f_abs, sp.tol_u, sp.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+            sp.dt, sp.n_steps = 0.01, 1
+            sp.traction_id = TRACTION_ID
+            sp.traction[:] = [0.0, -float(rng.uniform(50, 150)), 0.0]
+            sp.watch[:] = [8.0, 0.5, 0.5]
+        reqs.append(r)
+    return reqs
