@@ -299,6 +299,9 @@ typedef struct mfgpu_heat_result
 int mfgpu_heat_create(mfgpu_context *ctx, const mfgpu_heat_params *p,
                       mfgpu_heat **h);
 int mfgpu_heat_run(mfgpu_heat *h, mfgpu_heat_result *r);
+/* one backward-Euler step (the first call sets up the initial state);
+ * returns the CG iterations of the step */
+int mfgpu_heat_step(mfgpu_heat *h, int *cg_iterations);
 int mfgpu_heat_solution(mfgpu_heat *h, const double **u);
 int mfgpu_heat_destroy(mfgpu_heat *h);
 

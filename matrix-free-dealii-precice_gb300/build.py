@@ -30,8 +30,11 @@ def _nvcc():
 
 
 def _sources_mtime():
-    return max(os.path.getmtime(os.path.join(CSRC, f)) for f in os.listdir(CSRC)) \
-        if os.path.isdir(CSRC) else 0.0
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    app = os.path.join(HERE, "app")
+    if os.path.isdir(app):
+        files += [os.path.join(app, f) for f in os.listdir(app)]
+    return max(os.path.getmtime(f) for f in files)
 
 
 def _header_mtime():
@@ -72,7 +75,27 @@ def build(force=False, verbose=False, jobs=None):
     tmp = LIB + ".tmp"
     run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
+    build_apps(verbose=verbose)
     return LIB
+
+
+APPS = ["solid", "heat"]
+
+
+def build_apps(verbose=False):
+    """The prm-driven executables `solid` and `heat` (host C++ over the
+    C-ABI, linked against libmfgpu.so with an $ORIGIN rpath)."""
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    for app in APPS:
+        out = os.path.join(HERE, app)
+        cmd = ["g++", "-O2", "-std=c++17", "-I", inc, os.path.join(HERE, "app", app + ".cc"),
+               "-L", HERE, "-lmfgpu", "-Wl,-rpath,$ORIGIN", "-o", out + ".tmp"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        os.replace(out + ".tmp", out)
 
 
 if __name__ == "__main__":

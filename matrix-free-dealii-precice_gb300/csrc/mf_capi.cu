@@ -626,6 +626,18 @@ extern "C"
   }
 
   int
+  mfgpu_heat_step(mfgpu_heat *h, int *cg_iterations)
+  {
+    return guarded([&] {
+      need(h, "heat");
+      const int its = h->d->step();
+      h->d->ctx->sync();
+      if (cg_iterations)
+        *cg_iterations = its;
+    });
+  }
+
+  int
   mfgpu_heat_solution(mfgpu_heat *h, const double **u)
   {
     return guarded([&] {

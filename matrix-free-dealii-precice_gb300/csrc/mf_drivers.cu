@@ -502,19 +502,12 @@ namespace mfgpu
   }
 
   void
-  HeatDriver::run(mfgpu_heat_result &res)
+  HeatDriver::start()
   {
-    auto         t0 = std::chrono::steady_clock::now();
-    const size_t n  = op->m();
-    std::memset(&res, 0, sizeof(res));
-    if (P.n_steps > 64)
-      throw Error(ERR_ARG, "at most 64 time steps per run");
-    res.n_steps = P.n_steps;
-    const LevelGeom &G = op->geom;
-    std::vector<double> h;
+    const size_t n = op->m();
     if (P.analytic)
       {
-        h.resize(n);
+        std::vector<double> h(n);
         for (size_t g = 0; g < n; ++g)
           {
             double x[3];
@@ -534,7 +527,6 @@ namespace mfgpu
       }
     if (P.solver.preconditioner == 1)
       op->compute_diagonal();
-    SourceDesc src;
     std::memset(&src, 0, sizeof(src));
     src.constant = P.analytic ? P.beta - 2 - 2 * P.alpha : 0.0;
     src.n_gauss  = P.analytic ? 0 : P.n_gauss;
@@ -545,73 +537,95 @@ namespace mfgpu
         src.width[i] = P.g_width[i];
         src.amp[i]   = P.g_amp[i];
       }
-    double t = 0;
-    for (int step = 0; step < P.n_steps; ++step)
+    t       = 0;
+    step_no = 0;
+    started = true;
+  }
+
+  int
+  HeatDriver::step()
+  {
+    if (!started)
+      start();
+    const size_t     n = op->m();
+    const LevelGeom &G = op->geom;
+    t += P.dt;
+    ++step_no;
+    // inhomogeneous Dirichlet values on the constrained nodes at time t
+    MF_CK(cudaMemsetAsync(uD.ptr, 0, n * sizeof(double), ctx->stream));
+    if (P.analytic)
       {
-        t += P.dt;
-        // inhomogeneous Dirichlet values on the constrained nodes at time t
-        MF_CK(cudaMemsetAsync(uD.ptr, 0, n * sizeof(double), ctx->stream));
-        if (P.analytic)
+        std::vector<double> hd(n, 0.0);
+        for (size_t g = 0; g < n; ++g)
           {
-            std::vector<double> hd(n, 0.0);
-            for (size_t g = 0; g < n; ++g)
+            int    ii[3];
+            size_t gg = g;
+            ii[0]     = int(gg % G.Nn[0]);
+            gg /= G.Nn[0];
+            ii[1] = int(gg % G.Nn[1]);
+            ii[2] = int(gg / G.Nn[1]);
+            if (node_mask(G.face_mask, G.Nn, ii[0], ii[1], ii[2]) & 1u)
               {
-                int ii[3];
-                size_t gg = g;
-                ii[0] = int(gg % G.Nn[0]);
-                gg /= G.Nn[0];
-                ii[1] = int(gg % G.Nn[1]);
-                ii[2] = int(gg / G.Nn[1]);
-                if (node_mask(G.face_mask, G.Nn, ii[0], ii[1], ii[2]) & 1u)
-                  {
-                    double x[3];
-                    node_x(g, x);
-                    hd[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1] + P.beta * t;
-                  }
-              }
-            MF_CK(cudaMemcpyAsync(uD.ptr, hd.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-            ctx->sync();
-          }
-        // rhs = -A_unconstrained uD + int (u_old + dt f) v
-        op_u->vmult(rhs.ptr, uD.ptr);
-        vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
-        MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
-                                ctx->stream));
-        count_launch();
-        const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
-        FineOp A;
-        A.op = op.get();
-        CGStats st;
-        if (P.solver.preconditioner == 2)
-          {
-            if (lprec == 32)
-              {
-                mgf->setup(15., 5, 10, int(lops[0]->m()));
-                st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
-              }
-            else
-              {
-                mgd->setup(15., 5, 10, int(lops[0]->m()));
-                st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+                double x[3];
+                node_x(g, x);
+                hd[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1] + P.beta * t;
               }
           }
-        else if (P.solver.preconditioner == 1)
+        MF_CK(cudaMemcpyAsync(uD.ptr, hd.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->sync();
+      }
+    // rhs = -A_unconstrained uD + int (u_old + dt f) v
+    op_u->vmult(rhs.ptr, uD.ptr);
+    vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
+    MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
+                            ctx->stream));
+    count_launch();
+    const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+    FineOp A;
+    A.op = op.get();
+    CGStats st;
+    if (P.solver.preconditioner == 2)
+      {
+        if (lprec == 32)
           {
-            JacobiPre64 J;
-            J.ctx   = ctx;
-            J.A     = op.get();
-            J.omega = 0.7;
-            st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n));
+            mgf->setup(15., 5, 10, int(lops[0]->m()));
+            st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
           }
         else
-          st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
-        if (!st.converged)
-          throw Error(ERR_NOT_CONVERGED, "CG did not converge");
-        res.cg_its[step] = st.its;
-        constrained_op<double>(*ctx, G, 1, 2, nullptr, du.as<double>());
-        vec_axpbyz<double>(*ctx, n, 1.0, uD.as<double>(), 1.0, du.as<double>(), sol.as<double>());
-        vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
+          {
+            mgd->setup(15., 5, 10, int(lops[0]->m()));
+            st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+          }
       }
+    else if (P.solver.preconditioner == 1)
+      {
+        JacobiPre64 J;
+        J.ctx   = ctx;
+        J.A     = op.get();
+        J.omega = 0.7;
+        st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n));
+      }
+    else
+      st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
+    if (!st.converged)
+      throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+    constrained_op<double>(*ctx, G, 1, 2, nullptr, du.as<double>());
+    vec_axpbyz<double>(*ctx, n, 1.0, uD.as<double>(), 1.0, du.as<double>(), sol.as<double>());
+    vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
+    return st.its;
+  }
+
+  void
+  HeatDriver::run(mfgpu_heat_result &res)
+  {
+    auto t0 = std::chrono::steady_clock::now();
+    std::memset(&res, 0, sizeof(res));
+    if (P.n_steps > 64)
+      throw Error(ERR_ARG, "at most 64 time steps per run");
+    res.n_steps = P.n_steps;
+    start();
+    for (int s = 0; s < P.n_steps; ++s)
+      res.cg_its[s] = step();
     ctx->sync();
     res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }

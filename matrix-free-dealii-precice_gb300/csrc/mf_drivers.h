@@ -48,8 +48,14 @@ namespace mfgpu
     std::unique_ptr<Multigrid<float>>          mgf;
     std::unique_ptr<Multigrid<double>>         mgd;
     DevBuf                                     sol, sol_old, rhs, du, uD;
+    bool                                       started = false;
+    int                                        step_no = 0;
+    double                                     t       = 0;
+    SourceDesc                                 src{};
     HeatDriver(Context *c, const mfgpu_heat_params &p);
     void node_x(size_t g, double *x) const;
+    void start();          // initial condition, diagonals
+    int  step();           // one backward-Euler step; returns CG iterations
     void run(mfgpu_heat_result &res);
   };
 } // namespace mfgpu
