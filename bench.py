@@ -59,6 +59,24 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device=None):
+    """Max of a per-rank time over all replicas (identity on one rank).
+    Every rank gets the max, whichever process-group backend is initialised."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, seconds_max, world):
+    """Whole-job throughput of `world` independent replicas that each
+    processed `units_per_rank` units, timed by the slowest replica."""
+    return world * units_per_rank / seconds_max
+
+
 def algorithmic_bytes(n_dofs, n_cells, s=8, k_state=1):
     """B_alg = s*N_dof*(2 + k_state) + 4*s*N_cells (src read, dst write,
     linearisation state read, per-cell affine geometry)."""
@@ -493,10 +511,8 @@ def main():
     kms = [s.elapsed_time(e) for s, e in zip(kstarts, kends)]
     ms_step = sum(ms) / K
     k_ms = sum(kms) / K
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_step, world, dev)
+    k_ms = max_over_ranks(k_ms, world, dev)
 
     # end to end through the C-ABI with host buffers (pinned)
     src_pin = torch.from_numpy(src_h).pin_memory()
@@ -510,10 +526,7 @@ def main():
         op.vmult_host(dst_np, src_np)
     barrier()
     e2e_s = (time.perf_counter() - t0) / K
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world, dev)
 
     # the same operator in native FP64 arithmetic, for comparison
     native = None
@@ -521,7 +534,8 @@ def main():
         op.set_fp64_emulation(False)
         op.cache()
         t_nat = _timed_vmults(torch, op, dst, src, flush, stream, max(5, K // 4))
-        native = {"value": world * n / t_nat, "ms_per_step": t_nat * 1e3}
+        t_nat = max_over_ranks(t_nat, world, dev)
+        native = {"value": replica_throughput(n, t_nat, world), "ms_per_step": t_nat * 1e3}
         op.set_fp64_emulation(True)
         op.cache()
     ctx.synchronize()
@@ -530,7 +544,7 @@ def main():
     achieved = b_alg / (k_ms * 1e-3) / 1e9
     f_alg = algorithmic_flops(n_cells, 5)
     line = {
-        "metric": METRIC, "value": world * n / (ms_step * 1e-3), "unit": UNIT,
+        "metric": METRIC, "value": replica_throughput(n, ms_step * 1e-3, world), "unit": UNIT,
         "n_gpus": world, "steps": K, "warmup": max(args.warmup, 3),
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "df64" if args.arith == "df64" else "f64",
@@ -546,7 +560,7 @@ def main():
                                  "double-float (FP32 pipe), parity 1e-12 vs FP64",
                    "l2": "flushed (512 MB write) before every timed application",
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": world * n / e2e_s, "unit": UNIT,
+        "e2e": {"value": replica_throughput(n, e2e_s, world), "unit": UNIT,
                 "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profile_traffic(),
@@ -559,7 +573,7 @@ def main():
         "gpu_launches": launches,
         "wall_ms_per_step": t_wall / K * 1e3,
     }
-    if not args.no_extras:
+    if not args.no_extras and world == 1:  # secondary measurements: one GPU only
         extras = {}
         for key, fn in (("time_to_solve_1e-8", lambda: extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev)),
                         ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
