@@ -527,6 +527,15 @@ def main():
     barrier()
     e2e_s = (time.perf_counter() - t0) / K
     e2e_s = max_over_ranks(e2e_s, world, dev)
+    # the same without the z-slab overlap of copies and cells
+    op.set_host_chunks(1)
+    for _ in range(2):
+        op.vmult_host(dst_np, src_np)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        op.vmult_host(dst_np, src_np)
+    e2e_serial_s = max_over_ranks((time.perf_counter() - t0) / K, world, dev)
+    op.set_host_chunks(0)
 
     # the same operator in native FP64 arithmetic, for comparison
     native = None
@@ -561,7 +570,11 @@ def main():
                    "l2": "flushed (512 MB write) before every timed application",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": replica_throughput(n, e2e_s, world), "unit": UNIT,
-                "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
+                "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                "ms_per_step": e2e_s * 1e3,
+                "overlap": "4 z-slabs: copy-in, cell launches and copy-out overlapped on 4 streams",
+                "no_overlap": {"value": replica_throughput(n, e2e_serial_s, world),
+                               "ms_per_step": e2e_serial_s * 1e3}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profile_traffic(),
                      "peak_kind": peak_kind,

@@ -152,9 +152,16 @@ int mfgpu_operator_vmult(mfgpu_operator *op, void *dst, const void *src);
 int mfgpu_operator_vmult_add(mfgpu_operator *op, void *dst, const void *src);
 int mfgpu_operator_Tvmult(mfgpu_operator *op, void *dst, const void *src);
 int mfgpu_operator_Tvmult_add(mfgpu_operator *op, void *dst, const void *src);
-/* vmult with HOST buffers: copies src in, applies, copies dst out */
+/* vmult with HOST buffers (pinned for overlap): the source is copied in
+ * z-slabs, the cells of each slab start when their nodes have arrived and
+ * each slab of the result is copied out when the cells touching it are
+ * done; returns when dst_host holds the result */
 int mfgpu_operator_vmult_host(mfgpu_operator *op, void *dst_host,
                               const void *src_host);
+/* number of z-slabs of the host-buffer vmult: 0 = from the vector size
+ * (4 from 4 MB up), 1 = copy in, apply, copy out without overlap, <= 8.
+ * No counterpart in the reference (its vectors live in host memory). */
+int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
 /* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
 int mfgpu_operator_compute_diagonal(mfgpu_operator *op);
 /* get_matrix_diagonal_inverse: device pointer owned by the operator */
@@ -227,6 +234,7 @@ typedef struct mfgpu_solver_params
   int    mg_precision;    /* 32: FP32 level operators, 64: all-FP64 V-cycle */
   int    coarse_fp64;     /* level-0 Chebyshev solve in FP64                */
   int    fp64_emulation;  /* FP64 operators in double-float arithmetic      */
+  int    cuda_graphs;     /* replay the V-cycle as a CUDA graph              */
 } mfgpu_solver_params;
 
 typedef struct mfgpu_solid_params

@@ -149,6 +149,7 @@ main(int argc, char *argv[])
       P.solver.mg_precision    = prm.get_int("GPU", "MG precision");
       P.solver.coarse_fp64     = prm.get_bool("GPU", "FP64 coarse solve");
       P.solver.fp64_emulation  = prm.get_bool("GPU", "FP64 emulation");
+      P.solver.cuda_graphs     = prm.get_bool("GPU", "CUDA graphs");
       const double tick        = prm.get_double("Output", "Output tick");
 
       mfgpu_context *ctx = nullptr;

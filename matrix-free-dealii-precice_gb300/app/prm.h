@@ -169,6 +169,7 @@ namespace mfapp
     p.declare("GPU", "MG precision", "32");
     p.declare("GPU", "FP64 coarse solve", "false");
     p.declare("GPU", "FP64 emulation", "false");
+    p.declare("GPU", "CUDA graphs", "true");
   }
 
   inline void

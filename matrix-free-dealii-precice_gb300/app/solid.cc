@@ -84,6 +84,7 @@ main(int argc, char *argv[])
       P.solver.mg_precision    = prm.get_int("GPU", "MG precision");
       P.solver.coarse_fp64     = prm.get_bool("GPU", "FP64 coarse solve");
       P.solver.fp64_emulation  = prm.get_bool("GPU", "FP64 emulation");
+      P.solver.cuda_graphs     = prm.get_bool("GPU", "CUDA graphs");
       P.max_newton             = prm.get_int("Nonlinear solver", "Max iterations Newton-Raphson");
       P.tol_f                  = prm.get_double("Nonlinear solver", "Tolerance force");
       P.tol_f_abs              = prm.get_double("Nonlinear solver", "Absolute tolerance force");

@@ -20,6 +20,7 @@ struct mfgpu_operator
   std::unique_ptr<Operator> op;
   mfgpu_context            *ctx;
   DevBuf                    hsrc, hdst; // device staging for the host-buffer vmult
+  HostPipe                  pipe;       // streams of the overlapped host-buffer vmult
 };
 
 struct mfgpu_solid
@@ -347,11 +348,18 @@ extern "C"
           op->hsrc.alloc(bytes);
           op->hdst.alloc(bytes);
         }
-      cudaStream_t s = o->ctx->stream;
-      MF_CK(cudaMemcpyAsync(op->hsrc.ptr, src_host, bytes, cudaMemcpyHostToDevice, s));
-      o->vmult(op->hdst.ptr, op->hsrc.ptr);
-      MF_CK(cudaMemcpyAsync(dst_host, op->hdst.ptr, bytes, cudaMemcpyDeviceToHost, s));
-      MF_CK(cudaStreamSynchronize(s));
+      o->vmult_host(dst_host, src_host, op->hdst.ptr, op->hsrc.ptr, op->pipe);
+    });
+  }
+
+  int
+  mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks)
+  {
+    return guarded([&] {
+      need(op, "op");
+      if (n_chunks < 0 || n_chunks > HostPipe::MAXC)
+        throw Error(ERR_ARG, "n_chunks must be in [0, 8]");
+      op->pipe.chunks = n_chunks;
     });
   }
 

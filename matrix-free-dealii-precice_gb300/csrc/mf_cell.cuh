@@ -212,8 +212,19 @@ namespace mfgpu
            N == 3 ? 32 :
            N == 4 ? 8 :
            N == 5 ? 5 :
-           N == 6 ? (NC == 1 ? 8 : (EVAL_U ? 4 : 7)) :
-                    (NC == 1 ? 5 : (EVAL_U ? (sizeof(TS) == 8 ? 3 : 5) : 5));
+           N == 6 ? (NC == 1 ? 8 : (EVAL_U ? 4 : (sizeof(TS) == 8 ? 5 : 7))) :
+                    (NC == 1 ? 5 : (sizeof(TS) == 8 ? 3 : 5));
+  }
+
+  // shared memory per cell of the operator-application kernel (elements of
+  // T): NC*(value + 3 gradients); the 1D sweeps use the gradient slots of
+  // the component being evaluated or integrated as their scratch.  With
+  // EVAL_U, 3*NC gradients of the linearisation + one scratch array.
+  template <int N, int NC, bool EVAL_U>
+  __host__ __device__ constexpr int
+  apply_smem_per_cell()
+  {
+    return (NC * 4 + (EVAL_U ? 3 * NC + 1 : 0)) * N * N * N;
   }
 
   // shared memory per cell (in elements of T): NC*(value + 3 gradients)
@@ -370,7 +381,7 @@ namespace mfgpu
     constexpr int N2  = N * N;
     constexpr int N3  = N * N * N;
     constexpr int CPB = apply_cells_per_block<N, NC, TS, QOp::eval_u>();
-    constexpr int SPC = smem_per_cell<N, NC, QOp::eval_u>();
+    constexpr int SPC = apply_smem_per_cell<N, NC, QOp::eval_u>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
 
@@ -378,12 +389,11 @@ namespace mfgpu
     const int      l      = threadIdx.x - lc * N2;
     const int      a      = l % N;
     const int      b      = l / N;
-    const unsigned cell   = blockIdx.x * CPB + lc;
-    const bool     active = cell < g.n_cells;
+    const unsigned cell   = g.cell_begin + blockIdx.x * CPB + lc;
+    const bool     active = cell < g.cell_end;
     T             *cb     = sm + lc * SPC;
-    T             *T0     = cb + NC * 4 * N3;
-    T             *T1     = T0 + N3;
-    T             *GU     = T1 + N3; // 3*NC*N3 if eval_u
+    T             *GU     = cb + NC * 4 * N3; // 3*NC*N3 if eval_u
+    T             *XU     = GU + 3 * NC * N3; // N3 scratch if eval_u
 
     const unsigned cc  = active ? cell : 0u;
     const int      cx  = int(cc % unsigned(g.C[0]));
@@ -413,9 +423,10 @@ namespace mfgpu
               }
             col[k] = val;
           }
+        // sweep scratch: the y and z gradient slots of this component
         T *V = cb + c * 4 * N3;
         evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
-                          V + 3 * N3, T0, T1, a, b, true);
+                          V + 3 * N3, V + 2 * N3, V + 3 * N3, a, b, true);
       }
     if constexpr (QOp::eval_u)
       {
@@ -427,11 +438,12 @@ namespace mfgpu
 #pragma unroll
             for (int k = 0; k < N; ++k)
               col[k] = active ? op.ucell[(size_t(cc) * NC + c) * N3 + a + b * N + k * N2] : zero<T>();
-            // the values go to T1 (scratch); GU + c*3*N3 holds the gradients
+            // the values go to XU (scratch); GU + c*3*N3 holds the gradients
+            // and serves as the sweep scratch
             T *Gc = GU + c * 3 * N3;
             __syncthreads();
-            evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, T1, Gc, Gc + N3,
-                              Gc + 2 * N3, T0, T1, a, b, false);
+            evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, XU, Gc, Gc + N3,
+                              Gc + 2 * N3, Gc + N3, Gc + 2 * N3, a, b, false);
           }
       }
     __syncthreads();
@@ -484,8 +496,9 @@ namespace mfgpu
       {
         T *V = cb + c * 4 * N3;
         T  col[N];
+        // sweep scratch: the x and y gradient slots (consumed by then)
         integrate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + N3, V + 2 * N3,
-                           V + 3 * N3, T0, T1, a, b, true, true, col);
+                           V + 3 * N3, V + N3, V + 2 * N3, a, b, true, true, col);
         if (active)
           {
 #pragma unroll

@@ -66,6 +66,7 @@ namespace mfgpu
     int      Nn[3];
     int      p;
     unsigned n_cells;
+    unsigned cell_begin, cell_end; // cells [begin, end) of one application launch
     size_t   n_nodes;
     T        inv_h[3];
     T        vol; // h0*h1*h2
@@ -98,8 +99,10 @@ namespace mfgpu
         c.inv_h[d] = conv_host<T>(1.0 / g.h[d]);
       }
     c.p       = g.p;
-    c.n_cells = unsigned(g.n_cells);
-    c.n_nodes = g.n_nodes;
+    c.n_cells    = unsigned(g.n_cells);
+    c.cell_begin = 0;
+    c.cell_end   = unsigned(g.n_cells);
+    c.n_nodes    = g.n_nodes;
     c.vol     = conv_host<T>(g.h[0] * g.h[1] * g.h[2]);
     for (int f = 0; f < 6; ++f)
       c.face_mask[f] = g.face_mask[f];

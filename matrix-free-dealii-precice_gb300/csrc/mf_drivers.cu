@@ -165,7 +165,8 @@ namespace mfgpu
                 mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
                                                        lops[l]->geom, 3, lprec));
             }
-          mg.coarse64 = coarse64.get();
+          mg.coarse64   = coarse64.get();
+          mg.use_graphs = P.solver.cuda_graphs != 0;
         };
         if (lprec == 32)
           {
@@ -469,7 +470,8 @@ namespace mfgpu
                 mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
                                                        lops[l]->geom, 1, lprec));
             }
-          mg.coarse64 = coarse64.get();
+          mg.coarse64   = coarse64.get();
+          mg.use_graphs = P.solver.cuda_graphs != 0;
         };
         if (lprec == 32)
           {

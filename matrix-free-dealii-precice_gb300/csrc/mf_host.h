@@ -120,6 +120,39 @@ namespace mfgpu
   void    read_scalars(Context &c, int n); // D2H of the first n slots (sync)
 
   // ---------------------------------------------------------------------
+  // streams and events of the overlapped host-buffer vmult (created on
+  // first use, on the operator's device)
+  // ---------------------------------------------------------------------
+  struct HostPipe
+  {
+    static constexpr int MAXC = 8;
+    cudaStream_t         s_in = nullptr, s_out = nullptr, s_comp[2] = {nullptr, nullptr};
+    cudaEvent_t          e_zero = nullptr, e_con = nullptr, e_done = nullptr;
+    cudaEvent_t          e_in[MAXC] = {}, e_comp[MAXC] = {};
+    int                  chunks = 0; // 0: chosen from the vector size
+    // what a captured graph was built for: buffers, slab count, operator state
+    struct Key
+    {
+      void       *dst_h = nullptr, *dst_d = nullptr;
+      const void *src_h = nullptr, *src_d = nullptr;
+      int         n     = 0;
+      size_t      state = 0;
+      bool
+      operator==(const Key &o) const
+      {
+        return dst_h == o.dst_h && src_h == o.src_h && dst_d == o.dst_d && src_d == o.src_d &&
+               n == o.n && state == o.state && n > 0;
+      }
+    };
+    Key             last, g;
+    cudaGraphExec_t gexec      = nullptr;
+    long long       g_launches = 0;
+    void            init();
+    void            drop_graph();
+    ~HostPipe();
+  };
+
+  // ---------------------------------------------------------------------
   // operators
   // ---------------------------------------------------------------------
   struct Operator
@@ -148,12 +181,25 @@ namespace mfgpu
       return precision == 32 ? 4 : 8;
     }
     // dst += A src (cell part, constrained rows untouched)
-    virtual void apply_cells(void *dst, const void *src) = 0;
+    void apply_cells(void *dst, const void *src) { apply_cells_range(dst, src, 0, 0, ctx->stream); }
+    // the same for the cells [c0, c1) (all cells if c1 <= c0) on stream s
+    virtual void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) = 0;
     virtual void compute_diagonal() = 0;
     virtual size_t memory_consumption() const { return 0; }
     virtual void clear() {}
     void vmult(void *dst, const void *src);
     void vmult_add(void *dst, const void *src);
+    // dst_h = A src_h for host vectors, through the device buffers dst_d /
+    // src_d: the source is copied in z-slabs, each slab of cells starts as
+    // soon as its nodes have arrived, and each slab of the result is copied
+    // back as soon as the cells touching it are done.  Synchronous.
+    void vmult_host(void *dst_h, const void *src_h, void *dst_d, void *src_d, HostPipe &p);
+    // everything a vmult's kernels take as parameters (a captured graph of
+    // the host-buffer vmult is replayed only while this is unchanged)
+    virtual size_t vmult_state() const;
+  private:
+    void enqueue_vmult_host(void *dst_h, const void *src_h, void *dst_d, void *src_d, HostPipe &p, int n);
+  public:
     void finish_diagonal(); // constrained -> 1, invert
   };
 
@@ -161,8 +207,9 @@ namespace mfgpu
   {
     double delta_t     = 0;
     double coefficient = 1;
-    void   apply_cells(void *dst, const void *src) override;
+    void   apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) override;
     void   compute_diagonal() override;
+    size_t vmult_state() const override;
   };
 
   struct NHOperator : Operator
@@ -175,8 +222,9 @@ namespace mfgpu
     DevBuf      cache;
     DevBuf      ucell;
     bool        cached = false;
-    void   apply_cells(void *dst, const void *src) override;
+    void   apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) override;
     void   compute_diagonal() override;
+    size_t vmult_state() const override;
     void   do_cache();
     size_t memory_consumption() const override { return cache.bytes + ucell.bytes; }
     void   clear() override;

@@ -3,6 +3,9 @@
 // parallel.
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 #include "mf_launch.h"
 #include "mf_setup.cuh"
@@ -60,14 +63,41 @@ namespace mfgpu
       return r;
     }
 
+    // restrict an application launch to the cells [a.cell_begin, a.cell_end)
+    template <typename T>
+    CellGeom<T>
+    apply_range(CellGeom<T> c, const ApplyArgs &a)
+    {
+      if (a.cell_end > a.cell_begin)
+        {
+          c.cell_begin = unsigned(a.cell_begin);
+          c.cell_end   = unsigned(a.cell_end < c.n_cells ? a.cell_end : c.n_cells);
+        }
+      return c;
+    }
+
+    // raise a kernel's dynamic shared memory limit once per (kernel,
+    // device, size): the launch path then makes no attribute call
     template <typename K>
     cudaError_t
     prepare(K kernel, size_t smem)
     {
-      if (smem > 48 * 1024)
-        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(smem));
-      return cudaSuccess;
+      if (smem <= 48 * 1024)
+        return cudaSuccess;
+      static std::mutex                                    mu;
+      static std::set<std::tuple<const void *, int, size_t>> done;
+      int                                                  dev = 0;
+      cudaError_t                                          e   = cudaGetDevice(&dev);
+      if (e != cudaSuccess)
+        return e;
+      const auto                  key = std::make_tuple(reinterpret_cast<const void *>(kernel), dev, smem);
+      std::lock_guard<std::mutex> l(mu);
+      if (done.count(key))
+        return cudaSuccess;
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e == cudaSuccess)
+        done.insert(key);
+      return e;
     }
 
     template <int N, typename TS, typename T, int NC, class Op, bool CON>
@@ -76,12 +106,14 @@ namespace mfgpu
               const TS *src, TS *dst, cudaStream_t s)
     {
       constexpr int CPB  = apply_cells_per_block<N, NC, TS, Op::eval_u>();
-      const size_t  smem = size_t(CPB) * smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
+      const size_t  smem = size_t(CPB) * apply_smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
       auto          k    = cell_apply_kernel<N, TS, T, NC, Op, CON>;
       cudaError_t   e    = prepare(k, smem);
       if (e != cudaSuccess)
         return e;
-      const unsigned grid = (cg.n_cells + CPB - 1) / CPB;
+      const unsigned grid = (cg.cell_end - cg.cell_begin + CPB - 1) / CPB;
+      if (grid == 0)
+        return cudaSuccess;
       k<<<grid, CPB * N * N, smem, s>>>(sh, cg, op, src, dst);
       return cudaGetLastError();
     }
@@ -102,7 +134,7 @@ namespace mfgpu
                cudaStream_t s)
   {
     const ShapeA<N, T>   sh  = make_shape_apply<N, T>(b, g);
-    const CellGeom<T>    cg  = make_cell_geom<T>(g);
+    const CellGeom<T>    cg  = apply_range(make_cell_geom<T>(g), a);
     const T             *src = static_cast<const T *>(a.src);
     T                   *dst = static_cast<T *>(a.dst);
     constexpr int        N3  = N * N * N;
@@ -336,7 +368,7 @@ namespace mfgpu
                   cudaStream_t s)
   {
     const ShapeA<N, df64>   sh  = make_shape_apply<N, df64>(b, g);
-    const CellGeom<df64>    cg  = make_cell_geom<df64>(g);
+    const CellGeom<df64>    cg  = apply_range(make_cell_geom<df64>(g), a);
     const double           *src = static_cast<const double *>(a.src);
     double                 *dst = static_cast<double *>(a.dst);
     constexpr int           N3  = N * N * N;

@@ -41,6 +41,7 @@ namespace mfgpu
     const void *ucell;
     const void *src;
     void       *dst;
+    size_t      cell_begin = 0, cell_end = 0; // cell range; empty = all cells
   };
 
   template <int N, typename T>
@@ -89,7 +90,4 @@ namespace mfgpu
   cudaError_t launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
                               const SourceDesc &f, const double *u_old,
                               double *rhs, cudaStream_t s);
-
-  // number of cells per block / dynamic shared memory (for reporting)
-  int apply_cells_per_block(int N, int nc, int tsize);
 } // namespace mfgpu

@@ -1,8 +1,10 @@
 // Host side of the operators: basis data, context, vector kernels, the
 // heat and neo-Hookean operators (vmult, compute_diagonal, cache) and the
 // multigrid transfer.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <string>
 
@@ -549,6 +551,238 @@ namespace mfgpu
   }
 
   void
+  HostPipe::init()
+  {
+    if (s_in)
+      return;
+    MF_CK(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
+    MF_CK(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+    for (auto &s : s_comp)
+      MF_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&e_zero, &e_con, &e_done})
+      MF_CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (int k = 0; k < MAXC; ++k)
+      {
+        MF_CK(cudaEventCreateWithFlags(&e_in[k], cudaEventDisableTiming));
+        MF_CK(cudaEventCreateWithFlags(&e_comp[k], cudaEventDisableTiming));
+      }
+  }
+
+  void
+  HostPipe::drop_graph()
+  {
+    if (gexec)
+      cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    g     = Key{};
+  }
+
+  HostPipe::~HostPipe()
+  {
+    drop_graph();
+    if (!s_in)
+      return;
+    for (cudaStream_t s : {s_in, s_out, s_comp[0], s_comp[1]})
+      {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+    for (cudaEvent_t e : {e_zero, e_con, e_done})
+      cudaEventDestroy(e);
+    for (int k = 0; k < MAXC; ++k)
+      {
+        cudaEventDestroy(e_in[k]);
+        cudaEventDestroy(e_comp[k]);
+      }
+  }
+
+  static size_t
+  hmix(size_t h, size_t v)
+  {
+    return h ^ (v + size_t(0x9e3779b97f4a7c15ULL) + (h << 6) + (h >> 2));
+  }
+
+  static size_t
+  hbits(double d)
+  {
+    uint64_t u;
+    std::memcpy(&u, &d, sizeof(u));
+    return size_t(u);
+  }
+
+  size_t
+  Operator::vmult_state() const
+  {
+    size_t h = hmix(size_t(precision), size_t(arith));
+    h        = hmix(h, size_t(constrained));
+    return hmix(h, size_t(nc));
+  }
+
+  size_t
+  HeatOperator::vmult_state() const
+  {
+    return hmix(hmix(Operator::vmult_state(), hbits(delta_t)), hbits(coefficient));
+  }
+
+  size_t
+  NHOperator::vmult_state() const
+  {
+    size_t h = hmix(Operator::vmult_state(), size_t(variant) * 2 + size_t(formulation));
+    h        = hmix(h, size_t(reinterpret_cast<uintptr_t>(cache.ptr)));
+    h        = hmix(h, size_t(reinterpret_cast<uintptr_t>(ucell.ptr)));
+    for (double v : {mat.mu, mat.lambda, mat.rho_alpha, mat.kappa, mat.c_1})
+      h = hmix(h, hbits(v));
+    return hmix(h, size_t(cached));
+  }
+
+  static bool
+  host_pinned(const void *p)
+  {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+      {
+        cudaGetLastError();
+        return false;
+      }
+    return a.type == cudaMemoryTypeHost;
+  }
+
+  void
+  Operator::enqueue_vmult_host(void *dst_h, const void *src_h, void *dst_d, void *src_d,
+                               HostPipe &p, int n)
+  {
+    const size_t es    = elem_size();
+    const size_t bytes = m() * es;
+    const int    Cz    = geom.C[2];
+    cudaStream_t s0    = ctx->stream;
+    const size_t plane = size_t(geom.Nn[0]) * size_t(geom.Nn[1]); // nodes of one z-plane
+    const size_t layer = size_t(geom.C[0]) * size_t(geom.C[1]);   // cells of one z-layer
+    const size_t pitch = geom.n_nodes * es;                        // component stride
+    const int    deg   = geom.p;
+    int          zc[HostPipe::MAXC + 1];
+    for (int k = 0; k <= n; ++k)
+      zc[k] = int((long long)k * Cz / n);
+    // node planes of chunk k: [zc[k]*p, zc[k+1]*p), the last one up to the top plane
+    auto plane_lo = [&](int k) { return size_t(zc[k]) * deg; };
+    auto plane_hi = [&](int k) { return k == n - 1 ? size_t(geom.Nn[2]) : size_t(zc[k + 1]) * deg; };
+    char       *dd = static_cast<char *>(dst_d);
+    char       *sd = static_cast<char *>(src_d);
+    char       *dh = static_cast<char *>(dst_h);
+    const char *sh = static_cast<const char *>(src_h);
+
+    MF_CK(cudaMemsetAsync(dst_d, 0, bytes, s0));
+    MF_CK(cudaEventRecord(p.e_zero, s0));
+    // every stream starts after the memset (this is also the fork of a capture)
+    for (cudaStream_t s : {p.s_in, p.s_comp[0], p.s_comp[1], p.s_out})
+      MF_CK(cudaStreamWaitEvent(s, p.e_zero, 0));
+    for (int k = 0; k < n; ++k)
+      {
+        const size_t off = plane_lo(k) * plane * es, w = (plane_hi(k) - plane_lo(k)) * plane * es;
+        MF_CK(cudaMemcpy2DAsync(sd + off, pitch, sh + off, pitch, w, nc, cudaMemcpyHostToDevice, p.s_in));
+        MF_CK(cudaEventRecord(p.e_in[k], p.s_in));
+      }
+    for (int k = 0; k < n; ++k)
+      {
+        // the cells of z-slab k read the node planes up to the first plane of chunk k+1
+        cudaStream_t s = p.s_comp[k & 1];
+        MF_CK(cudaStreamWaitEvent(s, p.e_in[std::min(k + 1, n - 1)], 0));
+        apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s);
+        MF_CK(cudaEventRecord(p.e_comp[k], s));
+      }
+    if (constrained)
+      {
+        MF_CK(cudaStreamWaitEvent(s0, p.e_in[n - 1], 0));
+        if (precision == 32)
+          constrained_op<float>(*ctx, geom, nc, 0, (const float *)src_d, (float *)dst_d);
+        else
+          constrained_op<double>(*ctx, geom, nc, 0, (const double *)src_d, (double *)dst_d);
+      }
+    MF_CK(cudaEventRecord(p.e_con, s0));
+    for (int k = 0; k < n; ++k)
+      {
+        // planes of chunk k receive contributions from z-slabs k-1 and k
+        MF_CK(cudaStreamWaitEvent(p.s_out, p.e_comp[k], 0));
+        if (k > 0)
+          MF_CK(cudaStreamWaitEvent(p.s_out, p.e_comp[k - 1], 0));
+        MF_CK(cudaStreamWaitEvent(p.s_out, p.e_con, 0));
+        const size_t off = plane_lo(k) * plane * es, w = (plane_hi(k) - plane_lo(k)) * plane * es;
+        MF_CK(cudaMemcpy2DAsync(dh + off, pitch, dd + off, pitch, w, nc, cudaMemcpyDeviceToHost, p.s_out));
+      }
+    // join: every stream's work ends before s0 continues
+    MF_CK(cudaEventRecord(p.e_done, p.s_out));
+    MF_CK(cudaStreamWaitEvent(s0, p.e_done, 0));
+  }
+
+  void
+  Operator::vmult_host(void *dst_h, const void *src_h, void *dst_d, void *src_d, HostPipe &p)
+  {
+    const size_t bytes = m() * elem_size();
+    int          n     = p.chunks > 0 ? p.chunks : (bytes >= (size_t(4) << 20) ? 4 : 1);
+    n                  = std::min(std::min(n, HostPipe::MAXC), geom.C[2]);
+    cudaStream_t s0    = ctx->stream;
+    if (n < 2)
+      {
+        MF_CK(cudaMemcpyAsync(src_d, src_h, bytes, cudaMemcpyHostToDevice, s0));
+        vmult(dst_d, src_d);
+        MF_CK(cudaMemcpyAsync(dst_h, dst_d, bytes, cudaMemcpyDeviceToHost, s0));
+        MF_CK(cudaStreamSynchronize(s0));
+        return;
+      }
+    p.init();
+    HostPipe::Key key;
+    key.dst_h = dst_h;
+    key.src_h = src_h;
+    key.dst_d = dst_d;
+    key.src_d = src_d;
+    key.n     = n;
+    key.state = vmult_state();
+    if (p.gexec && key == p.g)
+      {
+        // replay: one launch for the whole overlapped copy/apply/copy
+        MF_CK(cudaGraphLaunch(p.gexec, s0));
+        count_launch(int(p.g_launches));
+        MF_CK(cudaStreamSynchronize(s0));
+        return;
+      }
+    // the second call with the same pinned buffers and operator state is
+    // captured into a graph; pageable buffers always take the eager path
+    if (key == p.last && host_pinned(dst_h) && host_pinned(src_h))
+      {
+        p.drop_graph();
+        const long long l0 = launch_count();
+        MF_CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+        cudaGraph_t g = nullptr;
+        try
+          {
+            enqueue_vmult_host(dst_h, src_h, dst_d, src_d, p, n);
+          }
+        catch (...)
+          {
+            cudaStreamEndCapture(s0, &g);
+            if (g)
+              cudaGraphDestroy(g);
+            throw;
+          }
+        MF_CK(cudaStreamEndCapture(s0, &g));
+        const cudaError_t e = cudaGraphInstantiate(&p.gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess)
+          {
+            p.gexec = nullptr;
+            MF_CK(e);
+          }
+        p.g          = key;
+        p.g_launches = launch_count() - l0;
+        MF_CK(cudaGraphLaunch(p.gexec, s0)); // the capture counted its launches
+        MF_CK(cudaStreamSynchronize(s0));
+        return;
+      }
+    p.last = key;
+    enqueue_vmult_host(dst_h, src_h, dst_d, src_d, p, n);
+    MF_CK(cudaStreamSynchronize(s0));
+  }
+
+  void
   Operator::finish_diagonal()
   {
     // set_constrained_entries_to_one, keep a copy of the diagonal, invert
@@ -571,7 +805,7 @@ namespace mfgpu
   }
 
   void
-  HeatOperator::apply_cells(void *dst, const void *src)
+  HeatOperator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
   {
     if (delta_t <= 0)
       throw Error(ERR_STATE, "delta_t not set (set_delta_t)");
@@ -581,9 +815,11 @@ namespace mfgpu
     a.kdt         = coefficient * delta_t;
     a.src         = src;
     a.dst         = dst;
-    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
-                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
-                                      dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
+    a.cell_begin  = c0;
+    a.cell_end    = c1;
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, s);
     count_launch();
     MF_CK(e);
   }
@@ -683,7 +919,7 @@ namespace mfgpu
   }
 
   void
-  NHOperator::apply_cells(void *dst, const void *src)
+  NHOperator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
   {
     if (!cached)
       throw Error(ERR_STATE, "NeoHookOperator: cache() before vmult");
@@ -696,9 +932,11 @@ namespace mfgpu
     a.ucell       = ucell.ptr;
     a.src         = src;
     a.dst         = dst;
-    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
-                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
-                                      dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
+    a.cell_begin  = c0;
+    a.cell_end    = c1;
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, s);
     count_launch();
     MF_CK(e);
   }

@@ -243,8 +243,21 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   template <typename T>
   void
+  Multigrid<T>::drop_graph()
+  {
+    if (gexec)
+      cudaGraphExecDestroy(gexec);
+    gexec      = nullptr;
+    g_dst      = nullptr;
+    g_src      = nullptr;
+    eager_done = false;
+  }
+
+  template <typename T>
+  void
   Multigrid<T>::setup(double range, unsigned degree, int eig_its, int coarse_eig_its)
   {
+    drop_graph();
     const int L = int(ops.size());
     smoothers.clear();
     smoothers.resize(L);
@@ -322,6 +335,59 @@ namespace mfgpu
   template <typename T>
   void
   Multigrid<T>::vmult(double *dst, const double *src)
+  {
+    if (use_graphs)
+      {
+        if (gexec && dst == g_dst && src == g_src)
+          {
+            MF_CK(cudaGraphLaunch(gexec, ctx->stream));
+            count_launch(int(g_launches));
+            ++graph_replays;
+            ++vcycles;
+            return;
+          }
+        if (eager_done)
+          {
+            // the smoothers' eigenvalue estimates ran in the eager V-cycle,
+            // so the captured work is launches, copies and memsets only
+            drop_graph();
+            const long long l0 = launch_count();
+            MF_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            cudaGraph_t g = nullptr;
+            try
+              {
+                vcycle(dst, src);
+              }
+            catch (...)
+              {
+                cudaStreamEndCapture(ctx->stream, &g);
+                if (g)
+                  cudaGraphDestroy(g);
+                throw;
+              }
+            MF_CK(cudaStreamEndCapture(ctx->stream, &g));
+            const cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess)
+              {
+                gexec = nullptr;
+                MF_CK(e);
+              }
+            g_launches = launch_count() - l0;
+            g_dst      = dst;
+            g_src      = src;
+            eager_done = true;
+            MF_CK(cudaGraphLaunch(gexec, ctx->stream)); // vcycle() counted it
+            return;
+          }
+        eager_done = true;
+      }
+    vcycle(dst, src);
+  }
+
+  template <typename T>
+  void
+  Multigrid<T>::vcycle(double *dst, const double *src)
   {
     const int    L = int(ops.size()) - 1;
     const size_t n = ops[L]->m();

@@ -88,8 +88,23 @@ namespace mfgpu
     Chebyshev<double>  coarse_cheb64;
     DevBuf             c64_sol, c64_def;
     int                vcycles = 0;
+    // CUDA-graph replay of the V-cycle: the first application after setup()
+    // runs eagerly, the second is captured into a graph (for its dst/src
+    // pair) and later applications with the same pair replay it.  setup()
+    // drops the graph (new eigenvalue bounds and diagonals).
+    bool               use_graphs = false;
+    cudaGraphExec_t    gexec      = nullptr;
+    double            *g_dst      = nullptr;
+    const double      *g_src      = nullptr;
+    long long          g_launches = 0;
+    bool               eager_done = false;
+    int                graph_replays = 0;
+    ~Multigrid() { drop_graph(); }
     void setup(double range, unsigned degree, int eig_its, int coarse_eig_its);
     void level_v_step(int l);
     void vmult(double *dst, const double *src) override;
+    void drop_graph();
+  private:
+    void vcycle(double *dst, const double *src);
   };
 } // namespace mfgpu

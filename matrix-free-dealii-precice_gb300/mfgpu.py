@@ -48,7 +48,8 @@ class SolverParams(C.Structure):
                 ("cheb_degree", C.c_int), ("cheb_range", C.c_double),
                 ("cheb_eig_its", C.c_int), ("coarse_accurate", C.c_int),
                 ("mg_precision", C.c_int), ("coarse_fp64", C.c_int),
-                ("fp64_emulation", C.c_int)]
+                ("fp64_emulation", C.c_int),
+                ("cuda_graphs", C.c_int)]
 
 
 class SolidParams(C.Structure):
@@ -221,6 +222,10 @@ class _Operator:
             self.h, dst_np.ctypes.data_as(C.c_void_p),
             src_np.ctypes.data_as(C.c_void_p)))
 
+    def set_host_chunks(self, n_chunks):
+        """z-slabs of the overlapped vmult_host (0 auto, 1 no overlap)."""
+        _check(lib().mfgpu_operator_set_host_chunks(self.h, int(n_chunks)))
+
     def set_fp64_emulation(self, enable=True):
         """Double-float arithmetic on the FP32 pipe for an FP64 operator."""
         _check(lib().mfgpu_operator_set_fp64_emulation(self.h, int(enable)))
@@ -338,7 +343,7 @@ def prolongate_noalloc(mesh, coarse_level, nc, coarse, fine, precision=64,
 def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
                   cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
                   coarse_accurate=True, mg_precision=32, coarse_fp64=False,
-                  max_it_mult=1, fp64_emulation=False):
+                  max_it_mult=1, fp64_emulation=False, cuda_graphs=True):
     s = SolverParams()
     s.preconditioner = {"none": 0, "jacobi": 1, "gmg": 2}[preconditioner]
     s.relaxation = relaxation
@@ -351,6 +356,7 @@ def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
     s.mg_precision = mg_precision
     s.coarse_fp64 = int(coarse_fp64)
     s.fp64_emulation = int(fp64_emulation)
+    s.cuda_graphs = int(cuda_graphs)
     return s
 
 

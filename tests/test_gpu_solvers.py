@@ -142,3 +142,32 @@ def test_heat_gaussian_step(ctx, degree):
     ul = u.cpu().numpy()
     assert np.linalg.norm(ul - uo) / np.linalg.norm(uo) < 1e-8
     assert abs(r.cg_its[0] - ro.cg_its[0]) <= 1
+
+
+@pytest.mark.parametrize("mg_precision", [32, 64])
+def test_vcycle_graph_replay_matches_eager(ctx, mg_precision):
+    """The V-cycle replayed as a CUDA graph gives the same Newton and CG
+    counts and the same displacement (to round-off of the atomic scatter) as
+    the eagerly launched V-cycle."""
+    spec = W.cantilever(2, 2, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    res = {}
+    for graphs in (False, True):
+        _, pl = solid_pair(spec, "referential_qp", mg_precision=mg_precision)
+        pl.solver.cuda_graphs = int(graphs)
+        res[graphs] = mfgpu.Solid(ctx, pl).run()
+    e, g = res[False], res[True]
+    assert list(e.newton_its[:2]) == list(g.newton_its[:2])
+    assert abs(e.total_cg - g.total_cg) <= 1
+    for st in range(2):
+        we, wg = np.array(e.watch_disp[st][:3]), np.array(g.watch_disp[st][:3])
+        assert np.linalg.norm(wg - we) <= 1e-10 * np.linalg.norm(we)
+
+
+def test_heat_graph_replay_matches_eager(ctx):
+    spec = W.unit_cube_heat(3, 3)
+    its = {}
+    for graphs in (False, True):
+        _, pl = heat_pair(spec, n_steps=2, tol=1e-10)
+        pl.solver.cuda_graphs = int(graphs)
+        its[graphs] = list(mfgpu.Heat(ctx, pl).run().cg_its[:2])
+    assert its[False] == its[True]
