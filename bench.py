@@ -297,11 +297,74 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
             h = mfgpu.Heat(ctx, hp)
             r = h.run()
             row[label] = r.seconds
-            row[label.replace("_s", "_its")] = r.cg_its[0]
+            row[label[:-2] + "_its"] = r.cg_its[0]
             h.close()
         res.append(row)
         torch.cuda.empty_cache()
     return res
+
+
+def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src, n, op, src_np, dst_np):
+    """Measurements behind the kernel choices on the headline workload (Q4
+    cantilever 64x8x8, 839,619 DoFs), L2 flushed before every application:
+    * scatter: atomic adds vs 8 parity colours with plain adds;
+    * quadrature data: each caching variant of the tangent in native FP64
+      (streamed bytes vs recomputation), referential_qp also in FP32;
+    * host-buffer vmult: number of overlapped z-slabs (1 = no overlap)."""
+    out = {"scatter": {}, "caching_fp64": {}, "host_slabs": {}}
+    dst = torch.zeros(n, dtype=torch.float64, device=dev)
+    for mode in ("atomic", "colored"):
+        op.set_scatter(mode)
+        t = _timed_vmults(torch, op, dst, src, flush, stream, 10)
+        out["scatter"]["nh_q4_df64_" + mode] = {"ms": t * 1e3, "dofs_per_s": n / t}
+    op.set_scatter("atomic")
+    heat = W.unit_cube_heat(2, 6)
+    hm = W.to_lib_mesh(mfgpu, heat)
+    hn = W.n_dofs(heat, 1)
+    for prec in (64, 32):
+        dt = torch.float64 if prec == 64 else torch.float32
+        hop = mfgpu.LaplaceOperator(ctx, hm, -1, prec, True, delta_t=0.1)
+        hs = torch.rand(hn, dtype=dt, device=dev) * 2 - 1
+        hd = torch.zeros_like(hs)
+        for mode in ("atomic", "colored"):
+            hop.set_scatter(mode)
+            hop.vmult(hd, hs)
+            t = _timed_vmults(torch, hop, hd, hs, flush, stream, 10)
+            out["scatter"][f"heat_64cube_q2_fp{prec}_{mode}"] = {"ms": t * 1e3, "dofs_per_s": hn / t}
+        hop.close()
+        del hs, hd
+    mat = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+    for caching in ("scalar_referential", "tensor2", "tensor4", "tensor4_ns", "referential_qp"):
+        for prec in ((64, 32) if caching in ("scalar_referential", "referential_qp") else (64,)):
+            dt = torch.float64 if prec == 64 else torch.float32
+            cop = mfgpu.NeoHookOperator(ctx, mesh, -1, prec, caching)
+            cop.set_material(mat)
+            uu = u if prec == 64 else u.to(torch.float32)
+            cop.initialize(uu)
+            cop.cache()
+            s2 = src.to(dt)
+            d2 = torch.zeros_like(s2)
+            cop.vmult(d2, s2)
+            t = _timed_vmults(torch, cop, d2, s2, flush, stream, 10)
+            out["caching_fp64" if prec == 64 else "caching_fp32"] = out.get(
+                "caching_fp64" if prec == 64 else "caching_fp32", {})
+            out["caching_fp64" if prec == 64 else "caching_fp32"][caching] = {
+                "ms": t * 1e3, "dofs_per_s": n / t, "cache_mb": cop.memory_consumption() / 1e6}
+            cop.close()
+            del s2, d2, uu
+    K = 20
+    for chunks in (1, 2, 4, 8):
+        op.set_host_chunks(chunks)
+        for _ in range(3):
+            op.vmult_host(dst_np, src_np)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            op.vmult_host(dst_np, src_np)
+        t = (time.perf_counter() - t0) / K
+        out["host_slabs"][str(chunks)] = {"ms": t * 1e3, "dofs_per_s": n / t}
+    op.set_host_chunks(0)
+    torch.cuda.empty_cache()
+    return out
 
 
 def extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush):
@@ -590,6 +653,8 @@ def main():
         extras = {}
         for key, fn in (("time_to_solve_1e-8", lambda: extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev)),
                         ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
+                        ("design_choices", lambda: extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush,
+                                                                         mesh, u, src, n, op, src_np, dst_np)),
                         ("degree_sweep_heat_64cube", lambda: extra_degree_sweep(torch, mfgpu, W, ctx, dev,
                                                                                stream, flush, peak)),
                         ("serving_300_requests", lambda: extra_serving(mfgpu, W))):

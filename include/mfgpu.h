@@ -158,6 +158,12 @@ int mfgpu_operator_Tvmult_add(mfgpu_operator *op, void *dst, const void *src);
  * done; returns when dst_host holds the result */
 int mfgpu_operator_vmult_host(mfgpu_operator *op, void *dst_host,
                               const void *src_host);
+/* scatter of the cell contributions: 0 = atomic adds (default), 1 = cells
+ * in 8 parity colours, one launch per colour with plain adds (results are
+ * bitwise reproducible from run to run, as the reference's CPU loop is).
+ * No counterpart in the reference (its CPU cell loop needs neither). */
+int mfgpu_operator_set_scatter(mfgpu_operator *op, int mode);
+
 /* number of z-slabs of the host-buffer vmult: 0 = from the vector size
  * (4 from 4 MB up), 1 = copy in, apply, copy out without overlap, <= 8.
  * No counterpart in the reference (its vectors live in host memory). */

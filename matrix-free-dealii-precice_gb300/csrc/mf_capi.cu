@@ -353,6 +353,17 @@ extern "C"
   }
 
   int
+  mfgpu_operator_set_scatter(mfgpu_operator *op, int mode)
+  {
+    return guarded([&] {
+      need(op, "op");
+      if (mode != 0 && mode != 1)
+        throw Error(ERR_ARG, "scatter mode must be 0 (atomic) or 1 (coloured)");
+      op->op->scatter = mode;
+    });
+  }
+
+  int
   mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks)
   {
     return guarded([&] {

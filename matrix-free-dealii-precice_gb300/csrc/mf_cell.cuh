@@ -22,6 +22,11 @@
 
 namespace mfgpu
 {
+  // quadrature data of operators without a separate load step
+  struct NoPre
+  {
+  };
+
   template <typename T>
   __device__ __forceinline__ T
   fma_(T a, T b, T c)
@@ -369,6 +374,10 @@ namespace mfgpu
   //   const T* ucell;                       // cell-local u values if eval_u
   //   __device__ void operator()(unsigned cell, int q, T (&v)[NC],
   //                              T (&H)[NC][3], const T (*Hu)[3]) const;
+  //   static constexpr bool prefetch;      // split into load() + apply():
+  //   using Pre;                            // the quadrature data of a point
+  //   __device__ Pre load(unsigned cell, int q) const;
+  //   __device__ void apply(const Pre &, T (&v)[NC], T (&H)[NC][3]) const;
   // v and H arrive as the values and REAL gradients at quadrature point q and
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
@@ -389,8 +398,25 @@ namespace mfgpu
     const int      l      = threadIdx.x - lc * N2;
     const int      a      = l % N;
     const int      b      = l / N;
-    const unsigned cell   = g.cell_begin + blockIdx.x * CPB + lc;
-    const bool     active = cell < g.cell_end;
+    unsigned cell;
+    bool     active;
+    if (g.color < 0)
+      {
+        cell   = g.cell_begin + blockIdx.x * CPB + lc;
+        active = cell < g.cell_end;
+      }
+    else
+      {
+        // cells (2i+px, 2j+py, 2k+pz) of one parity colour share no node
+        const unsigned idx = blockIdx.x * CPB + lc;
+        active             = idx < g.color_n;
+        const unsigned i   = active ? idx : 0u;
+        const unsigned ix  = i % unsigned(g.hc[0]), r = i / unsigned(g.hc[0]);
+        const unsigned iy = r % unsigned(g.hc[1]), iz = r / unsigned(g.hc[1]);
+        cell = (2 * ix + unsigned(g.color & 1)) +
+               unsigned(g.C[0]) * ((2 * iy + unsigned((g.color >> 1) & 1)) +
+                                   unsigned(g.C[1]) * (2 * iz + unsigned((g.color >> 2) & 1)));
+      }
     T             *cb     = sm + lc * SPC;
     T             *GU     = cb + NC * 4 * N3; // 3*NC*N3 if eval_u
     T             *XU     = GU + 3 * NC * N3; // N3 scratch if eval_u
@@ -402,27 +428,38 @@ namespace mfgpu
     const int      cz  = cyz / g.C[1];
 
     // -------- gather + evaluate ------------------------------------------
+    // z-column (x=a, y=b) of component c in the storage type; the column of
+    // the next component is loaded before the current one is evaluated
+    auto gather = [&](int c, TS (&raw)[N]) {
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        {
+          TS val = TS(0);
+          if (active)
+            {
+              const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
+              const size_t node =
+                size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+              bool skip = false;
+              if (CONSTRAINED)
+                skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
+              if (!skip)
+                val = __ldg(src + size_t(c) * g.n_nodes + node);
+            }
+          raw[k] = val;
+        }
+    };
+    TS next_col[N];
+    gather(0, next_col);
 #pragma unroll 1
     for (int c = 0; c < NC; ++c)
       {
         T col[N];
 #pragma unroll
         for (int k = 0; k < N; ++k)
-          {
-            T val = zero<T>();
-            if (active)
-              {
-                const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
-                const size_t node =
-                  size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
-                bool skip = false;
-                if (CONSTRAINED)
-                  skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
-                if (!skip)
-                  val = to_compute<T, TS>(__ldg(src + size_t(c) * g.n_nodes + node));
-              }
-            col[k] = val;
-          }
+          col[k] = to_compute<T, TS>(next_col[k]);
+        if (c + 1 < NC)
+          gather(c + 1, next_col);
         // sweep scratch: the y and z gradient slots of this component
         T *V = cb + c * 4 * N3;
         evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
@@ -452,6 +489,11 @@ namespace mfgpu
     if (active)
       {
         const T wab = sh.w[a] * sh.w[b] * g.vol;
+        // quadrature data of the next point is loaded before the current
+        // point is computed (operators with QOp::prefetch)
+        typename QOp::Pre pre{};
+        if constexpr (QOp::prefetch)
+          pre = op.load(cell, a + b * N);
 #pragma unroll 1
         for (int k = 0; k < N; ++k)
           {
@@ -476,7 +518,15 @@ namespace mfgpu
                   for (int d = 0; d < 3; ++d)
                     Hu[c][d] = GU[(c * 3 + d) * N3 + q];
               }
-            op(cell, q, v, H, Hu);
+            if constexpr (QOp::prefetch)
+              {
+                const typename QOp::Pre cur = pre;
+                if (k + 1 < N)
+                  pre = op.load(cell, q + N2);
+                op.apply(cur, v, H);
+              }
+            else
+              op(cell, q, v, H, Hu);
             const T jxw = wab * sh.w[k];
 #pragma unroll
             for (int c = 0; c < NC; ++c)
@@ -509,7 +559,11 @@ namespace mfgpu
                   continue;
                 const size_t node =
                   size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
-                atomicAdd(dst + size_t(c) * g.n_nodes + node, to_storage<TS, T>(col[k]));
+                TS *d = dst + size_t(c) * g.n_nodes + node;
+                if (g.color < 0)
+                  atomicAdd(d, to_storage<TS, T>(col[k]));
+                else
+                  *d += to_storage<TS, T>(col[k]); // no other cell of this launch owns the node
               }
           }
       }
@@ -523,8 +577,10 @@ namespace mfgpu
   template <typename T>
   struct HeatQOp
   {
-    static constexpr bool eval_u = false;
-    const T              *ucell  = nullptr;
+    static constexpr bool eval_u   = false;
+    static constexpr bool prefetch = false;
+    using Pre                      = NoPre;
+    const T              *ucell    = nullptr;
     T                     kdt;
     __device__ __forceinline__ void
     operator()(unsigned, int, T (&)[1], T (&H)[1][3], const T (*)[3]) const
@@ -547,7 +603,9 @@ namespace mfgpu
   template <typename T>
   struct NHScalarRefQOp
   {
-    static constexpr bool eval_u = true;
+    static constexpr bool eval_u   = true;
+    static constexpr bool prefetch = false;
+    using Pre                      = NoPre;
     const T              *ucell;  // [cell][3][N^3]
     const T              *scalar; // [cell][N^3]
     NHMat<T>              m;
@@ -641,23 +699,35 @@ namespace mfgpu
   template <typename T>
   struct NHQp10QOp
   {
-    static constexpr bool eval_u = false;
-    const T              *ucell  = nullptr;
+    static constexpr bool eval_u   = false;
+    static constexpr bool prefetch = true;
+    const T              *ucell    = nullptr;
     const T              *cache; // [cell][10][N^3]
     NHMat<T>              m;
     int                   n3;
-    __device__ __forceinline__ void
-    operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
-               const T (*)[3]) const
+    struct Pre
+    {
+      T M[3][3];
+      T c;
+    };
+    __device__ __forceinline__ Pre
+    load(unsigned cell, int q) const
     {
       const T *cp = cache + size_t(cell) * 10 * n3 + q;
-      T        M[3][3];
+      Pre      p;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
-          M[i][j] = ldg_(cp + (i * 3 + j) * n3);
-      const T c = ldg_(cp + 9 * n3);
+          p.M[i][j] = ldg_(cp + (i * 3 + j) * n3);
+      p.c = ldg_(cp + 9 * n3);
+      return p;
+    }
+    __device__ __forceinline__ void
+    apply(const Pre &p, T (&v)[3], T (&H)[3][3]) const
+    {
+      const auto &M = p.M;
+      const T     c = p.c;
       // t = M : H
       T t = M[0][0] * H[0][0];
 #pragma unroll
@@ -698,6 +768,12 @@ namespace mfgpu
 #pragma unroll
       for (int c2 = 0; c2 < 3; ++c2)
         v[c2] = v[c2] * m.rho_alpha;
+    }
+    __device__ __forceinline__ void
+    operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
+               const T (*)[3]) const
+    {
+      apply(load(cell, q), v, H);
     }
   };
 
@@ -784,8 +860,10 @@ namespace mfgpu
   template <typename T, int VAR>
   struct NHCachedQOp
   {
-    static constexpr bool eval_u = false;
-    const T              *ucell  = nullptr;
+    static constexpr bool eval_u   = false;
+    static constexpr bool prefetch = false;
+    using Pre                      = NoPre;
+    const T              *ucell    = nullptr;
     const T              *cache;
     NHMat<T>              m;
     int                   n3;

@@ -67,6 +67,12 @@ namespace mfgpu
     int      p;
     unsigned n_cells;
     unsigned cell_begin, cell_end; // cells [begin, end) of one application launch
+    // parity colour of a coloured application launch (-1: all cells, atomic
+    // scatter): cells (2i+px, 2j+py, 2k+pz), colour = px + 2 py + 4 pz, hc[d]
+    // cells per direction, color_n = hc[0]*hc[1]*hc[2]
+    int      color;
+    unsigned color_n;
+    int      hc[3];
     size_t   n_nodes;
     T        inv_h[3];
     T        vol; // h0*h1*h2
@@ -102,11 +108,28 @@ namespace mfgpu
     c.n_cells    = unsigned(g.n_cells);
     c.cell_begin = 0;
     c.cell_end   = unsigned(g.n_cells);
+    c.color      = -1;
+    c.color_n    = 0;
+    c.hc[0] = c.hc[1] = c.hc[2] = 0;
     c.n_nodes    = g.n_nodes;
     c.vol     = conv_host<T>(g.h[0] * g.h[1] * g.h[2]);
     for (int f = 0; f < 6; ++f)
       c.face_mask[f] = g.face_mask[f];
     return c;
+  }
+
+  // cells of parity colour `color` per direction (hc) and in total
+  inline unsigned
+  color_cells(const int *C, int color, int *hc)
+  {
+    unsigned n = 1;
+    for (int d = 0; d < 3; ++d)
+      {
+        const int p = (color >> d) & 1;
+        hc[d]       = (C[d] - p + 1) / 2;
+        n *= unsigned(hc[d] > 0 ? hc[d] : 0);
+      }
+    return n;
   }
 
   // component mask of the Dirichlet constraints on node (ix,iy,iz)

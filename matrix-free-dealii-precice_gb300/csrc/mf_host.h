@@ -166,6 +166,7 @@ namespace mfgpu
     int       nc          = 1;
     bool      constrained = true;
     int       arith       = 0; // 0 native, 1 double-float (FP64 operators only)
+    int       scatter     = 0; // 0 atomic adds, 1 parity colours with plain adds (deterministic)
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;
@@ -201,6 +202,8 @@ namespace mfgpu
     void enqueue_vmult_host(void *dst_h, const void *src_h, void *dst_d, void *src_d, HostPipe &p, int n);
   public:
     void finish_diagonal(); // constrained -> 1, invert
+    // kernel launches of one application of the cells [c0, c1) (all if c1 <= c0)
+    int cell_launches(size_t c0, size_t c1) const;
   };
 
   struct HeatOperator : Operator

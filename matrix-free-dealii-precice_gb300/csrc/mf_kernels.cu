@@ -73,6 +73,8 @@ namespace mfgpu
           c.cell_begin = unsigned(a.cell_begin);
           c.cell_end   = unsigned(a.cell_end < c.n_cells ? a.cell_end : c.n_cells);
         }
+      else if (a.colored)
+        c.color = 8; // all colours, one launch each
       return c;
     }
 
@@ -111,6 +113,22 @@ namespace mfgpu
       cudaError_t   e    = prepare(k, smem);
       if (e != cudaSuccess)
         return e;
+      if (cg.color == 8)
+        {
+          // coloured scatter: one launch per non-empty parity colour, in order
+          for (int color = 0; color < 8; ++color)
+            {
+              CellGeom<T> c = cg;
+              c.color       = color;
+              c.color_n     = color_cells(cg.C, color, c.hc);
+              if (c.color_n == 0)
+                continue;
+              k<<<(c.color_n + CPB - 1) / CPB, CPB * N * N, smem, s>>>(sh, c, op, src, dst);
+              if ((e = cudaGetLastError()) != cudaSuccess)
+                return e;
+            }
+          return cudaSuccess;
+        }
       const unsigned grid = (cg.cell_end - cg.cell_begin + CPB - 1) / CPB;
       if (grid == 0)
         return cudaSuccess;

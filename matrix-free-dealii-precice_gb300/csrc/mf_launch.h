@@ -42,6 +42,7 @@ namespace mfgpu
     const void *src;
     void       *dst;
     size_t      cell_begin = 0, cell_end = 0; // cell range; empty = all cells
+    bool        colored = false; // all cells by parity colour, plain (non-atomic) scatter
   };
 
   template <int N, typename T>

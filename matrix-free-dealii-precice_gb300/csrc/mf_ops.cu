@@ -610,10 +610,21 @@ namespace mfgpu
     return size_t(u);
   }
 
+  int
+  Operator::cell_launches(size_t c0, size_t c1) const
+  {
+    if (scatter != 1 || c1 > c0)
+      return 1;
+    int n = 0, hc[3];
+    for (int color = 0; color < 8; ++color)
+      n += color_cells(geom.C, color, hc) > 0 ? 1 : 0;
+    return n;
+  }
+
   size_t
   Operator::vmult_state() const
   {
-    size_t h = hmix(size_t(precision), size_t(arith));
+    size_t h = hmix(size_t(precision), size_t(arith) + 2 * size_t(scatter));
     h        = hmix(h, size_t(constrained));
     return hmix(h, size_t(nc));
   }
@@ -662,9 +673,15 @@ namespace mfgpu
     int          zc[HostPipe::MAXC + 1];
     for (int k = 0; k <= n; ++k)
       zc[k] = int((long long)k * Cz / n);
-    // node planes of chunk k: [zc[k]*p, zc[k+1]*p), the last one up to the top plane
-    auto plane_lo = [&](int k) { return size_t(zc[k]) * deg; };
-    auto plane_hi = [&](int k) { return k == n - 1 ? size_t(geom.Nn[2]) : size_t(zc[k + 1]) * deg; };
+    // node planes copied in with slab k: up to and including the top plane of
+    // z-slab k (so that its cells need nothing later), from the plane after
+    // the previous slab's top one
+    auto in_lo  = [&](int k) { return k == 0 ? size_t(0) : size_t(zc[k]) * deg + 1; };
+    auto in_hi  = [&](int k) { return k == n - 1 ? size_t(geom.Nn[2]) : size_t(zc[k + 1]) * deg + 1; };
+    // node planes copied out with slab k: [zc[k]*p, zc[k+1]*p), the last one
+    // up to the top plane
+    auto out_lo = [&](int k) { return size_t(zc[k]) * deg; };
+    auto out_hi = [&](int k) { return k == n - 1 ? size_t(geom.Nn[2]) : size_t(zc[k + 1]) * deg; };
     char       *dd = static_cast<char *>(dst_d);
     char       *sd = static_cast<char *>(src_d);
     char       *dh = static_cast<char *>(dst_h);
@@ -677,15 +694,15 @@ namespace mfgpu
       MF_CK(cudaStreamWaitEvent(s, p.e_zero, 0));
     for (int k = 0; k < n; ++k)
       {
-        const size_t off = plane_lo(k) * plane * es, w = (plane_hi(k) - plane_lo(k)) * plane * es;
+        const size_t off = in_lo(k) * plane * es, w = (in_hi(k) - in_lo(k)) * plane * es;
         MF_CK(cudaMemcpy2DAsync(sd + off, pitch, sh + off, pitch, w, nc, cudaMemcpyHostToDevice, p.s_in));
         MF_CK(cudaEventRecord(p.e_in[k], p.s_in));
       }
     for (int k = 0; k < n; ++k)
       {
-        // the cells of z-slab k read the node planes up to the first plane of chunk k+1
+        // the cells of z-slab k read node planes [zc[k]*p, zc[k+1]*p]: copied by slab k
         cudaStream_t s = p.s_comp[k & 1];
-        MF_CK(cudaStreamWaitEvent(s, p.e_in[std::min(k + 1, n - 1)], 0));
+        MF_CK(cudaStreamWaitEvent(s, p.e_in[k], 0));
         apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s);
         MF_CK(cudaEventRecord(p.e_comp[k], s));
       }
@@ -705,7 +722,7 @@ namespace mfgpu
         if (k > 0)
           MF_CK(cudaStreamWaitEvent(p.s_out, p.e_comp[k - 1], 0));
         MF_CK(cudaStreamWaitEvent(p.s_out, p.e_con, 0));
-        const size_t off = plane_lo(k) * plane * es, w = (plane_hi(k) - plane_lo(k)) * plane * es;
+        const size_t off = out_lo(k) * plane * es, w = (out_hi(k) - out_lo(k)) * plane * es;
         MF_CK(cudaMemcpy2DAsync(dh + off, pitch, dd + off, pitch, w, nc, cudaMemcpyDeviceToHost, p.s_out));
       }
     // join: every stream's work ends before s0 continues
@@ -719,6 +736,8 @@ namespace mfgpu
     const size_t bytes = m() * elem_size();
     int          n     = p.chunks > 0 ? p.chunks : (bytes >= (size_t(4) << 20) ? 4 : 1);
     n                  = std::min(std::min(n, HostPipe::MAXC), geom.C[2]);
+    if (scatter == 1)
+      n = 1; // concurrent z-slabs need the atomic scatter on their shared planes
     cudaStream_t s0    = ctx->stream;
     if (n < 2)
       {
@@ -817,10 +836,11 @@ namespace mfgpu
     a.dst         = dst;
     a.cell_begin  = c0;
     a.cell_end    = c1;
+    a.colored     = scatter == 1;
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, s);
-    count_launch();
+    count_launch(cell_launches(c0, c1));
     MF_CK(e);
   }
 
@@ -934,10 +954,11 @@ namespace mfgpu
     a.dst         = dst;
     a.cell_begin  = c0;
     a.cell_end    = c1;
+    a.colored     = scatter == 1;
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, s);
-    count_launch();
+    count_launch(cell_launches(c0, c1));
     MF_CK(e);
   }
 

@@ -222,6 +222,10 @@ class _Operator:
             self.h, dst_np.ctypes.data_as(C.c_void_p),
             src_np.ctypes.data_as(C.c_void_p)))
 
+    def set_scatter(self, mode):
+        """0: atomic scatter; 1: parity-coloured plain scatter (deterministic)."""
+        _check(lib().mfgpu_operator_set_scatter(self.h, {"atomic": 0, "colored": 1}.get(mode, mode)))
+
     def set_host_chunks(self, n_chunks):
         """z-slabs of the overlapped vmult_host (0 auto, 1 no overlap)."""
         _check(lib().mfgpu_operator_set_host_chunks(self.h, int(n_chunks)))
