@@ -131,6 +131,21 @@ namespace mfgpu
       }
   }
 
+  // dot-product accumulator: FMA chain in float/double, compensated
+  // (TwoSum-accumulated) in double-float
+  template <typename T>
+  struct Acc
+  {
+    T s;
+    __device__ __forceinline__ void init(T a, T b) { s = a * b; }
+    __device__ __forceinline__ void add(T a, T b) { s = fma_(a, b, s); }
+    __device__ __forceinline__ T result() const { return s; }
+  };
+  template <>
+  struct Acc<df64> : DfAcc
+  {
+  };
+
   template <typename T>
   __device__ __forceinline__ T
   zero()
@@ -142,6 +157,19 @@ namespace mfgpu
   zero<df64>()
   {
     return df64{0.f, 0.f};
+  }
+
+  template <typename T>
+  __device__ __forceinline__ T
+  one()
+  {
+    return T(1);
+  }
+  template <>
+  __device__ __forceinline__ df64
+  one<df64>()
+  {
+    return df64{1.f, 0.f};
   }
 
   template <typename T>
@@ -377,7 +405,8 @@ namespace mfgpu
   //   static constexpr bool prefetch;      // split into load() + apply():
   //   using Pre;                            // the quadrature data of a point
   //   __device__ Pre load(unsigned cell, int q) const;
-  //   __device__ void apply(const Pre &, T (&v)[NC], T (&H)[NC][3]) const;
+  //   __device__ void apply(const Pre &, T (&v)[NC], T (&H)[NC][3], T jxw) const;
+  //                                         // (returns value and flux times jxw)
   // v and H arrive as the values and REAL gradients at quadrature point q and
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
@@ -518,24 +547,35 @@ namespace mfgpu
                   for (int d = 0; d < 3; ++d)
                     Hu[c][d] = GU[(c * 3 + d) * N3 + q];
               }
+            const T jxw = wab * sh.w[k];
             if constexpr (QOp::prefetch)
               {
                 const typename QOp::Pre cur = pre;
                 if (k + 1 < N)
                   pre = op.load(cell, q + N2);
-                op.apply(cur, v, H);
+                op.apply(cur, v, H, jxw); // returns the JxW-scaled value and flux
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+                  {
+                    T *V = cb + c * 4 * N3;
+                    V[q] = v[c];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                      V[(d + 1) * N3 + q] = H[c][d];
+                  }
               }
             else
-              op(cell, q, v, H, Hu);
-            const T jxw = wab * sh.w[k];
-#pragma unroll
-            for (int c = 0; c < NC; ++c)
               {
-                T *V = cb + c * 4 * N3;
-                V[q] = v[c] * jxw;
+                op(cell, q, v, H, Hu);
 #pragma unroll
-                for (int d = 0; d < 3; ++d)
-                  V[(d + 1) * N3 + q] = H[c][d] * jxw;
+                for (int c = 0; c < NC; ++c)
+                  {
+                    T *V = cb + c * 4 * N3;
+                    V[q] = v[c] * jxw;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                      V[(d + 1) * N3 + q] = H[c][d] * jxw;
+                  }
               }
           }
       }
@@ -723,57 +763,66 @@ namespace mfgpu
       p.c = ldg_(cp + 9 * n3);
       return p;
     }
+    // P jxw = (mu jxw) H + (c jxw) (M H^T) M + (2 lambda jxw (M:H)) M, every
+    // entry one dot product; the value gets rho alpha_1 jxw
     __device__ __forceinline__ void
-    apply(const Pre &p, T (&v)[3], T (&H)[3][3]) const
+    apply(const Pre &p, T (&v)[3], T (&H)[3][3], T jxw) const
     {
       const auto &M = p.M;
-      const T     c = p.c;
-      // t = M : H
-      T t = M[0][0] * H[0][0];
+      const T     cj = p.c * jxw;
+      Acc<T>      at;
+      at.init(M[0][0], H[0][0]);
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           if (i + j > 0)
-            t = fma_(M[i][j], H[i][j], t);
-      // K = M H^T  (K_ik = sum_j M_ij H_kj)
-      T K[3][3];
+            at.add(M[i][j], H[i][j]);
+      const T tlj = (m.two_lambda * jxw) * at.result();
+      const T muj = m.mu * jxw;
+      // cK = c jxw M H^T  (K_ik = sum_j M_ij H_kj)
+      T cK[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int k = 0; k < 3; ++k)
           {
-            T s = M[i][0] * H[k][0];
-            s   = fma_(M[i][1], H[k][1], s);
-            s   = fma_(M[i][2], H[k][2], s);
-            K[i][k] = s;
+            Acc<T> ak;
+            ak.init(M[i][0], H[k][0]);
+            ak.add(M[i][1], H[k][1]);
+            ak.add(M[i][2], H[k][2]);
+            cK[i][k] = cj * ak.result();
           }
-      const T tl = m.two_lambda * t;
-      T       P[3][3];
+      T P[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           {
-            T s = K[i][0] * M[0][j];
-            s   = fma_(K[i][1], M[1][j], s);
-            s   = fma_(K[i][2], M[2][j], s);
-            P[i][j] = fma_(m.mu, H[i][j], fma_(c, s, tl * M[i][j]));
+            Acc<T> ap;
+            ap.init(muj, H[i][j]);
+            ap.add(cK[i][0], M[0][j]);
+            ap.add(cK[i][1], M[1][j]);
+            ap.add(cK[i][2], M[2][j]);
+            ap.add(tlj, M[i][j]);
+            P[i][j] = ap.result();
           }
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           H[i][j] = P[i][j];
+      const T raj = m.rho_alpha * jxw;
 #pragma unroll
       for (int c2 = 0; c2 < 3; ++c2)
-        v[c2] = v[c2] * m.rho_alpha;
+        v[c2] = v[c2] * raj;
     }
+    // unscaled form (value and flux before JxW)
     __device__ __forceinline__ void
     operator()(unsigned cell, int q, T (&v)[3], T (&H)[3][3],
                const T (*)[3]) const
     {
-      apply(load(cell, q), v, H);
+      apply(load(cell, q), v, H, one<T>());
     }
   };
 
