@@ -17,6 +17,8 @@
 // include/heat_transfer/heat_transfer.h:241,249).
 #pragma once
 
+#include <type_traits>
+
 #include "mf_common.cuh"
 #include "mf_df64.cuh"
 
@@ -376,6 +378,97 @@ namespace mfgpu
                        has_values, has_gradients, col);
   }
 
+  // runtime-direction line access (one copy of a sweep's code serves
+  // several directions)
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  load_line_rt(const T *buf, int base, int stride, T (&x)[N])
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      x[i] = buf[base + i * stride];
+  }
+
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  store_line_rt(T *buf, int base, int stride, const T (&x)[N])
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      buf[base + i * stride] = x[i];
+  }
+
+  // ---------------------------------------------------------------------
+  // Compact-code evaluate / integrate with ONE derivative matrix D for all
+  // three directions (reference-cell gradients): the sweeps that differ
+  // only in their direction run as loops over the direction, so the
+  // kernel carries 8 instead of 12 inlined copies of a line operation.
+  // Scratch: evaluate uses G1, G2; integrate uses G0, G1 (as in
+  // evaluate_field / integrate_field).
+  // ---------------------------------------------------------------------
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  evaluate_field_rg(const T *S, const T *D, const T (&col)[N], T *V, int a, int b)
+  {
+    constexpr int N3 = N * N * N;
+    T             x[N], y[N];
+    mat_apply<N>(S, col, y);
+    store_line<N, T, 2>(V + 2 * N3, a, b, y);
+    __syncthreads();
+    // y then x interpolation: G1 -> G2 -> V
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass)
+      {
+        const int dir = 1 - pass;
+        load_line_rt<N>(V + (2 + pass) * N3, line_base<N>(dir, a, b), dir == 1 ? N : 1, x);
+        mat_apply<N>(S, x, y);
+        store_line_rt<N>(pass == 0 ? V + 3 * N3 : V, line_base<N>(dir, a, b), dir == 1 ? N : 1, y);
+        __syncthreads();
+      }
+    // derivatives G_d = D V along direction d
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d)
+      {
+        const int base = line_base<N>(d, a, b), stride = d == 0 ? 1 : (d == 1 ? N : N * N);
+        load_line_rt<N>(V, base, stride, x);
+        mat_apply<N>(D, x, y);
+        store_line_rt<N>(V + (d + 1) * N3, base, stride, y);
+      }
+  }
+
+  template <int N, typename T>
+  __device__ __forceinline__ void
+  integrate_field_rg(const T *S, const T *D, T *V, int a, int b, T (&col)[N])
+  {
+    constexpr int N3 = N * N * N;
+    T             x[N], y[N];
+    __syncthreads();
+    // V += D^T G_d along z, then y
+#pragma unroll 1
+    for (int d = 2; d >= 1; --d)
+      {
+        const int base = line_base<N>(d, a, b), stride = d == 1 ? N : N * N;
+        load_line_rt<N>(V + (d + 1) * N3, base, stride, x);
+        load_line_rt<N>(V, base, stride, y);
+        mat_apply_t_add<N>(D, x, y);
+        store_line_rt<N>(V, base, stride, y);
+        __syncthreads();
+      }
+    // x: t = V + D^T G0, then S^T; result to G0 (x-lines)
+    load_line<N, T, 0>(V + N3, a, b, x);
+    load_line<N, T, 0>(V, a, b, y);
+    mat_apply_t_add<N>(D, x, y);
+    mat_apply_t<N>(S, y, x);
+    store_line<N, T, 0>(V + N3, a, b, x);
+    __syncthreads();
+    load_line<N, T, 1>(V + N3, a, b, x);
+    mat_apply_t<N>(S, x, y);
+    store_line<N, T, 1>(V + 2 * N3, a, b, y);
+    __syncthreads();
+    load_line<N, T, 2>(V + 2 * N3, a, b, x);
+    mat_apply_t<N>(S, x, col);
+  }
+
   // node index of local node (a, b, k) of cell (cx,cy,cz)
   template <typename T>
   __device__ __forceinline__ size_t
@@ -402,6 +495,8 @@ namespace mfgpu
   //   const T* ucell;                       // cell-local u values if eval_u
   //   __device__ void operator()(unsigned cell, int q, T (&v)[NC],
   //                              T (&H)[NC][3], const T (*Hu)[3]) const;
+  //   static constexpr bool ref_grad;      // H are reference-cell gradients
+  //                                         // (the op applies the Jacobian)
   //   static constexpr bool prefetch;      // split into load() + apply():
   //   using Pre;                            // the quadrature data of a point
   //   __device__ Pre load(unsigned cell, int q) const;
@@ -491,8 +586,11 @@ namespace mfgpu
           gather(c + 1, next_col);
         // sweep scratch: the y and z gradient slots of this component
         T *V = cb + c * 4 * N3;
-        evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
-                          V + 3 * N3, V + 2 * N3, V + 3 * N3, a, b, true);
+        if constexpr (QOp::ref_grad)
+          evaluate_field_rg<N>(sh.S, sh.Du, col, V, a, b);
+        else
+          evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
+                            V + 3 * N3, V + 2 * N3, V + 3 * N3, a, b, true);
       }
     if constexpr (QOp::eval_u)
       {
@@ -587,8 +685,11 @@ namespace mfgpu
         T *V = cb + c * 4 * N3;
         T  col[N];
         // sweep scratch: the x and y gradient slots (consumed by then)
-        integrate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + N3, V + 2 * N3,
-                           V + 3 * N3, V + N3, V + 2 * N3, a, b, true, true, col);
+        if constexpr (QOp::ref_grad)
+          integrate_field_rg<N>(sh.S, sh.Du, V, a, b, col);
+        else
+          integrate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + N3, V + 2 * N3,
+                             V + 3 * N3, V + N3, V + 2 * N3, a, b, true, true, col);
         if (active)
           {
 #pragma unroll
@@ -619,15 +720,16 @@ namespace mfgpu
   {
     static constexpr bool eval_u   = false;
     static constexpr bool prefetch = false;
+    static constexpr bool ref_grad = true; // H are reference-cell gradients
     using Pre                      = NoPre;
     const T              *ucell    = nullptr;
-    T                     kdt;
+    T                     kd[3]; // k dt / h_d^2: the Jacobian of both gradients
     __device__ __forceinline__ void
     operator()(unsigned, int, T (&)[1], T (&H)[1][3], const T (*)[3]) const
     {
-      H[0][0] *= kdt;
-      H[0][1] *= kdt;
-      H[0][2] *= kdt;
+      H[0][0] *= kd[0];
+      H[0][1] *= kd[1];
+      H[0][2] *= kd[2];
     }
   };
 
@@ -645,6 +747,7 @@ namespace mfgpu
   {
     static constexpr bool eval_u   = true;
     static constexpr bool prefetch = false;
+    static constexpr bool ref_grad = false;
     using Pre                      = NoPre;
     const T              *ucell;  // [cell][3][N^3]
     const T              *scalar; // [cell][N^3]
@@ -741,9 +844,11 @@ namespace mfgpu
   {
     static constexpr bool eval_u   = false;
     static constexpr bool prefetch = true;
+    static constexpr bool ref_grad = true; // H are reference-cell gradients
     const T              *ucell    = nullptr;
-    const T              *cache; // [cell][10][N^3]
+    const T              *cache; // [cell][10][N^3]: M~ = F^{-T} diag(1/h), c
     NHMat<T>              m;
+    T                     mu_d[3]; // mu / h_d^2
     int                   n3;
     struct Pre
     {
@@ -763,8 +868,12 @@ namespace mfgpu
       p.c = ldg_(cp + 9 * n3);
       return p;
     }
-    // P jxw = (mu jxw) H + (c jxw) (M H^T) M + (2 lambda jxw (M:H)) M, every
-    // entry one dot product; the value gets rho alpha_1 jxw
+    // With the reference gradient G (H = G J^{-1}, J^{-1} = diag(1/h)) and
+    // M~ = M J^{-1}, the flux against reference test gradients is
+    //   P J^{-T} = mu H J^{-T} + c (M H^T M) J^{-T} + 2 lambda (M:H) M J^{-T}
+    //            = mu_d G + c (M~ G^T) M~ + 2 lambda (M~:G) M~,   mu_d = mu/h_d^2
+    // (column d).  Times jxw, every entry one dot product; the value gets
+    // rho alpha_1 jxw.
     __device__ __forceinline__ void
     apply(const Pre &p, T (&v)[3], T (&H)[3][3], T jxw) const
     {
@@ -779,7 +888,10 @@ namespace mfgpu
           if (i + j > 0)
             at.add(M[i][j], H[i][j]);
       const T tlj = (m.two_lambda * jxw) * at.result();
-      const T muj = m.mu * jxw;
+      T       muj[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        muj[d] = mu_d[d] * jxw;
       // cK = c jxw M H^T  (K_ik = sum_j M_ij H_kj)
       T cK[3][3];
 #pragma unroll
@@ -800,7 +912,7 @@ namespace mfgpu
         for (int j = 0; j < 3; ++j)
           {
             Acc<T> ap;
-            ap.init(muj, H[i][j]);
+            ap.init(muj[j], H[i][j]);
             ap.add(cK[i][0], M[0][j]);
             ap.add(cK[i][1], M[1][j]);
             ap.add(cK[i][2], M[2][j]);
@@ -911,6 +1023,7 @@ namespace mfgpu
   {
     static constexpr bool eval_u   = false;
     static constexpr bool prefetch = false;
+    static constexpr bool ref_grad = false;
     using Pre                      = NoPre;
     const T              *ucell    = nullptr;
     const T              *cache;

@@ -55,6 +55,7 @@ namespace mfgpu
   {
     T S[N * N];
     T D[3][N * N];
+    T Du[N * N]; // unscaled (reference-cell) derivative matrix
     T w[N];
   };
 

@@ -40,7 +40,8 @@ namespace mfgpu
       ShapeA<N, T> s;
       for (int i = 0; i < N * N; ++i)
         {
-          s.S[i] = conv_host<T>(b.S[i]);
+          s.S[i]  = conv_host<T>(b.S[i]);
+          s.Du[i] = conv_host<T>(b.D[i]);
           for (int d = 0; d < 3; ++d)
             s.D[d][i] = conv_host<T>(b.D[i] / g.h[d]);
         }
@@ -159,7 +160,8 @@ namespace mfgpu
     if (a.kind == 0)
       {
         HeatQOp<T> op;
-        op.kdt = T(a.kdt);
+        for (int d = 0; d < 3; ++d)
+          op.kd[d] = conv_host<T>(a.kdt / (g.h[d] * g.h[d]));
         return run_apply_c<N, T, T, 1>(a.constrained, sh, cg, op, src, dst, s);
       }
     const NHMat<T> m     = to_mat<T>(a.mat);
@@ -181,6 +183,8 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
+            for (int d = 0; d < 3; ++d)
+              op.mu_d[d] = conv_host<T>(a.mat.mu / (g.h[d] * g.h[d]));
             return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
           }
         case V_TENSOR2:
@@ -393,7 +397,8 @@ namespace mfgpu
     if (a.kind == 0)
       {
         HeatQOp<df64> op;
-        op.kdt = conv_host<df64>(a.kdt);
+        for (int d = 0; d < 3; ++d)
+          op.kd[d] = conv_host<df64>(a.kdt / (g.h[d] * g.h[d]));
         return run_apply_c<N, double, df64, 1>(a.constrained, sh, cg, op, src, dst, s);
       }
     if (a.var != V_QP10)
@@ -402,6 +407,8 @@ namespace mfgpu
     op.cache = static_cast<const df64 *>(a.cache);
     op.m     = to_mat<df64>(a.mat);
     op.n3    = N3;
+    for (int d = 0; d < 3; ++d)
+      op.mu_d[d] = conv_host<df64>(a.mat.mu / (g.h[d] * g.h[d]));
     return run_apply_c<N, double, df64, 3>(a.constrained, sh, cg, op, src, dst, s);
   }
 

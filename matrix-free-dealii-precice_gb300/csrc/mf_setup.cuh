@@ -116,11 +116,13 @@ namespace mfgpu
           }
         else if constexpr (VAR == V_QP10)
           {
+            // M~ = F^{-T} diag(1/h): the operator works with reference-cell
+            // gradients (see NHQp10QOp)
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
-                st((i * 3 + j), Fi[j][i]); // M = F^{-T}
+                st((i * 3 + j), Fi[j][i] * g.inv_h[j]);
             st(9, scalar);
           }
         else if constexpr (VAR == V_TENSOR4_NS)

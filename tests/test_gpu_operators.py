@@ -121,6 +121,36 @@ def test_nh_vmult_fp64(ctx, degree, caching):
     assert rel(host(d_dst), ref) < TOL64, caching
 
 
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("arith", ["f64", "df64", "f32"])
+def test_qp10_anisotropic_cells(ctx, degree, arith):
+    """referential_qp works with reference-cell gradients and folds the
+    per-direction Jacobian into its cache and constants: checked on cells
+    with three different edge lengths (1.5 x 0.5 x 0.35)."""
+    spec = W.cantilever(degree, 1, rep=(2, 1, 1), length=(3.0, 0.5, 0.35))
+    spec["lo"] = (0.0, -0.25, 0.1)
+    spec["hi"] = (3.0, 0.25, 0.45)
+    u = W.smooth_displacement(degree, 1, spec["rep"], spec["lo"], spec["hi"], seed=6,
+                              amplitude=0.02)
+    m = W.to_lib_mesh(mfgpu, spec)
+    om = W.to_oracle_mesh(O, spec)
+    n = W.n_dofs(spec, 3)
+    src = W.uniform_vector(n, 8)
+    ref = O.nh_vmult(om, 1, O.material(0.5e6, 0.4, 1000.0, 0.01), "scalar_referential", u, src)
+    prec = 32 if arith == "f32" else 64
+    dt = np.float32 if prec == 32 else np.float64
+    op = mfgpu.NeoHookOperator(ctx, m, -1, prec, "referential_qp")
+    op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01))
+    d_u = dev(u.astype(dt))
+    op.initialize(d_u)
+    if arith == "df64":
+        op.set_fp64_emulation(True)
+    op.cache()
+    d_dst = dev(np.zeros(n, dt))
+    op.vmult(d_dst, dev(src.astype(dt)))
+    assert rel(host(d_dst).astype(np.float64), ref) < (TOL64 if prec == 64 else 5e-5)
+
+
 @pytest.mark.parametrize("degree", [1, 3, 5])
 def test_nh_vmult_fp32(ctx, degree):
     spec, u = nh_setup(degree)
