@@ -412,17 +412,18 @@ namespace mfgpu
   {
     constexpr int N3 = N * N * N;
     T             x[N], y[N];
-    mat_apply<N>(S, col, y);
-    store_line<N, T, 2>(V + 2 * N3, a, b, y);
-    __syncthreads();
-    // y then x interpolation: G1 -> G2 -> V
+    // the nodal z-column goes through G0 so that the three interpolation
+    // sweeps share one copy of the code: z G0 -> G1, y G1 -> G2, x G2 -> V
+    // (the z pass reads only the column this thread wrote)
+    store_line<N, T, 2>(V + N3, a, b, col);
 #pragma unroll 1
-    for (int pass = 0; pass < 2; ++pass)
+    for (int pass = 0; pass < 3; ++pass)
       {
-        const int dir = 1 - pass;
-        load_line_rt<N>(V + (2 + pass) * N3, line_base<N>(dir, a, b), dir == 1 ? N : 1, x);
+        const int dir = 2 - pass, base = line_base<N>(dir, a, b);
+        const int stride = dir == 0 ? 1 : (dir == 1 ? N : N * N);
+        load_line_rt<N>(V + (pass + 1) * N3, base, stride, x);
         mat_apply<N>(S, x, y);
-        store_line_rt<N>(pass == 0 ? V + 3 * N3 : V, line_base<N>(dir, a, b), dir == 1 ? N : 1, y);
+        store_line_rt<N>(pass == 2 ? V : V + (pass + 2) * N3, base, stride, y);
         __syncthreads();
       }
     // derivatives G_d = D V along direction d
@@ -443,28 +444,28 @@ namespace mfgpu
     constexpr int N3 = N * N * N;
     T             x[N], y[N];
     __syncthreads();
-    // V += D^T G_d along z, then y
+    // V += D^T G_d along z, y, x
 #pragma unroll 1
-    for (int d = 2; d >= 1; --d)
+    for (int d = 2; d >= 0; --d)
       {
-        const int base = line_base<N>(d, a, b), stride = d == 1 ? N : N * N;
+        const int base = line_base<N>(d, a, b), stride = d == 0 ? 1 : (d == 1 ? N : N * N);
         load_line_rt<N>(V + (d + 1) * N3, base, stride, x);
         load_line_rt<N>(V, base, stride, y);
         mat_apply_t_add<N>(D, x, y);
         store_line_rt<N>(V, base, stride, y);
         __syncthreads();
       }
-    // x: t = V + D^T G0, then S^T; result to G0 (x-lines)
-    load_line<N, T, 0>(V + N3, a, b, x);
-    load_line<N, T, 0>(V, a, b, y);
-    mat_apply_t_add<N>(D, x, y);
-    mat_apply_t<N>(S, y, x);
-    store_line<N, T, 0>(V + N3, a, b, x);
-    __syncthreads();
-    load_line<N, T, 1>(V + N3, a, b, x);
-    mat_apply_t<N>(S, x, y);
-    store_line<N, T, 1>(V + 2 * N3, a, b, y);
-    __syncthreads();
+    // S^T along x (V -> G0) and y (G0 -> G1)
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass)
+      {
+        const int dir = pass, base = line_base<N>(dir, a, b), stride = dir == 0 ? 1 : N;
+        load_line_rt<N>(pass == 0 ? V : V + N3, base, stride, x);
+        mat_apply_t<N>(S, x, y);
+        store_line_rt<N>(V + (pass + 1) * N3, base, stride, y);
+        __syncthreads();
+      }
+    // S^T along z into registers
     load_line<N, T, 2>(V + 2 * N3, a, b, x);
     mat_apply_t<N>(S, x, col);
   }
