@@ -126,7 +126,7 @@ namespace mfgpu
   struct HostPipe
   {
     static constexpr int MAXC = 8;
-    cudaStream_t         s_in = nullptr, s_out = nullptr, s_comp[2] = {nullptr, nullptr};
+    cudaStream_t         s_in = nullptr, s_out = nullptr, s_comp[MAXC] = {};
     cudaEvent_t          e_zero = nullptr, e_con = nullptr, e_done = nullptr;
     cudaEvent_t          e_in[MAXC] = {}, e_comp[MAXC] = {};
     int                  chunks = 0; // 0: chosen from the vector size

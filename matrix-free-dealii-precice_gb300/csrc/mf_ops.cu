@@ -557,8 +557,12 @@ namespace mfgpu
       return;
     MF_CK(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
     MF_CK(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
-    for (auto &s : s_comp)
-      MF_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    // earlier slabs get higher priority, so the first result slab is ready
+    // (and its copy-out starts) as early as possible
+    int lo = 0, hi = 0;
+    MF_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int k = 0; k < MAXC; ++k)
+      MF_CK(cudaStreamCreateWithPriority(&s_comp[k], cudaStreamNonBlocking, std::min(lo, hi + k)));
     for (cudaEvent_t *e : {&e_zero, &e_con, &e_done})
       MF_CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int k = 0; k < MAXC; ++k)
@@ -582,7 +586,12 @@ namespace mfgpu
     drop_graph();
     if (!s_in)
       return;
-    for (cudaStream_t s : {s_in, s_out, s_comp[0], s_comp[1]})
+    for (cudaStream_t s : {s_in, s_out})
+      {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+    for (cudaStream_t s : s_comp)
       {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
@@ -690,8 +699,10 @@ namespace mfgpu
     MF_CK(cudaMemsetAsync(dst_d, 0, bytes, s0));
     MF_CK(cudaEventRecord(p.e_zero, s0));
     // every stream starts after the memset (this is also the fork of a capture)
-    for (cudaStream_t s : {p.s_in, p.s_comp[0], p.s_comp[1], p.s_out})
-      MF_CK(cudaStreamWaitEvent(s, p.e_zero, 0));
+    MF_CK(cudaStreamWaitEvent(p.s_in, p.e_zero, 0));
+    MF_CK(cudaStreamWaitEvent(p.s_out, p.e_zero, 0));
+    for (int k = 0; k < n; ++k)
+      MF_CK(cudaStreamWaitEvent(p.s_comp[k], p.e_zero, 0));
     for (int k = 0; k < n; ++k)
       {
         const size_t off = in_lo(k) * plane * es, w = (in_hi(k) - in_lo(k)) * plane * es;
@@ -700,8 +711,9 @@ namespace mfgpu
       }
     for (int k = 0; k < n; ++k)
       {
-        // the cells of z-slab k read node planes [zc[k]*p, zc[k+1]*p]: copied by slab k
-        cudaStream_t s = p.s_comp[k & 1];
+        // the cells of z-slab k read node planes [zc[k]*p, zc[k+1]*p]: copied by slab k;
+        // every slab has its own stream, so slabs run concurrently as their nodes arrive
+        cudaStream_t s = p.s_comp[k];
         MF_CK(cudaStreamWaitEvent(s, p.e_in[k], 0));
         apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s);
         MF_CK(cudaEventRecord(p.e_comp[k], s));
