@@ -237,6 +237,7 @@ def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
     out = {"workload": "cantilever 128x16x16 cells Q3, 2,773,155 DoFs, first Newton system",
            "tolerance": 1e-8}
     for name, mgp, c64, emul in (("mixed_fp32_vcycle", 32, True, False),
+                                 ("mixed_fp32_vcycle_df64", 32, True, True),
                                  ("fp64_vcycle", 64, False, False),
                                  ("fp64_vcycle_df64", 64, False, True)):
         s = mfgpu.Solid(ctx, params(mgp, c64, 1e-8, emul))
@@ -252,6 +253,9 @@ def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
                      "max_rel_error_vs_fp64": float(err.abs().max() / du_ref.abs().max())}
         s.close()
     out["speedup_mixed_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle"]["solve_s"]
+    out["speedup_mixed_df64_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle_df64"]["solve_s"]
+    out["note"] = ("mixed: FP64 outer CG + FP32 V-cycle + FP64 coarse solve; _df64: the FP64 operators "
+                   "(fine level, coarse level) in double-float arithmetic")
     return out
 
 

@@ -506,15 +506,17 @@ namespace mfgpu
   // v and H arrive as the values and REAL gradients at quadrature point q and
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
-  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED>
-  __global__ void __launch_bounds__(apply_cells_per_block<N, NC, TS, QOp::eval_u>() * N * N)
+  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED, bool ONE_CELL = false>
+  __global__ void __launch_bounds__((ONE_CELL ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>()) * N * N)
   cell_apply_kernel(const __grid_constant__ ShapeA<N, T> sh,
                     const __grid_constant__ CellGeom<T> g, const QOp op,
                     const TS *__restrict__ src, TS *__restrict__ dst)
   {
     constexpr int N2  = N * N;
     constexpr int N3  = N * N * N;
-    constexpr int CPB = apply_cells_per_block<N, NC, TS, QOp::eval_u>();
+    // ONE_CELL: one cell per block, for grids smaller than the GPU (coarse
+    // levels), so that their cells spread over as many SMs as possible
+    constexpr int CPB = ONE_CELL ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>();
     constexpr int SPC = apply_smem_per_cell<N, NC, QOp::eval_u>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);

@@ -103,6 +103,10 @@ namespace mfgpu
       return e;
     }
 
+    // launches of fewer cells than this (the SM count of GB300) take the
+    // one-cell-per-block kernel
+    constexpr unsigned SMALL_GRID = 152;
+
     template <int N, typename TS, typename T, int NC, class Op, bool CON>
     cudaError_t
     run_apply(const ShapeA<N, T> &sh, const CellGeom<T> &cg, const Op &op,
@@ -130,9 +134,21 @@ namespace mfgpu
             }
           return cudaSuccess;
         }
-      const unsigned grid = (cg.cell_end - cg.cell_begin + CPB - 1) / CPB;
+      const unsigned cells = cg.cell_end - cg.cell_begin;
+      const unsigned grid  = (cells + CPB - 1) / CPB;
       if (grid == 0)
         return cudaSuccess;
+      if constexpr (Op::ref_grad && CPB > 1)
+        if (cells < SMALL_GRID)
+          {
+            // fewer cells than SMs: one cell per block, on as many SMs
+            auto         k1    = cell_apply_kernel<N, TS, T, NC, Op, CON, true>;
+            const size_t smem1 = apply_smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
+            if ((e = prepare(k1, smem1)) != cudaSuccess)
+              return e;
+            k1<<<cells, N * N, smem1, s>>>(sh, cg, op, src, dst);
+            return cudaGetLastError();
+          }
       k<<<grid, CPB * N * N, smem, s>>>(sh, cg, op, src, dst);
       return cudaGetLastError();
     }

@@ -172,6 +172,17 @@ def nh_vmult(mesh, level, mat, caching, u, src, precision=64):
     return dst
 
 
+def nh_residual(mesh, level, mat, u, acc):
+    """-int P(F(u)):grad v - rho int acc.v on the unconstrained rows (FP64)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    acc = np.ascontiguousarray(acc, dtype=np.float64)
+    out = np.zeros_like(u)
+    rc = lib().or_nh_residual(C.byref(mesh), level, C.byref(mat), _ptr(u), _ptr(acc), _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"or_nh_residual failed ({rc})")
+    return out
+
+
 def nh_inv_diagonal(mesh, level, mat, caching, u, precision=64):
     dt = _dt(precision)
     u = np.ascontiguousarray(u, dtype=dt)

@@ -221,6 +221,27 @@ extern "C"
                       (const double *)nullptr, (double *)out, 1);
   }
 
+  // internal-force + inertia residual (assemble_residual without the
+  // traction term): out = -int P(F(u)) : grad v - rho int acc . v, with the
+  // constrained rows zero (mf_elasticity.h:1649-1908).  With acc = alpha_1 u
+  // its derivative along v is minus the tangent vmult (mf_nh_operator.h:
+  // 545-625) on the unconstrained rows.
+  int
+  or_nh_residual(const or_mesh_t *m, int level, const or_material_t *mat,
+                 const double *u, const double *acc, double *out)
+  {
+    MeshSpec          s    = to_spec(m);
+    Basis1D           b(s.degree, s.n_q);
+    const Box         box  = s.box(level);
+    const Material    M    = to_mat(mat);
+    const double      body[3] = {0, 0, 0};
+    std::fill(out, out + size_t(s.dim) * box.n_nodes, 0.0);
+    ResidualQ<double> q{&M, &box, &b, acc, body};
+    cell_loop(box, b, s.dim, u, out, q, false);
+    set_constrained_zero(box, s.dim, out);
+    return 0;
+  }
+
   // transfer between level (coarse) and level+1; op: 0 prolongate
   // (fine = P coarse), 1 restrict (coarse += P^T fine), 2 interpolate
   // (coarse = fine at coarse nodes)

@@ -1,0 +1,203 @@
+"""Operator-level checks of the CPU oracle that need no reference golden.
+
+The reference pins no vmult vector, no 3D case and no degree above 2, so the
+oracle's matrix-free operators are checked two more ways:
+
+* tangent consistency: the central finite difference of the oracle's
+  residual (mf_elasticity.h:1649-1908, internal force + inertia) along v
+  equals minus the tangent vmult (mf_nh_operator.h:545-625) for every
+  caching variant, within 1e-7 relative;
+* an assembled operator: element matrices integrated here in numpy with the
+  full (non-sum-factorized) Q_p basis on QGauss(p+1) and the closed-form
+  derivative of P = mu F - (mu - 2 lambda ln J) F^{-T}
+  (material.h:116-161), assembled densely with identity rows and zero
+  columns for the Dirichlet DoFs, give the same A x as the oracle's
+  matrix-free vmult within 1e-12; likewise the heat operator M + k dt K
+  (heat_transfer.h:236-250).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import workloads as W
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# --- numpy reference element (independent of the oracle's kernels) --------
+
+def lagrange_1d(nodes, x):
+    """Values and derivatives of the Lagrange basis on `nodes` at points x."""
+    n = len(nodes)
+    V = np.ones((n, len(x)))
+    dV = np.zeros((n, len(x)))
+    for i in range(n):
+        others = [j for j in range(n) if j != i]
+        for j in others:
+            V[i] *= (x - nodes[j]) / (nodes[i] - nodes[j])
+        for k in others:
+            term = np.ones(len(x)) / (nodes[i] - nodes[k])
+            for j in others:
+                if j != k:
+                    term = term * (x - nodes[j]) / (nodes[i] - nodes[j])
+            dV[i] += term
+    return V, dV
+
+
+def element_basis(p, h):
+    """phi[q, a] and physical grad[q, a, d] on the reference cell (lexicographic
+    local nodes, x fastest) at the tensor Gauss points; JxW[q]."""
+    nodes = W.gauss_lobatto(p)
+    xg, wg = np.polynomial.legendre.leggauss(p + 1)
+    xg, wg = (xg + 1) / 2, wg / 2
+    V, dV = lagrange_1d(nodes, xg)
+    N, Q = p + 1, p + 1
+    phi = np.einsum("aq,br,cs->qrsabc", V, V, V).reshape(Q ** 3, N ** 3)
+    gx = np.einsum("aq,br,cs->qrsabc", dV, V, V).reshape(Q ** 3, N ** 3) / h[0]
+    gy = np.einsum("aq,br,cs->qrsabc", V, dV, V).reshape(Q ** 3, N ** 3) / h[1]
+    gz = np.einsum("aq,br,cs->qrsabc", V, V, dV).reshape(Q ** 3, N ** 3) / h[2]
+    # the einsum orders (qz, qy, qx) slowest to fastest when reshaping with
+    # (q, r, s) = (x, y, z) first: reorder to x fastest for both q and a
+    def to_lex(t):
+        t = t.reshape(Q, Q, Q, N, N, N)            # qx, qy, qz, a, b, c
+        t = t.transpose(2, 1, 0, 5, 4, 3)          # qz, qy, qx, c, b, a
+        return t.reshape(Q ** 3, N ** 3)
+    phi, gx, gy, gz = map(to_lex, (phi, gx, gy, gz))
+    w = np.einsum("i,j,k->kji", wg, wg, wg).reshape(-1) * h[0] * h[1] * h[2]
+    return phi, np.stack([gx, gy, gz], axis=2), w
+
+
+def mesh_geometry(spec):
+    p = spec["degree"]
+    C = [spec["rep"][d] << spec["n_ref"] for d in range(3)]
+    Nn = [C[d] * p + 1 for d in range(3)]
+    h = [(spec["hi"][d] - spec["lo"][d]) / C[d] for d in range(3)]
+    return p, C, Nn, h
+
+
+def cell_nodes(p, C, Nn, cx, cy, cz):
+    a = np.arange(p + 1)
+    ix = cx * p + a[None, None, :]
+    iy = cy * p + a[None, :, None]
+    iz = cz * p + a[:, None, None]
+    return (ix + Nn[0] * (iy + Nn[1] * iz)).reshape(-1)
+
+
+def constrained_nodes(spec, Nn, comp):
+    """Nodes constrained in component `comp` (face bitmask semantics)."""
+    X = np.arange(Nn[0])[None, None, :] + 0 * np.zeros((Nn[2], Nn[1], 1), int)
+    Y = np.arange(Nn[1])[None, :, None] + 0 * np.zeros((Nn[2], 1, Nn[0]), int)
+    Z = np.arange(Nn[2])[:, None, None] + 0 * np.zeros((1, Nn[1], Nn[0]), int)
+    faces = [X == 0, X == Nn[0] - 1, Y == 0, Y == Nn[1] - 1, Z == 0, Z == Nn[2] - 1]
+    mask = np.zeros((Nn[2], Nn[1], Nn[0]), bool)
+    for f in range(6):
+        for bid, cmask in spec["dirichlet"]:
+            if spec["boundary_id"][f] == bid and (cmask >> comp) & 1:
+                mask |= faces[f]
+    return np.nonzero(mask.reshape(-1))[0]
+
+
+def apply_constraints(K, spec, Nn, nc):
+    n_nodes = Nn[0] * Nn[1] * Nn[2]
+    cons = np.concatenate([c * n_nodes + constrained_nodes(spec, Nn, c) for c in range(nc)])
+    K[cons, :] = 0.0
+    K[:, cons] = 0.0
+    K[cons, cons] = 1.0
+    return K
+
+
+def assembled_heat(spec, kdt):
+    p, C, Nn, h = mesh_geometry(spec)
+    phi, grad, w = element_basis(p, h)
+    Ke = np.einsum("q,qa,qb->ab", w, phi, phi) + kdt * np.einsum("q,qad,qbd->ab", w, grad, grad)
+    n = Nn[0] * Nn[1] * Nn[2]
+    K = np.zeros((n, n))
+    for cz in range(C[2]):
+        for cy in range(C[1]):
+            for cx in range(C[0]):
+                g = cell_nodes(p, C, Nn, cx, cy, cz)
+                K[np.ix_(g, g)] += Ke
+    return apply_constraints(K, spec, Nn, 1)
+
+
+def assembled_nh_tangent(spec, u, mu, nu, rho_alpha):
+    """Consistent tangent of P = mu F - (mu - 2 lambda ln J) F^{-T} plus
+    rho alpha_1 times the mass matrix."""
+    lam = 2 * mu * nu / (1 - 2 * nu)
+    p, C, Nn, h = mesh_geometry(spec)
+    phi, grad, w = element_basis(p, h)
+    n_nodes = Nn[0] * Nn[1] * Nn[2]
+    nd = p + 1
+    K = np.zeros((3 * n_nodes, 3 * n_nodes))
+    U = u.reshape(3, n_nodes)
+    M_e = np.einsum("q,qa,qb->ab", w, phi, phi)
+    I3 = np.eye(3)
+    for cz in range(C[2]):
+        for cy in range(C[1]):
+            for cx in range(C[0]):
+                g = cell_nodes(p, C, Nn, cx, cy, cz)
+                ue = U[:, g]                                   # (3, nd^3)
+                F = I3[None] + np.einsum("ia,qaJ->qiJ", ue, grad)
+                Finv = np.linalg.inv(F)
+                FiT = np.transpose(Finv, (0, 2, 1))
+                lnJ = np.log(np.linalg.det(F))
+                c = 2 * lam * lnJ - mu
+                A = (mu * np.einsum("ik,JL->iJkL", I3, I3)[None]
+                     + 2 * lam * np.einsum("qkL,qiJ->qiJkL", FiT, FiT)
+                     - c[:, None, None, None, None] * np.einsum("qiL,qkJ->qiJkL", FiT, FiT))
+                Ke = np.einsum("q,qaJ,qiJkL,qbL->iakb", w, grad, A, grad).reshape(3 * nd ** 3, 3 * nd ** 3)
+                Ke += rho_alpha * np.kron(I3, M_e)
+                dofs = np.concatenate([ci * n_nodes + g for ci in range(3)])
+                K[np.ix_(dofs, dofs)] += Ke
+    return apply_constraints(K, spec, Nn, 3)
+
+
+# --- the checks -------------------------------------------------------------
+
+ANISO = dict(rep=(2, 1, 1), length=(3.0, 1.0, 0.7))
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4])
+def test_heat_oracle_matches_assembled(degree):
+    spec = W.unit_cube_heat(degree, 0, rep=(2, 1, 1))
+    spec["hi"] = (1.0, 0.6, 0.45)
+    om = W.to_oracle_mesh(O, spec)
+    K = assembled_heat(spec, 0.1)
+    x = W.uniform_vector(K.shape[0], 11)
+    assert rel(O.heat_vmult(om, 0, 0.1, x), K @ x) < 1e-12
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3])
+@pytest.mark.parametrize("caching", ["scalar_referential", "tensor2", "tensor4", "tensor4_ns"])
+def test_nh_oracle_matches_assembled_tangent(degree, caching):
+    spec = W.cantilever(degree, 0, **ANISO)
+    u = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=3)
+    om = W.to_oracle_mesh(O, spec)
+    mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+    K = assembled_nh_tangent(spec, u, 0.5e6, 0.4, 1000.0 * mat.alpha_1)
+    x = W.uniform_vector(K.shape[0], 12)
+    assert rel(O.nh_vmult(om, 0, mat, caching, u, x), K @ x) < 1e-12, caching
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4])
+@pytest.mark.parametrize("caching", ["scalar_referential", "tensor2", "tensor4", "tensor4_ns"])
+def test_nh_tangent_is_derivative_of_residual(degree, caching):
+    spec = W.cantilever(degree, 0, **ANISO)
+    u = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=4)
+    om = W.to_oracle_mesh(O, spec)
+    mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+    n = len(u)
+    v = W.uniform_vector(n, 13)
+    # zero the Dirichlet DoFs of the direction (the tangent's constrained rows
+    # are the identity, the residual's are zero)
+    probe = O.nh_residual(om, 0, mat, np.ones(n) * 0.0, np.ones(n))
+    free = probe != 0.0
+    v[~free] = 0.0
+    eps = 1e-6
+    rp = O.nh_residual(om, 0, mat, u + eps * v, mat.alpha_1 * (u + eps * v))
+    rm = O.nh_residual(om, 0, mat, u - eps * v, mat.alpha_1 * (u - eps * v))
+    fd = (rp - rm) / (2 * eps)
+    Av = O.nh_vmult(om, 0, mat, caching, u, v)
+    assert rel(-fd[free], Av[free]) < 1e-7, caching
