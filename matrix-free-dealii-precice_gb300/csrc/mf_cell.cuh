@@ -222,6 +222,99 @@ namespace mfgpu
       buf[base + i * line_stride<N>(DIR)] = x[i];
   }
 
+  // Shared-memory layout of a cell's N^3 arrays: element (x,y,z) at
+  // x + SY y + SZ z, arrays of A = SZ N elements.  The natural layout is
+  // SY = N, SZ = N^2.
+  template <int N, int SY_, int SZ_>
+  struct Lay
+  {
+    static constexpr int SY = SY_, SZ = SZ_, A = SZ_ * N;
+    __device__ static __forceinline__ int
+    base(int dir, int a, int b)
+    {
+      return dir == 0 ? (a * SY + b * SZ) : (dir == 1 ? (a + b * SZ) : (a + b * SY));
+    }
+    __host__ __device__ static constexpr int
+    stride(int dir)
+    {
+      return dir == 0 ? 1 : (dir == 1 ? SY : SZ);
+    }
+    // quadrature point / node (a, b, k) with a along x, b along y, k along z
+    __device__ static __forceinline__ int
+    at(int a, int b, int k)
+    {
+      return a + b * SY + k * SZ;
+    }
+  };
+
+  // Padded layouts of the operator-application kernel, by N and element
+  // size: SY, SZ and the cell padding PAD (for 12 arrays per cell) were
+  // chosen by an exhaustive search that counts the shared-memory
+  // wavefronts of every warp's line accesses in all three sweep directions
+  // (thread (a,b) of cell c on line (a,b), the cells per block of
+  // apply_cells_per_block), at most 25 % (4-byte) / 2 % (8-byte) more
+  // shared memory.  Wavefronts per block and sweep step, natural -> padded:
+  //   4-byte: N=2 192->40, 3 189->135, 4 160->64, 5 115->100, 6 306->234, 7 329->266
+  //   8-byte: N=2 192->128, 3 360->324, 4 288 (natural), 5 200->180, 6 390->360, 7 357->343
+  template <int N, int ES>
+  struct ApplyPad
+  {
+    static constexpr int SY = N, SZ = N * N, PAD = 0;
+  };
+#define MF_PAD(n, es, sy, sz, pad)                                                                   \
+  template <>                                                                                       \
+  struct ApplyPad<n, es>                                                                            \
+  {                                                                                                 \
+    static constexpr int SY = sy, SZ = sz, PAD = pad;                                               \
+  };
+  MF_PAD(2, 4, 2, 4, 4)
+  MF_PAD(3, 4, 3, 9, 23)
+  MF_PAD(4, 4, 4, 19, 0)
+  MF_PAD(5, 4, 5, 25, 1)
+  MF_PAD(6, 4, 6, 39, 12)
+  MF_PAD(7, 4, 7, 56, 17)
+  MF_PAD(2, 8, 2, 4, 1)
+  MF_PAD(3, 8, 3, 9, 1)
+  MF_PAD(5, 8, 5, 25, 1)
+  MF_PAD(6, 8, 6, 36, 7)
+  MF_PAD(7, 8, 7, 49, 13)
+#undef MF_PAD
+
+  template <int N, typename T>
+  using ApplyLay = Lay<N, ApplyPad<N, int(sizeof(T))>::SY, ApplyPad<N, int(sizeof(T))>::SZ>;
+
+  // cell stride (elements) of NA arrays in the padded layout: the bank
+  // offset between consecutive cells is that of the searched 12-array cell
+  template <int N, typename T>
+  __host__ __device__ constexpr int
+  apply_cell_stride(int na)
+  {
+    constexpr int P   = sizeof(T) == 4 ? 32 : 16; // elements per bank period
+    constexpr int A   = ApplyLay<N, T>::A;
+    const int     off = 12 * A + ApplyPad<N, int(sizeof(T))>::PAD - na * A;
+    return na * A + ((off % P) + P) % P;
+  }
+
+  template <int N, class L, typename T, int DIR>
+  __device__ __forceinline__ void
+  load_line_l(const T *buf, int a, int b, T (&x)[N])
+  {
+    const int base = L::base(DIR, a, b);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      x[i] = buf[base + i * L::stride(DIR)];
+  }
+
+  template <int N, class L, typename T, int DIR>
+  __device__ __forceinline__ void
+  store_line_l(T *buf, int a, int b, const T (&x)[N])
+  {
+    const int base = L::base(DIR, a, b);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      buf[base + i * L::stride(DIR)] = x[i];
+  }
+
   // Cells per block for a degree / number of components / precision: aim
   // at 100-256 threads and <= ~100 KB of shared memory.
   template <int N, int NC, typename T>
@@ -255,11 +348,11 @@ namespace mfgpu
   // T): NC*(value + 3 gradients); the 1D sweeps use the gradient slots of
   // the component being evaluated or integrated as their scratch.  With
   // EVAL_U, 3*NC gradients of the linearisation + one scratch array.
-  template <int N, int NC, bool EVAL_U>
+  template <int N, int NC, bool EVAL_U, typename T>
   __host__ __device__ constexpr int
   apply_smem_per_cell()
   {
-    return (NC * 4 + (EVAL_U ? 3 * NC + 1 : 0)) * N * N * N;
+    return apply_cell_stride<N, T>(NC * 4 + (EVAL_U ? 3 * NC + 1 : 0));
   }
 
   // shared memory per cell (in elements of T): NC*(value + 3 gradients)
@@ -276,7 +369,7 @@ namespace mfgpu
   // scalar field whose z-columns are in registers.  Writes V, G0, G1, G2.
   // Requires a __syncthreads() before V/G are read by other threads.
   // ---------------------------------------------------------------------
-  template <int N, typename T>
+  template <int N, typename T, class L = Lay<N, N, N * N>>
   __device__ __forceinline__ void
   evaluate_field(const T *S, const T *D0, const T *D1, const T *D2,
                  const T (&col)[N], T *V, T *G0, T *G1, T *G2, T *T0, T *T1,
@@ -285,28 +378,28 @@ namespace mfgpu
     T x[N], y[N];
     // z interpolation in registers, store z-line (x=a, y=b)
     mat_apply<N>(S, col, y);
-    store_line<N, T, 2>(T0, a, b, y);
+    store_line_l<N, L, T, 2>(T0, a, b, y);
     __syncthreads();
     // y interpolation: line (x=a, z=b)
-    load_line<N, T, 1>(T0, a, b, x);
+    load_line_l<N, L, T, 1>(T0, a, b, x);
     mat_apply<N>(S, x, y);
-    store_line<N, T, 1>(T1, a, b, y);
+    store_line_l<N, L, T, 1>(T1, a, b, y);
     __syncthreads();
     // x interpolation: line (y=a, z=b) -> values; x-derivative from registers
-    load_line<N, T, 0>(T1, a, b, x);
+    load_line_l<N, L, T, 0>(T1, a, b, x);
     mat_apply<N>(S, x, y);
-    store_line<N, T, 0>(V, a, b, y); // values (also needed for the y/z derivatives)
+    store_line_l<N, L, T, 0>(V, a, b, y); // values (also needed for the y/z derivatives)
     (void)want_values;
     mat_apply<N>(D0, y, x);
-    store_line<N, T, 0>(G0, a, b, x);
+    store_line_l<N, L, T, 0>(G0, a, b, x);
     __syncthreads();
     // y and z derivatives of the values
-    load_line<N, T, 1>(V, a, b, x);
+    load_line_l<N, L, T, 1>(V, a, b, x);
     mat_apply<N>(D1, x, y);
-    store_line<N, T, 1>(G1, a, b, y);
-    load_line<N, T, 2>(V, a, b, x);
+    store_line_l<N, L, T, 1>(G1, a, b, y);
+    load_line_l<N, L, T, 2>(V, a, b, x);
     mat_apply<N>(D2, x, y);
-    store_line<N, T, 2>(G2, a, b, y);
+    store_line_l<N, L, T, 2>(G2, a, b, y);
   }
 
   template <int N, typename T>
@@ -323,7 +416,7 @@ namespace mfgpu
   // z-column (x=a, y=b) in registers.  V is overwritten.  Starts with a
   // __syncthreads() so that the submitted values of all threads are visible.
   // ---------------------------------------------------------------------
-  template <int N, typename T>
+  template <int N, typename T, class L = Lay<N, N, N * N>>
   __device__ __forceinline__ void
   integrate_field(const T *S, const T *D0, const T *D1, const T *D2, T *V,
                   const T *G0, const T *G1, const T *G2, T *T0, T *T1, int a,
@@ -334,37 +427,37 @@ namespace mfgpu
     if (has_gradients)
       {
         // z: V += D^T G2 on z-line (x=a,y=b)
-        load_line<N, T, 2>(G2, a, b, x);
+        load_line_l<N, L, T, 2>(G2, a, b, x);
         if (has_values)
-          load_line<N, T, 2>(V, a, b, y);
+          load_line_l<N, L, T, 2>(V, a, b, y);
         else
 #pragma unroll
           for (int i = 0; i < N; ++i)
             y[i] = zero<T>();
         mat_apply_t_add<N>(D2, x, y);
-        store_line<N, T, 2>(V, a, b, y);
+        store_line_l<N, L, T, 2>(V, a, b, y);
         __syncthreads();
         // y: V += D^T G1 on y-line (x=a,z=b)
-        load_line<N, T, 1>(G1, a, b, x);
-        load_line<N, T, 1>(V, a, b, y);
+        load_line_l<N, L, T, 1>(G1, a, b, x);
+        load_line_l<N, L, T, 1>(V, a, b, y);
         mat_apply_t_add<N>(D1, x, y);
-        store_line<N, T, 1>(V, a, b, y);
+        store_line_l<N, L, T, 1>(V, a, b, y);
         __syncthreads();
         // x: t = V + D^T G0 on x-line (y=a,z=b); then S^T
-        load_line<N, T, 0>(G0, a, b, x);
-        load_line<N, T, 0>(V, a, b, y);
+        load_line_l<N, L, T, 0>(G0, a, b, x);
+        load_line_l<N, L, T, 0>(V, a, b, y);
         mat_apply_t_add<N>(D0, x, y);
       }
     else
-      load_line<N, T, 0>(V, a, b, y);
+      load_line_l<N, L, T, 0>(V, a, b, y);
     mat_apply_t<N>(S, y, x);
-    store_line<N, T, 0>(T0, a, b, x);
+    store_line_l<N, L, T, 0>(T0, a, b, x);
     __syncthreads();
-    load_line<N, T, 1>(T0, a, b, x);
+    load_line_l<N, L, T, 1>(T0, a, b, x);
     mat_apply_t<N>(S, x, y);
-    store_line<N, T, 1>(T1, a, b, y);
+    store_line_l<N, L, T, 1>(T1, a, b, y);
     __syncthreads();
-    load_line<N, T, 2>(T1, a, b, x);
+    load_line_l<N, L, T, 2>(T1, a, b, x);
     mat_apply_t<N>(S, x, col);
   }
 
@@ -406,50 +499,49 @@ namespace mfgpu
   // Scratch: evaluate uses G1, G2; integrate uses G0, G1 (as in
   // evaluate_field / integrate_field).
   // ---------------------------------------------------------------------
-  template <int N, typename T>
+  template <int N, class L, typename T>
   __device__ __forceinline__ void
   evaluate_field_rg(const T *S, const T *D, const T (&col)[N], T *V, int a, int b)
   {
-    constexpr int N3 = N * N * N;
+    constexpr int A = L::A;
     T             x[N], y[N];
     // the nodal z-column goes through G0 so that the three interpolation
     // sweeps share one copy of the code: z G0 -> G1, y G1 -> G2, x G2 -> V
     // (the z pass reads only the column this thread wrote)
-    store_line<N, T, 2>(V + N3, a, b, col);
+    store_line_l<N, L, T, 2>(V + A, a, b, col);
 #pragma unroll 1
     for (int pass = 0; pass < 3; ++pass)
       {
-        const int dir = 2 - pass, base = line_base<N>(dir, a, b);
-        const int stride = dir == 0 ? 1 : (dir == 1 ? N : N * N);
-        load_line_rt<N>(V + (pass + 1) * N3, base, stride, x);
+        const int dir = 2 - pass, base = L::base(dir, a, b), stride = L::stride(dir);
+        load_line_rt<N>(V + (pass + 1) * A, base, stride, x);
         mat_apply<N>(S, x, y);
-        store_line_rt<N>(pass == 2 ? V : V + (pass + 2) * N3, base, stride, y);
+        store_line_rt<N>(pass == 2 ? V : V + (pass + 2) * A, base, stride, y);
         __syncthreads();
       }
     // derivatives G_d = D V along direction d
 #pragma unroll 1
     for (int d = 0; d < 3; ++d)
       {
-        const int base = line_base<N>(d, a, b), stride = d == 0 ? 1 : (d == 1 ? N : N * N);
+        const int base = L::base(d, a, b), stride = L::stride(d);
         load_line_rt<N>(V, base, stride, x);
         mat_apply<N>(D, x, y);
-        store_line_rt<N>(V + (d + 1) * N3, base, stride, y);
+        store_line_rt<N>(V + (d + 1) * A, base, stride, y);
       }
   }
 
-  template <int N, typename T>
+  template <int N, class L, typename T>
   __device__ __forceinline__ void
   integrate_field_rg(const T *S, const T *D, T *V, int a, int b, T (&col)[N])
   {
-    constexpr int N3 = N * N * N;
+    constexpr int A = L::A;
     T             x[N], y[N];
     __syncthreads();
     // V += D^T G_d along z, y, x
 #pragma unroll 1
     for (int d = 2; d >= 0; --d)
       {
-        const int base = line_base<N>(d, a, b), stride = d == 0 ? 1 : (d == 1 ? N : N * N);
-        load_line_rt<N>(V + (d + 1) * N3, base, stride, x);
+        const int base = L::base(d, a, b), stride = L::stride(d);
+        load_line_rt<N>(V + (d + 1) * A, base, stride, x);
         load_line_rt<N>(V, base, stride, y);
         mat_apply_t_add<N>(D, x, y);
         store_line_rt<N>(V, base, stride, y);
@@ -459,14 +551,14 @@ namespace mfgpu
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass)
       {
-        const int dir = pass, base = line_base<N>(dir, a, b), stride = dir == 0 ? 1 : N;
-        load_line_rt<N>(pass == 0 ? V : V + N3, base, stride, x);
+        const int dir = pass, base = L::base(dir, a, b), stride = L::stride(dir);
+        load_line_rt<N>(pass == 0 ? V : V + A, base, stride, x);
         mat_apply_t<N>(S, x, y);
-        store_line_rt<N>(V + (pass + 1) * N3, base, stride, y);
+        store_line_rt<N>(V + (pass + 1) * A, base, stride, y);
         __syncthreads();
       }
     // S^T along z into registers
-    load_line<N, T, 2>(V + 2 * N3, a, b, x);
+    load_line_l<N, L, T, 2>(V + 2 * A, a, b, x);
     mat_apply_t<N>(S, x, col);
   }
 
@@ -517,7 +609,9 @@ namespace mfgpu
     // ONE_CELL: one cell per block, for grids smaller than the GPU (coarse
     // levels), so that their cells spread over as many SMs as possible
     constexpr int CPB = ONE_CELL ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>();
-    constexpr int SPC = apply_smem_per_cell<N, NC, QOp::eval_u>();
+    constexpr int SPC = apply_smem_per_cell<N, NC, QOp::eval_u, T>();
+    using LA          = ApplyLay<N, T>; // padded shared-memory layout of the cell arrays
+    constexpr int AS  = LA::A;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
 
@@ -545,8 +639,8 @@ namespace mfgpu
                                    unsigned(g.C[1]) * (2 * iz + unsigned((g.color >> 2) & 1)));
       }
     T             *cb     = sm + lc * SPC;
-    T             *GU     = cb + NC * 4 * N3; // 3*NC*N3 if eval_u
-    T             *XU     = GU + 3 * NC * N3; // N3 scratch if eval_u
+    T             *GU     = cb + NC * 4 * AS; // 3*NC arrays if eval_u
+    T             *XU     = GU + 3 * NC * AS; // 1 scratch array if eval_u
 
     const unsigned cc  = active ? cell : 0u;
     const int      cx  = int(cc % unsigned(g.C[0]));
@@ -588,12 +682,12 @@ namespace mfgpu
         if (c + 1 < NC)
           gather(c + 1, next_col);
         // sweep scratch: the y and z gradient slots of this component
-        T *V = cb + c * 4 * N3;
+        T *V = cb + c * 4 * AS;
         if constexpr (QOp::ref_grad)
-          evaluate_field_rg<N>(sh.S, sh.Du, col, V, a, b);
+          evaluate_field_rg<N, LA>(sh.S, sh.Du, col, V, a, b);
         else
-          evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + N3, V + 2 * N3,
-                            V + 3 * N3, V + 2 * N3, V + 3 * N3, a, b, true);
+          evaluate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + AS, V + 2 * AS,
+                                   V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
       }
     if constexpr (QOp::eval_u)
       {
@@ -605,12 +699,12 @@ namespace mfgpu
 #pragma unroll
             for (int k = 0; k < N; ++k)
               col[k] = active ? op.ucell[(size_t(cc) * NC + c) * N3 + a + b * N + k * N2] : zero<T>();
-            // the values go to XU (scratch); GU + c*3*N3 holds the gradients
+            // the values go to XU (scratch); GU + c*3*AS holds the gradients
             // and serves as the sweep scratch
-            T *Gc = GU + c * 3 * N3;
+            T *Gc = GU + c * 3 * AS;
             __syncthreads();
-            evaluate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, XU, Gc, Gc + N3,
-                              Gc + 2 * N3, Gc + N3, Gc + 2 * N3, a, b, false);
+            evaluate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, XU, Gc, Gc + AS,
+                                     Gc + 2 * AS, Gc + AS, Gc + 2 * AS, a, b, false);
           }
       }
     __syncthreads();
@@ -627,17 +721,18 @@ namespace mfgpu
 #pragma unroll 1
         for (int k = 0; k < N; ++k)
           {
-            const int q = a + b * N + k * N2;
+            const int q  = a + b * N + k * N2; // global (cache) index
+            const int qs = LA::at(a, b, k);     // shared-memory index
             T         v[NC];
             T         H[NC][3];
 #pragma unroll
             for (int c = 0; c < NC; ++c)
               {
-                const T *V = cb + c * 4 * N3;
-                v[c]       = V[q];
+                const T *V = cb + c * 4 * AS;
+                v[c]       = V[qs];
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
-                  H[c][d] = V[(d + 1) * N3 + q];
+                  H[c][d] = V[(d + 1) * AS + qs];
               }
             T Hu[NC][3];
             if constexpr (QOp::eval_u)
@@ -646,7 +741,7 @@ namespace mfgpu
                 for (int c = 0; c < NC; ++c)
 #pragma unroll
                   for (int d = 0; d < 3; ++d)
-                    Hu[c][d] = GU[(c * 3 + d) * N3 + q];
+                    Hu[c][d] = GU[(c * 3 + d) * AS + qs];
               }
             const T jxw = wab * sh.w[k];
             if constexpr (QOp::prefetch)
@@ -658,11 +753,11 @@ namespace mfgpu
 #pragma unroll
                 for (int c = 0; c < NC; ++c)
                   {
-                    T *V = cb + c * 4 * N3;
-                    V[q] = v[c];
+                    T *V  = cb + c * 4 * AS;
+                    V[qs] = v[c];
 #pragma unroll
                     for (int d = 0; d < 3; ++d)
-                      V[(d + 1) * N3 + q] = H[c][d];
+                      V[(d + 1) * AS + qs] = H[c][d];
                   }
               }
             else
@@ -671,11 +766,11 @@ namespace mfgpu
 #pragma unroll
                 for (int c = 0; c < NC; ++c)
                   {
-                    T *V = cb + c * 4 * N3;
-                    V[q] = v[c] * jxw;
+                    T *V  = cb + c * 4 * AS;
+                    V[qs] = v[c] * jxw;
 #pragma unroll
                     for (int d = 0; d < 3; ++d)
-                      V[(d + 1) * N3 + q] = H[c][d] * jxw;
+                      V[(d + 1) * AS + qs] = H[c][d] * jxw;
                   }
               }
           }
@@ -685,14 +780,14 @@ namespace mfgpu
 #pragma unroll 1
     for (int c = 0; c < NC; ++c)
       {
-        T *V = cb + c * 4 * N3;
+        T *V = cb + c * 4 * AS;
         T  col[N];
         // sweep scratch: the x and y gradient slots (consumed by then)
         if constexpr (QOp::ref_grad)
-          integrate_field_rg<N>(sh.S, sh.Du, V, a, b, col);
+          integrate_field_rg<N, LA>(sh.S, sh.Du, V, a, b, col);
         else
-          integrate_field<N>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + N3, V + 2 * N3,
-                             V + 3 * N3, V + N3, V + 2 * N3, a, b, true, true, col);
+          integrate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + AS, V + 2 * AS,
+                                    V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
         if (active)
           {
 #pragma unroll

@@ -113,7 +113,7 @@ namespace mfgpu
               const TS *src, TS *dst, cudaStream_t s)
     {
       constexpr int CPB  = apply_cells_per_block<N, NC, TS, Op::eval_u>();
-      const size_t  smem = size_t(CPB) * apply_smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
+      const size_t  smem = size_t(CPB) * apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
       auto          k    = cell_apply_kernel<N, TS, T, NC, Op, CON>;
       cudaError_t   e    = prepare(k, smem);
       if (e != cudaSuccess)
@@ -143,7 +143,7 @@ namespace mfgpu
           {
             // fewer cells than SMs: one cell per block, on as many SMs
             auto         k1    = cell_apply_kernel<N, TS, T, NC, Op, CON, true>;
-            const size_t smem1 = apply_smem_per_cell<N, NC, Op::eval_u>() * sizeof(T);
+            const size_t smem1 = apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
             if ((e = prepare(k1, smem1)) != cudaSuccess)
               return e;
             k1<<<cells, N * N, smem1, s>>>(sh, cg, op, src, dst);

@@ -136,8 +136,9 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
     zero Dirichlet on x = 0, a seeded Gaussian source, one backward-Euler
     step.  Solid: cantilever 8k x k x k cells, k in solid_k, clamped at x = 0,
     a seeded traction of magnitude U(50, 150) on x = 8, one Newton-Newmark
-    step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG
-    (mg_precision=32) or the plain FP64 solver (mg_precision=64)."""
+    step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG with
+    the FP64 operators (fine and coarse level) in double-float arithmetic
+    (mg_precision=32), or the plain FP64 solver (mg_precision=64)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     reqs = []
     for i in range(n):
@@ -152,7 +153,8 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
             hp.dt, hp.n_steps = 0.1, 1
             hp.solver = mfgpu.solver_params("gmg", tol=tol, cheb_range=15.0, cheb_eig_its=10,
                                             mg_precision=mg_precision,
-                                            coarse_fp64=(mg_precision == 32))
+                                            coarse_fp64=(mg_precision == 32),
+                                            fp64_emulation=(mg_precision == 32))
             c, w, a = gaussian_source(int(rng.integers(1 << 30)))
             hp.n_gauss = 8
             for j in range(8):
@@ -170,7 +172,8 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
             sp.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
             sp.caching = b"referential_qp"
             sp.solver = mfgpu.solver_params("gmg", tol=tol, mg_precision=mg_precision,
-                                            coarse_fp64=(mg_precision == 32))
+                                            coarse_fp64=(mg_precision == 32),
+                                            fp64_emulation=(mg_precision == 32))
             sp.max_newton = 10
             sp.tol_f, sp.tol_f_abs, sp.tol_u, sp.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
             sp.dt, sp.n_steps = 0.01, 1
