@@ -88,6 +88,8 @@ long long mfgpu_launch_count(void);
 
 /* context: one CUDA device + one stream + reduction scratch */
 int mfgpu_context_create(int device, mfgpu_context **ctx);
+/* fails with MFGPU_ERR_STATE while operators, solid or heat drivers created
+ * on the context are alive: destroy those first */
 int mfgpu_context_destroy(mfgpu_context *ctx);
 int mfgpu_context_synchronize(mfgpu_context *ctx);
 /* the cudaStream_t of the context, as void* */

@@ -1,6 +1,7 @@
 // extern "C" entry points of libmfgpu.so (declared in include/mfgpu.h).
 // Every entry point converts exceptions into a status code and a
 // per-thread error message.
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -13,12 +14,13 @@ using namespace mfgpu;
 struct mfgpu_context
 {
   std::unique_ptr<Context> c;
+  std::atomic<int>         live{0}; // operators and drivers created on this context
 };
 
 struct mfgpu_operator
 {
   std::unique_ptr<Operator> op;
-  mfgpu_context            *ctx;
+  mfgpu_context            *ctx = nullptr;
   DevBuf                    hsrc, hdst; // device staging for the host-buffer vmult
   HostPipe                  pipe;       // streams of the overlapped host-buffer vmult
 };
@@ -26,11 +28,13 @@ struct mfgpu_operator
 struct mfgpu_solid
 {
   std::unique_ptr<SolidDriver> d;
+  mfgpu_context               *ctx = nullptr;
 };
 
 struct mfgpu_heat
 {
   std::unique_ptr<HeatDriver> d;
+  mfgpu_context              *ctx = nullptr;
 };
 
 static thread_local std::string g_last_error;
@@ -116,7 +120,12 @@ extern "C"
   int
   mfgpu_context_destroy(mfgpu_context *ctx)
   {
-    return guarded([&] { delete ctx; });
+    return guarded([&] {
+      if (ctx && ctx->live.load() > 0)
+        throw Error(ERR_STATE, "context still has " + std::to_string(ctx->live.load()) +
+                                 " operators/drivers: destroy them first");
+      delete ctx;
+    });
   }
 
   int
@@ -175,6 +184,7 @@ extern "C"
         {
           o->op  = make_heat(ctx->c.get(), to_mesh(*mesh), level, precision, constrained != 0);
           o->ctx = ctx;
+          ++ctx->live;
         }
       catch (...)
         {
@@ -235,6 +245,7 @@ extern "C"
         {
           o->op  = make_nh(ctx->c.get(), to_mesh(*mesh), level, precision, var);
           o->ctx = ctx;
+          ++ctx->live;
         }
       catch (...)
         {
@@ -475,6 +486,8 @@ extern "C"
     return guarded([&] {
       if (op && op->op)
         op->op->ctx->sync();
+      if (op && op->ctx)
+        --op->ctx->live;
       delete op;
     });
   }
@@ -544,6 +557,8 @@ extern "C"
           delete o;
           throw;
         }
+      o->ctx = ctx;
+      ++ctx->live;
       *s = o;
     });
   }
@@ -610,7 +625,11 @@ extern "C"
   int
   mfgpu_solid_destroy(mfgpu_solid *s)
   {
-    return guarded([&] { delete s; });
+    return guarded([&] {
+      if (s && s->ctx)
+        --s->ctx->live;
+      delete s;
+    });
   }
 
   int
@@ -630,6 +649,8 @@ extern "C"
           delete o;
           throw;
         }
+      o->ctx = ctx;
+      ++ctx->live;
       *h = o;
     });
   }
@@ -669,6 +690,10 @@ extern "C"
   int
   mfgpu_heat_destroy(mfgpu_heat *h)
   {
-    return guarded([&] { delete h; });
+    return guarded([&] {
+      if (h && h->ctx)
+        --h->ctx->live;
+      delete h;
+    });
   }
 }

@@ -793,11 +793,21 @@ namespace mfgpu
 #pragma unroll
             for (int k = 0; k < N; ++k)
               {
-                const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
-                if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
-                  continue;
+                const int    ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
                 const size_t node =
                   size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+                if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
+                  {
+                    // constrained row: dst += src, written by the one cell
+                    // that owns the node (local index < p in every
+                    // direction, or the last cell along it); no other cell
+                    // touches this row
+                    const bool owner = (a < g.p || cx == g.C[0] - 1) && (b < g.p || cy == g.C[1] - 1) &&
+                                       (k < g.p || cz == g.C[2] - 1);
+                    if (owner)
+                      dst[size_t(c) * g.n_nodes + node] += __ldg(src + size_t(c) * g.n_nodes + node);
+                    continue;
+                  }
                 TS *d = dst + size_t(c) * g.n_nodes + node;
                 if (g.color < 0)
                   atomicAdd(d, to_storage<TS, T>(col[k]));

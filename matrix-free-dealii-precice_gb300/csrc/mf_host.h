@@ -73,6 +73,7 @@ namespace mfgpu
     int          device = 0;
     cudaStream_t stream = nullptr;
     DevBuf       err;      // int error flags
+    DevBuf       ticket;   // unsigned: block counter of the single-launch reductions
     DevBuf       partial;  // reduction partials
     DevBuf       scalars;  // device scalars (double[32])
     double      *host_scalars = nullptr; // pinned
@@ -112,6 +113,8 @@ namespace mfgpu
   template <typename T> double vec_dot(Context &c, size_t n, const T *x, const T *y);
   template <typename T> void cg_update(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q, int rr_slot);
   template <typename T> void cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p);
+  // rec[3k..3k+2] = (slots[rz]/slots[pq], slots[rr], slots[rzn]/slots[rz])
+  void lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int k);
   template <typename T> void cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold);
   template <typename T> void cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b, const T *Ax, const T *dinv, T *x, T *xold);
   // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1
@@ -181,9 +184,10 @@ namespace mfgpu
     {
       return precision == 32 ? 4 : 8;
     }
-    // dst += A src (cell part, constrained rows untouched)
+    // dst += A src; constrained rows (constrained operators): dst += src
     void apply_cells(void *dst, const void *src) { apply_cells_range(dst, src, 0, 0, ctx->stream); }
-    // the same for the cells [c0, c1) (all cells if c1 <= c0) on stream s
+    // the same for the cells [c0, c1) (all cells if c1 <= c0) on stream s;
+    // a constrained row is added by the launch that contains its owner cell
     virtual void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) = 0;
     virtual void compute_diagonal() = 0;
     virtual size_t memory_consumption() const { return 0; }

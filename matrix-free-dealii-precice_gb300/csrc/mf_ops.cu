@@ -218,6 +218,8 @@ namespace mfgpu
     MF_CK(cudaSetDevice(dev));
     MF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     err.alloc(sizeof(int) * 4);
+    ticket.alloc(sizeof(unsigned) * 4);
+    MF_CK(cudaMemsetAsync(ticket.ptr, 0, ticket.bytes, stream));
     partial.alloc(sizeof(double) * RED_BLOCKS);
     scalars.alloc(sizeof(double) * 32);
     MF_CK(cudaMemsetAsync(err.ptr, 0, err.bytes, stream));
@@ -335,10 +337,9 @@ namespace mfgpu
   void
   vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot)
   {
-    k_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>());
-    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, c.partial.as<double>(),
-                                                    scalar_slots(c) + slot);
-    count_launch(2);
+    k_dot<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
+                                                    c.ticket.as<unsigned>(), scalar_slots(c) + slot);
+    count_launch();
     MF_CK(cudaGetLastError());
   }
   template <typename T>
@@ -357,12 +358,20 @@ namespace mfgpu
             T *r, const T *q, int rr_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
-                                                          c.partial.as<double>());
-    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, c.partial.as<double>(), s + rr_slot);
-    count_launch(2);
+    k_cg_update_rr<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+                                                             c.partial.as<double>(),
+                                                             c.ticket.as<unsigned>(), s + rr_slot);
+    count_launch();
     MF_CK(cudaGetLastError());
   }
+  void
+  lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int k)
+  {
+    k_lanczos_record<<<1, 1, 0, c.stream>>>(scalar_slots(c), rz, rzn, pq, rr, rec, k);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+
   template <typename T>
   void
   cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p)
@@ -525,15 +534,8 @@ namespace mfgpu
   void
   Operator::vmult(void *dst, const void *src)
   {
-    // dst = 0 except constrained rows dst = src, then dst += A src
+    // dst = 0, then dst += A src (constrained rows: dst += src, in the cell kernel)
     MF_CK(cudaMemsetAsync(dst, 0, m() * elem_size(), ctx->stream));
-    if (constrained)
-      {
-        if (precision == 32)
-          constrained_op<float>(*ctx, geom, nc, 0, (const float *)src, (float *)dst);
-        else
-          constrained_op<double>(*ctx, geom, nc, 0, (const double *)src, (double *)dst);
-      }
     apply_cells(dst, src);
   }
 
@@ -541,14 +543,8 @@ namespace mfgpu
   Operator::vmult_add(void *dst, const void *src)
   {
     apply_cells(dst, src);
-    if (constrained)
-      {
-        if (precision == 32)
-          constrained_op<float>(*ctx, geom, nc, 1, (const float *)src, (float *)dst);
-        else
-          constrained_op<double>(*ctx, geom, nc, 1, (const double *)src, (double *)dst);
-      }
   }
+
 
   void
   HostPipe::init()
@@ -718,14 +714,7 @@ namespace mfgpu
         apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s);
         MF_CK(cudaEventRecord(p.e_comp[k], s));
       }
-    if (constrained)
-      {
-        MF_CK(cudaStreamWaitEvent(s0, p.e_in[n - 1], 0));
-        if (precision == 32)
-          constrained_op<float>(*ctx, geom, nc, 0, (const float *)src_d, (float *)dst_d);
-        else
-          constrained_op<double>(*ctx, geom, nc, 0, (const double *)src_d, (double *)dst_d);
-      }
+    // (constrained rows are written by the cells that own them, in their slab)
     MF_CK(cudaEventRecord(p.e_con, s0));
     for (int k = 0; k < n; ++k)
       {

@@ -3,6 +3,7 @@
 // device.  The host only sequences kernel launches; vectors never leave
 // HBM.  Per CG iteration one 8-byte residual norm is read back for the
 // convergence test.
+#include <algorithm>
 #include <cmath>
 
 #include "mf_solvers.h"
@@ -76,6 +77,83 @@ namespace mfgpu
       }
     return st;
   }
+
+  template <typename T>
+  CGStats
+  cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol, int maxit,
+             int check)
+  {
+    CGStats      st;
+    const size_t n = A.size();
+    DevBuf       rb(n * sizeof(T)), zb(n * sizeof(T)), pb(n * sizeof(T)), qb(n * sizeof(T));
+    DevBuf       recb(sizeof(double) * 3 * size_t(std::max(maxit, 1)));
+    T *r = rb.as<T>(), *z = zb.as<T>(), *p = pb.as<T>(), *q = qb.as<T>();
+    double *rec = recb.as<double>();
+    A.vmult(r, x);
+    vec_axpby<T>(c, n, T(1), b, T(-1), r);
+    vec_dot_dev<T>(c, n, r, r, S_RR);
+    read_scalars(c, S_RR + 1);
+    double res = std::sqrt(c.host_scalars[S_RR]);
+    st.res0    = res;
+    st.res     = res;
+    if (!std::isfinite(res))
+      throw Error(ERR_NONFINITE, "CG: non-finite residual");
+    if (res <= tol)
+      {
+        st.converged = true;
+        return st;
+      }
+    if (P)
+      P->vmult(z, r);
+    else
+      vec_copy<T>(c, n, r, z);
+    vec_dot_dev<T>(c, n, r, z, S_RZ);
+    vec_copy<T>(c, n, z, p);
+    int                 rz = S_RZ, rzn = S_RZN;
+    std::vector<double> h;
+    for (int it0 = 1; it0 <= maxit; it0 += check)
+      {
+        const int it1 = std::min(maxit, it0 + check - 1);
+        for (int it = it0; it <= it1; ++it)
+          {
+            A.vmult(q, p);
+            vec_dot_dev<T>(c, n, p, q, S_PQ);
+            cg_update<T>(c, n, rz, S_PQ, x, p, r, q, S_RR);
+            if (P)
+              P->vmult(z, r);
+            else
+              vec_copy<T>(c, n, r, z);
+            vec_dot_dev<T>(c, n, r, z, rzn);
+            cg_direction<T>(c, n, rzn, rz, z, p);
+            lanczos_record(c, rz, rzn, S_PQ, S_RR, rec, it - 1);
+            std::swap(rz, rzn);
+          }
+        const int cnt = it1 - it0 + 1;
+        h.resize(3 * size_t(cnt));
+        MF_CK(cudaMemcpyAsync(h.data(), rec + 3 * size_t(it0 - 1), sizeof(double) * h.size(),
+                              cudaMemcpyDeviceToHost, c.stream));
+        MF_CK(cudaStreamSynchronize(c.stream));
+        for (int j = 0; j < cnt; ++j)
+          {
+            res    = std::sqrt(h[3 * j + 1]);
+            st.its = it0 + j;
+            st.res = res;
+            st.alpha.push_back(h[3 * j]);
+            if (!std::isfinite(res))
+              throw Error(ERR_NONFINITE, "CG: non-finite residual");
+            if (res <= tol)
+              {
+                st.converged = true;
+                return st;
+              }
+            st.beta.push_back(h[3 * j + 2]);
+          }
+      }
+    return st;
+  }
+
+  template CGStats cg_lanczos<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, int);
+  template CGStats cg_lanczos<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, int);
 
   template CGStats cg_solve<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, bool, bool);
   template CGStats cg_solve<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, bool, bool);
@@ -162,7 +240,7 @@ namespace mfgpu
     JacobiPre<T> P;
     P.ctx     = ctx;
     P.A       = A;
-    CGStats st = cg_solve<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, true, false);
+    CGStats st = cg_lanczos<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations);
     const size_t k = st.alpha.size();
     if (k == 0)
       lambda_min = lambda_max = 1.0;
@@ -301,6 +379,13 @@ namespace mfgpu
         c64_sol.alloc(coarse64->m() * sizeof(double));
         c64_def.alloc(coarse64->m() * sizeof(double));
       }
+    // eigenvalue bounds of every smoother now (PreconditionChebyshev
+    // estimates on its first vmult; here setup carries that cost)
+    for (int l = 0; l < L; ++l)
+      if (l > 0 || !coarse64)
+        smoothers[l].estimate();
+    if (coarse64)
+      coarse_cheb64.estimate();
   }
 
   template <typename T>

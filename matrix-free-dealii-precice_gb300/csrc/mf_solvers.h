@@ -59,6 +59,15 @@ namespace mfgpu
                    double tol, int maxit, bool record = false,
                    bool fixed_iterations = false);
 
+  // CG as used for the Chebyshev eigenvalue estimate: the same iterates as
+  // cg_solve(record = true), with the Lanczos coefficients recorded on the
+  // device and the convergence test made every `check` iterations (the
+  // coefficients of iterations past convergence are discarded), so the
+  // host waits once per `check` iterations instead of twice per iteration
+  template <typename T>
+  CGStats cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol,
+                     int maxit, int check = 8);
+
   template <typename T>
   struct Chebyshev
   {

@@ -98,42 +98,55 @@ namespace mfgpu
     return v;
   }
 
-  // partial[block] = sum x.y over the block's grid-stride share
+  // Single-launch reduction: every block stores its partial; the block that
+  // finishes last (ticket) sums all partials in a fixed order (the same
+  // order for the same partials, so the result is deterministic) into *out and
+  // resets the ticket.
+  __device__ __forceinline__ void
+  finish_partials(double s, double *__restrict__ partial, unsigned *ticket,
+                  double *__restrict__ out)
+  {
+    __shared__ bool last;
+    if (threadIdx.x == 0)
+      {
+        partial[blockIdx.x] = s;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+      }
+    __syncthreads();
+    if (!last)
+      return;
+    __threadfence();
+    double r = 0;
+    for (int i = threadIdx.x; i < int(gridDim.x); i += blockDim.x)
+      r += __ldcg(partial + i);
+    r = block_sum(r);
+    if (threadIdx.x == 0)
+      {
+        *out    = r;
+        *ticket = 0u;
+      }
+  }
+
   template <typename T>
   __global__ void __launch_bounds__(RED_THREADS)
-  k_dot_partial(size_t n, const T *__restrict__ x, const T *__restrict__ y,
-                double *__restrict__ partial)
+  k_dot(size_t n, const T *__restrict__ x, const T *__restrict__ y,
+        double *__restrict__ partial, unsigned *ticket, double *__restrict__ out)
   {
     double s = 0;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       s += double(x[i]) * double(y[i]);
-    s = block_sum(s);
-    if (threadIdx.x == 0)
-      partial[blockIdx.x] = s;
+    finish_partials(block_sum(s), partial, ticket, out);
   }
 
-  // out[slot] = sum of nparts partials (fixed order: deterministic)
-  static __global__ void __launch_bounds__(RED_THREADS)
-  k_reduce_final(int nparts, const double *__restrict__ partial,
-                 double *__restrict__ out)
-  {
-    double s = 0;
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
-      s += partial[i];
-    s = block_sum(s);
-    if (threadIdx.x == 0)
-      *out = s;
-  }
-
-  // CG update: x += alpha p ; r -= alpha q ; partial |r|^2
-  // alpha = num/den read from device scalars
+  // CG update x += alpha p, r -= alpha q with alpha = num/den, and |r|^2
   template <typename T>
   __global__ void __launch_bounds__(RED_THREADS)
-  k_cg_update(size_t n, const double *__restrict__ num,
-              const double *__restrict__ den, T *__restrict__ x,
-              const T *__restrict__ p, T *__restrict__ r,
-              const T *__restrict__ q, double *__restrict__ partial)
+  k_cg_update_rr(size_t n, const double *__restrict__ num, const double *__restrict__ den,
+                 T *__restrict__ x, const T *__restrict__ p, T *__restrict__ r,
+                 const T *__restrict__ q, double *__restrict__ partial, unsigned *ticket,
+                 double *__restrict__ out)
   {
     const T alpha = T(*num / *den);
     double  s     = 0;
@@ -145,9 +158,7 @@ namespace mfgpu
         r[i]       = rr;
         s += double(rr) * double(rr);
       }
-    s = block_sum(s);
-    if (threadIdx.x == 0)
-      partial[blockIdx.x] = s;
+    finish_partials(block_sum(s), partial, ticket, out);
   }
 
   // p = z + beta p,  beta = num/den
@@ -161,6 +172,16 @@ namespace mfgpu
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       p[i] = z[i] + beta * p[i];
+  }
+
+  // Lanczos record of CG iteration k: alpha = rz/pq, |r|^2, beta = rzn/rz
+  static __global__ void
+  k_lanczos_record(const double *__restrict__ s, int rz, int rzn, int pq, int rr,
+                   double *__restrict__ rec, int k)
+  {
+    rec[3 * k]     = s[rz] / s[pq];
+    rec[3 * k + 1] = s[rr];
+    rec[3 * k + 2] = s[rzn] / s[rz];
   }
 
   // Chebyshev step (PreconditionChebyshev vector updates):

@@ -12,6 +12,7 @@ fallback: without the built library or a GPU the calls fail.
 """
 import ctypes as C
 import os
+import weakref
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmfgpu.so")
@@ -166,7 +167,11 @@ class Context:
 
     def __init__(self, device=0):
         self.h = C.c_void_p()
+        self._children = weakref.WeakSet()  # objects to release before the context
         _check(lib().mfgpu_context_create(device, C.byref(self.h)))
+
+    def _adopt(self, obj):
+        self._children.add(obj)
 
     def synchronize(self):
         _check(lib().mfgpu_context_synchronize(self.h))
@@ -181,7 +186,10 @@ class Context:
         return s.value
 
     def close(self):
+        """Release the context; operators and drivers created on it first."""
         if self.h:
+            for child in list(self._children):
+                child.close()
             lib().mfgpu_context_destroy(self.h)
             self.h = None
 
@@ -196,6 +204,7 @@ class _Operator:
     def __init__(self, ctx):
         self.ctx = ctx
         self.h = C.c_void_p()
+        ctx._adopt(self)
 
     def m(self):
         v = C.c_size_t()
@@ -371,6 +380,7 @@ class Solid:
         self.ctx = ctx
         self.params = params
         self.h = C.c_void_p()
+        ctx._adopt(self)
         _check(lib().mfgpu_solid_create(ctx.h, C.byref(params), C.byref(self.h)))
 
     def run(self):
@@ -415,6 +425,7 @@ class Heat:
         self.ctx = ctx
         self.params = params
         self.h = C.c_void_p()
+        ctx._adopt(self)
         _check(lib().mfgpu_heat_create(ctx.h, C.byref(params), C.byref(self.h)))
 
     def run(self):

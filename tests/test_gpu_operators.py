@@ -382,6 +382,17 @@ def test_colored_scatter(ctx, kind, degree, n_ref, rep):
     assert np.array_equal(out_h, outs[0])
 
 
+def test_context_outlives_its_operators():
+    """A context with live operators refuses to be destroyed (ERR_STATE);
+    the Python wrapper releases its operators first."""
+    c = mfgpu.Context(0)
+    spec = small_heat(1)
+    op = mfgpu.LaplaceOperator(c, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    assert mfgpu.lib().mfgpu_context_destroy(c.h) == 6
+    c.close()
+    assert op.h is None and c.h is None
+
+
 def test_set_host_chunks_rejects(ctx):
     spec = small_heat(2)
     op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
