@@ -113,8 +113,9 @@ namespace mfgpu
   template <typename T> double vec_dot(Context &c, size_t n, const T *x, const T *y);
   template <typename T> void cg_update(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q, int rr_slot);
   template <typename T> void cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p);
-  // rec[3k..3k+2] = (slots[rz]/slots[pq], slots[rr], slots[rzn]/slots[rz])
-  void lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int k);
+  // rec[3k..3k+2] = (slots[rz]/slots[pq], slots[rr], slots[rzn]/slots[rz]),
+  // k = (*counter)++ on the device
+  void lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int *counter);
   template <typename T> void cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold);
   template <typename T> void cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b, const T *Ax, const T *dinv, T *x, T *xold);
   // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1

@@ -272,6 +272,16 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // vector kernels
   // ---------------------------------------------------------------------
+  // blocks of a single-launch reduction over n entries: at least 8 entries
+  // per thread, at most RED_BLOCKS (the partials buffer); fixed per n, so a
+  // reduction over the same vector is reproducible
+  static inline unsigned
+  red_grid(size_t n)
+  {
+    const size_t per = size_t(RED_THREADS) * 8;
+    return unsigned(std::max<size_t>(1, std::min<size_t>(RED_BLOCKS, (n + per - 1) / per)));
+  }
+
   static inline unsigned
   grid_for(size_t n, int threads = 256)
   {
@@ -337,7 +347,7 @@ namespace mfgpu
   void
   vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot)
   {
-    k_dot<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
+    k_dot<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
                                                     c.ticket.as<unsigned>(), scalar_slots(c) + slot);
     count_launch();
     MF_CK(cudaGetLastError());
@@ -358,16 +368,16 @@ namespace mfgpu
             T *r, const T *q, int rr_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update_rr<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+    k_cg_update_rr<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
                                                              c.partial.as<double>(),
                                                              c.ticket.as<unsigned>(), s + rr_slot);
     count_launch();
     MF_CK(cudaGetLastError());
   }
   void
-  lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int k)
+  lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int *counter)
   {
-    k_lanczos_record<<<1, 1, 0, c.stream>>>(scalar_slots(c), rz, rzn, pq, rr, rec, k);
+    k_lanczos_record<<<1, 1, 0, c.stream>>>(scalar_slots(c), rz, rzn, pq, rr, rec, counter);
     count_launch();
     MF_CK(cudaGetLastError());
   }

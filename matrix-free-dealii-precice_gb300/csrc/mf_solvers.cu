@@ -111,24 +111,78 @@ namespace mfgpu
     vec_copy<T>(c, n, z, p);
     int                 rz = S_RZ, rzn = S_RZN;
     std::vector<double> h;
-    for (int it0 = 1; it0 <= maxit; it0 += check)
+    DevBuf              cntb(sizeof(int));
+    int                *counter = cntb.as<int>();
+    MF_CK(cudaMemsetAsync(counter, 0, sizeof(int), c.stream));
+    auto iteration = [&]() {
+      A.vmult(q, p);
+      vec_dot_dev<T>(c, n, p, q, S_PQ);
+      cg_update<T>(c, n, rz, S_PQ, x, p, r, q, S_RR);
+      if (P)
+        P->vmult(z, r);
+      else
+        vec_copy<T>(c, n, r, z);
+      vec_dot_dev<T>(c, n, r, z, rzn);
+      cg_direction<T>(c, n, rzn, rz, z, p);
+      lanczos_record(c, rz, rzn, S_PQ, S_RR, rec, counter);
+      std::swap(rz, rzn);
+    };
+    // a full batch (an even number of iterations, so the slot roles repeat)
+    // is the same work every time: the second one is captured into a CUDA
+    // graph and the later ones replay it
+    cudaGraphExec_t gx      = nullptr;
+    long long       gx_lnch = 0;
+    int             batch   = 0;
+    struct GraphGuard
+    {
+      cudaGraphExec_t &g;
+      ~GraphGuard()
       {
-        const int it1 = std::min(maxit, it0 + check - 1);
-        for (int it = it0; it <= it1; ++it)
+        if (g)
+          cudaGraphExecDestroy(g);
+      }
+    } guard{gx};
+    for (int it0 = 1; it0 <= maxit; it0 += check, ++batch)
+      {
+        const int it1  = std::min(maxit, it0 + check - 1);
+        const int cnt  = it1 - it0 + 1;
+        const bool full = cnt == check && check % 2 == 0;
+        if (full && gx)
           {
-            A.vmult(q, p);
-            vec_dot_dev<T>(c, n, p, q, S_PQ);
-            cg_update<T>(c, n, rz, S_PQ, x, p, r, q, S_RR);
-            if (P)
-              P->vmult(z, r);
-            else
-              vec_copy<T>(c, n, r, z);
-            vec_dot_dev<T>(c, n, r, z, rzn);
-            cg_direction<T>(c, n, rzn, rz, z, p);
-            lanczos_record(c, rz, rzn, S_PQ, S_RR, rec, it - 1);
-            std::swap(rz, rzn);
+            MF_CK(cudaGraphLaunch(gx, c.stream));
+            count_launch(int(gx_lnch));
           }
-        const int cnt = it1 - it0 + 1;
+        else if (full && batch == 1)
+          {
+            const long long l0 = launch_count();
+            MF_CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            cudaGraph_t g = nullptr;
+            try
+              {
+                for (int j = 0; j < cnt; ++j)
+                  iteration();
+              }
+            catch (...)
+              {
+                cudaStreamEndCapture(c.stream, &g);
+                if (g)
+                  cudaGraphDestroy(g);
+                throw;
+              }
+            MF_CK(cudaStreamEndCapture(c.stream, &g));
+            const cudaError_t e = cudaGraphInstantiate(&gx, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess)
+              {
+                gx = nullptr;
+                MF_CK(e);
+              }
+            gx_lnch = launch_count() - l0;
+            MF_CK(cudaGraphLaunch(gx, c.stream));
+          }
+        else
+          for (int j = 0; j < cnt; ++j)
+            iteration();
         h.resize(3 * size_t(cnt));
         MF_CK(cudaMemcpyAsync(h.data(), rec + 3 * size_t(it0 - 1), sizeof(double) * h.size(),
                               cudaMemcpyDeviceToHost, c.stream));

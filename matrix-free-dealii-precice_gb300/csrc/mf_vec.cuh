@@ -174,11 +174,13 @@ namespace mfgpu
       p[i] = z[i] + beta * p[i];
   }
 
-  // Lanczos record of CG iteration k: alpha = rz/pq, |r|^2, beta = rzn/rz
+  // Lanczos record of the next CG iteration (index from a device counter):
+  // alpha = rz/pq, |r|^2, beta = rzn/rz
   static __global__ void
   k_lanczos_record(const double *__restrict__ s, int rz, int rzn, int pq, int rr,
-                   double *__restrict__ rec, int k)
+                   double *__restrict__ rec, int *__restrict__ counter)
   {
+    const int k    = (*counter)++;
     rec[3 * k]     = s[rz] / s[pq];
     rec[3 * k + 1] = s[rr];
     rec[3 * k + 2] = s[rzn] / s[rz];
