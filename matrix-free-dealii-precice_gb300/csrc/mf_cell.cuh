@@ -683,8 +683,13 @@ namespace mfgpu
           gather(c + 1, next_col);
         // sweep scratch: the y and z gradient slots of this component
         T *V = cb + c * 4 * AS;
-        if constexpr (QOp::ref_grad)
+        // reference gradients: loops over the directions in double-float
+        // (instruction-cache bound), unrolled compile-time strides otherwise
+        if constexpr (QOp::ref_grad && std::is_same<T, df64>::value)
           evaluate_field_rg<N, LA>(sh.S, sh.Du, col, V, a, b);
+        else if constexpr (QOp::ref_grad)
+          evaluate_field<N, T, LA>(sh.S, sh.Du, sh.Du, sh.Du, col, V, V + AS, V + 2 * AS,
+                                   V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
         else
           evaluate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + AS, V + 2 * AS,
                                    V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
@@ -783,8 +788,11 @@ namespace mfgpu
         T *V = cb + c * 4 * AS;
         T  col[N];
         // sweep scratch: the x and y gradient slots (consumed by then)
-        if constexpr (QOp::ref_grad)
+        if constexpr (QOp::ref_grad && std::is_same<T, df64>::value)
           integrate_field_rg<N, LA>(sh.S, sh.Du, V, a, b, col);
+        else if constexpr (QOp::ref_grad)
+          integrate_field<N, T, LA>(sh.S, sh.Du, sh.Du, sh.Du, V, V + AS, V + 2 * AS,
+                                    V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
         else
           integrate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + AS, V + 2 * AS,
                                     V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
