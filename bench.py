@@ -438,6 +438,22 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
     srv.close()
     lat = np.array([r.latency_seconds for r in res])
     errors = sum(1 for r in res if r.status != 0)
+    # the same mixed-precision requests one at a time (first 100), closed loop:
+    # what the concurrent solves on per-worker streams add
+    srv = mfgpu.Server(0, 1, 0.8)
+    t0 = time.perf_counter()
+    ids = [srv.submit(r) for r in reqs[:100]]
+    for i in ids:
+        srv.wait(i)
+    one = 100 / (time.perf_counter() - t0)
+    srv.close()
+    srv = mfgpu.Server(0, workers, 0.8)
+    t0 = time.perf_counter()
+    ids = [srv.submit(r) for r in reqs[:100]]
+    for i in ids:
+        srv.wait(i)
+    many = 100 / (time.perf_counter() - t0)
+    srv.close()
     # baseline: one at a time, plain FP64 solver
     base_reqs = W.serving_requests(mfgpu, n_requests, seed=seed, mg_precision=64)
     srv = mfgpu.Server(0, 1, 0.8)
@@ -452,6 +468,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
             "solves_per_s": n_requests / span, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)), "max_concurrent": max_running,
             "errors": errors,
+            "closed_loop_first100_per_s": {"1_worker": one, f"{workers}_workers": many},
             "baseline_fp64_one_at_a_time": {"solves_per_s": n_requests / bspan,
                                             "service_p50_s": float(np.percentile(brun, 50)),
                                             "service_p99_s": float(np.percentile(brun, 99)),
