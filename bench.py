@@ -152,6 +152,21 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def profile_pipes():
+    """FP32-pipe utilisation of the double-float cell kernel from the
+    committed ncu summary of this workload (None when absent)."""
+    path = os.path.join(ROOT, "profiles", "nh_vmult_q4_cantilever_ncu.txt")
+    out = {}
+    try:
+        for line in open(path):
+            for key in ("pipe_fma_pct", "issue_active_pct", "pipe_fp64_pct", "dram_throughput_pct_of_peak"):
+                if line.startswith(key + ":"):
+                    out[key] = float(line.split(":", 1)[1].split()[0]) / 100.0
+    except OSError:
+        return None
+    return out or None
+
+
 def profile_traffic():
     """dram bytes per launch of the vmult cell kernel, from the committed
     ncu summary of this workload (None when absent)."""
@@ -666,6 +681,11 @@ def main():
                      "kernel_ms": k_ms, "bytes_alg_per_launch": b_alg},
         "fp64": {"alg_tflops": f_alg / (k_ms * 1e-3) / 1e12,
                  "note": "FP64 pipe of GB300 is ~1.25 TFLOP/s nominal: the FP64 operator is pipe-bound"},
+        "compute_roofline": {"bound": "FP32 pipe issue (double-float arithmetic)",
+                             "ncu": profile_pipes(),
+                             "source": "profiles/nh_vmult_q4_cantilever_ncu.txt",
+                             "note": "the binding roof of this kernel; the HBM fraction above is "
+                                     "the fixed B_alg convention"},
         "clocks": clk,
         "gpu_launches": launches,
         "wall_ms_per_step": t_wall / K * 1e3,
