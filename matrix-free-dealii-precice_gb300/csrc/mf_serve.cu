@@ -15,6 +15,7 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <string>
 #include <thread>
 
 #include "../../include/mfgpu.h"
@@ -98,14 +99,17 @@ namespace mfgpu
     loop()
     {
       cudaSetDevice(device);
+      // a worker without a context still takes jobs and fails them with the
+      // reason, so that no wait() blocks on a request nobody will run
       std::unique_ptr<Context> ctx;
+      std::string              ctx_error;
       try
         {
           ctx.reset(new Context(device));
         }
-      catch (...)
+      catch (const std::exception &e)
         {
-          return;
+          ctx_error = e.what();
         }
       for (;;)
         {
@@ -127,7 +131,14 @@ namespace mfgpu
             max_running = std::max(max_running, running);
             job->t_start = clock_t_::now();
           }
-          run(*ctx, *job);
+          if (ctx)
+            run(*ctx, *job);
+          else
+            {
+              job->res.status = MFGPU_ERR_CUDA;
+              std::strncpy(job->res.message, ("worker has no CUDA context: " + ctx_error).c_str(),
+                           sizeof(job->res.message) - 1);
+            }
           {
             std::lock_guard<std::mutex> l(mu);
             job->t_end = clock_t_::now();

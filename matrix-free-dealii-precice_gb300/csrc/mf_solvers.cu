@@ -378,7 +378,12 @@ namespace mfgpu
   Multigrid<T>::drop_graph()
   {
     if (gexec)
-      cudaGraphExecDestroy(gexec);
+      {
+        // a replay may still be running on the context's stream
+        if (ctx)
+          cudaStreamSynchronize(ctx->stream);
+        cudaGraphExecDestroy(gexec);
+      }
     gexec      = nullptr;
     g_dst      = nullptr;
     g_src      = nullptr;
