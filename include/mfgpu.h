@@ -65,6 +65,8 @@ typedef struct mfgpu_mesh
   int      n_dirichlet;       /* entries used in the two lists below */
   int      dirichlet_id[8];   /* boundary ids with Dirichlet data     */
   unsigned dirichlet_mask[8]; /* component mask per boundary id       */
+  int      dim;               /* 2 or 3 (0 means 3); in 2D the z
+                                 entries and faces z-, z+ are unused  */
 } mfgpu_mesh;
 
 /* Material_Compressible_Neo_Hook_One_Field(mu, nu, rho, alpha_1,

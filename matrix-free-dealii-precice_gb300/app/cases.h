@@ -45,9 +45,29 @@ namespace mfapp
   };
 
   inline SolidCase
-  make_solid_case(const std::string &name, mfgpu_mesh &m)
+  make_solid_case(const std::string &name, mfgpu_mesh &m, int dim = 3)
   {
     SolidCase c;
+    m.dim = dim;
+    if (name == "turek_hron" && dim == 2)
+      {
+        // the reference's 2D flap: clamped short side (id 1), interface (id
+        // 11) on the other three sides
+        const double lo[3] = {0.24899, 0.19, 0.0}, hi[3] = {0.6, 0.21, 1.0};
+        const int    rep[3] = {5, 1, 1};
+        set_box(m, lo, hi, rep);
+        const int ids[6] = {1, 11, 11, 11, -1, -1};
+        std::memcpy(m.boundary_id, ids, sizeof(ids));
+        m.n_dirichlet       = 1;
+        m.dirichlet_id[0]   = 1;
+        m.dirichlet_mask[0] = 0b11;
+        c.body[1]           = -0.5;
+        c.traction[1]       = -4.0;
+        return c;
+      }
+    if (dim == 2)
+      throw std::runtime_error("unknown two-dimensional elasticity test case '" + name +
+                               "' (available: turek_hron)");
     if (name == "turek_hron")
       {
         const double lo[3] = {0.24899, 0.19, -0.005}, hi[3] = {0.6, 0.21, 0.005};
@@ -82,14 +102,15 @@ namespace mfapp
   }
 
   inline void
-  make_heat_case(const std::string &name, mfgpu_heat_params &p)
+  make_heat_case(const std::string &name, mfgpu_heat_params &p, int dim = 3)
   {
     const double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
     const int    rep[3] = {1, 1, 1};
     set_box(p.mesh, lo, hi, rep);
+    p.mesh.dim = dim;
     if (name == "partitioned_heat_dirichlet")
       {
-        for (int f = 0; f < 6; ++f)
+        for (int f = 0; f < 2 * dim; ++f)
           p.mesh.boundary_id[f] = 1;
         p.mesh.n_dirichlet       = 1;
         p.mesh.dirichlet_id[0]   = 1;

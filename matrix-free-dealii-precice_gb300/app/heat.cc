@@ -86,32 +86,37 @@ l2_error(const mfgpu_mesh &m, const std::vector<double> &u, double alpha, double
             v *= (xq[q] - gl[j]) / (gl[i] - gl[j]);
         S[q * N + i] = v;
       }
-  int C[3], Nn[3];
-  double h[3];
+  // 2D: one node plane, one "quadrature point" of weight 1 along z
+  const bool two = m.dim == 2;
+  const int  Nz  = two ? 1 : N;
+  int        C[3], Nn[3];
+  double     h[3];
   for (int d = 0; d < 3; ++d)
     {
-      C[d]  = m.repetitions[d] << m.n_refinements;
-      Nn[d] = C[d] * p + 1;
-      h[d]  = (m.upper[d] - m.lower[d]) / C[d];
+      C[d]  = (two && d == 2) ? 1 : (m.repetitions[d] << m.n_refinements);
+      Nn[d] = (two && d == 2) ? 1 : C[d] * p + 1;
+      h[d]  = (two && d == 2) ? 1.0 : (m.upper[d] - m.lower[d]) / C[d];
     }
+  auto Sz = [&](int q, int k) { return two ? 1.0 : S[q * N + k]; };
+  auto wz = [&](int q) { return two ? 1.0 : wq[q]; };
   double err = 0;
   for (int cz = 0; cz < C[2]; ++cz)
     for (int cy = 0; cy < C[1]; ++cy)
       for (int cx = 0; cx < C[0]; ++cx)
-        for (int qz = 0; qz < N; ++qz)
+        for (int qz = 0; qz < Nz; ++qz)
           for (int qy = 0; qy < N; ++qy)
             for (int qx = 0; qx < N; ++qx)
               {
                 double v = 0;
-                for (int k = 0; k < N; ++k)
+                for (int k = 0; k < Nz; ++k)
                   for (int j = 0; j < N; ++j)
                     for (int i = 0; i < N; ++i)
-                      v += S[qx * N + i] * S[qy * N + j] * S[qz * N + k] *
+                      v += S[qx * N + i] * S[qy * N + j] * Sz(qz, k) *
                            u[size_t(cx * p + i) + size_t(Nn[0]) * (size_t(cy * p + j) + size_t(Nn[1]) * (cz * p + k))];
                 const double x = m.lower[0] + (cx + xq[qx]) * h[0];
                 const double y = m.lower[1] + (cy + xq[qy]) * h[1];
                 const double e = 1 + x * x + alpha * y * y + beta * t - v;
-                err += e * e * wq[qx] * wq[qy] * wq[qz] * h[0] * h[1] * h[2];
+                err += e * e * wq[qx] * wq[qy] * wz(qz) * h[0] * h[1] * h[2];
               }
   return std::sqrt(err);
 }
@@ -126,15 +131,14 @@ main(int argc, char *argv[])
       declare_common(prm);
       prm.parse(file);
       const int dim = prm.get_int("Geometry", "Dimension");
-      if (dim != 3)
-        throw std::runtime_error("The device path solves three-dimensional problems; this parameter "
-                                 "file sets Dimension = " + std::to_string(dim));
+      if (dim != 2 && dim != 3)
+        throw std::runtime_error("Dimension must be 2 or 3, not " + std::to_string(dim));
       mfgpu_heat_params P;
       std::memset(&P, 0, sizeof(P));
       P.mesh.degree        = prm.get_int("Finite element system", "Polynomial degree");
       P.mesh.n_q_1d        = prm.get_int("Finite element system", "Quadrature order");
       P.mesh.n_refinements = prm.get_int("Geometry", "Global refinement");
-      make_heat_case(prm.get("Geometry", "Testcase"), P);
+      make_heat_case(prm.get("Geometry", "Testcase"), P, dim);
       P.dt                     = prm.get_double("Time", "Time step size");
       const double end_time    = prm.get_double("Time", "End time");
       const int    n_steps     = int(std::lround(end_time / P.dt));
@@ -160,7 +164,7 @@ main(int argc, char *argv[])
       check(mfgpu_mesh_n_nodes(&P.mesh, -1, &nn));
       std::vector<double> u(nn);
       long                cells = 1;
-      for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < dim; ++d)
         cells *= long(P.mesh.repetitions[d]) << P.mesh.n_refinements;
       std::cout << "--     . dim       = " << dim << "\n"
                 << "--     . fe_degree = " << P.mesh.degree << "\n"

@@ -50,9 +50,8 @@ main(int argc, char *argv[])
       declare_solid(prm);
       prm.parse(file);
       const int dim = prm.get_int("Geometry", "Dimension");
-      if (dim != 3)
-        throw std::runtime_error("The device path solves three-dimensional problems; this parameter "
-                                 "file sets Dimension = " + std::to_string(dim));
+      if (dim != 2 && dim != 3)
+        throw std::runtime_error("Dimension must be 2 or 3, not " + std::to_string(dim));
       const int degree = prm.get_int("Finite element system", "Polynomial degree");
       const int nq     = prm.get_int("Finite element system", "Quadrature order");
       if (degree < 1)
@@ -63,7 +62,7 @@ main(int argc, char *argv[])
       P.mesh.degree        = degree;
       P.mesh.n_q_1d        = nq;
       P.mesh.n_refinements = prm.get_int("Geometry", "Global refinement");
-      const SolidCase sc   = make_solid_case(prm.get("Geometry", "Testcase"), P.mesh);
+      const SolidCase sc   = make_solid_case(prm.get("Geometry", "Testcase"), P.mesh, dim);
       P.material.mu          = prm.get_double("Material properties", "Shear modulus");
       P.material.nu          = prm.get_double("Material properties", "Poisson's ratio");
       P.material.rho         = prm.get_double("Material properties", "Density");
@@ -106,9 +105,10 @@ main(int argc, char *argv[])
           P.traction[d] = tr[d];
       P.traction_id                = 11;
       const std::vector<double> pt3 = prm.get_list("Output", "Output points");
-      if (pt3.size() != 3)
-        throw std::runtime_error("Output points must give one point with 3 coordinates");
-      for (int d = 0; d < 3; ++d)
+      if (int(pt3.size()) != dim)
+        throw std::runtime_error("Output points must give one point with " + std::to_string(dim) +
+                                 " coordinates");
+      for (int d = 0; d < dim; ++d)
         P.watch[d] = pt3[d];
 
       mfgpu_context *ctx = nullptr;
@@ -122,7 +122,7 @@ main(int argc, char *argv[])
       check(mfgpu_mesh_n_nodes(&P.mesh, -1, &nn));
       long cells = 1;
       double vol = 1;
-      for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < dim; ++d)
         {
           cells *= long(P.mesh.repetitions[d]) << P.mesh.n_refinements;
           vol *= P.mesh.upper[d] - P.mesh.lower[d];
@@ -133,7 +133,7 @@ main(int argc, char *argv[])
           << "--     . fe_degree = " << degree << "\n"
           << "--     . 1d_quad   = " << nq << "\n"
           << "--     . Number of active cells: " << cells << "\n"
-          << "--     . Number of degrees of freedom: " << 3 * nn << "\n"
+          << "--     . Number of degrees of freedom: " << dim * nn << "\n"
           << "\n";
       double t = 0;
       for (int s = 0; s < R.n_steps; ++s)
@@ -141,9 +141,13 @@ main(int argc, char *argv[])
           t += P.dt;
           out << "\nTimestep " << s + 1 << " @ " << t << "s\n"
               << "Converged in " << R.newton_its[s] << " Newton iterations\n"
-              << "Solution @ " << P.watch[0] << " " << P.watch[1] << " " << P.watch[2] << "\n"
-              << "  displacement: " << R.watch_disp[s][0] << " " << R.watch_disp[s][1] << " "
-              << R.watch_disp[s][2] << "\n";
+              << "Solution @";
+          for (int d = 0; d < dim; ++d)
+            out << " " << P.watch[d];
+          out << "\n  displacement:";
+          for (int d = 0; d < dim; ++d)
+            out << " " << R.watch_disp[s][d];
+          out << "\n";
         }
       out << "\nAverage CG iter = " << (R.n_solves ? R.total_cg / R.n_solves : 0) << "\n";
       std::cout << out.str();

@@ -25,6 +25,7 @@ namespace mfgpu
 
   struct LevelGeom
   {
+    int      dim; // 2: one node plane, C[2] = Nn[2] = 1, h[2] = 1
     int      C[3];
     int      Nn[3];
     int      p;

@@ -51,16 +51,25 @@ namespace mfgpu
   to_mesh(const mfgpu_mesh &m)
   {
     Mesh r;
+    r.dim    = m.dim == 0 ? 3 : m.dim;
+    if (r.dim != 2 && r.dim != 3)
+      throw Error(ERR_ARG, "mesh: dim must be 2 or 3");
     r.degree = m.degree;
     r.n_q    = m.n_q_1d;
     r.n_ref  = m.n_refinements;
-    for (int d = 0; d < 3; ++d)
+    for (int d = 0; d < r.dim; ++d)
       {
         r.rep[d] = m.repetitions[d];
         r.lo[d]  = m.lower[d];
         r.hi[d]  = m.upper[d];
         if (m.repetitions[d] < 1 || !(m.upper[d] > m.lower[d]))
           throw Error(ERR_ARG, "mesh: repetitions must be >= 1 and upper > lower");
+      }
+    if (r.dim == 2)
+      {
+        r.rep[2] = 1;
+        r.lo[2]  = 0;
+        r.hi[2]  = 1;
       }
     if (m.degree < 1 || m.degree > 6)
       throw Error(ERR_UNSUPPORTED, "mesh: degree must be 1..6");
@@ -163,7 +172,7 @@ namespace mfgpu
                 mg.transfers.emplace_back(nullptr);
               else
                 mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
-                                                       lops[l]->geom, 3, lprec));
+                                                       lops[l]->geom, mesh.dim, lprec));
             }
           mg.coarse64   = coarse64.get();
           mg.use_graphs = P.solver.cuda_graphs != 0;
@@ -225,12 +234,16 @@ namespace mfgpu
   {
     const size_t n = fine->m();
     MF_CK(cudaMemsetAsync(rhs.ptr, 0, n * sizeof(double), ctx->stream));
-    MF_CK(dispatch_residual(basis.N, basis, fine->geom, P.material.formulation, mat, P.material.rho,
-                            P.body_force, u.as<double>(), acc.as<double>(), rhs.as<double>(),
-                            ctx->stream));
+    if (mesh.dim == 2)
+      MF_CK(launch_residual2d(basis.N, basis, fine->geom, P.material.formulation, mat, P.material.rho,
+                              P.body_force, u.as<double>(), acc.as<double>(), rhs.as<double>(), ctx->stream));
+    else
+      MF_CK(dispatch_residual(basis.N, basis, fine->geom, P.material.formulation, mat, P.material.rho,
+                              P.body_force, u.as<double>(), acc.as<double>(), rhs.as<double>(),
+                              ctx->stream));
     count_launch();
     // traction faces
-    for (int f = 0; f < 6; ++f)
+    for (int f = 0; f < 2 * mesh.dim; ++f)
       {
         if (mesh.boundary_id[f] != P.traction_id)
           continue;
@@ -260,12 +273,14 @@ namespace mfgpu
             A.w[i]     = basis.w[i];
           }
         const int nd = f / 2, d1 = nd == 0 ? 1 : 0, d2 = nd == 2 ? 1 : 2;
-        const unsigned nfaces = unsigned(g.C[d1] * g.C[d2]);
-        k_traction<<<nfaces, 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
+        if (mesh.dim == 2)
+          k_traction2d<<<unsigned(g.C[1 - nd]), 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
+        else
+          k_traction<<<unsigned(g.C[d1] * g.C[d2]), 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
         count_launch();
         MF_CK(cudaGetLastError());
       }
-    constrained_op<double>(*ctx, fine->geom, 3, 2, nullptr, rhs.as<double>());
+    constrained_op<double>(*ctx, fine->geom, fine->nc, 2, nullptr, rhs.as<double>());
     return std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
   }
 
@@ -313,7 +328,7 @@ namespace mfgpu
       }
     else
       st = cg_solve<double>(*ctx, A, nullptr, x, b, tol, maxit);
-    constrained_op<double>(*ctx, fine->geom, 3, 2, nullptr, x);
+    constrained_op<double>(*ctx, fine->geom, fine->nc, 2, nullptr, x);
     if (!st.converged)
       throw Error(ERR_NOT_CONVERGED, "CG did not converge");
     return st.its;
@@ -326,9 +341,9 @@ namespace mfgpu
     std::vector<double> h(fine->m());
     MF_CK(cudaMemcpyAsync(h.data(), u.ptr, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    int    cc[3];
-    double xi[3];
-    for (int d = 0; d < 3; ++d)
+    int    cc[3] = {0, 0, 0};
+    double xi[3] = {0, 0, 0};
+    for (int d = 0; d < mesh.dim; ++d)
       {
         const double t = (x[d] - g.lo[d]) / g.h[d];
         int          c = int(std::floor(t));
@@ -344,14 +359,16 @@ namespace mfgpu
       return v;
     };
     std::vector<double> r(3, 0.0);
-    for (int c = 0; c < 3; ++c)
-      for (int k = 0; k < basis.N; ++k)
+    const int           nz = mesh.dim == 2 ? 1 : basis.N;
+    for (int c = 0; c < fine->nc; ++c)
+      for (int k = 0; k < nz; ++k)
         for (int j = 0; j < basis.N; ++j)
           for (int i = 0; i < basis.N; ++i)
             {
               const size_t node = size_t(cc[0] * g.p + i) +
                                   size_t(g.Nn[0]) * (size_t(cc[1] * g.p + j) + size_t(g.Nn[1]) * (cc[2] * g.p + k));
-              r[c] += lag(i, xi[0]) * lag(j, xi[1]) * lag(k, xi[2]) * h[size_t(c) * g.n_nodes + node];
+              const double lz = mesh.dim == 2 ? 1.0 : lag(k, xi[2]);
+              r[c] += lag(i, xi[0]) * lag(j, xi[1]) * lz * h[size_t(c) * g.n_nodes + node];
             }
     return r;
   }
@@ -579,8 +596,12 @@ namespace mfgpu
     // rhs = -A_unconstrained uD + int (u_old + dt f) v
     op_u->vmult(rhs.ptr, uD.ptr);
     vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
-    MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
-                            ctx->stream));
+    if (G.dim == 2)
+      MF_CK(launch_heat_rhs2d(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
+                              ctx->stream));
+    else
+      MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
+                              ctx->stream));
     count_launch();
     const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
     FineOp A;

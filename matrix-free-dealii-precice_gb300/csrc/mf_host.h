@@ -87,6 +87,7 @@ namespace mfgpu
   // geometry of one level of the box hierarchy
   struct Mesh
   {
+    int      dim = 3;
     int      degree, n_q, n_ref;
     int      rep[3];
     double   lo[3], hi[3];
@@ -209,6 +210,8 @@ namespace mfgpu
     void finish_diagonal(); // constrained -> 1, invert
     // kernel launches of one application of the cells [c0, c1) (all if c1 <= c0)
     int cell_launches(size_t c0, size_t c1) const;
+    // 2D meshes: FP32/FP64 arithmetic and the atomic scatter only
+    void check_2d() const;
   };
 
   struct HeatOperator : Operator

@@ -91,4 +91,18 @@ namespace mfgpu
   cudaError_t launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
                               const SourceDesc &f, const double *u_old,
                               double *rhs, cudaStream_t s);
+
+  // two-dimensional kernels (mf_kernels2d.cu); N = p+1, precision 32 / 64
+  cudaError_t launch_apply2d(int N, int precision, const HostBasis &b, const LevelGeom &g,
+                             const ApplyArgs &a, cudaStream_t s);
+  cudaError_t launch_nh_cache2d(int N, int precision, const HostBasis &b, const LevelGeom &g, int form,
+                                const NHMatD &m, const void *u, void *cache, int *err, cudaStream_t s);
+  // kind: 0 heat (kdt), 1 neo-Hookean formulation 1, 2 formulation 0 (from the cache)
+  cudaError_t launch_diag2d(int N, int precision, const HostBasis &b, const LevelGeom &g, int kind,
+                            const NHMatD &m, double kdt, const void *cache, void *diag, cudaStream_t s);
+  cudaError_t launch_residual2d(int N, const HostBasis &b, const LevelGeom &g, int form, const NHMatD &m,
+                                double rho, const double *body, const double *u, const double *acc,
+                                double *rhs, cudaStream_t s);
+  cudaError_t launch_heat_rhs2d(int N, const HostBasis &b, const LevelGeom &g, double dt,
+                                const SourceDesc &f, const double *u_old, double *rhs, cudaStream_t s);
 } // namespace mfgpu

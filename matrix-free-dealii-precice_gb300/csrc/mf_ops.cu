@@ -187,11 +187,19 @@ namespace mfgpu
     if (l > n_ref)
       throw Error(ERR_ARG, "level beyond the number of refinements");
     LevelGeom g;
+    g.dim     = dim;
     g.p       = degree;
     g.n_nodes = 1;
     g.n_cells = 1;
     for (int d = 0; d < 3; ++d)
       {
+        if (d == 2 && dim == 2)
+          {
+            g.C[d] = g.Nn[d] = 1;
+            g.lo[d]          = 0;
+            g.h[d]           = 1;
+            continue;
+          }
         g.C[d]  = rep[d] << l;
         g.Nn[d] = g.C[d] * degree + 1;
         g.lo[d] = lo[d];
@@ -202,6 +210,8 @@ namespace mfgpu
     for (int f = 0; f < 6; ++f)
       {
         g.face_mask[f] = 0;
+        if (f >= 2 * dim)
+          continue;
         for (int i = 0; i < n_dirichlet; ++i)
           if (boundary_id[f] == dirichlet_id[i])
             g.face_mask[f] |= dirichlet_mask[i];
@@ -625,6 +635,15 @@ namespace mfgpu
     return size_t(u);
   }
 
+  void
+  Operator::check_2d() const
+  {
+    if (arith == 1)
+      throw Error(ERR_UNSUPPORTED, "double-float arithmetic is not available for 2D meshes");
+    if (scatter == 1)
+      throw Error(ERR_UNSUPPORTED, "the coloured scatter is not available for 2D meshes");
+  }
+
   int
   Operator::cell_launches(size_t c0, size_t c1) const
   {
@@ -848,6 +867,13 @@ namespace mfgpu
     a.cell_begin  = c0;
     a.cell_end    = c1;
     a.colored     = scatter == 1;
+    if (geom.dim == 2)
+      {
+        check_2d();
+        MF_CK(launch_apply2d(basis.N, precision, basis, geom, a, s));
+        count_launch();
+        return;
+      }
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, s);
@@ -863,7 +889,16 @@ namespace mfgpu
     inv_diag.alloc(m() * elem_size());
     diag.alloc(m() * elem_size());
     MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
-    NHMatD      md{};
+    NHMatD md{};
+    if (geom.dim == 2)
+      {
+        check_2d();
+        MF_CK(launch_diag2d(basis.N, precision, basis, geom, 0, md, coefficient * delta_t, nullptr,
+                            inv_diag.ptr, ctx->stream));
+        count_launch();
+        finish_diagonal();
+        return;
+      }
     cudaError_t e = precision == 32 ?
                       dispatch_diag<float>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream) :
                       dispatch_diag<double>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream);
@@ -918,6 +953,27 @@ namespace mfgpu
           throw Error(ERR_UNSUPPORTED, "formulation 0 requires tensor2 caching");
         var = V_FORM0;
       }
+    if (geom.dim == 2)
+      {
+        // 2D: every formulation-1 caching is the referential tangent
+        // (M = F^{-T}, c: 5 values per qp); formulation 0 keeps F^{-1}, J,
+        // F, J^{-1/2} (10 values)
+        check_2d();
+        const size_t want2 = geom.n_cells * size_t(basis.N * basis.N) * (formulation == 0 ? 10 : 5) * elem_size();
+        if (cache.bytes != want2)
+          cache.alloc(want2);
+        ucell.release();
+        MF_CK(launch_nh_cache2d(basis.N, precision, basis, geom, formulation == 0 ? 0 : 1, mat, u, cache.ptr,
+                                ctx->err.as<int>(), ctx->stream));
+        count_launch();
+        if (ctx->take_error_flags() & 1)
+          {
+            cached = false;
+            throw Error(ERR_DET_F, "det_F is not positive");
+          }
+        cached = true;
+        return;
+      }
     const int    N3 = basis.N * basis.N * basis.N;
     const size_t nq = geom.n_cells * size_t(N3);
     const size_t want = nq * nh_cache_fields(var) * elem_size();
@@ -966,6 +1022,13 @@ namespace mfgpu
     a.cell_begin  = c0;
     a.cell_end    = c1;
     a.colored     = scatter == 1;
+    if (geom.dim == 2)
+      {
+        check_2d();
+        MF_CK(launch_apply2d(basis.N, precision, basis, geom, a, s));
+        count_launch();
+        return;
+      }
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, s);
@@ -981,7 +1044,18 @@ namespace mfgpu
     inv_diag.alloc(m() * elem_size());
     diag.alloc(m() * elem_size());
     MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
-    const int   kind = formulation == 0 ? 2 : 1;
+    const int kind = formulation == 0 ? 2 : 1;
+    if (geom.dim == 2)
+      {
+        // 2D: the exact diagonal from the cached quadrature data
+        if (!cached)
+          throw Error(ERR_STATE, "NeoHookOperator: cache() before compute_diagonal() (2D)");
+        MF_CK(launch_diag2d(basis.N, precision, basis, geom, kind, mat, 0.0, cache.ptr, inv_diag.ptr,
+                            ctx->stream));
+        count_launch();
+        finish_diagonal();
+        return;
+      }
     cudaError_t e    = precision == 32 ?
                          dispatch_diag<float>(basis.N, basis, geom, kind, mat, 0.0, u, inv_diag.ptr, ctx->stream) :
                          dispatch_diag<double>(basis.N, basis, geom, kind, mat, 0.0, u, inv_diag.ptr, ctx->stream);
@@ -1034,7 +1108,7 @@ namespace mfgpu
   {
     std::unique_ptr<NHOperator> op(new NHOperator());
     init_op(*op, c, m, level, precision);
-    op->nc      = 3;
+    op->nc      = m.dim;
     op->variant = variant;
     return op;
   }
@@ -1137,6 +1211,16 @@ namespace mfgpu
               MF_CK(cudaMemcpy(B.val.ptr, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
             }
         };
+        if (d == 2 && cg.dim == 2)
+          {
+            // 2D: the single node plane maps to itself
+            const std::vector<int>    c1{0};
+            const std::vector<double> v1{1.0};
+            upload(P[d], c1, v1, 1, 1);
+            upload(R[d], c1, v1, 1, 1);
+            upload(I[d], c1, v1, 1, 1);
+            continue;
+          }
         upload(P[d], pc, pv, nf, p + 1);
         upload(R[d], rc, rv, ncn, wr);
         upload(I[d], ic, iv, ncn, p + 1);

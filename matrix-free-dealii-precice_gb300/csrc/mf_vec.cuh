@@ -350,6 +350,80 @@ namespace mfgpu
     double   w[MAX_N];
   };
 
+  // the same for a 2D box (faces 0..3 are edges; one block per boundary cell)
+  static __global__ void
+  k_traction2d(const __grid_constant__ TractionArgs A, const double *__restrict__ u,
+               double *__restrict__ rhs)
+  {
+    __shared__ double tq[2][MAX_N];
+    const int nd = A.face / 2, side = A.face % 2;
+    const int d1 = 1 - nd;
+    const int N  = A.N;
+    int       cc[2];
+    cc[nd]       = side ? A.C[nd] - 1 : 0;
+    cc[d1]       = blockIdx.x;
+    const int ln = side ? N - 1 : 0;
+    for (int q1 = threadIdx.x; q1 < N; q1 += blockDim.x)
+      {
+        double F[2][2] = {{0, 0}, {0, 0}};
+        for (int j = 0; j < N; ++j)
+          for (int i = 0; i < N; ++i)
+            {
+              const int li[2] = {i, j};
+              double    vv[2], dd[2];
+              for (int d = 0; d < 2; ++d)
+                {
+                  if (d == nd)
+                    {
+                      vv[d] = li[d] == ln ? 1.0 : 0.0;
+                      dd[d] = A.Ge[side][li[d]];
+                    }
+                  else
+                    {
+                      vv[d] = A.S[q1 * N + li[d]];
+                      dd[d] = A.G[q1 * N + li[d]];
+                    }
+                }
+              const double g0   = dd[0] * vv[1] / A.h[0];
+              const double g1   = vv[0] * dd[1] / A.h[1];
+              const size_t node = size_t(cc[0] * A.p + i) + size_t(A.Nn[0]) * size_t(cc[1] * A.p + j);
+              for (int c = 0; c < 2; ++c)
+                {
+                  const double uv = u[size_t(c) * A.n_nodes + node];
+                  F[c][0] += g0 * uv;
+                  F[c][1] += g1 * uv;
+                }
+            }
+        F[0][0] += 1.0;
+        F[1][1] += 1.0;
+        // n* = J F^{-T} N = cof(F) N, cof(F) = [[F11, -F10], [-F01, F00]]
+        const double cof[2][2] = {{F[1][1], -F[1][0]}, {-F[0][1], F[0][0]}};
+        const double sgn       = side ? 1.0 : -1.0;
+        const double n0 = cof[0][nd] * sgn, n1 = cof[1][nd] * sgn;
+        const double ns = sqrt(n0 * n0 + n1 * n1);
+        const double jw = A.w[q1] * A.h[d1];
+        for (int c = 0; c < 2; ++c)
+          tq[c][q1] = A.t[c] * ns * jw;
+      }
+    __syncthreads();
+    for (int i1 = threadIdx.x; i1 < N; i1 += blockDim.x)
+      {
+        int li[2];
+        li[nd]      = ln;
+        li[d1]      = i1;
+        double r[2] = {0, 0};
+        for (int q1 = 0; q1 < N; ++q1)
+          {
+            const double phi = A.S[q1 * N + i1];
+            r[0] += phi * tq[0][q1];
+            r[1] += phi * tq[1][q1];
+          }
+        const size_t node = size_t(cc[0] * A.p + li[0]) + size_t(A.Nn[0]) * size_t(cc[1] * A.p + li[1]);
+        for (int c = 0; c < 2; ++c)
+          atomicAdd(rhs + size_t(c) * A.n_nodes + node, r[c]);
+      }
+  }
+
   static __global__ void
   k_traction(const __grid_constant__ TractionArgs A, const double *__restrict__ u,
              double *__restrict__ rhs)

@@ -35,7 +35,7 @@ class Mesh(C.Structure):
                 ("lower", C.c_double * 3), ("upper", C.c_double * 3),
                 ("boundary_id", C.c_int * 6), ("n_dirichlet", C.c_int),
                 ("dirichlet_id", C.c_int * 8),
-                ("dirichlet_mask", C.c_uint * 8)]
+                ("dirichlet_mask", C.c_uint * 8), ("dim", C.c_int)]
 
 
 class Material(C.Structure):
@@ -129,9 +129,16 @@ def _ptr(t):
 
 
 def make_mesh(degree, n_refinements, repetitions, lower, upper,
-              boundary_id=(0, 0, 0, 0, 0, 0), dirichlet=(), n_q_1d=None):
-    """Box mesh; dirichlet: iterable of (boundary_id, component_mask)."""
+              boundary_id=(0, 0, 0, 0, 0, 0), dirichlet=(), n_q_1d=None, dim=None):
+    """Box mesh (2D when repetitions/lower/upper have two entries, or dim=2);
+    dirichlet: iterable of (boundary_id, component_mask)."""
+    dim = dim or len(repetitions)
+    repetitions = tuple(repetitions) + (1,) * (3 - len(repetitions))
+    lower = tuple(lower) + (0.0,) * (3 - len(lower))
+    upper = tuple(upper) + (1.0,) * (3 - len(upper))
+    boundary_id = tuple(boundary_id) + (0,) * (6 - len(boundary_id))
     m = Mesh()
+    m.dim = dim
     m.degree = degree
     m.n_q_1d = degree + 1 if n_q_1d is None else n_q_1d
     m.n_refinements = n_refinements

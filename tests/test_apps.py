@@ -1,5 +1,6 @@
 """The prm-driven executables `solid` and `heat`: parameter-file handling
 (CPU) and full runs on the device compared with the oracle (GPU)."""
+import json
 import os
 import re
 import subprocess
@@ -29,13 +30,13 @@ def test_unknown_entry_is_rejected(tmp_path):
     assert "unknown entry 'No such key'" in r.stderr and "Aborting!" in r.stderr
 
 
-def test_two_dimensional_files_are_rejected_before_device_work(tmp_path):
+def test_invalid_dimension_is_rejected_before_device_work(tmp_path):
     txt = open(os.path.join(PRM, "turek3d_gmg_tensor4.prm")).read()
-    txt = txt.replace("set Dimension          = 3", "set Dimension          = 2")
-    prm = tmp_path / "t2d.prm"
+    txt = txt.replace("set Dimension          = 3", "set Dimension          = 4")
+    prm = tmp_path / "t4d.prm"
     prm.write_text(txt)
     r = run_app("solid", str(prm), tmp_path)
-    assert r.returncode == 1 and "three-dimensional" in r.stderr
+    assert r.returncode == 1 and "Dimension must be 2 or 3" in r.stderr
     r = run_app("heat", os.path.join(PRM, "heat3d_analytic_q2.prm").replace(".prm", "_missing.prm"),
                 tmp_path)
     assert r.returncode == 1 and "cannot open" in r.stderr
@@ -89,6 +90,32 @@ def test_solid_executable_matches_oracle(tmp_path, prm, degree, n_ref, caching):
 def test_heat_executable_reproduces_analytic_solution(tmp_path):
     r = run_app("heat", os.path.join(PRM, "heat3d_analytic_q2.prm"), tmp_path)
     assert r.returncode == 0, r.stderr
+    errs = [float(x) for x in re.findall(r"Error: (\S+)", r.stdout)]
+    assert len(errs) == 11
+    assert max(errs) < 1e-11, errs
+
+
+@pytest.mark.gpu
+def test_solid_executable_2d_matches_reference_golden(tmp_path):
+    """The reference's own 2D turek_hron case (tests/solid/turek_gmg_tensor4:
+    Q1, 320 cells, 738 DoFs) through the prm-driven executable."""
+    g = json.load(open(os.path.join(HERE, "golden", "reference_goldens.json")))["solid"]["turek_gmg_tensor4"]
+    r = run_app("solid", os.path.join(PRM, "turek2d_gmg_tensor4.prm"), tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "Number of degrees of freedom: %d" % g["n_dofs"] in r.stdout, r.stdout
+    newton, disp, avg = parse_output((tmp_path / "turek2d_out" / "output").read_text())
+    assert newton == g["newton_its"]
+    for s in range(2):
+        assert len(disp[s]) == 2
+        assert np.allclose(disp[s], g["watch_disp"][s], rtol=6e-6, atol=0), (disp[s], g["watch_disp"][s])
+    assert abs(avg - g["avg_cg"]) <= 1
+
+
+@pytest.mark.gpu
+def test_heat_executable_2d_reproduces_analytic_solution(tmp_path):
+    r = run_app("heat", os.path.join(PRM, "heat2d_analytic_q2.prm"), tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "dim       = 2" in r.stdout and "Number of active cells: 64" in r.stdout
     errs = [float(x) for x in re.findall(r"Error: (\S+)", r.stdout)]
     assert len(errs) == 11
     assert max(errs) < 1e-11, errs
