@@ -172,6 +172,12 @@ int mfgpu_operator_set_scatter(mfgpu_operator *op, int mode);
  * (4 from 4 MB up), 1 = copy in, apply, copy out without overlap, <= 8.
  * No counterpart in the reference (its vectors live in host memory). */
 int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
+/* Dense copy of a small operator (three-dimensional, constrained, at most
+ * 64 MiB): enable = 1 assembles A from the current state (cache(),
+ * set_delta_t() first) and vmult / vmult_add multiply by it until the state
+ * changes; 0 frees it.  The coarse-level counterpart of deal.II's assembled
+ * coarse matrices; the solvers use it on level 0 (coarse_dense). */
+int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
 /* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
 int mfgpu_operator_compute_diagonal(mfgpu_operator *op);
 /* get_matrix_diagonal_inverse: device pointer owned by the operator */
@@ -245,6 +251,9 @@ typedef struct mfgpu_solver_params
   int    coarse_fp64;     /* level-0 Chebyshev solve in FP64                */
   int    fp64_emulation;  /* FP64 operators in double-float arithmetic      */
   int    cuda_graphs;     /* replay the V-cycle as a CUDA graph              */
+  int    coarse_dense;    /* level-0 operator (three-dimensional, <= 64 MiB)
+                             assembled densely after each setup; the coarse
+                             Chebyshev steps multiply by it, one warp per row */
 } mfgpu_solver_params;
 
 typedef struct mfgpu_solid_params
@@ -290,6 +299,14 @@ int mfgpu_solid_displacement(mfgpu_solid *s, const double **u);
 int mfgpu_solid_linear_solve(mfgpu_solid *s, const double *u,
                              const double *rhs, double *du, int *iterations,
                              double *seconds);
+/* Wall-clock sections of the driver, as the reference's TimerOutput
+ * (mf_elasticity.h:219,431-432: "Assemble residual", "Linear solver",
+ * "Setup MF: ..."). enable = 1 turns timing on and clears the table; each
+ * section then synchronises the device at its start and end. */
+int mfgpu_solid_set_timing(mfgpu_solid *s, int enable);
+/* the section table as text: calls, wall time and share per section;
+ * NUL-terminated, truncated to len bytes */
+int mfgpu_solid_timing_summary(mfgpu_solid *s, char *buf, size_t len);
 int mfgpu_solid_destroy(mfgpu_solid *s);
 
 typedef struct mfgpu_heat_params
@@ -321,6 +338,10 @@ int mfgpu_heat_run(mfgpu_heat *h, mfgpu_heat_result *r);
  * returns the CG iterations of the step */
 int mfgpu_heat_step(mfgpu_heat *h, int *cg_iterations);
 int mfgpu_heat_solution(mfgpu_heat *h, const double **u);
+/* sections of LaplaceProblem's TimerOutput (heat_transfer.h:381,581,717:
+ * "assemble rhs", "solve system"; here also "GMG setup") */
+int mfgpu_heat_set_timing(mfgpu_heat *h, int enable);
+int mfgpu_heat_timing_summary(mfgpu_heat *h, char *buf, size_t len);
 int mfgpu_heat_destroy(mfgpu_heat *h);
 
 /* ---------------------------------------------------------------- */

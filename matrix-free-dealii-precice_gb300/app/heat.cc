@@ -154,6 +154,7 @@ main(int argc, char *argv[])
       P.solver.coarse_fp64     = prm.get_bool("GPU", "FP64 coarse solve");
       P.solver.fp64_emulation  = prm.get_bool("GPU", "FP64 emulation");
       P.solver.cuda_graphs     = prm.get_bool("GPU", "CUDA graphs");
+      P.solver.coarse_dense    = prm.get_bool("GPU", "Dense coarse operator");
       const double tick        = prm.get_double("Output", "Output tick");
 
       mfgpu_context *ctx = nullptr;

@@ -170,6 +170,7 @@ namespace mfapp
     p.declare("GPU", "FP64 coarse solve", "false");
     p.declare("GPU", "FP64 emulation", "false");
     p.declare("GPU", "CUDA graphs", "true");
+    p.declare("GPU", "Dense coarse operator", "true");
   }
 
   inline void

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <iostream>
 #include <sstream>
+#include <vector>
 
 #include "cases.h"
 #include "prm.h"
@@ -84,6 +85,7 @@ main(int argc, char *argv[])
       P.solver.coarse_fp64     = prm.get_bool("GPU", "FP64 coarse solve");
       P.solver.fp64_emulation  = prm.get_bool("GPU", "FP64 emulation");
       P.solver.cuda_graphs     = prm.get_bool("GPU", "CUDA graphs");
+      P.solver.coarse_dense    = prm.get_bool("GPU", "Dense coarse operator");
       P.max_newton             = prm.get_int("Nonlinear solver", "Max iterations Newton-Raphson");
       P.tol_f                  = prm.get_double("Nonlinear solver", "Tolerance force");
       P.tol_f_abs              = prm.get_double("Nonlinear solver", "Absolute tolerance force");
@@ -115,6 +117,9 @@ main(int argc, char *argv[])
       check(mfgpu_context_create(prm.get_int("GPU", "Device"), &ctx));
       mfgpu_solid *solid = nullptr;
       check(mfgpu_solid_create(ctx, &P, &solid));
+      // wall-clock sections, printed at the end as the reference's
+      // TimerOutput summary
+      check(mfgpu_solid_set_timing(solid, 1));
       mfgpu_solid_result R;
       check(mfgpu_solid_run(solid, &R));
 
@@ -164,6 +169,9 @@ main(int argc, char *argv[])
           std::fputs(out.str().c_str(), f);
           std::fclose(f);
         }
+      std::vector<char> table(1 << 16);
+      check(mfgpu_solid_timing_summary(solid, table.data(), table.size()));
+      std::cout << "\n" << table.data() << std::flush;
       mfgpu_solid_destroy(solid);
       mfgpu_context_destroy(ctx);
     }

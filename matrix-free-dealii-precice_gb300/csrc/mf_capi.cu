@@ -1,6 +1,7 @@
 // extern "C" entry points of libmfgpu.so (declared in include/mfgpu.h).
 // Every entry point converts exceptions into a status code and a
 // per-thread error message.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -69,6 +70,17 @@ guarded(F &&f)
       g_last_error = "unknown exception";
       return MFGPU_ERR_ARG;
     }
+}
+
+// copy a text result into a caller's buffer (NUL-terminated, truncated)
+static void
+copy_text(const std::string &t, char *buf, size_t len)
+{
+  if (len == 0)
+    throw Error(ERR_ARG, "buffer length 0");
+  const size_t k = std::min(t.size(), len - 1);
+  std::memcpy(buf, t.data(), k);
+  buf[k] = '\0';
 }
 
 static void
@@ -375,6 +387,18 @@ extern "C"
   }
 
   int
+  mfgpu_operator_set_dense(mfgpu_operator *op, int enable)
+  {
+    return guarded([&] {
+      need(op, "op");
+      if (enable)
+        op->op->assemble_dense();
+      else
+        op->op->drop_dense();
+    });
+  }
+
+  int
   mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks)
   {
     return guarded([&] {
@@ -589,6 +613,26 @@ extern "C"
   }
 
   int
+  mfgpu_solid_set_timing(mfgpu_solid *s, int enable)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      s->d->timer.reset();
+      s->d->timer.enabled = enable != 0;
+    });
+  }
+
+  int
+  mfgpu_solid_timing_summary(mfgpu_solid *s, char *buf, size_t len)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(buf, "buf");
+      copy_text(s->d->timer.summary(), buf, len);
+    });
+  }
+
+  int
   mfgpu_solid_displacement(mfgpu_solid *s, const double **u)
   {
     return guarded([&] {
@@ -684,6 +728,26 @@ extern "C"
       need(h, "heat");
       need(u, "u");
       *u = h->d->sol.as<double>();
+    });
+  }
+
+  int
+  mfgpu_heat_set_timing(mfgpu_heat *h, int enable)
+  {
+    return guarded([&] {
+      need(h, "heat");
+      h->d->timer.reset();
+      h->d->timer.enabled = enable != 0;
+    });
+  }
+
+  int
+  mfgpu_heat_timing_summary(mfgpu_heat *h, char *buf, size_t len)
+  {
+    return guarded([&] {
+      need(h, "heat");
+      need(buf, "buf");
+      copy_text(h->d->timer.summary(), buf, len);
     });
   }
 

@@ -140,6 +140,7 @@ namespace mfgpu
   {
     T s;
     __device__ __forceinline__ void init(T a, T b) { s = a * b; }
+    __device__ __forceinline__ void init_add(T c) { s = c; }
     __device__ __forceinline__ void add(T a, T b) { s = fma_(a, b, s); }
     __device__ __forceinline__ T result() const { return s; }
   };
@@ -147,6 +148,257 @@ namespace mfgpu
   struct Acc<df64> : DfAcc
   {
   };
+
+  // ---------------------------------------------------------------------
+  // Even-odd 1D line operations (the EO form of mf_common.cuh).  For
+  // out = M in, with p_k = in[k] + in[N-1-k], m_k = in[k] - in[N-1-k]:
+  //   E_r = sum_k e[r][k] p_k (+ e[r][H] in[H]),  O_r = sum_k o[r][k] m_k,
+  //   out[r] = E_r + O_r,  out[N-1-r] = SIG (E_r - O_r)
+  // (plus the middle row for odd N); for out = M^T in the sign moves into
+  // the pre-sums: p_r = in[r] + SIG in[N-1-r], m_r = in[r] - SIG in[N-1-r],
+  //   out[k] = E_k + O_k,  out[N-1-k] = E_k - O_k.
+  // N = 5 takes 13 products instead of 25, N = 7 25 instead of 49 (deal.II's
+  // FEEvaluation kernels use the same split for symmetric bases).
+  // ---------------------------------------------------------------------
+  template <typename T>
+  __device__ __forceinline__ T
+  eo_plus(T a, T b)
+  {
+    return a + b;
+  }
+  template <typename T>
+  __device__ __forceinline__ T
+  eo_minus(T a, T b)
+  {
+    return a - b;
+  }
+  // df64 pre-sums: one TwoSum of the high parts, the low parts added in
+  // float (absolute error ~2^-48 (|a| + |b|), as the dot products that use
+  // them)
+  __device__ __forceinline__ df64
+  eo_plus(df64 a, df64 b)
+  {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    quick_two_sum(s, e, s, e);
+    return {s, e};
+  }
+  __device__ __forceinline__ df64
+  eo_minus(df64 a, df64 b)
+  {
+    return eo_plus(a, df64{-b.hi, -b.lo});
+  }
+
+  // sum = E + O, diff = E - O
+  template <typename T>
+  __device__ __forceinline__ void
+  acc_pair(const Acc<T> &E, const Acc<T> &O, T &sum, T &diff)
+  {
+    sum  = E.s + O.s;
+    diff = E.s - O.s;
+  }
+  // sum += E + O, diff += E - O
+  template <typename T>
+  __device__ __forceinline__ void
+  acc_pair_add(const Acc<T> &E, const Acc<T> &O, T &sum, T &diff)
+  {
+    sum  = sum + (E.s + O.s);
+    diff = diff + (E.s - O.s);
+  }
+  __device__ __forceinline__ void
+  acc_pair(const Acc<df64> &E, const Acc<df64> &O, df64 &sum, df64 &diff)
+  {
+    float q, r;
+    two_sum(E.s, O.s, q, r);
+    quick_two_sum(q, __fadd_rn(__fadd_rn(E.t, O.t), r), sum.hi, sum.lo);
+    two_sum(E.s, -O.s, q, r);
+    quick_two_sum(q, __fadd_rn(__fsub_rn(E.t, O.t), r), diff.hi, diff.lo);
+  }
+  __device__ __forceinline__ void
+  acc_pair_add(const Acc<df64> &E, const Acc<df64> &O, df64 &sum, df64 &diff)
+  {
+    float q, r, q2, r2;
+    two_sum(E.s, O.s, q, r);
+    two_sum(q, sum.hi, q2, r2);
+    quick_two_sum(q2, __fadd_rn(__fadd_rn(__fadd_rn(E.t, O.t), __fadd_rn(r, r2)), sum.lo), sum.hi, sum.lo);
+    two_sum(E.s, -O.s, q, r);
+    two_sum(q, diff.hi, q2, r2);
+    quick_two_sum(q2, __fadd_rn(__fadd_rn(__fsub_rn(E.t, O.t), __fadd_rn(r, r2)), diff.lo), diff.hi, diff.lo);
+  }
+
+  // out = M in
+  template <int N, typename T, int SIG>
+  __device__ __forceinline__ void
+  mat_apply(const EO<N, T, SIG> &M, const T (&in)[N], T (&out)[N])
+  {
+    constexpr int  H = N / 2, HR = (N + 1) / 2;
+    constexpr bool ODD = N % 2 == 1;
+    T              p[H], m[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k)
+      {
+        p[k] = eo_plus(in[k], in[N - 1 - k]);
+        m[k] = eo_minus(in[k], in[N - 1 - k]);
+      }
+#pragma unroll
+    for (int r = 0; r < H; ++r)
+      {
+        Acc<T> E, O;
+        E.init(M.e[r * HR], p[0]);
+#pragma unroll
+        for (int k = 1; k < H; ++k)
+          E.add(M.e[r * HR + k], p[k]);
+        if constexpr (ODD)
+          E.add(M.e[r * HR + H], in[H]);
+        O.init(M.o[r * H], m[0]);
+#pragma unroll
+        for (int k = 1; k < H; ++k)
+          O.add(M.o[r * H + k], m[k]);
+        if constexpr (SIG > 0)
+          acc_pair(E, O, out[r], out[N - 1 - r]);
+        else
+          acc_pair(O, E, out[r], out[N - 1 - r]);
+      }
+    if constexpr (ODD)
+      {
+        Acc<T> C;
+        if constexpr (SIG > 0)
+          {
+            C.init(M.e[H * HR], p[0]);
+#pragma unroll
+            for (int k = 1; k < H; ++k)
+              C.add(M.e[H * HR + k], p[k]);
+            C.add(M.e[H * HR + H], in[H]);
+          }
+        else
+          {
+            C.init(M.o[H * H], m[0]);
+#pragma unroll
+            for (int k = 1; k < H; ++k)
+              C.add(M.o[H * H + k], m[k]);
+          }
+        out[H] = C.result();
+      }
+  }
+
+  // Whether the operator-application sweeps use the even-odd form for N
+  // points per direction in arithmetic T.  The split trades products for
+  // pre- and post-additions; on GB300 (heat operator, 64^3 cells) it wins
+  // for N >= 3 in double-float, N = 3 and N >= 5 in FP64 and N >= 5 in FP32,
+  // and loses at N = 2 (and N = 4 in FP64).
+  template <int N, typename T>
+  __host__ __device__ constexpr bool
+  use_even_odd()
+  {
+    return std::is_same<T, df64>::value ? N >= 3 : (std::is_same<T, double>::value ? (N == 3 || N >= 5) : N >= 5);
+  }
+
+  // the interpolation and derivative matrices of the operator-application
+  // sweeps, in the form use_even_odd selects
+  template <int N, typename T>
+  __device__ __forceinline__ const auto &
+  sweep_S(const ShapeA<N, T> &sh)
+  {
+    if constexpr (use_even_odd<N, T>())
+      return sh.Se;
+    else
+      return sh.S;
+  }
+  template <int N, typename T>
+  __device__ __forceinline__ const auto &
+  sweep_D(const ShapeA<N, T> &sh, int d)
+  {
+    if constexpr (use_even_odd<N, T>())
+      return sh.De[d];
+    else
+      return sh.D[d];
+  }
+  template <int N, typename T>
+  __device__ __forceinline__ const auto &
+  sweep_Du(const ShapeA<N, T> &sh)
+  {
+    if constexpr (use_even_odd<N, T>())
+      return sh.Due;
+    else
+      return sh.Du;
+  }
+
+  // out = M^T in (ADD: out += M^T in)
+  template <bool ADD, int N, typename T, int SIG>
+  __device__ __forceinline__ void
+  eo_apply_t(const EO<N, T, SIG> &M, const T (&in)[N], T (&out)[N])
+  {
+    constexpr int  H = N / 2, HR = (N + 1) / 2;
+    constexpr bool ODD = N % 2 == 1;
+    T              p[H], m[H];
+#pragma unroll
+    for (int r = 0; r < H; ++r)
+      {
+        if constexpr (SIG > 0)
+          {
+            p[r] = eo_plus(in[r], in[N - 1 - r]);
+            m[r] = eo_minus(in[r], in[N - 1 - r]);
+          }
+        else
+          {
+            p[r] = eo_minus(in[r], in[N - 1 - r]);
+            m[r] = eo_plus(in[r], in[N - 1 - r]);
+          }
+      }
+#pragma unroll
+    for (int k = 0; k < H; ++k)
+      {
+        Acc<T> E, O;
+        E.init(M.e[k], p[0]);
+#pragma unroll
+        for (int r = 1; r < H; ++r)
+          E.add(M.e[r * HR + k], p[r]);
+        O.init(M.o[k], m[0]);
+#pragma unroll
+        for (int r = 1; r < H; ++r)
+          O.add(M.o[r * H + k], m[r]);
+        if constexpr (ODD && SIG > 0)
+          E.add(M.e[H * HR + k], in[H]);
+        if constexpr (ODD && SIG < 0)
+          O.add(M.o[H * H + k], in[H]);
+        if constexpr (ADD)
+          acc_pair_add(E, O, out[k], out[N - 1 - k]);
+        else
+          acc_pair(E, O, out[k], out[N - 1 - k]);
+      }
+    if constexpr (ODD)
+      {
+        Acc<T> C;
+        if constexpr (ADD)
+          {
+            C.init_add(out[H]);
+            C.add(M.e[H], p[0]);
+          }
+        else
+          C.init(M.e[H], p[0]);
+#pragma unroll
+        for (int r = 1; r < H; ++r)
+          C.add(M.e[r * HR + H], p[r]);
+        if constexpr (SIG > 0)
+          C.add(M.e[H * HR + H], in[H]);
+        out[H] = C.result();
+      }
+  }
+
+  template <int N, typename T, int SIG>
+  __device__ __forceinline__ void
+  mat_apply_t(const EO<N, T, SIG> &M, const T (&in)[N], T (&out)[N])
+  {
+    eo_apply_t<false>(M, in, out);
+  }
+
+  template <int N, typename T, int SIG>
+  __device__ __forceinline__ void
+  mat_apply_t_add(const EO<N, T, SIG> &M, const T (&in)[N], T (&out)[N])
+  {
+    eo_apply_t<true>(M, in, out);
+  }
 
   template <typename T>
   __device__ __forceinline__ T
@@ -369,9 +621,9 @@ namespace mfgpu
   // scalar field whose z-columns are in registers.  Writes V, G0, G1, G2.
   // Requires a __syncthreads() before V/G are read by other threads.
   // ---------------------------------------------------------------------
-  template <int N, typename T, class L = Lay<N, N, N * N>>
+  template <int N, typename T, class L = Lay<N, N, N * N>, class MS, class MD>
   __device__ __forceinline__ void
-  evaluate_field(const T *S, const T *D0, const T *D1, const T *D2,
+  evaluate_field(const MS &S, const MD &D0, const MD &D1, const MD &D2,
                  const T (&col)[N], T *V, T *G0, T *G1, T *G2, T *T0, T *T1,
                  int a, int b, bool want_values)
   {
@@ -416,9 +668,9 @@ namespace mfgpu
   // z-column (x=a, y=b) in registers.  V is overwritten.  Starts with a
   // __syncthreads() so that the submitted values of all threads are visible.
   // ---------------------------------------------------------------------
-  template <int N, typename T, class L = Lay<N, N, N * N>>
+  template <int N, typename T, class L = Lay<N, N, N * N>, class MS, class MD>
   __device__ __forceinline__ void
-  integrate_field(const T *S, const T *D0, const T *D1, const T *D2, T *V,
+  integrate_field(const MS &S, const MD &D0, const MD &D1, const MD &D2, T *V,
                   const T *G0, const T *G1, const T *G2, T *T0, T *T1, int a,
                   int b, bool has_values, bool has_gradients, T (&col)[N])
   {
@@ -499,9 +751,9 @@ namespace mfgpu
   // Scratch: evaluate uses G1, G2; integrate uses G0, G1 (as in
   // evaluate_field / integrate_field).
   // ---------------------------------------------------------------------
-  template <int N, class L, typename T>
+  template <int N, class L, typename T, class MS, class MD>
   __device__ __forceinline__ void
-  evaluate_field_rg(const T *S, const T *D, const T (&col)[N], T *V, int a, int b)
+  evaluate_field_rg(const MS &S, const MD &D, const T (&col)[N], T *V, int a, int b)
   {
     constexpr int A = L::A;
     T             x[N], y[N];
@@ -529,9 +781,9 @@ namespace mfgpu
       }
   }
 
-  template <int N, class L, typename T>
+  template <int N, class L, typename T, class MS, class MD>
   __device__ __forceinline__ void
-  integrate_field_rg(const T *S, const T *D, T *V, int a, int b, T (&col)[N])
+  integrate_field_rg(const MS &S, const MD &D, T *V, int a, int b, T (&col)[N])
   {
     constexpr int A = L::A;
     T             x[N], y[N];
@@ -598,8 +850,16 @@ namespace mfgpu
   // v and H arrive as the values and REAL gradients at quadrature point q and
   // leave as the submitted value and flux (before JxW).
   // ---------------------------------------------------------------------
-  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED, bool ONE_CELL = false>
-  __global__ void __launch_bounds__((ONE_CELL ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>()) * N * N)
+  //
+  // UNIT: element columns instead of an application.  Block (c, j) applies
+  // the operator of cell c to the unit vector of its local DoF j (component
+  // j / N^3, node j % N^3) and adds the result to column j's global DoF of
+  // the dense row-major matrix dst (NC n_nodes rows and columns); src is
+  // not read, constrained rows and columns get nothing (the caller puts 1
+  // on their diagonal).
+  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED, bool ONE_CELL = false,
+            bool UNIT = false>
+  __global__ void __launch_bounds__((ONE_CELL || UNIT ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>()) * N * N)
   cell_apply_kernel(const __grid_constant__ ShapeA<N, T> sh,
                     const __grid_constant__ CellGeom<T> g, const QOp op,
                     const TS *__restrict__ src, TS *__restrict__ dst)
@@ -608,7 +868,7 @@ namespace mfgpu
     constexpr int N3  = N * N * N;
     // ONE_CELL: one cell per block, for grids smaller than the GPU (coarse
     // levels), so that their cells spread over as many SMs as possible
-    constexpr int CPB = ONE_CELL ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>();
+    constexpr int CPB = ONE_CELL || UNIT ? 1 : apply_cells_per_block<N, NC, TS, QOp::eval_u>();
     constexpr int SPC = apply_smem_per_cell<N, NC, QOp::eval_u, T>();
     using LA          = ApplyLay<N, T>; // padded shared-memory layout of the cell arrays
     constexpr int AS  = LA::A;
@@ -621,7 +881,18 @@ namespace mfgpu
     const int      b      = l / N;
     unsigned cell;
     bool     active;
-    if (g.color < 0)
+    int      jc = 0, ja = 0, jb = 0, jk = 0; // UNIT: the local DoF of the unit vector
+    if constexpr (UNIT)
+      {
+        const unsigned j = blockIdx.x % unsigned(NC * N3);
+        cell             = g.cell_begin + blockIdx.x / unsigned(NC * N3);
+        active           = cell < g.cell_end;
+        jc               = int(j) / N3;
+        ja               = int(j) % N;
+        jb               = (int(j) / N) % N;
+        jk               = (int(j) % N3) / N2;
+      }
+    else if (g.color < 0)
       {
         cell   = g.cell_begin + blockIdx.x * CPB + lc;
         active = cell < g.cell_end;
@@ -664,7 +935,9 @@ namespace mfgpu
               bool skip = false;
               if (CONSTRAINED)
                 skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
-              if (!skip)
+              if constexpr (UNIT)
+                val = (!skip && c == jc && a == ja && b == jb && k == jk) ? TS(1) : TS(0);
+              else if (!skip)
                 val = __ldg(src + size_t(c) * g.n_nodes + node);
             }
           raw[k] = val;
@@ -686,13 +959,13 @@ namespace mfgpu
         // reference gradients: loops over the directions in double-float
         // (instruction-cache bound), unrolled compile-time strides otherwise
         if constexpr (QOp::ref_grad && std::is_same<T, df64>::value)
-          evaluate_field_rg<N, LA>(sh.S, sh.Du, col, V, a, b);
+          evaluate_field_rg<N, LA>(sweep_S(sh), sweep_Du(sh), col, V, a, b);
         else if constexpr (QOp::ref_grad)
-          evaluate_field<N, T, LA>(sh.S, sh.Du, sh.Du, sh.Du, col, V, V + AS, V + 2 * AS,
-                                   V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
+          evaluate_field<N, T, LA>(sweep_S(sh), sweep_Du(sh), sweep_Du(sh), sweep_Du(sh), col, V, V + AS,
+                                   V + 2 * AS, V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
         else
-          evaluate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, V, V + AS, V + 2 * AS,
-                                   V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
+          evaluate_field<N, T, LA>(sweep_S(sh), sweep_D(sh, 0), sweep_D(sh, 1), sweep_D(sh, 2), col, V, V + AS,
+                                   V + 2 * AS, V + 3 * AS, V + 2 * AS, V + 3 * AS, a, b, true);
       }
     if constexpr (QOp::eval_u)
       {
@@ -708,8 +981,8 @@ namespace mfgpu
             // and serves as the sweep scratch
             T *Gc = GU + c * 3 * AS;
             __syncthreads();
-            evaluate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], col, XU, Gc, Gc + AS,
-                                     Gc + 2 * AS, Gc + AS, Gc + 2 * AS, a, b, false);
+            evaluate_field<N, T, LA>(sweep_S(sh), sweep_D(sh, 0), sweep_D(sh, 1), sweep_D(sh, 2), col, XU, Gc,
+                                     Gc + AS, Gc + 2 * AS, Gc + AS, Gc + 2 * AS, a, b, false);
           }
       }
     __syncthreads();
@@ -789,13 +1062,13 @@ namespace mfgpu
         T  col[N];
         // sweep scratch: the x and y gradient slots (consumed by then)
         if constexpr (QOp::ref_grad && std::is_same<T, df64>::value)
-          integrate_field_rg<N, LA>(sh.S, sh.Du, V, a, b, col);
+          integrate_field_rg<N, LA>(sweep_S(sh), sweep_Du(sh), V, a, b, col);
         else if constexpr (QOp::ref_grad)
-          integrate_field<N, T, LA>(sh.S, sh.Du, sh.Du, sh.Du, V, V + AS, V + 2 * AS,
-                                    V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
+          integrate_field<N, T, LA>(sweep_S(sh), sweep_Du(sh), sweep_Du(sh), sweep_Du(sh), V, V + AS,
+                                    V + 2 * AS, V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
         else
-          integrate_field<N, T, LA>(sh.S, sh.D[0], sh.D[1], sh.D[2], V, V + AS, V + 2 * AS,
-                                    V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
+          integrate_field<N, T, LA>(sweep_S(sh), sweep_D(sh, 0), sweep_D(sh, 1), sweep_D(sh, 2), V, V + AS,
+                                    V + 2 * AS, V + 3 * AS, V + AS, V + 2 * AS, a, b, true, true, col);
         if (active)
           {
 #pragma unroll
@@ -804,6 +1077,17 @@ namespace mfgpu
                 const int    ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
                 const size_t node =
                   size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+                if constexpr (UNIT)
+                  {
+                    if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
+                      continue;
+                    const size_t gcol = size_t(jc) * g.n_nodes + size_t(cx * g.p + ja) +
+                                        size_t(g.Nn[0]) * (size_t(cy * g.p + jb) +
+                                                           size_t(g.Nn[1]) * size_t(cz * g.p + jk));
+                    atomicAdd(dst + (size_t(c) * g.n_nodes + node) * (size_t(NC) * g.n_nodes) + gcol,
+                              to_storage<TS, T>(col[k]));
+                    continue;
+                  }
                 if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
                   {
                     // constrained row: dst += src, written by the one cell

@@ -48,9 +48,25 @@ namespace mfgpu
     T w[N];
   };
 
+  // Even-odd form of an N x N matrix M with M[N-1-r][N-1-k] = SIG M[r][k]
+  // (SIG = +1: the interpolation S from the Gauss-Lobatto nodes to the
+  // Gauss points, both symmetric about the cell centre; SIG = -1: the
+  // collocation derivative D).  With H = N/2 and HR = (N+1)/2:
+  //   e[r][k] = (M[r][k] + M[r][N-1-k]) / 2,  o[r][k] = (M[r][k] - M[r][N-1-k]) / 2
+  // for r < HR, k < H, and e[r][H] = M[r][H] for odd N.  M and M^T then
+  // apply with about half the products (see eo_apply in the cell kernels).
+  template <int N, typename T, int SIG>
+  struct EO
+  {
+    static constexpr int H = N / 2, HR = (N + 1) / 2;
+    T                    e[HR * HR];
+    T                    o[HR * H];
+  };
+
   // shape data of the operator-application kernels: the collocation
   // derivative per direction already divided by the cell size h_d, so the
-  // gradients come out in real coordinates
+  // gradients come out in real coordinates; the same matrices in even-odd
+  // form for the 1D sweeps
   template <int N, typename T>
   struct ShapeA
   {
@@ -58,6 +74,9 @@ namespace mfgpu
     T D[3][N * N];
     T Du[N * N]; // unscaled (reference-cell) derivative matrix
     T w[N];
+    EO<N, T, 1>  Se;
+    EO<N, T, -1> De[3];
+    EO<N, T, -1> Due;
   };
 
   // geometry of a level as seen by a cell kernel, in precision T

@@ -193,36 +193,63 @@ namespace mfgpu
   void
   SolidDriver::update_operators(const double *ulin)
   {
-    fine->u = ulin;
-    fine->do_cache();
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: cache()");
+      fine->u = ulin;
+      fine->do_cache();
+    }
     if (P.solver.preconditioner == 1)
-      fine->compute_diagonal();
+      {
+        PhaseTimer::Scope ts(timer, ctx, "Setup MF: diagonal()");
+        fine->compute_diagonal();
+      }
     if (P.solver.preconditioner != 2)
       return;
-    const size_t nf = lops[L]->m();
-    if (lprec == 32)
-      vec_convert<float, double>(*ctx, nf, ulin, u_levels[L].as<float>());
-    else
-      vec_copy<double>(*ctx, nf, ulin, u_levels[L].as<double>());
-    for (int l = L; l > 0; --l)
-      {
-        Transfer *t = lprec == 32 ? mgf->transfers[l].get() : mgd->transfers[l].get();
-        t->interpolate(u_levels[l - 1].ptr, u_levels[l].ptr);
-      }
-    for (int l = 0; l <= L; ++l)
-      {
-        lops[l]->u = u_levels[l].ptr;
-        lops[l]->do_cache();
-        lops[l]->compute_diagonal();
-      }
-    if (coarse64)
-      {
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: interpolate_to_mg");
+      const size_t      nf = lops[L]->m();
+      if (lprec == 32)
+        vec_convert<float, double>(*ctx, nf, ulin, u_levels[L].as<float>());
+      else
+        vec_copy<double>(*ctx, nf, ulin, u_levels[L].as<double>());
+      for (int l = L; l > 0; --l)
+        {
+          Transfer *t = lprec == 32 ? mgf->transfers[l].get() : mgd->transfers[l].get();
+          t->interpolate(u_levels[l - 1].ptr, u_levels[l].ptr);
+        }
+      if (coarse64)
         vec_convert<double, float>(*ctx, coarse64->m(), u_levels[0].as<float>(), u0_64.as<double>());
-        coarse64->u = u0_64.ptr;
-        coarse64->do_cache();
+    }
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: cache()");
+      for (int l = 0; l <= L; ++l)
+        {
+          lops[l]->u = u_levels[l].ptr;
+          lops[l]->do_cache();
+        }
+      if (coarse64)
+        {
+          coarse64->u = u0_64.ptr;
+          coarse64->do_cache();
+        }
+    }
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: diagonal()");
+      for (int l = 0; l <= L; ++l)
+        lops[l]->compute_diagonal();
+      if (coarse64)
         coarse64->compute_diagonal();
-      }
-    const int coarse_its = P.solver.coarse_accurate ? int(lops[0]->m()) : P.solver.cheb_eig_its;
+    }
+    {
+      Operator *co = coarse64 ? static_cast<Operator *>(coarse64.get()) : lops[0].get();
+      if (P.solver.coarse_dense && co->dense_fits())
+        {
+          PhaseTimer::Scope ts(timer, ctx, "Setup MF: coarse matrix");
+          co->assemble_dense();
+        }
+    }
+    PhaseTimer::Scope ts(timer, ctx, "Setup MF: GMG setup");
+    const int         coarse_its = P.solver.coarse_accurate ? int(lops[0]->m()) : P.solver.cheb_eig_its;
     if (lprec == 32)
       mgf->setup(P.solver.cheb_range, P.solver.cheb_degree, P.solver.cheb_eig_its, coarse_its);
     else
@@ -232,7 +259,8 @@ namespace mfgpu
   double
   SolidDriver::assemble_residual()
   {
-    const size_t n = fine->m();
+    PhaseTimer::Scope ts(timer, ctx, "Assemble residual");
+    const size_t      n = fine->m();
     MF_CK(cudaMemsetAsync(rhs.ptr, 0, n * sizeof(double), ctx->stream));
     if (mesh.dim == 2)
       MF_CK(launch_residual2d(basis.N, basis, fine->geom, P.material.formulation, mat, P.material.rho,
@@ -306,7 +334,8 @@ namespace mfgpu
   int
   SolidDriver::solve_linear(const double *b, double *x, double tol)
   {
-    const size_t n = fine->m();
+    PhaseTimer::Scope ts(timer, ctx, "Linear solver");
+    const size_t      n = fine->m();
     MF_CK(cudaMemsetAsync(x, 0, n * sizeof(double), ctx->stream));
     FineOp A;
     A.op            = fine.get();
@@ -543,6 +572,11 @@ namespace mfgpu
           lo->compute_diagonal();
         if (coarse64)
           coarse64->compute_diagonal();
+        // the level operators stay fixed over the time steps: the coarse
+        // one is assembled once
+        Operator *co = coarse64 ? static_cast<Operator *>(coarse64.get()) : lops[0].get();
+        if (P.solver.coarse_dense && co->dense_fits())
+          co->assemble_dense();
       }
     if (P.solver.preconditioner == 1)
       op->compute_diagonal();
@@ -570,6 +604,7 @@ namespace mfgpu
     const LevelGeom &G = op->geom;
     t += P.dt;
     ++step_no;
+    std::unique_ptr<PhaseTimer::Scope> ts(new PhaseTimer::Scope(timer, ctx, "assemble rhs"));
     // inhomogeneous Dirichlet values on the constrained nodes at time t
     MF_CK(cudaMemsetAsync(uD.ptr, 0, n * sizeof(double), ctx->stream));
     if (P.analytic)
@@ -604,32 +639,39 @@ namespace mfgpu
                               ctx->stream));
     count_launch();
     const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+    ts.reset();
     FineOp A;
     A.op = op.get();
     CGStats st;
     if (P.solver.preconditioner == 2)
       {
-        if (lprec == 32)
-          {
+        {
+          PhaseTimer::Scope tg(timer, ctx, "GMG setup");
+          if (lprec == 32)
             mgf->setup(15., 5, 10, int(lops[0]->m()));
-            st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
-          }
-        else
-          {
+          else
             mgd->setup(15., 5, 10, int(lops[0]->m()));
-            st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
-          }
+        }
+        PhaseTimer::Scope tsol(timer, ctx, "solve system");
+        if (lprec == 32)
+          st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+        else
+          st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
       }
     else if (P.solver.preconditioner == 1)
       {
-        JacobiPre64 J;
+        PhaseTimer::Scope tsol(timer, ctx, "solve system");
+        JacobiPre64       J;
         J.ctx   = ctx;
         J.A     = op.get();
         J.omega = 0.7;
         st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n));
       }
     else
-      st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
+      {
+        PhaseTimer::Scope tsol(timer, ctx, "solve system");
+        st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
+      }
     if (!st.converged)
       throw Error(ERR_NOT_CONVERGED, "CG did not converge");
     constrained_op<double>(*ctx, G, 1, 2, nullptr, du.as<double>());

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
+
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -59,6 +61,12 @@ namespace mfgpu
     }
     ~DevBuf() { release(); }
     void alloc(size_t b);
+    // allocate b bytes unless the buffer already has exactly that size
+    void ensure(size_t b)
+    {
+      if (bytes != b || (b != 0 && !ptr))
+        alloc(b);
+    }
     void release();
     template <typename T>
     T *
@@ -84,6 +92,86 @@ namespace mfgpu
     void sync();
   };
 
+  // pinned host array of doubles (move-only), grown on demand
+  struct HostPinned
+  {
+    double *p = nullptr;
+    size_t  n = 0;
+    HostPinned() = default;
+    HostPinned(const HostPinned &) = delete;
+    HostPinned &operator=(const HostPinned &) = delete;
+    HostPinned(HostPinned &&o) noexcept
+      : p(o.p)
+      , n(o.n)
+    {
+      o.p = nullptr;
+      o.n = 0;
+    }
+    HostPinned &
+    operator=(HostPinned &&o) noexcept
+    {
+      std::swap(p, o.p);
+      std::swap(n, o.n);
+      return *this;
+    }
+    ~HostPinned()
+    {
+      if (p)
+        cudaFreeHost(p);
+    }
+    void
+    ensure(size_t count)
+    {
+      if (count <= n)
+        return;
+      if (p)
+        cudaFreeHost(p);
+      p = nullptr;
+      n = 0;
+      if (cudaMallocHost(&p, count * sizeof(double)) != cudaSuccess)
+        {
+          p = nullptr;
+          (void)cudaGetLastError();
+          throw std::runtime_error("cudaMallocHost failed");
+        }
+      n = count;
+    }
+  };
+
+  // Wall-clock sections of a driver, as the reference's TimerOutput with
+  // wall_times (mf_elasticity.h:219,431-432; heat_transfer.h:381,405).
+  // With timing enabled a section synchronises the context's stream when it
+  // opens and when it closes, so that the device work a section issues is
+  // charged to it; disabled, a section costs nothing.
+  struct PhaseTimer
+  {
+    bool                                  enabled = false;
+    std::vector<std::string>              names;
+    std::vector<double>                   secs;
+    std::vector<long>                     calls;
+    std::chrono::steady_clock::time_point start = std::chrono::steady_clock::now();
+    void                                  reset();
+    int                                   index(const char *name);
+    // the table of sections (calls, wall time, share of the time since
+    // reset), in the order the sections first opened
+    std::string summary() const;
+
+    class Scope
+    {
+    public:
+      Scope(PhaseTimer &t, Context *c, const char *name);
+      ~Scope();
+      Scope(const Scope &)            = delete;
+      Scope &operator=(const Scope &) = delete;
+
+    private:
+      PhaseTimer                           *t_;
+      Context                              *c_;
+      int                                   i_ = -1;
+      std::chrono::steady_clock::time_point t0_;
+    };
+  };
+
   // geometry of one level of the box hierarchy
   struct Mesh
   {
@@ -103,6 +191,10 @@ namespace mfgpu
   // vector kernels (instantiated for float and double)
   // ---------------------------------------------------------------------
   template <typename T> void vec_fill(Context &c, size_t n, T v, T *x);
+  // x[i] = (i % 11 == 0 ? 0 : 1) - mean of those values: the start vector of
+  // the Chebyshev eigenvalue estimate (high-frequency content and the
+  // constant mode)
+  template <typename T> void vec_estimate_start(Context &c, size_t n, T *x);
   template <typename T> void vec_axpby(Context &c, size_t n, T a, const T *x, T b, T *y);
   template <typename T> void vec_axpbyz(Context &c, size_t n, T a, const T *x, T b, const T *y, T *z);
   template <typename T> void vec_copy(Context &c, size_t n, const T *x, T *y);
@@ -114,13 +206,32 @@ namespace mfgpu
   template <typename T> double vec_dot(Context &c, size_t n, const T *x, const T *y);
   template <typename T> void cg_update(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q, int rr_slot);
   template <typename T> void cg_direction(Context &c, size_t n, int num_slot, int den_slot, const T *z, T *p);
+  // Jacobi-preconditioned CG, fused: x += a p, r -= a q, z = dinv r, |r|^2
+  // and r.z into two slots (one launch)
+  template <typename T>
+  void cg_update_jacobi(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q,
+                        const T *dinv, T *z, int rr_slot, int rz_slot);
+  // p = z + (s[rzn]/s[rz]) p, q_zero = 0 (if given), and the Lanczos record
+  // of lanczos_record (one launch)
+  template <typename T>
+  void cg_direction_rec(Context &c, size_t n, int rz, int rzn, int pq, int rr, const T *z, T *p, T *q_zero,
+                        double *rec, int *counter);
   // rec[3k..3k+2] = (slots[rz]/slots[pq], slots[rr], slots[rzn]/slots[rz]),
   // k = (*counter)++ on the device
   void lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int *counter);
   template <typename T> void cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold);
   template <typename T> void cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b, const T *Ax, const T *dinv, T *x, T *xold);
-  // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1
+  // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1, 4 (dst a
+  // dense nc n_nodes square matrix) unit diagonal entry
   template <typename T> void constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst);
+  // dense row-major n x n operators in precision 32 (float) or 64 (double)
+  void dense_mv(Context &c, int precision, size_t n, const void *A, const void *x, void *y, bool add);
+  void dense_constrained_identity(Context &c, int precision, const LevelGeom &g, int nc, void *A);
+  // one Chebyshev step x_new = x + f1 (x - xo) + f2 dinv (b - A x) (first:
+  // x_new = (1 + f1) x + f2 dinv (b - A x)) into xo
+  template <typename T>
+  void cheby_dense_step(Context &c, size_t n, const T *A, T f1, T f2, bool first, const T *b, const T *dinv,
+                        const T *x, T *xo);
   double *scalar_slots(Context &c); // device pointer to the scalars
   void    read_scalars(Context &c, int n); // D2H of the first n slots (sync)
 
@@ -190,8 +301,25 @@ namespace mfgpu
     void apply_cells(void *dst, const void *src) { apply_cells_range(dst, src, 0, 0, ctx->stream); }
     // the same for the cells [c0, c1) (all cells if c1 <= c0) on stream s;
     // a constrained row is added by the launch that contains its owner cell
-    virtual void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) = 0;
-    virtual void compute_diagonal() = 0;
+    void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s);
+    // the kernel arguments of the operator (no vectors, all cells); checks
+    // that the operator is ready to apply
+    virtual ApplyArgs cell_args() const = 0;
+    virtual void      compute_diagonal() = 0;
+    // Dense copy of a small operator (at most DENSE_MAX_BYTES): the entries
+    // of A assembled from element columns (one launch), constrained rows
+    // and columns as the identity.  vmult / vmult_add multiply by it (one
+    // warp per row) while value_state() is what it was at assembly.
+    static constexpr size_t DENSE_MAX_BYTES = size_t(64) << 20;
+    DevBuf                  dense;
+    size_t                  dense_key = 0;
+    bool                    dense_on  = false;
+    bool                    dense_fits() const;
+    void                    assemble_dense();
+    void                    drop_dense();
+    bool                    use_dense() const { return dense_on && dense.ptr && dense_key == value_state(); }
+    // vmult_state() plus the cached quadrature data's generation
+    virtual size_t value_state() const { return vmult_state(); }
     virtual size_t memory_consumption() const { return 0; }
     virtual void clear() {}
     void vmult(void *dst, const void *src);
@@ -216,11 +344,11 @@ namespace mfgpu
 
   struct HeatOperator : Operator
   {
-    double delta_t     = 0;
-    double coefficient = 1;
-    void   apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) override;
-    void   compute_diagonal() override;
-    size_t vmult_state() const override;
+    double    delta_t     = 0;
+    double    coefficient = 1;
+    ApplyArgs cell_args() const override;
+    void      compute_diagonal() override;
+    size_t    vmult_state() const override;
   };
 
   struct NHOperator : Operator
@@ -232,10 +360,12 @@ namespace mfgpu
     const void *u      = nullptr; // linearisation (not owned)
     DevBuf      cache;
     DevBuf      ucell;
-    bool        cached = false;
-    void   apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s) override;
-    void   compute_diagonal() override;
-    size_t vmult_state() const override;
+    bool        cached    = false;
+    size_t      cache_gen = 0; // incremented by every do_cache()
+    ApplyArgs cell_args() const override;
+    void      compute_diagonal() override;
+    size_t    vmult_state() const override;
+    size_t    value_state() const override;
     void   do_cache();
     size_t memory_consumption() const override { return cache.bytes + ucell.bytes; }
     void   clear() override;

@@ -31,6 +31,27 @@ namespace mfgpu
       return s;
     }
 
+    // even-odd form of the row-major N x N matrix scale * M (FP64 on the
+    // host, then rounded to the compute type)
+    template <int N, typename T, int SIG>
+    EO<N, T, SIG>
+    make_eo(const double *M, double scale)
+    {
+      using E = EO<N, T, SIG>;
+      E r;
+      for (int i = 0; i < E::HR; ++i)
+        {
+          for (int k = 0; k < E::H; ++k)
+            {
+              r.e[i * E::HR + k] = conv_host<T>(0.5 * scale * (M[i * N + k] + M[i * N + N - 1 - k]));
+              r.o[i * E::H + k]  = conv_host<T>(0.5 * scale * (M[i * N + k] - M[i * N + N - 1 - k]));
+            }
+          if (N % 2 == 1)
+            r.e[i * E::HR + E::H] = conv_host<T>(scale * M[i * N + E::H]);
+        }
+      return r;
+    }
+
     template <int N, typename T>
     ShapeA<N, T>
     make_shape_apply(const HostBasis &b, const LevelGeom &g)
@@ -45,6 +66,10 @@ namespace mfgpu
         }
       for (int i = 0; i < N; ++i)
         s.w[i] = conv_host<T>(b.w[i]);
+      s.Se  = make_eo<N, T, 1>(b.S, 1.0);
+      s.Due = make_eo<N, T, -1>(b.D, 1.0);
+      for (int d = 0; d < 3; ++d)
+        s.De[d] = make_eo<N, T, -1>(b.D, 1.0 / g.h[d]);
       return s;
     }
 

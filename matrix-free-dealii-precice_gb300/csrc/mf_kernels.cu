@@ -26,13 +26,33 @@ namespace mfgpu
     template <int N, typename TS, typename T, int NC, class Op, bool CON>
     cudaError_t
     run_apply(const ShapeA<N, T> &sh, const CellGeom<T> &cg, const Op &op,
-              const TS *src, TS *dst, cudaStream_t s)
+              const TS *src, TS *dst, bool unit, cudaStream_t s)
     {
       constexpr int CPB  = apply_cells_per_block<N, NC, TS, Op::eval_u>();
       const size_t  smem = size_t(CPB) * apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
-      auto          k    = cell_apply_kernel<N, TS, T, NC, Op, CON>;
-      cudaError_t   e    = prepare(k, smem);
-      if (e != cudaSuccess)
+      cudaError_t   e    = cudaSuccess;
+      if (unit)
+        {
+          // element columns: one block per (cell, local DoF), constrained
+          // operators only (the coarse levels)
+          if constexpr (CON)
+            {
+              auto         ku    = cell_apply_kernel<N, TS, T, NC, Op, true, true, true>;
+              const size_t smemu = apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
+              if ((e = prepare(ku, smemu)) != cudaSuccess)
+                return e;
+              const size_t blocks = size_t(cg.cell_end - cg.cell_begin) * NC * N * N * N;
+              if (blocks == 0)
+                return cudaSuccess;
+              if (blocks > 0x7fffffffu || cg.color >= 0)
+                return cudaErrorInvalidValue;
+              ku<<<unsigned(blocks), N * N, smemu, s>>>(sh, cg, op, src, dst);
+              return cudaGetLastError();
+            }
+          return cudaErrorInvalidValue;
+        }
+      auto k = cell_apply_kernel<N, TS, T, NC, Op, CON>;
+      if ((e = prepare(k, smem)) != cudaSuccess)
         return e;
       if (cg.color == 8)
         {
@@ -71,11 +91,11 @@ namespace mfgpu
 
     template <int N, typename TS, typename T, int NC, class Op>
     cudaError_t
-    run_apply_c(bool con, const ShapeA<N, T> &sh, const CellGeom<T> &cg,
+    run_apply_c(const ApplyArgs &a, const ShapeA<N, T> &sh, const CellGeom<T> &cg,
                 const Op &op, const TS *src, TS *dst, cudaStream_t s)
     {
-      return con ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, s) :
-                   run_apply<N, TS, T, NC, Op, false>(sh, cg, op, src, dst, s);
+      return a.constrained ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, a.unit, s) :
+                             run_apply<N, TS, T, NC, Op, false>(sh, cg, op, src, dst, a.unit, s);
     }
   } // namespace
 
@@ -94,7 +114,7 @@ namespace mfgpu
         HeatQOp<T> op;
         for (int d = 0; d < 3; ++d)
           op.kd[d] = conv_host<T>(a.kdt / (g.h[d] * g.h[d]));
-        return run_apply_c<N, T, T, 1>(a.constrained, sh, cg, op, src, dst, s);
+        return run_apply_c<N, T, T, 1>(a, sh, cg, op, src, dst, s);
       }
     const NHMat<T> m     = to_mat<T>(a.mat);
     const T       *cache = static_cast<const T *>(a.cache);
@@ -107,7 +127,7 @@ namespace mfgpu
             op.scalar = cache;
             op.m      = m;
             op.n3     = N3;
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
         case V_QP10:
           {
@@ -117,7 +137,7 @@ namespace mfgpu
             op.n3    = N3;
             for (int d = 0; d < 3; ++d)
               op.mu_d[d] = conv_host<T>(a.mat.mu / (g.h[d] * g.h[d]));
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
         case V_TENSOR2:
           {
@@ -125,7 +145,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
         case V_TENSOR4:
           {
@@ -133,7 +153,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
         case V_TENSOR4_NS:
           {
@@ -141,7 +161,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
         case V_FORM0:
           {
@@ -149,7 +169,7 @@ namespace mfgpu
             op.cache = cache;
             op.m     = m;
             op.n3    = N3;
-            return run_apply_c<N, T, T, 3>(a.constrained, sh, cg, op, src, dst, s);
+            return run_apply_c<N, T, T, 3>(a, sh, cg, op, src, dst, s);
           }
       }
     return cudaErrorInvalidValue;
@@ -331,7 +351,7 @@ namespace mfgpu
         HeatQOp<df64> op;
         for (int d = 0; d < 3; ++d)
           op.kd[d] = conv_host<df64>(a.kdt / (g.h[d] * g.h[d]));
-        return run_apply_c<N, double, df64, 1>(a.constrained, sh, cg, op, src, dst, s);
+        return run_apply_c<N, double, df64, 1>(a, sh, cg, op, src, dst, s);
       }
     if (a.var != V_QP10)
       return cudaErrorInvalidValue;
@@ -341,7 +361,7 @@ namespace mfgpu
     op.n3    = N3;
     for (int d = 0; d < 3; ++d)
       op.mu_d[d] = conv_host<df64>(a.mat.mu / (g.h[d] * g.h[d]));
-    return run_apply_c<N, double, df64, 3>(a.constrained, sh, cg, op, src, dst, s);
+    return run_apply_c<N, double, df64, 3>(a, sh, cg, op, src, dst, s);
   }
 
   template <int N>

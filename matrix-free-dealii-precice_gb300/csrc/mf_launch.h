@@ -43,6 +43,10 @@ namespace mfgpu
     void       *dst;
     size_t      cell_begin = 0, cell_end = 0; // cell range; empty = all cells
     bool        colored = false; // all cells by parity colour, plain (non-atomic) scatter
+    // element columns: dst is the dense row-major m x m matrix (m = NC
+    // n_nodes, zeroed by the caller) and receives the operator's entries of
+    // the unconstrained rows and columns; src is not read
+    bool        unit = false;
   };
 
   template <int N, typename T>

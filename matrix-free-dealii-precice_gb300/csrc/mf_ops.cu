@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -230,7 +231,7 @@ namespace mfgpu
     err.alloc(sizeof(int) * 4);
     ticket.alloc(sizeof(unsigned) * 4);
     MF_CK(cudaMemsetAsync(ticket.ptr, 0, ticket.bytes, stream));
-    partial.alloc(sizeof(double) * RED_BLOCKS);
+    partial.alloc(sizeof(double) * 2 * RED_BLOCKS);
     scalars.alloc(sizeof(double) * 32);
     MF_CK(cudaMemsetAsync(err.ptr, 0, err.bytes, stream));
     MF_CK(cudaMemsetAsync(scalars.ptr, 0, scalars.bytes, stream));
@@ -263,6 +264,77 @@ namespace mfgpu
   Context::sync()
   {
     MF_CK(cudaStreamSynchronize(stream));
+  }
+
+  void
+  PhaseTimer::reset()
+  {
+    names.clear();
+    secs.clear();
+    calls.clear();
+    start = std::chrono::steady_clock::now();
+  }
+
+  int
+  PhaseTimer::index(const char *name)
+  {
+    for (size_t i = 0; i < names.size(); ++i)
+      if (names[i] == name)
+        return int(i);
+    names.emplace_back(name);
+    secs.push_back(0.0);
+    calls.push_back(0);
+    return int(names.size()) - 1;
+  }
+
+  std::string
+  PhaseTimer::summary() const
+  {
+    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    size_t       w     = 28; // "Total wallclock time elapsed"
+    for (const auto &n : names)
+      w = std::max(w, n.size());
+    const std::string rule = "+" + std::string(w + 2, '-') + "+-----------+------------+------------+\n";
+    char              line[512];
+    std::string       out = rule;
+    std::snprintf(line, sizeof(line), "| %-*s | %9s | %9.3gs | %10s |\n", int(w), "Total wallclock time elapsed", "",
+                  total, "");
+    out += line;
+    out += rule;
+    std::snprintf(line, sizeof(line), "| %-*s | %9s | %10s | %10s |\n", int(w), "Section", "no. calls", "wall time",
+                  "% of total");
+    out += line;
+    out += rule;
+    for (size_t i = 0; i < names.size(); ++i)
+      {
+        std::snprintf(line, sizeof(line), "| %-*s | %9ld | %9.3gs | %9.2g%% |\n", int(w), names[i].c_str(), calls[i],
+                      secs[i], total > 0 ? 100.0 * secs[i] / total : 0.0);
+        out += line;
+      }
+    out += rule;
+    return out;
+  }
+
+  PhaseTimer::Scope::Scope(PhaseTimer &t, Context *c, const char *name)
+    : t_(t.enabled ? &t : nullptr)
+    , c_(c)
+  {
+    if (!t_)
+      return;
+    c_->sync();
+    i_  = t_->index(name);
+    t0_ = std::chrono::steady_clock::now();
+  }
+
+  PhaseTimer::Scope::~Scope()
+  {
+    if (!t_)
+      return;
+    // no throw from a destructor: an error of the section's work surfaces
+    // at the next checked call
+    cudaStreamSynchronize(c_->stream);
+    t_->secs[size_t(i_)] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+    t_->calls[size_t(i_)] += 1;
   }
 
   double *
@@ -304,6 +376,16 @@ namespace mfgpu
   vec_fill(Context &c, size_t n, T v, T *x)
   {
     k_fill<<<grid_for(n), 256, 0, c.stream>>>(n, v, x);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  vec_estimate_start(Context &c, size_t n, T *x)
+  {
+    // the mean of the 0/1 pattern in double, rounded to T once
+    const double ones = double(n - (n + 10) / 11);
+    k_estimate_start<<<grid_for(n), 256, 0, c.stream>>>(n, T(n ? ones / double(n) : 0.0), x);
     count_launch();
     MF_CK(cudaGetLastError());
   }
@@ -384,6 +466,29 @@ namespace mfgpu
     count_launch();
     MF_CK(cudaGetLastError());
   }
+  template <typename T>
+  void
+  cg_update_jacobi(Context &c, size_t n, int num_slot, int den_slot, T *x, const T *p, T *r, const T *q,
+                   const T *dinv, T *z, int rr_slot, int rz_slot)
+  {
+    double *s = scalar_slots(c);
+    k_cg_update_jacobi<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+                                                                 dinv, z, c.partial.as<double>(),
+                                                                 c.ticket.as<unsigned>(), s + rr_slot,
+                                                                 s + rz_slot);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+  template <typename T>
+  void
+  cg_direction_rec(Context &c, size_t n, int rz, int rzn, int pq, int rr, const T *z, T *p, T *q_zero,
+                   double *rec, int *counter)
+  {
+    k_cg_direction_rec<<<grid_for(n), 256, 0, c.stream>>>(n, scalar_slots(c), rz, rzn, pq, rr, z, p, q_zero,
+                                                         rec, counter);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
   void
   lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int *counter)
   {
@@ -443,8 +548,49 @@ namespace mfgpu
     MF_CK(cudaGetLastError());
   }
 
+  static unsigned
+  warp_rows_grid(size_t n)
+  {
+    return unsigned((n * 32 + 255) / 256);
+  }
+
+  void
+  dense_mv(Context &c, int precision, size_t n, const void *A, const void *x, void *y, bool add)
+  {
+    if (precision == 32)
+      k_dense_mv<float><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, static_cast<const float *>(A),
+                                                                 static_cast<const float *>(x),
+                                                                 static_cast<float *>(y), int(add));
+    else
+      k_dense_mv<double><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, static_cast<const double *>(A),
+                                                                  static_cast<const double *>(x),
+                                                                  static_cast<double *>(y), int(add));
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+
+  void
+  dense_constrained_identity(Context &c, int precision, const LevelGeom &g, int nc, void *A)
+  {
+    if (precision == 32)
+      constrained_op<float>(c, g, nc, 4, nullptr, static_cast<float *>(A));
+    else
+      constrained_op<double>(c, g, nc, 4, nullptr, static_cast<double *>(A));
+  }
+
+  template <typename T>
+  void
+  cheby_dense_step(Context &c, size_t n, const T *A, T f1, T f2, bool first, const T *b, const T *dinv,
+                   const T *x, T *xo)
+  {
+    k_cheby_dense<T><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, A, f1, f2, int(first), b, dinv, x, xo);
+    count_launch();
+    MF_CK(cudaGetLastError());
+  }
+
 #define MF_INST_VEC(T)                                                                      \
   template void vec_fill<T>(Context &, size_t, T, T *);                                     \
+  template void vec_estimate_start<T>(Context &, size_t, T *);                              \
   template void vec_axpby<T>(Context &, size_t, T, const T *, T, T *);                      \
   template void vec_axpbyz<T>(Context &, size_t, T, const T *, T, const T *, T *);          \
   template void vec_copy<T>(Context &, size_t, const T *, T *);                             \
@@ -454,7 +600,11 @@ namespace mfgpu
   template double vec_dot<T>(Context &, size_t, const T *, const T *);                      \
   template void cg_update<T>(Context &, size_t, int, int, T *, const T *, T *, const T *, int); \
   template void cg_direction<T>(Context &, size_t, int, int, const T *, T *);               \
+  template void cg_update_jacobi<T>(Context &, size_t, int, int, T *, const T *, T *, const T *, const T *, T *, \
+                                    int, int);                                                                 \
+  template void cg_direction_rec<T>(Context &, size_t, int, int, int, int, const T *, T *, T *, double *, int *); \
   template void cheby_start<T>(Context &, size_t, T, const T *, const T *, T *, T *);       \
+  template void cheby_dense_step<T>(Context &, size_t, const T *, T, T, bool, const T *, const T *, const T *, T *); \
   template void cheby_update<T>(Context &, size_t, T, T, bool, const T *, const T *, const T *, T *, T *); \
   template void constrained_op<T>(Context &, const LevelGeom &, int, int, const T *, T *);
   MF_INST_VEC(float)
@@ -554,6 +704,11 @@ namespace mfgpu
   void
   Operator::vmult(void *dst, const void *src)
   {
+    if (use_dense())
+      {
+        dense_mv(*ctx, precision, m(), dense.ptr, src, dst, false);
+        return;
+      }
     // dst = 0, then dst += A src (constrained rows: dst += src, in the cell kernel)
     MF_CK(cudaMemsetAsync(dst, 0, m() * elem_size(), ctx->stream));
     apply_cells(dst, src);
@@ -562,7 +717,71 @@ namespace mfgpu
   void
   Operator::vmult_add(void *dst, const void *src)
   {
+    if (use_dense())
+      {
+        dense_mv(*ctx, precision, m(), dense.ptr, src, dst, true);
+        return;
+      }
     apply_cells(dst, src);
+  }
+
+  void
+  Operator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
+  {
+    ApplyArgs a  = cell_args();
+    a.src        = src;
+    a.dst        = dst;
+    a.cell_begin = c0;
+    a.cell_end   = c1;
+    a.colored    = scatter == 1;
+    if (geom.dim == 2)
+      {
+        check_2d();
+        MF_CK(launch_apply2d(basis.N, precision, basis, geom, a, s));
+        count_launch();
+        return;
+      }
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, s);
+    count_launch(cell_launches(c0, c1));
+    MF_CK(e);
+  }
+
+  bool
+  Operator::dense_fits() const
+  {
+    const size_t n = m();
+    return geom.dim == 3 && constrained && n > 0 && n <= DENSE_MAX_BYTES / elem_size() / n;
+  }
+
+  void
+  Operator::assemble_dense()
+  {
+    if (!dense_fits())
+      throw Error(ERR_UNSUPPORTED, "dense copy: three-dimensional constrained operators of at most " +
+                                     std::to_string(DENSE_MAX_BYTES >> 20) + " MiB only");
+    const size_t n = m();
+    ApplyArgs    a = cell_args();
+    dense.ensure(n * n * elem_size());
+    MF_CK(cudaMemsetAsync(dense.ptr, 0, dense.bytes, ctx->stream));
+    a.dst  = dense.ptr;
+    a.unit = true;
+    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
+                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
+                                      dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);
+    count_launch();
+    MF_CK(e);
+    dense_constrained_identity(*ctx, precision, geom, nc, dense.ptr);
+    dense_key = value_state();
+    dense_on  = true;
+  }
+
+  void
+  Operator::drop_dense()
+  {
+    dense.release();
+    dense_on = false;
   }
 
 
@@ -667,6 +886,12 @@ namespace mfgpu
   HeatOperator::vmult_state() const
   {
     return hmix(hmix(Operator::vmult_state(), hbits(delta_t)), hbits(coefficient));
+  }
+
+  size_t
+  NHOperator::value_state() const
+  {
+    return hmix(vmult_state(), cache_gen);
   }
 
   size_t
@@ -853,8 +1078,8 @@ namespace mfgpu
       throw Error(ERR_NONFINITE, "non-positive diagonal entry in a positive definite operator");
   }
 
-  void
-  HeatOperator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
+  ApplyArgs
+  HeatOperator::cell_args() const
   {
     if (delta_t <= 0)
       throw Error(ERR_STATE, "delta_t not set (set_delta_t)");
@@ -862,23 +1087,7 @@ namespace mfgpu
     a.kind        = 0;
     a.constrained = constrained;
     a.kdt         = coefficient * delta_t;
-    a.src         = src;
-    a.dst         = dst;
-    a.cell_begin  = c0;
-    a.cell_end    = c1;
-    a.colored     = scatter == 1;
-    if (geom.dim == 2)
-      {
-        check_2d();
-        MF_CK(launch_apply2d(basis.N, precision, basis, geom, a, s));
-        count_launch();
-        return;
-      }
-    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
-                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
-                                      dispatch_apply<double>(basis.N, basis, geom, a, s);
-    count_launch(cell_launches(c0, c1));
-    MF_CK(e);
+    return a;
   }
 
   void
@@ -886,8 +1095,8 @@ namespace mfgpu
   {
     if (delta_t <= 0)
       throw Error(ERR_STATE, "delta_t not set (set_delta_t)");
-    inv_diag.alloc(m() * elem_size());
-    diag.alloc(m() * elem_size());
+    inv_diag.ensure(m() * elem_size());
+    diag.ensure(m() * elem_size());
     MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
     NHMatD md{};
     if (geom.dim == 2)
@@ -946,6 +1155,7 @@ namespace mfgpu
       throw Error(ERR_STATE, "NeoHookOperator: initialize() with a displacement first");
     if (!have_material)
       throw Error(ERR_STATE, "NeoHookOperator: set_material() first");
+    ++cache_gen; // the cached data changes (a dense copy goes stale)
     int var = variant;
     if (formulation == 0)
       {
@@ -1005,8 +1215,8 @@ namespace mfgpu
     cached = true;
   }
 
-  void
-  NHOperator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
+  ApplyArgs
+  NHOperator::cell_args() const
   {
     if (!cached)
       throw Error(ERR_STATE, "NeoHookOperator: cache() before vmult");
@@ -1017,23 +1227,7 @@ namespace mfgpu
     a.mat         = mat;
     a.cache       = cache.ptr;
     a.ucell       = ucell.ptr;
-    a.src         = src;
-    a.dst         = dst;
-    a.cell_begin  = c0;
-    a.cell_end    = c1;
-    a.colored     = scatter == 1;
-    if (geom.dim == 2)
-      {
-        check_2d();
-        MF_CK(launch_apply2d(basis.N, precision, basis, geom, a, s));
-        count_launch();
-        return;
-      }
-    cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
-                    arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
-                                      dispatch_apply<double>(basis.N, basis, geom, a, s);
-    count_launch(cell_launches(c0, c1));
-    MF_CK(e);
+    return a;
   }
 
   void
@@ -1041,8 +1235,8 @@ namespace mfgpu
   {
     if (!u || !have_material)
       throw Error(ERR_STATE, "NeoHookOperator: initialize() and set_material() first");
-    inv_diag.alloc(m() * elem_size());
-    diag.alloc(m() * elem_size());
+    inv_diag.ensure(m() * elem_size());
+    diag.ensure(m() * elem_size());
     MF_CK(cudaMemsetAsync(inv_diag.ptr, 0, inv_diag.bytes, ctx->stream));
     const int kind = formulation == 0 ? 2 : 1;
     if (geom.dim == 2)

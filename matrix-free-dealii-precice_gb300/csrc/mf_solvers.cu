@@ -81,27 +81,41 @@ namespace mfgpu
   template <typename T>
   CGStats
   cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol, int maxit,
-             int check)
+             int check, DevBuf *ws, double *host_rec)
   {
     CGStats      st;
     const size_t n = A.size();
-    DevBuf       rb(n * sizeof(T)), zb(n * sizeof(T)), pb(n * sizeof(T)), qb(n * sizeof(T));
-    DevBuf       recb(sizeof(double) * 3 * size_t(std::max(maxit, 1)));
-    T *r = rb.as<T>(), *z = zb.as<T>(), *p = pb.as<T>(), *q = qb.as<T>();
-    double *rec = recb.as<double>();
+    // r, z, p, q, the Lanczos records and the record counter in one
+    // allocation (256-byte aligned parts)
+    const size_t vb    = (n * sizeof(T) + 255) / 256 * 256;
+    const size_t recb  = (sizeof(double) * 3 * size_t(std::max(maxit, 1)) + 255) / 256 * 256;
+    const size_t total = 4 * vb + recb + 256;
+    DevBuf       own;
+    DevBuf      &W = ws ? *ws : own;
+    if (W.bytes < total)
+      W.alloc(total);
+    char   *base = static_cast<char *>(W.ptr);
+    T      *r = reinterpret_cast<T *>(base), *z = reinterpret_cast<T *>(base + vb);
+    T      *p = reinterpret_cast<T *>(base + 2 * vb), *q = reinterpret_cast<T *>(base + 3 * vb);
+    double *rec     = reinterpret_cast<double *>(base + 4 * vb);
+    int    *counter = reinterpret_cast<int *>(base + 4 * vb + recb);
     A.vmult(r, x);
     vec_axpby<T>(c, n, T(1), b, T(-1), r);
     vec_dot_dev<T>(c, n, r, r, S_RR);
-    read_scalars(c, S_RR + 1);
-    double res = std::sqrt(c.host_scalars[S_RR]);
-    st.res0    = res;
-    st.res     = res;
-    if (!std::isfinite(res))
-      throw Error(ERR_NONFINITE, "CG: non-finite residual");
-    if (res <= tol)
+    double res = 0;
+    if (!host_rec)
       {
-        st.converged = true;
-        return st;
+        read_scalars(c, S_RR + 1);
+        res     = std::sqrt(c.host_scalars[S_RR]);
+        st.res0 = res;
+        st.res  = res;
+        if (!std::isfinite(res))
+          throw Error(ERR_NONFINITE, "CG: non-finite residual");
+        if (res <= tol)
+          {
+            st.converged = true;
+            return st;
+          }
       }
     if (P)
       P->vmult(z, r);
@@ -111,10 +125,23 @@ namespace mfgpu
     vec_copy<T>(c, n, z, p);
     int                 rz = S_RZ, rzn = S_RZN;
     std::vector<double> h;
-    DevBuf              cntb(sizeof(int));
-    int                *counter = cntb.as<int>();
     MF_CK(cudaMemsetAsync(counter, 0, sizeof(int), c.stream));
+    // point-Jacobi preconditioner and an operator that adds: four launches
+    // per iteration (q = A p into the q that the previous direction kernel
+    // zeroed; p.q; x, r, z with |r|^2 and r.z; p and the record)
+    const T *jd = P ? P->jacobi_diagonal() : nullptr;
+    if (jd && A.can_add())
+      MF_CK(cudaMemsetAsync(q, 0, n * sizeof(T), c.stream));
     auto iteration = [&]() {
+      if (jd && A.can_add())
+        {
+          A.vmult_add(q, p);
+          vec_dot_dev<T>(c, n, p, q, S_PQ);
+          cg_update_jacobi<T>(c, n, rz, S_PQ, x, p, r, q, jd, z, S_RR, rzn);
+          cg_direction_rec<T>(c, n, rz, rzn, S_PQ, S_RR, z, p, q, rec, counter);
+          std::swap(rz, rzn);
+          return;
+        }
       A.vmult(q, p);
       vec_dot_dev<T>(c, n, p, q, S_PQ);
       cg_update<T>(c, n, rz, S_PQ, x, p, r, q, S_RR);
@@ -127,6 +154,14 @@ namespace mfgpu
       lanczos_record(c, rz, rzn, S_PQ, S_RR, rec, counter);
       std::swap(rz, rzn);
     };
+    if (host_rec)
+      {
+        for (int j = 0; j < maxit; ++j)
+          iteration();
+        MF_CK(cudaMemcpyAsync(host_rec, rec, sizeof(double) * 3 * size_t(maxit), cudaMemcpyDeviceToHost,
+                              c.stream));
+        return st;
+      }
     // a full batch (an even number of iterations, so the slot roles repeat)
     // is the same work every time: the second one is captured into a CUDA
     // graph and the later ones replay it
@@ -206,8 +241,32 @@ namespace mfgpu
     return st;
   }
 
-  template CGStats cg_lanczos<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, int);
-  template CGStats cg_lanczos<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, int);
+  template CGStats cg_lanczos<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int,
+                                      int, DevBuf *, double *);
+  template CGStats cg_lanczos<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, int,
+                                     DevBuf *, double *);
+
+  CGStats
+  lanczos_collect(const double *h, int maxit, double tol)
+  {
+    CGStats st;
+    for (int j = 0; j < maxit; ++j)
+      {
+        const double res = std::sqrt(h[3 * j + 1]);
+        st.its           = j + 1;
+        st.res           = res;
+        st.alpha.push_back(h[3 * j]);
+        if (!std::isfinite(res))
+          throw Error(ERR_NONFINITE, "CG: non-finite residual");
+        if (res <= tol)
+          {
+            st.converged = true;
+            return st;
+          }
+        st.beta.push_back(h[3 * j + 2]);
+      }
+    return st;
+  }
 
   template CGStats cg_solve<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, bool, bool);
   template CGStats cg_solve<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, bool, bool);
@@ -265,6 +324,7 @@ namespace mfgpu
     {
       vec_scale<T>(*ctx, A->m(), T(1), A->inv_diag.as<T>(), src, dst);
     }
+    const T *jacobi_diagonal() const override { return A->inv_diag.as<T>(); }
   };
 
   template <typename T>
@@ -272,29 +332,66 @@ namespace mfgpu
   Chebyshev<T>::estimate()
   {
     const size_t n = A->m();
-    xold.alloc(n * sizeof(T));
-    t1.alloc(n * sizeof(T));
-    w0.alloc(n * sizeof(T));
-    w1.alloc(n * sizeof(T));
+    xold.ensure(n * sizeof(T));
+    t1.ensure(n * sizeof(T));
+    w0.ensure(n * sizeof(T));
+    w1.ensure(n * sizeof(T));
     // initial guess with high-frequency content and the constant mode:
     // entries 1 except every 11th, mean removed
-    std::vector<T> h(n);
-    double         mean = 0;
-    for (size_t i = 0; i < n; ++i)
-      {
-        h[i] = (i % 11 == 0) ? T(0) : T(1);
-        mean += double(h[i]);
-      }
-    mean /= double(n);
-    for (size_t i = 0; i < n; ++i)
-      h[i] -= T(mean);
-    MF_CK(cudaMemcpyAsync(w0.ptr, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    vec_estimate_start<T>(*ctx, n, w0.as<T>());
     MF_CK(cudaMemsetAsync(w1.ptr, 0, n * sizeof(T), ctx->stream));
     OpRef<T>     Aop(A);
     JacobiPre<T> P;
-    P.ctx     = ctx;
-    P.A       = A;
-    CGStats st = cg_lanczos<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations);
+    P.ctx      = ctx;
+    P.A        = A;
+    CGStats st = cg_lanczos<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, 8, &cg_ws);
+    set_bounds(st);
+  }
+
+  template <typename T>
+  void
+  Chebyshev<T>::estimate_begin(Context *ec)
+  {
+    const size_t n = A->m();
+    xold.ensure(n * sizeof(T));
+    t1.ensure(n * sizeof(T));
+    w0.ensure(n * sizeof(T));
+    w1.ensure(n * sizeof(T));
+    host_rec.ensure(3 * size_t(std::max(eig_cg_iterations, 1)));
+    // the operator launches on ec's stream until the work is enqueued
+    struct Restore
+    {
+      Operator *op;
+      Context  *c;
+      ~Restore() { op->ctx = c; }
+    } restore{A, A->ctx};
+    A->ctx = ec;
+    vec_estimate_start<T>(*ec, n, w0.as<T>());
+    MF_CK(cudaMemsetAsync(w1.ptr, 0, n * sizeof(T), ec->stream));
+    OpRef<T>     Aop(A);
+    JacobiPre<T> P;
+    P.ctx = ec;
+    P.A   = A;
+    cg_lanczos<T>(*ec, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, 8, &cg_ws, host_rec.p);
+    est_ctx = ec;
+  }
+
+  template <typename T>
+  void
+  Chebyshev<T>::estimate_end()
+  {
+    if (!est_ctx)
+      throw Error(ERR_STATE, "Chebyshev: estimate_end without estimate_begin");
+    Context *ec = est_ctx;
+    est_ctx     = nullptr;
+    MF_CK(cudaStreamSynchronize(ec->stream));
+    set_bounds(lanczos_collect(host_rec.p, eig_cg_iterations, 1e-10));
+  }
+
+  template <typename T>
+  void
+  Chebyshev<T>::set_bounds(const CGStats &st)
+  {
     const size_t k = st.alpha.size();
     if (k == 0)
       lambda_min = lambda_max = 1.0;
@@ -334,6 +431,25 @@ namespace mfgpu
     if (degree < 2)
       return;
     double rhok = delta / theta, sigma = theta / delta;
+    if (A->use_dense())
+      {
+        // dense operator: each step is one kernel (row products and the
+        // update); the new iterate goes into the older buffer, then the two
+        // swap
+        const T *Ad  = A->dense.as<T>();
+        T       *cur = x, *old = xold.as<T>();
+        for (unsigned k = 0; k + 1 < degree; ++k)
+          {
+            const double rhokp = 1. / (2. * sigma - rhok);
+            const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
+            rhok = rhokp;
+            cheby_dense_step<T>(*ctx, n, Ad, T(f1), T(f2), k == 0, b, dinv, cur, old);
+            std::swap(cur, old);
+          }
+        if (cur != x)
+          vec_copy<T>(*ctx, n, cur, x);
+        return;
+      }
     for (unsigned k = 0; k + 1 < degree; ++k)
       {
         A->vmult(t1.ptr, x);
@@ -396,8 +512,12 @@ namespace mfgpu
   {
     drop_graph();
     const int L = int(ops.size());
-    smoothers.clear();
-    smoothers.resize(L);
+    // the smoothers keep their work buffers across setups (same level sizes)
+    if (int(smoothers.size()) != L)
+      {
+        smoothers.clear();
+        smoothers.resize(L);
+      }
     sol.resize(L);
     def.resize(L);
     tmp.resize(L);
@@ -429,22 +549,58 @@ namespace mfgpu
       }
     if (coarse64)
       {
-        coarse_cheb64                   = Chebyshev<double>();
         coarse_cheb64.ctx               = ctx;
         coarse_cheb64.A                 = coarse64;
         coarse_cheb64.smoothing_range   = 1e-3;
         coarse_cheb64.degree            = 0;
         coarse_cheb64.eig_cg_iterations = coarse_eig_its;
-        c64_sol.alloc(coarse64->m() * sizeof(double));
-        c64_def.alloc(coarse64->m() * sizeof(double));
+        coarse_cheb64.initialized       = false;
+        c64_sol.ensure(coarse64->m() * sizeof(double));
+        c64_def.ensure(coarse64->m() * sizeof(double));
       }
     // eigenvalue bounds of every smoother now (PreconditionChebyshev
     // estimates on its first vmult; here setup carries that cost)
+    // The level estimates are independent: the ones with a fixed, small
+    // iteration count are enqueued on their own contexts (finest first,
+    // no host wait), the coarse one with m() iterations and convergence
+    // checks runs on the main stream meanwhile; the small, launch-bound
+    // levels then overlap instead of adding up.
+    std::vector<int> deferred;
+    for (int l = L - 1; l >= 0; --l)
+      if ((l > 0 || !coarse64) && smoothers[l].eig_cg_iterations <= 64)
+        deferred.push_back(l);
+    if (!deferred.empty())
+      {
+        if (int(aux.size()) < L)
+          aux.resize(L);
+        if (!setup_ev)
+          MF_CK(cudaEventCreateWithFlags(&setup_ev, cudaEventDisableTiming));
+        // the diagonals and caches were written on the main stream
+        MF_CK(cudaEventRecord(setup_ev, ctx->stream));
+        for (int l : deferred)
+          {
+            if (!aux[l])
+              aux[l].reset(new Context(ctx->device));
+            MF_CK(cudaStreamWaitEvent(aux[l]->stream, setup_ev, 0));
+            smoothers[l].estimate_begin(aux[l].get());
+          }
+      }
     for (int l = 0; l < L; ++l)
-      if (l > 0 || !coarse64)
+      if ((l > 0 || !coarse64) && smoothers[l].eig_cg_iterations > 64)
         smoothers[l].estimate();
     if (coarse64)
       coarse_cheb64.estimate();
+    for (int l : deferred)
+      smoothers[l].estimate_end();
+  }
+
+  template <typename T>
+  Multigrid<T>::~Multigrid()
+  {
+    drop_graph();
+    aux.clear(); // synchronises their streams
+    if (setup_ev)
+      cudaEventDestroy(setup_ev);
   }
 
   template <typename T>

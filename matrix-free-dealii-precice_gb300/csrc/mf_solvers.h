@@ -23,6 +23,9 @@ namespace mfgpu
     virtual ~LinOp() = default;
     virtual size_t size() const = 0;
     virtual void   vmult(T *dst, const T *src) = 0;
+    // dst += A src, where the operator offers it (can_add())
+    virtual bool can_add() const { return false; }
+    virtual void vmult_add(T *, const T *) {}
   };
 
   template <typename T>
@@ -34,6 +37,8 @@ namespace mfgpu
     {}
     size_t size() const override { return op->m(); }
     void   vmult(T *dst, const T *src) override { op->vmult(dst, src); }
+    bool   can_add() const override { return true; }
+    void   vmult_add(T *dst, const T *src) override { op->vmult_add(dst, src); }
   };
 
   template <typename T>
@@ -41,6 +46,9 @@ namespace mfgpu
   {
     virtual ~Precond() = default;
     virtual void vmult(T *dst, const T *src) = 0;
+    // the inverse diagonal of a point-Jacobi preconditioner (omega = 1), so
+    // that CG can fuse it into its vector update; null otherwise
+    virtual const T *jacobi_diagonal() const { return nullptr; }
   };
 
   struct CGStats
@@ -64,9 +72,16 @@ namespace mfgpu
   // device and the convergence test made every `check` iterations (the
   // coefficients of iterations past convergence are discarded), so the
   // host waits once per `check` iterations instead of twice per iteration
+  // (ws: optional workspace kept by the caller across calls; grown to fit)
+  // host_rec (pinned, >= 3 maxit doubles): deferred mode.  All maxit
+  // iterations are enqueued without a host wait and the records are copied
+  // to host_rec on the context's stream; after the stream has finished,
+  // lanczos_collect turns them into the statistics (iterations past
+  // convergence discarded as above).
   template <typename T>
   CGStats cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol,
-                     int maxit, int check = 8);
+                     int maxit, int check = 8, DevBuf *ws = nullptr, double *host_rec = nullptr);
+  CGStats lanczos_collect(const double *host_rec, int maxit, double tol);
 
   template <typename T>
   struct Chebyshev
@@ -78,8 +93,16 @@ namespace mfgpu
     int       eig_cg_iterations = 30;
     bool      initialized       = false;
     double    theta = 0, delta = 0, lambda_max = 0, lambda_min = 0;
-    DevBuf    xold, t1, w0, w1;
+    DevBuf     xold, t1, w0, w1;
+    DevBuf     cg_ws;    // work vectors of the eigenvalue-estimate CG, kept across setups
+    HostPinned host_rec; // Lanczos records of a deferred estimate
+    Context   *est_ctx = nullptr;
     void estimate();
+    // the same estimate enqueued on another context's stream (the operator
+    // launches there meanwhile), finished by estimate_end()
+    void estimate_begin(Context *ec);
+    void estimate_end();
+    void set_bounds(const CGStats &st);
     void vmult(T *x, const T *b); // zero initial guess
     void step(T *x, const T *b);  // nonzero initial guess
   };
@@ -102,13 +125,17 @@ namespace mfgpu
     // pair) and later applications with the same pair replay it.  setup()
     // drops the graph (new eigenvalue bounds and diagonals).
     bool               use_graphs = false;
+    // contexts (streams, scalar slots, reduction buffers) of the level
+    // eigenvalue estimates, which run concurrently in setup()
+    std::vector<std::unique_ptr<Context>> aux;
+    cudaEvent_t                           setup_ev = nullptr;
+    ~Multigrid();
     cudaGraphExec_t    gexec      = nullptr;
     double            *g_dst      = nullptr;
     const double      *g_src      = nullptr;
     long long          g_launches = 0;
     bool               eager_done = false;
     int                graph_replays = 0;
-    ~Multigrid() { drop_graph(); }
     void setup(double range, unsigned degree, int eig_its, int coarse_eig_its);
     void level_v_step(int l);
     void vmult(double *dst, const double *src) override;

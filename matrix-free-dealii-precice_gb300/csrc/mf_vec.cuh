@@ -41,6 +41,15 @@ namespace mfgpu
       z[i] = a * x[i] + b * y[i];
   }
 
+  template <typename T>
+  __global__ void
+  k_estimate_start(size_t n, T mean, T *__restrict__ x)
+  {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      x[i] = (i % 11 == 0 ? T(0) : T(1)) - mean;
+  }
+
   template <typename TD, typename TS>
   __global__ void
   k_convert(size_t n, const TS *__restrict__ s, TD *__restrict__ d)
@@ -128,16 +137,78 @@ namespace mfgpu
       }
   }
 
+  // two reductions of one launch: partial holds 2 gridDim.x values
+  __device__ __forceinline__ void
+  finish_partials2(double s0, double s1, double *__restrict__ partial, unsigned *ticket,
+                   double *__restrict__ out0, double *__restrict__ out1)
+  {
+    __shared__ bool last;
+    if (threadIdx.x == 0)
+      {
+        partial[blockIdx.x]              = s0;
+        partial[gridDim.x + blockIdx.x]  = s1;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+      }
+    __syncthreads();
+    if (!last)
+      return;
+    __threadfence();
+    double r0 = 0, r1 = 0;
+    for (int i = threadIdx.x; i < int(gridDim.x); i += blockDim.x)
+      {
+        r0 += __ldcg(partial + i);
+        r1 += __ldcg(partial + gridDim.x + i);
+      }
+    r0 = block_sum(r0);
+    __syncthreads(); // block_sum's shared scratch is reused
+    r1 = block_sum(r1);
+    if (threadIdx.x == 0)
+      {
+        *out0   = r0;
+        *out1   = r1;
+        *ticket = 0u;
+      }
+  }
+
+  // per-thread sum of products x y: FP64 fused multiply-adds for double
+  // vectors; for float vectors a compensated float pair on the FP32 pipe
+  // (the product's rounding error from an FMA, the sum's from TwoSum), as
+  // accurate as FP64 accumulation for the few terms one thread adds
+  template <typename T>
+  struct ProdAcc
+  {
+    double s = 0;
+    __device__ __forceinline__ void add(T x, T y) { s = fma(double(x), double(y), s); }
+    __device__ __forceinline__ double value() const { return s; }
+  };
+  template <>
+  struct ProdAcc<float>
+  {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void
+    add(float x, float y)
+    {
+      const float p = __fmul_rn(x, y);
+      const float e = __fmaf_rn(x, y, -p);
+      float       s, t;
+      two_sum(hi, p, s, t);
+      hi = s;
+      lo = __fadd_rn(lo, __fadd_rn(t, e));
+    }
+    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+  };
+
   template <typename T>
   __global__ void __launch_bounds__(RED_THREADS)
   k_dot(size_t n, const T *__restrict__ x, const T *__restrict__ y,
         double *__restrict__ partial, unsigned *ticket, double *__restrict__ out)
   {
-    double s = 0;
+    ProdAcc<T> s;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
-      s += double(x[i]) * double(y[i]);
-    finish_partials(block_sum(s), partial, ticket, out);
+      s.add(x[i], y[i]);
+    finish_partials(block_sum(s.value()), partial, ticket, out);
   }
 
   // CG update x += alpha p, r -= alpha q with alpha = num/den, and |r|^2
@@ -148,17 +219,72 @@ namespace mfgpu
                  const T *__restrict__ q, double *__restrict__ partial, unsigned *ticket,
                  double *__restrict__ out)
   {
-    const T alpha = T(*num / *den);
-    double  s     = 0;
+    const T    alpha = T(*num / *den);
+    ProdAcc<T> s;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       {
         x[i] += alpha * p[i];
         const T rr = r[i] - alpha * q[i];
         r[i]       = rr;
-        s += double(rr) * double(rr);
+        s.add(rr, rr);
       }
-    finish_partials(block_sum(s), partial, ticket, out);
+    finish_partials(block_sum(s.value()), partial, ticket, out);
+  }
+
+  // Jacobi-preconditioned CG step: x += alpha p, r -= alpha q (alpha =
+  // num/den), z = dinv r, and |r|^2 -> out_rr, r.z -> out_rz
+  template <typename T>
+  __global__ void __launch_bounds__(RED_THREADS)
+  k_cg_update_jacobi(size_t n, const double *__restrict__ num, const double *__restrict__ den,
+                     T *__restrict__ x, const T *__restrict__ p, T *__restrict__ r,
+                     const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z,
+                     double *__restrict__ partial, unsigned *ticket, double *__restrict__ out_rr,
+                     double *__restrict__ out_rz)
+  {
+    const T    alpha = T(*num / *den);
+    ProdAcc<T> srr, srz;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        x[i] += alpha * p[i];
+        const T rr = r[i] - alpha * q[i];
+        const T zz = T(1) * dinv[i] * rr;
+        r[i]       = rr;
+        z[i]       = zz;
+        srr.add(rr, rr);
+        srz.add(rr, zz);
+      }
+    const double a = block_sum(srr.value());
+    __syncthreads(); // block_sum's shared scratch is reused
+    const double b = block_sum(srz.value());
+    finish_partials2(a, b, partial, ticket, out_rr, out_rz);
+  }
+
+  // p = z + beta p (beta = s[rzn]/s[rz]); q = 0 for the next application
+  // (q_zero, may be null); and the Lanczos record of this iteration
+  // (k_lanczos_record) written by one thread
+  template <typename T>
+  __global__ void
+  k_cg_direction_rec(size_t n, const double *__restrict__ s, int rz, int rzn, int pq, int rr,
+                     const T *__restrict__ z, T *__restrict__ p, T *__restrict__ q_zero,
+                     double *__restrict__ rec, int *__restrict__ counter)
+  {
+    const T beta = T(s[rzn] / s[rz]);
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+      {
+        p[i] = z[i] + beta * p[i];
+        if (q_zero)
+          q_zero[i] = T(0);
+      }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      {
+        const int k    = (*counter)++;
+        rec[3 * k]     = s[rz] / s[pq];
+        rec[3 * k + 1] = s[rr];
+        rec[3 * k + 2] = s[rzn] / s[rz];
+      }
   }
 
   // p = z + beta p,  beta = num/den
@@ -226,6 +352,57 @@ namespace mfgpu
   // numbered face that constrains that component at that node.
   // op: 0 dst = src, 1 dst += src, 2 dst = 0, 3 dst = 1
   // ---------------------------------------------------------------------
+  // ---------------------------------------------------------------------
+  // Dense row-major n x n operators (small coarse levels): one warp per row
+  // ---------------------------------------------------------------------
+  template <typename T>
+  __device__ __forceinline__ T
+  dense_row_dot(size_t n, const T *__restrict__ row, const T *__restrict__ x, int lane)
+  {
+    T s = T(0);
+    for (size_t j = size_t(lane); j < n; j += 32)
+      s = fma(row[j], x[j], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      s += __shfl_down_sync(0xffffffffu, s, o);
+    return s;
+  }
+
+  // y = A x (add: y += A x)
+  template <typename T>
+  __global__ void
+  k_dense_mv(size_t n, const T *__restrict__ A, const T *__restrict__ x, T *__restrict__ y, int add)
+  {
+    const size_t row  = (blockIdx.x * size_t(blockDim.x) + threadIdx.x) / 32;
+    const int    lane = int(threadIdx.x & 31u);
+    if (row >= n) // whole warps leave together
+      return;
+    const T s = dense_row_dot(n, A + row * n, x, lane);
+    if (lane == 0)
+      y[row] = add ? y[row] + s : s;
+  }
+
+  // one Chebyshev step with the dense operator (k_cheby_update with
+  // Ax = A x computed in place): xo <- the new iterate; x keeps the
+  // current one (the caller swaps the two)
+  template <typename T>
+  __global__ void
+  k_cheby_dense(size_t n, const T *__restrict__ A, T f1, T f2, int first, const T *__restrict__ b,
+                const T *__restrict__ dinv, const T *__restrict__ x, T *__restrict__ xo)
+  {
+    const size_t i    = (blockIdx.x * size_t(blockDim.x) + threadIdx.x) / 32;
+    const int    lane = int(threadIdx.x & 31u);
+    if (i >= n)
+      return;
+    const T s = dense_row_dot(n, A + i * n, x, lane);
+    if (lane == 0)
+      {
+        const T t  = dinv[i] * (b[i] - s);
+        const T xi = x[i];
+        xo[i]      = first ? (T(1) + f1) * xi + f2 * t : xi + f1 * (xi - xo[i]) + f2 * t;
+      }
+  }
+
   struct FaceInfo
   {
     int      Nn[3];
@@ -274,8 +451,10 @@ namespace mfgpu
               dst[i] += src[i];
             else if (op == 2)
               dst[i] = T(0);
-            else
+            else if (op == 3)
               dst[i] = T(1);
+            else // dense matrix: unit diagonal entry of row i
+              dst[i * (size_t(fi.nc) * fi.n_nodes + 1)] = T(1);
           }
       }
   }

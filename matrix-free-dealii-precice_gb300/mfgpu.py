@@ -50,7 +50,7 @@ class SolverParams(C.Structure):
                 ("cheb_eig_its", C.c_int), ("coarse_accurate", C.c_int),
                 ("mg_precision", C.c_int), ("coarse_fp64", C.c_int),
                 ("fp64_emulation", C.c_int),
-                ("cuda_graphs", C.c_int)]
+                ("cuda_graphs", C.c_int), ("coarse_dense", C.c_int)]
 
 
 class SolidParams(C.Structure):
@@ -114,6 +114,22 @@ def lib():
 def _check(rc):
     if rc != OK:
         raise MfgpuError(rc, lib().mfgpu_last_error().decode())
+
+
+def _text(call, size=1 << 16):
+    buf = C.create_string_buffer(size)
+    _check(call(buf, C.c_size_t(size)))
+    return buf.value.decode()
+
+
+def timing_table(text):
+    """{section: (calls, seconds)} from a timing summary."""
+    out = {}
+    for line in text.splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) == 4 and cells[1].isdigit():
+            out[cells[0]] = (int(cells[1]), float(cells[2].rstrip("s")))
+    return out
 
 
 def launch_count():
@@ -242,6 +258,11 @@ class _Operator:
         """0: atomic scatter; 1: parity-coloured plain scatter (deterministic)."""
         _check(lib().mfgpu_operator_set_scatter(self.h, {"atomic": 0, "colored": 1}.get(mode, mode)))
 
+    def set_dense(self, enable=True):
+        """Dense copy of a small operator (assembled now; used while the
+        operator's state is unchanged)."""
+        _check(lib().mfgpu_operator_set_dense(self.h, int(enable)))
+
     def set_host_chunks(self, n_chunks):
         """z-slabs of the overlapped vmult_host (0 auto, 1 no overlap)."""
         _check(lib().mfgpu_operator_set_host_chunks(self.h, int(n_chunks)))
@@ -363,7 +384,7 @@ def prolongate_noalloc(mesh, coarse_level, nc, coarse, fine, precision=64,
 def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
                   cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
                   coarse_accurate=True, mg_precision=32, coarse_fp64=False,
-                  max_it_mult=1, fp64_emulation=False, cuda_graphs=True):
+                  max_it_mult=1, fp64_emulation=False, cuda_graphs=True, coarse_dense=True):
     s = SolverParams()
     s.preconditioner = {"none": 0, "jacobi": 1, "gmg": 2}[preconditioner]
     s.relaxation = relaxation
@@ -377,6 +398,7 @@ def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
     s.coarse_fp64 = int(coarse_fp64)
     s.fp64_emulation = int(fp64_emulation)
     s.cuda_graphs = int(cuda_graphs)
+    s.coarse_dense = int(coarse_dense)
     return s
 
 
@@ -413,6 +435,13 @@ class Solid:
                                               C.byref(its), C.byref(secs)))
         return its.value, secs.value
 
+    def set_timing(self, enable=True):
+        """Per-section wall times (the reference's TimerOutput); clears the table."""
+        _check(lib().mfgpu_solid_set_timing(self.h, int(enable)))
+
+    def timing_summary(self):
+        return _text(lambda buf, n: lib().mfgpu_solid_timing_summary(self.h, buf, n))
+
     def close(self):
         if self.h:
             lib().mfgpu_solid_destroy(self.h)
@@ -444,6 +473,17 @@ class Heat:
         p = C.c_void_p()
         _check(lib().mfgpu_heat_solution(self.h, C.byref(p)))
         return p.value
+
+    def step(self):
+        its = C.c_int()
+        _check(lib().mfgpu_heat_step(self.h, C.byref(its)))
+        return its.value
+
+    def set_timing(self, enable=True):
+        _check(lib().mfgpu_heat_set_timing(self.h, int(enable)))
+
+    def timing_summary(self):
+        return _text(lambda buf, n: lib().mfgpu_heat_timing_summary(self.h, buf, n))
 
     def close(self):
         if self.h:

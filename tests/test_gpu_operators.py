@@ -491,3 +491,76 @@ def test_fp64_emulation_rejects_unsupported(ctx):
                                  delta_t=0.1)
     with pytest.raises(mfgpu.MfgpuError):
         op32.set_fp64_emulation(True)
+
+
+DENSE_CASES = [("heat", 64, False, None), ("heat", 32, False, None), ("heat", 64, True, None),
+               ("nh", 64, False, "scalar_referential"), ("nh", 64, False, "tensor4"),
+               ("nh", 64, False, "tensor4_ns"), ("nh", 32, False, "tensor2"),
+               ("nh", 64, True, "referential_qp"), ("nh0", 64, False, "tensor2")]
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 6])
+@pytest.mark.parametrize("kind,precision,df64,caching", DENSE_CASES)
+def test_dense_copy_matches_matrix_free(ctx, degree, kind, precision, df64, caching):
+    """The dense copy of a coarse-level operator (element columns from unit
+    vectors, constrained rows and columns as the identity) multiplies like
+    the matrix-free operator, is symmetric, and is not used once the
+    operator's state has changed."""
+    import torch
+    dt = np.float64 if precision == 64 else np.float32
+    tol = 1e-13 if precision == 64 else 2e-6
+    if kind == "heat":
+        spec = W.unit_cube_heat(degree, 0, rep=(2, 1, 1))
+        n = W.n_dofs(spec, 1)
+        op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, precision, True, delta_t=0.1)
+    else:
+        spec = W.cantilever(degree, 0, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+        n = W.n_dofs(spec, 3)
+        u1 = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=2)
+        op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, precision, caching)
+        op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01, 0 if kind == "nh0" else 1))
+        d_u = dev(u1.astype(dt))
+        op.initialize(d_u)
+    if df64:
+        op.set_fp64_emulation(True)
+    if kind != "heat":
+        op.cache()
+    x = dev(W.uniform_vector(n, 5, dt))
+    y = dev(W.uniform_vector(n, 6, dt))
+    mf_x, dn_x, dn_y = (torch.zeros_like(x) for _ in range(3))
+    op.vmult(mf_x, x)
+    op.set_dense(True)
+    op.vmult(dn_x, x)
+    op.vmult(dn_y, y)
+    ref = host(mf_x).astype(np.float64)
+    assert rel(host(dn_x).astype(np.float64), ref) < tol
+    # symmetric: y . A x == x . A y
+    xa, ya = host(x).astype(np.float64), host(y).astype(np.float64)
+    assert abs(ya @ host(dn_x) - xa @ host(dn_y)) <= tol * np.linalg.norm(ya) * np.linalg.norm(ref)
+    # vmult_add on the dense copy
+    op.vmult_add(dn_x, x)
+    assert rel(host(dn_x).astype(np.float64), 2 * ref) < tol
+    if kind != "heat":
+        # a new linearisation: the stale dense copy is bypassed
+        u2 = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=7)
+        d_u.copy_(dev(u2.astype(dt)))
+        op.cache()
+        op.vmult(dn_x, x)
+        op.set_dense(False)
+        op.vmult(mf_x, x)
+        assert rel(host(dn_x), host(mf_x)) == 0.0
+    else:
+        op.set_delta_t(0.05)
+        op.vmult(dn_x, x)
+        op.set_dense(False)
+        op.vmult(mf_x, x)
+        assert rel(host(dn_x), host(mf_x)) == 0.0
+    op.close()
+
+
+def test_dense_copy_rejects_large_operators(ctx):
+    spec = W.unit_cube_heat(4, 2)
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    with pytest.raises(mfgpu.MfgpuError, match="dense copy"):
+        op.set_dense(True)
+    op.close()

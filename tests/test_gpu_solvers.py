@@ -171,3 +171,36 @@ def test_heat_graph_replay_matches_eager(ctx):
         pl.solver.cuda_graphs = int(graphs)
         its[graphs] = list(mfgpu.Heat(ctx, pl).run().cg_its[:2])
     assert its[False] == its[True]
+
+
+def test_driver_timing_sections(ctx):
+    """The drivers' wall-clock sections (the reference's TimerOutput): every
+    section of a Newton-Newmark run and of a heat step is reported with its
+    call count, the results do not change with timing on, and the sections
+    add up to no more than the elapsed time."""
+    spec = W.cantilever(2, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    _, pl = solid_pair(spec, "referential_qp")
+    plain = mfgpu.Solid(ctx, pl).run()
+    s = mfgpu.Solid(ctx, pl)
+    s.set_timing(True)
+    r = s.run()
+    text = s.timing_summary()
+    tab = mfgpu.timing_table(text)
+    newton = sum(r.newton_its[:2])
+    assert tab["Linear solver"][0] == r.n_solves == newton
+    assert tab["Assemble residual"][0] == newton + 2  # one more residual per step: the converged one
+    for name in ("Setup MF: cache()", "Setup MF: diagonal()", "Setup MF: interpolate_to_mg",
+                 "Setup MF: GMG setup"):
+        assert tab[name][0] >= r.n_solves and tab[name][1] > 0, (name, text)
+    assert sum(v[1] for v in tab.values()) <= r.seconds * 1.05 + 1e-3, text
+    assert list(r.newton_its[:2]) == list(plain.newton_its[:2]) and r.total_cg == plain.total_cg
+    s.set_timing(False)
+    assert mfgpu.timing_table(s.timing_summary()) == {}
+    s.close()
+    _, ph = heat_pair(W.unit_cube_heat(2, 2), n_steps=3, tol=1e-10)
+    h = mfgpu.Heat(ctx, ph)
+    h.set_timing(True)
+    h.run()
+    th = mfgpu.timing_table(h.timing_summary())
+    assert th["assemble rhs"][0] == 3 and th["GMG setup"][0] == 3 and th["solve system"][0] == 3
+    h.close()
