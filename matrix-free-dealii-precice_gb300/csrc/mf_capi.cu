@@ -387,6 +387,17 @@ extern "C"
   }
 
   int
+  mfgpu_operator_set_cell_kernel(mfgpu_operator *op, int mode)
+  {
+    return guarded([&] {
+      need(op, "op");
+      if (mode < 0 || mode > 2)
+        throw Error(ERR_ARG, "cell kernel must be 0 (by grid size), 1 (line) or 2 (point)");
+      op->op->cell_kernel = mode;
+    });
+  }
+
+  int
   mfgpu_operator_set_dense(mfgpu_operator *op, int enable)
   {
     return guarded([&] {

@@ -1111,6 +1111,195 @@ namespace mfgpu
   }
 
   // ---------------------------------------------------------------------
+  // Point-parallel application for launches with few cells (coarse
+  // levels): one block per cell, one thread per point (N^3 threads).  In a
+  // 1D sweep every thread computes one output, an N-term dot product along
+  // the sweep direction; the three derivative contractions of evaluate
+  // (and of integrate) are one pass.  The dependency chains are N times
+  // shorter than cell_apply_kernel's (one line of N outputs per thread),
+  // which is what a grid of a few hundred blocks is bound by.
+  // ---------------------------------------------------------------------
+  // out(t) = sum_i M[q][i] in(t with its DIR coordinate q replaced by i)
+  // (TR: sum_i M[i][q] in(...)); M in shared memory
+  template <int N, int DIR, bool TR, typename T>
+  __device__ __forceinline__ T
+  point_sweep(const T *M, const T *in, int t, int q)
+  {
+    constexpr int st   = DIR == 0 ? 1 : (DIR == 1 ? N : N * N);
+    const int     base = t - q * st;
+    Acc<T>        s;
+    s.init(TR ? M[q] : M[q * N], in[base]);
+#pragma unroll
+    for (int i = 1; i < N; ++i)
+      s.add(TR ? M[i * N + q] : M[q * N + i], in[base + i * st]);
+    return s.result();
+  }
+
+  template <int N, int NC, bool EVAL_U>
+  __host__ __device__ constexpr int
+  point_smem_elems()
+  {
+    return 4 * N * N + (2 + 4 * NC + (EVAL_U ? 3 * NC + 1 : 0)) * N * N * N;
+  }
+
+  template <int N, typename TS, typename T, int NC, class QOp, bool CONSTRAINED>
+  __global__ void __launch_bounds__(N *N *N)
+  cell_apply_point_kernel(const __grid_constant__ ShapeA<N, T> sh, const __grid_constant__ CellGeom<T> g,
+                          const QOp op, const TS *__restrict__ src, TS *__restrict__ dst)
+  {
+    constexpr int N2 = N * N, N3 = N * N * N;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Sm = reinterpret_cast<T *>(smem_raw); // S, then the derivative matrix of x, y, z
+    T *Dm = Sm + N2;
+    T *U0 = Sm + 4 * N2, *U1 = U0 + N3;
+    T *VG = U1 + N3; // [c][value, grad x, grad y, grad z][N3]
+    T *GU = VG + 4 * NC * N3; // [c][3][N3] gradients of the linearisation (EVAL_U)
+    T *XU = GU + 3 * NC * N3; // scratch values of the linearisation (EVAL_U)
+
+    const int      t    = threadIdx.x;
+    const int      a    = t % N, b = (t / N) % N, k = t / N2;
+    const unsigned cell = g.cell_begin + blockIdx.x;
+    const int      cx   = int(cell % unsigned(g.C[0]));
+    const int      cyz  = int(cell / unsigned(g.C[0]));
+    const int      cy = cyz % g.C[1], cz = cyz / g.C[1];
+    const int      ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
+    const size_t   node = size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+    const unsigned mask = CONSTRAINED ? node_mask_g(g, ix, iy, iz) : 0u;
+    for (int i = t; i < N2; i += N3)
+      {
+        Sm[i] = sh.S[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          Dm[d * N2 + i] = QOp::ref_grad ? sh.Du[i] : sh.D[d][i];
+      }
+
+    // values (V) and gradients (G + d N3) at the Gauss points of the nodal
+    // field in U0; U0 is free again when it returns (its last reader, the
+    // z sweep, is behind a barrier)
+    auto evaluate = [&](T *V, T *G) {
+      __syncthreads();
+      U1[t] = point_sweep<N, 0, false>(Sm, U0, t, a);
+      __syncthreads();
+      U0[t] = point_sweep<N, 1, false>(Sm, U1, t, b);
+      __syncthreads();
+      V[t] = point_sweep<N, 2, false>(Sm, U0, t, k);
+      __syncthreads();
+      G[t]          = point_sweep<N, 0, false>(Dm, V, t, a);
+      G[N3 + t]     = point_sweep<N, 1, false>(Dm + N2, V, t, b);
+      G[2 * N3 + t] = point_sweep<N, 2, false>(Dm + 2 * N2, V, t, k);
+    };
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c)
+      {
+        TS raw = TS(0);
+        if (!((mask >> c) & 1u))
+          raw = __ldg(src + size_t(c) * g.n_nodes + node);
+        U0[t] = to_compute<T, TS>(raw);
+        evaluate(VG + c * 4 * N3, VG + c * 4 * N3 + N3);
+      }
+    if constexpr (QOp::eval_u)
+      {
+        // gradients of the cached linearisation values (cell-local layout);
+        // the values go to the scratch XU
+#pragma unroll 1
+        for (int c = 0; c < NC; ++c)
+          {
+            U0[t] = op.ucell[(size_t(cell) * NC + c) * N3 + t];
+            evaluate(XU, GU + c * 3 * N3);
+          }
+      }
+    __syncthreads();
+
+    // -------- quadrature-point operation (point t) ------------------------
+    {
+      T v[NC], H[NC][3];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        {
+          v[c] = VG[c * 4 * N3 + t];
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            H[c][d] = VG[(c * 4 + d + 1) * N3 + t];
+        }
+      const T jxw = (sh.w[a] * sh.w[b] * g.vol) * sh.w[k];
+      if constexpr (QOp::prefetch)
+        {
+          const typename QOp::Pre pre = op.load(cell, t);
+          op.apply(pre, v, H, jxw);
+        }
+      else
+        {
+          T Hu[NC][3];
+          if constexpr (QOp::eval_u)
+            {
+#pragma unroll
+              for (int c = 0; c < NC; ++c)
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                  Hu[c][d] = GU[(c * 3 + d) * N3 + t];
+            }
+          op(cell, t, v, H, Hu);
+#pragma unroll
+          for (int c = 0; c < NC; ++c)
+            {
+              v[c] = v[c] * jxw;
+#pragma unroll
+              for (int d = 0; d < 3; ++d)
+                H[c][d] = H[c][d] * jxw;
+            }
+        }
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        {
+          VG[c * 4 * N3 + t] = v[c];
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            VG[(c * 4 + d + 1) * N3 + t] = H[c][d];
+        }
+    }
+
+    // -------- integrate + scatter ------------------------------------------
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c)
+      {
+        const T *V = VG + c * 4 * N3;
+        __syncthreads();
+        // value + D^T (x, y, z gradients) in one pass
+        {
+          Acc<T> s;
+          s.init_add(V[t]);
+          const int b0 = t - a, b1 = t - b * N, b2 = t - k * N2;
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            s.add(Dm[i * N + a], V[N3 + b0 + i]);
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            s.add(Dm[N2 + i * N + b], V[2 * N3 + b1 + i * N]);
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            s.add(Dm[2 * N2 + i * N + k], V[3 * N3 + b2 + i * N2]);
+          U0[t] = s.result();
+        }
+        __syncthreads();
+        U1[t] = point_sweep<N, 0, true>(Sm, U0, t, a);
+        __syncthreads();
+        U0[t] = point_sweep<N, 1, true>(Sm, U1, t, b);
+        __syncthreads();
+        const T out = point_sweep<N, 2, true>(Sm, U0, t, k);
+        if ((mask >> c) & 1u)
+          {
+            // constrained row: dst += src by the cell that owns the node
+            const bool owner = (a < g.p || cx == g.C[0] - 1) && (b < g.p || cy == g.C[1] - 1) &&
+                               (k < g.p || cz == g.C[2] - 1);
+            if (owner)
+              dst[size_t(c) * g.n_nodes + node] += __ldg(src + size_t(c) * g.n_nodes + node);
+          }
+        else
+          atomicAdd(dst + size_t(c) * g.n_nodes + node, to_storage<TS, T>(out));
+      }
+  }
+
+  // ---------------------------------------------------------------------
   // quadrature-point operations
   // ---------------------------------------------------------------------
 

@@ -283,6 +283,7 @@ namespace mfgpu
     bool      constrained = true;
     int       arith       = 0; // 0 native, 1 double-float (FP64 operators only)
     int       scatter     = 0; // 0 atomic adds, 1 parity colours with plain adds (deterministic)
+    int       cell_kernel = 0; // 0 by grid size, 1 line-parallel, 2 point-parallel (ApplyArgs::kernel)
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;

@@ -26,7 +26,7 @@ namespace mfgpu
     template <int N, typename TS, typename T, int NC, class Op, bool CON>
     cudaError_t
     run_apply(const ShapeA<N, T> &sh, const CellGeom<T> &cg, const Op &op,
-              const TS *src, TS *dst, bool unit, cudaStream_t s)
+              const TS *src, TS *dst, bool unit, int kernel, cudaStream_t s)
     {
       constexpr int CPB  = apply_cells_per_block<N, NC, TS, Op::eval_u>();
       const size_t  smem = size_t(CPB) * apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
@@ -50,6 +50,17 @@ namespace mfgpu
               return cudaGetLastError();
             }
           return cudaErrorInvalidValue;
+        }
+      const unsigned n_cells = cg.cell_end - cg.cell_begin;
+      if (cg.color < 0 && n_cells > 0 && (kernel == 2 || (kernel == 0 && n_cells < POINT_CELLS)))
+        {
+          // few cells: one block per cell, one thread per point
+          auto         kp    = cell_apply_point_kernel<N, TS, T, NC, Op, CON>;
+          const size_t smemp = point_smem_elems<N, NC, Op::eval_u>() * sizeof(T);
+          if ((e = prepare(kp, smemp)) != cudaSuccess)
+            return e;
+          kp<<<n_cells, N * N * N, smemp, s>>>(sh, cg, op, src, dst);
+          return cudaGetLastError();
         }
       auto k = cell_apply_kernel<N, TS, T, NC, Op, CON>;
       if ((e = prepare(k, smem)) != cudaSuccess)
@@ -94,8 +105,8 @@ namespace mfgpu
     run_apply_c(const ApplyArgs &a, const ShapeA<N, T> &sh, const CellGeom<T> &cg,
                 const Op &op, const TS *src, TS *dst, cudaStream_t s)
     {
-      return a.constrained ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, a.unit, s) :
-                             run_apply<N, TS, T, NC, Op, false>(sh, cg, op, src, dst, a.unit, s);
+      return a.constrained ? run_apply<N, TS, T, NC, Op, true>(sh, cg, op, src, dst, a.unit, a.kernel, s) :
+                             run_apply<N, TS, T, NC, Op, false>(sh, cg, op, src, dst, a.unit, a.kernel, s);
     }
   } // namespace
 

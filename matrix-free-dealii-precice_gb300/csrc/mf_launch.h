@@ -47,7 +47,13 @@ namespace mfgpu
     // n_nodes, zeroed by the caller) and receives the operator's entries of
     // the unconstrained rows and columns; src is not read
     bool        unit = false;
+    // cell kernel: 0 by grid size (point-parallel below POINT_CELLS cells),
+    // 1 line-parallel (cell_apply_kernel), 2 point-parallel
+    int         kernel = 0;
   };
+
+  // launches of fewer cells than this take the point-parallel kernel
+  constexpr unsigned POINT_CELLS = 1024;
 
   template <int N, typename T>
   cudaError_t launch_apply(const HostBasis &b, const LevelGeom &g,

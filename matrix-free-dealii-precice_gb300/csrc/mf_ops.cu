@@ -734,6 +734,7 @@ namespace mfgpu
     a.cell_begin = c0;
     a.cell_end   = c1;
     a.colored    = scatter == 1;
+    a.kernel     = cell_kernel;
     if (geom.dim == 2)
       {
         check_2d();
@@ -878,7 +879,7 @@ namespace mfgpu
   Operator::vmult_state() const
   {
     size_t h = hmix(size_t(precision), size_t(arith) + 2 * size_t(scatter));
-    h        = hmix(h, size_t(constrained));
+    h        = hmix(h, size_t(constrained) + 2 * size_t(cell_kernel));
     return hmix(h, size_t(nc));
   }
 

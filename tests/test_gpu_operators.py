@@ -366,6 +366,9 @@ def test_colored_scatter(ctx, kind, degree, n_ref, rep):
         tol = TOL64 if precision == 64 else TOL32
     d_src = dev(src)
     d_at = dev(np.zeros(n, dt))
+    # the coloured scatter is a mode of the line-parallel kernel: compare
+    # with the atomic scatter of the same kernel
+    op.set_cell_kernel("line")
     op.vmult(d_at, d_src)
     op.set_scatter("colored")
     outs = []
@@ -563,4 +566,45 @@ def test_dense_copy_rejects_large_operators(ctx):
     op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
     with pytest.raises(mfgpu.MfgpuError, match="dense copy"):
         op.set_dense(True)
+    op.close()
+
+
+KERNEL_CASES = [("heat", 64, False, None), ("heat", 32, False, None), ("heat", 64, True, None),
+                ("nh", 64, False, "scalar_referential"), ("nh", 32, False, "scalar_referential"),
+                ("nh", 64, False, "tensor2"), ("nh", 64, False, "tensor4"), ("nh", 32, False, "tensor4_ns"),
+                ("nh", 64, False, "referential_qp"), ("nh", 32, False, "referential_qp"),
+                ("nh", 64, True, "referential_qp"), ("nh0", 64, False, "tensor2")]
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("kind,precision,df64,caching", KERNEL_CASES)
+def test_line_and_point_kernels_agree(ctx, degree, kind, precision, df64, caching):
+    """The line-parallel and the point-parallel cell kernels apply the same
+    operator (constrained rows included) to round-off."""
+    import torch
+    dt = np.float64 if precision == 64 else np.float32
+    tol = 1e-13 if precision == 64 else 3e-6
+    if kind == "heat":
+        spec = small_heat(degree)
+        n = W.n_dofs(spec, 1)
+        op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, precision, True, delta_t=0.1)
+    else:
+        spec, u = nh_setup(degree)
+        n = W.n_dofs(spec, 3)
+        op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, precision, caching)
+        op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01, 0 if kind == "nh0" else 1))
+        d_u = dev(u.astype(dt))
+        op.initialize(d_u)
+    if df64:
+        op.set_fp64_emulation(True)
+    if kind != "heat":
+        op.cache()
+    x = dev(W.uniform_vector(n, 9, dt))
+    out = {}
+    for mode in ("line", "point"):
+        op.set_cell_kernel(mode)
+        y = torch.zeros_like(x)
+        op.vmult(y, x)
+        out[mode] = host(y).astype(np.float64)
+    assert rel(out["point"], out["line"]) < tol
     op.close()
