@@ -318,9 +318,18 @@ def test_vmult_host_overlapped(ctx, kind, chunks):
         assert rel(dst_p.astype(np.float64), np.asarray(ref, np.float64)) < tol
     d_dst = dev(np.zeros(n, dt))
     op.vmult(d_dst, dev(src))
-    assert rel(dst_p, host(d_dst)) < (1e-14 if precision == 64 else 1e-6)
+    # (the whole-grid and the per-slab launches may take different cell
+    # kernels on this small mesh: summation orders differ)
+    assert rel(dst_p, host(d_dst)) < (1e-13 if precision == 64 else 1e-6)
     # a new source in the same pinned buffer is picked up by the replay
     src_p[:] = -2.0 * src
+    op.vmult_host(dst_p, src_p)
+    assert rel(dst_p.astype(np.float64), -2.0 * np.asarray(ref, np.float64)) < tol
+    # pageable buffers in between (another path through the same staging
+    # buffers), then pinned again
+    out_pg = np.zeros(n, dt)
+    op.vmult_host(out_pg, src)
+    assert rel(out_pg.astype(np.float64), np.asarray(ref, np.float64)) < tol
     op.vmult_host(dst_p, src_p)
     assert rel(dst_p.astype(np.float64), -2.0 * np.asarray(ref, np.float64)) < tol
     if nc == 1:
