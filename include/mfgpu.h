@@ -290,6 +290,12 @@ typedef struct mfgpu_solid_result
 int mfgpu_solid_create(mfgpu_context *ctx, const mfgpu_solid_params *p,
                        mfgpu_solid **s);
 int mfgpu_solid_run(mfgpu_solid *s, mfgpu_solid_result *r);
+/* one time step of Solid::run from the current state (solve_nonlinear_
+ * timestep, update_velocity and the watchpoint, mf_elasticity.h:576-613):
+ * its Newton iterations, CG iterations and linear solves, and the
+ * watchpoint displacement (any output pointer may be null) */
+int mfgpu_solid_step(mfgpu_solid *s, int *newton_iterations, long *cg_iterations,
+                     int *linear_solves, double *watch_displacement);
 /* Newton residual (Solid::assemble_residual, mf_elasticity.h:1649-1908):
  * rhs = -int tau F^{-T} : Grad v + int rho (b - a) . v + traction term,
  * constrained rows zero; u, acceleration, rhs are device vectors */

@@ -12,6 +12,7 @@
 
 #include "cases.h"
 #include "prm.h"
+#include "vtu.h"
 
 using namespace mfapp;
 
@@ -20,34 +21,6 @@ check(int rc)
 {
   if (rc != MFGPU_OK)
     throw std::runtime_error(mfgpu_last_error());
-}
-
-// Gauss-Lobatto support points of FE_Q(p) on [0,1]
-static std::vector<double>
-lobatto(int p)
-{
-  std::vector<double> x(p + 1);
-  x[0] = 0;
-  x[p] = 1;
-  for (int i = 1; i < p; ++i)
-    {
-      long double z = -std::cos(3.14159265358979323846L * i / p);
-      for (int it = 0; it < 100; ++it)
-        {
-          long double p0 = 1, p1 = z;
-          for (int k = 2; k <= p; ++k)
-            {
-              long double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
-              p0             = p1;
-              p1             = p2;
-            }
-          const long double dp = p * (z * p1 - p0) / (z * z - 1);
-          const long double d2 = (2 * z * dp - p * (p + 1) * p1) / (1 - z * z);
-          z -= dp / d2;
-        }
-      x[i] = double((1 + z) / 2);
-    }
-  return x;
 }
 
 // L2 error of the nodal field u against 1 + x^2 + alpha y^2 + beta t with
@@ -172,11 +145,20 @@ main(int argc, char *argv[])
                 << "--     . 1d_quad   = " << P.mesh.n_q_1d << "\n"
                 << "--     . Number of active cells: " << cells << "\n"
                 << "--     . Number of degrees of freedom: " << nn << "\n\n";
-      const bool report = P.analytic && cells <= 32768;
-      if (report)
+      const bool report    = P.analytic && cells <= 32768;
+      const bool write_sol = prm.get_bool("Output", "Output solution");
+      std::string folder   = prm.get("Output", "Output folder");
+      if (!folder.empty() && folder.back() != '/')
+        folder += '/';
+      if (write_sol && !folder.empty())
+        make_dirs(folder);
+      // output_results (heat_transfer.h:854-880): the solution and the MPI
+      // owner of every cell, at t = 0, every output tick and the end
+      const std::vector<std::pair<std::string, double>> cell_data = {{"owner", 0.0}};
+      std::vector<double> u0(nn, 0.0);
+      if (report || (write_sol && P.analytic))
         {
-          // initial condition: error at t = 0
-          std::vector<double> u0(nn);
+          // initial condition
           const std::vector<double> gl = lobatto(P.mesh.degree);
           int Nn[3], C[3];
           for (int d = 0; d < 3; ++d)
@@ -195,8 +177,11 @@ main(int argc, char *argv[])
               const double x = coord(ix, 0), y = coord(iy, 1);
               u0[g]          = 1 + x * x + P.alpha * y * y;
             }
-          std::cout << "Error: " << l2_error(P.mesh, u0, P.alpha, P.beta, 0.0) << "\n\n";
         }
+      if (report)
+        std::cout << "Error: " << l2_error(P.mesh, u0, P.alpha, P.beta, 0.0) << "\n\n";
+      if (write_sol)
+        write_vtu(vtu_name(folder, 0), P.mesh, dim, 1, u0, "solution", false, cell_data);
       long total_its = 0;
       double t = 0;
       for (int s = 0; s < n_steps; ++s)
@@ -208,12 +193,16 @@ main(int argc, char *argv[])
           const bool tick_crossed = int(std::round(t / tick * 1e12) / 1e12) !=
                                       int(std::round((t - P.dt) / tick * 1e12) / 1e12) ||
                                     s == n_steps - 1;
-          if (report && tick_crossed)
+          if ((report || write_sol) && tick_crossed)
             {
               const double *dptr = nullptr;
               check(mfgpu_heat_solution(heat, &dptr));
               check(mfgpu_copy(ctx, u.data(), dptr, nn * sizeof(double)));
-              std::cout << "Error: " << l2_error(P.mesh, u, P.alpha, P.beta, t) << "\n\n";
+              if (report)
+                std::cout << "Error: " << l2_error(P.mesh, u, P.alpha, P.beta, t) << "\n\n";
+              if (write_sol)
+                write_vtu(vtu_name(folder, int(std::lround(t / tick))), P.mesh, dim, 1, u, "solution", false,
+                          cell_data);
             }
         }
       std::cout << "\nAverage CG iter = " << (n_steps ? total_its / n_steps : 0) << "\n"

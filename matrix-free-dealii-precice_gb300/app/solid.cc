@@ -11,12 +11,14 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <iostream>
 #include <sstream>
 #include <vector>
 
 #include "cases.h"
 #include "prm.h"
+#include "vtu.h"
 
 using namespace mfapp;
 
@@ -25,20 +27,6 @@ check(int rc)
 {
   if (rc != MFGPU_OK)
     throw std::runtime_error(mfgpu_last_error());
-}
-
-static void
-make_dirs(const std::string &path)
-{
-  std::string acc;
-  for (size_t i = 0; i < path.size(); ++i)
-    {
-      acc += path[i];
-      if (path[i] == '/' && acc.size() > 1)
-        mkdir(acc.c_str(), 0755);
-    }
-  if (!acc.empty())
-    mkdir(acc.c_str(), 0755);
 }
 
 int
@@ -120,11 +108,49 @@ main(int argc, char *argv[])
       // wall-clock sections, printed at the end as the reference's
       // TimerOutput summary
       check(mfgpu_solid_set_timing(solid, 1));
-      mfgpu_solid_result R;
-      check(mfgpu_solid_run(solid, &R));
 
+      // time loop of Solid::run (mf_elasticity.h:555-613): the solution is
+      // written at t = 0, at every output tick and at the end
+      const bool   write_sol = prm.get_bool("Output", "Output solution");
+      const double tick      = prm.get_double("Output", "Output tick");
+      std::string  folder    = prm.get("Output", "Output folder");
+      if (!folder.empty() && folder.back() != '/')
+        folder += '/';
+      if (!folder.empty())
+        make_dirs(folder);
       size_t nn = 0;
       check(mfgpu_mesh_n_nodes(&P.mesh, -1, &nn));
+      std::vector<double> uh(size_t(dim) * nn, 0.0);
+      // cell data of the reference's output: MPI subdomain, material id and
+      // manifold id (flat_manifold_id of the box cells)
+      const std::vector<std::pair<std::string, double>> cell_data = {
+        {"subdomain", 0.0}, {"material_id", 0.0}, {"manifold_id", 4294967295.0}};
+      auto write_solution = [&](int number) {
+        const double *ud = nullptr;
+        check(mfgpu_solid_displacement(solid, &ud));
+        check(mfgpu_copy(ctx, uh.data(), ud, uh.size() * sizeof(double)));
+        write_vtu(vtu_name(folder, number), P.mesh, dim, dim, uh, "displacement", true, cell_data);
+      };
+      mfgpu_solid_result R;
+      std::memset(&R, 0, sizeof(R));
+      R.n_steps = P.n_steps;
+      if (write_sol)
+        write_solution(0);
+      double tt = 0;
+      for (int s = 0; s < P.n_steps; ++s)
+        {
+          long cg     = 0;
+          int  solves = 0;
+          check(mfgpu_solid_step(solid, &R.newton_its[s], &cg, &solves, R.watch_disp[s]));
+          R.total_cg += cg;
+          R.n_solves += solves;
+          tt += P.dt;
+          const bool crossed = int(std::round(tt / tick * 1e12) / 1e12) !=
+                                 int(std::round((tt - P.dt) / tick * 1e12) / 1e12) ||
+                               s == P.n_steps - 1;
+          if (write_sol && crossed)
+            write_solution(int(std::lround(tt / tick)));
+        }
       long cells = 1;
       double vol = 1;
       for (int d = 0; d < dim; ++d)
@@ -156,13 +182,8 @@ main(int argc, char *argv[])
         }
       out << "\nAverage CG iter = " << (R.n_solves ? R.total_cg / R.n_solves : 0) << "\n";
       std::cout << out.str();
-      if (prm.get_bool("Output", "Output solution"))
+      if (write_sol)
         {
-          std::string folder = prm.get("Output", "Output folder");
-          if (!folder.empty() && folder.back() != '/')
-            folder += '/';
-          if (!folder.empty())
-            make_dirs(folder);
           std::FILE *f = std::fopen((folder + "output").c_str(), "w");
           if (!f)
             throw std::runtime_error("can't create: " + folder + "output");

@@ -609,6 +609,28 @@ extern "C"
   }
 
   int
+  mfgpu_solid_step(mfgpu_solid *s, int *newton_iterations, long *cg_iterations, int *linear_solves,
+                   double *watch_displacement)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      int    nits = 0, solves = 0;
+      long   cg   = 0;
+      double w[3] = {0, 0, 0};
+      s->d->step(nits, cg, solves, w);
+      if (newton_iterations)
+        *newton_iterations = nits;
+      if (cg_iterations)
+        *cg_iterations = cg;
+      if (linear_solves)
+        *linear_solves = solves;
+      if (watch_displacement)
+        for (int d = 0; d < 3; ++d)
+          watch_displacement[d] = w[d];
+    });
+  }
+
+  int
   mfgpu_solid_residual(mfgpu_solid *s, const double *u, const double *acceleration,
                        double *rhs, double *l2_norm)
   {

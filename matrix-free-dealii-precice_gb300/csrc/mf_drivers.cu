@@ -405,65 +405,78 @@ namespace mfgpu
   void
   SolidDriver::run(mfgpu_solid_result &res)
   {
-    auto         t0 = std::chrono::steady_clock::now();
-    const size_t n  = fine->m();
-    const double dt = P.dt, beta = 0.25, gamma = 0.5;
-    const double a1 = 1. / (beta * dt * dt), a2 = 1. / (beta * dt), a3 = (1 - 2 * beta) / (2 * beta),
-                 a4 = gamma / (beta * dt), a5 = 1 - gamma / beta, a6 = (1 - gamma / (2 * beta)) * dt;
+    auto t0 = std::chrono::steady_clock::now();
     std::memset(&res, 0, sizeof(res));
     if (P.n_steps > 64)
       throw Error(ERR_ARG, "at most 64 time steps per run");
     res.n_steps = P.n_steps;
-    double *U = u.as<double>(), *Dl = delta.as<double>(), *V = v_old.as<double>(),
-           *Ao = a_old.as<double>(), *Ac = acc.as<double>(), *R = rhs.as<double>(), *DU = du.as<double>();
-    for (int step = 0; step < P.n_steps; ++step)
+    for (int s = 0; s < P.n_steps; ++s)
       {
-        MF_CK(cudaMemsetAsync(Dl, 0, n * sizeof(double), ctx->stream));
-        double err_res0 = 0, err_upd = 0, err_upd0 = 0, err_upd_norm = 0;
-        int    it       = 0;
-        for (; it < P.max_newton; ++it)
-          {
-            // update_acceleration (mf_elasticity.h:1616-1620)
-            vec_axpbyz<double>(*ctx, n, a1, Dl, -a2, V, Ac);
-            vec_axpby<double>(*ctx, n, -a3, Ao, 1.0, Ac);
-            const double err_res = assemble_residual();
-            if (!std::isfinite(err_res))
-              throw Error(ERR_NONFINITE, "non-finite residual");
-            if (it == 0)
-              err_res0 = err_res;
-            const double err_res_norm = err_res0 != 0 ? err_res / err_res0 : err_res;
-            if (it > 2)
-              {
-                bool conv = (err_res <= P.tol_f_abs || err_upd <= P.tol_u_abs);
-                if (err_res_norm <= P.tol_f && err_upd_norm <= P.tol_u)
-                  conv = true;
-                if (conv)
-                  break;
-              }
-            update_operators(U);
-            const int its = solve_linear(R, DU, P.solver.tol * err_res);
-            res.total_cg += its;
-            res.n_solves++;
-            err_upd = std::sqrt(vec_dot<double>(*ctx, n, DU, DU));
-            if (it == 0)
-              err_upd0 = err_upd;
-            err_upd_norm = err_upd0 != 0 ? err_upd / err_upd0 : err_upd;
-            vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, Dl);
-            vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, U);
-          }
-        if (it >= P.max_newton)
-          throw Error(ERR_NOT_CONVERGED, "no convergence in nonlinear solver");
-        res.newton_its[step] = it;
-        // update_velocity (mf_elasticity.h:1602-1610): v = a4 delta + a5 v_old + a6 a_old
-        vec_axpby<double>(*ctx, n, a6, Ao, a5, V);
-        vec_axpby<double>(*ctx, n, a4, Dl, 1.0, V);
-        vec_copy<double>(*ctx, n, Ac, Ao);
-        const std::vector<double> w = point_value(P.watch);
-        for (int d = 0; d < 3; ++d)
-          res.watch_disp[step][d] = w[d];
+        long cg = 0;
+        int  solves = 0;
+        step(res.newton_its[s], cg, solves, res.watch_disp[s]);
+        res.total_cg += cg;
+        res.n_solves += solves;
       }
     ctx->sync();
     res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  void
+  SolidDriver::step(int &newton_its, long &total_cg, int &n_solves, double *watch)
+  {
+    const size_t n  = fine->m();
+    const double dt = P.dt, beta = 0.25, gamma = 0.5;
+    const double a1 = 1. / (beta * dt * dt), a2 = 1. / (beta * dt), a3 = (1 - 2 * beta) / (2 * beta),
+                 a4 = gamma / (beta * dt), a5 = 1 - gamma / beta, a6 = (1 - gamma / (2 * beta)) * dt;
+    double *U = u.as<double>(), *Dl = delta.as<double>(), *V = v_old.as<double>(),
+           *Ao = a_old.as<double>(), *Ac = acc.as<double>(), *R = rhs.as<double>(), *DU = du.as<double>();
+    total_cg = 0;
+    n_solves = 0;
+    MF_CK(cudaMemsetAsync(Dl, 0, n * sizeof(double), ctx->stream));
+    double err_res0 = 0, err_upd = 0, err_upd0 = 0, err_upd_norm = 0;
+    int    it       = 0;
+    for (; it < P.max_newton; ++it)
+      {
+        // update_acceleration (mf_elasticity.h:1616-1620)
+        vec_axpbyz<double>(*ctx, n, a1, Dl, -a2, V, Ac);
+        vec_axpby<double>(*ctx, n, -a3, Ao, 1.0, Ac);
+        const double err_res = assemble_residual();
+        if (!std::isfinite(err_res))
+          throw Error(ERR_NONFINITE, "non-finite residual");
+        if (it == 0)
+          err_res0 = err_res;
+        const double err_res_norm = err_res0 != 0 ? err_res / err_res0 : err_res;
+        if (it > 2)
+          {
+            bool conv = (err_res <= P.tol_f_abs || err_upd <= P.tol_u_abs);
+            if (err_res_norm <= P.tol_f && err_upd_norm <= P.tol_u)
+              conv = true;
+            if (conv)
+              break;
+          }
+        update_operators(U);
+        const int its = solve_linear(R, DU, P.solver.tol * err_res);
+        total_cg += its;
+        n_solves++;
+        err_upd = std::sqrt(vec_dot<double>(*ctx, n, DU, DU));
+        if (it == 0)
+          err_upd0 = err_upd;
+        err_upd_norm = err_upd0 != 0 ? err_upd / err_upd0 : err_upd;
+        vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, Dl);
+        vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, U);
+      }
+    if (it >= P.max_newton)
+      throw Error(ERR_NOT_CONVERGED, "no convergence in nonlinear solver");
+    newton_its = it;
+    // update_velocity (mf_elasticity.h:1602-1610): v = a4 delta + a5 v_old + a6 a_old
+    vec_axpby<double>(*ctx, n, a6, Ao, a5, V);
+    vec_axpby<double>(*ctx, n, a4, Dl, 1.0, V);
+    vec_copy<double>(*ctx, n, Ac, Ao);
+    const std::vector<double> w = point_value(P.watch);
+    for (int d = 0; d < 3; ++d)
+      watch[d] = w[d];
+    ++step_no;
   }
 
   // ---------------------------------------------------------------------

@@ -34,6 +34,9 @@ namespace mfgpu
     int                 solve_linear(const double *b, double *x, double tol);
     std::vector<double> point_value(const double *x);
     void                run(mfgpu_solid_result &res);
+    // one time step: Newton-Newmark iterations, velocity update, watchpoint
+    void step(int &newton_its, long &total_cg, int &n_solves, double *watch);
+    int  step_no = 0;
   };
 
   struct HeatDriver

@@ -427,6 +427,14 @@ class Solid:
         _check(lib().mfgpu_solid_displacement(self.h, C.byref(p)))
         return p.value
 
+    def step(self):
+        """One time step: (Newton iterations, CG iterations, linear solves,
+        watchpoint displacement)."""
+        nits, cg, solves = C.c_int(), C.c_long(), C.c_int()
+        w = (C.c_double * 3)()
+        _check(lib().mfgpu_solid_step(self.h, C.byref(nits), C.byref(cg), C.byref(solves), w))
+        return nits.value, cg.value, solves.value, list(w)
+
     def residual(self, u, acc, rhs):
         nrm = C.c_double()
         _check(lib().mfgpu_solid_residual(self.h, _ptr(u), _ptr(acc), _ptr(rhs),
