@@ -347,16 +347,16 @@ namespace mfgpu
         J.ctx   = ctx;
         J.A     = fine.get();
         J.omega = P.solver.relaxation;
-        st      = cg_solve<double>(*ctx, A, &J, x, b, tol, maxit);
+        st      = cg_solve<double>(*ctx, A, &J, x, b, tol, maxit, false, false, &cg_ws);
       }
     else if (P.solver.preconditioner == 2)
       {
         Precond<double> *M = lprec == 32 ? static_cast<Precond<double> *>(mgf.get()) :
                                            static_cast<Precond<double> *>(mgd.get());
-        st = cg_solve<double>(*ctx, A, M, x, b, tol, maxit);
+        st = cg_solve<double>(*ctx, A, M, x, b, tol, maxit, false, false, &cg_ws);
       }
     else
-      st = cg_solve<double>(*ctx, A, nullptr, x, b, tol, maxit);
+      st = cg_solve<double>(*ctx, A, nullptr, x, b, tol, maxit, false, false, &cg_ws);
     constrained_op<double>(*ctx, fine->geom, fine->nc, 2, nullptr, x);
     if (!st.converged)
       throw Error(ERR_NOT_CONVERGED, "CG did not converge");
@@ -667,9 +667,9 @@ namespace mfgpu
         }
         PhaseTimer::Scope tsol(timer, ctx, "solve system");
         if (lprec == 32)
-          st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+          st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
         else
-          st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n));
+          st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
       }
     else if (P.solver.preconditioner == 1)
       {
@@ -678,12 +678,12 @@ namespace mfgpu
         J.ctx   = ctx;
         J.A     = op.get();
         J.omega = 0.7;
-        st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n));
+        st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
       }
     else
       {
         PhaseTimer::Scope tsol(timer, ctx, "solve system");
-        st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n));
+        st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
       }
     if (!st.converged)
       throw Error(ERR_NOT_CONVERGED, "CG did not converge");

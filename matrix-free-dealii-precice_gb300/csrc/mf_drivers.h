@@ -26,6 +26,7 @@ namespace mfgpu
     std::vector<DevBuf>                       u_levels;
     DevBuf                                    u0_64;
     DevBuf                                    u, delta, v_old, a_old, acc, rhs, du;
+    DevBuf                                    cg_ws; // vectors of the outer CG, kept across solves
     PhaseTimer                                timer;
     SolidDriver(Context *c, const mfgpu_solid_params &p);
     void                update_operators(const double *ulin);
@@ -56,6 +57,7 @@ namespace mfgpu
     int                                        step_no = 0;
     double                                     t       = 0;
     SourceDesc                                 src{};
+    DevBuf                                     cg_ws; // vectors of the outer CG, kept across steps
     PhaseTimer                                 timer;
     HeatDriver(Context *c, const mfgpu_heat_params &p);
     void node_x(size_t g, double *x) const;

@@ -5,6 +5,7 @@
 // convergence test.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 
 #include "mf_solvers.h"
 
@@ -16,12 +17,18 @@ namespace mfgpu
   template <typename T>
   CGStats
   cg_solve(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol,
-           int maxit, bool record, bool fixed_iterations)
+           int maxit, bool record, bool fixed_iterations, DevBuf *ws)
   {
     CGStats      st;
-    const size_t n = A.size();
-    DevBuf       rb(n * sizeof(T)), zb(n * sizeof(T)), pb(n * sizeof(T)), qb(n * sizeof(T));
-    T *r = rb.as<T>(), *z = zb.as<T>(), *p = pb.as<T>(), *q = qb.as<T>();
+    const size_t n  = A.size();
+    const size_t vb = (n * sizeof(T) + 255) / 256 * 256;
+    DevBuf       own;
+    DevBuf      &W = ws ? *ws : own;
+    if (W.bytes < 4 * vb)
+      W.alloc(4 * vb);
+    char *base = static_cast<char *>(W.ptr);
+    T    *r = reinterpret_cast<T *>(base), *z = reinterpret_cast<T *>(base + vb);
+    T    *p = reinterpret_cast<T *>(base + 2 * vb), *q = reinterpret_cast<T *>(base + 3 * vb);
     // r = b - A x
     A.vmult(r, x);
     vec_axpby<T>(c, n, T(1), b, T(-1), r);
@@ -268,8 +275,10 @@ namespace mfgpu
     return st;
   }
 
-  template CGStats cg_solve<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int, bool, bool);
-  template CGStats cg_solve<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, bool, bool);
+  template CGStats cg_solve<double>(Context &, LinOp<double> &, Precond<double> *, double *, const double *, double, int,
+                                    bool, bool, DevBuf *);
+  template CGStats cg_solve<float>(Context &, LinOp<float> &, Precond<float> *, float *, const float *, double, int, bool,
+                                   bool, DevBuf *);
 
   // ---------------------------------------------------------------------
   // symmetric tridiagonal extreme eigenvalues (bisection, Sturm counts)
@@ -506,10 +515,31 @@ namespace mfgpu
     eager_done = false;
   }
 
+  namespace
+  {
+    size_t
+    key_mix(size_t h, size_t v)
+    {
+      return h ^ (v + size_t(0x9e3779b97f4a7c15ULL) + (h << 6) + (h >> 2));
+    }
+  } // namespace
+
   template <typename T>
   void
   Multigrid<T>::setup(double range, unsigned degree, int eig_its, int coarse_eig_its)
   {
+    // unchanged operators and parameters: the eigenvalue bounds, the
+    // Chebyshev coefficients and the captured V-cycle stay valid (they are
+    // functions of the operators; the reference rebuilds them every solve)
+    size_t key = key_mix(std::hash<double>()(range), size_t(degree));
+    key        = key_mix(key_mix(key, size_t(eig_its)), size_t(coarse_eig_its));
+    for (Operator *op : ops)
+      key = key_mix(key_mix(key, op->value_state()), reinterpret_cast<uintptr_t>(op->inv_diag.ptr));
+    if (coarse64)
+      key = key_mix(key_mix(key, coarse64->value_state()), reinterpret_cast<uintptr_t>(coarse64->inv_diag.ptr));
+    if (setup_done && key == setup_key)
+      return;
+    setup_done = false;
     drop_graph();
     const int L = int(ops.size());
     // the smoothers keep their work buffers across setups (same level sizes)
@@ -592,6 +622,8 @@ namespace mfgpu
       coarse_cheb64.estimate();
     for (int l : deferred)
       smoothers[l].estimate_end();
+    setup_key  = key;
+    setup_done = true;
   }
 
   template <typename T>

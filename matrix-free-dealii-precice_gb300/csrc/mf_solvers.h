@@ -62,10 +62,12 @@ namespace mfgpu
 
   // deal.II SolverCG semantics: stops when |r| <= tol (absolute), counts
   // iterations; x is the initial guess
+  // (ws: optional workspace kept by the caller across solves, so that the
+  // preconditioner sees the same vectors every time; grown to fit)
   template <typename T>
   CGStats cg_solve(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b,
                    double tol, int maxit, bool record = false,
-                   bool fixed_iterations = false);
+                   bool fixed_iterations = false, DevBuf *ws = nullptr);
 
   // CG as used for the Chebyshev eigenvalue estimate: the same iterates as
   // cg_solve(record = true), with the Lanczos coefficients recorded on the
@@ -129,6 +131,11 @@ namespace mfgpu
     // eigenvalue estimates, which run concurrently in setup()
     std::vector<std::unique_ptr<Context>> aux;
     cudaEvent_t                           setup_ev = nullptr;
+    // what the last setup() was made for: the level operators' value
+    // states and the smoother parameters (a setup with the same key, e.g.
+    // every heat time step, keeps the smoothers and the captured V-cycle)
+    size_t setup_key  = 0;
+    bool   setup_done = false;
     ~Multigrid();
     cudaGraphExec_t    gexec      = nullptr;
     double            *g_dst      = nullptr;
