@@ -220,7 +220,10 @@ namespace mfgpu
   // k = (*counter)++ on the device
   void lanczos_record(Context &c, int rz, int rzn, int pq, int rr, double *rec, int *counter);
   template <typename T> void cheby_start(Context &c, size_t n, T f, const T *b, const T *dinv, T *x, T *xold);
-  template <typename T> void cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b, const T *Ax, const T *dinv, T *x, T *xold);
+  // (zero_ax: Ax is left zero)
+  template <typename T>
+  void cheby_update(Context &c, size_t n, T f1, T f2, bool first, bool zero_ax, const T *b, T *Ax, const T *dinv,
+                    T *x, T *xold);
   // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1, 4 (dst a
   // dense nc n_nodes square matrix) unit diagonal entry
   template <typename T> void constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst);

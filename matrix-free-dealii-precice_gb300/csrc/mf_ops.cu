@@ -516,10 +516,10 @@ namespace mfgpu
   }
   template <typename T>
   void
-  cheby_update(Context &c, size_t n, T f1, T f2, bool first, const T *b,
-               const T *Ax, const T *dinv, T *x, T *xold)
+  cheby_update(Context &c, size_t n, T f1, T f2, bool first, bool zero_ax, const T *b,
+               T *Ax, const T *dinv, T *x, T *xold)
   {
-    k_cheby_update<<<grid_for(n), 256, 0, c.stream>>>(n, f1, f2, int(first), b, Ax, dinv, x, xold);
+    k_cheby_update<<<grid_for(n), 256, 0, c.stream>>>(n, f1, f2, int(first), int(zero_ax), b, Ax, dinv, x, xold);
     count_launch();
     MF_CK(cudaGetLastError());
   }
@@ -605,7 +605,7 @@ namespace mfgpu
   template void cg_direction_rec<T>(Context &, size_t, int, int, int, int, const T *, T *, T *, double *, int *); \
   template void cheby_start<T>(Context &, size_t, T, const T *, const T *, T *, T *);       \
   template void cheby_dense_step<T>(Context &, size_t, const T *, T, T, bool, const T *, const T *, const T *, T *); \
-  template void cheby_update<T>(Context &, size_t, T, T, bool, const T *, const T *, const T *, T *, T *); \
+  template void cheby_update<T>(Context &, size_t, T, T, bool, bool, const T *, T *, const T *, T *, T *); \
   template void constrained_op<T>(Context &, const LevelGeom &, int, int, const T *, T *);
   MF_INST_VEC(float)
   MF_INST_VEC(double)

@@ -342,6 +342,8 @@ namespace mfgpu
   {
     const size_t n = A->m();
     xold.ensure(n * sizeof(T));
+    if (t1.bytes != n * sizeof(T))
+      t1_zero = false;
     t1.ensure(n * sizeof(T));
     w0.ensure(n * sizeof(T));
     w1.ensure(n * sizeof(T));
@@ -363,6 +365,8 @@ namespace mfgpu
   {
     const size_t n = A->m();
     xold.ensure(n * sizeof(T));
+    if (t1.bytes != n * sizeof(T))
+      t1_zero = false;
     t1.ensure(n * sizeof(T));
     w0.ensure(n * sizeof(T));
     w1.ensure(n * sizeof(T));
@@ -459,14 +463,24 @@ namespace mfgpu
           vec_copy<T>(*ctx, n, cur, x);
         return;
       }
+    // small levels (launch-bound): t1 = A x accumulates into a zero t1,
+    // which every update leaves zero again, so no memset per step; large
+    // levels zero t1 before every application (measured faster there)
+    const bool keep_zero = small_level();
+    if (!t1_zero || !keep_zero)
+      MF_CK(cudaMemsetAsync(t1.ptr, 0, n * sizeof(T), ctx->stream));
+    t1_zero = false;
     for (unsigned k = 0; k + 1 < degree; ++k)
       {
-        A->vmult(t1.ptr, x);
+        if (k > 0 && !keep_zero)
+          MF_CK(cudaMemsetAsync(t1.ptr, 0, n * sizeof(T), ctx->stream));
+        A->vmult_add(t1.ptr, x);
         const double rhokp = 1. / (2. * sigma - rhok);
         const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
         rhok = rhokp;
-        cheby_update<T>(*ctx, n, T(f1), T(f2), k == 0, b, t1.as<T>(), dinv, x, xold.as<T>());
+        cheby_update<T>(*ctx, n, T(f1), T(f2), k == 0, keep_zero, b, t1.as<T>(), dinv, x, xold.as<T>());
       }
+    t1_zero = keep_zero;
   }
 
   template <typename T>
@@ -477,19 +491,28 @@ namespace mfgpu
       estimate();
     const size_t n    = A->m();
     const T     *dinv = A->inv_diag.as<T>();
-    A->vmult(t1.ptr, x);
-    cheby_update<T>(*ctx, n, T(0), T(1. / theta), true, b, t1.as<T>(), dinv, x, xold.as<T>());
-    if (degree < 2)
-      return;
-    double rhok = delta / theta, sigma = theta / delta;
-    for (unsigned k = 0; k + 1 < degree; ++k)
+    // t1 as in vmult()
+    const bool keep_zero = small_level();
+    if (!t1_zero || !keep_zero)
+      MF_CK(cudaMemsetAsync(t1.ptr, 0, n * sizeof(T), ctx->stream));
+    t1_zero = false;
+    A->vmult_add(t1.ptr, x);
+    cheby_update<T>(*ctx, n, T(0), T(1. / theta), true, keep_zero, b, t1.as<T>(), dinv, x, xold.as<T>());
+    if (degree >= 2)
       {
-        A->vmult(t1.ptr, x);
-        const double rhokp = 1. / (2. * sigma - rhok);
-        const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
-        rhok = rhokp;
-        cheby_update<T>(*ctx, n, T(f1), T(f2), false, b, t1.as<T>(), dinv, x, xold.as<T>());
+        double rhok = delta / theta, sigma = theta / delta;
+        for (unsigned k = 0; k + 1 < degree; ++k)
+          {
+            if (!keep_zero)
+              MF_CK(cudaMemsetAsync(t1.ptr, 0, n * sizeof(T), ctx->stream));
+            A->vmult_add(t1.ptr, x);
+            const double rhokp = 1. / (2. * sigma - rhok);
+            const double f1 = rhokp * rhok, f2 = 2. * rhokp / delta;
+            rhok = rhokp;
+            cheby_update<T>(*ctx, n, T(f1), T(f2), false, keep_zero, b, t1.as<T>(), dinv, x, xold.as<T>());
+          }
       }
+    t1_zero = keep_zero;
   }
 
   template struct Chebyshev<float>;

@@ -96,6 +96,10 @@ namespace mfgpu
     bool      initialized       = false;
     double    theta = 0, delta = 0, lambda_max = 0, lambda_min = 0;
     DevBuf     xold, t1, w0, w1;
+    bool       t1_zero = false; // t1 is all zero between applications
+    // levels of at most 8 MB per vector skip the memset before each
+    // application (launch-bound there)
+    bool small_level() const { return A->m() * sizeof(T) <= (size_t(8) << 20); }
     DevBuf     cg_ws;    // work vectors of the eigenvalue-estimate CG, kept across setups
     HostPinned host_rec; // Lanczos records of a deferred estimate
     Context   *est_ctx = nullptr;

@@ -315,16 +315,19 @@ namespace mfgpu
   // Chebyshev step (PreconditionChebyshev vector updates):
   //   t  = Dinv (b - Ax)
   //   xn = first ? (1+f1) x + f2 t : x + f1 (x - xold) + f2 t ; xold = x ; x = xn
+  // (zero_ax: Ax is left zero, so the next application can add into it)
   template <typename T>
   __global__ void
-  k_cheby_update(size_t n, T f1, T f2, int first, const T *__restrict__ b,
-                 const T *__restrict__ Ax, const T *__restrict__ dinv,
+  k_cheby_update(size_t n, T f1, T f2, int first, int zero_ax, const T *__restrict__ b,
+                 T *__restrict__ Ax, const T *__restrict__ dinv,
                  T *__restrict__ x, T *__restrict__ xold)
   {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       {
         const T t  = dinv[i] * (b[i] - Ax[i]);
+        if (zero_ax)
+          Ax[i] = T(0);
         const T xi = x[i];
         const T xn = first ? (T(1) + f1) * xi + f2 * t : xi + f1 * (xi - xold[i]) + f2 * t;
         xold[i]    = xi;
