@@ -204,3 +204,43 @@ def test_driver_timing_sections(ctx):
     th = mfgpu.timing_table(h.timing_summary())
     assert th["assemble rhs"][0] == 3 and th["GMG setup"][0] == 3 and th["solve system"][0] == 3
     h.close()
+
+
+@pytest.mark.parametrize("mg_precision", [32, 64])
+def test_dense_coarse_operator_solver_equivalence(ctx, mg_precision):
+    """The level-0 operator as a dense matrix (default) and matrix-free give
+    the same Newton and CG counts and the same displacement to round-off
+    (the dense copy changes only the summation order of the coarse
+    Chebyshev steps)."""
+    spec = W.cantilever(2, 2, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    res = {}
+    for dense in (False, True):
+        _, pl = solid_pair(spec, "referential_qp", mg_precision=mg_precision)
+        pl.solver.coarse_dense = int(dense)
+        res[dense] = mfgpu.Solid(ctx, pl).run()
+    a, b = res[False], res[True]
+    assert list(a.newton_its[:2]) == list(b.newton_its[:2])
+    assert abs(a.total_cg - b.total_cg) <= 1
+    for st in range(2):
+        wa, wb = np.array(a.watch_disp[st][:3]), np.array(b.watch_disp[st][:3])
+        assert np.linalg.norm(wb - wa) <= 1e-9 * np.linalg.norm(wa)
+
+
+def test_heat_steps_reuse_the_multigrid_setup(ctx):
+    """Heat time steps after the first keep the multigrid setup (unchanged
+    level operators): the "GMG setup" section of the later steps costs a
+    small fraction of the first, and the CG counts equal the oracle's."""
+    spec = W.unit_cube_heat(2, 3)
+    po, pl = heat_pair(spec, n_steps=4, tol=1e-10)
+    ro = O.heat_run(po)
+    h = mfgpu.Heat(ctx, pl)
+    h.set_timing(True)
+    its = [h.step() for _ in range(4)]
+    first = mfgpu.timing_table(h.timing_summary())["GMG setup"][1]
+    h.set_timing(True)  # clears the table
+    for _ in range(3):
+        its.append(h.step())
+    later = mfgpu.timing_table(h.timing_summary())["GMG setup"][1] / 3
+    assert later < 0.2 * first, (first, later)
+    assert all(abs(a - b) <= 1 for a, b in zip(its[:4], ro.cg_its[:4]))
+    h.close()
