@@ -305,7 +305,8 @@ namespace mfgpu
     void apply_cells(void *dst, const void *src) { apply_cells_range(dst, src, 0, 0, ctx->stream); }
     // the same for the cells [c0, c1) (all cells if c1 <= c0) on stream s;
     // a constrained row is added by the launch that contains its owner cell
-    void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s);
+    // (kernel >= 0: this launch's cell kernel instead of cell_kernel)
+    void apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s, int kernel = -1);
     // the kernel arguments of the operator (no vectors, all cells); checks
     // that the operator is ready to apply
     virtual ApplyArgs cell_args() const = 0;

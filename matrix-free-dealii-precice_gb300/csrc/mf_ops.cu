@@ -726,7 +726,7 @@ namespace mfgpu
   }
 
   void
-  Operator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s)
+  Operator::apply_cells_range(void *dst, const void *src, size_t c0, size_t c1, cudaStream_t s, int kernel)
   {
     ApplyArgs a  = cell_args();
     a.src        = src;
@@ -734,7 +734,7 @@ namespace mfgpu
     a.cell_begin = c0;
     a.cell_end   = c1;
     a.colored    = scatter == 1;
-    a.kernel     = cell_kernel;
+    a.kernel     = kernel >= 0 ? kernel : cell_kernel;
     if (geom.dim == 2)
       {
         check_2d();
@@ -966,7 +966,12 @@ namespace mfgpu
         // every slab has its own stream, so slabs run concurrently as their nodes arrive
         cudaStream_t s = p.s_comp[k];
         MF_CK(cudaStreamWaitEvent(s, p.e_in[k], 0));
-        apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s);
+        // slabs of up to 2048 cells take the point-parallel kernel: one
+        // block per cell fills the SMs that the other slabs and the copies
+        // leave (Q4 cantilever, 4 slabs of 1024 cells: 136 -> 126 us)
+        const size_t sc   = size_t(zc[k + 1] - zc[k]) * layer;
+        const int    kern = (cell_kernel == 0 && sc <= 2 * size_t(POINT_CELLS)) ? 2 : -1;
+        apply_cells_range(dst_d, src_d, size_t(zc[k]) * layer, size_t(zc[k + 1]) * layer, s, kern);
         MF_CK(cudaEventRecord(p.e_comp[k], s));
       }
     // (constrained rows are written by the cells that own them, in their slab)
