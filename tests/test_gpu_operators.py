@@ -1,7 +1,7 @@
 """Device operators through the C-ABI against the CPU oracle.
 
 Tolerances: FP64 operator applications agree with the oracle within 1e-12
-relative l2 (the spec bar); FP32 within 2e-5 relative l2; FP64
+relative l2 (the FP64 parity bar); FP32 within 2e-5 relative l2; FP64
 diagonals within 1e-11 (the device uses the tensor-product diagonal, the
 oracle applies the cell operator to local unit vectors).
 """
