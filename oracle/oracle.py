@@ -4,7 +4,8 @@ ctypes binding of the oracle library (the C++ CPU restatement of the
 reference's matrix-free path, built from oracle/*.cpp into
 oracle/_build/liboracle.so).  Imported only by tests/, by
 __graft_entry__.smoke() and by the CPU-baseline leg of bench.py, always as
-the checker; the product never imports it.
+the CPU computation the device results are compared with; the product never
+imports it.
 """
 import ctypes as C
 import os
