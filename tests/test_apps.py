@@ -240,3 +240,31 @@ int main()
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()
     assert out == [str(v) for p in range(1, 7) for v in (p, 1)]
+
+
+def test_gpu_entries_are_checked_before_device_work(tmp_path):
+    """The GPU section's entries (here the dense coarse operator switch)
+    are parsed with the rest of the file: a bad value stops the run before
+    any device work."""
+    txt = open(os.path.join(PRM, "turek3d_gmg_tensor4.prm")).read()
+    txt += "\nsubsection GPU\n  set Dense coarse operator = maybe\nend\n"
+    prm = tmp_path / "g.prm"
+    prm.write_text(txt)
+    r = run_app("solid", str(prm), tmp_path)
+    assert r.returncode == 1
+    assert "Dense coarse operator is not a bool: maybe" in r.stderr
+
+
+def test_timing_table_parser():
+    """mfgpu.timing_table reads the drivers' section table."""
+    import mfgpu
+    text = """+------------------------------+-----------+------------+------------+
+| Total wallclock time elapsed |           |    0.0436s |            |
++------------------------------+-----------+------------+------------+
+| Section                      | no. calls |  wall time | % of total |
++------------------------------+-----------+------------+------------+
+| Setup MF: cache()            |         2 |  0.000953s |       2.2% |
+| Linear solver                |         1 |    0.0275s |        63% |
++------------------------------+-----------+------------+------------+
+"""
+    assert mfgpu.timing_table(text) == {"Setup MF: cache()": (2, 0.000953), "Linear solver": (1, 0.0275)}
