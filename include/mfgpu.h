@@ -179,8 +179,9 @@ int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
  * coarse matrices; the solvers use it on level 0 (coarse_dense). */
 int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
 /* cell kernel of vmult: 0 by grid size (default: point-parallel, one
- * thread per quadrature point, below 1024 cells; line-parallel above),
- * 1 line-parallel, 2 point-parallel.  The results agree to round-off. */
+ * thread per quadrature point, below 1024 cells, up to 4096 in native
+ * FP64; line-parallel above), 1 line-parallel, 2 point-parallel.  The
+ * results agree to round-off. */
 int mfgpu_operator_set_cell_kernel(mfgpu_operator *op, int mode);
 /* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
 int mfgpu_operator_compute_diagonal(mfgpu_operator *op);

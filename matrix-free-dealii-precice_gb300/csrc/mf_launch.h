@@ -53,6 +53,7 @@ namespace mfgpu
   };
 
   // launches of fewer cells than this take the point-parallel kernel
+  // (native FP64: up to 4096 cells)
   constexpr unsigned POINT_CELLS = 1024;
 
   template <int N, typename T>
