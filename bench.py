@@ -180,31 +180,41 @@ def profile_traffic():
     return None
 
 
-def cpu_baseline(spec, u, src, budget_s, threads=None):
+CPU_CACHINGS = ("scalar_referential", "tensor2", "tensor4", "tensor4_ns")
+
+
+def oracle_vmult_rates(spec, u, src, budget_s, threads=None):
     """The oracle (C++ OpenMP restatement of the reference's CPU matrix-free
-    vmult) on the host cores: repeated applications of the same operator on
-    the same inputs until the time budget is used (at least one)."""
+    vmult) on the host cores: for each caching variant of the reference, the
+    operator cached once and then applied repeatedly, the applications timed
+    without the cache (as the GPU vmult is).  Returns ({caching: DoF/s},
+    threads, applications per variant)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import workloads as W
+    O.build()
     nthreads = O.set_threads(threads or (os.cpu_count() or 1))
     om = W.to_oracle_mesh(O, spec)
     mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
-    t0 = time.perf_counter()
-    O.nh_vmult(om, spec["n_ref"], mat, "scalar_referential", u, src)  # includes cache
-    t_first = time.perf_counter() - t0
-    # the oracle entry point caches and applies per call; time whole calls
-    reps, t_sum = 0, 0.0
-    while reps == 0 or (t_sum < budget_s and reps < 50):
-        t0 = time.perf_counter()
-        O.nh_vmult(om, spec["n_ref"], mat, "scalar_referential", u, src)
-        t_sum += time.perf_counter() - t0
-        reps += 1
     n = len(src)
-    return {"value": n / (t_sum / reps), "unit": UNIT, "cores": nthreads,
-            "kind": "port",
-            "sample": f"{reps} full applications (cache + vmult, scalar_referential) of "
-                      f"the {n}-DoF Q4 operator on {nthreads} threads; first call {t_first:.2f}s"}
+    # one timed application per variant sizes the rest of the budget
+    first = {c: O.nh_vmult_timed(om, spec["n_ref"], mat, c, u, src, 1)[1] for c in CPU_CACHINGS}
+    reps = max(1, min(20, int(budget_s / max(sum(first.values()), 1e-9))))
+    rates = {}
+    for c in CPU_CACHINGS:
+        _, secs = O.nh_vmult_timed(om, spec["n_ref"], mat, c, u, src, reps)
+        rates[c] = n / (secs / reps)
+    return rates, nthreads, reps
+
+
+def cpu_baseline(spec, u, src, budget_s, threads=None):
+    rates, nthreads, reps = oracle_vmult_rates(spec, u, src, budget_s, threads)
+    best = max(rates, key=rates.get)
+    return {"value": rates[best], "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{reps} applications per caching variant of the {len(src)}-DoF Q4 operator, "
+                      f"cached once, vmult timed alone, on {nthreads} threads; the fastest variant "
+                      f"({best}) is reported; all: " +
+                      ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) + " MDoF/s"}
 
 
 def _timed_vmults(torch, op, dst, src, flush, stream, reps):
@@ -499,29 +509,24 @@ def run_reference(args):
     n = W.n_dofs(spec, 3)
     u = W.smooth_displacement(spec["degree"], spec["n_ref"], spec["rep"], spec["lo"], spec["hi"], seed=2)
     src = W.uniform_vector(n, 3)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    O.build()
-    nthreads = O.set_threads(os.cpu_count() or 1)
-    om = W.to_oracle_mesh(O, spec)
-    mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
-    for _ in range(max(args.warmup, 0) and 1):
-        O.nh_vmult(om, spec["n_ref"], mat, "scalar_referential", u, src)
-    steps = max(1, min(args.steps, 10))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        O.nh_vmult(om, spec["n_ref"], mat, "scalar_referential", u, src)
-    dt = (time.perf_counter() - t0) / steps
-    value = n / dt
+    # every caching variant of the reference, cached once, vmults timed
+    # alone; the fastest one is the reference arm's number
+    budget = max(2.0, min(30.0, 3.0 * max(args.steps, 1)))
+    rates, nthreads, reps = oracle_vmult_rates(spec, u, src, budget)
+    best = max(rates, key=rates.get)
+    value = rates[best]
+    dt = n / value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-            "n_gpus": world, "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3,
+            "n_gpus": world, "steps": reps, "warmup": 1, "ms_per_step": dt * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "nh_tangent_vmult_q4_cantilever_64x8x8",
-                       "n_dofs": n, "caching": "scalar_referential"},
+                       "n_dofs": n, "caching": best},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{steps} full cache+vmult applications on {nthreads} threads "
-                                       "(the reference itself needs deal.II/p4est/MPI, absent here)"},
+                             "sample": f"{reps} applications per caching variant, cached once, vmult "
+                                       f"timed alone, on {nthreads} threads; fastest: {best}; all: " +
+                                       ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) +
+                                       " MDoF/s (the reference itself needs deal.II/p4est/MPI, absent here)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

@@ -173,6 +173,20 @@ def nh_vmult(mesh, level, mat, caching, u, src, precision=64):
     return dst
 
 
+def nh_vmult_timed(mesh, level, mat, caching, u, src, reps):
+    """(dst, seconds): the tangent cached once, then `reps` FP64 applications
+    timed without the cache."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    dst = np.zeros_like(src)
+    secs = C.c_double()
+    rc = lib().or_nh_vmult_timed(C.byref(mesh), level, C.byref(mat), CACHING.get(caching, caching),
+                                 _ptr(u), _ptr(src), _ptr(dst), int(reps), C.byref(secs))
+    if rc != 0:
+        raise RuntimeError(f"oracle nh_vmult_timed failed: {rc}")
+    return dst, secs.value
+
+
 def nh_residual(mesh, level, mat, u, acc):
     """-int P(F(u)):grad v - rho int acc.v on the unconstrained rows (FP64)."""
     u = np.ascontiguousarray(u, dtype=np.float64)

@@ -210,6 +210,39 @@ extern "C"
                       (const double *)src, (double *)dst, 0);
   }
 
+  // the CPU timing of the matrix-free tangent: cache once, then `reps`
+  // applications, *seconds = their wall time (the cache excluded)
+  int
+  or_nh_vmult_timed(const or_mesh_t *m, int level, const or_material_t *mat, int caching, const double *u,
+                    const double *src, double *dst, int reps, double *seconds)
+  {
+    MeshSpec        s = to_spec(m);
+    Basis1D         b(s.degree, s.n_q);
+    LevelOp<double> op;
+    op.box        = s.box(level);
+    op.basis      = &b;
+    op.nc         = s.dim;
+    op.kind       = op_nh;
+    op.nh.mat     = to_mat(mat);
+    op.nh.caching = Caching(caching);
+    try
+      {
+        nh_cache(op.nh, op.box, b, u);
+      }
+    catch (...)
+      {
+        return -2;
+      }
+    if (!op.nh.positive_J)
+      return -3;
+    op.vmult(dst, src); // first touch of the caches and vectors, not timed
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < reps; ++r)
+      op.vmult(dst, src);
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+  }
+
   int
   or_nh_inv_diagonal(const or_mesh_t *m, int level, const or_material_t *mat,
                      int caching, int precision, const void *u, void *out)
