@@ -319,7 +319,10 @@ extern "C"
   mfgpu_server_stats(mfgpu_server *server, int *max_running, size_t *budget_bytes)
   {
     if (!server)
-      return MFGPU_ERR_ARG;
+      {
+        set_last_error("server_stats: null argument");
+        return MFGPU_ERR_ARG;
+      }
     std::lock_guard<std::mutex> l(server->s->mu);
     if (max_running)
       *max_running = server->s->max_running;

@@ -38,3 +38,53 @@ def test_status_without_gpu_call_paths():
     assert rc == 8  # MFGPU_ERR_UNSUPPORTED
     assert b"degree" in lib.mfgpu_last_error()
     assert lib.mfgpu_operator_vmult(None, None, None) == 1
+
+
+_NULL_CHECK = r'''
+import ctypes, re, sys
+sys.path[:0] = sys.argv[2:]
+import mfgpu
+lib = mfgpu.lib()
+lib.mfgpu_last_error.restype = ctypes.c_char_p
+src = open(sys.argv[1]).read()
+src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+src = re.sub(r"//[^\n]*", "", src)
+kinds = {"int": ctypes.c_int, "double": ctypes.c_double, "size_t": ctypes.c_size_t,
+         "long long": ctypes.c_longlong}
+for m in re.finditer(r"\b(mfgpu_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+    name = m.group(1)
+    params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+    if not any("*" in p for p in params):
+        continue
+    types = [ctypes.c_void_p if "*" in p else kinds[p.rsplit(" ", 1)[0]] for p in params]
+    f = getattr(lib, name)
+    f.restype, f.argtypes = ctypes.c_int, types
+    lib.mfgpu_mesh_n_nodes(None, 0, None)  # leaves a different message behind
+    rc = f(*[None if t is ctypes.c_void_p else t(0) for t in types])
+    print(name, rc, (lib.mfgpu_last_error() or b"").decode())
+'''
+
+
+def test_every_entry_rejects_null_handles():
+    """Every entry point that takes a pointer, called with null pointers and
+    zero scalars, returns MFGPU_ERR_ARG with a message (destroy functions
+    accept null and return MFGPU_OK); none dereferences a null handle. Run in
+    a child process so that a crash fails the test instead of the session."""
+    import subprocess
+    import sys
+
+    r = subprocess.run(
+        [sys.executable, "-c", _NULL_CHECK, os.path.join(ROOT, "include", "mfgpu.h"),
+         os.path.join(ROOT, "matrix-free-dealii-precice_gb300"), ROOT],
+        capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rows = [line.split(" ", 2) for line in r.stdout.splitlines()]
+    assert len(rows) >= 50
+    for row in rows:
+        name, rc = row[0], int(row[1])
+        msg = row[2] if len(row) > 2 else ""
+        if name.endswith("_destroy"):
+            assert rc == 0, name
+        else:
+            assert rc == 1, (name, rc)
+            assert msg and (name == "mfgpu_mesh_n_nodes" or "mesh" not in msg), (name, msg)
