@@ -212,3 +212,28 @@ def test_nh_tangent_is_derivative_of_residual(degree, caching):
     fd = (rp - rm) / (2 * eps)
     Av = O.nh_vmult(om, 0, mat, caching, u, v)
     assert rel(-fd[free], Av[free]) < 1e-7, caching
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+def test_formulation0_tangent_is_derivative_of_residual(degree):
+    """Formulation 0 (isochoric/volumetric split, tensor2 caching only,
+    mf_nh_operator.h:701-840): its tangent is the derivative of its residual
+    (mf_elasticity.h:1649-1908) within 1e-7 relative."""
+    spec = W.cantilever(degree, 0, **ANISO)
+    u = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=5)
+    om = W.to_oracle_mesh(O, spec)
+    mat = O.material(0.5e6, 0.4, 1000.0, 0.01, formulation=0)
+    n = len(u)
+    v = W.uniform_vector(n, 14)
+    probe = O.nh_residual(om, 0, mat, np.zeros(n), np.ones(n))
+    free = probe != 0.0
+    v[~free] = 0.0
+    eps = 1e-6
+    rp = O.nh_residual(om, 0, mat, u + eps * v, mat.alpha_1 * (u + eps * v))
+    rm = O.nh_residual(om, 0, mat, u - eps * v, mat.alpha_1 * (u - eps * v))
+    fd = (rp - rm) / (2 * eps)
+    Av = O.nh_vmult(om, 0, mat, "tensor2", u, v)
+    assert rel(-fd[free], Av[free]) < 1e-7
+    # and it is a different operator from formulation 1 on the same state
+    Av1 = O.nh_vmult(om, 0, O.material(0.5e6, 0.4, 1000.0, 0.01), "tensor2", u, v)
+    assert rel(Av1, Av) > 1e-6
