@@ -1,6 +1,7 @@
 """Operator-level checks of the CPU oracle that need no reference golden.
 
-The reference pins no vmult vector, no 3D case and no degree above 2, so the
+The reference pins no vmult vector, no 3D case and no degree above 1 (solid)
+or 2 (heat), so the
 oracle's matrix-free operators are checked two more ways:
 
 * tangent consistency: the central finite difference of the oracle's
@@ -237,3 +238,94 @@ def test_formulation0_tangent_is_derivative_of_residual(degree):
     # and it is a different operator from formulation 1 on the same state
     Av1 = O.nh_vmult(om, 0, O.material(0.5e6, 0.4, 1000.0, 0.01), "tensor2", u, v)
     assert rel(Av1, Av) > 1e-6
+
+
+# --- two dimensions (the reference's own test cases are 2D) -----------------
+
+def element_basis_2d(p, h):
+    nodes = W.gauss_lobatto(p)
+    xg, wg = np.polynomial.legendre.leggauss(p + 1)
+    xg, wg = (xg + 1) / 2, wg / 2
+    V, dV = lagrange_1d(nodes, xg)
+    N = p + 1
+    # index order: (qy, qx) slowest to fastest, (ay, ax) likewise
+    phi = np.einsum("aq,br->rqba", V, V).reshape(N * N, N * N)
+    gx = np.einsum("aq,br->rqba", dV, V).reshape(N * N, N * N) / h[0]
+    gy = np.einsum("aq,br->rqba", V, dV).reshape(N * N, N * N) / h[1]
+    w = np.einsum("i,j->ji", wg, wg).reshape(-1) * h[0] * h[1]
+    return phi, np.stack([gx, gy], axis=2), w
+
+
+SPEC2 = dict(rep=(2, 1), lo=(0.0, 0.0), hi=(1.5, 0.6), bid=(1, 0, 0, 0))
+
+
+def mesh2d(degree, nc):
+    C = SPEC2["rep"]
+    Nn = [C[0] * degree + 1, C[1] * degree + 1]
+    h = [(SPEC2["hi"][d] - SPEC2["lo"][d]) / C[d] for d in range(2)]
+    om = O.make_mesh(2, degree, degree + 1, 0, SPEC2["rep"], SPEC2["lo"], SPEC2["hi"],
+                     boundary_id=SPEC2["bid"], dirichlet=[(1, (1 << nc) - 1)])
+    return om, C, Nn, h
+
+
+def assemble_2d(degree, nc, Ke, C, Nn):
+    n_nodes = Nn[0] * Nn[1]
+    K = np.zeros((nc * n_nodes, nc * n_nodes))
+    a = np.arange(degree + 1)
+    for cy in range(C[1]):
+        for cx in range(C[0]):
+            g = ((cx * degree + a[None, :]) + Nn[0] * (cy * degree + a[:, None])).reshape(-1)
+            dofs = np.concatenate([ci * n_nodes + g for ci in range(nc)])
+            K[np.ix_(dofs, dofs)] += Ke(g)
+    # boundary id 1 is the face x = 0, constrained in every component
+    left = np.arange(Nn[1]) * Nn[0]
+    cons = np.concatenate([ci * n_nodes + left for ci in range(nc)])
+    K[cons, :] = 0.0
+    K[:, cons] = 0.0
+    K[cons, cons] = 1.0
+    return K
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+def test_heat_oracle_matches_assembled_2d(degree):
+    om, C, Nn, h = mesh2d(degree, 1)
+    phi, grad, w = element_basis_2d(degree, h)
+    Ke = np.einsum("q,qa,qb->ab", w, phi, phi) + 0.1 * np.einsum("q,qad,qbd->ab", w, grad, grad)
+    K = assemble_2d(degree, 1, lambda g: Ke, C, Nn)
+    x = W.uniform_vector(K.shape[0], 15)
+    assert rel(O.heat_vmult(om, 0, 0.1, x), K @ x) < 1e-12
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("caching", ["scalar_referential", "tensor2", "tensor4", "tensor4_ns"])
+def test_nh_oracle_matches_assembled_tangent_2d(degree, caching):
+    """Plane (dim = 2) neo-Hookean tangent: F is 2 x 2, J = det F."""
+    om, C, Nn, h = mesh2d(degree, 2)
+    mu, nu = 0.5e6, 0.4
+    lam = 2 * mu * nu / (1 - 2 * nu)
+    mat = O.material(mu, nu, 1000.0, 0.01)
+    phi, grad, w = element_basis_2d(degree, h)
+    n_nodes = Nn[0] * Nn[1]
+    xs = W.axis_coords(C[0], SPEC2["lo"][0], SPEC2["hi"][0], degree)
+    ys = W.axis_coords(C[1], SPEC2["lo"][1], SPEC2["hi"][1], degree)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    u = np.concatenate([0.03 * np.sin(2.1 * X + 0.4) * np.cos(1.3 * Y),
+                        0.02 * np.cos(1.7 * X - 0.2 * Y + 0.9)]).reshape(-1)
+    U = u.reshape(2, n_nodes)
+    M_e = np.einsum("q,qa,qb->ab", w, phi, phi)
+    I2 = np.eye(2)
+    nb = grad.shape[1]
+
+    def Ke(g):
+        F = I2[None] + np.einsum("ia,qaJ->qiJ", U[:, g], grad)
+        FiT = np.transpose(np.linalg.inv(F), (0, 2, 1))
+        c = 2 * lam * np.log(np.linalg.det(F)) - mu
+        A = (mu * np.einsum("ik,JL->iJkL", I2, I2)[None]
+             + 2 * lam * np.einsum("qkL,qiJ->qiJkL", FiT, FiT)
+             - c[:, None, None, None, None] * np.einsum("qiL,qkJ->qiJkL", FiT, FiT))
+        k = np.einsum("q,qaJ,qiJkL,qbL->iakb", w, grad, A, grad, optimize=True).reshape(2 * nb, 2 * nb)
+        return k + 1000.0 * mat.alpha_1 * np.kron(I2, M_e)
+
+    K = assemble_2d(degree, 2, Ke, C, Nn)
+    x = W.uniform_vector(K.shape[0], 16)
+    assert rel(O.nh_vmult(om, 0, mat, caching, u, x), K @ x) < 1e-12, caching
