@@ -1,8 +1,8 @@
 """Operator-level checks of the CPU oracle that need no reference golden.
 
 The reference pins no vmult vector, no 3D case and no degree above 1 (solid)
-or 2 (heat), so the
-oracle's matrix-free operators are checked two more ways:
+or 2 (heat), so the oracle's matrix-free operators are checked two more ways,
+at every degree 1-6 (the assembled operators also in 2D):
 
 * tangent consistency: the central finite difference of the oracle's
   residual (mf_elasticity.h:1649-1908, internal force + inertia) along v
