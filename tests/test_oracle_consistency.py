@@ -329,3 +329,74 @@ def test_nh_oracle_matches_assembled_tangent_2d(degree, caching):
     K = assemble_2d(degree, 2, Ke, C, Nn)
     x = W.uniform_vector(K.shape[0], 16)
     assert rel(O.nh_vmult(om, 0, mat, caching, u, x), K @ x) < 1e-12, caching
+
+
+# --- diagonal and level transfer --------------------------------------------
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+def test_inverse_diagonals_match_assembled(degree):
+    """compute_diagonal (heat_transfer.h:205-230, mf_nh_operator.h:1025-1060):
+    the oracle's inverse diagonal is 1 / diag of the assembled operator, with
+    1 on the constrained rows."""
+    spec = W.unit_cube_heat(degree, 0, rep=(2, 1, 1))
+    spec["hi"] = (1.0, 0.6, 0.45)
+    K = assembled_heat(spec, 0.1)
+    got = O.heat_inv_diagonal(W.to_oracle_mesh(O, spec), 0, 0.1)
+    assert rel(got, 1.0 / np.diag(K)) < 1e-13
+    if degree <= 4:
+        spec = W.cantilever(degree, 0, **ANISO)
+        u = W.smooth_displacement(degree, 0, spec["rep"], spec["lo"], spec["hi"], seed=3)
+        mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+        K = assembled_nh_tangent(spec, u, 0.5e6, 0.4, 1000.0 * mat.alpha_1)
+        got = O.nh_inv_diagonal(W.to_oracle_mesh(O, spec), 0, mat, "tensor4", u)
+        assert rel(got, 1.0 / np.diag(K)) < 1e-12
+
+
+def _box(degree, dirichlet):
+    return dict(degree=degree, n_ref=1, rep=(2, 1, 1), lo=(0.0, -0.5, 0.2), hi=(1.4, 0.5, 0.9),
+                boundary_id=(1, 0, 0, 0, 0, 0), dirichlet=dirichlet)
+
+
+def _qp_poly(degree, seed):
+    """A random tensor-product polynomial of degree `degree` in each variable
+    (an element of Q_p, so FE_Q on either level represents it exactly)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cs = [rng.uniform(-1, 1, degree + 1) for _ in range(3)]
+    return lambda X, Y, Z: (np.polyval(cs[0], X) * np.polyval(cs[1], Y) * np.polyval(cs[2], Z))
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5, 6])
+def test_transfer_reproduces_qp_and_restriction_is_transpose(degree):
+    """MGTransferMatrixFree for continuous elements (used at
+    mf_elasticity.h:865-929, heat_transfer.h:515-573): prolongation and
+    interpolation to the coarse level are exact on Q_p; restriction is the
+    transpose of prolongation on the unconstrained DoFs."""
+    spec = _box(degree, [])
+    om = W.to_oracle_mesh(O, spec)
+    f = _qp_poly(degree, 21)
+    Xc = W.node_coords(degree, 0, spec["rep"], spec["lo"], spec["hi"])
+    Xf = W.node_coords(degree, 1, spec["rep"], spec["lo"], spec["hi"])
+    coarse = f(*Xc)
+    fine = np.zeros(len(Xf[0]))
+    O.transfer(om, 0, 1, "prolongate", coarse, fine)
+    assert rel(fine, f(*Xf)) < 1e-12
+    back = np.zeros_like(coarse)
+    O.transfer(om, 0, 1, "interpolate", back, f(*Xf))
+    assert rel(back, coarse) < 1e-12
+
+    # transpose, with a Dirichlet face and three components
+    spec = _box(degree, [(1, 0b101)])
+    om = W.to_oracle_mesh(O, spec)
+    nc_, nf_ = 3 * len(Xc[0]), 3 * len(Xf[0])
+    c = W.uniform_vector(nc_, 22)
+    g = W.uniform_vector(nf_, 23)
+    Pc = np.zeros(nf_)
+    O.transfer(om, 0, 3, "prolongate", c, Pc)
+    Rg = np.zeros(nc_)
+    O.transfer(om, 0, 3, "restrict", Rg, g)
+    # constrained entries: P reads them as zero and writes zero, R skips them
+    free_c = Rg != 0.0
+    lhs = float(Pc @ g)
+    rhs = float(c[free_c] @ Rg[free_c])
+    assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + np.linalg.norm(Pc) * np.linalg.norm(g))
+    assert (~free_c).sum() == 2 * (spec["rep"][1] * degree + 1) * (spec["rep"][2] * degree + 1)
