@@ -79,3 +79,20 @@ def test_heat_analytic_roundoff(dim):
     errs = np.array(r.l2_error[:10])
     gold = GOLD["heat"]["partitioned-heat"]["max_l2_error"]
     assert errs.max() < 10 * gold, errs
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("degree", [3, 4, 5, 6])
+def test_heat_analytic_roundoff_higher_degree(dim, degree):
+    """The same analytic solution lies in Q_p for every p >= 2, so the heat
+    step reproduces it to round-off at every degree the path supports (CG to
+    1e-12 relative; the errors seen are 5e-14 .. 1.6e-12)."""
+    p = O.HeatParams()
+    p.mesh = O.make_mesh(dim, degree, degree + 1, 2 if dim == 2 else 1, (1,) * dim,
+                         (0.0,) * dim, (1.0,) * dim, boundary_id=(1,) * 6,
+                         dirichlet=[(1, 1)])
+    p.dt, p.n_steps, p.tol_rel, p.precond = 0.1, 10, 1e-12, 2
+    p.analytic, p.alpha, p.beta, p.mg_float = 1, 3.0, 1.3, 1
+    r = O.heat_run(p)
+    errs = np.array(r.l2_error[:10])
+    assert errs.max() < 1e-11, errs
