@@ -13,14 +13,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "mfgpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(mfgpu_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(mfgpu_[A-Za-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_function():
     path = pkg_build.build()
     lib = ctypes.CDLL(path)
     names = declared_functions()
-    assert len(names) >= 35
+    assert len(names) >= 59
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
@@ -51,7 +51,7 @@ src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
 src = re.sub(r"//[^\n]*", "", src)
 kinds = {"int": ctypes.c_int, "double": ctypes.c_double, "size_t": ctypes.c_size_t,
          "long long": ctypes.c_longlong}
-for m in re.finditer(r"\b(mfgpu_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+for m in re.finditer(r"\b(mfgpu_[A-Za-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
     name = m.group(1)
     params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
     if not any("*" in p for p in params):
@@ -79,7 +79,7 @@ def test_every_entry_rejects_null_handles():
         capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     rows = [line.split(" ", 2) for line in r.stdout.splitlines()]
-    assert len(rows) >= 50
+    assert len(rows) >= 56
     for row in rows:
         name, rc = row[0], int(row[1])
         msg = row[2] if len(row) > 2 else ""
