@@ -181,14 +181,20 @@ def profile_traffic():
 
 
 CPU_CACHINGS = ("scalar_referential", "tensor2", "tensor4", "tensor4_ns")
+# the throughput form (oracle/oracle_fast.hpp): cell batches across SIMD
+# lanes, compile-time degree, even-odd collocation sweeps, as deal.II runs
+# the reference's vmult
+CPU_FAST = tuple((c, w) for c in ("scalar_referential", "tensor4_ns") for w in (2, 4, 8))
 
 
 def oracle_vmult_rates(spec, u, src, budget_s, threads=None):
-    """The oracle (C++ OpenMP restatement of the reference's CPU matrix-free
-    vmult) on the host cores: for each caching variant of the reference, the
-    operator cached once and then applied repeatedly, the applications timed
-    without the cache (as the GPU vmult is).  Returns ({caching: DoF/s},
-    threads, applications per variant)."""
+    """The reference's CPU matrix-free vmult restated in C++/OpenMP, on the
+    host cores: each caching variant of the reference in the oracle's plain
+    form, and the variants the throughput form covers at each lane count;
+    every one cached once and then applied repeatedly, the applications timed
+    without the cache (as the GPU vmult is).  The throughput form's result is
+    checked against the plain form's before it is timed.  Returns
+    ({variant: DoF/s}, threads, applications per variant)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import workloads as W
@@ -197,13 +203,24 @@ def oracle_vmult_rates(spec, u, src, budget_s, threads=None):
     om = W.to_oracle_mesh(O, spec)
     mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
     n = len(src)
+    level = spec["n_ref"]
+    plain = {c: (lambda reps, c=c: O.nh_vmult_timed(om, level, mat, c, u, src, reps)) for c in CPU_CACHINGS}
+    fast = {f"{c}/simd{w}": (lambda reps, c=c, w=w: O.nh_vmult_fast_timed(om, level, mat, c, u, src, reps, lanes=w))
+            for c, w in CPU_FAST}
     # one timed application per variant sizes the rest of the budget
-    first = {c: O.nh_vmult_timed(om, spec["n_ref"], mat, c, u, src, 1)[1] for c in CPU_CACHINGS}
+    first, ref = {}, {}
+    for name, fn in plain.items():
+        ref[name], first[name] = fn(1)
+    for name, fn in fast.items():
+        out, first[name] = fn(1)
+        err = np.linalg.norm(out - ref[name.split("/")[0]]) / np.linalg.norm(ref[name.split("/")[0]])
+        if not err < 1e-12:
+            raise RuntimeError(f"throughput form {name} differs from the oracle: {err:.2e}")
     reps = max(1, min(20, int(budget_s / max(sum(first.values()), 1e-9))))
     rates = {}
-    for c in CPU_CACHINGS:
-        _, secs = O.nh_vmult_timed(om, spec["n_ref"], mat, c, u, src, reps)
-        rates[c] = n / (secs / reps)
+    for name, fn in {**plain, **fast}.items():
+        _, secs = fn(reps)
+        rates[name] = n / (secs / reps)
     return rates, nthreads, reps
 
 
@@ -211,9 +228,10 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
     rates, nthreads, reps = oracle_vmult_rates(spec, u, src, budget_s, threads)
     best = max(rates, key=rates.get)
     return {"value": rates[best], "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{reps} applications per caching variant of the {len(src)}-DoF Q4 operator, "
-                      f"cached once, vmult timed alone, on {nthreads} threads; the fastest variant "
-                      f"({best}) is reported; all: " +
+            "sample": f"{reps} applications per variant of the {len(src)}-DoF Q4 operator, cached once, "
+                      f"vmult timed alone, on {nthreads} threads; variants: each caching of the reference "
+                      f"in plain loops, and the cell-batched SIMD form (/simdW: W cells per batch); the "
+                      f"fastest ({best}) is reported; all: " +
                       ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) + " MDoF/s"}
 
 
@@ -509,8 +527,9 @@ def run_reference(args):
     n = W.n_dofs(spec, 3)
     u = W.smooth_displacement(spec["degree"], spec["n_ref"], spec["rep"], spec["lo"], spec["hi"], seed=2)
     src = W.uniform_vector(n, 3)
-    # every caching variant of the reference, cached once, vmults timed
-    # alone; the fastest one is the reference arm's number
+    # every caching variant of the reference (plain loops) and the
+    # cell-batched SIMD form, cached once, vmults timed alone; the fastest
+    # one is the reference arm's number
     budget = max(2.0, min(30.0, 3.0 * max(args.steps, 1)))
     rates, nthreads, reps = oracle_vmult_rates(spec, u, src, budget)
     best = max(rates, key=rates.get)
@@ -523,8 +542,9 @@ def run_reference(args):
             "config": {"workload": "nh_tangent_vmult_q4_cantilever_64x8x8",
                        "n_dofs": n, "caching": best},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{reps} applications per caching variant, cached once, vmult "
-                                       f"timed alone, on {nthreads} threads; fastest: {best}; all: " +
+                             "sample": f"{reps} applications per variant (each caching of the reference in "
+                                       f"plain loops, and the cell-batched SIMD form /simdW), cached once, "
+                                       f"vmult timed alone, on {nthreads} threads; fastest: {best}; all: " +
                                        ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) +
                                        " MDoF/s (the reference itself needs deal.II/p4est/MPI, absent here)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -15,19 +15,29 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = ["oracle_capi.cpp", "oracle_core.hpp", "oracle_ops.hpp",
-           "oracle_solvers.hpp", "oracle_problems.hpp"]
+SOURCES = ["oracle_capi.cpp", "oracle_fast.cpp", "oracle_core.hpp", "oracle_ops.hpp",
+           "oracle_fast.hpp", "oracle_solvers.hpp", "oracle_problems.hpp"]
+FAST_LANES = (2, 4, 8)
+FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-fPIC", "-Wno-psabi"]
 
 
 def build(force=False):
-    """Compile the oracle with g++ (portable flags: no -march=native)."""
-    os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
+    """Compile the oracle with g++ (portable flags: no -march=native): the
+    main unit and one unit per lane count of the throughput form, compiled in
+    parallel, then linked."""
+    bdir = os.path.join(HERE, "_build")
+    os.makedirs(bdir, exist_ok=True)
     newest = max(os.path.getmtime(os.path.join(HERE, s)) for s in SOURCES)
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
-           os.path.join(HERE, "oracle_capi.cpp"), "-o", LIB_PATH + ".tmp"]
-    subprocess.check_call(cmd)
+    units = [(os.path.join(HERE, "oracle_capi.cpp"), os.path.join(bdir, "capi.o"), [])]
+    units += [(os.path.join(HERE, "oracle_fast.cpp"), os.path.join(bdir, f"fast_w{w}.o"), [f"-DORC_FAST_W={w}"])
+              for w in FAST_LANES]
+    procs = [(subprocess.Popen(["g++", *FLAGS, *d, "-c", src, "-o", obj]), src) for src, obj, d in units]
+    failed = [src for p, src in procs if p.wait() != 0]
+    if failed:
+        raise subprocess.CalledProcessError(1, f"g++ {' '.join(failed)}")
+    subprocess.check_call(["g++", "-shared", "-fopenmp", *[obj for _, obj, _ in units], "-o", LIB_PATH + ".tmp"])
     os.replace(LIB_PATH + ".tmp", LIB_PATH)
     return LIB_PATH
 
@@ -184,6 +194,23 @@ def nh_vmult_timed(mesh, level, mat, caching, u, src, reps):
                                  _ptr(u), _ptr(src), _ptr(dst), int(reps), C.byref(secs))
     if rc != 0:
         raise RuntimeError(f"oracle nh_vmult_timed failed: {rc}")
+    return dst, secs.value
+
+
+def nh_vmult_fast_timed(mesh, level, mat, caching, u, src, reps, lanes=8):
+    """(dst, seconds) of the throughput form of the FP64 tangent vmult
+    (cell batches of `lanes` = 2, 4 or 8 cells across SIMD lanes, compile-time
+    degree, even-odd collocation sweeps; 3D, n_q = p + 1, tensor4_ns or
+    scalar_referential): cached once, applied once untimed, then `reps`
+    applications timed."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    dst = np.zeros_like(src)
+    secs = C.c_double()
+    rc = lib().or_nh_vmult_fast_timed(C.byref(mesh), level, C.byref(mat), CACHING.get(caching, caching),
+                                      int(lanes), _ptr(u), _ptr(src), _ptr(dst), int(reps), C.byref(secs))
+    if rc != 0:
+        raise RuntimeError(f"oracle nh_vmult_fast_timed failed: {rc}")
     return dst, secs.value
 
 

@@ -9,6 +9,18 @@
 
 using namespace orc;
 
+namespace orc
+{
+  // oracle_fast.cpp, one object per lane count
+#define ORC_FAST_DECL(w)                                                                                  \
+  int nh_vmult_fast_timed_w##w(const Box &box, const Basis1D &b, const Material &mat, Caching caching,   \
+                               const double *u, const double *src, double *dst, int reps, double *seconds);
+  ORC_FAST_DECL(2)
+  ORC_FAST_DECL(4)
+  ORC_FAST_DECL(8)
+#undef ORC_FAST_DECL
+} // namespace orc
+
 extern "C"
 {
   struct or_mesh_t
@@ -241,6 +253,38 @@ extern "C"
       op.vmult(dst, src);
     *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 0;
+  }
+
+  // the throughput form (oracle_fast.hpp) of the same vmult, 3D, n_q = p + 1,
+  // tensor4_ns or scalar_referential, cell batches of `lanes` = 2, 4 or 8:
+  // cached once, applied once untimed, then `reps` applications timed (dst
+  // holds the result); returns 0, -2 when the case is outside the fast form,
+  // -3 when det F <= 0
+  int
+  or_nh_vmult_fast_timed(const or_mesh_t *m, int level, const or_material_t *mat, int caching, int lanes,
+                         const double *u, const double *src, double *dst, int reps, double *seconds)
+  {
+    MeshSpec s = to_spec(m);
+    if (s.dim != 3 || s.n_q != s.degree + 1 || mat->formulation != 1 ||
+        (caching != tensor4_ns && caching != scalar_referential))
+      return -2;
+    Basis1D  b(s.degree, s.n_q);
+    Box      box = s.box(level);
+    Material mt  = to_mat(mat);
+    try
+      {
+        switch (lanes)
+          {
+            case 2: return nh_vmult_fast_timed_w2(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 4: return nh_vmult_fast_timed_w4(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 8: return nh_vmult_fast_timed_w8(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            default: return -2;
+          }
+      }
+    catch (...)
+      {
+        return -2;
+      }
   }
 
   int
