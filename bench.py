@@ -184,7 +184,7 @@ CPU_CACHINGS = ("scalar_referential", "tensor2", "tensor4", "tensor4_ns")
 # the throughput form (oracle/oracle_fast.hpp): cell batches across SIMD
 # lanes, compile-time degree, even-odd collocation sweeps, as deal.II runs
 # the reference's vmult
-CPU_FAST = tuple((c, w) for c in ("scalar_referential", "tensor4_ns") for w in (2, 4, 8))
+CPU_FAST = tuple((c, w) for c in CPU_CACHINGS for w in (2, 4, 8))
 
 
 def oracle_vmult_rates(spec, u, src, budget_s, threads=None):

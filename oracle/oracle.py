@@ -200,8 +200,8 @@ def nh_vmult_timed(mesh, level, mat, caching, u, src, reps):
 def nh_vmult_fast_timed(mesh, level, mat, caching, u, src, reps, lanes=8):
     """(dst, seconds) of the throughput form of the FP64 tangent vmult
     (cell batches of `lanes` = 2, 4 or 8 cells across SIMD lanes, compile-time
-    degree, even-odd collocation sweeps; 3D, n_q = p + 1, tensor4_ns or
-    scalar_referential): cached once, applied once untimed, then `reps`
+    degree, even-odd collocation sweeps; 3D, n_q = p + 1, formulation 1, any
+    caching variant): cached once, applied once untimed, then `reps`
     applications timed."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     src = np.ascontiguousarray(src, dtype=np.float64)

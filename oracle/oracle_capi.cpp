@@ -256,7 +256,7 @@ extern "C"
   }
 
   // the throughput form (oracle_fast.hpp) of the same vmult, 3D, n_q = p + 1,
-  // tensor4_ns or scalar_referential, cell batches of `lanes` = 2, 4 or 8:
+  // formulation 1, any caching variant, cell batches of `lanes` = 2, 4 or 8:
   // cached once, applied once untimed, then `reps` applications timed (dst
   // holds the result); returns 0, -2 when the case is outside the fast form,
   // -3 when det F <= 0
@@ -265,8 +265,7 @@ extern "C"
                          const double *u, const double *src, double *dst, int reps, double *seconds)
   {
     MeshSpec s = to_spec(m);
-    if (s.dim != 3 || s.n_q != s.degree + 1 || mat->formulation != 1 ||
-        (caching != tensor4_ns && caching != scalar_referential))
+    if (s.dim != 3 || s.n_q != s.degree + 1 || mat->formulation != 1 || caching < 0 || caching > 3)
       return -2;
     Basis1D  b(s.degree, s.n_q);
     Box      box = s.box(level);

@@ -16,9 +16,11 @@
 //     then derivative sweeps on the Gauss points, each 1D product in even-odd
 //     form (deal.II's EvaluatorTensorProduct<evaluate_evenodd>);
 //   * the quadrature-point operations are those of oracle_ops.hpp (NHQ) for
-//     tensor4_ns (mf_nh_operator.h:996-1010) and scalar_referential
+//     every caching variant of formulation 1: scalar_referential
 //     (mf_nh_operator.h:848-943, with the second gradient evaluation of the
-//     cached linearisation values, :865-867);
+//     cached linearisation values, :865-867), tensor2 and tensor4 (deformed
+//     frame, :945-994; tensor4 stored on symmetric index pairs like
+//     SymmetricTensor<4,3>) and tensor4_ns (:996-1010);
 //   * cells are coloured by parity (cells of one colour share no DoF), so
 //     threads scatter without atomics; constrained DoFs read as zero and are
 //     skipped on the scatter, and the constrained rows get dst += src.
@@ -248,6 +250,11 @@ namespace orc
       std::vector<unsigned char>         touches;    // batch has a constrained node
       std::vector<size_t>                colour_end; // batches of colour c end here
       std::vector<vd>                    A;          // tensor4_ns: [batch][q][81]
+      // tensor2 / tensor4 (deformed frame): per qp F^{-1} (9), det F, tau / J
+      // (9), then tensor2: 2c / J, 1 / J; tensor4: 1 / J and the symmetric
+      // 4th-order tensor as a 6 x 6 matrix on (00, 11, 22, 01, 02, 12)
+      std::vector<vd>                    E;
+      int                                es = 0; // entries of E per qp
       std::vector<vd>                    cscal;      // scalar_referential: [batch][q]
       std::vector<vd>                    ucell;      // scalar_referential: [batch][c][Nd]
       std::vector<size_t>                constrained_rows; // c * n_nodes + node
@@ -260,8 +267,9 @@ namespace orc
         , lambda(mat.lambda())
         , ra(mat.rho_alpha())
       {
-        if (cach != tensor4_ns && cach != scalar_referential)
-          throw std::runtime_error("fast form: tensor4_ns and scalar_referential only");
+        if (mat.formulation != 1)
+          throw std::runtime_error("fast form: formulation 1 only");
+        es = cach == tensor2 ? 21 : (cach == tensor4 ? 56 : 0);
         for (int colour = 0; colour < 8; ++colour)
           {
             const std::vector<size_t> cs = colour_cells(box, colour);
@@ -366,14 +374,16 @@ namespace orc
           }
       }
 
-      // NeoHookOperator::cache (mf_nh_operator.h:394-523) for the two
-      // variants, from the linearisation u read without constraints
+      // NeoHookOperator::cache (mf_nh_operator.h:394-523), from the
+      // linearisation u read without constraints
       bool
       cache(const double *u)
       {
         const size_t nb = cells.size();
         if (caching == tensor4_ns)
           A.assign(nb * Nd * 81, splat(0.0));
+        else if (es > 0)
+          E.assign(nb * Nd * es, splat(0.0));
         else
           {
             cscal.assign(nb * Nd, splat(0.0));
@@ -414,6 +424,40 @@ namespace orc
                         continue;
                       }
                     invert(3, F, Fi);
+                    if (es > 0)
+                      {
+                        const double c = mu - 2.0 * lambda * lnJ;
+                        vd          *x = &E[(bt * Nd + q) * es];
+                        for (int i = 0; i < 9; ++i)
+                          x[i][l] = Fi[i];
+                        x[9][l] = J;
+                        for (int i = 0; i < 3; ++i)
+                          for (int j = 0; j < 3; ++j)
+                            {
+                              const double bb = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+                              x[10 + i * 3 + j][l] = (mu * bb - (i == j ? c : 0.0)) / J;
+                            }
+                        if (caching == tensor2)
+                          {
+                            x[19][l] = c * 2.0 / J;
+                            x[20][l] = 1.0 / J;
+                            continue;
+                          }
+                        x[19][l] = 1.0 / J;
+                        // (2c / J) S + (2 lambda / J) I x I on the symmetric
+                        // pairs (mf_nh_operator.h:490-494)
+                        static const int vi[6] = {0, 1, 2, 0, 0, 1}, vj[6] = {0, 1, 2, 1, 2, 2};
+                        const double     a = c * 2.0 / J, bl = lambda * 2.0 / J;
+                        for (int r = 0; r < 6; ++r)
+                          for (int t = 0; t < 6; ++t)
+                            {
+                              const int i = vi[r], j = vj[r], k = vi[t], m = vj[t];
+                              x[20 + r * 6 + t][l] =
+                                a * 0.5 * (double(i == k && j == m) + double(i == m && j == k)) +
+                                bl * double(i == j && k == m);
+                            }
+                        continue;
+                      }
                     vd *a = &A[(bt * Nd + q) * 81];
                     for (int i = 0; i < 3; ++i)
                       for (int j = 0; j < 3; ++j)
@@ -476,10 +520,62 @@ namespace orc
         const vd rav = splat(ra), lam2 = splat(2.0 * lambda), muv = splat(mu);
         for (int q = 0; q < Nd; ++q)
           {
-            vd H[9], P[9];
+            vd H[9], P[9], vs = rav;
             for (int i = 0; i < 9; ++i)
               H[i] = g[i * Nd + q];
-            if (caching == tensor4_ns)
+            if (es > 0)
+              {
+                // deformed frame (mf_nh_operator.h:945-994), pulled back:
+                // P = J Pc F^{-T}
+                const vd *x  = &E[(bt * Nd + q) * es];
+                const vd *Fi = x, *T2 = x + 10;
+                const vd  J  = x[9];
+                vd        gg[9], Pc[9];
+                for (int i = 0; i < 3; ++i)
+                  for (int j = 0; j < 3; ++j)
+                    gg[i * 3 + j] = H[i * 3] * Fi[j] + H[i * 3 + 1] * Fi[3 + j] + H[i * 3 + 2] * Fi[6 + j];
+                for (int i = 0; i < 3; ++i)
+                  for (int j = 0; j < 3; ++j)
+                    Pc[i * 3 + j] = gg[i * 3] * T2[j] + gg[i * 3 + 1] * T2[3 + j] + gg[i * 3 + 2] * T2[6 + j];
+                if (caching == tensor2)
+                  {
+                    const vd sc = x[19], tmp = lam2 * x[20] * (gg[0] + gg[4] + gg[8]);
+                    for (int i = 0; i < 3; ++i)
+                      for (int j = 0; j < 3; ++j)
+                        Pc[i * 3 + j] += sc * 0.5 * (gg[i * 3 + j] + gg[j * 3 + i]);
+                    Pc[0] += tmp;
+                    Pc[4] += tmp;
+                    Pc[8] += tmp;
+                    vs = rav * x[20] * J;
+                  }
+                else
+                  {
+                    const vd *C = x + 20;
+                    const vd  e[6] = {gg[0], gg[4], gg[8], gg[1] + gg[3], gg[2] + gg[6], gg[5] + gg[7]};
+                    vd        r[6];
+                    for (int a = 0; a < 6; ++a)
+                      {
+                        // off-diagonal pairs count twice: 2 * 0.5 (g_kl + g_lk)
+                        vd t = C[a * 6] * e[0] + C[a * 6 + 1] * e[1] + C[a * 6 + 2] * e[2];
+                        t += C[a * 6 + 3] * e[3] + C[a * 6 + 4] * e[4] + C[a * 6 + 5] * e[5];
+                        r[a] = t;
+                      }
+                    Pc[0] += r[0];
+                    Pc[4] += r[1];
+                    Pc[8] += r[2];
+                    Pc[1] += r[3];
+                    Pc[3] += r[3];
+                    Pc[2] += r[4];
+                    Pc[6] += r[4];
+                    Pc[5] += r[5];
+                    Pc[7] += r[5];
+                    vs = rav * x[19] * J;
+                  }
+                for (int i = 0; i < 3; ++i)
+                  for (int j = 0; j < 3; ++j)
+                    P[i * 3 + j] = J * (Pc[i * 3] * Fi[j * 3] + Pc[i * 3 + 1] * Fi[j * 3 + 1] + Pc[i * 3 + 2] * Fi[j * 3 + 2]);
+              }
+            else if (caching == tensor4_ns)
               {
                 // P = A : H (mf_nh_operator.h:996-1010)
                 const vd *a = &A[(bt * Nd + q) * 81];
@@ -526,7 +622,7 @@ namespace orc
             const vd jw = splat(sh.jxw[q]);
             for (int c = 0; c < 3; ++c)
               {
-                val[c * Nd + q] *= rav * jw;
+                val[c * Nd + q] *= vs * jw;
                 for (int d = 0; d < 3; ++d)
                   g[(3 * c + d) * Nd + q] = P[c * 3 + d] * jw;
               }
