@@ -235,6 +235,34 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
                       ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) + " MDoF/s"}
 
 
+def cpu_heat_step():
+    """The heat workload beside the GPU's (unit cube, 16^3 cells, Q2, 35,937
+    DoFs) on the host cores, with the oracle's plain loops: one backward-Euler
+    step by GMG-CG to 1e-10 (FP32 levels, as on the GPU), setup included, and
+    100 FP64 vmults on U(-1,1)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import workloads as W
+    spec = W.unit_cube_heat(2, 4)
+    om = W.to_oracle_mesh(O, spec)
+    c, w, a = W.gaussian_source(0)
+    p = O.HeatParams()
+    p.mesh = om
+    p.dt, p.n_steps, p.tol_rel, p.precond, p.mg_float = 0.1, 1, 1e-10, 2, 1
+    p.n_gauss = 8
+    for i in range(8):
+        for d in range(3):
+            p.g_center[i][d] = c[i, d]
+        p.g_width[i] = w[i]
+        p.g_amp[i] = a[i]
+    r = O.heat_run(p)
+    n = W.n_dofs(spec, 1)
+    _, secs = O.heat_vmult_timed(om, spec["n_ref"], 0.1, W.uniform_vector(n, 1), 100)
+    return {"workload": "heat unit cube 16^3 Q2, 35,937 DoFs", "form": "oracle plain loops",
+            "step_s": r.seconds, "cg_its": int(r.cg_its[0]), "vmult_100_s": secs,
+            "vmult_dofs_per_s": 100 * n / secs}
+
+
 def _timed_vmults(torch, op, dst, src, flush, stream, reps):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(reps)]
@@ -737,6 +765,10 @@ def main():
         except Exception as e:  # reported, never fatal for the GPU number
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
                                     "sample": f"failed: {e}"}
+        try:
+            line["cpu_baseline"]["heat_step_16cube_q2"] = cpu_heat_step()
+        except Exception as e:
+            line["cpu_baseline"]["heat_step_16cube_q2"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

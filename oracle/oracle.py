@@ -154,6 +154,16 @@ def heat_vmult(mesh, level, k_dt, src, precision=64, constrained=True):
     return dst
 
 
+def heat_vmult_timed(mesh, level, k_dt, src, reps):
+    """(dst, seconds) of `reps` FP64 heat vmults after one untimed one."""
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    dst = np.zeros_like(src)
+    secs = C.c_double()
+    lib().or_heat_vmult_timed(C.byref(mesh), level, C.c_double(k_dt), _ptr(src), _ptr(dst), int(reps),
+                              C.byref(secs))
+    return dst, secs.value
+
+
 def heat_inv_diagonal(mesh, level, k_dt, precision=64):
     out = np.zeros(n_nodes(mesh, level), dtype=_dt(precision))
     lib().or_heat_inv_diagonal(C.byref(mesh), level, C.c_double(k_dt),

@@ -286,6 +286,28 @@ extern "C"
       }
   }
 
+  // heat vmult (M + k dt K, constrained) applied once untimed, then `reps`
+  // applications timed; dst holds the result
+  int
+  or_heat_vmult_timed(const or_mesh_t *m, int level, double k_dt, const double *src, double *dst, int reps,
+                      double *seconds)
+  {
+    MeshSpec        s = to_spec(m);
+    Basis1D         b(s.degree, s.n_q);
+    LevelOp<double> op;
+    op.box   = s.box(level);
+    op.basis = &b;
+    op.nc    = 1;
+    op.kind  = op_heat;
+    op.k_dt  = k_dt;
+    op.vmult(dst, src);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < reps; ++r)
+      op.vmult(dst, src);
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+  }
+
   int
   or_nh_inv_diagonal(const or_mesh_t *m, int level, const or_material_t *mat,
                      int caching, int precision, const void *u, void *out)
