@@ -237,9 +237,10 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
 
 def cpu_heat_step():
     """The heat workload beside the GPU's (unit cube, 16^3 cells, Q2, 35,937
-    DoFs) on the host cores, with the oracle's plain loops: one backward-Euler
-    step by GMG-CG to 1e-10 (FP32 levels, as on the GPU), setup included, and
-    100 FP64 vmults on U(-1,1)."""
+    DoFs) on the host cores: one backward-Euler step by GMG-CG to 1e-10 (FP32
+    levels, as on the GPU), setup included, with the oracle's plain loops; and
+    100 FP64 vmults on U(-1,1), the fastest of the plain loops and the
+    cell-batched form at 2, 4 and 8 lanes."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import workloads as W
@@ -257,10 +258,19 @@ def cpu_heat_step():
         p.g_amp[i] = a[i]
     r = O.heat_run(p)
     n = W.n_dofs(spec, 1)
-    _, secs = O.heat_vmult_timed(om, spec["n_ref"], 0.1, W.uniform_vector(n, 1), 100)
-    return {"workload": "heat unit cube 16^3 Q2, 35,937 DoFs", "form": "oracle plain loops",
-            "step_s": r.seconds, "cg_its": int(r.cg_its[0]), "vmult_100_s": secs,
-            "vmult_dofs_per_s": 100 * n / secs}
+    x = W.uniform_vector(n, 1)
+    ref, secs = O.heat_vmult_timed(om, spec["n_ref"], 0.1, x, 100)
+    rates = {"plain": 100 * n / secs}
+    for w in (2, 4, 8):
+        out, secs = O.heat_vmult_fast_timed(om, spec["n_ref"], 0.1, x, 100, lanes=w)
+        if not np.linalg.norm(out - ref) <= 1e-12 * np.linalg.norm(ref):
+            raise RuntimeError(f"throughput heat form ({w} lanes) differs from the oracle")
+        rates[f"simd{w}"] = 100 * n / secs
+    best = max(rates, key=rates.get)
+    return {"workload": "heat unit cube 16^3 Q2, 35,937 DoFs",
+            "step_s": r.seconds, "step_form": "oracle plain loops", "cg_its": int(r.cg_its[0]),
+            "vmult_100_s": 100 * n / rates[best], "vmult_dofs_per_s": rates[best], "vmult_form": best,
+            "vmult_all_dofs_per_s": rates}
 
 
 def _timed_vmults(torch, op, dst, src, flush, stream, reps):

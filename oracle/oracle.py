@@ -164,6 +164,21 @@ def heat_vmult_timed(mesh, level, k_dt, src, reps):
     return dst, secs.value
 
 
+def heat_vmult_fast_timed(mesh, level, k_dt, src, reps, lanes=2):
+    """(dst, seconds) of the throughput form of the FP64 heat vmult (cell
+    batches of `lanes` cells across SIMD lanes, compile-time degree, even-odd
+    collocation sweeps; 3D, n_q = p + 1): one untimed application, then
+    `reps` timed."""
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    dst = np.zeros_like(src)
+    secs = C.c_double()
+    rc = lib().or_heat_vmult_fast_timed(C.byref(mesh), level, C.c_double(k_dt), int(lanes), _ptr(src),
+                                        _ptr(dst), int(reps), C.byref(secs))
+    if rc != 0:
+        raise RuntimeError(f"oracle heat_vmult_fast_timed failed: {rc}")
+    return dst, secs.value
+
+
 def heat_inv_diagonal(mesh, level, k_dt, precision=64):
     out = np.zeros(n_nodes(mesh, level), dtype=_dt(precision))
     lib().or_heat_inv_diagonal(C.byref(mesh), level, C.c_double(k_dt),

@@ -14,7 +14,9 @@ namespace orc
   // oracle_fast.cpp, one object per lane count
 #define ORC_FAST_DECL(w)                                                                                  \
   int nh_vmult_fast_timed_w##w(const Box &box, const Basis1D &b, const Material &mat, Caching caching,   \
-                               const double *u, const double *src, double *dst, int reps, double *seconds);
+                               const double *u, const double *src, double *dst, int reps, double *seconds); \
+  int heat_vmult_fast_timed_w##w(const Box &box, const Basis1D &b, double k_dt, const double *src, double *dst, \
+                                 int reps, double *seconds);
   ORC_FAST_DECL(2)
   ORC_FAST_DECL(4)
   ORC_FAST_DECL(8)
@@ -306,6 +308,26 @@ extern "C"
       op.vmult(dst, src);
     *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 0;
+  }
+
+  // the throughput form of the heat vmult (3D, n_q = p + 1, `lanes` = 2, 4
+  // or 8), applied once untimed, then `reps` applications timed
+  int
+  or_heat_vmult_fast_timed(const or_mesh_t *m, int level, double k_dt, int lanes, const double *src, double *dst,
+                           int reps, double *seconds)
+  {
+    MeshSpec s = to_spec(m);
+    if (s.dim != 3 || s.n_q != s.degree + 1)
+      return -2;
+    Basis1D b(s.degree, s.n_q);
+    Box     box = s.box(level);
+    switch (lanes)
+      {
+        case 2: return heat_vmult_fast_timed_w2(box, b, k_dt, src, dst, reps, seconds);
+        case 4: return heat_vmult_fast_timed_w4(box, b, k_dt, src, dst, reps, seconds);
+        case 8: return heat_vmult_fast_timed_w8(box, b, k_dt, src, dst, reps, seconds);
+        default: return -2;
+      }
   }
 
   int

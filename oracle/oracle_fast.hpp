@@ -1,7 +1,7 @@
 // CPU ORACLE — TEST INFRASTRUCTURE ONLY (see oracle_core.hpp).
 //
-// Throughput form of the neo-Hookean tangent vmult for the timed CPU
-// baseline.  It restates how the reference's CPU path is executed by deal.II
+// Throughput form of the neo-Hookean tangent vmult and of the heat operator
+// for the timed CPU baseline.  It restates how the reference's CPU path is executed by deal.II
 // rather than the plain loops of oracle_ops.hpp, so that the baseline is not
 // slowed by the oracle's generality:
 //   * cells are processed in batches of W lanes, one cell per lane, as
@@ -235,41 +235,24 @@ namespace orc
         Fi[i] *= r;
     }
 
-    // the tangent on one level, cached for one linearisation point
-    template <int N>
-    struct NHFast
+    // cell batches of one level: cells of one parity colour in groups of W
+    // (a partly filled last group repeats its last cell in the spare lanes,
+    // which are never scattered), lane-interleaved gather and scatter of NC
+    // component-blocked fields
+    template <int N, int NC>
+    struct CellBatches
     {
-      static constexpr int Nd = N * N * N;
-      const Box           &box;
-      Shape<N>             sh;
-      Caching              caching;
-      double               mu, lambda, ra;
-      // cell batches, by colour: batch b holds cells[b][0..W)
+      static constexpr int                Nd = N * N * N;
+      const Box                          &box;
       std::vector<std::array<size_t, W>> cells;
       std::vector<int>                   lanes;      // filled lanes per batch
       std::vector<unsigned char>         touches;    // batch has a constrained node
       std::vector<size_t>                colour_end; // batches of colour c end here
-      std::vector<vd>                    A;          // tensor4_ns: [batch][q][81]
-      // tensor2 / tensor4 (deformed frame): per qp F^{-1} (9), det F, tau / J
-      // (9), then tensor2: 2c / J, 1 / J; tensor4: 1 / J and the symmetric
-      // 4th-order tensor as a 6 x 6 matrix on (00, 11, 22, 01, 02, 12)
-      std::vector<vd>                    E;
-      int                                es = 0; // entries of E per qp
-      std::vector<vd>                    cscal;      // scalar_referential: [batch][q]
-      std::vector<vd>                    ucell;      // scalar_referential: [batch][c][Nd]
       std::vector<size_t>                constrained_rows; // c * n_nodes + node
 
-      NHFast(const Box &bx, const Basis1D &b, const Material &mat, Caching cach)
+      explicit CellBatches(const Box &bx)
         : box(bx)
-        , sh(b, bx)
-        , caching(cach)
-        , mu(mat.mu)
-        , lambda(mat.lambda())
-        , ra(mat.rho_alpha())
       {
-        if (mat.formulation != 1)
-          throw std::runtime_error("fast form: formulation 1 only");
-        es = cach == tensor2 ? 21 : (cach == tensor4 ? 56 : 0);
         for (int colour = 0; colour < 8; ++colour)
           {
             const std::vector<size_t> cs = colour_cells(box, colour);
@@ -289,7 +272,7 @@ namespace orc
               }
             colour_end.push_back(cells.size());
           }
-        for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < NC; ++c)
           for (size_t g = 0; g < box.n_nodes; ++g)
             if (box.constrained(g, c))
               constrained_rows.push_back(size_t(c) * box.n_nodes + g);
@@ -314,7 +297,7 @@ namespace orc
         return box.node(cc[0] * box.p, cc[1] * box.p, cc[2] * box.p);
       }
 
-      // read the 3 components of the batch's cells into lane-interleaved form
+      // read the NC components of the batch's cells into lane-interleaved form
       void
       gather(size_t bt, const double *src, vd *u, bool constrained) const
       {
@@ -323,7 +306,7 @@ namespace orc
           {
             const size_t e  = cells[bt][l];
             const size_t g0 = first_node(e);
-            for (int c = 0; c < 3; ++c)
+            for (int c = 0; c < NC; ++c)
               {
                 const double *s = src + size_t(c) * box.n_nodes + g0;
                 vd           *o = u + c * Nd;
@@ -336,7 +319,7 @@ namespace orc
               {
                 size_t nodes[Nd];
                 box.cell_nodes(e, nodes);
-                for (int c = 0; c < 3; ++c)
+                for (int c = 0; c < NC; ++c)
                   for (int n = 0; n < Nd; ++n)
                     if (box.constrained(nodes[n], c))
                       u[c * Nd + n][l] = 0.0;
@@ -356,13 +339,13 @@ namespace orc
               {
                 size_t nodes[Nd];
                 box.cell_nodes(e, nodes);
-                for (int c = 0; c < 3; ++c)
+                for (int c = 0; c < NC; ++c)
                   for (int n = 0; n < Nd; ++n)
                     if (!box.constrained(nodes[n], c))
                       dst[size_t(c) * box.n_nodes + nodes[n]] += out[c * Nd + n][l];
                 continue;
               }
-            for (int c = 0; c < 3; ++c)
+            for (int c = 0; c < NC; ++c)
               {
                 double   *d = dst + size_t(c) * box.n_nodes + g0;
                 const vd *o = out + c * Nd;
@@ -374,12 +357,75 @@ namespace orc
           }
       }
 
+      // dst = A src with A given cell batch by cell batch: dst zeroed, the
+      // colours in turn (the loop's closing barrier orders them), then the
+      // identity on the constrained rows.  apply(bt, scratch) handles a batch.
+      template <typename Apply>
+      void
+      run(double *dst, const double *src, size_t scratch, const Apply &apply) const
+      {
+        const size_t n = size_t(NC) * box.n_nodes;
+#pragma omp parallel
+        {
+          std::vector<vd> w(scratch);
+#pragma omp for schedule(static)
+          for (long i = 0; i < long(n); ++i)
+            dst[i] = 0.0;
+          size_t b0 = 0;
+          for (size_t colour = 0; colour < colour_end.size(); ++colour)
+            {
+              const size_t b1 = colour_end[colour];
+#pragma omp for schedule(static)
+              for (long bl = long(b0); bl < long(b1); ++bl)
+                apply(size_t(bl), w.data());
+              b0 = b1;
+            }
+#pragma omp for schedule(static)
+          for (long i = 0; i < long(constrained_rows.size()); ++i)
+            dst[constrained_rows[i]] += src[constrained_rows[i]];
+        }
+      }
+    };
+
+    // the tangent on one level, cached for one linearisation point
+    template <int N>
+    struct NHFast
+    {
+      static constexpr int Nd = N * N * N;
+      const Box           &box;
+      CellBatches<N, 3>    cb;
+      Shape<N>             sh;
+      Caching              caching;
+      double               mu, lambda, ra;
+      std::vector<vd>      A; // tensor4_ns: [batch][q][81]
+      // tensor2 / tensor4 (deformed frame): per qp F^{-1} (9), det F, tau / J
+      // (9), then tensor2: 2c / J, 1 / J; tensor4: 1 / J and the symmetric
+      // 4th-order tensor as a 6 x 6 matrix on (00, 11, 22, 01, 02, 12)
+      std::vector<vd> E;
+      int             es = 0; // entries of E per qp
+      std::vector<vd> cscal;  // scalar_referential: [batch][q]
+      std::vector<vd> ucell;  // scalar_referential: [batch][c][Nd]
+
+      NHFast(const Box &bx, const Basis1D &b, const Material &mat, Caching cach)
+        : box(bx)
+        , cb(bx)
+        , sh(b, bx)
+        , caching(cach)
+        , mu(mat.mu)
+        , lambda(mat.lambda())
+        , ra(mat.rho_alpha())
+      {
+        if (mat.formulation != 1)
+          throw std::runtime_error("fast form: formulation 1 only");
+        es = cach == tensor2 ? 21 : (cach == tensor4 ? 56 : 0);
+      }
+
       // NeoHookOperator::cache (mf_nh_operator.h:394-523), from the
       // linearisation u read without constraints
       bool
       cache(const double *u)
       {
-        const size_t nb = cells.size();
+        const size_t nb = cb.cells.size();
         if (caching == tensor4_ns)
           A.assign(nb * Nd * 81, splat(0.0));
         else if (es > 0)
@@ -398,7 +444,7 @@ namespace orc
           for (long bl = 0; bl < long(nb); ++bl)
             {
               const size_t bt = size_t(bl);
-              gather(bt, u, uu, false);
+              cb.gather(bt, u, uu, false);
               for (int c = 0; c < 3; ++c)
                 sh.gradients(uu + c * Nd, g + (3 * c) * Nd, g + (3 * c + 1) * Nd, g + (3 * c + 2) * Nd, t0, t1,
                              val);
@@ -477,36 +523,18 @@ namespace orc
       void
       vmult(double *dst, const double *src) const
       {
-        const size_t n = 3 * box.n_nodes;
-#pragma omp parallel
-        {
-          std::vector<vd> w(32 * Nd);
-          vd             *u = w.data(), *val = u + 3 * Nd, *g = val + 3 * Nd, *gu = g + 9 * Nd, *t0 = gu + 9 * Nd,
-             *t1 = t0 + Nd, *t2 = t1 + Nd, *out = t2 + Nd;
-#pragma omp for schedule(static)
-          for (long i = 0; i < long(n); ++i)
-            dst[i] = 0.0;
-          size_t b0 = 0;
-          for (size_t colour = 0; colour < colour_end.size(); ++colour)
-            {
-              const size_t b1 = colour_end[colour];
-              // the loop's closing barrier orders the colours
-#pragma omp for schedule(static)
-              for (long bl = long(b0); bl < long(b1); ++bl)
-                apply_batch(size_t(bl), src, dst, u, val, g, gu, t0, t1, t2, out);
-              b0 = b1;
-            }
-#pragma omp for schedule(static)
-          for (long i = 0; i < long(constrained_rows.size()); ++i)
-            dst[constrained_rows[i]] += src[constrained_rows[i]];
-        }
+        cb.run(dst, src, 32 * Nd, [&](size_t bt, vd *w) {
+          vd *u = w, *val = u + 3 * Nd, *g = val + 3 * Nd, *gu = g + 9 * Nd, *t0 = gu + 9 * Nd, *t1 = t0 + Nd,
+             *t2 = t1 + Nd, *out = t2 + Nd;
+          apply_batch(bt, src, dst, u, val, g, gu, t0, t1, t2, out);
+        });
       }
 
       void
       apply_batch(size_t bt, const double *src, double *dst, vd *u, vd *val, vd *g, vd *gu, vd *t0, vd *t1,
                   vd *t2, vd *out) const
       {
-        gather(bt, src, u, true);
+        cb.gather(bt, src, u, true);
         for (int c = 0; c < 3; ++c)
           sh.evaluate(u + c * Nd, val + c * Nd, g + (3 * c) * Nd, g + (3 * c + 1) * Nd, g + (3 * c + 2) * Nd, t0,
                       t1);
@@ -629,9 +657,61 @@ namespace orc
           }
         for (int c = 0; c < 3; ++c)
           sh.integrate(val + c * Nd, g + (3 * c) * Nd, g + (3 * c + 1) * Nd, g + (3 * c + 2) * Nd, out + c * Nd, t0);
-        scatter(bt, out, dst);
+        cb.scatter(bt, out, dst);
       }
     };
+
+    // the heat operator M + k dt K (heat_transfer.h:236-250: submit_value(u),
+    // submit_gradient(k dt grad u), k == 1)
+    template <int N>
+    struct HeatFast
+    {
+      static constexpr int Nd = N * N * N;
+      CellBatches<N, 1>    cb;
+      Shape<N>             sh;
+      double               kdt;
+
+      HeatFast(const Box &bx, const Basis1D &b, double k_dt)
+        : cb(bx)
+        , sh(b, bx)
+        , kdt(k_dt)
+      {}
+
+      void
+      vmult(double *dst, const double *src) const
+      {
+        cb.run(dst, src, 8 * Nd, [&](size_t bt, vd *w) {
+          vd *u = w, *val = u + Nd, *gx = val + Nd, *gy = gx + Nd, *gz = gy + Nd, *t0 = gz + Nd, *t1 = t0 + Nd,
+             *out = t1 + Nd;
+          cb.gather(bt, src, u, true);
+          sh.evaluate(u, val, gx, gy, gz, t0, t1);
+          for (int q = 0; q < Nd; ++q)
+            {
+              const vd jw = splat(sh.jxw[q]), kj = splat(kdt * sh.jxw[q]);
+              val[q] *= jw;
+              gx[q] *= kj;
+              gy[q] *= kj;
+              gz[q] *= kj;
+            }
+          sh.integrate(val, gx, gy, gz, out, t0);
+          cb.scatter(bt, out, dst);
+        });
+      }
+    };
+
+    template <int N>
+    int
+    heat_vmult_timed(const Box &box, const Basis1D &b, double k_dt, const double *src, double *dst, int reps,
+                     double *seconds)
+    {
+      HeatFast<N> op(box, b, k_dt);
+      op.vmult(dst, src);
+      const auto t0 = std::chrono::steady_clock::now();
+      for (int r = 0; r < reps; ++r)
+        op.vmult(dst, src);
+      *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return 0;
+    }
 
     // build, cache, apply once (untimed: first touch), then time `reps`
     // applications; returns 0, -2 (unsupported), -3 (det F <= 0)
