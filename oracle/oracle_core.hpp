@@ -3,8 +3,8 @@
 // This file is part of the CPU restatement of the reference's matrix-free
 // hot path (davidscn/matrix-free-dealii-precice).  It is used only by the
 // tests, by the smoke check and by the CPU-baseline leg of the benchmark, as
-// the checker.  The product (the CUDA library) never includes, links or calls
-// anything in this directory.
+// the CPU computation the device results are compared with.  The product (the
+// CUDA library) never includes, links or calls anything in this directory.
 //
 // What is restated here:
 //   * deal.II FE_Q(p) on Gauss-Lobatto support points and QGauss(n_q)
