@@ -28,8 +28,8 @@
 // oracle_fast.cpp instantiates this file once per lane count ORC_FAST_W.
 #include "oracle_ops.hpp"
 
+#include <array>
 #include <chrono>
-#include <memory>
 
 #ifndef ORC_FAST_W
 #define ORC_FAST_W 4
@@ -197,6 +197,8 @@ namespace orc
         sweep<N, 2, false>(D[2], val, gz);
       }
 
+      // gradients only (evaluate(gradients)); the collocation scheme passes
+      // through the values, which land in the scratch array val
       inline void
       gradients(const vd *u, vd *gx, vd *gy, vd *gz, vd *t0, vd *t1, vd *val) const
       {
