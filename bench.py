@@ -211,16 +211,25 @@ def oracle_vmult_rates(spec, u, src, budget_s, threads=None):
     first, ref = {}, {}
     for name, fn in plain.items():
         ref[name], first[name] = fn(1)
-    for name, fn in fast.items():
-        out, first[name] = fn(1)
-        err = np.linalg.norm(out - ref[name.split("/")[0]]) / np.linalg.norm(ref[name.split("/")[0]])
-        if not err < 1e-12:
-            raise RuntimeError(f"throughput form {name} differs from the oracle: {err:.2e}")
+    skipped = {}
+    for name, fn in list(fast.items()):
+        try:
+            out, first[name] = fn(1)
+            base = ref[name.split("/")[0]]
+            err = np.linalg.norm(out - base) / np.linalg.norm(base)
+            if not err < 1e-12:
+                raise RuntimeError(f"differs from the oracle: {err:.2e}")
+        except Exception as e:  # a variant that fails its check is not timed
+            skipped[name] = str(e)
+            fast.pop(name)
+            first.pop(name, None)
     reps = max(1, min(20, int(budget_s / max(sum(first.values()), 1e-9))))
     rates = {}
     for name, fn in {**plain, **fast}.items():
         _, secs = fn(reps)
         rates[name] = n / (secs / reps)
+    if skipped:
+        print(f"CPU variants not timed: {skipped}", file=sys.stderr, flush=True)
     return rates, nthreads, reps
 
 
