@@ -88,3 +88,36 @@ def test_every_entry_rejects_null_handles():
         else:
             assert rc == 1, (name, rc)
             assert msg and (name == "mfgpu_mesh_n_nodes" or "mesh" not in msg), (name, msg)
+
+
+def test_mesh_validation_edge_cases():
+    """Degenerate and out-of-range meshes are rejected with a reason before
+    any device work: no cells, inverted boxes, degrees outside 1..6,
+    refinement counts out of range, unknown dimensions, levels beyond the
+    hierarchy, too many Dirichlet entries."""
+    lib = mfgpu.lib()
+    lib.mfgpu_last_error.restype = ctypes.c_char_p
+    n = ctypes.c_size_t()
+
+    def rc_of(m, level=-1):
+        return lib.mfgpu_mesh_n_nodes(ctypes.byref(m), level, ctypes.byref(n))
+
+    bad = [mfgpu.make_mesh(2, 0, (0, 1, 1), (0, 0, 0), (1, 1, 1)),
+           mfgpu.make_mesh(2, 0, (-1, 1, 1), (0, 0, 0), (1, 1, 1)),
+           mfgpu.make_mesh(2, 0, (1, 1, 1), (0, 0, 0), (-1, 1, 1)),
+           mfgpu.make_mesh(2, -1, (1, 1, 1), (0, 0, 0), (1, 1, 1)),
+           mfgpu.make_mesh(2, 40, (1, 1, 1), (0, 0, 0), (1, 1, 1))]
+    for m in bad:
+        assert rc_of(m) == 1 and lib.mfgpu_last_error()
+    for degree in (0, 7):
+        assert rc_of(mfgpu.make_mesh(degree, 0, (1, 1, 1), (0, 0, 0), (1, 1, 1))) == 8
+    m = mfgpu.make_mesh(2, 0, (1, 1, 1), (0, 0, 0), (1, 1, 1))
+    m.dim = 4
+    assert rc_of(m) == 1 and b"dim" in lib.mfgpu_last_error()
+    m = mfgpu.make_mesh(2, 1, (1, 1, 1), (0, 0, 0), (1, 1, 1))
+    assert rc_of(m, 5) == 1 and b"level" in lib.mfgpu_last_error()
+    m.n_dirichlet = 9
+    assert rc_of(m) == 1 and b"n_dirichlet" in lib.mfgpu_last_error()
+    # the largest degree on one cell, and a 2D mesh
+    assert rc_of(mfgpu.make_mesh(6, 0, (1, 1, 1), (0, 0, 0), (1, 1, 1))) == 0 and n.value == 7 ** 3
+    assert rc_of(mfgpu.make_mesh(3, 1, (2, 1), (0, 0), (1, 1))) == 0 and n.value == 13 * 7
