@@ -282,6 +282,35 @@ def cpu_heat_step():
             "vmult_all_dofs_per_s": rates}
 
 
+def cpu_heat_sweep(reps=3):
+    """The degree sweep's heat operator (unit cube, 64^3 cells, Q1..Q6, FP64)
+    on the host cores in the cell-batched form, the fastest of 2, 4 and 8
+    lanes per degree; each degree's form is first checked against the
+    oracle's plain loops on a 2x1x1-cell mesh.  Returns {degree: DoF/s}."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import workloads as W
+    out = {}
+    for deg in range(1, 7):
+        small = W.unit_cube_heat(deg, 0, rep=(2, 1, 1))
+        om = W.to_oracle_mesh(O, small)
+        x = W.uniform_vector(W.n_dofs(small, 1), 5)
+        ref = O.heat_vmult(om, 0, 0.1, x)
+        spec = W.unit_cube_heat(deg, 6)
+        n = W.n_dofs(spec, 1)
+        big = W.to_oracle_mesh(O, spec)
+        src = W.uniform_vector(n, 1)
+        best = 0.0
+        for w in (2, 4, 8):
+            got, _ = O.heat_vmult_fast_timed(om, 0, 0.1, x, 1, lanes=w)
+            if not np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref):
+                raise RuntimeError(f"throughput heat form, degree {deg}, {w} lanes, differs from the oracle")
+            _, secs = O.heat_vmult_fast_timed(big, spec["n_ref"], 0.1, src, reps, lanes=w)
+            best = max(best, n * reps / secs)
+        out[str(deg)] = best
+    return out
+
+
 def _timed_vmults(torch, op, dst, src, flush, stream, reps):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(reps)]
@@ -788,6 +817,11 @@ def main():
             line["cpu_baseline"]["heat_step_16cube_q2"] = cpu_heat_step()
         except Exception as e:
             line["cpu_baseline"]["heat_step_16cube_q2"] = {"error": str(e)}
+        if not args.no_extras:
+            try:
+                line["cpu_baseline"]["heat_vmult_64cube_dofs_per_s"] = cpu_heat_sweep()
+            except Exception as e:
+                line["cpu_baseline"]["heat_vmult_64cube_dofs_per_s"] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
