@@ -247,9 +247,9 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
 def cpu_heat_step():
     """The heat workload beside the GPU's (unit cube, 16^3 cells, Q2, 35,937
     DoFs) on the host cores: one backward-Euler step by GMG-CG to 1e-10 (FP32
-    levels, as on the GPU), setup included, with the oracle's plain loops; and
-    100 FP64 vmults on U(-1,1), the fastest of the plain loops and the
-    cell-batched form at 2, 4 and 8 lanes."""
+    levels, as on the GPU), setup included, with every operator in the
+    cell-batched form; and 100 FP64 vmults on U(-1,1), the fastest of the
+    plain loops and the cell-batched form at 2, 4 and 8 lanes."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import workloads as W
@@ -258,7 +258,7 @@ def cpu_heat_step():
     c, w, a = W.gaussian_source(0)
     p = O.HeatParams()
     p.mesh = om
-    p.dt, p.n_steps, p.tol_rel, p.precond, p.mg_float = 0.1, 1, 1e-10, 2, 1
+    p.dt, p.n_steps, p.tol_rel, p.precond, p.mg_float, p.fast = 0.1, 1, 1e-10, 2, 1, 1
     p.n_gauss = 8
     for i in range(8):
         for d in range(3):
@@ -277,9 +277,39 @@ def cpu_heat_step():
         rates[f"simd{w}"] = 100 * n / secs
     best = max(rates, key=rates.get)
     return {"workload": "heat unit cube 16^3 Q2, 35,937 DoFs",
-            "step_s": r.seconds, "step_form": "oracle plain loops", "cg_its": int(r.cg_its[0]),
+            "step_s": r.seconds, "step_form": "cell-batched", "cg_its": int(r.cg_its[0]),
             "vmult_100_s": 100 * n / rates[best], "vmult_dofs_per_s": rates[best], "vmult_form": best,
             "vmult_all_dofs_per_s": rates}
+
+
+def cpu_mixed_solve():
+    """The config-2 system on the host cores (128x16x16-cell Q3 cantilever,
+    2,773,155 DoFs; first Newton system from rest, traction (0,-100,0) on
+    x = 8) set up and solved to a 1e-8 relative residual by FP64 CG with an
+    FP32 V-cycle and with an all-FP64 V-cycle, every operator, level operator
+    and diagonal in the cell-batched form (tensor2 caching, the fastest CPU
+    variant of the vmult)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import workloads as W
+    spec = W.cantilever(3, 4)
+    out = {"workload": "cantilever 128x16x16 cells Q3, 2,773,155 DoFs, first Newton system",
+           "tolerance": 1e-8, "form": "cell-batched, tensor2"}
+    for name, mg_float in (("mixed_fp32_vcycle", 1), ("fp64_vcycle", 0)):
+        p = O.SolidParams()
+        p.mesh = W.to_oracle_mesh(O, spec)
+        p.mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+        p.caching = O.CACHING["tensor2"]
+        p.precond, p.dt, p.n_steps, p.max_newton, p.max_it_mult = 2, 0.01, 1, 10, 1
+        p.relaxation, p.tol_lin = 0.65, 1e-8
+        p.traction_id = W.TRACTION_ID
+        p.traction[:] = [0.0, -100.0, 0.0]
+        p.cheb_degree, p.cheb_range, p.cheb_eig_its, p.coarse_accurate = 5, 20.0, 30, 1
+        p.mg_float, p.fast = mg_float, 1
+        its, setup_s, solve_s, _ = O.solid_first_solve(p, 1e-8)
+        out[name] = {"cg_iterations": its, "setup_s": setup_s, "solve_s": solve_s,
+                     "setup_plus_solve_s": setup_s + solve_s}
+    return out
 
 
 def cpu_heat_sweep(reps=3):
@@ -818,10 +848,12 @@ def main():
         except Exception as e:
             line["cpu_baseline"]["heat_step_16cube_q2"] = {"error": str(e)}
         if not args.no_extras:
-            try:
-                line["cpu_baseline"]["heat_vmult_64cube_dofs_per_s"] = cpu_heat_sweep()
-            except Exception as e:
-                line["cpu_baseline"]["heat_vmult_64cube_dofs_per_s"] = {"error": str(e)}
+            for key, fn in (("heat_vmult_64cube_dofs_per_s", cpu_heat_sweep),
+                            ("time_to_solve_1e-8", cpu_mixed_solve)):
+                try:
+                    line["cpu_baseline"][key] = fn()
+                except Exception as e:
+                    line["cpu_baseline"][key] = {"error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

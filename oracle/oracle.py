@@ -16,23 +16,25 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 SOURCES = ["oracle_capi.cpp", "oracle_fast.cpp", "oracle_core.hpp", "oracle_ops.hpp",
-           "oracle_fast.hpp", "oracle_solvers.hpp", "oracle_problems.hpp"]
+           "oracle_fast.hpp", "oracle_fast_api.hpp", "oracle_solvers.hpp", "oracle_problems.hpp"]
 FAST_LANES = (2, 4, 8)
 FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-fPIC", "-Wno-psabi"]
 
 
 def build(force=False):
     """Compile the oracle with g++ (portable flags: no -march=native): the
-    main unit and one unit per lane count of the throughput form, compiled in
-    parallel, then linked."""
+    main unit and one unit per lane count and scalar type of the throughput
+    form, compiled in parallel, then linked."""
     bdir = os.path.join(HERE, "_build")
     os.makedirs(bdir, exist_ok=True)
     newest = max(os.path.getmtime(os.path.join(HERE, s)) for s in SOURCES)
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     units = [(os.path.join(HERE, "oracle_capi.cpp"), os.path.join(bdir, "capi.o"), [])]
-    units += [(os.path.join(HERE, "oracle_fast.cpp"), os.path.join(bdir, f"fast_w{w}.o"), [f"-DORC_FAST_W={w}"])
+    units += [(os.path.join(HERE, "oracle_fast.cpp"), os.path.join(bdir, f"fast_w{w}d.o"), [f"-DORC_FAST_W={w}"])
               for w in FAST_LANES]
+    units += [(os.path.join(HERE, "oracle_fast.cpp"), os.path.join(bdir, "fast_w4f.o"),
+               ["-DORC_FAST_W=4", "-DORC_FAST_T=float", "-DORC_FAST_TS=f"])]
     procs = [(subprocess.Popen(["g++", *FLAGS, *d, "-c", src, "-o", obj]), src) for src, obj, d in units]
     failed = [src for p, src in procs if p.wait() != 0]
     if failed:
@@ -67,7 +69,7 @@ class SolidParams(C.Structure):
                 ("traction_id", C.c_int), ("traction", C.c_double * 3),
                 ("watch", C.c_double * 3), ("cheb_degree", C.c_int),
                 ("cheb_range", C.c_double), ("cheb_eig_its", C.c_int),
-                ("coarse_accurate", C.c_int), ("mg_float", C.c_int)]
+                ("coarse_accurate", C.c_int), ("mg_float", C.c_int), ("fast", C.c_int)]
 
 
 class SolidResult(C.Structure):
@@ -85,7 +87,7 @@ class HeatParams(C.Structure):
                 ("beta", C.c_double), ("n_gauss", C.c_int),
                 ("g_center", (C.c_double * 3) * 8),
                 ("g_width", C.c_double * 8), ("g_amp", C.c_double * 8),
-                ("mg_float", C.c_int)]
+                ("mg_float", C.c_int), ("fast", C.c_int)]
 
 
 class HeatResult(C.Structure):
@@ -280,6 +282,20 @@ def solid_run(params, return_u=False):
     if rc != 0:
         raise RuntimeError(f"oracle solid_run failed: {rc}")
     return (res, u) if return_u else res
+
+
+def solid_first_solve(params, tol):
+    """The first Newton system from rest, set up and solved to tol * |rhs|:
+    (cg_iterations, setup_seconds, solve_seconds, du).  params.fast = 1
+    routes every operator through the throughput form."""
+    n = params.mesh.dim * n_nodes(params.mesh, params.mesh.n_ref)
+    du = np.zeros(n)
+    its, t_setup, t_solve = C.c_int(), C.c_double(), C.c_double()
+    rc = lib().or_solid_first_solve(C.byref(params), C.c_double(tol), C.byref(its), C.byref(t_setup),
+                                    C.byref(t_solve), _ptr(du))
+    if rc != 0:
+        raise RuntimeError(f"oracle solid_first_solve failed: {rc}")
+    return its.value, t_setup.value, t_solve.value, du
 
 
 def heat_run(params, return_u=False):

@@ -3,25 +3,13 @@
 // C entry points of the oracle library (oracle/_build/liboracle.so), called
 // through ctypes by the tests, by __graft_entry__.smoke() and by the CPU
 // baseline leg of bench.py.  Never linked into the product.
+#include "oracle_fast_api.hpp"
 #include "oracle_problems.hpp"
 
 #include <chrono>
 
 using namespace orc;
 
-namespace orc
-{
-  // oracle_fast.cpp, one object per lane count
-#define ORC_FAST_DECL(w)                                                                                  \
-  int nh_vmult_fast_timed_w##w(const Box &box, const Basis1D &b, const Material &mat, Caching caching,   \
-                               const double *u, const double *src, double *dst, int reps, double *seconds); \
-  int heat_vmult_fast_timed_w##w(const Box &box, const Basis1D &b, double k_dt, const double *src, double *dst, \
-                                 int reps, double *seconds);
-  ORC_FAST_DECL(2)
-  ORC_FAST_DECL(4)
-  ORC_FAST_DECL(8)
-#undef ORC_FAST_DECL
-} // namespace orc
 
 extern "C"
 {
@@ -276,9 +264,9 @@ extern "C"
       {
         switch (lanes)
           {
-            case 2: return nh_vmult_fast_timed_w2(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
-            case 4: return nh_vmult_fast_timed_w4(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
-            case 8: return nh_vmult_fast_timed_w8(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 2: return nh_vmult_fast_timed_w2d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 4: return nh_vmult_fast_timed_w4d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 8: return nh_vmult_fast_timed_w8d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
             default: return -2;
           }
       }
@@ -323,9 +311,9 @@ extern "C"
     Box     box = s.box(level);
     switch (lanes)
       {
-        case 2: return heat_vmult_fast_timed_w2(box, b, k_dt, src, dst, reps, seconds);
-        case 4: return heat_vmult_fast_timed_w4(box, b, k_dt, src, dst, reps, seconds);
-        case 8: return heat_vmult_fast_timed_w8(box, b, k_dt, src, dst, reps, seconds);
+        case 2: return heat_vmult_fast_timed_w2d(box, b, k_dt, src, dst, reps, seconds);
+        case 4: return heat_vmult_fast_timed_w4d(box, b, k_dt, src, dst, reps, seconds);
+        case 8: return heat_vmult_fast_timed_w8d(box, b, k_dt, src, dst, reps, seconds);
         default: return -2;
       }
   }
@@ -399,6 +387,7 @@ extern "C"
     int           cheb_degree;
     double        cheb_range;
     int           cheb_eig_its, coarse_accurate, mg_float;
+    int           fast;
   };
 
   struct or_solid_result_t
@@ -410,9 +399,8 @@ extern "C"
     double seconds;
   };
 
-  int
-  or_solid_run(const or_solid_params_t *p, or_solid_result_t *r,
-               double *u_out)
+  static SolidParams
+  to_solid(const or_solid_params_t *p)
   {
     SolidParams P;
     P.mesh            = to_spec(&p->mesh);
@@ -435,11 +423,75 @@ extern "C"
     P.cheb_eig_its    = p->cheb_eig_its;
     P.coarse_accurate = p->coarse_accurate;
     P.mg_float        = p->mg_float;
+    P.fast            = p->fast;
     for (int d = 0; d < 3; ++d)
       {
         P.body_force[d] = p->body_force[d];
         P.traction[d]   = p->traction[d];
         P.watch[d]      = p->watch[d];
+      }
+    return P;
+  }
+
+  // the first Newton system of a time step from rest (u = 0, zero
+  // acceleration; the right-hand side is the traction term), set up and
+  // solved to tol * |rhs| as Solid::update_matrix_free + solve_linear_system
+  // do (mf_elasticity.h:1291-1353, 1983-2070); setup and solve timed apart.
+  // du (may be null) receives the update.  Returns 0, -1 on an exception,
+  // -3 when det F <= 0.
+  extern "C++"
+  {
+  template <typename LT>
+  static int
+  solid_first_solve_t(const SolidParams &P, double tol, int *its, double *setup_s, double *solve_s, double *du_out)
+  {
+    SolidDriver<LT>     drv(P);
+    const size_t        n = drv.fine.m();
+    std::vector<double> u(n, 0.0), acc(n, 0.0), rhs(n, 0.0), du(n, 0.0);
+    drv.assemble_residual(u, acc, rhs);
+    const auto t0 = std::chrono::steady_clock::now();
+    drv.update_operators(u);
+    if (!drv.fine.nh.positive_J)
+      return -3;
+    const auto t1 = std::chrono::steady_clock::now();
+    *its          = drv.solve_linear(rhs, du, tol * norm(n, rhs.data()));
+    const auto t2 = std::chrono::steady_clock::now();
+    *setup_s      = std::chrono::duration<double>(t1 - t0).count();
+    *solve_s      = std::chrono::duration<double>(t2 - t1).count();
+    if (du_out)
+      std::copy(du.begin(), du.end(), du_out);
+    return 0;
+  }
+  }
+
+  int
+  or_solid_first_solve(const or_solid_params_t *p, double tol, int *its, double *setup_s, double *solve_s,
+                       double *du_out)
+  {
+    try
+      {
+        const SolidParams P = to_solid(p);
+        return P.mg_float ? solid_first_solve_t<float>(P, tol, its, setup_s, solve_s, du_out) :
+                            solid_first_solve_t<double>(P, tol, its, setup_s, solve_s, du_out);
+      }
+    catch (...)
+      {
+        return -1;
+      }
+  }
+
+  int
+  or_solid_run(const or_solid_params_t *p, or_solid_result_t *r,
+               double *u_out)
+  {
+    SolidParams P;
+    try
+      {
+        P = to_solid(p);
+      }
+    catch (...)
+      {
+        return -1;
       }
     SolidResult R;
     auto        t0 = std::chrono::steady_clock::now();
@@ -493,6 +545,7 @@ extern "C"
     double    g_width[8];
     double    g_amp[8];
     int       mg_float;
+    int       fast;
   };
 
   struct or_heat_result_t
@@ -517,6 +570,7 @@ extern "C"
     P.beta     = p->beta;
     P.n_gauss  = p->n_gauss;
     P.mg_float = p->mg_float;
+    P.fast     = p->fast;
     for (int i = 0; i < 8; ++i)
       {
         for (int d = 0; d < 3; ++d)

@@ -1,15 +1,20 @@
 // CPU ORACLE — TEST INFRASTRUCTURE ONLY (see oracle_core.hpp).
 //
-// One lane count of the throughput form of the tangent and heat vmults
-// (oracle_fast.hpp), compiled once per -DORC_FAST_W=2,4,8; the C entry
-// or_nh_vmult_fast_timed in oracle_capi.cpp dispatches on the lane count.
+// One lane count and scalar type of the throughput form of the tangent and
+// heat operators (oracle_fast.hpp), compiled once per -DORC_FAST_W=2,4,8
+// (double) and for the FP32 levels (-DORC_FAST_T=float -DORC_FAST_TS=f).
+// The C entries in oracle_capi.cpp and the drivers in oracle_problems.hpp
+// call the functions below by their suffixed names.
 #include "oracle_fast.hpp"
+
+#define ORC_FAST_FN(name) ORC_FAST_CAT3(name, ORC_FAST_W, ORC_FAST_TS)
 
 namespace orc
 {
-  int ORC_FAST_CAT(nh_vmult_fast_timed_w, ORC_FAST_W)(const Box &box, const Basis1D &b, const Material &mat,
-                                                       Caching caching, const double *u, const double *src,
-                                                       double *dst, int reps, double *seconds)
+  using ORC_FAST_NS::real;
+
+  int ORC_FAST_FN(nh_vmult_fast_timed_w)(const Box &box, const Basis1D &b, const Material &mat, Caching caching,
+                                         const real *u, const real *src, real *dst, int reps, double *seconds)
   {
     using namespace ORC_FAST_NS;
     switch (box.p)
@@ -24,9 +29,8 @@ namespace orc
       }
   }
 
-  int ORC_FAST_CAT(heat_vmult_fast_timed_w, ORC_FAST_W)(const Box &box, const Basis1D &b, double k_dt,
-                                                         const double *src, double *dst, int reps,
-                                                         double *seconds)
+  int ORC_FAST_FN(heat_vmult_fast_timed_w)(const Box &box, const Basis1D &b, double k_dt, const real *src,
+                                           real *dst, int reps, double *seconds)
   {
     using namespace ORC_FAST_NS;
     switch (box.p)
@@ -38,6 +42,37 @@ namespace orc
         case 5: return heat_vmult_timed<6>(box, b, k_dt, src, dst, reps, seconds);
         case 6: return heat_vmult_timed<7>(box, b, k_dt, src, dst, reps, seconds);
         default: return -2;
+      }
+  }
+
+  FastLevel<real> ORC_FAST_FN(make_fast_nh_w)(const Box &box, const Basis1D &b, const Material &mat,
+                                              Caching caching, const real *u, bool &ok)
+  {
+    using namespace ORC_FAST_NS;
+    switch (box.p)
+      {
+        case 1: return make_nh_level<2>(box, b, mat, caching, u, ok);
+        case 2: return make_nh_level<3>(box, b, mat, caching, u, ok);
+        case 3: return make_nh_level<4>(box, b, mat, caching, u, ok);
+        case 4: return make_nh_level<5>(box, b, mat, caching, u, ok);
+        case 5: return make_nh_level<6>(box, b, mat, caching, u, ok);
+        case 6: return make_nh_level<7>(box, b, mat, caching, u, ok);
+        default: throw std::runtime_error("fast form: degree 1..6");
+      }
+  }
+
+  FastLevel<real> ORC_FAST_FN(make_fast_heat_w)(const Box &box, const Basis1D &b, double k_dt)
+  {
+    using namespace ORC_FAST_NS;
+    switch (box.p)
+      {
+        case 1: return make_heat_level<2>(box, b, k_dt);
+        case 2: return make_heat_level<3>(box, b, k_dt);
+        case 3: return make_heat_level<4>(box, b, k_dt);
+        case 4: return make_heat_level<5>(box, b, k_dt);
+        case 5: return make_heat_level<6>(box, b, k_dt);
+        case 6: return make_heat_level<7>(box, b, k_dt);
+        default: throw std::runtime_error("fast form: degree 1..6");
       }
   }
 } // namespace orc

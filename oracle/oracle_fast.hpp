@@ -30,25 +30,34 @@
 
 #include <array>
 #include <chrono>
+#include <memory>
 
 #ifndef ORC_FAST_W
 #define ORC_FAST_W 4
 #endif
+// scalar type of the lanes (double, or float for FP32 multigrid levels) and
+// its namespace suffix
+#ifndef ORC_FAST_T
+#define ORC_FAST_T double
+#define ORC_FAST_TS d
+#endif
 #define ORC_FAST_CAT2(a, b) a##b
 #define ORC_FAST_CAT(a, b) ORC_FAST_CAT2(a, b)
-#define ORC_FAST_NS ORC_FAST_CAT(fast_w, ORC_FAST_W)
+#define ORC_FAST_CAT3(a, b, c) ORC_FAST_CAT(ORC_FAST_CAT(a, b), c)
+#define ORC_FAST_NS ORC_FAST_CAT3(fast_w, ORC_FAST_W, ORC_FAST_TS)
 
 namespace orc
 {
-  // one namespace per lane count, so that several widths link together
+  // one namespace per lane count and scalar type, so that several link together
   namespace ORC_FAST_NS
   {
     constexpr int W = ORC_FAST_W; // lanes per cell batch
 
-    typedef double vd __attribute__((vector_size(W * sizeof(double))));
+    typedef ORC_FAST_T real;
+    typedef real       vd __attribute__((vector_size(W * sizeof(real))));
 
     inline vd
-    splat(double x)
+    splat(real x)
     {
       vd r;
       for (int l = 0; l < W; ++l)
@@ -63,8 +72,8 @@ namespace orc
     {
       static constexpr int H  = N / 2;
       static constexpr int HR = (N + 1) / 2;
-      double               e[HR][HR]; // even part; column H holds the middle column (N odd)
-      double               o[HR][H > 0 ? H : 1];
+      real                 e[HR][HR]; // even part; column H holds the middle column (N odd)
+      real                 o[HR][H > 0 ? H : 1];
 
       void
       set(const double *M)
@@ -151,7 +160,7 @@ namespace orc
     {
       EvenOdd<N, 1>  S, St;           // nodes -> Gauss points, and transpose
       EvenOdd<N, -1> D[3], Dt[3];     // collocation derivative / h_d, and transpose
-      double         jxw[N * N * N];  // quadrature weight times cell volume
+      real           jxw[N * N * N];  // quadrature weight times cell volume
 
       Shape(const Basis1D &b, const Box &box)
       {
@@ -232,7 +241,7 @@ namespace orc
       Fi[7] = F[1] * F[6] - F[0] * F[7];
       Fi[8] = F[0] * F[4] - F[1] * F[3];
       J          = F[0] * Fi[0] + F[1] * Fi[3] + F[2] * Fi[6];
-      const vd r = splat(1.0) / J;
+      const vd r = splat(real(1)) / J;
       for (int i = 0; i < 9; ++i)
         Fi[i] *= r;
     }
@@ -301,7 +310,7 @@ namespace orc
 
       // read the NC components of the batch's cells into lane-interleaved form
       void
-      gather(size_t bt, const double *src, vd *u, bool constrained) const
+      gather(size_t bt, const real *src, vd *u, bool constrained) const
       {
         const size_t plane = size_t(box.Nn[0]) * box.Nn[1];
         for (int l = 0; l < W; ++l)
@@ -310,7 +319,7 @@ namespace orc
             const size_t g0 = first_node(e);
             for (int c = 0; c < NC; ++c)
               {
-                const double *s = src + size_t(c) * box.n_nodes + g0;
+                const real   *s = src + size_t(c) * box.n_nodes + g0;
                 vd           *o = u + c * Nd;
                 for (int k = 0; k < N; ++k)
                   for (int j = 0; j < N; ++j)
@@ -330,7 +339,7 @@ namespace orc
       }
 
       void
-      scatter(size_t bt, const vd *out, double *dst) const
+      scatter(size_t bt, const vd *out, real *dst) const
       {
         const size_t plane = size_t(box.Nn[0]) * box.Nn[1];
         for (int l = 0; l < lanes[bt]; ++l)
@@ -349,7 +358,7 @@ namespace orc
               }
             for (int c = 0; c < NC; ++c)
               {
-                double   *d = dst + size_t(c) * box.n_nodes + g0;
+                real     *d = dst + size_t(c) * box.n_nodes + g0;
                 const vd *o = out + c * Nd;
                 for (int k = 0; k < N; ++k)
                   for (int j = 0; j < N; ++j)
@@ -361,10 +370,11 @@ namespace orc
 
       // dst = A src with A given cell batch by cell batch: dst zeroed, the
       // colours in turn (the loop's closing barrier orders them), then the
-      // identity on the constrained rows.  apply(bt, scratch) handles a batch.
+      // identity on the constrained rows (skipped when src is null).
+      // apply(bt, scratch) handles a batch.
       template <typename Apply>
       void
-      run(double *dst, const double *src, size_t scratch, const Apply &apply) const
+      run(real *dst, const real *src, size_t scratch, const Apply &apply) const
       {
         const size_t n = size_t(NC) * box.n_nodes;
 #pragma omp parallel
@@ -382,9 +392,12 @@ namespace orc
                 apply(size_t(bl), w.data());
               b0 = b1;
             }
+          if (src)
+            {
 #pragma omp for schedule(static)
-          for (long i = 0; i < long(constrained_rows.size()); ++i)
-            dst[constrained_rows[i]] += src[constrained_rows[i]];
+              for (long i = 0; i < long(constrained_rows.size()); ++i)
+                dst[constrained_rows[i]] += src[constrained_rows[i]];
+            }
         }
       }
     };
@@ -425,7 +438,7 @@ namespace orc
       // NeoHookOperator::cache (mf_nh_operator.h:394-523), from the
       // linearisation u read without constraints
       bool
-      cache(const double *u)
+      cache(const real *u)
       {
         const size_t nb = cb.cells.size();
         if (caching == tensor4_ns)
@@ -523,7 +536,7 @@ namespace orc
 
       // dst = A src (cell part + constrained identity), dst zeroed here
       void
-      vmult(double *dst, const double *src) const
+      vmult(real *dst, const real *src) const
       {
         cb.run(dst, src, 32 * Nd, [&](size_t bt, vd *w) {
           vd *u = w, *val = u + 3 * Nd, *g = val + 3 * Nd, *gu = g + 9 * Nd, *t0 = gu + 9 * Nd, *t1 = t0 + Nd,
@@ -533,10 +546,40 @@ namespace orc
       }
 
       void
-      apply_batch(size_t bt, const double *src, double *dst, vd *u, vd *val, vd *g, vd *gu, vd *t0, vd *t1,
+      apply_batch(size_t bt, const real *src, real *dst, vd *u, vd *val, vd *g, vd *gu, vd *t0, vd *t1,
                   vd *t2, vd *out) const
       {
         cb.gather(bt, src, u, true);
+        cell_op(bt, u, val, g, gu, t0, t1, t2, out);
+        cb.scatter(bt, out, dst);
+      }
+
+      // diagonal of the cell part (MatrixFreeTools::compute_diagonal,
+      // mf_nh_operator.h:1025-1060): every local unit vector of a batch
+      // through the cell operator; the constrained rows stay zero
+      void
+      cell_diagonal(real *diag) const
+      {
+        cb.run(diag, nullptr, 36 * Nd, [&](size_t bt, vd *w) {
+          vd *u = w, *val = u + 3 * Nd, *g = val + 3 * Nd, *gu = g + 9 * Nd, *t0 = gu + 9 * Nd, *t1 = t0 + Nd,
+             *t2 = t1 + Nd, *out = t2 + Nd, *dg = out + 3 * Nd;
+          for (int i = 0; i < 3 * Nd; ++i)
+            u[i] = splat(real(0));
+          for (int i = 0; i < 3 * Nd; ++i)
+            {
+              u[i] = splat(real(1));
+              cell_op(bt, u, val, g, gu, t0, t1, t2, out);
+              dg[i] = out[i];
+              u[i] = splat(real(0));
+            }
+          cb.scatter(bt, dg, diag);
+        });
+      }
+
+      // the cell operator of batch bt on its 3-component values u, into out
+      void
+      cell_op(size_t bt, const vd *u, vd *val, vd *g, vd *gu, vd *t0, vd *t1, vd *t2, vd *out) const
+      {
         for (int c = 0; c < 3; ++c)
           sh.evaluate(u + c * Nd, val + c * Nd, g + (3 * c) * Nd, g + (3 * c + 1) * Nd, g + (3 * c + 2) * Nd, t0,
                       t1);
@@ -572,7 +615,7 @@ namespace orc
                     const vd sc = x[19], tmp = lam2 * x[20] * (gg[0] + gg[4] + gg[8]);
                     for (int i = 0; i < 3; ++i)
                       for (int j = 0; j < 3; ++j)
-                        Pc[i * 3 + j] += sc * 0.5 * (gg[i * 3 + j] + gg[j * 3 + i]);
+                        Pc[i * 3 + j] += sc * real(0.5) * (gg[i * 3 + j] + gg[j * 3 + i]);
                     Pc[0] += tmp;
                     Pc[4] += tmp;
                     Pc[8] += tmp;
@@ -623,9 +666,9 @@ namespace orc
                 vd F[9], Fi[9], J, tau[9], gg[9], q9[9];
                 for (int i = 0; i < 9; ++i)
                   F[i] = gu[i * Nd + q];
-                F[0] += 1.0;
-                F[4] += 1.0;
-                F[8] += 1.0;
+                F[0] += real(1);
+                F[4] += real(1);
+                F[8] += real(1);
                 const vd c = cscal[bt * Nd + q];
                 for (int i = 0; i < 3; ++i)
                   for (int j = 0; j < 3; ++j)
@@ -659,7 +702,6 @@ namespace orc
           }
         for (int c = 0; c < 3; ++c)
           sh.integrate(val + c * Nd, g + (3 * c) * Nd, g + (3 * c + 1) * Nd, g + (3 * c + 2) * Nd, out + c * Nd, t0);
-        cb.scatter(bt, out, dst);
       }
     };
 
@@ -680,30 +722,80 @@ namespace orc
       {}
 
       void
-      vmult(double *dst, const double *src) const
+      vmult(real *dst, const real *src) const
       {
         cb.run(dst, src, 8 * Nd, [&](size_t bt, vd *w) {
-          vd *u = w, *val = u + Nd, *gx = val + Nd, *gy = gx + Nd, *gz = gy + Nd, *t0 = gz + Nd, *t1 = t0 + Nd,
-             *out = t1 + Nd;
-          cb.gather(bt, src, u, true);
-          sh.evaluate(u, val, gx, gy, gz, t0, t1);
-          for (int q = 0; q < Nd; ++q)
-            {
-              const vd jw = splat(sh.jxw[q]), kj = splat(kdt * sh.jxw[q]);
-              val[q] *= jw;
-              gx[q] *= kj;
-              gy[q] *= kj;
-              gz[q] *= kj;
-            }
-          sh.integrate(val, gx, gy, gz, out, t0);
-          cb.scatter(bt, out, dst);
+          cb.gather(bt, src, w, true);
+          cell_op(w, w + Nd, w + 7 * Nd);
+          cb.scatter(bt, w + 7 * Nd, dst);
         });
+      }
+
+      // diagonal of the cell part (heat_transfer.h:205-230), constrained
+      // rows zero
+      void
+      cell_diagonal(real *diag) const
+      {
+        cb.run(diag, nullptr, 10 * Nd, [&](size_t bt, vd *w) {
+          vd *u = w, *out = w + 7 * Nd, *dg = out + Nd;
+          for (int i = 0; i < Nd; ++i)
+            u[i] = splat(real(0));
+          for (int i = 0; i < Nd; ++i)
+            {
+              u[i] = splat(real(1));
+              cell_op(u, w + Nd, out);
+              dg[i] = out[i];
+              u[i] = splat(real(0));
+            }
+          cb.scatter(bt, dg, diag);
+        });
+      }
+
+      // cell operator on values u into out; s holds 6 Nd of scratch
+      void
+      cell_op(const vd *u, vd *s, vd *out) const
+      {
+        vd *val = s, *gx = val + Nd, *gy = gx + Nd, *gz = gy + Nd, *t0 = gz + Nd, *t1 = t0 + Nd;
+        sh.evaluate(u, val, gx, gy, gz, t0, t1);
+        for (int q = 0; q < Nd; ++q)
+          {
+            const vd jw = splat(sh.jxw[q]), kj = splat(kdt * sh.jxw[q]);
+            val[q] *= jw;
+            gx[q] *= kj;
+            gy[q] *= kj;
+            gz[q] *= kj;
+          }
+        sh.integrate(val, gx, gy, gz, out, t0);
       }
     };
 
+    // level operators for a driver (oracle_solvers.hpp LevelOp::fast)
+    template <int N>
+    FastLevel<real>
+    make_nh_level(const Box &box, const Basis1D &b, const Material &mat, Caching caching, const real *u, bool &ok)
+    {
+      auto            op = std::make_shared<NHFast<N>>(box, b, mat, caching);
+      FastLevel<real> f;
+      ok              = op->cache(u);
+      f.vmult         = [op](real *d, const real *s) { op->vmult(d, s); };
+      f.cell_diagonal = [op](real *d) { op->cell_diagonal(d); };
+      return f;
+    }
+
+    template <int N>
+    FastLevel<real>
+    make_heat_level(const Box &box, const Basis1D &b, double k_dt)
+    {
+      auto            op = std::make_shared<HeatFast<N>>(box, b, k_dt);
+      FastLevel<real> f;
+      f.vmult         = [op](real *d, const real *s) { op->vmult(d, s); };
+      f.cell_diagonal = [op](real *d) { op->cell_diagonal(d); };
+      return f;
+    }
+
     template <int N>
     int
-    heat_vmult_timed(const Box &box, const Basis1D &b, double k_dt, const double *src, double *dst, int reps,
+    heat_vmult_timed(const Box &box, const Basis1D &b, double k_dt, const real *src, real *dst, int reps,
                      double *seconds)
     {
       HeatFast<N> op(box, b, k_dt);
@@ -719,8 +811,8 @@ namespace orc
     // applications; returns 0, -2 (unsupported), -3 (det F <= 0)
     template <int N>
     int
-    nh_vmult_timed(const Box &box, const Basis1D &b, const Material &mat, Caching caching, const double *u,
-                   const double *src, double *dst, int reps, double *seconds)
+    nh_vmult_timed(const Box &box, const Basis1D &b, const Material &mat, Caching caching, const real *u,
+                   const real *src, real *dst, int reps, double *seconds)
     {
       NHFast<N> op(box, b, mat, caching);
       if (!op.cache(u))

@@ -22,8 +22,20 @@
 
 #include "oracle_core.hpp"
 
+#include <functional>
+
 namespace orc
 {
+  // a level operator in the throughput form (oracle_fast.hpp), as a driver
+  // holds it: vmult = A with the constrained identity; cell_diagonal = the
+  // cell part of diag(A), constrained rows left zero
+  template <typename T>
+  struct FastLevel
+  {
+    std::function<void(T *, const T *)> vmult;
+    std::function<void(T *)>            cell_diagonal;
+  };
+
   struct Material
   {
     double mu = 0, nu = 0, rho = 0, alpha_1 = 0;

@@ -9,6 +9,7 @@
 // Dirichlet data.
 #pragma once
 
+#include "oracle_fast_api.hpp"
 #include "oracle_solvers.hpp"
 
 namespace orc
@@ -84,6 +85,7 @@ namespace orc
     int      cheb_eig_its   = 30;
     int      coarse_accurate = 1;
     int      mg_float       = 1; // level operators in FP32 (reference)
+    int      fast           = 0; // operators in the throughput form (oracle_fast.hpp)
   };
 
   struct SolidResult
@@ -300,7 +302,14 @@ namespace orc
     void
     update_operators(const std::vector<double> &u)
     {
-      nh_cache(fine.nh, fine.box, basis, u.data());
+      if (P.fast)
+        {
+          bool ok = true;
+          fine.fast = make_fast_nh(fine.box, basis, P.mat, Caching(P.caching), u.data(), ok);
+          fine.nh.positive_J = ok;
+        }
+      else
+        nh_cache(fine.nh, fine.box, basis, u.data());
       if (P.precond == 1)
         fine.compute_diagonal();
       if (P.precond != 2)
@@ -317,7 +326,13 @@ namespace orc
         }
       for (int l = 0; l <= L; ++l)
         {
-          nh_cache(lops[l].nh, lops[l].box, basis, u_levels[l].data());
+          if (P.fast)
+            {
+              bool ok = true;
+              lops[l].fast = make_fast_nh(lops[l].box, basis, P.mat, Caching(P.caching), u_levels[l].data(), ok);
+            }
+          else
+            nh_cache(lops[l].nh, lops[l].box, basis, u_levels[l].data());
           lops[l].compute_diagonal();
         }
       mg.setup(P.cheb_range, P.cheb_degree, P.cheb_eig_its,
@@ -457,6 +472,7 @@ namespace orc
     double   g_width[8]{};
     double   g_amp[8]{};
     int      mg_float = 1;
+    int      fast     = 0; // operators in the throughput form (oracle_fast.hpp)
   };
 
   struct HeatResult
@@ -513,6 +529,12 @@ namespace orc
                 mg.transfers.emplace_back(
                   new LevelTransfer<LT>(basis, lops[l - 1].box, lops[l].box, 1));
             }
+        }
+      if (P.fast)
+        {
+          op.fast = make_fast_heat<double>(op.box, basis, P.dt);
+          for (auto &lo : lops)
+            lo.fast = make_fast_heat<LT>(lo.box, basis, P.dt);
         }
     }
 

@@ -63,6 +63,9 @@ namespace orc
     bool           constrained = true;
     NHState<T>     nh;
     std::vector<T> inv_diag;
+    // when set, the throughput form (oracle_fast.hpp) applies the operator
+    // and its cell diagonal in place of the loops below
+    FastLevel<T>   fast;
 
     size_t
     m() const
@@ -73,6 +76,11 @@ namespace orc
     void
     vmult(T *dst, const T *src)
     {
+      if (fast.vmult && constrained)
+        {
+          fast.vmult(dst, src);
+          return;
+        }
       std::fill(dst, dst + m(), T(0));
       vmult_add(dst, src);
     }
@@ -80,6 +88,14 @@ namespace orc
     void
     vmult_add(T *dst, const T *src)
     {
+      if (fast.vmult && constrained)
+        {
+          std::vector<T> t(m());
+          fast.vmult(t.data(), src);
+          for (size_t i = 0; i < m(); ++i)
+            dst[i] += t[i];
+          return;
+        }
       if (kind == op_heat)
         {
           HeatQ<T> q{box.dim, k_dt};
@@ -99,7 +115,9 @@ namespace orc
     compute_diagonal()
     {
       std::vector<T> diag(m(), T(0));
-      if (kind == op_heat)
+      if (fast.cell_diagonal)
+        fast.cell_diagonal(diag.data());
+      else if (kind == op_heat)
         {
           HeatQ<T> q{box.dim, k_dt};
           cell_diagonal(box, *basis, nc, diag.data(), q);
@@ -185,6 +203,7 @@ namespace orc
     (void)Kout;
     if (!transposed)
       {
+#pragma omp parallel for collapse(2) schedule(static)
         for (int o = 0; o < outer; ++o)
           for (int s = 0; s < stride; ++s)
             for (int r = 0; r < rows; ++r)
@@ -203,6 +222,8 @@ namespace orc
         int ncols = 0;
         for (int r = 0; r < rows; ++r)
           ncols = std::max(ncols, col[r] + p + 1);
+        // each (o, s) line is written by one thread
+#pragma omp parallel for collapse(2) schedule(static)
         for (int o = 0; o < outer; ++o)
           for (int s = 0; s < stride; ++s)
             for (int r = 0; r < rows; ++r)
@@ -243,6 +264,7 @@ namespace orc
         {
           a.assign(coarse_v + size_t(c) * coarse->n_nodes,
                    coarse_v + size_t(c + 1) * coarse->n_nodes);
+#pragma omp parallel for schedule(static)
           for (size_t g = 0; g < coarse->n_nodes; ++g)
             if (coarse->constrained(g, c))
               a[g] = T(0);
@@ -257,6 +279,7 @@ namespace orc
               a.swap(bbuf);
               ext[d] = ext_out[d];
             }
+#pragma omp parallel for schedule(static)
           for (size_t g = 0; g < fine->n_nodes; ++g)
             fine_v[size_t(c) * fine->n_nodes + g] =
               fine->constrained(g, c) ? T(0) : a[g];
@@ -274,6 +297,7 @@ namespace orc
         {
           a.assign(fine_v + size_t(c) * fine->n_nodes,
                    fine_v + size_t(c + 1) * fine->n_nodes);
+#pragma omp parallel for schedule(static)
           for (size_t g = 0; g < fine->n_nodes; ++g)
             if (fine->constrained(g, c))
               a[g] = T(0);
@@ -288,6 +312,7 @@ namespace orc
               a.swap(bbuf);
               ext[d] = ext_out[d];
             }
+#pragma omp parallel for schedule(static)
           for (size_t g = 0; g < coarse->n_nodes; ++g)
             if (!coarse->constrained(g, c))
               coarse_v[size_t(c) * coarse->n_nodes + g] += a[g];
@@ -389,6 +414,7 @@ namespace orc
     CGResult       R;
     std::vector<T> r(n), z(n), p(n), q(n);
     A(q.data(), x);
+#pragma omp parallel for schedule(static)
     for (size_t i = 0; i < n; ++i)
       r[i] = b[i] - q[i];
     double res = norm(n, r.data());
@@ -407,6 +433,7 @@ namespace orc
         A(q.data(), p.data());
         const double pq    = dot(n, p.data(), q.data());
         const double alpha = rz / pq;
+#pragma omp parallel for schedule(static)
         for (size_t i = 0; i < n; ++i)
           {
             x[i] += T(alpha) * p[i];
@@ -430,6 +457,7 @@ namespace orc
         const double rz_new = dot(n, r.data(), z.data());
         const double beta   = rz_new / rz;
         rz                  = rz_new;
+#pragma omp parallel for schedule(static)
         for (size_t i = 0; i < n; ++i)
           p[i] = z[i] + T(beta) * p[i];
         alpha_old = alpha;
@@ -468,6 +496,7 @@ namespace orc
         rhs[i] -= T(mean);
       auto Aop = [&](T *d, const T *s) { A->vmult(d, s); };
       auto Pop = [&](T *d, const T *s) {
+#pragma omp parallel for schedule(static)
         for (size_t i = 0; i < n; ++i)
           d[i] = A->inv_diag[i] * s[i];
       };
@@ -507,6 +536,7 @@ namespace orc
     update(const T *b, T *x, double f1, double f2, bool first)
     {
       const size_t n = A->m();
+#pragma omp parallel for schedule(static)
       for (size_t i = 0; i < n; ++i)
         {
           const T t  = A->inv_diag[i] * (b[i] - t1[i]);
@@ -524,6 +554,7 @@ namespace orc
       if (!initialized)
         estimate();
       const size_t n = A->m();
+#pragma omp parallel for schedule(static)
       for (size_t i = 0; i < n; ++i)
         {
           x[i]     = T(1. / theta) * A->inv_diag[i] * b[i];
@@ -616,6 +647,7 @@ namespace orc
       const size_t n = ops[l]->m();
       smoothers[l].vmult(sol[l].data(), def[l].data());
       ops[l]->vmult(tmp[l].data(), sol[l].data());
+#pragma omp parallel for schedule(static)
       for (size_t i = 0; i < n; ++i)
         tmp[l][i] = def[l][i] - tmp[l][i];
       std::fill(def[l - 1].begin(), def[l - 1].end(), T(0));
@@ -623,6 +655,7 @@ namespace orc
       std::fill(sol[l - 1].begin(), sol[l - 1].end(), T(0));
       level_v_step(l - 1);
       transfers[l]->prolongate(tmp[l].data(), sol[l - 1].data());
+#pragma omp parallel for schedule(static)
       for (size_t i = 0; i < n; ++i)
         sol[l][i] += tmp[l][i];
       smoothers[l].step(sol[l].data(), def[l].data());

@@ -59,3 +59,53 @@ def test_fast_heat_matches_oracle(degree, lanes):
         got, secs = O.heat_vmult_fast_timed(om, n_ref, 0.1, x, 2, lanes=lanes)
         assert rel(got, ref) < 1e-13, (n_ref, rel(got, ref))
         assert secs > 0.0
+
+
+def _solid_params(spec, caching, mg_float, fast):
+    p = O.SolidParams()
+    p.mesh = W.to_oracle_mesh(O, spec)
+    p.mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+    p.caching = O.CACHING[caching]
+    p.precond, p.dt, p.n_steps, p.max_newton, p.max_it_mult = 2, 0.01, 1, 10, 1
+    p.relaxation, p.tol_lin = 0.65, 1e-8
+    p.traction_id = W.TRACTION_ID
+    p.traction[:] = [0.0, -100.0, 0.0]
+    p.cheb_degree, p.cheb_range, p.cheb_eig_its, p.coarse_accurate = 5, 20.0, 30, 1
+    p.mg_float, p.fast = mg_float, fast
+    return p
+
+
+@pytest.mark.parametrize("degree,n_ref", [(1, 2), (2, 1), (3, 1)])
+@pytest.mark.parametrize("caching", ["scalar_referential", "tensor2", "tensor4", "tensor4_ns"])
+@pytest.mark.parametrize("mg_float", [1, 0])
+def test_fast_first_solve_matches_plain(degree, n_ref, caching, mg_float):
+    """The GMG-CG solve of the first Newton system (mf_elasticity.h:1983-2070)
+    with every operator, level operator and diagonal in the throughput form
+    takes the same CG iterations as with the oracle's loops and gives the
+    same update (FP64 levels to round-off, FP32 levels to FP32 round-off
+    amplified by the solve)."""
+    spec = W.cantilever(degree, n_ref)
+    a = O.solid_first_solve(_solid_params(spec, caching, mg_float, 0), 1e-8)
+    b = O.solid_first_solve(_solid_params(spec, caching, mg_float, 1), 1e-8)
+    assert a[0] == b[0]
+    assert rel(b[3], a[3]) < (1e-12 if mg_float == 0 else 1e-10)
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3])
+def test_fast_heat_step_matches_plain(degree):
+    c, w, a = W.gaussian_source(0)
+    res = []
+    for fast in (0, 1):
+        p = O.HeatParams()
+        p.mesh = W.to_oracle_mesh(O, W.unit_cube_heat(degree, 2))
+        p.dt, p.n_steps, p.tol_rel, p.precond, p.mg_float, p.fast = 0.1, 2, 1e-10, 2, 1, fast
+        p.n_gauss = 8
+        for i in range(8):
+            for d in range(3):
+                p.g_center[i][d] = c[i, d]
+            p.g_width[i] = w[i]
+            p.g_amp[i] = a[i]
+        res.append(O.heat_run(p, return_u=True))
+    (ra, ua), (rb, ub) = res
+    assert list(ra.cg_its[:2]) == list(rb.cg_its[:2])
+    assert rel(ub, ua) < 1e-10
