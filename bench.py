@@ -312,6 +312,35 @@ def cpu_mixed_solve():
     return out
 
 
+def cpu_solid_first_step():
+    """The first Newmark step of the 64x8x8-cell Q4 cantilever (839,619
+    DoFs, traction (0,-100,0) on x = 8, Newton to 1e-9 / 1e-6, GMG-CG to
+    1e-6 with an FP32 V-cycle) on the host cores, every operator in the
+    cell-batched form (tensor2 caching)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import workloads as W
+    spec = W.cantilever(4, 3)
+    p = O.SolidParams()
+    p.mesh = W.to_oracle_mesh(O, spec)
+    p.mat = O.material(0.5e6, 0.4, 1000.0, 0.01)
+    p.caching = O.CACHING["tensor2"]
+    p.precond = 2
+    p.relaxation, p.tol_lin, p.max_it_mult, p.max_newton = 0.65, 1e-6, 1, 10
+    p.tol_f, p.tol_f_abs, p.tol_u, p.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+    p.dt, p.n_steps = 0.01, 1
+    p.traction_id = W.TRACTION_ID
+    p.traction[:] = [0.0, -100.0, 0.0]
+    p.watch[:] = [8.0, 0.5, 0.5]
+    p.cheb_degree, p.cheb_range, p.cheb_eig_its, p.coarse_accurate = 5, 20.0, 30, 1
+    p.mg_float, p.fast = 1, 1
+    r = O.solid_run(p)
+    return {"workload": "cantilever 64x8x8 cells Q4, 839,619 DoFs, first Newmark step",
+            "form": "cell-batched, tensor2", "newton_its": int(r.newton_its[0]),
+            "cg_iterations": int(r.total_cg), "linear_solves": int(r.n_solves), "seconds": r.seconds,
+            "watch_displacement": list(r.watch_disp[0][:3])}
+
+
 def cpu_heat_sweep(reps=3):
     """The degree sweep's heat operator (unit cube, 64^3 cells, Q1..Q6, FP64)
     on the host cores in the cell-batched form, the fastest of 2, 4 and 8
@@ -405,6 +434,39 @@ def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
     out["speedup_mixed_df64_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle_df64"]["solve_s"]
     out["note"] = ("mixed: FP64 outer CG + FP32 V-cycle + FP64 coarse solve; _df64: the FP64 operators "
                    "(fine level, coarse level) in double-float arithmetic")
+    return out
+
+
+def _config1_solid_params(mfgpu, W, n_steps):
+    spec = W.cantilever(4, 3)
+    p = mfgpu.SolidParams()
+    p.mesh = W.to_lib_mesh(mfgpu, spec)
+    p.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+    p.caching = b"referential_qp"
+    p.solver = mfgpu.solver_params("gmg", tol=1e-6, mg_precision=32)
+    p.max_newton = 10
+    p.tol_f, p.tol_f_abs, p.tol_u, p.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+    p.dt, p.n_steps = 0.01, n_steps
+    p.traction_id = W.TRACTION_ID
+    p.traction[:] = [0.0, -100.0, 0.0]
+    p.watch[:] = [8.0, 0.5, 0.5]
+    return p
+
+
+def extra_solid_newton(mfgpu, W, ctx):
+    """The 64x8x8-cell Q4 cantilever (839,619 DoFs): Newmark steps of
+    dt = 0.01 under the traction (0,-100,0) on x = 8, Newton to 1e-9
+    (residual) and 1e-6 (update), each system by GMG-CG to 1e-6 (FP32
+    V-cycle, native FP64 fine operator): the first step alone and five
+    steps, each from rest on a fresh solver."""
+    out = {"workload": "cantilever 64x8x8 cells Q4, 839,619 DoFs, Newton-Newmark"}
+    for key, steps in (("first_step", 1), ("five_steps", 5)):
+        s = mfgpu.Solid(ctx, _config1_solid_params(mfgpu, W, steps))
+        r = s.run()
+        s.close()
+        out[key] = {"newton_its": list(r.newton_its[:steps]), "cg_iterations": int(r.total_cg),
+                    "linear_solves": int(r.n_solves), "seconds": r.seconds,
+                    "watch_displacement": list(r.watch_disp[steps - 1][:3])}
     return out
 
 
@@ -825,6 +887,7 @@ def main():
         extras = {}
         for key, fn in (("time_to_solve_1e-8", lambda: extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev)),
                         ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
+                        ("solid_newton_64x8x8_q4", lambda: extra_solid_newton(mfgpu, W, ctx)),
                         ("design_choices", lambda: extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush,
                                                                          mesh, u, src, n, op, src_np, dst_np)),
                         ("degree_sweep_heat_64cube", lambda: extra_degree_sweep(torch, mfgpu, W, ctx, dev,
@@ -849,7 +912,8 @@ def main():
             line["cpu_baseline"]["heat_step_16cube_q2"] = {"error": str(e)}
         if not args.no_extras:
             for key, fn in (("heat_vmult_64cube_dofs_per_s", cpu_heat_sweep),
-                            ("time_to_solve_1e-8", cpu_mixed_solve)):
+                            ("time_to_solve_1e-8", cpu_mixed_solve),
+                            ("solid_newton_first_step", cpu_solid_first_step)):
                 try:
                     line["cpu_baseline"][key] = fn()
                 except Exception as e:
