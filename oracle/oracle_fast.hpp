@@ -1,9 +1,9 @@
 // CPU ORACLE — TEST INFRASTRUCTURE ONLY (see oracle_core.hpp).
 //
-// Throughput form of the neo-Hookean tangent vmult and of the heat operator
-// for the timed CPU baseline.  It restates how the reference's CPU path is executed by deal.II
-// rather than the plain loops of oracle_ops.hpp, so that the baseline is not
-// slowed by the oracle's generality:
+// Throughput form of the neo-Hookean tangent and of the heat operator for
+// the timed CPU baseline.  It restates how deal.II executes the reference's
+// CPU path, rather than the plain loops of oracle_ops.hpp, so that the
+// baseline is not slowed by the oracle's generality:
 //   * cells are processed in batches of W lanes, one cell per lane, as
 //     deal.II's VectorizedArray<double> does (FEEvaluation over a cell batch,
 //     NeoHookOperator::local_apply_cell, mf_nh_operator.h:631-647); the lanes
@@ -23,9 +23,14 @@
 //     SymmetricTensor<4,3>) and tensor4_ns (:996-1010);
 //   * cells are coloured by parity (cells of one colour share no DoF), so
 //     threads scatter without atomics; constrained DoFs read as zero and are
-//     skipped on the scatter, and the constrained rows get dst += src.
-// Results equal the oracle's vmult to round-off (tests/test_oracle_fast.py).
-// oracle_fast.cpp instantiates this file once per lane count ORC_FAST_W.
+//     skipped on the scatter, and the constrained rows get dst += src;
+//   * diagonals apply every local unit vector of a batch to the cell
+//     operator (MatrixFreeTools::compute_diagonal), and make_*_level hands
+//     vmult and diagonal to the oracle's solvers (LevelOp::fast), in FP64 or,
+//     for the multigrid levels, FP32 lanes.
+// Results equal the oracle's to round-off (tests/test_oracle_fast.py).
+// oracle_fast.cpp instantiates this file once per lane count ORC_FAST_W and
+// scalar type ORC_FAST_T.
 #include "oracle_ops.hpp"
 
 #include <array>
