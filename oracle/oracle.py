@@ -210,32 +210,33 @@ def nh_vmult(mesh, level, mat, caching, u, src, precision=64):
     return dst
 
 
-def nh_vmult_timed(mesh, level, mat, caching, u, src, reps):
-    """(dst, seconds): the tangent cached once, then `reps` FP64 applications
-    timed without the cache."""
+def nh_vmult_timed(mesh, level, mat, caching, u, src, reps, warmup=1):
+    """(dst, seconds): the tangent cached once, `warmup` untimed FP64
+    applications, then `reps` applications timed without the cache."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     src = np.ascontiguousarray(src, dtype=np.float64)
     dst = np.zeros_like(src)
     secs = C.c_double()
     rc = lib().or_nh_vmult_timed(C.byref(mesh), level, C.byref(mat), CACHING.get(caching, caching),
-                                 _ptr(u), _ptr(src), _ptr(dst), int(reps), C.byref(secs))
+                                 _ptr(u), _ptr(src), _ptr(dst), int(warmup), int(reps), C.byref(secs))
     if rc != 0:
         raise RuntimeError(f"oracle nh_vmult_timed failed: {rc}")
     return dst, secs.value
 
 
-def nh_vmult_fast_timed(mesh, level, mat, caching, u, src, reps, lanes=8):
+def nh_vmult_fast_timed(mesh, level, mat, caching, u, src, reps, lanes=8, warmup=1):
     """(dst, seconds) of the throughput form of the FP64 tangent vmult
     (cell batches of `lanes` = 2, 4 or 8 cells across SIMD lanes, compile-time
     degree, even-odd collocation sweeps; 3D, n_q = p + 1, formulation 1, any
-    caching variant): cached once, applied once untimed, then `reps`
-    applications timed."""
+    caching variant): cached once, applied `warmup` times untimed, then
+    `reps` applications timed."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     src = np.ascontiguousarray(src, dtype=np.float64)
     dst = np.zeros_like(src)
     secs = C.c_double()
     rc = lib().or_nh_vmult_fast_timed(C.byref(mesh), level, C.byref(mat), CACHING.get(caching, caching),
-                                      int(lanes), _ptr(u), _ptr(src), _ptr(dst), int(reps), C.byref(secs))
+                                      int(lanes), _ptr(u), _ptr(src), _ptr(dst), int(warmup), int(reps),
+                                      C.byref(secs))
     if rc != 0:
         raise RuntimeError(f"oracle nh_vmult_fast_timed failed: {rc}")
     return dst, secs.value

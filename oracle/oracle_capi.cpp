@@ -216,7 +216,7 @@ extern "C"
   // applications, *seconds = their wall time (the cache excluded)
   int
   or_nh_vmult_timed(const or_mesh_t *m, int level, const or_material_t *mat, int caching, const double *u,
-                    const double *src, double *dst, int reps, double *seconds)
+                    const double *src, double *dst, int warmup, int reps, double *seconds)
   {
     MeshSpec        s = to_spec(m);
     Basis1D         b(s.degree, s.n_q);
@@ -237,7 +237,8 @@ extern "C"
       }
     if (!op.nh.positive_J)
       return -3;
-    op.vmult(dst, src); // first touch of the caches and vectors, not timed
+    for (int w = 0; w < std::max(warmup, 1); ++w)
+      op.vmult(dst, src); // first touch of the caches and vectors, not timed
     const auto t0 = std::chrono::steady_clock::now();
     for (int r = 0; r < reps; ++r)
       op.vmult(dst, src);
@@ -252,7 +253,8 @@ extern "C"
   // -3 when det F <= 0
   int
   or_nh_vmult_fast_timed(const or_mesh_t *m, int level, const or_material_t *mat, int caching, int lanes,
-                         const double *u, const double *src, double *dst, int reps, double *seconds)
+                         const double *u, const double *src, double *dst, int warmup, int reps,
+                         double *seconds)
   {
     MeshSpec s = to_spec(m);
     if (s.dim != 3 || s.n_q != s.degree + 1 || mat->formulation != 1 || caching < 0 || caching > 3)
@@ -264,9 +266,9 @@ extern "C"
       {
         switch (lanes)
           {
-            case 2: return nh_vmult_fast_timed_w2d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
-            case 4: return nh_vmult_fast_timed_w4d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
-            case 8: return nh_vmult_fast_timed_w8d(box, b, mt, Caching(caching), u, src, dst, reps, seconds);
+            case 2: return nh_vmult_fast_timed_w2d(box, b, mt, Caching(caching), u, src, dst, warmup, reps, seconds);
+            case 4: return nh_vmult_fast_timed_w4d(box, b, mt, Caching(caching), u, src, dst, warmup, reps, seconds);
+            case 8: return nh_vmult_fast_timed_w8d(box, b, mt, Caching(caching), u, src, dst, warmup, reps, seconds);
             default: return -2;
           }
       }

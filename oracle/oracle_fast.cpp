@@ -14,17 +14,18 @@ namespace orc
   using ORC_FAST_NS::real;
 
   int ORC_FAST_FN(nh_vmult_fast_timed_w)(const Box &box, const Basis1D &b, const Material &mat, Caching caching,
-                                         const real *u, const real *src, real *dst, int reps, double *seconds)
+                                         const real *u, const real *src, real *dst, int warmup, int reps,
+                                         double *seconds)
   {
     using namespace ORC_FAST_NS;
     switch (box.p)
       {
-        case 1: return nh_vmult_timed<2>(box, b, mat, caching, u, src, dst, reps, seconds);
-        case 2: return nh_vmult_timed<3>(box, b, mat, caching, u, src, dst, reps, seconds);
-        case 3: return nh_vmult_timed<4>(box, b, mat, caching, u, src, dst, reps, seconds);
-        case 4: return nh_vmult_timed<5>(box, b, mat, caching, u, src, dst, reps, seconds);
-        case 5: return nh_vmult_timed<6>(box, b, mat, caching, u, src, dst, reps, seconds);
-        case 6: return nh_vmult_timed<7>(box, b, mat, caching, u, src, dst, reps, seconds);
+        case 1: return nh_vmult_timed<2>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
+        case 2: return nh_vmult_timed<3>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
+        case 3: return nh_vmult_timed<4>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
+        case 4: return nh_vmult_timed<5>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
+        case 5: return nh_vmult_timed<6>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
+        case 6: return nh_vmult_timed<7>(box, b, mat, caching, u, src, dst, warmup, reps, seconds);
         default: return -2;
       }
   }

@@ -817,12 +817,13 @@ namespace orc
     template <int N>
     int
     nh_vmult_timed(const Box &box, const Basis1D &b, const Material &mat, Caching caching, const real *u,
-                   const real *src, real *dst, int reps, double *seconds)
+                   const real *src, real *dst, int warmup, int reps, double *seconds)
     {
       NHFast<N> op(box, b, mat, caching);
       if (!op.cache(u))
         return -3;
-      op.vmult(dst, src);
+      for (int w = 0; w < std::max(warmup, 1); ++w)
+        op.vmult(dst, src);
       const auto t0 = std::chrono::steady_clock::now();
       for (int r = 0; r < reps; ++r)
         op.vmult(dst, src);

@@ -10,7 +10,7 @@ namespace orc
 {
 #define ORC_FAST_DECL(sfx, T)                                                                                    \
   int nh_vmult_fast_timed_##sfx(const Box &box, const Basis1D &b, const Material &mat, Caching caching,         \
-                                const T *u, const T *src, T *dst, int reps, double *seconds);                   \
+                                const T *u, const T *src, T *dst, int warmup, int reps, double *seconds);       \
   int heat_vmult_fast_timed_##sfx(const Box &box, const Basis1D &b, double k_dt, const T *src, T *dst, int reps, \
                                   double *seconds);                                                             \
   FastLevel<T> make_fast_nh_##sfx(const Box &box, const Basis1D &b, const Material &mat, Caching caching,        \
