@@ -1,19 +1,22 @@
 """Benchmark of the matrix-free hot path on GB300.
 
-Headline workload (the BASELINE configuration the metric is quoted on):
-neo-Hookean tangent vmult, cantilever [0,8]x[0,1]^2, 8x1x1 coarse cells
-refined 3 times (64x8x8 = 4096 cells), Q4 vector elements with 5^3 Gauss
-points, 839,619 DoFs, FP64, linearised at a seeded smooth displacement;
-source vector U(-1,1) (seed 3).  A "step" is one operator application.
+Headline workload: neo-Hookean tangent vmult, cantilever [0,8]x[0,1]^2,
+8x1x1 coarse cells refined 3 times (64x8x8 = 4096 cells), Q4 vector
+elements with 5^3 Gauss points, 839,619 DoFs, native FP64 arithmetic,
+linearised at a seeded smooth displacement; source vector U(-1,1) (seed 3).
+A "step" is one operator application.
 
 Output: one JSON line (rank 0).  `value` is DoF/s of the device-resident
 vmult (L2 flushed before every timed application, CUDA events on the
 library's stream); `e2e` is the same metric through the C-ABI host-buffer
 call mfgpu_operator_vmult_host (host->device copy of the source and
-device->host copy of the result inside the timed region).
+device->host copy of the result inside the timed region).  The key `df64`
+reports the same operator in double-float arithmetic (FP32 pipe), with its
+own roofline and e2e figures.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--caching referential_qp|scalar_referential|...]
+                    [--arith native|df64] [--caching referential_qp|...]
+    python bench.py --kernel-case NAME --steps K   # one operator, for ncu
 """
 import argparse
 import json
@@ -38,12 +41,16 @@ WORKLOAD = dict(degree=4, n_ref=3, rep=(8, 1, 1), length=(8.0, 1.0, 1.0))
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=3000)
+    p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--caching", default="referential_qp")
-    p.add_argument("--arith", default="df64", choices=["native", "df64"],
-                   help="FP64 operator arithmetic: native FP64 or double-float on the FP32 pipe")
+    p.add_argument("--arith", default="native", choices=["native", "df64"],
+                   help="arithmetic of the headline FP64 operator: native FP64 (the reference's) or "
+                        "double-float on the FP32 pipe")
+    p.add_argument("--kernel-case", default=None, choices=sorted(KERNEL_CASES),
+                   help="apply one operator `--steps` times on its workload and exit (the cases the "
+                        "ncu summaries under profiles/ were taken on)")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -90,7 +97,9 @@ def algorithmic_flops(n_cells, n, nc=3, f_qp=250):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons, sampled every 100 ms from
+    start() to stop(); stop() keeps the samples read inside mark()ed windows
+    (the timed regions), or all of them when no window holds one."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -100,8 +109,9 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines = []
+        self.windows = []
 
-    def start(self):
+    def start(self, settle_s=1.0):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
@@ -111,28 +121,42 @@ class ClockSampler:
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        # nvidia-smi takes a moment to print its first sample
+        t0 = time.perf_counter()
+        while not self.lines and time.perf_counter() - t0 < settle_s:
+            time.sleep(0.02)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t0, t1):
+        self.windows.append((t0, t1))
 
     def stop(self):
         if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
+        time.sleep(0.15)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        inside = [ln for t, ln in self.lines if any(a <= t <= b + 0.1 for a, b in self.windows)]
+        scope = "timed regions" if inside else "whole run"
+        rows = inside or [ln for _, ln in self.lines]
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in rows:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[5:9]):
@@ -140,7 +164,89 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "power_w_max": max(power) if power else None,
+                "reasons": sorted(reasons), "samples": len(sm), "scope": scope,
+                "timed_window_s": sum(b - a for a, b in self.windows)}
+
+
+class NvmlSampler:
+    """SM clock, power and clock-event reasons read through NVML (ctypes on
+    libnvidia-ml.so.1, read-only queries) every 2 ms from start() to stop(),
+    so that even a timed region of a few milliseconds holds samples;
+    stop() keeps the samples inside the mark()ed windows.  Falls back to
+    nvidia-smi polling (ClockSampler) when NVML cannot be loaded."""
+
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
+
+    def __init__(self, device, torch_device=None):
+        import ctypes
+        self.C = ctypes
+        self.samples = []
+        self.windows = []
+        self.running = False
+        self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        uuid = None
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(torch_device).uuid)
+        except Exception:
+            uuid = None
+        ok = False
+        if uuid:
+            key = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            ok = self.nv.nvmlDeviceGetHandleByUUID(key.encode(), ctypes.byref(self.h)) == 0
+        if not ok and self.nv.nvmlDeviceGetHandleByIndex_v2(device, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        mx = ctypes.c_uint()
+        self.max_mhz = None
+        if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        self.get_reasons = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def _loop(self):
+        C = self.C
+        mhz, mw, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while self.running:
+            t = time.perf_counter()
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0:
+                p = mw.value if self.nv.nvmlDeviceGetPowerUsage(self.h, C.byref(mw)) == 0 else 0
+                r = rs.value if self.get_reasons(self.h, C.byref(rs)) == 0 else 0
+                self.samples.append((t, float(mhz.value), p / 1000.0, r))
+            time.sleep(0.002)
+
+    def start(self):
+        self.running = True
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def mark(self, t0, t1):
+        self.windows.append((t0, t1))
+
+    def stop(self):
+        self.running = False
+        self.t.join(timeout=2)
+        inside = [x for x in self.samples if any(a <= x[0] <= b for a, b in self.windows)]
+        rows = inside or self.samples
+        reasons = sorted({nm for _, _, _, r in rows for bit, nm in self.REASONS.items() if r & bit})
+        sm = [x[1] for x in rows]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                "sm_mhz_min": min(sm) if sm else None,
+                "power_w_max": max(x[2] for x in rows) if rows else None,
+                "reasons": reasons, "samples": len(sm),
+                "scope": "timed regions" if inside else "whole run", "source": "NVML, every 2 ms",
+                "timed_window_s": sum(b - a for a, b in self.windows)}
+
+
+def clock_sampler(device, torch_device=None):
+    try:
+        return NvmlSampler(device, torch_device)
+    except (OSError, AttributeError):
+        return ClockSampler(device)
 
 
 def measured_peak_hbm():
@@ -152,33 +258,52 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profile_pipes():
-    """FP32-pipe utilisation of the double-float cell kernel from the
-    committed ncu summary of this workload (None when absent)."""
-    path = os.path.join(ROOT, "profiles", "nh_vmult_q4_cantilever_ncu.txt")
+HEADLINE_PROFILE = {"native": "nh_vmult_q4_cantilever_native_fp64_ncu.txt",
+                    "df64": "nh_vmult_q4_cantilever_df64_ncu.txt"}
+
+
+def profile_summary(name):
+    """Figures of a committed ncu summary under profiles/ (None when absent):
+    pipe and DRAM fractions, and the DRAM bytes per launch."""
+    path = os.path.join(ROOT, "profiles", name)
     out = {}
     try:
         for line in open(path):
             for key in ("pipe_fma_pct", "issue_active_pct", "pipe_fp64_pct", "dram_throughput_pct_of_peak"):
                 if line.startswith(key + ":"):
-                    out[key] = float(line.split(":", 1)[1].split()[0]) / 100.0
+                    out[key[:-4] + "_frac"] = float(line.split(":", 1)[1].split()[0]) / 100.0
+            if line.startswith("traffic_bytes_per_launch:"):
+                out["traffic_bytes_per_launch"] = float(line.split(":", 1)[1])
+            if line.startswith("duration"):
+                out["ncu_duration"] = line.split(":", 1)[1].strip()
     except OSError:
         return None
     return out or None
 
 
-def profile_traffic():
-    """dram bytes per launch of the vmult cell kernel, from the committed
-    ncu summary of this workload (None when absent)."""
-    path = os.path.join(ROOT, "profiles", "nh_vmult_q4_cantilever_ncu.txt")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+def measured_fp64_peak(torch, dev):
+    """FP64 throughput of cuBLAS DGEMM (4096^3, best of 3) on this GPU, in
+    TFLOP/s: the measured FP64 roof of the native-FP64 operator."""
+    n = 4096
+    a = torch.rand(n, n, dtype=torch.float64, device=dev)
+    b = torch.rand(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    del a, b
+    return 2 * n ** 3 / best / 1e12
 
+
+# device solutions kept by the secondary measurements for the oracle's check
+SOLUTIONS = {}
+CPU_FLAGS = "g++ -O3 -fopenmp (portable: no -march/-mcpu=native)"
 
 CPU_CACHINGS = ("scalar_referential", "tensor2", "tensor4", "tensor4_ns")
 # the throughput form (oracle/oracle_fast.hpp): cell batches across SIMD
@@ -241,7 +366,8 @@ def cpu_baseline(spec, u, src, budget_s, threads=None):
     best = max(rates, key=rates.get)
     return {"value": rates[best], "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"{reps} applications per variant of the {len(src)}-DoF Q4 operator, cached once, "
-                      f"vmult timed alone, on {nthreads} threads; variants: each caching of the reference "
+                      f"vmult timed alone, on {nthreads} threads, built {CPU_FLAGS}; variants: each "
+                      f"caching of the reference "
                       f"in plain loops, and the cell-batched SIMD form (/simdW: W cells per batch); the "
                       f"fastest ({best}) is reported; all: " +
                       ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) + " MDoF/s"}
@@ -312,6 +438,18 @@ def cpu_mixed_solve():
         its, setup_s, solve_s, _ = O.solid_first_solve(p, 1e-8)
         out[name] = {"cg_iterations": its, "setup_s": setup_s, "solve_s": solve_s,
                      "setup_plus_solve_s": setup_s + solve_s}
+    # the device solutions (FP32 and FP64 V-cycles, to 1e-8) against the
+    # oracle's FP64-everywhere solve to 1e-12
+    dev_sol = SOLUTIONS.get("time_to_solve_1e-8")
+    if dev_sol:
+        p.mg_float = 0
+        _, _, _, du_ref = O.solid_first_solve(p, 1e-12)
+        out["device_error_vs_oracle_fp64"] = {
+            name: {"l2_rel": float(np.linalg.norm(du - du_ref) / np.linalg.norm(du_ref)),
+                   "max_rel": float(np.max(np.abs(du - du_ref)) / np.max(np.abs(du_ref)))}
+            for name, du in dev_sol.items()}
+        out["device_error_vs_oracle_fp64"]["oracle"] = (
+            "FP64 CG + FP64 V-cycle, cell-batched form, relative residual 1e-12")
     return out
 
 
@@ -410,6 +548,7 @@ def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
         p.traction[:] = [0.0, -100.0, 0.0]
         return p
 
+    out_solutions = SOLUTIONS.setdefault("time_to_solve_1e-8", {})
     ref_solver = mfgpu.Solid(ctx, params(64, False, 1e-12))
     ref_solver.residual(zero, zero, rhs)
     du_ref = torch.zeros_like(rhs)
@@ -430,13 +569,15 @@ def extra_mixed_precision_solve(torch, mfgpu, W, ctx, dev):
         total = time.perf_counter() - t0
         err = (du - du_ref)
         out[name] = {"cg_iterations": its, "solve_s": secs, "setup_plus_solve_s": total,
-                     "l2_rel_error_vs_fp64": float(err.norm() / du_ref.norm()),
-                     "max_rel_error_vs_fp64": float(err.abs().max() / du_ref.abs().max())}
+                     "l2_rel_error_vs_device_fp64_1e-12": float(err.norm() / du_ref.norm()),
+                     "max_rel_error_vs_device_fp64_1e-12": float(err.abs().max() / du_ref.abs().max())}
+        out_solutions[name] = du.cpu().numpy()
         s.close()
     out["speedup_mixed_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle"]["solve_s"]
     out["speedup_mixed_df64_vs_fp64"] = out["fp64_vcycle"]["solve_s"] / out["mixed_fp32_vcycle_df64"]["solve_s"]
     out["note"] = ("mixed: FP64 outer CG + FP32 V-cycle + FP64 coarse solve; _df64: the FP64 operators "
-                   "(fine level, coarse level) in double-float arithmetic")
+                   "(fine level, coarse level) in double-float arithmetic; the errors against the "
+                   "oracle's FP64-everywhere solve are in cpu_baseline.time_to_solve_1e-8")
     return out
 
 
@@ -522,7 +663,8 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
     return res
 
 
-def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src, n, op, src_np, dst_np):
+def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src, n, op, src_np, dst_np,
+                         arith="native"):
     """Measurements behind the kernel choices on the headline workload (Q4
     cantilever 64x8x8, 839,619 DoFs), L2 flushed before every application:
     * scatter: atomic adds vs 8 parity colours with plain adds;
@@ -534,7 +676,7 @@ def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src,
     for mode in ("atomic", "colored"):
         op.set_scatter(mode)
         t = _timed_vmults(torch, op, dst, src, flush, stream, 10)
-        out["scatter"]["nh_q4_df64_" + mode] = {"ms": t * 1e3, "dofs_per_s": n / t}
+        out["scatter"]["nh_q4_" + arith + "_" + mode] = {"ms": t * 1e3, "dofs_per_s": n / t}
     op.set_scatter("atomic")
     heat = W.unit_cube_heat(2, 6)
     hm = W.to_lib_mesh(mfgpu, heat)
@@ -717,7 +859,8 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{reps} applications per variant (each caching of the reference in "
                                        f"plain loops, and the cell-batched SIMD form /simdW), cached once, "
-                                       f"vmult timed alone, on {nthreads} threads; the fastest, {best}, then "
+                                       f"vmult timed alone, on {nthreads} threads, built {CPU_FLAGS}; the "
+                                       f"fastest, {best}, then "
                                        f"timed over {K} steps after {Wu} untimed; all: " +
                                        ", ".join(f"{c} {v / 1e6:.1f}" for c, v in rates.items()) +
                                        " MDoF/s (the reference itself needs deal.II/p4est/MPI, absent here)"},
@@ -726,10 +869,124 @@ def run_reference(args):
     return 0
 
 
+KERNEL_CASES = {
+    # name: (operator, degree, refinements, precision, arithmetic)
+    "nh_fp64_q4": ("nh", 4, 3, 64, "native"),   # the headline: 64x8x8 cells, 839,619 DoFs
+    "nh_df64_q4": ("nh", 4, 3, 64, "df64"),
+    "nh_fp32_q3": ("nh", 3, 4, 32, "native"),   # finest level of the mixed solve, 2,773,155 DoFs
+    "nh_fp32_q3_scalar_ref": ("nh_sr", 3, 4, 32, "native"),
+    "heat_fp32_q2": ("heat", 2, 6, 32, "native"),  # unit cube 64^3 cells
+    "heat_fp32_q6": ("heat", 6, 6, 32, "native"),
+    "heat_fp64_q2": ("heat", 2, 6, 64, "native"),
+}
+
+
+def run_kernel_case(args):
+    """One operator applied `--steps` times on its workload (for ncu)."""
+    import torch
+    import build as pkg_build
+    import mfgpu
+    import workloads as W
+    kind, deg, nref, prec, arith = KERNEL_CASES[args.kernel_case]
+    pkg_build.build()
+    dev = torch.device("cuda", 0)
+    ctx = mfgpu.Context(0)
+    dt = torch.float32 if prec == 32 else torch.float64
+    if kind.startswith("nh"):
+        spec = W.cantilever(deg, nref)
+        n = W.n_dofs(spec, 3)
+        u = torch.from_numpy(W.smooth_displacement(deg, nref, spec["rep"], spec["lo"], spec["hi"],
+                                                   seed=2)).to(dev).to(dt)
+        caching = "scalar_referential" if kind == "nh_sr" else "referential_qp"
+        op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, prec, caching)
+        op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01))
+        op.initialize(u)
+        if arith == "df64":
+            op.set_fp64_emulation(True)
+        op.cache()
+    else:
+        spec = W.unit_cube_heat(deg, nref)
+        n = W.n_dofs(spec, 1)
+        op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, prec, True, delta_t=0.1)
+    src = torch.from_numpy(W.uniform_vector(n, 3)).to(dev).to(dt)
+    dst = torch.zeros_like(src)
+    for _ in range(max(args.steps, 1)):
+        op.vmult(dst, src)
+    ctx.synchronize()
+    print(json.dumps({"kernel_case": args.kernel_case, "n_dofs": n, "vmults": max(args.steps, 1)}))
+    op.close()
+    ctx.close()
+    return 0
+
+
+def time_operator(torch, op, dst, src, flush, stream, K, warmup, clocks=None):
+    """K device-resident vmults (L2 flushed before each, CUDA events on the
+    library's stream) and K vmult_adds (the cell kernel and the constrained-
+    row add, the dominant launch): per-step ms, kernel ms, launches."""
+    import mfgpu
+    for _ in range(warmup):
+        op.vmult(dst, src)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    kends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    launches0 = mfgpu.launch_count()
+    t0 = time.perf_counter()
+    for i in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+        op.vmult(dst, src)
+        with torch.cuda.stream(stream):
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    launches = mfgpu.launch_count() - launches0
+    for i in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            kstarts[i].record(stream)
+        op.vmult_add(dst, src)
+        with torch.cuda.stream(stream):
+            kends[i].record(stream)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    if clocks is not None:
+        clocks.mark(t0, t2)
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / K
+    kms = sum(s.elapsed_time(e) for s, e in zip(kstarts, kends)) / K
+    return ms, kms, launches, t1 - t0
+
+
+def time_host_vmult(op, dst_np, src_np, K, warmup, clocks=None):
+    """K host-buffer vmults through the C-ABI (pinned source and result):
+    seconds per call, with the z-slab overlap and without it."""
+    for _ in range(warmup):
+        op.vmult_host(dst_np, src_np)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        op.vmult_host(dst_np, src_np)
+    t1 = time.perf_counter()
+    if clocks is not None:
+        clocks.mark(t0, t1)
+    op.set_host_chunks(1)
+    for _ in range(2):
+        op.vmult_host(dst_np, src_np)
+    t2 = time.perf_counter()
+    for _ in range(K):
+        op.vmult_host(dst_np, src_np)
+    serial = (time.perf_counter() - t2) / K
+    op.set_host_chunks(0)
+    return (t1 - t0) / K, serial
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return run_kernel_case(args)
     rank, world, local = dist_info()
     import torch
     import build as pkg_build
@@ -761,6 +1018,9 @@ def main():
     op.cache()
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 512 MB > L2
+    src_pin = torch.from_numpy(src_h).pin_memory()
+    dst_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+    src_np, dst_np = src_pin.numpy(), dst_pin.numpy()
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -768,98 +1028,62 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
-    # warm-up
-    for _ in range(max(args.warmup, 3)):
-        op.vmult(dst, src)
-    ctx.synchronize()
-
-    # timed: K device-resident vmults, L2 flushed before each (not timed)
     K = args.steps
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    kstarts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    kends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    clocks = ClockSampler(local)
-    barrier()
+    Wu = max(args.warmup, 3)
+    clocks = clock_sampler(local, dev)
     clocks.start()
-    launches0 = mfgpu.launch_count()
-    t_wall0 = time.perf_counter()
-    for i in range(K):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(i))
-            starts[i].record(stream)
-        op.vmult(dst, src)
-        with torch.cuda.stream(stream):
-            ends[i].record(stream)
     barrier()
-    t_wall = time.perf_counter() - t_wall0
-    launches = mfgpu.launch_count() - launches0
-    # dominant kernel alone: cell application (vmult_add = cell kernel +
-    # constrained-row add), also L2-flushed
-    for i in range(K):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(i))
-            kstarts[i].record(stream)
-        op.vmult_add(dst, src)
-        with torch.cuda.stream(stream):
-            kends[i].record(stream)
+    ms_step, k_ms, launches, t_wall = time_operator(torch, op, dst, src, flush, stream, K, Wu, clocks)
     barrier()
-    clk = clocks.stop()
-    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    kms = [s.elapsed_time(e) for s, e in zip(kstarts, kends)]
-    ms_step = sum(ms) / K
-    k_ms = sum(kms) / K
     ms_step = max_over_ranks(ms_step, world, dev)
     k_ms = max_over_ranks(k_ms, world, dev)
-
     # end to end through the C-ABI with host buffers (pinned)
-    src_pin = torch.from_numpy(src_h).pin_memory()
-    dst_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
-    src_np, dst_np = src_pin.numpy(), dst_pin.numpy()
-    for _ in range(max(args.warmup, 3)):
-        op.vmult_host(dst_np, src_np)
+    e2e_s, e2e_serial_s = time_host_vmult(op, dst_np, src_np, K, Wu, clocks)
     barrier()
-    t0 = time.perf_counter()
-    for _ in range(K):
-        op.vmult_host(dst_np, src_np)
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / K
     e2e_s = max_over_ranks(e2e_s, world, dev)
-    # the same without the z-slab overlap of copies and cells
-    op.set_host_chunks(1)
-    for _ in range(2):
-        op.vmult_host(dst_np, src_np)
-    t0 = time.perf_counter()
-    for _ in range(K):
-        op.vmult_host(dst_np, src_np)
-    e2e_serial_s = max_over_ranks((time.perf_counter() - t0) / K, world, dev)
-    op.set_host_chunks(0)
+    e2e_serial_s = max_over_ranks(e2e_serial_s, world, dev)
 
-    # the same operator in native FP64 arithmetic, for comparison
-    native = None
-    if args.arith == "df64":
-        op.set_fp64_emulation(False)
-        op.cache()
-        t_nat = _timed_vmults(torch, op, dst, src, flush, stream, max(5, K // 4))
-        t_nat = max_over_ranks(t_nat, world, dev)
-        native = {"value": replica_throughput(n, t_nat, world), "ms_per_step": t_nat * 1e3}
-        op.set_fp64_emulation(True)
-        op.cache()
+    # the other arithmetic of the same operator, reported beside the headline
+    other = "df64" if args.arith == "native" else "native"
+    op.set_fp64_emulation(other == "df64")
+    op.cache()
+    o_ms, o_kms, _, _ = time_operator(torch, op, dst, src, flush, stream, K, Wu, clocks)
+    o_e2e, _ = time_host_vmult(op, dst_np, src_np, K, Wu, clocks)
+    o_ms, o_kms, o_e2e = (max_over_ranks(x, world, dev) for x in (o_ms, o_kms, o_e2e))
+    op.set_fp64_emulation(args.arith == "df64")
+    op.cache()
+    clk = clocks.stop()
     ctx.synchronize()
+
     peak, peak_kind = measured_peak_hbm()
     b_alg = algorithmic_bytes(n, n_cells)
     achieved = b_alg / (k_ms * 1e-3) / 1e9
     f_alg = algorithmic_flops(n_cells, 5)
+    fp64_peak = measured_fp64_peak(torch, dev)
+    prof = profile_summary(HEADLINE_PROFILE[args.arith])
+    oprof = profile_summary(HEADLINE_PROFILE[other])
+    o_block = {
+        "arithmetic": ("double-float: each FP64 value carried as a pair of FP32 (48-bit significand, "
+                       "FP32 exponent range) on the FP32 pipe; agrees with the FP64 oracle within "
+                       "1e-12 relative l2 (tests/test_gpu_operators.py)") if other == "df64" else
+                      "native FP64",
+        "value": replica_throughput(n, o_ms * 1e-3, world), "unit": UNIT, "ms_per_step": o_ms,
+        "kernel_ms": o_kms,
+        "roofline": {"bound": "hbm", "achieved": b_alg / (o_kms * 1e-3) / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": b_alg / (o_kms * 1e-3) / 1e9 / peak,
+                     "traffic": (oprof or {}).get("traffic_bytes_per_launch"),
+                     "traffic_source": "ncu, profiles/" + HEADLINE_PROFILE[other]},
+        "e2e": {"value": replica_throughput(n, o_e2e, world), "unit": UNIT,
+                "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8, "ms_per_step": o_e2e * 1e3},
+    }
     line = {
         "metric": METRIC, "value": replica_throughput(n, ms_step * 1e-3, world), "unit": UNIT,
-        "n_gpus": world, "steps": K, "warmup": max(args.warmup, 3),
+        "n_gpus": world, "steps": K, "warmup": Wu,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "df64" if args.arith == "df64" else "f64",
-        "dtype_note": ("FP64 vectors in and out; arithmetic in double-float (each FP64 value "
-                       "carried as a pair of FP32, 48-bit significand) on the FP32 pipe; agrees "
-                       "with the FP64 oracle within 1e-12 relative l2 (tests/test_gpu_operators.py)")
-                      if args.arith == "df64" else "native FP64 arithmetic",
-        "native_f64": native,
+        "dtype_note": "native FP64 arithmetic, the reference's" if args.arith == "native" else
+                      ("FP64 vectors in and out; arithmetic in double-float (a pair of FP32, 48-bit "
+                       "significand) on the FP32 pipe"),
         "data": "synthetic",
         "config": {"workload": "nh_tangent_vmult_q4_cantilever_64x8x8", "n_dofs": n,
                    "n_cells": n_cells, "degree": 4, "n_q_1d": 5, "caching": args.caching,
@@ -870,21 +1094,26 @@ def main():
         "e2e": {"value": replica_throughput(n, e2e_s, world), "unit": UNIT,
                 "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
                 "ms_per_step": e2e_s * 1e3,
-                "overlap": "4 z-slabs: copy-in, cell launches and copy-out overlapped on 4 streams",
+                "overlap": "z-slabs: copy-in, cell launches and copy-out overlapped, replayed as a CUDA graph",
                 "no_overlap": {"value": replica_throughput(n, e2e_serial_s, world),
                                "ms_per_step": e2e_serial_s * 1e3}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profile_traffic(),
+                     "frac": achieved / peak, "traffic": (prof or {}).get("traffic_bytes_per_launch"),
+                     "traffic_source": "ncu, profiles/" + HEADLINE_PROFILE[args.arith] +
+                                       " (dram__bytes_read.sum + dram__bytes_write.sum of one launch)",
                      "peak_kind": peak_kind,
-                     "kernel": "cell_apply_kernel (vmult_add, CUDA events, L2 flushed)",
+                     "kernel": "cell kernel of vmult_add (CUDA events, L2 flushed)",
                      "kernel_ms": k_ms, "bytes_alg_per_launch": b_alg},
-        "fp64": {"alg_tflops": f_alg / (k_ms * 1e-3) / 1e12,
-                 "note": "FP64 pipe of GB300 is ~1.25 TFLOP/s nominal: the FP64 operator is pipe-bound"},
-        "compute_roofline": {"bound": "FP32 pipe issue (double-float arithmetic)",
-                             "ncu": profile_pipes(),
-                             "source": "profiles/nh_vmult_q4_cantilever_ncu.txt",
-                             "note": "the binding roof of this kernel; the HBM fraction above is "
-                                     "the fixed B_alg convention"},
+        "compute_roofline": {
+            "bound": "FP64 pipe" if args.arith == "native" else "FP32 pipe issue (double-float)",
+            "fp64_peak_tflops_measured": fp64_peak,
+            "fp64_peak_source": "cuBLAS DGEMM 4096^3 on this GPU, best of 3",
+            "alg_tflops": f_alg / (k_ms * 1e-3) / 1e12,
+            "alg_flop_per_launch": f_alg,
+            "ncu": prof, "source": "profiles/" + HEADLINE_PROFILE[args.arith],
+            "note": "the roof that binds this kernel; the HBM fraction above is the fixed "
+                    "algorithmic-bytes convention"},
+        other: o_block,
         "clocks": clk,
         "gpu_launches": launches,
         "wall_ms_per_step": t_wall / K * 1e3,
@@ -895,7 +1124,8 @@ def main():
                         ("heat_step_16cube_q2", lambda: extra_heat_step(torch, mfgpu, W, ctx, dev, stream, flush)),
                         ("solid_newton_64x8x8_q4", lambda: extra_solid_newton(mfgpu, W, ctx)),
                         ("design_choices", lambda: extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush,
-                                                                         mesh, u, src, n, op, src_np, dst_np)),
+                                                                         mesh, u, src, n, op, src_np, dst_np,
+                                                                         args.arith)),
                         ("degree_sweep_heat_64cube", lambda: extra_degree_sweep(torch, mfgpu, W, ctx, dev,
                                                                                stream, flush, peak)),
                         ("serving_300_requests", lambda: extra_serving(mfgpu, W))):

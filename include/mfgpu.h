@@ -228,7 +228,8 @@ int mfgpu_transfer_interpolate(mfgpu_context *ctx, const mfgpu_mesh *mesh,
  * static 4 MiB device array that every GPU loading the library keeps until
  * exit, so each intermediate (fine-x by coarse-y,z, then fine-x,y by
  * coarse-z, times n_components) may hold at most 262,144 doubles or 524,288
- * floats; larger levels return MFGPU_ERR_ARG.  Needs no context: it runs
+ * floats; larger levels return MFGPU_ERR_ARG.  Three- and two-dimensional
+ * meshes (dim = 2: the single z node plane is copied through).  Needs no context: it runs
  * on `stream` (a cudaStream_t, NULL for the default stream) of the current
  * device and returns without synchronising.  The first call on a device
  * looks up the array's device address, so make it before any stream

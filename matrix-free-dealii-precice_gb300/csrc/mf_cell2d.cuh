@@ -379,13 +379,17 @@ namespace mfgpu
     for (int a = 0; a < N; ++a)
       {
         const int q = a + N * l;
-        T         F[2][2];
+        T         H[2][2], F[2][2];
 #pragma unroll
         for (int i = 0; i < 2; ++i)
 #pragma unroll
           for (int j = 0; j < 2; ++j)
-            F[i][j] = W[i * 3 * N2 + (j + 1) * N2 + q] + (i == j ? T(1) : T(0));
-        const T J = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+            {
+              H[i][j] = W[i * 3 * N2 + (j + 1) * N2 + q];
+              F[i][j] = H[i][j] + (i == j ? T(1) : T(0));
+            }
+        const T Jm1 = jm1_from_grad2(H);
+        const T J   = T(1) + Jm1;
         if (!(J > T(0)))
           {
             atomicOr(err, 1);
@@ -400,7 +404,7 @@ namespace mfgpu
 #pragma unroll
               for (int j = 0; j < 2; ++j)
                 cp[(i * 2 + j) * N2] = Fi[j][i];
-            cp[4 * N2] = m.mu - m.two_lambda * log(J);
+            cp[4 * N2] = m.mu - m.two_lambda * log1p(Jm1);
           }
         else
           {
@@ -413,7 +417,7 @@ namespace mfgpu
                   cp[(5 + i * 2 + j) * N2] = F[i][j];
                 }
             cp[4 * N2] = J;
-            cp[9 * N2] = T(1) / sqrt(J);
+            cp[9 * N2] = exp(log1p(Jm1) * T(-0.5));
           }
       }
   }
@@ -513,34 +517,40 @@ namespace mfgpu
           {
             const int q   = a + N * l;
             const T   jxw = sh.w[a] * sh.w[l] * g.vol;
-            T         F[2][2];
+            T         H[2][2], F[2][2];
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
               for (int j = 0; j < 2; ++j)
-                F[i][j] = W[i * 3 * N2 + (j + 1) * N2 + q] + (i == j ? 1.0 : 0.0);
-            const T J     = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+                {
+                  H[i][j] = W[i * 3 * N2 + (j + 1) * N2 + q];
+                  F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
+                }
+            const T Jm1   = jm1_from_grad2(H);
+            const T J     = 1.0 + Jm1;
+            const T lnJ   = log1p(Jm1);
             T       Fi[2][2] = {{F[1][1] / J, -F[0][1] / J}, {-F[1][0] / J, F[0][0] / J}};
             T       tau[2][2];
             if constexpr (FORM == 1)
               {
-                const T tmp = m.mu - 2.0 * m.lambda * log(J);
+                // mu b - (mu - 2 lambda ln J) I = mu (H + H^T + H H^T) + 2 lambda ln J I
 #pragma unroll
                 for (int i = 0; i < 2; ++i)
 #pragma unroll
                   for (int j = 0; j < 2; ++j)
-                    tau[i][j] = m.mu * (F[i][0] * F[j][0] + F[i][1] * F[j][1]) - (i == j ? tmp : 0.0);
+                    tau[i][j] = m.mu * (H[i][j] + H[j][i] + (H[i][0] * H[j][0] + H[i][1] * H[j][1])) +
+                                (i == j ? 2.0 * m.lambda * lnJ : 0.0);
               }
             else
               {
-                const T f = pow(J, -0.5);
+                const T f = exp(-0.5 * lnJ);
 #pragma unroll
                 for (int i = 0; i < 2; ++i)
 #pragma unroll
                   for (int j = 0; j < 2; ++j)
                     tau[i][j] = 2.0 * m.c_1 * f * f * (F[i][0] * F[j][0] + F[i][1] * F[j][1]);
                 const T tr  = tau[0][0] + tau[1][1];
-                const T tmp = (m.kappa / 2.0) * (J - 1.0 / J) * J;
+                const T tmp = (m.kappa / 2.0) * Jm1 * (2.0 + Jm1);
                 tau[0][0] += tmp - tr / 2.0;
                 tau[1][1] += tmp - tr / 2.0;
               }

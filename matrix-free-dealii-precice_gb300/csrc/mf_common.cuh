@@ -153,6 +153,34 @@ namespace mfgpu
     return n;
   }
 
+  // J - 1 = det(I + H) - 1 from the displacement gradient H = Grad u,
+  // without forming det F: the principal invariants of H, tr H + (sum of
+  // its principal 2x2 minors) + det H.  det F - 1 loses the relative
+  // accuracy of a small strain to cancellation; this form keeps it, and
+  // ln J = log1p(J - 1) follows.  The reference evaluates
+  // std::log(determinant(F)) (mf_nh_operator.h:448,457).
+  template <typename T>
+  __host__ __device__ inline T
+  jm1_from_grad3(const T (&H)[3][3])
+  {
+    const T i1 = H[0][0] + H[1][1] + H[2][2];
+    const T i2 = (H[0][0] * H[1][1] - H[0][1] * H[1][0]) +
+                 (H[0][0] * H[2][2] - H[0][2] * H[2][0]) +
+                 (H[1][1] * H[2][2] - H[1][2] * H[2][1]);
+    const T i3 = H[0][0] * (H[1][1] * H[2][2] - H[1][2] * H[2][1]) -
+                 H[0][1] * (H[1][0] * H[2][2] - H[1][2] * H[2][0]) +
+                 H[0][2] * (H[1][0] * H[2][1] - H[1][1] * H[2][0]);
+    return i1 + (i2 + i3);
+  }
+
+  // the same in two dimensions: det(I + H) - 1 = tr H + det H
+  template <typename T>
+  __host__ __device__ inline T
+  jm1_from_grad2(const T (&H)[2][2])
+  {
+    return (H[0][0] + H[1][1]) + (H[0][0] * H[1][1] - H[0][1] * H[1][0]);
+  }
+
   // component mask of the Dirichlet constraints on node (ix,iy,iz)
   __host__ __device__ inline unsigned
   node_mask(const unsigned *fm, const int *Nn, int ix, int iy, int iz)

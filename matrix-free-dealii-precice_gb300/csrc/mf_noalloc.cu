@@ -10,9 +10,12 @@
 // altogether.  mfgpu_transfer_prolongate() builds a transfer object with
 // device tables and two intermediate arrays on every call.  This variant
 // runs the same three tensor-product passes, but:
-//   * it computes the 1D prolongation weights inside the kernel from the
-//     Gauss-Lobatto nodes, which it receives by value;
+//   * it tabulates the 1D prolongation weights on the host and passes them
+//     to the kernel by value;
 //   * it keeps the two intermediate arrays in the file-scope array below.
+//
+// Two-dimensional meshes (mesh.dim = 2) are supported: their single node
+// plane in z is copied through by the third pass.
 //
 // Limit: each intermediate array holds at most SCRATCH_BYTES / 2 bytes
 // (2 MiB, i.e. 262,144 doubles or 524,288 floats per intermediate,
@@ -47,6 +50,7 @@ namespace
 
   std::mutex g_setup_mutex;
   void      *g_scratch_addr[MAX_DEVICES] = {};
+  int        g_sm_count[MAX_DEVICES]     = {};
 
   struct NoAllocPass
   {
@@ -55,7 +59,9 @@ namespace
     int      nc;
     int      dir;
     int      p;
-    double   nodes[MAX_N];
+    // weight[h][lf][i]: Lagrange polynomial i of the coarse cell at the
+    // fine node lf of its half h (0 lower, 1 upper), tabulated on the host
+    double   weight[2][MAX_N][MAX_N];
     // pass 0 reads the coarse vector: zero its constrained entries
     int      mask_input;
     unsigned in_face_mask[6];
@@ -64,10 +70,13 @@ namespace
     unsigned out_face_mask[6];
   };
 
+  // One tensor-product pass of the prolongation along P.dir.  A direction
+  // with a single node plane on both levels (z of a two-dimensional mesh)
+  // is copied through unchanged.
   template <typename T>
   __global__ void
-  k_prolongate_pass_noalloc(const NoAllocPass P, const T *__restrict__ in,
-                            T *__restrict__ out)
+  k_prolongate_pass_noalloc(const __grid_constant__ NoAllocPass P,
+                            const T *__restrict__ in, T *__restrict__ out)
   {
     const size_t per_c = size_t(P.ext_out[0]) * P.ext_out[1] * P.ext_out[2];
     const size_t total = per_c * P.nc;
@@ -75,7 +84,8 @@ namespace
     size_t       stride_in = 1;
     for (int d = 0; d < P.dir; ++d)
       stride_in *= P.ext_in[d];
-    const int n_fine_cells = (P.ext_out[P.dir] - 1) / P.p;
+    const bool copy_through = P.ext_in[P.dir] == 1 && P.ext_out[P.dir] == 1;
+    const int  n_fine_cells = (P.ext_out[P.dir] - 1) / P.p;
     for (size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x; o < total;
          o += size_t(gridDim.x) * blockDim.x)
       {
@@ -92,24 +102,30 @@ namespace
             out[o] = T(0);
             continue;
           }
-        // fine node f along dir: fine cell, local node, position in the
-        // coarse cell
-        const int    f  = idx[P.dir];
-        const int    fc = min(f / P.p, n_fine_cells - 1);
-        const int    lf = f - fc * P.p;
-        const int    cc = fc / 2;
-        const double xi = 0.5 * (fc % 2) + 0.5 * P.nodes[lf];
-        idx[P.dir]      = 0;
+        if (copy_through)
+          {
+            // same node grid on both sides in this direction
+            const size_t io = size_t(c) * in_c + size_t(idx[0]) +
+                              size_t(P.ext_in[0]) * (size_t(idx[1]) + size_t(P.ext_in[1]) * idx[2]);
+            T v = in[io];
+            if (P.mask_input &&
+                ((node_mask(P.in_face_mask, P.ext_in, idx[0], idx[1], idx[2]) >> c) & 1u))
+              v = T(0);
+            out[o] = v;
+            continue;
+          }
+        // fine node f along dir: fine cell, local node, coarse cell
+        const int f  = idx[P.dir];
+        const int fc = min(f / P.p, n_fine_cells - 1);
+        const int lf = f - fc * P.p;
+        const int cc = fc / 2;
+        const int h  = fc % 2;
+        idx[P.dir]   = 0;
         const size_t base = size_t(c) * in_c + size_t(idx[0]) +
                             size_t(P.ext_in[0]) * (size_t(idx[1]) + size_t(P.ext_in[1]) * idx[2]);
         T s = T(0);
         for (int i = 0; i <= P.p; ++i)
           {
-            // Lagrange polynomial i on the Gauss-Lobatto nodes at xi
-            double w = 1.0;
-            for (int j = 0; j <= P.p; ++j)
-              if (j != i)
-                w *= (xi - P.nodes[j]) / (P.nodes[i] - P.nodes[j]);
             const int col = cc * P.p + i;
             T         v   = in[base + size_t(col) * stride_in];
             if (P.mask_input)
@@ -119,7 +135,7 @@ namespace
                 if ((node_mask(P.in_face_mask, P.ext_in, ii[0], ii[1], ii[2]) >> c) & 1u)
                   v = T(0);
               }
-            s += T(w) * v;
+            s += T(P.weight[h][lf][i]) * v;
           }
         out[o] = s;
       }
@@ -129,7 +145,7 @@ namespace
   void
   run_passes(const LevelGeom &coarse, const LevelGeom &fine, int nc,
              const HostBasis &b, const T *coarse_v, T *fine_v, T *s0, T *s1,
-             cudaStream_t stream)
+             int n_sm, cudaStream_t stream)
   {
     int         ext[3] = {coarse.Nn[0], coarse.Nn[1], coarse.Nn[2]};
     const T    *cur    = coarse_v;
@@ -146,8 +162,24 @@ namespace
         P.nc         = nc;
         P.dir        = d;
         P.p          = coarse.p;
-        for (int i = 0; i < MAX_N; ++i)
-          P.nodes[i] = i < b.N ? b.nodes[i] : 0.0;
+        for (int h = 0; h < 2; ++h)
+          for (int lf = 0; lf < MAX_N; ++lf)
+            for (int i = 0; i < MAX_N; ++i)
+              P.weight[h][lf][i] = 0.0;
+        for (int h = 0; h < 2; ++h)
+          for (int lf = 0; lf <= coarse.p; ++lf)
+            {
+              const long double xi = 0.5L * h + 0.5L * (long double)b.nodes[lf];
+              for (int i = 0; i <= coarse.p; ++i)
+                {
+                  long double w = 1.0L;
+                  for (int j = 0; j <= coarse.p; ++j)
+                    if (j != i)
+                      w *= (xi - (long double)b.nodes[j]) /
+                           ((long double)b.nodes[i] - (long double)b.nodes[j]);
+                  P.weight[h][lf][i] = double(w);
+                }
+            }
         P.mask_input  = d == 0;
         P.mask_output = d == 2;
         for (int f = 0; f < 6; ++f)
@@ -156,8 +188,8 @@ namespace
             P.out_face_mask[f] = fine.face_mask[f];
           }
         const size_t total = size_t(P.ext_out[0]) * P.ext_out[1] * P.ext_out[2] * nc;
-        const unsigned grid =
-          unsigned(std::min<size_t>(std::max<size_t>((total + 255) / 256, 1), 152 * 16));
+        const unsigned grid = unsigned(
+          std::min<size_t>(std::max<size_t>((total + 255) / 256, 1), size_t(n_sm) * 8));
         k_prolongate_pass_noalloc<T><<<grid, 256, 0, stream>>>(P, cur, dsts[d]);
         count_launch();
         MF_CK(cudaGetLastError());
@@ -166,10 +198,10 @@ namespace
       }
   }
 
-  // device address of the static scratch on the current device (set-up on
-  // the first call per device)
+  // device address of the static scratch on the current device and the
+  // device's SM count (set-up on the first call per device)
   void *
-  scratch_address()
+  scratch_address(int &n_sm)
   {
     int dev = 0;
     MF_CK(cudaGetDevice(&dev));
@@ -183,8 +215,12 @@ namespace
         if (rc != cudaSuccess || !ptr)
           throw Error(ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
                                   cudaGetErrorString(rc));
+        int sms = 0;
+        MF_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        g_sm_count[dev]     = sms > 0 ? sms : 1;
         g_scratch_addr[dev] = ptr;
       }
+    n_sm = g_sm_count[dev];
     return g_scratch_addr[dev];
   }
 } // namespace
@@ -217,16 +253,17 @@ mfgpu_transfer_prolongate_noalloc(const mfgpu_mesh *mesh, int coarse_level,
                                "scratch holds " + std::to_string(cap));
       HostBasis b;
       make_host_basis(m.degree, b);
-      unsigned char *base = static_cast<unsigned char *>(scratch_address());
+      int            n_sm = 1;
+      unsigned char *base = static_cast<unsigned char *>(scratch_address(n_sm));
       cudaStream_t   s    = static_cast<cudaStream_t>(stream);
       if (precision == 32)
         run_passes<float>(cg, fg, n_components, b, static_cast<const float *>(coarse),
                           static_cast<float *>(fine), reinterpret_cast<float *>(base),
-                          reinterpret_cast<float *>(base + HALF_BYTES), s);
+                          reinterpret_cast<float *>(base + HALF_BYTES), n_sm, s);
       else
         run_passes<double>(cg, fg, n_components, b, static_cast<const double *>(coarse),
                            static_cast<double *>(fine), reinterpret_cast<double *>(base),
-                           reinterpret_cast<double *>(base + HALF_BYTES), s);
+                           reinterpret_cast<double *>(base + HALF_BYTES), n_sm, s);
       return MFGPU_OK;
     }
   catch (const Error &e)

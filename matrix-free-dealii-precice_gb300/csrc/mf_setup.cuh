@@ -92,13 +92,17 @@ namespace mfgpu
     for (int k = 0; k < N; ++k)
       {
         const int q = a + b * N + k * N2;
-        T         F[3][3];
+        T         H[3][3], F[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j)
-            F[i][j] = cb[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j] + (i == j ? T(1) : T(0));
-        const T J = det3(F);
+            {
+              H[i][j] = cb[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j];
+              F[i][j] = H[i][j] + (i == j ? T(1) : T(0));
+            }
+        const T Jm1 = jm1_from_grad3(H);
+        const T J   = T(1) + Jm1;
         if (!(J > T(0)))
           {
             atomicOr(err, 1);
@@ -108,7 +112,7 @@ namespace mfgpu
         inv3(F, J, Fi);
         TO      *cp     = cache + size_t(cc) * NF * N3 + q;
         auto     st     = [&](int f, T v) { cp[size_t(f) * N3] = to_compute<TO, T>(v); };
-        const T  lnJ    = log(J);
+        const T  lnJ    = log1p(Jm1);
         const T  scalar = m.mu - T(2.0) * m.lambda * lnJ;
         if constexpr (VAR == V_SCALAR_REF)
           {
@@ -151,17 +155,20 @@ namespace mfgpu
 #pragma unroll
                   for (int j = 0; j < 3; ++j)
                     st((10 + i * 3 + j), F[i][j]);
-                st(19, pow(J, T(-1.0 / 3.0)));
+                st(19, exp(lnJ * T(-1.0 / 3.0)));
               }
             else
               {
+                // tau = mu b - (mu - 2 lambda ln J) I
+                //     = mu (H + H^T + H H^T) + 2 lambda ln J I
                 T tau[3][3];
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                   for (int j = 0; j < 3; ++j)
-                    tau[i][j] = m.mu * (F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]) -
-                                (i == j ? scalar : T(0));
+                    tau[i][j] = m.mu * (H[i][j] + H[j][i] +
+                                        (H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2])) +
+                                (i == j ? T(2.0) * m.lambda * lnJ : T(0));
                 const T iJ = T(1.) / J;
                 if constexpr (VAR == V_TENSOR2)
                   {
@@ -302,19 +309,23 @@ namespace mfgpu
                 }
               else
                 {
-                  T F[3][3];
+                  T H[3][3], F[3][3];
 #pragma unroll
                   for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
-                      F[i][j] = GU[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j] + (i == j ? T(1) : T(0));
-                  const T J = det3(F);
+                      {
+                        H[i][j] = GU[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j];
+                        F[i][j] = H[i][j] + (i == j ? T(1) : T(0));
+                      }
+                  const T Jm1 = jm1_from_grad3(H);
+                  const T J   = T(1) + Jm1;
                   T       Fi[3][3];
                   inv3(F, J, Fi);
                   mass = m.rho_alpha;
                   if constexpr (KIND == 1)
                     {
-                      const T cl = m.mu - T(2.0) * m.lambda * log(J) + T(2.0) * m.lambda;
+                      const T cl = m.mu - T(2.0) * m.lambda * log1p(Jm1) + T(2.0) * m.lambda;
 #pragma unroll
                       for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -323,7 +334,7 @@ namespace mfgpu
                     }
                   else
                     {
-                      const T js = pow(J, T(-1.0 / 3.0));
+                      const T js = exp(log1p(Jm1) * T(-1.0 / 3.0));
 #pragma unroll 1
                       for (int e = 0; e < 3; ++e)
                         {
@@ -471,29 +482,37 @@ namespace mfgpu
           {
             const int q   = a + b * N + k * N2;
             const T   jxw = sh.w[a] * sh.w[b] * sh.w[k] * g.vol;
-            T         F[3][3];
+            T         H[3][3], F[3][3];
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
-                F[i][j] = cb[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j] + (i == j ? T(1) : T(0));
-            const T J = det3(F);
+                {
+                  H[i][j] = cb[i * 4 * N3 + (j + 1) * N3 + q] * g.inv_h[j];
+                  F[i][j] = H[i][j] + (i == j ? T(1) : T(0));
+                }
+            const T Jm1 = jm1_from_grad3(H);
+            const T J   = T(1) + Jm1;
+            const T lnJ = log1p(Jm1);
             T       Fi[3][3];
             inv3(F, J, Fi);
             T tau[3][3];
             if constexpr (FORM == 1)
               {
-                const T tmp = m.mu - T(2.0) * m.lambda * log(J);
+                // tau = mu b - (mu - 2 lambda ln J) I (material.h:116-161),
+                // evaluated as mu (H + H^T + H H^T) + 2 lambda ln J I so that
+                // small strains keep their relative accuracy
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                   for (int j = 0; j < 3; ++j)
-                    tau[i][j] = m.mu * (F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]) -
-                                (i == j ? tmp : T(0));
+                    tau[i][j] = m.mu * (H[i][j] + H[j][i] +
+                                        (H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2])) +
+                                (i == j ? T(2.0) * m.lambda * lnJ : T(0));
               }
             else
               {
-                const T f = pow(J, T(-1.0 / 3.0));
+                const T f = exp(lnJ * T(-1.0 / 3.0));
                 T       tr = T(0);
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
@@ -504,7 +523,8 @@ namespace mfgpu
                                   (F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]);
                     }
                 tr           = tau[0][0] + tau[1][1] + tau[2][2];
-                const T tmp  = (m.kappa / T(2.0)) * (J - T(1) / J) * J;
+                // (kappa / 2) (J - 1/J) J = (kappa / 2) (J - 1)(J + 1)
+                const T tmp  = (m.kappa / T(2.0)) * Jm1 * (T(2) + Jm1);
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
                   tau[d][d] += tmp - tr / T(3);

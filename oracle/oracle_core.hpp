@@ -736,6 +736,24 @@ namespace orc
            F[2] * (F[3] * F[7] - F[4] * F[6]);
   }
 
+  // det(I + H) - 1 from the displacement gradient H (row-major dim x dim)
+  // by the principal invariants of H: tr H + (sum of principal 2x2 minors)
+  // + det H.  The reference takes std::log(determinant(F))
+  // (mf_nh_operator.h:448,457; material.h:116-161); the two agree in exact
+  // arithmetic, and this form keeps the relative accuracy of J - 1 and of
+  // ln J = log1p(J - 1) at small strains, where det F - 1 cancels.
+  template <typename T>
+  T
+  jm1_from_grad(int dim, const T *H)
+  {
+    if (dim == 2)
+      return (H[0] + H[3]) + (H[0] * H[3] - H[1] * H[2]);
+    const T i1 = H[0] + H[4] + H[8];
+    const T i2 = (H[0] * H[4] - H[1] * H[3]) + (H[0] * H[8] - H[2] * H[6]) +
+                 (H[4] * H[8] - H[5] * H[7]);
+    return i1 + (i2 + det(3, H));
+  }
+
   template <typename T>
   void
   invert(int dim, const T *F, T *Fi)

@@ -473,17 +473,21 @@ namespace orc
               for (int q = 0; q < Nd; ++q)
                 for (int l = 0; l < W; ++l)
                   {
-                    double F[9], Fi[9];
+                    double H[9], F[9], Fi[9];
                     for (int c = 0; c < 3; ++c)
                       for (int d = 0; d < 3; ++d)
-                        F[c * 3 + d] = g[(3 * c + d) * Nd + q][l] + (c == d ? 1.0 : 0.0);
-                    const double J = det(3, F);
+                        {
+                          H[c * 3 + d] = g[(3 * c + d) * Nd + q][l];
+                          F[c * 3 + d] = H[c * 3 + d] + (c == d ? 1.0 : 0.0);
+                        }
+                    const double Jm1 = jm1_from_grad(3, H);
+                    const double J   = 1.0 + Jm1;
                     if (!(J > 0.0))
                       {
                         ok = false;
                         continue;
                       }
-                    const double lnJ = std::log(J);
+                    const double lnJ = std::log1p(Jm1);
                     if (caching == scalar_referential)
                       {
                         cscal[bt * Nd + q][l] = mu - 2.0 * lambda * lnJ;
@@ -500,8 +504,11 @@ namespace orc
                         for (int i = 0; i < 3; ++i)
                           for (int j = 0; j < 3; ++j)
                             {
-                              const double bb = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
-                              x[10 + i * 3 + j][l] = (mu * bb - (i == j ? c : 0.0)) / J;
+                              // tau = mu (H + H^T + H H^T) + 2 lambda ln J I
+                              const double hh = H[i * 3] * H[j * 3] + H[i * 3 + 1] * H[j * 3 + 1] +
+                                                H[i * 3 + 2] * H[j * 3 + 2];
+                              x[10 + i * 3 + j][l] =
+                                (mu * (H[i * 3 + j] + H[j * 3 + i] + hh) + (i == j ? 2.0 * lambda * lnJ : 0.0)) / J;
                             }
                         if (caching == tensor2)
                           {

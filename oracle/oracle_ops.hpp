@@ -78,32 +78,39 @@ namespace orc
   // neo-Hookean
   // ---------------------------------------------------------------------
 
-  // Kirchhoff stress tau (material.h:116-161) as a full dim x dim tensor.
+  // Kirchhoff stress tau (material.h:116-161) as a full dim x dim tensor,
+  // from the displacement gradient H (F = I + H).  Formulation 1 is
+  // evaluated as mu (H + H^T + H H^T) + 2 lambda ln J I, which equals the
+  // reference's mu b - (mu - 2 lambda ln J) I, with ln J = log1p(J - 1) and
+  // J - 1 from the invariants of H (jm1_from_grad).
   template <typename T>
   void
-  get_tau(const Material &mat, int dim, const T *F, T *tau)
+  get_tau(const Material &mat, int dim, const T *H, T *tau)
   {
-    const T J = det(dim, F);
+    const T Jm1 = jm1_from_grad(dim, H);
+    const T J   = T(1) + Jm1;
+    const T lnJ = std::log1p(Jm1);
     if (mat.formulation == 1)
       {
-        // tau = mu b - (mu - 2 lambda ln J) I
         for (int i = 0; i < dim; ++i)
           for (int j = 0; j < dim; ++j)
             {
               T s = T(0);
               for (int k = 0; k < dim; ++k)
-                s += F[i * dim + k] * F[j * dim + k];
-              tau[i * dim + j] = T(mat.mu) * s;
+                s += H[i * dim + k] * H[j * dim + k];
+              tau[i * dim + j] = T(mat.mu) * (H[i * dim + j] + H[j * dim + i] + s);
             }
-        const T tmp = T(mat.mu) - T(2.0 * mat.lambda()) * std::log(J);
         for (int d = 0; d < dim; ++d)
-          tau[d * dim + d] -= tmp;
+          tau[d * dim + d] += T(2.0 * mat.lambda()) * lnJ;
       }
     else
       {
         // tau = tau_vol + P : tau_bar, tau_bar = 2 c1 b_bar
-        const T f = std::pow(J, T(-1.0 / dim));
-        T       tau_bar[9];
+        const T f = std::exp(lnJ * T(-1.0 / dim));
+        T       F[9], tau_bar[9];
+        for (int i = 0; i < dim; ++i)
+          for (int j = 0; j < dim; ++j)
+            F[i * dim + j] = H[i * dim + j] + (i == j ? T(1) : T(0));
         for (int i = 0; i < dim; ++i)
           for (int j = 0; j < dim; ++j)
             {
@@ -115,7 +122,9 @@ namespace orc
         T tr = T(0);
         for (int d = 0; d < dim; ++d)
           tr += tau_bar[d * dim + d];
-        const T tmp = T(mat.kappa() / 2.0) * (J - T(1) / J) * J;
+        // (kappa / 2) (J - 1/J) J = (kappa / 2) (J - 1)(J + 1)
+        const T tmp = T(mat.kappa() / 2.0) * Jm1 * (T(2) + Jm1);
+        (void)J;
         for (int i = 0; i < dim * dim; ++i)
           tau[i] = tau_bar[i];
         for (int d = 0; d < dim; ++d)
@@ -215,12 +224,16 @@ namespace orc
           cell_gradients_plain(box, b, u, e, s, grad.data());
           for (int q = 0; q < Qp; ++q)
             {
-              T F[9], Fi[9];
+              T H[9], F[9], Fi[9];
               for (int c = 0; c < dim; ++c)
                 for (int d = 0; d < dim; ++d)
-                  F[c * dim + d] = grad[(size_t(c) * dim + d) * Qp + q] +
-                                   (c == d ? T(1) : T(0));
-              const T J = det(dim, F);
+                  {
+                    H[c * dim + d] = grad[(size_t(c) * dim + d) * Qp + q];
+                    F[c * dim + d] = H[c * dim + d] + (c == d ? T(1) : T(0));
+                  }
+              const T Jm1 = jm1_from_grad(dim, H);
+              const T J   = T(1) + Jm1;
+              const T lnJ = std::log1p(Jm1);
               if (!(J > T(0)))
                 {
                   ok = false;
@@ -233,23 +246,14 @@ namespace orc
               st.map_J[iq] = J;
               if (mat.formulation == 0)
                 {
-                  st.scalar[iq] = std::pow(J, T(-1.0 / dim));
+                  st.scalar[iq] = std::exp(lnJ * T(-1.0 / dim));
                   for (int i = 0; i < d2; ++i)
                     st.t2[iq * d2 + i] = F[i];
                   continue;
                 }
-              const T scalar = mu - T(2.0) * lambda * std::log(J);
+              const T scalar = mu - T(2.0) * lambda * lnJ;
               T       tau[9];
-              for (int i = 0; i < dim; ++i)
-                for (int j = 0; j < dim; ++j)
-                  {
-                    T sum = T(0);
-                    for (int k = 0; k < dim; ++k)
-                      sum += F[i * dim + k] * F[j * dim + k];
-                    tau[i * dim + j] = mu * sum;
-                  }
-              for (int d = 0; d < dim; ++d)
-                tau[d * dim + d] -= scalar;
+              get_tau(mat, dim, H, tau);
               switch (st.caching)
                 {
                   case scalar_referential:
@@ -285,8 +289,7 @@ namespace orc
                     {
                       // 2 lambda F^{-T} (x) F^{-T} + (mu - 2 lambda ln J)
                       // [F^{-T}]_il [F^{-1}]_jk + mu delta_ik delta_jl
-                      const T lnJ = std::log(J);
-                      T      *A   = &st.t4ns[iq * d4];
+                      T *A = &st.t4ns[iq * d4];
                       for (int i = 0; i < dim; ++i)
                         for (int j = 0; j < dim; ++j)
                           for (int k = 0; k < dim; ++k)

@@ -136,12 +136,14 @@ namespace orc
         }
       for (int q = 0; q < Qp; ++q)
         {
-          T F[9], Fi[9], tau[9];
+          T H[9], F[9], Fi[9], tau[9];
           for (int c = 0; c < dim; ++c)
             for (int d = 0; d < dim; ++d)
-              F[c * dim + d] =
-                grad[(size_t(c) * dim + d) * Qp + q] + (c == d ? T(1) : T(0));
-          get_tau(*mat, dim, F, tau);
+              {
+                H[c * dim + d] = grad[(size_t(c) * dim + d) * Qp + q];
+                F[c * dim + d] = H[c * dim + d] + (c == d ? T(1) : T(0));
+              }
+          get_tau(*mat, dim, H, tau);
           invert(dim, F, Fi);
           for (int i = 0; i < dim; ++i)
             for (int j = 0; j < dim; ++j)

@@ -10,6 +10,7 @@ through the C-ABI and check, on two calls in a row, that:
     1e-13 relative tolerance as the other transfer tests; 1e-6 in FP32);
   * it leaves the device's free memory unchanged;
   * it rejects levels larger than the scratch with MFGPU_ERR_ARG.
+Meshes are three- and two-dimensional (a single node plane in z).
 This file is named so that pytest collects it last.
 """
 import ctypes
@@ -29,17 +30,34 @@ def _call_noalloc(mesh, coarse_level, nc, precision, coarse, fine):
         ctypes.c_void_p(coarse.data_ptr()), ctypes.c_void_p(fine.data_ptr()), None)
 
 
-@pytest.mark.parametrize("spec_kind,degree,nc,precision", [
+def _mesh(kind, degree):
+    if kind == "cantilever":
+        return W.to_lib_mesh(mfgpu, W.cantilever(degree, 2, rep=(2, 1, 1),
+                                                 length=(2.0, 1.0, 1.0)))
+    if kind == "heat":
+        return W.to_lib_mesh(mfgpu, W.unit_cube_heat(degree, 2, rep=(2, 1, 1)))
+    if kind == "heat2d":
+        # two-dimensional box, Dirichlet on x = 0 (one component)
+        return mfgpu.make_mesh(degree, 2, (3, 2), (0.0, 0.0), (1.2, 0.5),
+                               boundary_id=(1, 0, 0, 0), dirichlet=[(1, 1)])
+    # "beam2d": the 2D flap shape, both components clamped at x = 0
+    return mfgpu.make_mesh(degree, 2, (5, 1), (0.24899, 0.19), (0.6, 0.21),
+                           boundary_id=(1, 11, 11, 11), dirichlet=[(1, 0b11)])
+
+
+@pytest.mark.parametrize("kind,degree,nc,precision", [
     ("cantilever", 2, 3, 64),
     ("cantilever", 3, 3, 32),
     ("heat", 4, 1, 64),
+    ("heat2d", 2, 1, 64),
+    ("heat2d", 2, 1, 32),
+    ("beam2d", 2, 2, 64),
+    ("beam2d", 2, 2, 32),
 ])
-def test_noalloc_prolongation_matches_allocating_entry_point(ctx, spec_kind, degree,
-                                                             nc, precision):
+def test_noalloc_prolongation_matches_allocating_entry_point(ctx, kind, degree, nc,
+                                                             precision):
     import torch
-    spec = (W.cantilever(degree, 2, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
-            if spec_kind == "cantilever" else W.unit_cube_heat(degree, 2, rep=(2, 1, 1)))
-    mesh = W.to_lib_mesh(mfgpu, spec)
+    mesh = _mesh(kind, degree)
     dt = torch.float64 if precision == 64 else torch.float32
     tol = 1e-13 if precision == 64 else 1e-6
     nco = mfgpu.n_nodes(mesh, 0) * nc
