@@ -241,8 +241,11 @@ int mfgpu_transfer_prolongate_noalloc(const mfgpu_mesh *mesh, int coarse_level,
                                       void *stream);
 
 /* ---------------------------------------------------------------- */
-/* drivers                                                           */
+/* geometric multigrid preconditioner and CG                         */
 /* ---------------------------------------------------------------- */
+/* parameters of the linear solvers: CG, its preconditioner and the
+ * multigrid smoothers (the reference's "Linear solver" section,
+ * parameter_handling.h:177-253) */
 typedef struct mfgpu_solver_params
 {
   int    preconditioner;  /* 0 none, 1 jacobi, 2 gmg                        */
@@ -260,7 +263,110 @@ typedef struct mfgpu_solver_params
   int    coarse_dense;    /* level-0 operator (three-dimensional, <= 64 MiB)
                              assembled densely after each setup; the coarse
                              Chebyshev steps multiply by it, one warp per row */
+  int    estimate_condition; /* "Estimate condition number": before each
+                                linear solve of the solid, unpreconditioned
+                                CG (Lanczos) estimates the condition number
+                                (mf_elasticity.h:1998-2013); no effect on
+                                the solution                                 */
+  int    cond_cg_iterations; /* "Condition number CG iterations" (20)        */
 } mfgpu_solver_params;
+
+/* PreconditionMG<dim, VectorType, MGTransferMatrixFree> over the level
+ * hierarchy of a box mesh, as Solid::setup_gmg (mf_elasticity.h:
+ * 1142-1279) and LaplaceProblem::setup_gmg / solve_gmg_preconditioner
+ * (heat_transfer.h:515-573, 759-812) build it: level operators in FP32
+ * (mg_precision 32, the reference's) or FP64, MGTransferMatrixFree,
+ * mg::SmootherRelaxation with PreconditionChebyshev on levels > 0 and the
+ * Chebyshev solver on level 0 (MGCoarseGridApplySmoother). */
+typedef struct mfgpu_mg_params
+{
+  int            kind;     /* 0 heat (LaplaceOperator levels, M + dt K),
+                              1 neo-Hookean (NeoHookOperator levels)       */
+  double         delta_t;  /* heat: the time step of the level operators    */
+  const char    *caching;  /* neo-Hookean: MF caching of the level operators */
+  mfgpu_material material; /* neo-Hookean: alpha_1 as for the fine operator  */
+  mfgpu_solver_params solver; /* mg_precision, coarse_fp64, coarse_dense,
+                                 cuda_graphs, fp64_emulation and, for the
+                                 neo-Hookean levels, cheb_degree, cheb_range,
+                                 cheb_eig_its, coarse_accurate (the heat
+                                 levels use degree 5, range 15 and 10
+                                 iterations, as the reference)              */
+} mfgpu_mg_params;
+
+int mfgpu_mg_create(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                    const mfgpu_mg_params *params, mfgpu_mg **mg);
+/* Solid::update_matrix_free's level part (mf_elasticity.h:1291-1353):
+ * neo-Hookean levels interpolate the finest-level FP64 linearisation
+ * (device pointer, read during the call only) to every level
+ * (interpolate_to_mg), cache() and compute_diagonal() there; heat levels
+ * (linearisation NULL) compute their diagonals once.  Then the Chebyshev
+ * eigenvalue estimates (PreconditionChebyshev::initialize).  A setup with
+ * unchanged level operators keeps the previous smoothers. */
+int mfgpu_mg_setup(mfgpu_mg *mg, const double *linearisation);
+/* PreconditionMG::vmult: dst = one V-cycle applied to src (finest-level
+ * FP64 device vectors, dst != src) */
+int mfgpu_mg_vmult(mfgpu_mg *mg, double *dst, const double *src);
+/* number of levels and degrees of freedom of the finest one */
+int mfgpu_mg_info(mfgpu_mg *mg, int *n_levels, size_t *n_dofs);
+int mfgpu_mg_destroy(mfgpu_mg *mg);
+
+/* SolverCG<Vector<double>>::solve(A, x, b, preconditioner) under
+ * SolverControl(max_iterations, tol) (mf_elasticity.h:2015-2051,
+ * heat_transfer.h:729-737, 811): x holds the initial guess and receives
+ * the solution; stops when |r|_2 <= tol (absolute, as SolverControl).
+ * The preconditioner is mg when non-NULL, else PreconditionJacobi with
+ * relaxation jacobi_omega (> 0; compute_diagonal() of A first), else the
+ * identity.  A is an FP64 operator on the same context as mg.  Returns
+ * MFGPU_ERR_NOT_CONVERGED after max_iterations; iterations and residual
+ * (may be NULL) receive solver_control.last_step() / last_value(). */
+int mfgpu_pcg_solve(mfgpu_operator *A, mfgpu_mg *mg, double jacobi_omega,
+                    double *x, const double *b, double tol,
+                    int max_iterations, int *iterations, double *residual);
+/* SolverCG::connect_condition_number_slot under IterationNumberControl
+ * (mf_elasticity.h:1998-2013): n_iterations unpreconditioned CG iterations
+ * on A y = b from y = 0 (fewer when |r| <= tol), then the ratio of the
+ * extreme eigenvalues of the Lanczos tridiagonal matrix.  b is not
+ * changed. */
+int mfgpu_estimate_condition_number(mfgpu_operator *A, const double *b,
+                                    int n_iterations, double tol,
+                                    double *condition_number);
+
+/* ---------------------------------------------------------------- */
+/* DoF numbering: a caller's numbering <-> the library's              */
+/* ---------------------------------------------------------------- */
+/* deal.II numbers the DoFs of the reference's solid by DoFRenumbering::
+ * Cuthill_McKee (mf_elasticity.h:669), the heat problem's in the
+ * DoFHandler's default order; the library
+ * numbers them component-blocked on the lexicographic node grid.  Given the
+ * support point (x, y, z; z ignored in 2D) and the vector component of each
+ * of the caller's n_dofs DoFs (DoFTools::map_dofs_to_support_points and
+ * FiniteElement::system_to_component_index; components NULL means all 0),
+ * library_dof[i] receives the library's index of the caller's DoF i.
+ * Points must lie within tol (relative to the cell size) of a node of the
+ * level; every library DoF must be hit exactly once (MFGPU_ERR_ARG
+ * otherwise).  Host only. */
+int mfgpu_dof_permutation(const mfgpu_mesh *mesh, int level, size_t n_dofs,
+                          const double *support_points,
+                          const unsigned *components, double tol,
+                          size_t *library_dof);
+/* the same map kept on the device, to move vectors between the numberings
+ * on the context's stream: to_library dst[library_dof[i]] = src[i],
+ * from_library dst[i] = src[library_dof[i]] (precision 32 or 64) */
+typedef struct mfgpu_permutation mfgpu_permutation;
+int mfgpu_permutation_create(mfgpu_context *ctx, const mfgpu_mesh *mesh,
+                             int level, size_t n_dofs,
+                             const double *support_points,
+                             const unsigned *components, double tol,
+                             mfgpu_permutation **perm);
+int mfgpu_permutation_to_library(mfgpu_permutation *perm, int precision,
+                                 const void *src, void *dst);
+int mfgpu_permutation_from_library(mfgpu_permutation *perm, int precision,
+                                   const void *src, void *dst);
+int mfgpu_permutation_destroy(mfgpu_permutation *perm);
+
+/* ---------------------------------------------------------------- */
+/* drivers                                                           */
+/* ---------------------------------------------------------------- */
 
 typedef struct mfgpu_solid_params
 {
@@ -319,6 +425,12 @@ int mfgpu_solid_set_timing(mfgpu_solid *s, int enable);
 /* the section table as text: calls, wall time and share per section;
  * NUL-terminated, truncated to len bytes */
 int mfgpu_solid_timing_summary(mfgpu_solid *s, char *buf, size_t len);
+/* The convergence table of the last time step, as Solid::
+ * solve_nonlinear_timestep prints it (mf_elasticity.h:1402-1491,1502-1515):
+ * per Newton iteration LIN_IT, LIN_RES, COND_NUM (1 unless
+ * estimate_condition), RES_NORM, RES_U, NU_NORM, NU_U; NUL-terminated,
+ * truncated to len bytes */
+int mfgpu_solid_convergence_table(mfgpu_solid *s, char *buf, size_t len);
 int mfgpu_solid_destroy(mfgpu_solid *s);
 
 typedef struct mfgpu_heat_params

@@ -69,6 +69,12 @@ main(int argc, char *argv[])
       P.solver.cheb_range      = 20;
       P.solver.cheb_eig_its    = prm.get_int("Linear solver", "MF Chebyshev number CG iterations");
       P.solver.coarse_accurate = prm.get_bool("Linear solver", "MF Chebyshev coarse accurate eigenvalues");
+      // the level-0 solver: Chebyshev (the default); the alternative CG
+      // coarse solver of mf_elasticity.h:1183-1198 is not built
+      if (P.solver.preconditioner == 2 && !prm.get_bool("Linear solver", "MF Chebyshev coarse"))
+        throw std::runtime_error("MF Chebyshev coarse = false (CG coarse-grid solver) is not supported");
+      P.solver.estimate_condition = prm.get_bool("Linear solver", "Estimate condition number");
+      P.solver.cond_cg_iterations = prm.get_int("Linear solver", "Condition number CG iterations");
       P.solver.mg_precision    = prm.get_int("GPU", "MG precision");
       P.solver.coarse_fp64     = prm.get_bool("GPU", "FP64 coarse solve");
       P.solver.fp64_emulation  = prm.get_bool("GPU", "FP64 emulation");
@@ -142,6 +148,10 @@ main(int argc, char *argv[])
           long cg     = 0;
           int  solves = 0;
           check(mfgpu_solid_step(solid, &R.newton_its[s], &cg, &solves, R.watch_disp[s]));
+          // the Newton convergence table the reference prints per step
+          std::vector<char> conv(1 << 14);
+          check(mfgpu_solid_convergence_table(solid, conv.data(), conv.size()));
+          std::cout << conv.data();
           R.total_cg += cg;
           R.n_solves += solves;
           tt += P.dt;

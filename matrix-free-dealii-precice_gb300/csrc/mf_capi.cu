@@ -1,42 +1,9 @@
 // extern "C" entry points of libmfgpu.so (declared in include/mfgpu.h).
 // Every entry point converts exceptions into a status code and a
 // per-thread error message.
-#include <algorithm>
-#include <atomic>
 #include <chrono>
-#include <cstring>
-#include <string>
 
-#include "../../include/mfgpu.h"
-#include "mf_drivers.h"
-
-using namespace mfgpu;
-
-struct mfgpu_context
-{
-  std::unique_ptr<Context> c;
-  std::atomic<int>         live{0}; // operators and drivers created on this context
-};
-
-struct mfgpu_operator
-{
-  std::unique_ptr<Operator> op;
-  mfgpu_context            *ctx = nullptr;
-  DevBuf                    hsrc, hdst; // device staging for the host-buffer vmult
-  HostPipe                  pipe;       // streams of the overlapped host-buffer vmult
-};
-
-struct mfgpu_solid
-{
-  std::unique_ptr<SolidDriver> d;
-  mfgpu_context               *ctx = nullptr;
-};
-
-struct mfgpu_heat
-{
-  std::unique_ptr<HeatDriver> d;
-  mfgpu_context              *ctx = nullptr;
-};
+#include "mf_capi.h"
 
 static thread_local std::string g_last_error;
 
@@ -44,50 +11,6 @@ void
 mfgpu::set_last_error(const char *msg)
 {
   g_last_error = msg ? msg : "";
-}
-
-template <typename F>
-static int
-guarded(F &&f)
-{
-  try
-    {
-      f();
-      return MFGPU_OK;
-    }
-  catch (const Error &e)
-    {
-      g_last_error = e.what();
-      return e.code;
-    }
-  catch (const std::exception &e)
-    {
-      g_last_error = e.what();
-      return MFGPU_ERR_ARG;
-    }
-  catch (...)
-    {
-      g_last_error = "unknown exception";
-      return MFGPU_ERR_ARG;
-    }
-}
-
-// copy a text result into a caller's buffer (NUL-terminated, truncated)
-static void
-copy_text(const std::string &t, char *buf, size_t len)
-{
-  if (len == 0)
-    throw Error(ERR_ARG, "buffer length 0");
-  const size_t k = std::min(t.size(), len - 1);
-  std::memcpy(buf, t.data(), k);
-  buf[k] = '\0';
-}
-
-static void
-need(const void *p, const char *what)
-{
-  if (!p)
-    throw Error(ERR_ARG, std::string("null argument: ") + what);
 }
 
 extern "C"
@@ -696,6 +619,16 @@ extern "C"
         *iterations = its;
       if (seconds)
         *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+  }
+
+  int
+  mfgpu_solid_convergence_table(mfgpu_solid *s, char *buf, size_t len)
+  {
+    return guarded([&] {
+      need(s, "solid");
+      need(buf, "buf");
+      copy_text(s->d->convergence_table(), buf, len);
     });
   }
 

@@ -5,6 +5,7 @@
 // (include/heat_transfer/heat_transfer.h:579-655, 715-812), with preCICE
 // replaced by a constant boundary traction / analytic Dirichlet data.
 #include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 
@@ -88,6 +89,19 @@ namespace mfgpu
     return r;
   }
 
+  double
+  estimate_condition_number(Operator &A, const double *b, int n_its, double tol)
+  {
+    DevBuf        y, ws;
+    const size_t  n = A.m();
+    y.alloc(n * sizeof(double));
+    MF_CK(cudaMemsetAsync(y.ptr, 0, n * sizeof(double), A.ctx->stream));
+    OpRef<double> L(&A);
+    const CGStats st = cg_solve<double>(*A.ctx, L, nullptr, y.as<double>(), b, tol, n_its, true, false, &ws);
+    const auto    ev = lanczos_extreme_eigenvalues(st);
+    return ev.first > 0 ? ev.second / ev.first : 1.0;
+  }
+
   // ---------------------------------------------------------------------
   // preconditioner wrappers
   // ---------------------------------------------------------------------
@@ -109,6 +123,190 @@ namespace mfgpu
       vec_scale<double>(*ctx, A->m(), omega, A->inv_diag.as<double>(), s, d);
     }
   };
+
+  // ---------------------------------------------------------------------
+  // multigrid hierarchy
+  // ---------------------------------------------------------------------
+  std::unique_ptr<GMGHierarchy>
+  GMGHierarchy::heat(Context *c, const Mesh &m, const mfgpu_solver_params &s, double delta_t)
+  {
+    std::unique_ptr<GMGHierarchy> h(new GMGHierarchy());
+    h->mesh  = m;
+    h->S     = s;
+    h->kind  = 0;
+    h->nc    = 1;
+    h->lprec = s.mg_precision == 64 ? 64 : 32;
+    // LaplaceProblem::setup_gmg (heat_transfer.h:515-573): Chebyshev degree
+    // 5, smoothing range 15, 10 eigenvalue-estimate iterations; the coarse
+    // level's estimate runs m() iterations
+    h->range      = 15.;
+    h->degree     = 5;
+    h->eig_its    = 10;
+    h->coarse_its = -1;
+    const bool emul = s.fp64_emulation != 0;
+    for (int l = 0; l <= m.n_ref; ++l)
+      {
+        auto lo     = make_heat(c, m, l, h->lprec, true);
+        lo->delta_t = delta_t;
+        lo->arith   = (emul && h->lprec == 64) ? 1 : 0;
+        h->lops.push_back(std::move(lo));
+      }
+    if (s.coarse_fp64 && h->lprec == 32)
+      {
+        auto co     = make_heat(c, m, 0, 64, true);
+        co->delta_t = delta_t;
+        co->arith   = emul ? 1 : 0;
+        h->coarse64 = std::move(co);
+      }
+    h->finish(c);
+    return h;
+  }
+
+  std::unique_ptr<GMGHierarchy>
+  GMGHierarchy::solid(Context *c, const Mesh &m, const mfgpu_solver_params &s, const NHMatD &mat,
+                      int formulation, int variant)
+  {
+    std::unique_ptr<GMGHierarchy> h(new GMGHierarchy());
+    h->mesh       = m;
+    h->S          = s;
+    h->kind       = 1;
+    h->nc         = m.dim;
+    h->lprec      = s.mg_precision == 64 ? 64 : 32;
+    h->range      = s.cheb_range;
+    h->degree     = unsigned(s.cheb_degree);
+    h->eig_its    = s.cheb_eig_its;
+    h->coarse_its = s.coarse_accurate ? -1 : s.cheb_eig_its;
+    const bool emul = s.fp64_emulation != 0;
+    auto       nh   = [&](int l, int prec, int arith) {
+      auto op           = make_nh(c, m, l, prec, variant);
+      op->mat           = mat;
+      op->formulation   = formulation;
+      op->have_material = true;
+      op->arith         = arith;
+      return op;
+    };
+    for (int l = 0; l <= m.n_ref; ++l)
+      {
+        h->lops.push_back(nh(l, h->lprec, (emul && h->lprec == 64) ? 1 : 0));
+        h->u_levels.emplace_back(h->lops.back()->m() * (h->lprec == 32 ? 4 : 8));
+      }
+    if (s.coarse_fp64 && h->lprec == 32)
+      {
+        h->coarse64 = nh(0, 64, emul ? 1 : 0);
+        h->u0_64.alloc(h->coarse64->m() * sizeof(double));
+      }
+    h->finish(c);
+    return h;
+  }
+
+  void
+  GMGHierarchy::finish(Context *c)
+  {
+    ctx = c;
+    L   = mesh.n_ref;
+    make_host_basis(mesh.degree, basis);
+    auto fill = [&](auto &mg) {
+      mg.ctx = ctx;
+      for (int l = 0; l <= L; ++l)
+        {
+          mg.ops.push_back(lops[l].get());
+          if (l == 0)
+            mg.transfers.emplace_back(nullptr);
+          else
+            mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom, lops[l]->geom, nc, lprec));
+        }
+      mg.coarse64   = coarse64.get();
+      mg.use_graphs = S.cuda_graphs != 0;
+    };
+    if (lprec == 32)
+      {
+        mgf.reset(new Multigrid<float>());
+        fill(*mgf);
+      }
+    else
+      {
+        mgd.reset(new Multigrid<double>());
+        fill(*mgd);
+      }
+  }
+
+  void
+  GMGHierarchy::set_linearisation(const double *ulin, PhaseTimer &timer)
+  {
+    if (kind != 1)
+      throw Error(ERR_STATE, "only neo-Hookean levels take a linearisation");
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: interpolate_to_mg");
+      const size_t      nf = lops[L]->m();
+      if (lprec == 32)
+        vec_convert<float, double>(*ctx, nf, ulin, u_levels[L].as<float>());
+      else
+        vec_copy<double>(*ctx, nf, ulin, u_levels[L].as<double>());
+      for (int l = L; l > 0; --l)
+        {
+          Transfer *t = lprec == 32 ? mgf->transfers[l].get() : mgd->transfers[l].get();
+          t->interpolate(u_levels[l - 1].ptr, u_levels[l].ptr);
+        }
+      if (coarse64)
+        vec_convert<double, float>(*ctx, coarse64->m(), u_levels[0].as<float>(), u0_64.as<double>());
+    }
+    PhaseTimer::Scope ts(timer, ctx, "Setup MF: cache()");
+    for (int l = 0; l <= L; ++l)
+      {
+        auto *op = static_cast<NHOperator *>(lops[l].get());
+        op->u    = u_levels[l].ptr;
+        op->do_cache();
+      }
+    if (coarse64)
+      {
+        auto *op = static_cast<NHOperator *>(coarse64.get());
+        op->u    = u0_64.ptr;
+        op->do_cache();
+      }
+  }
+
+  void
+  GMGHierarchy::update_diagonals(PhaseTimer &timer)
+  {
+    size_t key = 1469598103934665603ull;
+    for (auto &op : lops)
+      key = (key ^ op->value_state()) * 1099511628211ull;
+    if (coarse64)
+      key = (key ^ coarse64->value_state()) * 1099511628211ull;
+    if (key == diag_key)
+      return;
+    {
+      PhaseTimer::Scope ts(timer, ctx, "Setup MF: diagonal()");
+      for (auto &op : lops)
+        op->compute_diagonal();
+      if (coarse64)
+        coarse64->compute_diagonal();
+    }
+    Operator *co = coarse64 ? coarse64.get() : lops[0].get();
+    if (S.coarse_dense && co->dense_fits())
+      {
+        PhaseTimer::Scope ts(timer, ctx, "Setup MF: coarse matrix");
+        co->assemble_dense();
+      }
+    diag_key = key;
+  }
+
+  void
+  GMGHierarchy::setup_smoothers(PhaseTimer &timer)
+  {
+    PhaseTimer::Scope ts(timer, ctx, kind == 1 ? "Setup MF: GMG setup" : "GMG setup");
+    const int         cits = coarse_its < 0 ? int(lops[0]->m()) : coarse_its;
+    if (lprec == 32)
+      mgf->setup(range, degree, eig_its, cits);
+    else
+      mgd->setup(range, degree, eig_its, cits);
+  }
+
+  Precond<double> *
+  GMGHierarchy::precond()
+  {
+    return lprec == 32 ? static_cast<Precond<double> *>(mgf.get()) : static_cast<Precond<double> *>(mgd.get());
+  }
 
   // ---------------------------------------------------------------------
   // solid
@@ -143,50 +341,8 @@ namespace mfgpu
       }
     if (P.solver.preconditioner == 2)
       {
-        lprec = P.solver.mg_precision == 64 ? 64 : 32;
-        for (int l = 0; l <= L; ++l)
-          {
-            auto op           = make_nh(ctx, mesh, l, lprec, variant);
-            op->mat           = mat;
-            op->formulation   = P.material.formulation;
-            op->have_material = true;
-            op->arith         = (emul && lprec == 64) ? 1 : 0;
-            lops.push_back(std::move(op));
-            u_levels.emplace_back(lops.back()->m() * (lprec == 32 ? 4 : 8));
-          }
-        if (P.solver.coarse_fp64 && lprec == 32)
-          {
-            coarse64                = make_nh(ctx, mesh, 0, 64, variant);
-            coarse64->mat           = mat;
-            coarse64->formulation   = P.material.formulation;
-            coarse64->have_material = true;
-            coarse64->arith         = emul ? 1 : 0;
-            u0_64.alloc(coarse64->m() * sizeof(double));
-          }
-        auto fill = [&](auto &mg) {
-          mg.ctx = ctx;
-          for (int l = 0; l <= L; ++l)
-            {
-              mg.ops.push_back(lops[l].get());
-              if (l == 0)
-                mg.transfers.emplace_back(nullptr);
-              else
-                mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
-                                                       lops[l]->geom, mesh.dim, lprec));
-            }
-          mg.coarse64   = coarse64.get();
-          mg.use_graphs = P.solver.cuda_graphs != 0;
-        };
-        if (lprec == 32)
-          {
-            mgf.reset(new Multigrid<float>());
-            fill(*mgf);
-          }
-        else
-          {
-            mgd.reset(new Multigrid<double>());
-            fill(*mgd);
-          }
+        gmg   = GMGHierarchy::solid(ctx, mesh, P.solver, mat, P.material.formulation, variant);
+        lprec = gmg->lprec;
       }
   }
 
@@ -205,55 +361,9 @@ namespace mfgpu
       }
     if (P.solver.preconditioner != 2)
       return;
-    {
-      PhaseTimer::Scope ts(timer, ctx, "Setup MF: interpolate_to_mg");
-      const size_t      nf = lops[L]->m();
-      if (lprec == 32)
-        vec_convert<float, double>(*ctx, nf, ulin, u_levels[L].as<float>());
-      else
-        vec_copy<double>(*ctx, nf, ulin, u_levels[L].as<double>());
-      for (int l = L; l > 0; --l)
-        {
-          Transfer *t = lprec == 32 ? mgf->transfers[l].get() : mgd->transfers[l].get();
-          t->interpolate(u_levels[l - 1].ptr, u_levels[l].ptr);
-        }
-      if (coarse64)
-        vec_convert<double, float>(*ctx, coarse64->m(), u_levels[0].as<float>(), u0_64.as<double>());
-    }
-    {
-      PhaseTimer::Scope ts(timer, ctx, "Setup MF: cache()");
-      for (int l = 0; l <= L; ++l)
-        {
-          lops[l]->u = u_levels[l].ptr;
-          lops[l]->do_cache();
-        }
-      if (coarse64)
-        {
-          coarse64->u = u0_64.ptr;
-          coarse64->do_cache();
-        }
-    }
-    {
-      PhaseTimer::Scope ts(timer, ctx, "Setup MF: diagonal()");
-      for (int l = 0; l <= L; ++l)
-        lops[l]->compute_diagonal();
-      if (coarse64)
-        coarse64->compute_diagonal();
-    }
-    {
-      Operator *co = coarse64 ? static_cast<Operator *>(coarse64.get()) : lops[0].get();
-      if (P.solver.coarse_dense && co->dense_fits())
-        {
-          PhaseTimer::Scope ts(timer, ctx, "Setup MF: coarse matrix");
-          co->assemble_dense();
-        }
-    }
-    PhaseTimer::Scope ts(timer, ctx, "Setup MF: GMG setup");
-    const int         coarse_its = P.solver.coarse_accurate ? int(lops[0]->m()) : P.solver.cheb_eig_its;
-    if (lprec == 32)
-      mgf->setup(P.solver.cheb_range, P.solver.cheb_degree, P.solver.cheb_eig_its, coarse_its);
-    else
-      mgd->setup(P.solver.cheb_range, P.solver.cheb_degree, P.solver.cheb_eig_its, coarse_its);
+    gmg->set_linearisation(ulin, timer);
+    gmg->update_diagonals(timer);
+    gmg->setup_smoothers(timer);
   }
 
   double
@@ -334,6 +444,11 @@ namespace mfgpu
   int
   SolidDriver::solve_linear(const double *b, double *x, double tol)
   {
+    // "Estimate condition number" (mf_elasticity.h:1998-2013): a dummy CG
+    // before the solve, whose result only enters the convergence table
+    last_cond = P.solver.estimate_condition
+                  ? estimate_condition_number(*fine, b, std::max(P.solver.cond_cg_iterations, 1), tol)
+                  : 1.0;
     PhaseTimer::Scope ts(timer, ctx, "Linear solver");
     const size_t      n = fine->m();
     MF_CK(cudaMemsetAsync(x, 0, n * sizeof(double), ctx->stream));
@@ -351,16 +466,37 @@ namespace mfgpu
       }
     else if (P.solver.preconditioner == 2)
       {
-        Precond<double> *M = lprec == 32 ? static_cast<Precond<double> *>(mgf.get()) :
-                                           static_cast<Precond<double> *>(mgd.get());
-        st = cg_solve<double>(*ctx, A, M, x, b, tol, maxit, false, false, &cg_ws);
+        st = cg_solve<double>(*ctx, A, gmg->precond(), x, b, tol, maxit, false, false, &cg_ws);
       }
     else
       st = cg_solve<double>(*ctx, A, nullptr, x, b, tol, maxit, false, false, &cg_ws);
     constrained_op<double>(*ctx, fine->geom, fine->nc, 2, nullptr, x);
     if (!st.converged)
       throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+    last_lin_res = st.res;
     return st.its;
+  }
+
+  std::string
+  SolidDriver::convergence_table() const
+  {
+    // Solid::print_conv_header / solve_nonlinear_timestep / print_conv_footer
+    // (mf_elasticity.h:1402-1491, 1498-1530)
+    const std::string rule(98, '_');
+    std::string       out = "\nTimestep " + std::to_string(table_step) + "\n" + rule + "\n" +
+                      "    SOLVER STEP     |  LIN_IT    LIN_RES   COND_NUM   RES_NORM      RES_U      NU_NORM"
+                      "       NU_U\n" +
+                      rule + "\n";
+    char line[256];
+    for (const NewtonRow &r : table)
+      {
+        std::snprintf(line, sizeof(line), " %2d  | %7d  %.3e  %.3e  %.3e  %.3e    %.3e  %.3e\n", r.it,
+                      r.lin_its, r.lin_res, r.cond, r.res_norm, r.res, r.upd_norm, r.upd);
+        out += line;
+      }
+    std::snprintf(line, sizeof(line), " %2d  CONVERGED! \n", int(table.size()));
+    out += line;
+    return out + rule + "\n";
   }
 
   std::vector<double>
@@ -433,6 +569,8 @@ namespace mfgpu
            *Ao = a_old.as<double>(), *Ac = acc.as<double>(), *R = rhs.as<double>(), *DU = du.as<double>();
     total_cg = 0;
     n_solves = 0;
+    table.clear();
+    table_step = step_no + 1;
     MF_CK(cudaMemsetAsync(Dl, 0, n * sizeof(double), ctx->stream));
     double err_res0 = 0, err_upd = 0, err_upd0 = 0, err_upd_norm = 0;
     int    it       = 0;
@@ -463,6 +601,7 @@ namespace mfgpu
         if (it == 0)
           err_upd0 = err_upd;
         err_upd_norm = err_upd0 != 0 ? err_upd / err_upd0 : err_upd;
+        table.push_back({it, its, last_lin_res, last_cond, err_res_norm, err_res, err_upd_norm, err_upd});
         vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, Dl);
         vec_axpby<double>(*ctx, n, 1.0, DU, 1.0, U);
       }
@@ -504,44 +643,8 @@ namespace mfgpu
       }
     if (P.solver.preconditioner == 2)
       {
-        lprec = P.solver.mg_precision == 64 ? 64 : 32;
-        for (int l = 0; l <= L; ++l)
-          {
-            auto lo     = make_heat(ctx, mesh, l, lprec, true);
-            lo->delta_t = P.dt;
-            lo->arith   = (emul && lprec == 64) ? 1 : 0;
-            lops.push_back(std::move(lo));
-          }
-        if (P.solver.coarse_fp64 && lprec == 32)
-          {
-            coarse64          = make_heat(ctx, mesh, 0, 64, true);
-            coarse64->delta_t = P.dt;
-            coarse64->arith   = emul ? 1 : 0;
-          }
-        auto fill = [&](auto &mg) {
-          mg.ctx = ctx;
-          for (int l = 0; l <= L; ++l)
-            {
-              mg.ops.push_back(lops[l].get());
-              if (l == 0)
-                mg.transfers.emplace_back(nullptr);
-              else
-                mg.transfers.emplace_back(new Transfer(ctx, basis, lops[l - 1]->geom,
-                                                       lops[l]->geom, 1, lprec));
-            }
-          mg.coarse64   = coarse64.get();
-          mg.use_graphs = P.solver.cuda_graphs != 0;
-        };
-        if (lprec == 32)
-          {
-            mgf.reset(new Multigrid<float>());
-            fill(*mgf);
-          }
-        else
-          {
-            mgd.reset(new Multigrid<double>());
-            fill(*mgd);
-          }
+        gmg   = GMGHierarchy::heat(ctx, mesh, P.solver, P.dt);
+        lprec = gmg->lprec;
       }
   }
 
@@ -579,18 +682,10 @@ namespace mfgpu
         ctx->sync();
       }
     vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
+    // the level operators stay fixed over the time steps: their diagonals
+    // and the dense coarse operator are made once
     if (P.solver.preconditioner == 2)
-      {
-        for (auto &lo : lops)
-          lo->compute_diagonal();
-        if (coarse64)
-          coarse64->compute_diagonal();
-        // the level operators stay fixed over the time steps: the coarse
-        // one is assembled once
-        Operator *co = coarse64 ? static_cast<Operator *>(coarse64.get()) : lops[0].get();
-        if (P.solver.coarse_dense && co->dense_fits())
-          co->assemble_dense();
-      }
+      gmg->update_diagonals(timer);
     if (P.solver.preconditioner == 1)
       op->compute_diagonal();
     std::memset(&src, 0, sizeof(src));
@@ -658,18 +753,10 @@ namespace mfgpu
     CGStats st;
     if (P.solver.preconditioner == 2)
       {
-        {
-          PhaseTimer::Scope tg(timer, ctx, "GMG setup");
-          if (lprec == 32)
-            mgf->setup(15., 5, 10, int(lops[0]->m()));
-          else
-            mgd->setup(15., 5, 10, int(lops[0]->m()));
-        }
+        gmg->setup_smoothers(timer);
         PhaseTimer::Scope tsol(timer, ctx, "solve system");
-        if (lprec == 32)
-          st = cg_solve<double>(*ctx, A, mgf.get(), du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
-        else
-          st = cg_solve<double>(*ctx, A, mgd.get(), du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
+        st = cg_solve<double>(*ctx, A, gmg->precond(), du.as<double>(), rhs.as<double>(), tol, int(n), false,
+                              false, &cg_ws);
       }
     else if (P.solver.preconditioner == 1)
       {

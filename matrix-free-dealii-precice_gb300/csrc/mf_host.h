@@ -79,6 +79,7 @@ namespace mfgpu
   struct Context
   {
     int          device = 0;
+    int          n_sm   = 1; // multiprocessors of the device
     cudaStream_t stream = nullptr;
     DevBuf       err;      // int error flags
     DevBuf       ticket;   // unsigned: block counter of the single-launch reductions

@@ -227,6 +227,7 @@ namespace mfgpu
     : device(dev)
   {
     MF_CK(cudaSetDevice(dev));
+    MF_CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
     MF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     err.alloc(sizeof(int) * 4);
     ticket.alloc(sizeof(unsigned) * 4);

@@ -320,6 +320,20 @@ namespace mfgpu
     return 0.5 * (lo + hi);
   }
 
+  std::pair<double, double>
+  lanczos_extreme_eigenvalues(const CGStats &st)
+  {
+    const size_t k = st.alpha.size();
+    if (k == 0)
+      return {1.0, 1.0};
+    std::vector<double> d(k), e(k - 1);
+    for (size_t i = 0; i < k; ++i)
+      d[i] = 1. / st.alpha[i] + (i > 0 ? st.beta[i - 1] / st.alpha[i - 1] : 0.);
+    for (size_t i = 0; i + 1 < k; ++i)
+      e[i] = std::sqrt(st.beta[i]) / st.alpha[i];
+    return {tridiag_eig(d, e, 0), tridiag_eig(d, e, int(k) - 1)};
+  }
+
   // ---------------------------------------------------------------------
   // Chebyshev
   // ---------------------------------------------------------------------
@@ -405,19 +419,9 @@ namespace mfgpu
   void
   Chebyshev<T>::set_bounds(const CGStats &st)
   {
-    const size_t k = st.alpha.size();
-    if (k == 0)
-      lambda_min = lambda_max = 1.0;
-    else
-      {
-        std::vector<double> d(k), e(k > 0 ? k - 1 : 0);
-        for (size_t i = 0; i < k; ++i)
-          d[i] = 1. / st.alpha[i] + (i > 0 ? st.beta[i - 1] / st.alpha[i - 1] : 0.);
-        for (size_t i = 0; i + 1 < k; ++i)
-          e[i] = std::sqrt(st.beta[i]) / st.alpha[i];
-        lambda_min = tridiag_eig(d, e, 0);
-        lambda_max = 1.2 * tridiag_eig(d, e, int(k) - 1);
-      }
+    const auto ev = lanczos_extreme_eigenvalues(st);
+    lambda_min    = ev.first;
+    lambda_max    = st.alpha.empty() ? 1.0 : 1.2 * ev.second;
     const double alpha = smoothing_range > 1. ? lambda_max / smoothing_range :
                                                 std::min(0.9 * lambda_max, lambda_min);
     if (degree == 0)

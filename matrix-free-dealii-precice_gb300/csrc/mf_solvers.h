@@ -84,6 +84,9 @@ namespace mfgpu
   CGStats cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol,
                      int maxit, int check = 8, DevBuf *ws = nullptr, double *host_rec = nullptr);
   CGStats lanczos_collect(const double *host_rec, int maxit, double tol);
+  // extreme eigenvalues of the Lanczos tridiagonal matrix of a recorded CG
+  // (the CG coefficients alpha, beta): {lambda_min, lambda_max}
+  std::pair<double, double> lanczos_extreme_eigenvalues(const CGStats &st);
 
   template <typename T>
   struct Chebyshev

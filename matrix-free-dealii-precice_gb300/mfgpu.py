@@ -50,7 +50,13 @@ class SolverParams(C.Structure):
                 ("cheb_eig_its", C.c_int), ("coarse_accurate", C.c_int),
                 ("mg_precision", C.c_int), ("coarse_fp64", C.c_int),
                 ("fp64_emulation", C.c_int),
-                ("cuda_graphs", C.c_int), ("coarse_dense", C.c_int)]
+                ("cuda_graphs", C.c_int), ("coarse_dense", C.c_int),
+                ("estimate_condition", C.c_int), ("cond_cg_iterations", C.c_int)]
+
+
+class MGParams(C.Structure):
+    _fields_ = [("kind", C.c_int), ("delta_t", C.c_double), ("caching", C.c_char_p),
+                ("material", Material), ("solver", SolverParams)]
 
 
 class SolidParams(C.Structure):
@@ -389,7 +395,8 @@ def prolongate_noalloc(mesh, coarse_level, nc, coarse, fine, precision=64,
 def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
                   cheb_degree=5, cheb_range=20.0, cheb_eig_its=30,
                   coarse_accurate=True, mg_precision=32, coarse_fp64=False,
-                  max_it_mult=1, fp64_emulation=False, cuda_graphs=True, coarse_dense=True):
+                  max_it_mult=1, fp64_emulation=False, cuda_graphs=True, coarse_dense=True,
+                  estimate_condition=False, cond_cg_iterations=20):
     s = SolverParams()
     s.preconditioner = {"none": 0, "jacobi": 1, "gmg": 2}[preconditioner]
     s.relaxation = relaxation
@@ -404,7 +411,115 @@ def solver_params(preconditioner="gmg", tol=1e-6, relaxation=0.65,
     s.fp64_emulation = int(fp64_emulation)
     s.cuda_graphs = int(cuda_graphs)
     s.coarse_dense = int(coarse_dense)
+    s.estimate_condition = int(estimate_condition)
+    s.cond_cg_iterations = cond_cg_iterations
     return s
+
+
+class Multigrid:
+    """PreconditionMG over the level hierarchy of a mesh (mfgpu_mg):
+    kind "heat" (LaplaceOperator levels, delta_t) or "nh" (NeoHookOperator
+    levels, caching and material)."""
+
+    def __init__(self, ctx, mesh, kind="nh", delta_t=0.1, caching="referential_qp",
+                 material=None, solver=None):
+        p = MGParams()
+        p.kind = {"heat": 0, "nh": 1}[kind]
+        p.delta_t = delta_t
+        self._caching = caching.encode()
+        p.caching = self._caching
+        p.material = material if material is not None else globals()["material"]()
+        p.solver = solver if solver is not None else solver_params("gmg")
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_mg_create(ctx.h, C.byref(mesh), C.byref(p), C.byref(self.h)))
+        ctx._adopt(self)
+
+    def setup(self, linearisation=None):
+        _check(lib().mfgpu_mg_setup(self.h, _ptr(linearisation) if linearisation is not None else None))
+
+    def vmult(self, dst, src):
+        _check(lib().mfgpu_mg_vmult(self.h, _ptr(dst), _ptr(src)))
+
+    def info(self):
+        nl, nd = C.c_int(), C.c_size_t()
+        _check(lib().mfgpu_mg_info(self.h, C.byref(nl), C.byref(nd)))
+        return nl.value, nd.value
+
+    def close(self):
+        if self.h:
+            _check(lib().mfgpu_mg_destroy(self.h))
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pcg_solve(op, x, b, tol, max_iterations, mg=None, jacobi_omega=0.0):
+    """SolverCG::solve under SolverControl(max_iterations, tol): (iterations,
+    final residual); x holds the initial guess."""
+    its, res = C.c_int(), C.c_double()
+    _check(lib().mfgpu_pcg_solve(op.h, mg.h if mg is not None else None, C.c_double(jacobi_omega),
+                                 _ptr(x), _ptr(b), C.c_double(tol), int(max_iterations),
+                                 C.byref(its), C.byref(res)))
+    return its.value, res.value
+
+
+def estimate_condition_number(op, b, n_iterations=20, tol=0.0):
+    c = C.c_double()
+    _check(lib().mfgpu_estimate_condition_number(op.h, _ptr(b), int(n_iterations), C.c_double(tol),
+                                                 C.byref(c)))
+    return c.value
+
+
+def dof_permutation(mesh, level, support_points, components=None, tol=1e-6):
+    """library_dof[i] of the caller's DoF i (host; numpy arrays)."""
+    import numpy as np
+    pts = np.ascontiguousarray(support_points, dtype=np.float64).reshape(-1, 3)
+    n = pts.shape[0]
+    comps = None if components is None else np.ascontiguousarray(components, dtype=np.uint32)
+    out = np.zeros(n, dtype=np.uint64)
+    _check(lib().mfgpu_dof_permutation(C.byref(mesh), level, C.c_size_t(n),
+                                       pts.ctypes.data_as(C.c_void_p),
+                                       comps.ctypes.data_as(C.c_void_p) if comps is not None else None,
+                                       C.c_double(tol), out.ctypes.data_as(C.c_void_p)))
+    return out
+
+
+class Permutation:
+    """The DoF map on the device (mfgpu_permutation)."""
+
+    def __init__(self, ctx, mesh, level, support_points, components=None, tol=1e-6):
+        import numpy as np
+        pts = np.ascontiguousarray(support_points, dtype=np.float64).reshape(-1, 3)
+        comps = None if components is None else np.ascontiguousarray(components, dtype=np.uint32)
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        _check(lib().mfgpu_permutation_create(ctx.h, C.byref(mesh), level, C.c_size_t(pts.shape[0]),
+                                              pts.ctypes.data_as(C.c_void_p),
+                                              comps.ctypes.data_as(C.c_void_p) if comps is not None else None,
+                                              C.c_double(tol), C.byref(self.h)))
+        ctx._adopt(self)
+
+    def to_library(self, src, dst, precision=64):
+        _check(lib().mfgpu_permutation_to_library(self.h, precision, _ptr(src), _ptr(dst)))
+
+    def from_library(self, src, dst, precision=64):
+        _check(lib().mfgpu_permutation_from_library(self.h, precision, _ptr(src), _ptr(dst)))
+
+    def close(self):
+        if self.h:
+            _check(lib().mfgpu_permutation_destroy(self.h))
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Solid:
@@ -454,6 +569,10 @@ class Solid:
 
     def timing_summary(self):
         return _text(lambda buf, n: lib().mfgpu_solid_timing_summary(self.h, buf, n))
+
+    def convergence_table(self):
+        """The Newton convergence table of the last time step."""
+        return _text(lambda buf, n: lib().mfgpu_solid_convergence_table(self.h, buf, n))
 
     def close(self):
         if self.h:
