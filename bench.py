@@ -791,6 +791,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
     res = [srv.wait(i) for i in ids]
     span = time.perf_counter() - t0
     max_running, budget = srv.stats()
+    reused, built = srv.pool_stats()
     srv.close()
     lat = np.array([r.latency_seconds for r in res])
     errors = sum(1 for r in res if r.status != 0)
@@ -823,6 +824,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
             "capacity_closed_loop_per_s": capacity,
             "solves_per_s": n_requests / span, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)), "max_concurrent": max_running,
+            "resident_problems": {"reused": reused, "built": built},
             "errors": errors,
             "closed_loop_first100_per_s": {"1_worker": one, f"{workers}_workers": many},
             "baseline_fp64_one_at_a_time": {"solves_per_s": n_requests / bspan,

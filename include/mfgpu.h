@@ -128,11 +128,23 @@ int mfgpu_heat_operator_evaluate_coefficient(mfgpu_operator *op,
 int mfgpu_nh_operator_create(mfgpu_context *ctx, const mfgpu_mesh *mesh,
                              int level, int precision, const char *caching,
                              mfgpu_operator **op);
-/* NeoHookOperator::set_material (mf_nh_operator.h:529-539); the inclusion
- * material may be NULL (all cells carry material id 0) */
+/* NeoHookOperator::set_material (mf_nh_operator.h:529-539): `material`
+ * applies to cells of material id 0, `inclusion` (may be NULL; the
+ * reference passes mu x 100, mf_elasticity.h:470-493) to the others
+ * (mf_nh_operator.h:402-404,656-658).  Box meshes carry material id 0 on
+ * every cell, as all of the reference's cases do, so the inclusion is
+ * stored and checked (same formulation) but applies to no cell. */
 int mfgpu_nh_operator_set_material(mfgpu_operator *op,
                                    const mfgpu_material *material,
                                    const mfgpu_material *inclusion);
+/* Material ids of the level's cells (n_cells bytes, cells numbered
+ * lexicographically, x fastest), as cell->material_id() gives them.  All
+ * zero is accepted (the default); a cell with a nonzero id, i.e. the
+ * inclusion material, returns MFGPU_ERR_UNSUPPORTED: the device cell
+ * kernels apply one material to every cell. */
+int mfgpu_nh_operator_set_cell_material_ids(mfgpu_operator *op,
+                                            const unsigned char *ids,
+                                            size_t n_cells);
 /* NeoHookOperator::initialize (mf_nh_operator.h:333-388): registers the
  * linearisation displacement (device pointer of the operator's precision,
  * NOT owned; keep it alive while the operator is used) */
@@ -473,11 +485,15 @@ int mfgpu_heat_destroy(mfgpu_heat *h);
 /* ---------------------------------------------------------------- */
 /* No counterpart in the reference (one problem per MPI job there).
  * Requests queue FIFO; a request starts when a worker is free and its
- * estimated device memory fits in the budget (memory_fraction of the free
- * HBM at creation).  Each worker owns a CUDA stream, so admitted solves
- * overlap on the device; a solve keeps its hierarchy resident until it
- * finishes.  Results do not depend on what else runs (deterministic
- * reductions; scatter round-off only). */
+ * estimated device memory fits in the budget (half of memory_fraction of
+ * the free HBM at creation).  Each worker owns a CUDA stream, so admitted
+ * solves overlap on the device; a solve keeps its hierarchy resident until
+ * it finishes, and afterwards in its worker's pool of resident problems
+ * (the other half of the budget, split among the workers): a later
+ * request of the same shape (everything but its loads) reuses operators,
+ * multigrid setup and buffers.  A free worker prefers, among the first 8
+ * queued requests, one whose shape it holds.  Results do not depend on
+ * what else runs (deterministic reductions; scatter round-off only). */
 typedef struct mfgpu_server mfgpu_server;
 
 typedef struct mfgpu_request
@@ -512,6 +528,10 @@ int mfgpu_server_wait(mfgpu_server *server, long long id,
 /* highest number of solves that ran at the same time; memory budget */
 int mfgpu_server_stats(mfgpu_server *server, int *max_running,
                        size_t *budget_bytes);
+/* requests that reused a resident problem of their shape, and requests
+ * that built a new one */
+int mfgpu_server_pool_stats(mfgpu_server *server, long long *reused,
+                            long long *built);
 /* finishes queued requests, then stops the workers */
 int mfgpu_server_destroy(mfgpu_server *server);
 

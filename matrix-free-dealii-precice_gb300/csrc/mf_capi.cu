@@ -197,7 +197,10 @@ extern "C"
   {
     return guarded([&] {
       need(material, "material");
-      (void)inclusion; // every cell carries material id 0 on box meshes
+      if (inclusion && inclusion->formulation != material->formulation)
+        throw Error(ERR_UNSUPPORTED, "the inclusion material must use the formulation of the material");
+      if (inclusion && !(inclusion->mu > 0 && inclusion->nu > -1 && inclusion->nu < 0.5))
+        throw Error(ERR_ARG, "inclusion material: mu > 0 and -1 < nu < 0.5 required");
       NHOperator *h    = as_nh(op);
       h->mat           = make_material(material->mu, material->nu, material->rho, material->alpha_1);
       h->formulation   = material->formulation;
@@ -205,6 +208,22 @@ extern "C"
         throw Error(ERR_ARG, "Unknown material formulation");
       h->have_material = true;
       h->cached        = false;
+    });
+  }
+
+  int
+  mfgpu_nh_operator_set_cell_material_ids(mfgpu_operator *op, const unsigned char *ids, size_t n_cells)
+  {
+    return guarded([&] {
+      NHOperator *h = as_nh(op);
+      need(ids, "ids");
+      if (n_cells != h->geom.n_cells)
+        throw Error(ERR_ARG, "n_cells must be the level's cell count (" + std::to_string(h->geom.n_cells) + ")");
+      for (size_t c = 0; c < n_cells; ++c)
+        if (ids[c] != 0)
+          throw Error(ERR_UNSUPPORTED, "cell " + std::to_string(c) +
+                                         " carries a nonzero material id (the inclusion material): the device "
+                                         "cell kernels apply one material to all cells");
     });
   }
 

@@ -323,6 +323,7 @@ namespace mfgpu
     P.material.alpha_1 = a1;
     mat      = make_material(P.material.mu, P.material.nu, P.material.rho, a1);
     variant  = parse_caching(P.caching);
+    P.caching = nullptr; // parsed into variant; the caller's string need not outlive the driver
     if (P.material.formulation != 0 && P.material.formulation != 1)
       throw Error(ERR_ARG, "formulation must be 0 or 1");
     fine                = make_nh(ctx, mesh, -1, 64, variant);
@@ -536,6 +537,20 @@ namespace mfgpu
               r[c] += lag(i, xi[0]) * lag(j, xi[1]) * lz * h[size_t(c) * g.n_nodes + node];
             }
     return r;
+  }
+
+  void
+  SolidDriver::reset(const mfgpu_solid_params &p)
+  {
+    const double a1 = P.material.alpha_1;
+    P               = p;
+    P.material.alpha_1 = a1;
+    P.caching          = nullptr;
+    const size_t n     = fine->m();
+    for (DevBuf *b : {&u, &delta, &v_old, &a_old, &acc, &rhs, &du})
+      MF_CK(cudaMemsetAsync(b->ptr, 0, n * sizeof(double), ctx->stream));
+    step_no = 0;
+    table.clear();
   }
 
   void
@@ -778,6 +793,18 @@ namespace mfgpu
     vec_axpbyz<double>(*ctx, n, 1.0, uD.as<double>(), 1.0, du.as<double>(), sol.as<double>());
     vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
     return st.its;
+  }
+
+  void
+  HeatDriver::reset(const mfgpu_heat_params &p)
+  {
+    P              = p;
+    const size_t n = op->m();
+    for (DevBuf *b : {&sol, &sol_old, &rhs, &du, &uD})
+      MF_CK(cudaMemsetAsync(b->ptr, 0, n * sizeof(double), ctx->stream));
+    started = false;
+    step_no = 0;
+    t       = 0;
   }
 
   void

@@ -101,6 +101,11 @@ namespace mfgpu
     // one time step: Newton-Newmark iterations, velocity update, watchpoint
     void step(int &newton_its, long &total_cg, int &n_solves, double *watch);
     int  step_no = 0;
+    // a new problem of the same shape (mesh, material, caching, solver and
+    // Newton parameters, time step): the state starts from rest again and
+    // the loads, watchpoint and step count are p's; the operators, the
+    // multigrid hierarchy and every device buffer are kept
+    void reset(const mfgpu_solid_params &p);
   };
 
   struct HeatDriver
@@ -125,5 +130,10 @@ namespace mfgpu
     void start();          // initial condition, diagonals
     int  step();           // one backward-Euler step; returns CG iterations
     void run(mfgpu_heat_result &res);
+    // a new problem of the same shape (mesh, time step, solver parameters):
+    // the source / analytic data and step count are p's and the solution
+    // starts from zero; operators, diagonals, smoothers and the captured
+    // V-cycle are kept
+    void reset(const mfgpu_heat_params &p);
   };
 } // namespace mfgpu

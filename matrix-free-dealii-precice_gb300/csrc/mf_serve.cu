@@ -1,18 +1,27 @@
 // Request server: independent heat and neo-Hookean solves on one GPU.
 //
 // Requests are queued FIFO.  A request is admitted when its estimated
-// device memory fits in the remaining budget (a fraction of the free HBM
-// at server start) and a worker is free.  Every worker owns a context with
-// its own CUDA stream, so admitted solves run concurrently and their
-// kernels overlap on the device.  A solve keeps its geometry, multigrid
-// hierarchy and vectors resident in HBM for its lifetime and releases
-// them (and its budget) when it finishes.  Latency = completion time -
-// submit time.
+// device memory fits in the remaining budget (half of the memory fraction
+// of the free HBM at server start) and a worker is free.  Every worker owns
+// a context with its own CUDA stream, so admitted solves run concurrently
+// and their kernels overlap on the device.  A solve keeps its geometry,
+// multigrid hierarchy and vectors resident in HBM for its lifetime.
+//
+// Problems stay resident after they finish: each worker keeps the drivers
+// of the shapes it solved (mesh, degree, material, solver parameters, time
+// step) in a pool with its own memory cap (the other half of the budget,
+// split among the workers; least recently used first out).  A request of a
+// pooled shape takes that driver and only resets its loads and state: no
+// allocation, no operator or transfer construction, and for the heat
+// problem no diagonal, no eigenvalue estimate and no V-cycle capture.  A
+// free worker prefers, among the first queued requests, one whose shape it
+// holds.  Latency = completion time - submit time.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <list>
 #include <map>
 #include <mutex>
 #include <string>
@@ -30,6 +39,7 @@ namespace mfgpu
     long long            id;
     mfgpu_request        req;
     std::string          caching; // keeps req.solid.caching alive
+    std::string          shape;   // pool key
     size_t               bytes = 0;
     clock_t_::time_point t_submit, t_start, t_end;
     mfgpu_request_result res{};
@@ -58,6 +68,72 @@ namespace mfgpu
     return size_t(nd * 8 * 15 + nq * 80 * ml + nd * ml * 4 * 10 + (64 << 20));
   }
 
+  // the shape of a request: everything but its loads (heat source or
+  // analytic data, solid traction and body force), watchpoint and step
+  // count; requests of one shape share operators and multigrid setups
+  template <typename V>
+  void
+  put(std::string &k, const V &v)
+  {
+    k.append(reinterpret_cast<const char *>(&v), sizeof(V));
+  }
+
+  void
+  put_mesh(std::string &k, const mfgpu_mesh &m)
+  {
+    put(k, m.degree), put(k, m.n_q_1d), put(k, m.n_refinements), put(k, m.dim), put(k, m.n_dirichlet);
+    for (int d = 0; d < 3; ++d)
+      put(k, m.repetitions[d]), put(k, m.lower[d]), put(k, m.upper[d]);
+    for (int f = 0; f < 6; ++f)
+      put(k, m.boundary_id[f]);
+    for (int i = 0; i < m.n_dirichlet && i < 8; ++i)
+      put(k, m.dirichlet_id[i]), put(k, m.dirichlet_mask[i]);
+  }
+
+  void
+  put_solver(std::string &k, const mfgpu_solver_params &s)
+  {
+    put(k, s.preconditioner), put(k, s.relaxation), put(k, s.tol), put(k, s.max_it_mult);
+    put(k, s.cheb_degree), put(k, s.cheb_range), put(k, s.cheb_eig_its), put(k, s.coarse_accurate);
+    put(k, s.mg_precision), put(k, s.coarse_fp64), put(k, s.fp64_emulation), put(k, s.cuda_graphs);
+    put(k, s.coarse_dense), put(k, s.estimate_condition), put(k, s.cond_cg_iterations);
+  }
+
+  std::string
+  request_shape(const mfgpu_request &r, const std::string &caching)
+  {
+    std::string k;
+    put(k, r.kind);
+    if (r.kind == 0)
+      {
+        put_mesh(k, r.heat.mesh);
+        put(k, r.heat.dt);
+        put_solver(k, r.heat.solver);
+      }
+    else
+      {
+        const mfgpu_solid_params &p = r.solid;
+        put_mesh(k, p.mesh);
+        put(k, p.material.mu), put(k, p.material.nu), put(k, p.material.rho), put(k, p.material.formulation);
+        k += caching;
+        k.push_back('\0');
+        put_solver(k, p.solver);
+        put(k, p.max_newton), put(k, p.tol_f), put(k, p.tol_f_abs), put(k, p.tol_u), put(k, p.tol_u_abs);
+        put(k, p.dt), put(k, p.traction_id);
+      }
+    return k;
+  }
+
+  // a resident problem kept by a worker between requests
+  struct PoolEntry
+  {
+    std::string                  shape;
+    std::string                  caching; // the solid driver's caching string
+    std::unique_ptr<HeatDriver>  heat;
+    std::unique_ptr<SolidDriver> solid;
+    size_t                       bytes = 0;
+  };
+
   struct Server
   {
     int                                   device;
@@ -71,6 +147,10 @@ namespace mfgpu
     bool                                  stop = false;
     long long                             next_id = 1;
     int                                   running = 0, max_running = 0;
+    size_t                                pool_cap = 0; // per worker
+    long long                             reused = 0, built = 0;
+    // how far down the queue a free worker looks for a shape it holds
+    static constexpr int                  LOOKAHEAD = 8;
 
     Server(int dev, int nw, double fraction)
       : device(dev)
@@ -79,7 +159,9 @@ namespace mfgpu
       MF_CK(cudaSetDevice(dev));
       size_t free_b = 0, total_b = 0;
       MF_CK(cudaMemGetInfo(&free_b, &total_b));
-      budget = size_t(double(free_b) * fraction);
+      const size_t all = size_t(double(free_b) * fraction);
+      budget           = all / 2;
+      pool_cap         = all / 2 / size_t(nw);
       for (int i = 0; i < nw; ++i)
         workers.emplace_back([this] { loop(); });
     }
@@ -111,28 +193,44 @@ namespace mfgpu
         {
           ctx_error = e.what();
         }
+      std::list<PoolEntry> pool; // this worker's resident problems, most recent first
+      size_t               pool_bytes = 0;
+      auto                 holds = [&](const std::string &shape) {
+        for (const PoolEntry &e : pool)
+          if (e.shape == shape)
+            return true;
+        return false;
+      };
       for (;;)
         {
           ServerJob *job = nullptr;
           {
             std::unique_lock<std::mutex> l(mu);
-            cv_work.wait(l, [&] {
-              return stop || (!queue.empty() && reserved + queue.front()->bytes <= budget) ||
-                     (!queue.empty() && running == 0); // a job larger than the budget runs alone
-            });
+            auto fits = [&](const ServerJob *j) {
+              return reserved + j->bytes <= budget || running == 0; // a job larger than the budget runs alone
+            };
+            cv_work.wait(l, [&] { return stop || (!queue.empty() && fits(queue.front())); });
             if (stop && queue.empty())
               return;
             if (queue.empty())
               continue;
-            job = queue.front();
-            queue.pop_front();
+            auto pick = queue.begin();
+            int  look = 0;
+            for (auto it = queue.begin(); it != queue.end() && look < LOOKAHEAD; ++it, ++look)
+              if (fits(*it) && holds((*it)->shape))
+                {
+                  pick = it;
+                  break;
+                }
+            job = *pick;
+            queue.erase(pick);
             reserved += job->bytes;
             ++running;
             max_running = std::max(max_running, running);
             job->t_start = clock_t_::now();
           }
           if (ctx)
-            run(*ctx, *job);
+            run(*ctx, *job, pool, pool_bytes);
           else
             {
               job->res.status = MFGPU_ERR_CUDA;
@@ -155,14 +253,29 @@ namespace mfgpu
     }
 
     void
-    run(Context &ctx, ServerJob &job)
+    run(Context &ctx, ServerJob &job, std::list<PoolEntry> &pool, size_t &pool_bytes)
     {
       mfgpu_request_result &r = job.res;
+      // the resident problem of this shape, or a new one
+      PoolEntry e;
+      for (auto it = pool.begin(); it != pool.end(); ++it)
+        if (it->shape == job.shape)
+          {
+            e = std::move(*it);
+            pool.erase(it);
+            pool_bytes -= e.bytes;
+            break;
+          }
+      const bool reuse = e.heat || e.solid;
       try
         {
           if (job.req.kind == 0)
             {
-              HeatDriver        d(&ctx, job.req.heat);
+              if (reuse)
+                e.heat->reset(job.req.heat);
+              else
+                e.heat.reset(new HeatDriver(&ctx, job.req.heat));
+              HeatDriver       &d = *e.heat;
               mfgpu_heat_result hr;
               d.run(hr);
               int its = 0;
@@ -176,9 +289,16 @@ namespace mfgpu
           else
             {
               mfgpu_solid_params p = job.req.solid;
-              p.caching            = job.caching.c_str();
-              SolidDriver         d(&ctx, p);
-              mfgpu_solid_result  sr;
+              if (reuse)
+                e.solid->reset(p);
+              else
+                {
+                  e.caching = job.caching;
+                  p.caching = e.caching.c_str();
+                  e.solid.reset(new SolidDriver(&ctx, p));
+                }
+              SolidDriver       &d = *e.solid;
+              mfgpu_solid_result sr;
               d.run(sr);
               r.cg_iterations     = int(sr.total_cg);
               r.newton_iterations = 0;
@@ -191,16 +311,33 @@ namespace mfgpu
               r.n_dofs        = double(n);
             }
           r.status = MFGPU_OK;
+          {
+            std::lock_guard<std::mutex> l(mu);
+            (reuse ? reused : built) += 1;
+          }
+          // keep the problem resident, within this worker's cap
+          e.shape = job.shape;
+          e.bytes = job.bytes;
+          if (e.bytes <= pool_cap)
+            {
+              pool.push_front(std::move(e));
+              pool_bytes += job.bytes;
+              while (pool_bytes > pool_cap && !pool.empty())
+                {
+                  pool_bytes -= pool.back().bytes;
+                  pool.pop_back();
+                }
+            }
         }
-      catch (const Error &e)
+      catch (const Error &e2)
         {
-          r.status = e.code;
-          std::strncpy(r.message, e.what(), sizeof(r.message) - 1);
+          r.status = e2.code;
+          std::strncpy(r.message, e2.what(), sizeof(r.message) - 1);
         }
-      catch (const std::exception &e)
+      catch (const std::exception &e2)
         {
           r.status = MFGPU_ERR_ARG;
-          std::strncpy(r.message, e.what(), sizeof(r.message) - 1);
+          std::strncpy(r.message, e2.what(), sizeof(r.message) - 1);
         }
     }
 
@@ -217,6 +354,7 @@ namespace mfgpu
       else if (req.kind != 0)
         throw Error(ERR_ARG, "request kind must be 0 (heat) or 1 (solid)");
       j->bytes    = estimate_request_bytes(req);
+      j->shape    = request_shape(req, j->caching);
       j->t_submit = clock_t_::now();
       std::lock_guard<std::mutex> l(mu);
       const long long id = next_id++;
@@ -328,6 +466,22 @@ extern "C"
       *max_running = server->s->max_running;
     if (budget_bytes)
       *budget_bytes = server->s->budget;
+    return MFGPU_OK;
+  }
+
+  int
+  mfgpu_server_pool_stats(mfgpu_server *server, long long *reused, long long *built)
+  {
+    if (!server)
+      {
+        set_last_error("server_pool_stats: null argument");
+        return MFGPU_ERR_ARG;
+      }
+    std::lock_guard<std::mutex> l(server->s->mu);
+    if (reused)
+      *reused = server->s->reused;
+    if (built)
+      *built = server->s->built;
     return MFGPU_OK;
   }
 

@@ -355,6 +355,12 @@ class NeoHookOperator(_Operator):
         _check(lib().mfgpu_nh_operator_set_material(
             self.h, C.byref(mat), C.byref(inclusion) if inclusion else None))
 
+    def set_cell_material_ids(self, ids):
+        import numpy as np
+        a = np.ascontiguousarray(ids, dtype=np.uint8)
+        _check(lib().mfgpu_nh_operator_set_cell_material_ids(self.h, a.ctypes.data_as(C.c_void_p),
+                                                               C.c_size_t(a.size)))
+
     def initialize(self, displacement):
         self._u = displacement  # keep the linearisation alive
         _check(lib().mfgpu_nh_operator_initialize(self.h, _ptr(displacement)))
@@ -656,6 +662,12 @@ class Server:
         b = C.c_size_t()
         _check(lib().mfgpu_server_stats(self.h, C.byref(mr), C.byref(b)))
         return mr.value, b.value
+
+    def pool_stats(self):
+        """(requests that reused a resident problem, requests that built one)"""
+        reused, built = C.c_longlong(), C.c_longlong()
+        _check(lib().mfgpu_server_pool_stats(self.h, C.byref(reused), C.byref(built)))
+        return reused.value, built.value
 
     def close(self):
         if self.h:

@@ -178,7 +178,7 @@ def test_solid_condition_estimate_changes_no_result(ctx):
     (n1, cg1, sol1, w1), t1 = run(True)
     # equal up to the round-off of the atomic scatter
     assert (n0, sol0) == (n1, sol1) and abs(cg0 - cg1) <= sol0
-    assert np.allclose(w0, w1, rtol=1e-9, atol=0)
+    assert np.linalg.norm(np.array(w1) - np.array(w0)) <= 1e-9 * np.linalg.norm(w0)
     rows0 = [r for r in t0.splitlines() if "|" in r and "LIN_IT" not in r]
     rows1 = [r for r in t1.splitlines() if "|" in r and "LIN_IT" not in r]
     assert len(rows0) == len(rows1) == n0 and "CONVERGED" in t1
@@ -223,3 +223,42 @@ def test_permutation_on_the_device(ctx):
     perm.from_library(yl, yc)
     assert np.array_equal(host(yc), host(yl)[lib_index])
     perm.close()
+
+
+def test_inclusion_material_and_material_ids(ctx):
+    """set_material(material, inclusion) as the reference calls it (the
+    inclusion with mu x 100, mf_elasticity.h:470-493): with every cell of
+    material id 0 the inclusion applies to no cell and the vmult is the
+    one without it; a nonzero material id is refused with
+    MFGPU_ERR_UNSUPPORTED, as is an inclusion of another formulation."""
+    import torch
+    spec = W.cantilever(2, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    mesh = W.to_lib_mesh(mfgpu, spec)
+    n = W.n_dofs(spec, 3)
+    u = dev(W.smooth_displacement(2, 1, spec["rep"], spec["lo"], spec["hi"], seed=2))
+    src = dev(W.uniform_vector(n, 3))
+    out = []
+    for with_inclusion in (False, True):
+        op = mfgpu.NeoHookOperator(ctx, mesh, -1, 64, "referential_qp")
+        op.set_scatter("colored")
+        mat = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+        op.set_material(mat, mfgpu.material(0.5e8, 0.4, 1000.0, 0.01) if with_inclusion else None)
+        op.set_cell_material_ids(np.zeros(32, dtype=np.uint8))
+        op.initialize(u)
+        op.cache()
+        d = torch.zeros_like(src)
+        op.vmult(d, src)
+        out.append(host(d))
+        ids = np.zeros(32, dtype=np.uint8)
+        ids[5] = 1
+        with pytest.raises(mfgpu.MfgpuError) as e:
+            op.set_cell_material_ids(ids)
+        assert e.value.code == 8
+        with pytest.raises(mfgpu.MfgpuError) as e:
+            op.set_cell_material_ids(np.zeros(31, dtype=np.uint8))
+        assert e.value.code == 1
+        with pytest.raises(mfgpu.MfgpuError) as e:
+            op.set_material(mat, mfgpu.material(0.5e8, 0.4, 1000.0, 0.01, formulation=0))
+        assert e.value.code == 8
+        op.close()
+    assert np.array_equal(out[0], out[1])

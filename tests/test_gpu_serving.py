@@ -50,3 +50,38 @@ def test_request_errors_are_reported_per_request(ctx):
     srv.close()
     assert res[0].status == 0 and res[1].status == 0
     assert res[2].status == 1 and b"caching" in res[2].message
+
+
+def test_resident_problems_are_reused_with_the_same_results(ctx):
+    """A worker keeps the problems it solved: a second request of the same
+    shape (another source or traction) reuses the driver, and the result
+    equals that of a fresh server solving the request alone."""
+    reqs = W.serving_requests(mfgpu, 6, seed=11, max_heat_ref=4, solid_k=(2,), degrees=(2,))
+    # two rounds of the same shapes: the second round's loads differ
+    again = W.serving_requests(mfgpu, 6, seed=12, max_heat_ref=4, solid_k=(2,), degrees=(2,))
+    srv = mfgpu.Server(0, 1, 0.5)
+    first = [srv.wait(srv.submit(r)) for r in reqs]
+    assert srv.pool_stats()[0] >= 0
+    built_before = srv.pool_stats()[1]
+    # the same requests once more: every shape is resident now
+    second = [srv.wait(srv.submit(r)) for r in reqs]
+    reused, built = srv.pool_stats()
+    assert built == built_before and reused >= len(reqs)
+    srv.close()
+    for a, b in zip(first, second):
+        assert a.status == 0 and b.status == 0
+        assert abs(a.cg_iterations - b.cg_iterations) <= 1
+        assert a.newton_iterations == b.newton_iterations
+        assert abs(a.solution_norm - b.solution_norm) <= 1e-9 * abs(a.solution_norm)
+    # other loads on resident shapes equal a fresh server's results
+    srv = mfgpu.Server(0, 1, 0.5)
+    for r in reqs:
+        srv.wait(srv.submit(r))
+    pooled = [srv.wait(srv.submit(r)) for r in again]
+    srv.close()
+    fresh, _ = run_all(again, 1)
+    for a, b in zip(pooled, fresh):
+        assert a.status == 0 and b.status == 0
+        assert abs(a.cg_iterations - b.cg_iterations) <= 1
+        assert a.newton_iterations == b.newton_iterations
+        assert abs(a.solution_norm - b.solution_norm) <= 1e-9 * abs(a.solution_norm)
