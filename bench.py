@@ -617,8 +617,9 @@ def extra_solid_newton(mfgpu, W, ctx):
 def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
     """Heat operator on the unit cube with 64^3 cells, Q1..Q6: vmult DoF/s
     and achieved GB/s (B_alg = 2 s N_dof + 4 s N_cells) in FP64 (native and
-    double-float) and FP32; FP32-GMG vs FP64-GMG CG to 1e-8 with the seeded
-    Gaussian source."""
+    double-float) and FP32 (sum factorization on the CUDA cores, and for
+    Q1..Q5 the element-matrix product on the tensor cores); FP32-GMG vs
+    FP64-GMG CG to 1e-8 with the seeded Gaussian source."""
     res = []
     c, w, a = W.gaussian_source(0)
     for deg in range(1, 7):
@@ -627,11 +628,16 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
         n = W.n_dofs(spec, 1)
         cells = 64 ** 3
         row = {"degree": deg, "n_dofs": n}
-        for label, prec, emul in (("fp64", 64, False), ("fp64_df64", 64, True), ("fp32", 32, False)):
+        for label, prec, emul in (("fp64", 64, False), ("fp64_df64", 64, True), ("fp32", 32, False),
+                                  ("fp32_tensor", 32, False)):
+            if label == "fp32_tensor" and deg > 5:
+                continue
             dt = torch.float64 if prec == 64 else torch.float32
             op = mfgpu.LaplaceOperator(ctx, mesh, -1, prec, True, delta_t=0.1)
             if emul:
                 op.set_fp64_emulation(True)
+            if label == "fp32_tensor":
+                op.set_cell_kernel("tensor")
             src = torch.rand(n, dtype=dt, device=dev) * 2 - 1
             dst = torch.zeros_like(src)
             op.vmult(dst, src)
@@ -669,7 +675,8 @@ def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src,
     cantilever 64x8x8, 839,619 DoFs), L2 flushed before every application:
     * scatter: atomic adds vs 8 parity colours with plain adds;
     * quadrature data: each caching variant of the tangent in native FP64
-      (streamed bytes vs recomputation), referential_qp also in FP32;
+      (streamed bytes vs recomputation), referential_qp also in FP32, and
+      both referential cachings on the FP32 Q3 level of the mixed solve;
     * host-buffer vmult: number of overlapped z-slabs (1 = no overlap)."""
     out = {"scatter": {}, "caching_fp64": {}, "host_slabs": {}}
     dst = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -712,6 +719,28 @@ def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src,
                 "ms": t * 1e3, "dofs_per_s": n / t, "cache_mb": cop.memory_consumption() / 1e6}
             cop.close()
             del s2, d2, uu
+    # the finest multigrid level of the mixed solve (cantilever 128x16x16 cells
+    # Q3, 2,773,155 DoFs, FP32): streamed referential_qp cache (10 values per
+    # quadrature point) against scalar_referential (1 value per quadrature
+    # point, the second gradient recomputed from the cell's displacement)
+    q3 = W.cantilever(3, 4)
+    q3m = W.to_lib_mesh(mfgpu, q3)
+    nq3 = W.n_dofs(q3, 3)
+    uq3 = torch.from_numpy(W.smooth_displacement(3, 4, q3["rep"], q3["lo"], q3["hi"], seed=2)).to(dev).float()
+    sq3 = torch.rand(nq3, dtype=torch.float32, device=dev) * 2 - 1
+    dq3 = torch.zeros_like(sq3)
+    out["caching_fp32_q3_level"] = {}
+    for caching in ("referential_qp", "scalar_referential"):
+        cop = mfgpu.NeoHookOperator(ctx, q3m, -1, 32, caching)
+        cop.set_material(mat)
+        cop.initialize(uq3)
+        cop.cache()
+        cop.vmult(dq3, sq3)
+        t = _timed_vmults(torch, cop, dq3, sq3, flush, stream, 10)
+        out["caching_fp32_q3_level"][caching] = {"ms": t * 1e3, "dofs_per_s": nq3 / t,
+                                                 "cache_mb": cop.memory_consumption() / 1e6}
+        cop.close()
+    del uq3, sq3, dq3
     K = 20
     for chunks in (1, 2, 4, 8):
         op.set_host_chunks(chunks)
@@ -880,6 +909,9 @@ KERNEL_CASES = {
     "heat_fp32_q2": ("heat", 2, 6, 32, "native"),  # unit cube 64^3 cells
     "heat_fp32_q6": ("heat", 6, 6, 32, "native"),
     "heat_fp64_q2": ("heat", 2, 6, 64, "native"),
+    "heat_fp32_q2_tensor": ("heat", 2, 6, 32, "tensor"),  # element matrix on the tensor cores
+    "heat_fp32_q3_tensor": ("heat", 3, 6, 32, "tensor"),
+    "heat_fp32_q4_tensor": ("heat", 4, 6, 32, "tensor"),
 }
 
 
@@ -910,6 +942,8 @@ def run_kernel_case(args):
         spec = W.unit_cube_heat(deg, nref)
         n = W.n_dofs(spec, 1)
         op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, prec, True, delta_t=0.1)
+        if arith == "tensor":
+            op.set_cell_kernel("tensor")
     src = torch.from_numpy(W.uniform_vector(n, 3)).to(dev).to(dt)
     dst = torch.zeros_like(src)
     for _ in range(max(args.steps, 1)):

@@ -192,7 +192,10 @@ int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
 int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
 /* cell kernel of vmult: 0 by grid size (default: point-parallel, one
  * thread per quadrature point, below 1024 cells, up to 4096 in native
- * FP64; line-parallel above), 1 line-parallel, 2 point-parallel.  The
+ * FP64; line-parallel above), 1 line-parallel, 2 point-parallel,
+ * 3 tensor cores (three-dimensional FP32 heat operators, degree 1..5: the
+ * cells' common element matrix applied to batches of 128 cells by
+ * tcgen05.mma in TF32 with a three-term split, FP32 accuracy).  The
  * results agree to round-off. */
 int mfgpu_operator_set_cell_kernel(mfgpu_operator *op, int mode);
 /* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
@@ -486,14 +489,16 @@ int mfgpu_heat_destroy(mfgpu_heat *h);
 /* No counterpart in the reference (one problem per MPI job there).
  * Requests queue FIFO; a request starts when a worker is free and its
  * estimated device memory fits in the budget (half of memory_fraction of
- * the free HBM at creation).  Each worker owns a CUDA stream, so admitted
- * solves overlap on the device; a solve keeps its hierarchy resident until
- * it finishes, and afterwards in its worker's pool of resident problems
- * (the other half of the budget, split among the workers): a later
- * request of the same shape (everything but its loads) reuses operators,
- * multigrid setup and buffers.  A free worker prefers, among the first 8
- * queued requests, one whose shape it holds.  Results do not depend on
- * what else runs (deterministic reductions; scatter round-off only). */
+ * the free HBM at creation).  Every problem runs on its own CUDA stream,
+ * so admitted solves overlap on the device; a solve keeps its hierarchy
+ * resident until
+ * it finishes, and afterwards in the server's pool of resident problems
+ * (the other half of the budget, shared by the workers): a later request
+ * of the same shape
+ * (everything but its loads) reuses operators, multigrid setup and
+ * buffers.  A free worker prefers, among the first 16 queued requests, one
+ * whose shape is resident.  Results do not depend on what else runs
+ * (deterministic reductions; scatter round-off only). */
 typedef struct mfgpu_server mfgpu_server;
 
 typedef struct mfgpu_request

@@ -333,8 +333,16 @@ extern "C"
   {
     return guarded([&] {
       need(op, "op");
-      if (mode < 0 || mode > 2)
-        throw Error(ERR_ARG, "cell kernel must be 0 (by grid size), 1 (line) or 2 (point)");
+      if (mode < 0 || mode > 3)
+        throw Error(ERR_ARG, "cell kernel must be 0 (by grid size), 1 (line), 2 (point) or 3 (tensor cores)");
+      if (mode == 3)
+        {
+          Operator *o = op->op.get();
+          if (!dynamic_cast<HeatOperator *>(o) || o->precision != 32 || o->geom.dim != 3 ||
+              !heat_em_supported(o->basis.N))
+            throw Error(ERR_UNSUPPORTED,
+                        "the tensor-core cell kernel applies to three-dimensional FP32 heat operators of degree 1..5");
+        }
       op->op->cell_kernel = mode;
     });
   }

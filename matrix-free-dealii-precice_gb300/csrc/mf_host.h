@@ -287,7 +287,8 @@ namespace mfgpu
     bool      constrained = true;
     int       arith       = 0; // 0 native, 1 double-float (FP64 operators only)
     int       scatter     = 0; // 0 atomic adds, 1 parity colours with plain adds (deterministic)
-    int       cell_kernel = 0; // 0 by grid size, 1 line-parallel, 2 point-parallel (ApplyArgs::kernel)
+    int       cell_kernel = 0; // 0 by grid size, 1 line-parallel, 2 point-parallel (ApplyArgs::kernel),
+                               // 3 element matrix on the tensor cores (FP32 heat, degree <= 5)
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;
@@ -352,6 +353,11 @@ namespace mfgpu
   {
     double    delta_t     = 0;
     double    coefficient = 1;
+    // the element matrix in the tensor-core kernel's layout (mf_heat_em.cu),
+    // for the vmult_state() it was built for
+    DevBuf    em_mat;
+    size_t    em_key = 0;
+    const void *element_matrix();
     ApplyArgs cell_args() const override;
     void      compute_diagonal() override;
     size_t    vmult_state() const override;

@@ -743,6 +743,16 @@ namespace mfgpu
         count_launch();
         return;
       }
+    if (a.kernel == 3 && !a.colored)
+      {
+        auto *h = dynamic_cast<HeatOperator *>(this);
+        if (!h || precision != 32 || !heat_em_supported(basis.N))
+          throw Error(ERR_UNSUPPORTED, "the tensor-core cell kernel applies to FP32 heat operators of degree 1..5");
+        MF_CK(launch_heat_em(basis, geom, constrained, h->element_matrix(), static_cast<const float *>(src),
+                             static_cast<float *>(dst), c0, c1, ctx->err.as<int>(), s));
+        count_launch();
+        return;
+      }
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, s) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, s) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, s);
@@ -1095,6 +1105,21 @@ namespace mfgpu
     a.constrained = constrained;
     a.kdt         = coefficient * delta_t;
     return a;
+  }
+
+  const void *
+  HeatOperator::element_matrix()
+  {
+    const size_t key = vmult_state();
+    if (em_mat.ptr && em_key == key)
+      return em_mat.ptr;
+    std::vector<unsigned char> h;
+    heat_em_matrix(basis, geom, coefficient * delta_t, h);
+    em_mat.ensure(h.size());
+    MF_CK(cudaMemcpyAsync(em_mat.ptr, h.data(), h.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MF_CK(cudaStreamSynchronize(ctx->stream));
+    em_key = key;
+    return em_mat.ptr;
   }
 
   void

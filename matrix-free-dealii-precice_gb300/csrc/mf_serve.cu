@@ -7,15 +7,18 @@
 // and their kernels overlap on the device.  A solve keeps its geometry,
 // multigrid hierarchy and vectors resident in HBM for its lifetime.
 //
-// Problems stay resident after they finish: each worker keeps the drivers
-// of the shapes it solved (mesh, degree, material, solver parameters, time
-// step) in a pool with its own memory cap (the other half of the budget,
-// split among the workers; least recently used first out).  A request of a
-// pooled shape takes that driver and only resets its loads and state: no
+// Problems stay resident after they finish: a resident problem is a driver
+// together with its own context (CUDA stream, reduction buffers), kept in
+// one pool shared by the workers with its own memory cap (the other half of
+// the budget; least recently used first out).  A request of a pooled shape
+// (mesh, degree, material, solver parameters, time step) checks that
+// problem out, resets its loads and state and runs it on its stream: no
 // allocation, no operator or transfer construction, and for the heat
-// problem no diagonal, no eigenvalue estimate and no V-cycle capture.  A
-// free worker prefers, among the first queued requests, one whose shape it
-// holds.  Latency = completion time - submit time.
+// problem no diagonal, no eigenvalue estimate and no V-cycle capture.
+// Workers are host threads; concurrency on the device comes from the
+// problems' streams.  A free worker prefers, among the first queued
+// requests, one whose shape is resident and free.  Latency = completion
+// time - submit time.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -124,14 +127,24 @@ namespace mfgpu
     return k;
   }
 
-  // a resident problem kept by a worker between requests
+  // a resident problem kept between requests: the driver and the context
+  // it runs on (members in this order: the driver goes first)
   struct PoolEntry
   {
+    std::unique_ptr<Context>     ctx;
     std::string                  shape;
     std::string                  caching; // the solid driver's caching string
     std::unique_ptr<HeatDriver>  heat;
     std::unique_ptr<SolidDriver> solid;
     size_t                       bytes = 0;
+    ~PoolEntry()
+    {
+      heat.reset();
+      solid.reset();
+    }
+    PoolEntry() = default;
+    PoolEntry(PoolEntry &&) = default;
+    PoolEntry &operator=(PoolEntry &&) = default;
   };
 
   struct Server
@@ -147,10 +160,12 @@ namespace mfgpu
     bool                                  stop = false;
     long long                             next_id = 1;
     int                                   running = 0, max_running = 0;
-    size_t                                pool_cap = 0; // per worker
+    size_t                                pool_cap = 0;
+    std::list<PoolEntry>                  pool; // resident problems, most recent first
+    size_t                                pool_bytes = 0;
     long long                             reused = 0, built = 0;
-    // how far down the queue a free worker looks for a shape it holds
-    static constexpr int                  LOOKAHEAD = 8;
+    // how far down the queue a free worker looks for a resident shape
+    static constexpr int                  LOOKAHEAD = 16;
 
     Server(int dev, int nw, double fraction)
       : device(dev)
@@ -161,7 +176,7 @@ namespace mfgpu
       MF_CK(cudaMemGetInfo(&free_b, &total_b));
       const size_t all = size_t(double(free_b) * fraction);
       budget           = all / 2;
-      pool_cap         = all / 2 / size_t(nw);
+      pool_cap         = all / 2;
       for (int i = 0; i < nw; ++i)
         workers.emplace_back([this] { loop(); });
     }
@@ -175,32 +190,22 @@ namespace mfgpu
       cv_work.notify_all();
       for (auto &t : workers)
         t.join();
+      pool.clear();
+    }
+
+    bool
+    resident(const std::string &shape) const
+    {
+      for (const PoolEntry &e : pool)
+        if (e.shape == shape)
+          return true;
+      return false;
     }
 
     void
     loop()
     {
       cudaSetDevice(device);
-      // a worker without a context still takes jobs and fails them with the
-      // reason, so that no wait() blocks on a request nobody will run
-      std::unique_ptr<Context> ctx;
-      std::string              ctx_error;
-      try
-        {
-          ctx.reset(new Context(device));
-        }
-      catch (const std::exception &e)
-        {
-          ctx_error = e.what();
-        }
-      std::list<PoolEntry> pool; // this worker's resident problems, most recent first
-      size_t               pool_bytes = 0;
-      auto                 holds = [&](const std::string &shape) {
-        for (const PoolEntry &e : pool)
-          if (e.shape == shape)
-            return true;
-        return false;
-      };
       for (;;)
         {
           ServerJob *job = nullptr;
@@ -217,7 +222,7 @@ namespace mfgpu
             auto pick = queue.begin();
             int  look = 0;
             for (auto it = queue.begin(); it != queue.end() && look < LOOKAHEAD; ++it, ++look)
-              if (fits(*it) && holds((*it)->shape))
+              if (fits(*it) && resident((*it)->shape))
                 {
                   pick = it;
                   break;
@@ -229,14 +234,7 @@ namespace mfgpu
             max_running = std::max(max_running, running);
             job->t_start = clock_t_::now();
           }
-          if (ctx)
-            run(*ctx, *job, pool, pool_bytes);
-          else
-            {
-              job->res.status = MFGPU_ERR_CUDA;
-              std::strncpy(job->res.message, ("worker has no CUDA context: " + ctx_error).c_str(),
-                           sizeof(job->res.message) - 1);
-            }
+          run(*job);
           {
             std::lock_guard<std::mutex> l(mu);
             job->t_end = clock_t_::now();
@@ -253,22 +251,28 @@ namespace mfgpu
     }
 
     void
-    run(Context &ctx, ServerJob &job, std::list<PoolEntry> &pool, size_t &pool_bytes)
+    run(ServerJob &job)
     {
       mfgpu_request_result &r = job.res;
-      // the resident problem of this shape, or a new one
+      // check out the resident problem of this shape, or make a new one
       PoolEntry e;
-      for (auto it = pool.begin(); it != pool.end(); ++it)
-        if (it->shape == job.shape)
-          {
-            e = std::move(*it);
-            pool.erase(it);
-            pool_bytes -= e.bytes;
-            break;
-          }
+      {
+        std::lock_guard<std::mutex> l(mu);
+        for (auto it = pool.begin(); it != pool.end(); ++it)
+          if (it->shape == job.shape)
+            {
+              e = std::move(*it);
+              pool.erase(it);
+              pool_bytes -= e.bytes;
+              break;
+            }
+      }
       const bool reuse = e.heat || e.solid;
       try
         {
+          if (!reuse)
+            e.ctx.reset(new Context(device));
+          Context &ctx = *e.ctx;
           if (job.req.kind == 0)
             {
               if (reuse)
@@ -311,23 +315,26 @@ namespace mfgpu
               r.n_dofs        = double(n);
             }
           r.status = MFGPU_OK;
+          ctx.sync();
+          // keep the problem resident, within the pool's cap; evicted
+          // problems are released outside the lock
+          e.shape = job.shape;
+          e.bytes = job.bytes;
+          std::list<PoolEntry> evicted;
           {
             std::lock_guard<std::mutex> l(mu);
             (reuse ? reused : built) += 1;
+            if (e.bytes <= pool_cap)
+              {
+                pool.push_front(std::move(e));
+                pool_bytes += job.bytes;
+                while (pool_bytes > pool_cap && pool.size() > 1)
+                  {
+                    pool_bytes -= pool.back().bytes;
+                    evicted.splice(evicted.begin(), pool, std::prev(pool.end()));
+                  }
+              }
           }
-          // keep the problem resident, within this worker's cap
-          e.shape = job.shape;
-          e.bytes = job.bytes;
-          if (e.bytes <= pool_cap)
-            {
-              pool.push_front(std::move(e));
-              pool_bytes += job.bytes;
-              while (pool_bytes > pool_cap && !pool.empty())
-                {
-                  pool_bytes -= pool.back().bytes;
-                  pool.pop_back();
-                }
-            }
         }
       catch (const Error &e2)
         {

@@ -265,9 +265,10 @@ class _Operator:
         _check(lib().mfgpu_operator_set_scatter(self.h, {"atomic": 0, "colored": 1}.get(mode, mode)))
 
     def set_cell_kernel(self, mode):
-        """0 by grid size, 1 line-parallel, 2 point-parallel."""
+        """0 by grid size, 1 line-parallel, 2 point-parallel, 3 tensor cores
+        (FP32 heat operators, element matrix)."""
         _check(lib().mfgpu_operator_set_cell_kernel(
-            self.h, {"auto": 0, "line": 1, "point": 2}.get(mode, mode)))
+            self.h, {"auto": 0, "line": 1, "point": 2, "tensor": 3}.get(mode, mode)))
 
     def set_dense(self, enable=True):
         """Dense copy of a small operator (assembled now; used while the

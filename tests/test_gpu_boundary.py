@@ -237,25 +237,26 @@ def test_inclusion_material_and_material_ids(ctx):
     n = W.n_dofs(spec, 3)
     u = dev(W.smooth_displacement(2, 1, spec["rep"], spec["lo"], spec["hi"], seed=2))
     src = dev(W.uniform_vector(n, 3))
+    n_cells = 4 * 2 * 2
     out = []
     for with_inclusion in (False, True):
         op = mfgpu.NeoHookOperator(ctx, mesh, -1, 64, "referential_qp")
         op.set_scatter("colored")
         mat = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
         op.set_material(mat, mfgpu.material(0.5e8, 0.4, 1000.0, 0.01) if with_inclusion else None)
-        op.set_cell_material_ids(np.zeros(32, dtype=np.uint8))
+        op.set_cell_material_ids(np.zeros(n_cells, dtype=np.uint8))
         op.initialize(u)
         op.cache()
         d = torch.zeros_like(src)
         op.vmult(d, src)
         out.append(host(d))
-        ids = np.zeros(32, dtype=np.uint8)
+        ids = np.zeros(n_cells, dtype=np.uint8)
         ids[5] = 1
         with pytest.raises(mfgpu.MfgpuError) as e:
             op.set_cell_material_ids(ids)
         assert e.value.code == 8
         with pytest.raises(mfgpu.MfgpuError) as e:
-            op.set_cell_material_ids(np.zeros(31, dtype=np.uint8))
+            op.set_cell_material_ids(np.zeros(n_cells - 1, dtype=np.uint8))
         assert e.value.code == 1
         with pytest.raises(mfgpu.MfgpuError) as e:
             op.set_material(mat, mfgpu.material(0.5e8, 0.4, 1000.0, 0.01, formulation=0))
