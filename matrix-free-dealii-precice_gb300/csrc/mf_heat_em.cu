@@ -29,6 +29,7 @@
 //   * each warp reads its 32 TMEM lanes (tcgen05.ld) and scatters.
 // Every wait is bounded: after its limit the kernel sets an error flag,
 // skips the rest of the batch, and still frees its tensor memory.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -176,41 +177,66 @@ namespace mfgpu
       size_t   n_nodes;
       unsigned face_mask[6];
       int      constrained;
-      size_t   cell_begin, cell_end;
     };
 
+    // a brick of 8 x 4 x 4 cells (x fastest), one cell per thread and per
+    // TMEM lane; its (8p+1) x (4p+1) x (4p+1) nodes are staged in shared
+    // memory, first as the source values, then as the accumulator of the
+    // cells' results
+    constexpr int BX = 8, BY = 4, BZ = 4;
+    static_assert(BX * BY * BZ == CELLS, "one cell per thread");
+
+    template <int N>
+    struct Layout
+    {
+      using Dm                          = Dims<N>;
+      static constexpr int P            = N - 1;
+      static constexpr int NX           = BX * P + 1, NY = BY * P + 1, NZ = BZ * P + 1;
+      static constexpr int NODES        = NX * NY * NZ;
+      static constexpr int NODE_BYTES   = (NODES * 4 + 127) / 128 * 128;
+      static constexpr int B_ALL        = Dm::KCH * 2 * Dm::B_BYTES;
+      static constexpr bool RESIDENT_B  = B_ALL <= 140 * 1024; // the whole element matrix stays in smem
+      static constexpr int B_REGION     = RESIDENT_B ? B_ALL : 2 * Dm::B_BYTES;
+      static constexpr int OFF_B        = 2 * Dm::A_BYTES;
+      static constexpr int OFF_NODES    = OFF_B + B_REGION;
+      static constexpr int OFF_BAR      = OFF_NODES + NODE_BYTES;
+      static constexpr int SMEM         = OFF_BAR + 64;
+      static_assert(SMEM <= 227 * 1024, "shared memory");
+    };
+
+    // Persistent: each CTA walks bricks blockIdx.x, blockIdx.x + gridDim.x, ...
+    // Per brick: stage the nodes (coalesced, constrained ones zeroed); per K
+    // chunk build the tf32 hi/lo tile of the 128 cells from shared memory
+    // and issue the MMAs; accumulate the results per node in shared memory
+    // (red.shared); write the brick's nodes out, plain adds on nodes no other
+    // brick touches and atomics on the shared faces.  Constrained rows get
+    // dst += src from the cell that owns the node.
     template <int N>
     __global__ void __launch_bounds__(CELLS)
     heat_em_kernel(const __grid_constant__ Args g, const unsigned char *__restrict__ bmat,
                    const float *__restrict__ src, float *__restrict__ dst, int *__restrict__ err)
     {
       using Dm = Dims<N>;
-      constexpr int NE = Dm::NE, NP = Dm::NP, KCH = Dm::KCH;
+      using Lo = Layout<N>;
+      constexpr int NE = Dm::NE, NP = Dm::NP, KCH = Dm::KCH, P = N - 1;
+      constexpr int NX = Lo::NX, NY = Lo::NY;
       extern __shared__ __align__(1024) unsigned char smem[];
       unsigned char *sA_hi = smem;
       unsigned char *sA_lo = smem + Dm::A_BYTES;
-      unsigned char *sB    = smem + 2 * Dm::A_BYTES; // hi then lo, one chunk
-      uint64_t      *bar_b = reinterpret_cast<uint64_t *>(smem + 2 * Dm::A_BYTES + 2 * Dm::B_BYTES);
+      unsigned char *sB    = smem + Lo::OFF_B;
+      float         *sN    = reinterpret_cast<float *>(smem + Lo::OFF_NODES);
+      uint64_t      *bar_b = reinterpret_cast<uint64_t *>(smem + Lo::OFF_BAR);
       uint64_t      *bar_m = bar_b + 1;
       uint32_t      *tslot = reinterpret_cast<uint32_t *>(bar_b + 2);
       int           *fail  = reinterpret_cast<int *>(bar_b + 3);
 
-      const int    t    = threadIdx.x;
-      const int    warp = t >> 5;
-      const size_t cell = g.cell_begin + size_t(blockIdx.x) * CELLS + t;
-      const bool   active = cell < g.cell_end;
-      const size_t cc   = active ? cell : g.cell_begin;
-      const int    cx = int(cc % unsigned(g.C[0])), cyz = int(cc / unsigned(g.C[0]));
-      const int    cy = cyz % g.C[1], cz = cyz / g.C[1];
-      const size_t base = size_t(cx * g.p) + size_t(g.Nn[0]) * (size_t(cy * g.p) + size_t(g.Nn[1]) * (cz * g.p));
-      // constraint tests only on cells touching the box boundary
-      const bool boundary = g.constrained && (cx == 0 || cy == 0 || cz == 0 || cx == g.C[0] - 1 ||
-                                              cy == g.C[1] - 1 || cz == g.C[2] - 1);
-      auto node_of = [&](int l, int &ix, int &iy, int &iz) {
-        const int a = l % N, b = (l / N) % N, c = l / (N * N);
-        ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + c;
-        return base + size_t(a) + size_t(g.Nn[0]) * (size_t(b) + size_t(g.Nn[1]) * size_t(c));
-      };
+      const int t    = threadIdx.x;
+      const int warp = t >> 5;
+      const int tx = t % BX, ty = (t / BX) % BY, tz = t / (BX * BY);
+      // the thread's cell's first node inside the brick
+      const int cbase = tx * P + NX * (ty * P + NY * (tz * P));
+      const int nbx = (g.C[0] + BX - 1) / BX, nby = (g.C[1] + BY - 1) / BY, nbz = (g.C[2] + BZ - 1) / BZ;
+      const int n_bricks = nbx * nby * nbz;
 
       if (t == 0)
         {
@@ -230,99 +256,125 @@ namespace mfgpu
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t tmem  = *tslot;
+      const uint32_t     tmem  = *tslot;
       constexpr uint32_t IDESC = instr_desc(NP, CELLS);
-      int loads = 0, commits = 0; // thread 0: bulk loads and MMA commits issued
-
-      for (int kc = 0; kc < KCH; ++kc)
+      // thread 0: bulk loads issued and waited for, MMA commits issued;
+      // every thread: MMA commits waited for (in order, so parity = count)
+      int loads = 0, bwaits = 0, commits = 0, mwaits = 0;
+      if (Lo::RESIDENT_B && t == 0)
         {
-          if (kc > 0)
+          bulk_load(sB, bmat, Lo::B_ALL, bar_b);
+          ++loads;
+        }
+
+#pragma unroll 1
+      for (int brick = blockIdx.x; brick < n_bricks; brick += gridDim.x)
+        {
+          const int bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
+          const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;          // first cell
+          const int n0x = x0 * P, n0y = y0 * P, n0z = z0 * P;          // first node
+          const int ex = min(NX, g.Nn[0] - n0x), ey = min(NY, g.Nn[1] - n0y), ez = min(Lo::NZ, g.Nn[2] - n0z);
+          const bool touches = g.constrained && (x0 == 0 || y0 == 0 || z0 == 0 || x0 + BX >= g.C[0] ||
+                                                 y0 + BY >= g.C[1] || z0 + BZ >= g.C[2]);
+          // 1. the brick's nodes (zero outside the mesh and on constrained nodes)
+          for (int i = t; i < Lo::NODES; i += CELLS)
             {
-              // the previous chunk's MMAs have read the tiles
-              if (!mbar_wait(bar_m, unsigned(kc - 1) & 1u))
-                atomicOr(fail, 1);
+              const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
+              float     v  = 0.f;
+              if (ix < ex && iy < ey && iz < ez)
+                {
+                  const int gx = n0x + ix, gy = n0y + iy, gz = n0z + iz;
+                  if (!(touches && (node_mask(g.face_mask, g.Nn, gx, gy, gz) & 1u)))
+                    v = __ldg(src + size_t(gx) + size_t(g.Nn[0]) * (size_t(gy) + size_t(g.Nn[1]) * gz));
+                }
+              sN[i] = v;
+            }
+          __syncthreads();
+          const int  cx = x0 + tx, cy = y0 + ty, cz = z0 + tz;
+          const bool active = cx < g.C[0] && cy < g.C[1] && cz < g.C[2];
+          // 2. K chunks
+#pragma unroll 1
+          for (int kc = 0; kc < KCH; ++kc)
+            {
+              if (kc > 0)
+                {
+                  // the previous chunk's MMAs have read the tiles
+                  if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
+                    atomicOr(fail, 1);
+                  ++mwaits;
+                }
+              if (!Lo::RESIDENT_B && t == 0)
+                {
+                  bulk_load(sB, bmat + size_t(kc) * 2 * Dm::B_BYTES, 2 * Dm::B_BYTES, bar_b);
+                  ++loads;
+                }
+#pragma unroll
+              for (int k4 = 0; k4 < KC; k4 += 4)
+                {
+                  float hi[4], lo[4];
+#pragma unroll
+                  for (int q = 0; q < 4; ++q)
+                    {
+                      const int l = kc * KC + k4 + q;
+                      float     v = 0.f;
+                      if (l < NE && active)
+                        v = sN[cbase + (l % N) + NX * ((l / N) % N + NY * (l / (N * N)))];
+                      hi[q] = to_tf32(v);
+                      lo[q] = to_tf32(v - hi[q]);
+                    }
+                  const unsigned off = tile_offset(t, k4);
+                  *reinterpret_cast<float4 *>(sA_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                  *reinterpret_cast<float4 *>(sA_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                }
+              // generic-proxy stores -> visible to the tensor core's async proxy
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
               __syncthreads();
               if (*fail)
                 break;
-            }
-          if (t == 0)
-            {
-              bulk_load(sB, bmat + size_t(kc) * 2 * Dm::B_BYTES, 2 * Dm::B_BYTES, bar_b);
-              ++loads;
-            }
-          // this thread's cell: values kc*32 .. kc*32+31, split into tf32 hi/lo
-#pragma unroll
-          for (int k4 = 0; k4 < KC; k4 += 4)
-            {
-              float hi[4], lo[4];
-#pragma unroll
-              for (int q = 0; q < 4; ++q)
+              if (t == 0)
                 {
-                  const int l = kc * KC + k4 + q;
-                  float     v = 0.f;
-                  if (active && l < NE)
+                  const bool need = !Lo::RESIDENT_B || bwaits == 0;
+                  if (need && !mbar_wait(bar_b, unsigned(bwaits) & 1u))
+                    atomicOr(fail, 2);
+                  else
                     {
-                      int          ix, iy, iz;
-                      const size_t node = node_of(l, ix, iy, iz);
-                      bool         skip = false;
-                      if (boundary)
-                        skip = node_mask(g.face_mask, g.Nn, ix, iy, iz) & 1u;
-                      if (!skip)
-                        v = __ldg(src + node);
+                      if (need)
+                        ++bwaits;
+                      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                      const uint32_t a_hi = smem_addr(sA_hi), a_lo = smem_addr(sA_lo);
+                      const uint32_t bb   = smem_addr(sB) + (Lo::RESIDENT_B ? uint32_t(kc) * 2u * Dm::B_BYTES : 0u);
+                      const uint32_t b_hi = bb, b_lo = bb + Dm::B_BYTES;
+#pragma unroll
+                      for (int ks = 0; ks < KC / 8; ++ks)
+                        {
+                          // one K-step = 8 tf32 = two core matrices along K
+                          const uint32_t o = uint32_t(ks) * 2u * LBO;
+                          mma_tf32(tmem, smem_desc(a_hi + o), smem_desc(b_hi + o), IDESC,
+                                   (kc > 0 || ks > 0) ? 1u : 0u);
+                          mma_tf32(tmem, smem_desc(a_hi + o), smem_desc(b_lo + o), IDESC, 1u);
+                          mma_tf32(tmem, smem_desc(a_lo + o), smem_desc(b_hi + o), IDESC, 1u);
+                        }
                     }
-                  hi[q] = to_tf32(v);
-                  lo[q] = to_tf32(v - hi[q]);
+                  mma_commit(bar_m);
+                  ++commits;
                 }
-              const unsigned off = tile_offset(t, k4);
-              *reinterpret_cast<float4 *>(sA_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-              *reinterpret_cast<float4 *>(sA_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
             }
-          // generic-proxy stores -> visible to the tensor core's async proxy
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          // thread 0's MMA issue and any failure flag are visible to all
           __syncthreads();
-          if (t == 0)
-            {
-              if (!mbar_wait(bar_b, unsigned(kc) & 1u))
-                atomicOr(fail, 2);
-              else
-                {
-                  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                  const uint32_t a_hi = smem_addr(sA_hi), a_lo = smem_addr(sA_lo);
-                  const uint32_t b_hi = smem_addr(sB), b_lo = smem_addr(sB + Dm::B_BYTES);
-#pragma unroll
-                  for (int ks = 0; ks < KC / 8; ++ks)
-                    {
-                      // one K-step = 8 tf32 = two core matrices along K
-                      const uint32_t o = uint32_t(ks) * 2u * LBO;
-                      mma_tf32(tmem, smem_desc(a_hi + o), smem_desc(b_hi + o), IDESC, (kc > 0 || ks > 0) ? 1u : 0u);
-                      mma_tf32(tmem, smem_desc(a_hi + o), smem_desc(b_lo + o), IDESC, 1u);
-                      mma_tf32(tmem, smem_desc(a_lo + o), smem_desc(b_hi + o), IDESC, 1u);
-                    }
-                }
-              mma_commit(bar_m);
-              ++commits;
-            }
-        }
-      // all MMAs done before the accumulator is read
-      if (!*fail && !mbar_wait(bar_m, unsigned(KCH - 1) & 1u))
-        atomicOr(fail, 4);
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (*fail)
-        {
-          if (t == 0)
-            {
-              atomicOr(err, 8 | *fail);
-              // let the copies and MMAs in flight land before the shared and
-              // tensor memory is released (bounded as well)
-              if (loads > 0)
-                mbar_wait(bar_b, unsigned(loads - 1) & 1u);
-              if (commits > 0)
-                mbar_wait(bar_m, unsigned(commits - 1) & 1u);
-            }
-        }
-      else
-        {
+          if (*fail)
+            break;
+          // 3. the staged values are consumed: the node array becomes the
+          // accumulator (while the last MMAs run)
+          for (int i = t; i < Lo::NODES; i += CELLS)
+            sN[i] = 0.f;
+          if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
+            atomicOr(fail, 4);
+          ++mwaits;
+          __syncthreads();
+          if (*fail)
+            break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // 4. the cell's results into the node accumulator
           const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
 #pragma unroll 1
           for (int c0 = 0; c0 < NP; c0 += 8)
@@ -337,22 +389,65 @@ namespace mfgpu
                   const int l = c0 + q;
                   if (l >= NE)
                     break;
-                  int          ix, iy, iz;
-                  const size_t node = node_of(l, ix, iy, iz);
-                  if (boundary && (node_mask(g.face_mask, g.Nn, ix, iy, iz) & 1u))
+                  const int a = l % N, b = (l / N) % N, c = l / (N * N);
+                  if (touches)
                     {
-                      // constrained row: dst += src, by the node's owner cell
-                      const int  a = l % N, b = (l / N) % N, c = l / (N * N);
-                      const bool owner = (a < g.p || cx == g.C[0] - 1) && (b < g.p || cy == g.C[1] - 1) &&
-                                         (c < g.p || cz == g.C[2] - 1);
-                      if (owner)
-                        dst[node] += __ldg(src + node);
-                      continue;
+                      const int gx = cx * P + a, gy = cy * P + b, gz = cz * P + c;
+                      if (node_mask(g.face_mask, g.Nn, gx, gy, gz) & 1u)
+                        {
+                          // constrained row: dst += src, by the node's owner cell
+                          const bool owner = (a < P || cx == g.C[0] - 1) && (b < P || cy == g.C[1] - 1) &&
+                                             (c < P || cz == g.C[2] - 1);
+                          if (owner)
+                            {
+                              const size_t gn = size_t(gx) + size_t(g.Nn[0]) * (size_t(gy) + size_t(g.Nn[1]) * gz);
+                              dst[gn] += __ldg(src + gn);
+                            }
+                          continue;
+                        }
                     }
-                  atomicAdd(dst + node, y[q]);
+                  atomicAdd(sN + cbase + a + NX * (b + NY * c), y[q]);
                 }
             }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncthreads();
+          // 5. write the brick's nodes: plain adds on nodes only this brick
+          // touches, atomics on faces shared with a neighbouring brick
+          for (int i = t; i < Lo::NODES; i += CELLS)
+            {
+              const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
+              if (!(ix < ex && iy < ey && iz < ez))
+                continue;
+              const int gx = n0x + ix, gy = n0y + iy, gz = n0z + iz;
+              if (touches && (node_mask(g.face_mask, g.Nn, gx, gy, gz) & 1u))
+                continue;
+              const size_t gn  = size_t(gx) + size_t(g.Nn[0]) * (size_t(gy) + size_t(g.Nn[1]) * gz);
+              const bool   own = (ix > 0 || bx == 0) && (ix < NX - 1 || bx == nbx - 1) && (iy > 0 || by == 0) &&
+                               (iy < NY - 1 || by == nby - 1) && (iz > 0 || bz == 0) &&
+                               (iz < Lo::NZ - 1 || bz == nbz - 1);
+              if (own)
+                dst[gn] += sN[i];
+              else
+                atomicAdd(dst + gn, sN[i]);
+            }
+          __syncthreads();
         }
+      __syncthreads();
+      if (*fail)
+        {
+          if (t == 0)
+            {
+              atomicOr(err, 8 | *fail);
+              // let the copies and MMAs in flight land before the shared and
+              // tensor memory is released (bounded as well)
+              if (loads > bwaits)
+                mbar_wait(bar_b, unsigned(loads - 1) & 1u);
+              if (commits > mwaits)
+                mbar_wait(bar_m, unsigned(commits - 1) & 1u);
+            }
+        }
+      else if (Lo::RESIDENT_B && t == 0 && loads > bwaits)
+        mbar_wait(bar_b, 0u); // a CTA without bricks still lets its copy land
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       if (warp == 0)
@@ -415,21 +510,27 @@ namespace mfgpu
     cudaError_t
     launch(const Args &a, const void *bmat, const float *src, float *dst, int *err, cudaStream_t s)
     {
-      using Dm           = Dims<N>;
-      static bool attr   = false;
-      cudaError_t e      = cudaSuccess;
-      if (!attr)
+      using Lo         = Layout<N>;
+      static int occ   = 0; // resident CTAs per SM
+      static int n_sm  = 0;
+      cudaError_t e    = cudaSuccess;
+      if (occ == 0)
         {
-          e = cudaFuncSetAttribute(heat_em_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, Dm::SMEM);
+          e = cudaFuncSetAttribute(heat_em_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lo::SMEM);
           if (e != cudaSuccess)
             return e;
-          attr = true;
+          int dev = 0;
+          if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+              (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+              (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heat_em_kernel<N>, CELLS, Lo::SMEM)) !=
+                cudaSuccess)
+            return e;
+          // tensor memory: at most 512 columns per SM
+          occ = std::max(1, std::min(occ, 512 / Dims<N>::TCOLS));
         }
-      const size_t n = a.cell_end - a.cell_begin;
-      if (n == 0)
-        return cudaSuccess;
-      const unsigned grid = unsigned((n + CELLS - 1) / CELLS);
-      heat_em_kernel<N><<<grid, CELLS, Dm::SMEM, s>>>(a, static_cast<const unsigned char *>(bmat), src, dst, err);
+      const long n_bricks = long((a.C[0] + BX - 1) / BX) * ((a.C[1] + BY - 1) / BY) * ((a.C[2] + BZ - 1) / BZ);
+      const unsigned grid = unsigned(std::max(1L, std::min(n_bricks, long(n_sm) * occ)));
+      heat_em_kernel<N><<<grid, CELLS, Lo::SMEM, s>>>(a, static_cast<const unsigned char *>(bmat), src, dst, err);
       return cudaGetLastError();
     }
   } // namespace em
@@ -457,7 +558,7 @@ namespace mfgpu
 
   cudaError_t
   launch_heat_em(const HostBasis &b, const LevelGeom &g, bool constrained, const void *bmat, const float *src,
-                 float *dst, size_t c0, size_t c1, int *err, cudaStream_t s)
+                 float *dst, int *err, cudaStream_t s)
   {
     em::Args a;
     for (int d = 0; d < 3; ++d)
@@ -470,8 +571,6 @@ namespace mfgpu
     for (int f = 0; f < 6; ++f)
       a.face_mask[f] = g.face_mask[f];
     a.constrained = constrained ? 1 : 0;
-    a.cell_begin  = c1 > c0 ? c0 : 0;
-    a.cell_end    = c1 > c0 ? c1 : g.n_cells;
     switch (b.N)
       {
         case 2: return em::launch<2>(a, bmat, src, dst, err, s);

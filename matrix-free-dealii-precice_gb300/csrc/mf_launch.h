@@ -56,12 +56,11 @@ namespace mfgpu
 
   // the heat operator as a batched-cell product with its element matrix on
   // the tensor cores (FP32, three-dimensional, N = 2..6; mf_heat_em.cu):
-  // the matrix in the kernel's layout, and dst += A src on cells [c0, c1)
-  // (all if c1 <= c0)
+  // the matrix in the kernel's layout, and dst += A src over all cells
   bool        heat_em_supported(int N);
   size_t      heat_em_matrix(const HostBasis &b, const LevelGeom &g, double kdt, std::vector<unsigned char> &out);
   cudaError_t launch_heat_em(const HostBasis &b, const LevelGeom &g, bool constrained, const void *bmat,
-                             const float *src, float *dst, size_t c0, size_t c1, int *err, cudaStream_t s);
+                             const float *src, float *dst, int *err, cudaStream_t s);
 
   // launches of fewer cells than this take the point-parallel kernel
   // (native FP64: up to 4096 cells)

@@ -743,13 +743,17 @@ namespace mfgpu
         count_launch();
         return;
       }
-    if (a.kernel == 3 && !a.colored)
+    // the tensor-core kernel runs over all cells; a cell range (the z-slabs
+    // of the host-buffer vmult) takes the line- or point-parallel kernel
+    if (a.kernel == 3 && (a.colored || c1 > c0))
+      a.kernel = 0;
+    if (a.kernel == 3)
       {
         auto *h = dynamic_cast<HeatOperator *>(this);
         if (!h || precision != 32 || !heat_em_supported(basis.N))
           throw Error(ERR_UNSUPPORTED, "the tensor-core cell kernel applies to FP32 heat operators of degree 1..5");
         MF_CK(launch_heat_em(basis, geom, constrained, h->element_matrix(), static_cast<const float *>(src),
-                             static_cast<float *>(dst), c0, c1, ctx->err.as<int>(), s));
+                             static_cast<float *>(dst), ctx->err.as<int>(), s));
         count_launch();
         return;
       }
