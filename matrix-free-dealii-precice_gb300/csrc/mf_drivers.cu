@@ -500,15 +500,38 @@ namespace mfgpu
     return out + rule + "\n";
   }
 
+  // the displacement at a point of a cell: sum over the cell's nodes of
+  // the tensor-product Lagrange weights times the nodal values, one thread
+  // per component, in a fixed order
+  struct PointArgs
+  {
+    size_t n_nodes, base;
+    int    N, nz, nc, Nn0, Nn1;
+    double lx[MAX_N], ly[MAX_N], lz[MAX_N];
+  };
+
+  __global__ void
+  k_point_value(const __grid_constant__ PointArgs a, const double *__restrict__ u, double *__restrict__ out)
+  {
+    const int c = threadIdx.x;
+    if (c >= a.nc)
+      return;
+    double r = 0;
+    for (int k = 0; k < a.nz; ++k)
+      for (int j = 0; j < a.N; ++j)
+        for (int i = 0; i < a.N; ++i)
+          r += a.lx[i] * a.ly[j] * a.lz[k] *
+               u[size_t(c) * a.n_nodes + a.base + size_t(i) + size_t(a.Nn0) * (size_t(j) + size_t(a.Nn1) * k)];
+    out[c] = r;
+  }
+
   std::vector<double>
   SolidDriver::point_value(const double *x)
   {
+    // evaluated on the device: only the three values cross to the host
     const LevelGeom &g = fine->geom;
-    std::vector<double> h(fine->m());
-    MF_CK(cudaMemcpyAsync(h.data(), u.ptr, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->sync();
-    int    cc[3] = {0, 0, 0};
-    double xi[3] = {0, 0, 0};
+    int              cc[3] = {0, 0, 0};
+    double           xi[3] = {0, 0, 0};
     for (int d = 0; d < mesh.dim; ++d)
       {
         const double t = (x[d] - g.lo[d]) / g.h[d];
@@ -524,18 +547,30 @@ namespace mfgpu
           v *= (t - basis.nodes[j]) / (basis.nodes[i] - basis.nodes[j]);
       return v;
     };
+    PointArgs a{};
+    a.n_nodes = g.n_nodes;
+    a.base    = size_t(cc[0] * g.p) + size_t(g.Nn[0]) * (size_t(cc[1] * g.p) + size_t(g.Nn[1]) * (cc[2] * g.p));
+    a.N       = basis.N;
+    a.nz      = mesh.dim == 2 ? 1 : basis.N;
+    a.nc      = fine->nc;
+    a.Nn0     = g.Nn[0];
+    a.Nn1     = g.Nn[1];
+    for (int i = 0; i < basis.N; ++i)
+      {
+        a.lx[i] = lag(i, xi[0]);
+        a.ly[i] = lag(i, xi[1]);
+        a.lz[i] = mesh.dim == 2 ? 1.0 : lag(i, xi[2]);
+      }
+    point_dev.ensure(4 * sizeof(double));
+    point_host.ensure(4);
+    k_point_value<<<1, 32, 0, ctx->stream>>>(a, u.as<double>(), point_dev.as<double>());
+    count_launch();
+    MF_CK(cudaGetLastError());
+    MF_CK(cudaMemcpyAsync(point_host.p, point_dev.ptr, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
     std::vector<double> r(3, 0.0);
-    const int           nz = mesh.dim == 2 ? 1 : basis.N;
     for (int c = 0; c < fine->nc; ++c)
-      for (int k = 0; k < nz; ++k)
-        for (int j = 0; j < basis.N; ++j)
-          for (int i = 0; i < basis.N; ++i)
-            {
-              const size_t node = size_t(cc[0] * g.p + i) +
-                                  size_t(g.Nn[0]) * (size_t(cc[1] * g.p + j) + size_t(g.Nn[1]) * (cc[2] * g.p + k));
-              const double lz = mesh.dim == 2 ? 1.0 : lag(k, xi[2]);
-              r[c] += lag(i, xi[0]) * lag(j, xi[1]) * lz * h[size_t(c) * g.n_nodes + node];
-            }
+      r[c] = point_host.p[c];
     return r;
   }
 

@@ -79,7 +79,8 @@ namespace mfgpu
     DevBuf                                    u, delta, v_old, a_old, acc, rhs, du;
     DevBuf                                    cg_ws; // vectors of the outer CG, kept across solves
     PhaseTimer                                timer;
-    DevBuf                                    cond_y, cond_ws; // condition-number estimate
+    DevBuf                                    point_dev; // the watchpoint value
+    HostPinned                                point_host;
     // the convergence table of the current / last time step (one row per
     // Newton iteration with a linear solve, as the reference prints it)
     struct NewtonRow

@@ -259,7 +259,7 @@ namespace mfgpu
       const uint32_t     tmem  = *tslot;
       constexpr uint32_t IDESC = instr_desc(NP, CELLS);
       // thread 0: bulk loads issued and waited for, MMA commits issued;
-      // every thread: MMA commits waited for (in order, so parity = count)
+      // and MMA commits waited for (in order, so parity = count)
       int loads = 0, bwaits = 0, commits = 0, mwaits = 0;
       if (Lo::RESIDENT_B && t == 0)
         {
@@ -277,6 +277,7 @@ namespace mfgpu
           const bool touches = g.constrained && (x0 == 0 || y0 == 0 || z0 == 0 || x0 + BX >= g.C[0] ||
                                                  y0 + BY >= g.C[1] || z0 + BZ >= g.C[2]);
           // 1. the brick's nodes (zero outside the mesh and on constrained nodes)
+#pragma unroll 4
           for (int i = t; i < Lo::NODES; i += CELLS)
             {
               const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
@@ -298,10 +299,15 @@ namespace mfgpu
             {
               if (kc > 0)
                 {
-                  // the previous chunk's MMAs have read the tiles
-                  if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
-                    atomicOr(fail, 1);
-                  ++mwaits;
+                  // the previous chunk's MMAs have read the tiles (one
+                  // thread polls; the others wait at the barrier)
+                  if (t == 0)
+                    {
+                      if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
+                        atomicOr(fail, 1);
+                      ++mwaits;
+                    }
+                  __syncthreads();
                 }
               if (!Lo::RESIDENT_B && t == 0)
                 {
@@ -367,9 +373,12 @@ namespace mfgpu
           // accumulator (while the last MMAs run)
           for (int i = t; i < Lo::NODES; i += CELLS)
             sN[i] = 0.f;
-          if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
-            atomicOr(fail, 4);
-          ++mwaits;
+          if (t == 0)
+            {
+              if (!mbar_wait(bar_m, unsigned(mwaits) & 1u))
+                atomicOr(fail, 4);
+              ++mwaits;
+            }
           __syncthreads();
           if (*fail)
             break;
@@ -413,6 +422,7 @@ namespace mfgpu
           __syncthreads();
           // 5. write the brick's nodes: plain adds on nodes only this brick
           // touches, atomics on faces shared with a neighbouring brick
+#pragma unroll 4
           for (int i = t; i < Lo::NODES; i += CELLS)
             {
               const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
@@ -511,25 +521,19 @@ namespace mfgpu
     launch(const Args &a, const void *bmat, const float *src, float *dst, int *err, cudaStream_t s)
     {
       using Lo         = Layout<N>;
-      static int occ   = 0; // resident CTAs per SM
-      static int n_sm  = 0;
+      static bool attr = false;
       cudaError_t e    = cudaSuccess;
-      if (occ == 0)
+      if (!attr)
         {
           e = cudaFuncSetAttribute(heat_em_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lo::SMEM);
           if (e != cudaSuccess)
             return e;
-          int dev = 0;
-          if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
-              (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-              (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heat_em_kernel<N>, CELLS, Lo::SMEM)) !=
-                cudaSuccess)
-            return e;
-          // tensor memory: at most 512 columns per SM
-          occ = std::max(1, std::min(occ, 512 / Dims<N>::TCOLS));
+          attr = true;
         }
       const long n_bricks = long((a.C[0] + BX - 1) / BX) * ((a.C[1] + BY - 1) / BY) * ((a.C[2] + BZ - 1) / BZ);
-      const unsigned grid = unsigned(std::max(1L, std::min(n_bricks, long(n_sm) * occ)));
+      // one CTA per brick: the resident CTAs of an SM hide each other's
+      // load, MMA and scatter latencies
+      const unsigned grid = unsigned(std::max(1L, n_bricks));
       heat_em_kernel<N><<<grid, CELLS, Lo::SMEM, s>>>(a, static_cast<const unsigned char *>(bmat), src, dst, err);
       return cudaGetLastError();
     }
