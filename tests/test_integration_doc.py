@@ -28,13 +28,19 @@ def cpp_blocks():
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 def test_integration_sketches_compile(tmp_path):
     blocks = cpp_blocks()
-    assert len(blocks) == 2
-    wrapper, loop = blocks
+    assert len(blocks) == 4
+    perm, mg, wrapper, loop = blocks
     src = (PRELUDE + wrapper +
            "\ntemplate class NeoHookOperatorGPU<3, double>;\n"
            "template class NeoHookOperatorGPU<2, float>;\n"
            "static void check(int rc) { AssertThrow(rc == MFGPU_OK, ExcMessage(mfgpu_last_error())); }\n"
-           "void solid_driver(mfgpu_context *ctx, const mfgpu_solid_params &params)\n{\n" + loop + "}\n")
+           "void solid_driver(mfgpu_context *ctx, const mfgpu_solid_params &params)\n{\n" + loop + "}\n"
+           "void numbering(mfgpu_context *ctx, const mfgpu_mesh &mesh, size_t n_dofs, double *d_dealii,\n"
+           "               double *d_lib)\n{\n" + perm + "mfgpu_permutation_destroy(perm);\n}\n"
+           "void own_cg(mfgpu_context *ctx, const mfgpu_mesh &mesh, const mfgpu_material &mat,\n"
+           "            const mfgpu_solver_params &solver_params, mfgpu_operator *op, const double *u_dev,\n"
+           "            double *du_dev, const double *rhs_dev, double tol, int max_it)\n{\n" + mg + "(void)its;\n"
+           "(void)res;\n}\n")
     f = tmp_path / "integration_sketch.cc"
     f.write_text(src)
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror",
