@@ -537,6 +537,18 @@ int mfgpu_server_stats(mfgpu_server *server, int *max_running,
  * that built a new one */
 int mfgpu_server_pool_stats(mfgpu_server *server, long long *reused,
                             long long *built);
+/* Continuous batching: a worker that takes a heat request also takes the
+ * queued heat requests of the same shape and step count (among the first
+ * 16, up to max_batch in all, default 4; 1 turns batching off) and solves
+ * them together: one operator, one multigrid hierarchy and one CG for all,
+ * so every cell kernel, transfer and smoother step is one launch over all
+ * of them, replayed as one CUDA graph per V-cycle; each problem keeps its
+ * own CG scalars and stopping test, so its iterates are the ones it gets
+ * alone. */
+int mfgpu_server_set_max_batch(mfgpu_server *server, int max_batch);
+/* requests that ran in a batch of two or more, and the largest batch */
+int mfgpu_server_batch_stats(mfgpu_server *server, long long *batched_requests,
+                             int *largest_batch);
 /* finishes queued requests, then stops the workers */
 int mfgpu_server_destroy(mfgpu_server *server);
 

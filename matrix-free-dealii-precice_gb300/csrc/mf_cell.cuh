@@ -874,6 +874,9 @@ namespace mfgpu
     constexpr int AS  = LA::A;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
+    // problem blockIdx.y of a batch
+    src += size_t(blockIdx.y) * g.bstride;
+    dst += size_t(blockIdx.y) * g.bstride;
 
     const int      lc     = threadIdx.x / N2;
     const int      l      = threadIdx.x - lc * N2;
@@ -1156,6 +1159,8 @@ namespace mfgpu
     T *GU = VG + 4 * NC * N3; // [c][3][N3] gradients of the linearisation (EVAL_U)
     T *XU = GU + 3 * NC * N3; // scratch values of the linearisation (EVAL_U)
 
+    src += size_t(blockIdx.y) * g.bstride; // problem blockIdx.y of a batch
+    dst += size_t(blockIdx.y) * g.bstride;
     const int      t    = threadIdx.x;
     const int      a    = t % N, b = (t / N) % N, k = t / N2;
     const unsigned cell = g.cell_begin + blockIdx.x;

@@ -98,6 +98,10 @@ namespace mfgpu
     T        inv_h[3];
     T        vol; // h0*h1*h2
     unsigned face_mask[6];
+    // a batch of problems on this level (same operator, different vectors):
+    // problem blockIdx.y reads src and writes dst at offset blockIdx.y * bstride
+    unsigned batch;
+    size_t   bstride;
   };
 
   // host-side conversion of a double constant to a compute type
@@ -126,6 +130,8 @@ namespace mfgpu
         c.inv_h[d] = conv_host<T>(1.0 / g.h[d]);
       }
     c.p       = g.p;
+    c.batch   = 1;
+    c.bstride = 0;
     c.n_cells    = unsigned(g.n_cells);
     c.cell_begin = 0;
     c.cell_end   = unsigned(g.n_cells);

@@ -128,13 +128,14 @@ namespace mfgpu
   // multigrid hierarchy
   // ---------------------------------------------------------------------
   std::unique_ptr<GMGHierarchy>
-  GMGHierarchy::heat(Context *c, const Mesh &m, const mfgpu_solver_params &s, double delta_t)
+  GMGHierarchy::heat(Context *c, const Mesh &m, const mfgpu_solver_params &s, double delta_t, int batch)
   {
     std::unique_ptr<GMGHierarchy> h(new GMGHierarchy());
     h->mesh  = m;
     h->S     = s;
     h->kind  = 0;
-    h->nc    = 1;
+    h->nc    = batch; // the transfers move every problem of a batch
+    h->batch = batch;
     h->lprec = s.mg_precision == 64 ? 64 : 32;
     // LaplaceProblem::setup_gmg (heat_transfer.h:515-573): Chebyshev degree
     // 5, smoothing range 15, 10 eigenvalue-estimate iterations; the coarse
@@ -146,14 +147,14 @@ namespace mfgpu
     const bool emul = s.fp64_emulation != 0;
     for (int l = 0; l <= m.n_ref; ++l)
       {
-        auto lo     = make_heat(c, m, l, h->lprec, true);
+        auto lo     = make_heat(c, m, l, h->lprec, true, batch);
         lo->delta_t = delta_t;
         lo->arith   = (emul && h->lprec == 64) ? 1 : 0;
         h->lops.push_back(std::move(lo));
       }
     if (s.coarse_fp64 && h->lprec == 32)
       {
-        auto co     = make_heat(c, m, 0, 64, true);
+        auto co     = make_heat(c, m, 0, 64, true, batch);
         co->delta_t = delta_t;
         co->arith   = emul ? 1 : 0;
         h->coarse64 = std::move(co);
@@ -295,7 +296,9 @@ namespace mfgpu
   GMGHierarchy::setup_smoothers(PhaseTimer &timer)
   {
     PhaseTimer::Scope ts(timer, ctx, kind == 1 ? "Setup MF: GMG setup" : "GMG setup");
-    const int         cits = coarse_its < 0 ? int(lops[0]->m()) : coarse_its;
+    // the coarse estimate runs m() iterations of one problem (a batch's
+    // problems are identical)
+    const int         cits = coarse_its < 0 ? int(lops[0]->m() / size_t(batch)) : coarse_its;
     if (lprec == 32)
       mgf->setup(range, degree, eig_its, cits);
     else
@@ -671,16 +674,20 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // heat
   // ---------------------------------------------------------------------
-  HeatDriver::HeatDriver(Context *c, const mfgpu_heat_params &p)
+  HeatDriver::HeatDriver(Context *c, const mfgpu_heat_params &p, int batch)
     : ctx(c)
     , P(p)
+    , nb(batch)
+    , Pb(size_t(batch), p)
   {
     mesh = to_mesh(P.mesh);
     L    = mesh.n_ref;
     make_host_basis(mesh.degree, basis);
-    op          = make_heat(ctx, mesh, -1, 64, true);
+    if (nb < 1 || nb > 6 || (nb > 1 && mesh.dim != 3))
+      throw Error(ERR_ARG, "heat batches: 1..6 three-dimensional problems");
+    op          = make_heat(ctx, mesh, -1, 64, true, nb);
     op->delta_t = P.dt;
-    op_u        = make_heat(ctx, mesh, -1, 64, false);
+    op_u        = make_heat(ctx, mesh, -1, 64, false, nb);
     op_u->delta_t = P.dt;
     const bool emul = P.solver.fp64_emulation != 0;
     op->arith       = emul ? 1 : 0;
@@ -693,7 +700,7 @@ namespace mfgpu
       }
     if (P.solver.preconditioner == 2)
       {
-        gmg   = GMGHierarchy::heat(ctx, mesh, P.solver, P.dt);
+        gmg   = GMGHierarchy::heat(ctx, mesh, P.solver, P.dt, nb);
         lprec = gmg->lprec;
       }
   }
@@ -718,19 +725,22 @@ namespace mfgpu
   void
   HeatDriver::start()
   {
-    const size_t n = op->m();
-    if (P.analytic)
-      {
-        std::vector<double> h(n);
-        for (size_t g = 0; g < n; ++g)
-          {
-            double x[3];
-            node_x(g, x);
-            h[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1];
-          }
-        MF_CK(cudaMemcpyAsync(sol.ptr, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        ctx->sync();
-      }
+    const size_t n  = op->m();
+    const size_t n0 = op->geom.n_nodes; // one problem
+    for (int b = 0; b < nb; ++b)
+      if (Pb[b].analytic)
+        {
+          std::vector<double> h(n0);
+          for (size_t g = 0; g < n0; ++g)
+            {
+              double x[3];
+              node_x(g, x);
+              h[g] = 1 + x[0] * x[0] + Pb[b].alpha * x[1] * x[1];
+            }
+          MF_CK(cudaMemcpyAsync(sol.as<double>() + b * n0, h.data(), n0 * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+          ctx->sync();
+        }
     vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
     // the level operators stay fixed over the time steps: their diagonals
     // and the dense coarse operator are made once
@@ -738,16 +748,23 @@ namespace mfgpu
       gmg->update_diagonals(timer);
     if (P.solver.preconditioner == 1)
       op->compute_diagonal();
-    std::memset(&src, 0, sizeof(src));
-    src.constant = P.analytic ? P.beta - 2 - 2 * P.alpha : 0.0;
-    src.n_gauss  = P.analytic ? 0 : P.n_gauss;
-    for (int i = 0; i < 8; ++i)
+    srcs.assign(size_t(nb), SourceDesc{});
+    for (int b = 0; b < nb; ++b)
       {
-        for (int d = 0; d < 3; ++d)
-          src.center[i][d] = P.g_center[i][d];
-        src.width[i] = P.g_width[i];
-        src.amp[i]   = P.g_amp[i];
+        const mfgpu_heat_params &q  = Pb[b];
+        SourceDesc              &sd = srcs[b];
+        std::memset(&sd, 0, sizeof(sd));
+        sd.constant = q.analytic ? q.beta - 2 - 2 * q.alpha : 0.0;
+        sd.n_gauss  = q.analytic ? 0 : q.n_gauss;
+        for (int i = 0; i < 8; ++i)
+          {
+            for (int d = 0; d < 3; ++d)
+              sd.center[i][d] = q.g_center[i][d];
+            sd.width[i] = q.g_width[i];
+            sd.amp[i]   = q.g_amp[i];
+          }
       }
+    src     = srcs[0];
     t       = 0;
     step_no = 0;
     started = true;
@@ -756,84 +773,109 @@ namespace mfgpu
   int
   HeatDriver::step()
   {
+    return step_batch()[0];
+  }
+
+  std::vector<int>
+  HeatDriver::step_batch()
+  {
     if (!started)
       start();
-    const size_t     n = op->m();
-    const LevelGeom &G = op->geom;
+    const size_t     n  = op->m();
+    const size_t     n0 = op->geom.n_nodes;
+    const LevelGeom &G  = op->geom;
     t += P.dt;
     ++step_no;
     std::unique_ptr<PhaseTimer::Scope> ts(new PhaseTimer::Scope(timer, ctx, "assemble rhs"));
     // inhomogeneous Dirichlet values on the constrained nodes at time t
     MF_CK(cudaMemsetAsync(uD.ptr, 0, n * sizeof(double), ctx->stream));
-    if (P.analytic)
-      {
-        std::vector<double> hd(n, 0.0);
-        for (size_t g = 0; g < n; ++g)
-          {
-            int    ii[3];
-            size_t gg = g;
-            ii[0]     = int(gg % G.Nn[0]);
-            gg /= G.Nn[0];
-            ii[1] = int(gg % G.Nn[1]);
-            ii[2] = int(gg / G.Nn[1]);
-            if (node_mask(G.face_mask, G.Nn, ii[0], ii[1], ii[2]) & 1u)
-              {
-                double x[3];
-                node_x(g, x);
-                hd[g] = 1 + x[0] * x[0] + P.alpha * x[1] * x[1] + P.beta * t;
-              }
-          }
-        MF_CK(cudaMemcpyAsync(uD.ptr, hd.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        ctx->sync();
-      }
+    for (int b = 0; b < nb; ++b)
+      if (Pb[b].analytic)
+        {
+          std::vector<double> hd(n0, 0.0);
+          for (size_t g = 0; g < n0; ++g)
+            {
+              int    ii[3];
+              size_t gg = g;
+              ii[0]     = int(gg % G.Nn[0]);
+              gg /= G.Nn[0];
+              ii[1] = int(gg % G.Nn[1]);
+              ii[2] = int(gg / G.Nn[1]);
+              if (node_mask(G.face_mask, G.Nn, ii[0], ii[1], ii[2]) & 1u)
+                {
+                  double x[3];
+                  node_x(g, x);
+                  hd[g] = 1 + x[0] * x[0] + Pb[b].alpha * x[1] * x[1] + Pb[b].beta * t;
+                }
+            }
+          MF_CK(cudaMemcpyAsync(uD.as<double>() + b * n0, hd.data(), n0 * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+          ctx->sync();
+        }
     // rhs = -A_unconstrained uD + int (u_old + dt f) v
     op_u->vmult(rhs.ptr, uD.ptr);
     vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
-    if (G.dim == 2)
-      MF_CK(launch_heat_rhs2d(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
-                              ctx->stream));
-    else
-      MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, src, sol_old.as<double>(), rhs.as<double>(),
-                              ctx->stream));
-    count_launch();
-    const double tol = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n, rhs.as<double>(), rhs.as<double>()));
+    std::vector<double> tol(static_cast<size_t>(nb), 0.0);
+    for (int b = 0; b < nb; ++b)
+      {
+        double *rb = rhs.as<double>() + b * n0;
+        if (G.dim == 2)
+          MF_CK(launch_heat_rhs2d(basis.N, basis, G, P.dt, srcs[b], sol_old.as<double>() + b * n0, rb, ctx->stream));
+        else
+          MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, srcs[b], sol_old.as<double>() + b * n0, rb, ctx->stream));
+        count_launch();
+        tol[b] = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n0, rb, rb));
+      }
     ts.reset();
     FineOp A;
     A.op = op.get();
-    CGStats st;
+    JacobiPre64      J;
+    Precond<double> *M = nullptr;
     if (P.solver.preconditioner == 2)
       {
         gmg->setup_smoothers(timer);
-        PhaseTimer::Scope tsol(timer, ctx, "solve system");
-        st = cg_solve<double>(*ctx, A, gmg->precond(), du.as<double>(), rhs.as<double>(), tol, int(n), false,
-                              false, &cg_ws);
+        M = gmg->precond();
       }
     else if (P.solver.preconditioner == 1)
       {
-        PhaseTimer::Scope tsol(timer, ctx, "solve system");
-        JacobiPre64       J;
         J.ctx   = ctx;
         J.A     = op.get();
         J.omega = 0.7;
-        st      = cg_solve<double>(*ctx, A, &J, du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
+        M       = &J;
       }
-    else
-      {
-        PhaseTimer::Scope tsol(timer, ctx, "solve system");
-        st = cg_solve<double>(*ctx, A, nullptr, du.as<double>(), rhs.as<double>(), tol, int(n), false, false, &cg_ws);
-      }
-    if (!st.converged)
-      throw Error(ERR_NOT_CONVERGED, "CG did not converge");
-    constrained_op<double>(*ctx, G, 1, 2, nullptr, du.as<double>());
+    std::vector<int> its(size_t(nb), 0);
+    {
+      PhaseTimer::Scope tsol(timer, ctx, "solve system");
+      if (nb == 1)
+        {
+          const CGStats st = cg_solve<double>(*ctx, A, M, du.as<double>(), rhs.as<double>(), tol[0], int(n), false,
+                                              false, &cg_ws);
+          if (!st.converged)
+            throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+          its[0] = st.its;
+        }
+      else if (!cg_solve_batched(*ctx, A, M, du.as<double>(), rhs.as<double>(), nb, n0, tol, int(n0), its, &cg_ws))
+        throw Error(ERR_NOT_CONVERGED, "CG did not converge");
+    }
+    constrained_op<double>(*ctx, G, nb, 2, nullptr, du.as<double>());
     vec_axpbyz<double>(*ctx, n, 1.0, uD.as<double>(), 1.0, du.as<double>(), sol.as<double>());
     vec_copy<double>(*ctx, n, sol.as<double>(), sol_old.as<double>());
-    return st.its;
+    return its;
   }
 
   void
   HeatDriver::reset(const mfgpu_heat_params &p)
   {
-    P              = p;
+    reset_batch(std::vector<mfgpu_heat_params>(size_t(nb), p));
+  }
+
+  void
+  HeatDriver::reset_batch(const std::vector<mfgpu_heat_params> &ps)
+  {
+    if (int(ps.size()) != nb)
+      throw Error(ERR_ARG, "reset_batch: one parameter set per problem of the batch");
+    Pb             = ps;
+    P              = ps[0];
     const size_t n = op->m();
     for (DevBuf *b : {&sol, &sol_old, &rhs, &du, &uD})
       MF_CK(cudaMemsetAsync(b->ptr, 0, n * sizeof(double), ctx->stream));

@@ -28,6 +28,7 @@ namespace mfgpu
     int                                    L = 0;
     int                                    kind = 0; // 0 heat (LaplaceOperator), 1 neo-Hookean
     int                                    nc = 1;
+    int                                    batch = 1;
     int                                    lprec = 32;
     mfgpu_solver_params                    S{};
     HostBasis                              basis;
@@ -45,8 +46,9 @@ namespace mfgpu
     int      coarse_its = -1;
     size_t   diag_key   = 0; // value states the level diagonals were made for
     // heat levels: M + delta_t K
+    // batch > 1: the levels of a batch of identical heat problems
     static std::unique_ptr<GMGHierarchy> heat(Context *c, const Mesh &m, const mfgpu_solver_params &s,
-                                              double delta_t);
+                                              double delta_t, int batch = 1);
     // neo-Hookean levels of caching `variant`
     static std::unique_ptr<GMGHierarchy> solid(Context *c, const Mesh &m, const mfgpu_solver_params &s,
                                                const NHMatD &mat, int formulation, int variant);
@@ -126,11 +128,22 @@ namespace mfgpu
     SourceDesc                                 src{};
     DevBuf                                     cg_ws; // vectors of the outer CG, kept across steps
     PhaseTimer                                 timer;
-    HeatDriver(Context *c, const mfgpu_heat_params &p);
+    // a batch of nb problems of one shape (mesh, time step, solver) with
+    // their own loads: one operator, one multigrid hierarchy and one CG
+    // for all of them, every application one launch (make_heat(..., nb),
+    // cg_solve_batched); problem i's vectors are block i of sol, rhs, ...
+    int                                        nb = 1;
+    std::vector<mfgpu_heat_params>             Pb;   // per problem (Pb[0] == P)
+    std::vector<SourceDesc>                    srcs; // per problem
+    HeatDriver(Context *c, const mfgpu_heat_params &p, int batch = 1);
     void node_x(size_t g, double *x) const;
     void start();          // initial condition, diagonals
     int  step();           // one backward-Euler step; returns CG iterations
+    // one step of every problem of the batch; CG iterations per problem
+    std::vector<int> step_batch();
     void run(mfgpu_heat_result &res);
+    // new loads for the nb problems (same shape as the driver's)
+    void reset_batch(const std::vector<mfgpu_heat_params> &ps);
     // a new problem of the same shape (mesh, time step, solver parameters):
     // the source / analytic data and step count are p's and the solution
     // starts from zero; operators, diagonals, smoothers and the captured

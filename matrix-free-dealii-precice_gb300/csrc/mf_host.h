@@ -195,7 +195,9 @@ namespace mfgpu
   // x[i] = (i % 11 == 0 ? 0 : 1) - mean of those values: the start vector of
   // the Chebyshev eigenvalue estimate (high-frequency content and the
   // constant mode)
-  template <typename T> void vec_estimate_start(Context &c, size_t n, T *x);
+  // the eigenvalue estimate's start vector; period > 0: the pattern repeats
+  // every `period` entries (the blocks of a batch start alike)
+  template <typename T> void vec_estimate_start(Context &c, size_t n, T *x, size_t period = 0);
   template <typename T> void vec_axpby(Context &c, size_t n, T a, const T *x, T b, T *y);
   template <typename T> void vec_axpbyz(Context &c, size_t n, T a, const T *x, T b, const T *y, T *z);
   template <typename T> void vec_copy(Context &c, size_t n, const T *x, T *y);
@@ -292,6 +294,9 @@ namespace mfgpu
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;
+    // heat operators of a batch of problems (make_heat(..., batch)): nc is
+    // the number of problems, each a scalar field of n_nodes entries
+    bool      heat_batch = false;
     virtual ~Operator() = default;
     size_t
     m() const
@@ -385,7 +390,11 @@ namespace mfgpu
 
   int  parse_caching(const char *s);
   NHMatD make_material(double mu, double nu, double rho, double alpha_1);
-  std::unique_ptr<HeatOperator> make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained);
+  // batch > 1: one operator applied to `batch` problems on the same level
+  // (vectors of batch blocks of n_nodes entries; one launch per application);
+  // the Dirichlet bits of every face mask cover all blocks
+  std::unique_ptr<HeatOperator> make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained,
+                                          int batch = 1);
   std::unique_ptr<NHOperator>   make_nh(Context *c, const Mesh &m, int level, int precision, int variant);
 
   // ---------------------------------------------------------------------

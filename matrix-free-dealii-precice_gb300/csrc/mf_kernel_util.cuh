@@ -92,6 +92,8 @@ namespace mfgpu
     CellGeom<T>
     apply_range(CellGeom<T> c, const ApplyArgs &a)
     {
+      c.batch   = unsigned(a.batch > 1 ? a.batch : 1);
+      c.bstride = a.batch > 1 ? a.bstride : 0;
       if (a.cell_end > a.cell_begin)
         {
           c.cell_begin = unsigned(a.cell_begin);

@@ -62,7 +62,7 @@ namespace mfgpu
           const size_t smemp = point_smem_elems<N, NC, Op::eval_u>() * sizeof(T);
           if ((e = prepare(kp, smemp)) != cudaSuccess)
             return e;
-          kp<<<n_cells, N * N * N, smemp, s>>>(sh, cg, op, src, dst);
+          kp<<<dim3(n_cells, cg.batch), N * N * N, smemp, s>>>(sh, cg, op, src, dst);
           return cudaGetLastError();
         }
       auto k = cell_apply_kernel<N, TS, T, NC, Op, CON>;
@@ -78,7 +78,7 @@ namespace mfgpu
               c.color_n     = color_cells(cg.C, color, c.hc);
               if (c.color_n == 0)
                 continue;
-              k<<<(c.color_n + CPB - 1) / CPB, CPB * N * N, smem, s>>>(sh, c, op, src, dst);
+              k<<<dim3((c.color_n + CPB - 1) / CPB, cg.batch), CPB * N * N, smem, s>>>(sh, c, op, src, dst);
               if ((e = cudaGetLastError()) != cudaSuccess)
                 return e;
             }
@@ -96,10 +96,10 @@ namespace mfgpu
             const size_t smem1 = apply_smem_per_cell<N, NC, Op::eval_u, T>() * sizeof(T);
             if ((e = prepare(k1, smem1)) != cudaSuccess)
               return e;
-            k1<<<cells, N * N, smem1, s>>>(sh, cg, op, src, dst);
+            k1<<<dim3(cells, cg.batch), N * N, smem1, s>>>(sh, cg, op, src, dst);
             return cudaGetLastError();
           }
-      k<<<grid, CPB * N * N, smem, s>>>(sh, cg, op, src, dst);
+      k<<<dim3(grid, cg.batch), CPB * N * N, smem, s>>>(sh, cg, op, src, dst);
       return cudaGetLastError();
     }
 

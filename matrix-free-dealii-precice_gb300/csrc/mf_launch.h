@@ -52,6 +52,10 @@ namespace mfgpu
     // cell kernel: 0 by grid size (point-parallel below POINT_CELLS cells),
     // 1 line-parallel (cell_apply_kernel), 2 point-parallel
     int         kernel = 0;
+    // a batch of problems sharing the operator: vectors of `batch` blocks of
+    // `bstride` entries, all blocks in one launch (grid.y = batch)
+    int         batch   = 1;
+    size_t      bstride = 0;
   };
 
   // the heat operator as a batched-cell product with its element matrix on

@@ -382,11 +382,12 @@ namespace mfgpu
   }
   template <typename T>
   void
-  vec_estimate_start(Context &c, size_t n, T *x)
+  vec_estimate_start(Context &c, size_t n, T *x, size_t period)
   {
-    // the mean of the 0/1 pattern in double, rounded to T once
-    const double ones = double(n - (n + 10) / 11);
-    k_estimate_start<<<grid_for(n), 256, 0, c.stream>>>(n, T(n ? ones / double(n) : 0.0), x);
+    // the mean of the 0/1 pattern (over one period) in double, rounded to T once
+    const size_t pr   = period ? period : n;
+    const double ones = double(pr - (pr + 10) / 11);
+    k_estimate_start<<<grid_for(n), 256, 0, c.stream>>>(n, pr, T(pr ? ones / double(pr) : 0.0), x);
     count_launch();
     MF_CK(cudaGetLastError());
   }
@@ -591,7 +592,7 @@ namespace mfgpu
 
 #define MF_INST_VEC(T)                                                                      \
   template void vec_fill<T>(Context &, size_t, T, T *);                                     \
-  template void vec_estimate_start<T>(Context &, size_t, T *);                              \
+  template void vec_estimate_start<T>(Context &, size_t, T *, size_t);                              \
   template void vec_axpby<T>(Context &, size_t, T, const T *, T, T *);                      \
   template void vec_axpbyz<T>(Context &, size_t, T, const T *, T, const T *, T *);          \
   template void vec_copy<T>(Context &, size_t, const T *, T *);                             \
@@ -736,6 +737,13 @@ namespace mfgpu
     a.cell_end   = c1;
     a.colored    = scatter == 1;
     a.kernel     = kernel >= 0 ? kernel : cell_kernel;
+    if (heat_batch)
+      {
+        // the scalar heat kernel over nc problems: grid.y = problem
+        a.batch   = nc;
+        a.bstride = geom.n_nodes;
+        a.colored = false;
+      }
     if (geom.dim == 2)
       {
         check_2d();
@@ -745,7 +753,7 @@ namespace mfgpu
       }
     // the tensor-core kernel runs over all cells; a cell range (the z-slabs
     // of the host-buffer vmult) takes the line- or point-parallel kernel
-    if (a.kernel == 3 && (a.colored || c1 > c0))
+    if (a.kernel == 3 && (a.colored || c1 > c0 || heat_batch))
       a.kernel = 0;
     if (a.kernel == 3)
       {
@@ -768,7 +776,7 @@ namespace mfgpu
   Operator::dense_fits() const
   {
     const size_t n = m();
-    return geom.dim == 3 && constrained && n > 0 && n <= DENSE_MAX_BYTES / elem_size() / n;
+    return geom.dim == 3 && constrained && !heat_batch && n > 0 && n <= DENSE_MAX_BYTES / elem_size() / n;
   }
 
   void
@@ -1149,6 +1157,10 @@ namespace mfgpu
                       dispatch_diag<double>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream);
     count_launch();
     MF_CK(e);
+    // a batch: the problems share the operator, hence the diagonal
+    for (int b = 1; heat_batch && b < nc; ++b)
+      MF_CK(cudaMemcpyAsync(static_cast<char *>(inv_diag.ptr) + size_t(b) * geom.n_nodes * elem_size(), inv_diag.ptr,
+                            geom.n_nodes * elem_size(), cudaMemcpyDeviceToDevice, ctx->stream));
     finish_diagonal();
   }
 
@@ -1324,12 +1336,23 @@ namespace mfgpu
   }
 
   std::unique_ptr<HeatOperator>
-  make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained)
+  make_heat(Context *c, const Mesh &m, int level, int precision, bool constrained, int batch)
   {
+    if (batch < 1 || batch > 8)
+      throw Error(ERR_ARG, "heat batch must be 1..8");
     std::unique_ptr<HeatOperator> op(new HeatOperator());
     init_op(*op, c, m, level, precision);
-    op->nc          = 1;
+    op->nc          = batch;
     op->constrained = constrained;
+    if (batch > 1)
+      {
+        if (op->geom.dim != 3)
+          throw Error(ERR_UNSUPPORTED, "batched heat operators are three-dimensional");
+        op->heat_batch = true;
+        for (int f = 0; f < 6; ++f)
+          if (op->geom.face_mask[f] & 1u)
+            op->geom.face_mask[f] = (1u << batch) - 1u;
+      }
     return op;
   }
 

@@ -164,6 +164,9 @@ namespace mfgpu
     std::list<PoolEntry>                  pool; // resident problems, most recent first
     size_t                                pool_bytes = 0;
     long long                             reused = 0, built = 0;
+    int                                   max_batch      = 4; // heat requests solved together, at most
+    int                                   max_batch_seen = 1;
+    long long                             batched        = 0; // requests that ran in a batch of two or more
     // how far down the queue a free worker looks for a resident shape
     static constexpr int                  LOOKAHEAD = 16;
 
@@ -208,7 +211,7 @@ namespace mfgpu
       cudaSetDevice(device);
       for (;;)
         {
-          ServerJob *job = nullptr;
+          std::vector<ServerJob *> batch;
           {
             std::unique_lock<std::mutex> l(mu);
             auto fits = [&](const ServerJob *j) {
@@ -227,26 +230,149 @@ namespace mfgpu
                   pick = it;
                   break;
                 }
-            job = *pick;
+            ServerJob *job = *pick;
             queue.erase(pick);
+            batch.push_back(job);
             reserved += job->bytes;
-            ++running;
+            // continuous batching: queued heat requests of the same shape and
+            // step count join this one, one solve for all of them
+            if (job->req.kind == 0 && max_batch > 1)
+              {
+                look = 0;
+                for (auto it = queue.begin(); it != queue.end() && look < LOOKAHEAD && int(batch.size()) < max_batch;
+                     ++look)
+                  if ((*it)->shape == job->shape && (*it)->req.heat.n_steps == job->req.heat.n_steps &&
+                      reserved + (*it)->bytes <= budget)
+                    {
+                      reserved += (*it)->bytes;
+                      batch.push_back(*it);
+                      it = queue.erase(it);
+                    }
+                  else
+                    ++it;
+              }
+            running += int(batch.size());
             max_running = std::max(max_running, running);
-            job->t_start = clock_t_::now();
+            max_batch_seen = std::max(max_batch_seen, int(batch.size()));
+            if (batch.size() > 1)
+              batched += static_cast<long long>(batch.size());
+            for (ServerJob *j : batch)
+              j->t_start = clock_t_::now();
           }
-          run(*job);
+          if (batch.size() == 1)
+            run(*batch[0]);
+          else
+            run_batch(batch);
           {
             std::lock_guard<std::mutex> l(mu);
-            job->t_end = clock_t_::now();
-            reserved -= job->bytes;
-            --running;
-            job->done                = true;
-            job->res.queue_seconds   = std::chrono::duration<double>(job->t_start - job->t_submit).count();
-            job->res.run_seconds     = std::chrono::duration<double>(job->t_end - job->t_start).count();
-            job->res.latency_seconds = std::chrono::duration<double>(job->t_end - job->t_submit).count();
+            const auto t_end = clock_t_::now();
+            for (ServerJob *job : batch)
+              {
+                job->t_end = t_end;
+                reserved -= job->bytes;
+                --running;
+                job->done                = true;
+                job->res.queue_seconds   = std::chrono::duration<double>(job->t_start - job->t_submit).count();
+                job->res.run_seconds     = std::chrono::duration<double>(job->t_end - job->t_start).count();
+                job->res.latency_seconds = std::chrono::duration<double>(job->t_end - job->t_submit).count();
+              }
           }
           cv_done.notify_all();
           cv_work.notify_all();
+        }
+    }
+
+    // check out the resident problem of a pool key (null entry if none)
+    PoolEntry
+    checkout(const std::string &key)
+    {
+      PoolEntry                   e;
+      std::lock_guard<std::mutex> l(mu);
+      for (auto it = pool.begin(); it != pool.end(); ++it)
+        if (it->shape == key)
+          {
+            e = std::move(*it);
+            pool.erase(it);
+            pool_bytes -= e.bytes;
+            break;
+          }
+      return e;
+    }
+
+    // return a problem to the pool, within its cap; evicted problems are
+    // released outside the lock
+    void
+    checkin(PoolEntry &&e, bool reuse)
+    {
+      std::list<PoolEntry> evicted;
+      std::lock_guard<std::mutex> l(mu);
+      (reuse ? reused : built) += 1;
+      if (e.bytes <= pool_cap)
+        {
+          pool_bytes += e.bytes;
+          pool.push_front(std::move(e));
+          while (pool_bytes > pool_cap && pool.size() > 1)
+            {
+              pool_bytes -= pool.back().bytes;
+              evicted.splice(evicted.begin(), pool, std::prev(pool.end()));
+            }
+        }
+    }
+
+    // heat requests of one shape solved together: one batched driver (one
+    // operator, one V-cycle, one CG for all), resident under its own key
+    void
+    run_batch(std::vector<ServerJob *> &batch)
+    {
+      const int         nb  = int(batch.size());
+      const std::string key = batch[0]->shape + "|batch" + std::to_string(nb);
+      PoolEntry         e   = checkout(key);
+      const bool        reuse = bool(e.heat);
+      try
+        {
+          std::vector<mfgpu_heat_params> ps;
+          for (ServerJob *j : batch)
+            ps.push_back(j->req.heat);
+          if (!reuse)
+            {
+              e.ctx.reset(new Context(device));
+              e.heat.reset(new HeatDriver(e.ctx.get(), ps[0], nb));
+            }
+          HeatDriver &d = *e.heat;
+          d.reset_batch(ps);
+          d.start();
+          std::vector<int> its(size_t(nb), 0);
+          for (int s = 0; s < ps[0].n_steps; ++s)
+            {
+              const std::vector<int> st = d.step_batch();
+              for (int b = 0; b < nb; ++b)
+                its[b] += st[b];
+            }
+          const size_t n0 = d.op->geom.n_nodes;
+          for (int b = 0; b < nb; ++b)
+            {
+              mfgpu_request_result &r = batch[b]->res;
+              const double         *x = d.sol.as<double>() + b * n0;
+              r.cg_iterations         = its[b];
+              r.solution_norm         = std::sqrt(vec_dot<double>(*e.ctx, n0, x, x));
+              r.n_dofs                = double(n0);
+              r.status                = MFGPU_OK;
+            }
+          e.ctx->sync();
+          e.shape = key;
+          e.bytes = 0;
+          for (ServerJob *j : batch)
+            e.bytes += j->bytes;
+          checkin(std::move(e), reuse);
+        }
+      catch (const std::exception &x)
+        {
+          const Error *err = dynamic_cast<const Error *>(&x);
+          for (ServerJob *j : batch)
+            {
+              j->res.status = err ? err->code : MFGPU_ERR_ARG;
+              std::strncpy(j->res.message, x.what(), sizeof(j->res.message) - 1);
+            }
         }
     }
 
@@ -255,18 +381,7 @@ namespace mfgpu
     {
       mfgpu_request_result &r = job.res;
       // check out the resident problem of this shape, or make a new one
-      PoolEntry e;
-      {
-        std::lock_guard<std::mutex> l(mu);
-        for (auto it = pool.begin(); it != pool.end(); ++it)
-          if (it->shape == job.shape)
-            {
-              e = std::move(*it);
-              pool.erase(it);
-              pool_bytes -= e.bytes;
-              break;
-            }
-      }
+      PoolEntry  e     = checkout(job.shape);
       const bool reuse = e.heat || e.solid;
       try
         {
@@ -316,25 +431,10 @@ namespace mfgpu
             }
           r.status = MFGPU_OK;
           ctx.sync();
-          // keep the problem resident, within the pool's cap; evicted
-          // problems are released outside the lock
+          // keep the problem resident
           e.shape = job.shape;
           e.bytes = job.bytes;
-          std::list<PoolEntry> evicted;
-          {
-            std::lock_guard<std::mutex> l(mu);
-            (reuse ? reused : built) += 1;
-            if (e.bytes <= pool_cap)
-              {
-                pool.push_front(std::move(e));
-                pool_bytes += job.bytes;
-                while (pool_bytes > pool_cap && pool.size() > 1)
-                  {
-                    pool_bytes -= pool.back().bytes;
-                    evicted.splice(evicted.begin(), pool, std::prev(pool.end()));
-                  }
-              }
-          }
+          checkin(std::move(e), reuse);
         }
       catch (const Error &e2)
         {
@@ -489,6 +589,35 @@ extern "C"
       *reused = server->s->reused;
     if (built)
       *built = server->s->built;
+    return MFGPU_OK;
+  }
+
+  int
+  mfgpu_server_set_max_batch(mfgpu_server *server, int max_batch)
+  {
+    if (!server || max_batch < 1 || max_batch > 6)
+      {
+        set_last_error("server_set_max_batch: null server or max_batch outside 1..6");
+        return MFGPU_ERR_ARG;
+      }
+    std::lock_guard<std::mutex> l(server->s->mu);
+    server->s->max_batch = max_batch;
+    return MFGPU_OK;
+  }
+
+  int
+  mfgpu_server_batch_stats(mfgpu_server *server, long long *batched_requests, int *largest_batch)
+  {
+    if (!server)
+      {
+        set_last_error("server_batch_stats: null argument");
+        return MFGPU_ERR_ARG;
+      }
+    std::lock_guard<std::mutex> l(server->s->mu);
+    if (batched_requests)
+      *batched_requests = server->s->batched;
+    if (largest_batch)
+      *largest_batch = server->s->max_batch_seen;
     return MFGPU_OK;
   }
 

@@ -85,6 +85,93 @@ namespace mfgpu
     return st;
   }
 
+  bool
+  cg_solve_batched(Context &c, LinOp<double> &A, Precond<double> *P, double *x, const double *b, int nb, size_t n,
+                   const std::vector<double> &tol, int maxit, std::vector<int> &its, DevBuf *ws)
+  {
+    if (nb < 1 || nb > 6 || A.size() != size_t(nb) * n || int(tol.size()) != nb)
+      throw Error(ERR_ARG, "cg_solve_batched: 1..6 systems of n unknowns");
+    const size_t N  = size_t(nb) * n;
+    const size_t vb = (N * sizeof(double) + 255) / 256 * 256;
+    DevBuf       own;
+    DevBuf      &W = ws ? *ws : own;
+    if (W.bytes < 4 * vb)
+      W.alloc(4 * vb);
+    char   *base = static_cast<char *>(W.ptr);
+    double *r = reinterpret_cast<double *>(base), *z = reinterpret_cast<double *>(base + vb);
+    double *p = reinterpret_cast<double *>(base + 2 * vb), *q = reinterpret_cast<double *>(base + 3 * vb);
+    // slots of system i: 5 i + {RR, RZ, RZN, PQ}
+    auto slot = [](int i, int s) { return 5 * i + s; };
+    std::vector<int>  rz(nb, S_RZ), rzn(nb, S_RZN);
+    std::vector<char> active(nb, 1);
+    its.assign(nb, 0);
+    A.vmult(r, x);
+    vec_axpby<double>(c, N, 1.0, b, -1.0, r);
+    for (int i = 0; i < nb; ++i)
+      vec_dot_dev<double>(c, n, r + i * n, r + i * n, slot(i, S_RR));
+    read_scalars(c, 5 * nb);
+    int n_active = 0;
+    for (int i = 0; i < nb; ++i)
+      {
+        const double res = std::sqrt(c.host_scalars[slot(i, S_RR)]);
+        if (!std::isfinite(res))
+          throw Error(ERR_NONFINITE, "CG: non-finite residual");
+        active[i] = res > tol[i];
+        n_active += active[i];
+      }
+    if (n_active == 0)
+      return true;
+    if (P)
+      P->vmult(z, r);
+    else
+      vec_copy<double>(c, N, r, z);
+    for (int i = 0; i < nb; ++i)
+      if (active[i])
+        {
+          vec_dot_dev<double>(c, n, r + i * n, z + i * n, slot(i, rz[i]));
+          vec_copy<double>(c, n, z + i * n, p + i * n);
+        }
+    for (int it = 1; it <= maxit && n_active > 0; ++it)
+      {
+        A.vmult(q, p);
+        for (int i = 0; i < nb; ++i)
+          if (active[i])
+            {
+              vec_dot_dev<double>(c, n, p + i * n, q + i * n, slot(i, S_PQ));
+              cg_update<double>(c, n, slot(i, rz[i]), slot(i, S_PQ), x + i * n, p + i * n, r + i * n, q + i * n,
+                                slot(i, S_RR));
+            }
+        read_scalars(c, 5 * nb);
+        for (int i = 0; i < nb; ++i)
+          if (active[i])
+            {
+              const double res = std::sqrt(c.host_scalars[slot(i, S_RR)]);
+              its[i]           = it;
+              if (!std::isfinite(res))
+                throw Error(ERR_NONFINITE, "CG: non-finite residual");
+              if (res <= tol[i])
+                {
+                  active[i] = 0;
+                  --n_active;
+                }
+            }
+        if (n_active == 0)
+          break;
+        if (P)
+          P->vmult(z, r);
+        else
+          vec_copy<double>(c, N, r, z);
+        for (int i = 0; i < nb; ++i)
+          if (active[i])
+            {
+              vec_dot_dev<double>(c, n, r + i * n, z + i * n, slot(i, rzn[i]));
+              cg_direction<double>(c, n, slot(i, rzn[i]), slot(i, rz[i]), z + i * n, p + i * n);
+              std::swap(rz[i], rzn[i]);
+            }
+      }
+    return n_active == 0;
+  }
+
   template <typename T>
   CGStats
   cg_lanczos(Context &c, LinOp<T> &A, Precond<T> *P, T *x, const T *b, double tol, int maxit,
@@ -363,13 +450,14 @@ namespace mfgpu
     w1.ensure(n * sizeof(T));
     // initial guess with high-frequency content and the constant mode:
     // entries 1 except every 11th, mean removed
-    vec_estimate_start<T>(*ctx, n, w0.as<T>());
+    vec_estimate_start<T>(*ctx, n, w0.as<T>(), start_period());
     MF_CK(cudaMemsetAsync(w1.ptr, 0, n * sizeof(T), ctx->stream));
     OpRef<T>     Aop(A);
     JacobiPre<T> P;
     P.ctx      = ctx;
     P.A        = A;
-    CGStats st = cg_lanczos<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, 8, &cg_ws);
+    CGStats st = cg_lanczos<T>(*ctx, Aop, &P, w1.as<T>(), w0.as<T>(), estimate_tol(), eig_cg_iterations, 8,
+                               &cg_ws);
     set_bounds(st);
   }
 
@@ -393,13 +481,14 @@ namespace mfgpu
       ~Restore() { op->ctx = c; }
     } restore{A, A->ctx};
     A->ctx = ec;
-    vec_estimate_start<T>(*ec, n, w0.as<T>());
+    vec_estimate_start<T>(*ec, n, w0.as<T>(), start_period());
     MF_CK(cudaMemsetAsync(w1.ptr, 0, n * sizeof(T), ec->stream));
     OpRef<T>     Aop(A);
     JacobiPre<T> P;
     P.ctx = ec;
     P.A   = A;
-    cg_lanczos<T>(*ec, Aop, &P, w1.as<T>(), w0.as<T>(), 1e-10, eig_cg_iterations, 8, &cg_ws, host_rec.p);
+    cg_lanczos<T>(*ec, Aop, &P, w1.as<T>(), w0.as<T>(), estimate_tol(), eig_cg_iterations, 8, &cg_ws,
+                  host_rec.p);
     est_ctx = ec;
   }
 
@@ -412,7 +501,7 @@ namespace mfgpu
     Context *ec = est_ctx;
     est_ctx     = nullptr;
     MF_CK(cudaStreamSynchronize(ec->stream));
-    set_bounds(lanczos_collect(host_rec.p, eig_cg_iterations, 1e-10));
+    set_bounds(lanczos_collect(host_rec.p, eig_cg_iterations, estimate_tol()));
   }
 
   template <typename T>

@@ -2,6 +2,8 @@
 // and the solid (Newton-Newmark) and heat (backward Euler) drivers.
 #pragma once
 
+#include <cmath>
+
 #include "mf_host.h"
 
 namespace mfgpu
@@ -69,6 +71,16 @@ namespace mfgpu
                    double tol, int maxit, bool record = false,
                    bool fixed_iterations = false, DevBuf *ws = nullptr);
 
+  // nb independent systems of n unknowns each, stacked in x and b, solved
+  // together: every operator and preconditioner application covers all of
+  // them (one launch per stage), the scalars are per system, and each
+  // system's iterates are those cg_solve gives it alone; a system stops
+  // updating when it has converged.  its[i]: system i's iterations;
+  // returns false if a system did not converge in maxit.  nb <= 6 (the
+  // context's scalar slots).
+  bool cg_solve_batched(Context &c, LinOp<double> &A, Precond<double> *P, double *x, const double *b, int nb,
+                        size_t n, const std::vector<double> &tol, int maxit, std::vector<int> &its, DevBuf *ws);
+
   // CG as used for the Chebyshev eigenvalue estimate: the same iterates as
   // cg_solve(record = true), with the Lanczos coefficients recorded on the
   // device and the convergence test made every `check` iterations (the
@@ -107,6 +119,19 @@ namespace mfgpu
     HostPinned host_rec; // Lanczos records of a deferred estimate
     Context   *est_ctx = nullptr;
     void estimate();
+    // a batch of identical problems (a batched heat operator) starts every
+    // block from the single problem's vector and stops at the single
+    // problem's residual, so its bounds equal the single problem's
+    size_t
+    start_period() const
+    {
+      return A->heat_batch ? A->geom.n_nodes : 0;
+    }
+    double
+    estimate_tol() const
+    {
+      return A->heat_batch ? 1e-10 * std::sqrt(double(A->nc)) : 1e-10;
+    }
     // the same estimate enqueued on another context's stream (the operator
     // launches there meanwhile), finished by estimate_end()
     void estimate_begin(Context *ec);

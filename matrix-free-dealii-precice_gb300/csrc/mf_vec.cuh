@@ -43,11 +43,11 @@ namespace mfgpu
 
   template <typename T>
   __global__ void
-  k_estimate_start(size_t n, T mean, T *__restrict__ x)
+  k_estimate_start(size_t n, size_t period, T mean, T *__restrict__ x)
   {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
-      x[i] = (i % 11 == 0 ? T(0) : T(1)) - mean;
+      x[i] = ((i % period) % 11 == 0 ? T(0) : T(1)) - mean;
   }
 
   template <typename TD, typename TS>

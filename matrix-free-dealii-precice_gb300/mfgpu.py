@@ -664,6 +664,16 @@ class Server:
         _check(lib().mfgpu_server_stats(self.h, C.byref(mr), C.byref(b)))
         return mr.value, b.value
 
+    def set_max_batch(self, k):
+        """Heat requests of one shape solved together, at most (1: no batching)."""
+        _check(lib().mfgpu_server_set_max_batch(self.h, int(k)))
+
+    def batch_stats(self):
+        """(requests that ran in a batch of two or more, largest batch)"""
+        n, k = C.c_longlong(), C.c_int()
+        _check(lib().mfgpu_server_batch_stats(self.h, C.byref(n), C.byref(k)))
+        return n.value, k.value
+
     def pool_stats(self):
         """(requests that reused a resident problem, requests that built one)"""
         reused, built = C.c_longlong(), C.c_longlong()

@@ -85,3 +85,52 @@ def test_resident_problems_are_reused_with_the_same_results(ctx):
         assert abs(a.cg_iterations - b.cg_iterations) <= 1
         assert a.newton_iterations == b.newton_iterations
         assert abs(a.solution_norm - b.solution_norm) <= 1e-9 * abs(a.solution_norm)
+
+
+def _heat_request(degree, n_ref, seed, n_steps=1):
+    r = mfgpu.Request()
+    r.kind = 0
+    hp = r.heat
+    hp.mesh = W.to_lib_mesh(mfgpu, W.unit_cube_heat(degree, n_ref))
+    hp.dt, hp.n_steps = 0.1, n_steps
+    hp.solver = mfgpu.solver_params("gmg", tol=1e-8, cheb_range=15.0, cheb_eig_its=10, mg_precision=32,
+                                    coarse_fp64=True, fp64_emulation=True)
+    c, w, a = W.gaussian_source(seed)
+    hp.n_gauss = 8
+    for j in range(8):
+        for d in range(3):
+            hp.g_center[j][d] = c[j, d]
+        hp.g_width[j] = w[j]
+        hp.g_amp[j] = a[j]
+    return r
+
+
+@pytest.mark.parametrize("degree,n_ref", [(2, 3), (3, 4)])
+def test_batched_heat_requests_equal_their_solo_solves(ctx, degree, n_ref):
+    """Continuous batching: heat requests of one shape queued behind a busy
+    worker are solved together (one operator, V-cycle and CG over all of
+    them); each result equals the request solved alone."""
+    heat = [_heat_request(degree, n_ref, seed) for seed in (31, 32, 33, 34)]
+    # a solid request keeps the single worker busy while the heat requests queue
+    blocker = next(r for r in W.serving_requests(mfgpu, 30, seed=5, max_heat_ref=3, solid_k=(8,), degrees=(3,))
+                   if r.kind == 1)
+    srv = mfgpu.Server(0, 1, 0.5)
+    ids = [srv.submit(blocker)] + [srv.submit(r) for r in heat]
+    batched = [srv.wait(i) for i in ids][1:]
+    n_batched, largest = srv.batch_stats()
+    srv.close()
+    assert n_batched >= 2 and largest >= 2, (n_batched, largest)
+    solo_srv = mfgpu.Server(0, 1, 0.5)
+    solo_srv.set_max_batch(1)
+    solo = [solo_srv.wait(solo_srv.submit(r)) for r in heat]
+    assert solo_srv.batch_stats() == (0, 1)
+    solo_srv.close()
+    for a, b in zip(solo, batched):
+        assert a.status == 0, a.message
+        assert b.status == 0, b.message
+        assert abs(a.cg_iterations - b.cg_iterations) <= 1, (a.cg_iterations, b.cg_iterations)
+        assert abs(a.solution_norm - b.solution_norm) <= 1e-9 * abs(a.solution_norm)
+        assert a.n_dofs == b.n_dofs
+    # the problems differ: the batch did not hand one result to all
+    norms = [b.solution_norm for b in batched]
+    assert len(set(norms)) == len(norms)
