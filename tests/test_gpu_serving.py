@@ -1,8 +1,9 @@
 """The request server: independent heat and neo-Hookean solves submitted
-together run concurrently (their kernels overlap on separate streams), and
-every result equals the same request solved alone: same CG and Newton
-iteration counts (+-1 CG for round-off in the scatter), solution norms
-within 1e-9 relative, watchpoints within 1e-8 relative."""
+together run concurrently (their kernels overlap on separate streams, and
+heat requests of one shape are solved as one batch), and every result
+equals the same request solved alone: same CG and Newton iteration counts
+(+-1 CG for round-off in the scatter), solution norms within 1e-9 relative,
+watchpoints within 1e-8 relative."""
 import numpy as np
 import pytest
 
@@ -12,8 +13,11 @@ import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def run_all(reqs, workers):
+def run_all(reqs, workers, max_batch=None):
+    """All requests submitted at once; max_batch 1 solves each alone."""
     srv = mfgpu.Server(0, workers, 0.5)
+    if max_batch is not None:
+        srv.set_max_batch(max_batch)
     ids = [srv.submit(r) for r in reqs]
     res = [srv.wait(i) for i in ids]
     max_running, _ = srv.stats()
@@ -24,7 +28,7 @@ def run_all(reqs, workers):
 def test_results_alone_equal_results_in_the_mix(ctx):
     reqs = W.serving_requests(mfgpu, 12, seed=3, max_heat_ref=4, solid_k=(2, 4),
                               degrees=(1, 2, 3))
-    alone, mr1 = run_all(reqs, 1)
+    alone, mr1 = run_all(reqs, 1, max_batch=1)
     mix, mr4 = run_all(reqs, 4)
     assert mr1 == 1
     assert mr4 > 1, "requests did not overlap"
@@ -79,7 +83,7 @@ def test_resident_problems_are_reused_with_the_same_results(ctx):
         srv.wait(srv.submit(r))
     pooled = [srv.wait(srv.submit(r)) for r in again]
     srv.close()
-    fresh, _ = run_all(again, 1)
+    fresh, _ = run_all(again, 1, max_batch=1)
     for a, b in zip(pooled, fresh):
         assert a.status == 0 and b.status == 0
         assert abs(a.cg_iterations - b.cg_iterations) <= 1
