@@ -617,9 +617,12 @@ def extra_solid_newton(mfgpu, W, ctx):
 def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
     """Heat operator on the unit cube with 64^3 cells, Q1..Q6: vmult DoF/s
     and achieved GB/s (B_alg = 2 s N_dof + 4 s N_cells) in FP64 (native and
-    double-float) and FP32 (sum factorization on the CUDA cores, and for
-    Q1..Q5 the element-matrix product on the tensor cores); FP32-GMG vs
-    FP64-GMG CG to 1e-8 with the seeded Gaussian source."""
+    double-float) and FP32, with the default cell kernel (the tensor-product
+    kernel for FP32 Q1..Q3 and FP64 Q1..Q2, sum factorization through the
+    Gauss points above), the sum-factorization kernel beside it where the
+    default differs (`*_sumfact`), and for FP32 Q1..Q5 the element-matrix
+    product on the tensor cores; FP32-GMG vs FP64-GMG CG to 1e-8 with the
+    seeded Gaussian source."""
     res = []
     c, w, a = W.gaussian_source(0)
     for deg in range(1, 7):
@@ -628,9 +631,13 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
         n = W.n_dofs(spec, 1)
         cells = 64 ** 3
         row = {"degree": deg, "n_dofs": n}
-        for label, prec, emul in (("fp64", 64, False), ("fp64_df64", 64, True), ("fp32", 32, False),
-                                  ("fp32_tensor", 32, False)):
+        for label, prec, emul in (("fp64", 64, False), ("fp64_sumfact", 64, False), ("fp64_df64", 64, True),
+                                  ("fp32", 32, False), ("fp32_sumfact", 32, False), ("fp32_tensor", 32, False)):
             if label == "fp32_tensor" and deg > 5:
+                continue
+            # the sum-factorization kernel beside the default where the
+            # default is the tensor-product kernel (FP32 Q1-Q3, FP64 Q1-Q2)
+            if label.endswith("_sumfact") and deg > (3 if prec == 32 else 2):
                 continue
             dt = torch.float64 if prec == 64 else torch.float32
             op = mfgpu.LaplaceOperator(ctx, mesh, -1, prec, True, delta_t=0.1)
@@ -638,6 +645,8 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
                 op.set_fp64_emulation(True)
             if label == "fp32_tensor":
                 op.set_cell_kernel("tensor")
+            if label.endswith("_sumfact"):
+                op.set_cell_kernel("line")
             src = torch.rand(n, dtype=dt, device=dev) * 2 - 1
             dst = torch.zeros_like(src)
             op.vmult(dst, src)
@@ -906,9 +915,13 @@ KERNEL_CASES = {
     "nh_df64_q4": ("nh", 4, 3, 64, "df64"),
     "nh_fp32_q3": ("nh", 3, 4, 32, "native"),   # finest level of the mixed solve, 2,773,155 DoFs
     "nh_fp32_q3_scalar_ref": ("nh_sr", 3, 4, 32, "native"),
-    "heat_fp32_q2": ("heat", 2, 6, 32, "native"),  # unit cube 64^3 cells
+    "heat_fp32_q1": ("heat", 1, 6, 32, "native"),  # unit cube 64^3 cells (tensor-product kernel)
+    "heat_fp32_q2": ("heat", 2, 6, 32, "native"),
+    "heat_fp32_q3": ("heat", 3, 6, 32, "native"),
     "heat_fp32_q6": ("heat", 6, 6, 32, "native"),
     "heat_fp64_q2": ("heat", 2, 6, 64, "native"),
+    "heat_fp32_q2_sumfact": ("heat", 2, 6, 32, "line"),  # sum factorization through the Gauss points
+    "heat_fp64_q2_sumfact": ("heat", 2, 6, 64, "line"),
     "heat_fp32_q2_tensor": ("heat", 2, 6, 32, "tensor"),  # element matrix on the tensor cores
     "heat_fp32_q3_tensor": ("heat", 3, 6, 32, "tensor"),
     "heat_fp32_q4_tensor": ("heat", 4, 6, 32, "tensor"),
@@ -942,8 +955,8 @@ def run_kernel_case(args):
         spec = W.unit_cube_heat(deg, nref)
         n = W.n_dofs(spec, 1)
         op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, prec, True, delta_t=0.1)
-        if arith == "tensor":
-            op.set_cell_kernel("tensor")
+        if arith in ("tensor", "line"):
+            op.set_cell_kernel(arith)
     src = torch.from_numpy(W.uniform_vector(n, 3)).to(dev).to(dt)
     dst = torch.zeros_like(src)
     for _ in range(max(args.steps, 1)):

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
          "-diag-suppress", "550,177"]
 HOST_TUS = ["mf_ops", "mf_solvers", "mf_drivers", "mf_capi", "mf_capi_solvers", "mf_noalloc", "mf_serve",
-            "mf_kernels2d", "mf_heat_em"]
+            "mf_kernels2d", "mf_heat_em", "mf_heat_tp"]
 DEGREE_NS = [2, 3, 4, 5, 6, 7]
 
 

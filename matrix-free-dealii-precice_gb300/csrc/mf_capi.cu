@@ -333,8 +333,17 @@ extern "C"
   {
     return guarded([&] {
       need(op, "op");
-      if (mode < 0 || mode > 3)
-        throw Error(ERR_ARG, "cell kernel must be 0 (by grid size), 1 (line), 2 (point) or 3 (tensor cores)");
+      if (mode < 0 || mode > 4)
+        throw Error(ERR_ARG,
+                    "cell kernel must be 0 (by grid size), 1 (line), 2 (point), 3 (tensor cores) or 4 (tensor product)");
+      if (mode == 4)
+        {
+          Operator *o = op->op.get();
+          if (!dynamic_cast<HeatOperator *>(o) || o->geom.dim != 3 || o->arith != 0 ||
+              !heat_tp_supported(o->basis.N, o->precision))
+            throw Error(ERR_UNSUPPORTED, "the tensor-product cell kernel applies to three-dimensional heat operators "
+                                         "of degree 1..3 (FP32) or 1..2 (native FP64)");
+        }
       if (mode == 3)
         {
           Operator *o = op->op.get();

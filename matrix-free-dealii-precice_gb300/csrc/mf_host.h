@@ -290,7 +290,8 @@ namespace mfgpu
     int       arith       = 0; // 0 native, 1 double-float (FP64 operators only)
     int       scatter     = 0; // 0 atomic adds, 1 parity colours with plain adds (deterministic)
     int       cell_kernel = 0; // 0 by grid size, 1 line-parallel, 2 point-parallel (ApplyArgs::kernel),
-                               // 3 element matrix on the tensor cores (FP32 heat, degree <= 5)
+                               // 3 element matrix on the tensor cores (FP32 heat, degree <= 5),
+                               // 4 tensor-product form (heat; 0 takes it where supported)
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;

@@ -66,6 +66,29 @@ namespace mfgpu
   cudaError_t launch_heat_em(const HostBasis &b, const LevelGeom &g, bool constrained, const void *bmat,
                              const float *src, float *dst, int *err, cudaStream_t s);
 
+  // the heat operator in its tensor-product form (1D mass and stiffness
+  // matrices, 7 sweeps per cell), one thread per column segment of zlen
+  // cells, registers only (mf_heat_tp.cu): FP32 N = 2..4, FP64 N = 2..3,
+  // three-dimensional levels; dst += A src over the cells of z-planes
+  // [zc0, zc1), grid.y = problem of a batch
+  struct HeatTPArgs
+  {
+    double      kdt;
+    bool        constrained;
+    int         zc0, zc1, zlen;
+    const void *src;
+    void       *dst;
+    int         batch   = 1;
+    size_t      bstride = 0;
+  };
+  bool        heat_tp_supported(int N, int precision);
+  int         heat_tp_zlen(const LevelGeom &g, int zc0, int zc1);
+  cudaError_t launch_heat_tp(const HostBasis &b, const LevelGeom &g, int precision, const HeatTPArgs &a,
+                             cudaStream_t s);
+  // launches of fewer cells than this keep the point-parallel kernel for
+  // the heat operator instead of the tensor-product one
+  constexpr unsigned TP_MIN_CELLS = 512;
+
   // launches of fewer cells than this take the point-parallel kernel
   // (native FP64: up to 4096 cells)
   constexpr unsigned POINT_CELLS = 1024;

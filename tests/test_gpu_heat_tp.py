@@ -1,0 +1,120 @@
+"""The heat operator in its tensor-product form (cell kernel 4: the element
+operator as sums of products of the 1D mass and stiffness matrices, one
+thread per cell column segment in registers) against the oracle's vmult
+(heat_transfer.h:236-250) and against the sum-factorization kernel.
+
+Tolerances: FP64 1e-12 relative l2 (the operator parity bar), FP32 5e-5 as
+the other FP32 operator tests.  The meshes exercise what the kernel's
+work split depends on: rows of cells shorter and longer than a warp (the
+x-neighbour exchange by shuffles across warp ends), column segments that do
+not divide the z extent (the z-carry of results between the cells of a
+segment), anisotropic cells, constrained faces on every side
+and none, and cell ranges (the z-slabs of the host-buffer vmult)."""
+import numpy as np
+import pytest
+
+import mfgpu
+import oracle as O
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = {32: 5e-5, 64: 1e-12}
+DEGREES = {32: [1, 2, 3], 64: [1, 2]}
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy().astype(np.float64)
+
+
+def _spec(degree, rep, n_ref, hi, boundary_id, dirichlet):
+    return dict(degree=degree, n_ref=n_ref, rep=rep, lo=(0.0, 0.0, 0.0), hi=hi,
+                boundary_id=boundary_id, dirichlet=dirichlet)
+
+
+# (repetitions, refinements, upper corner, boundary ids, dirichlet)
+MESHES = {
+    # 6 x 4 x 10 cells: rows shorter than a warp, anisotropic cells, two
+    # clamped faces
+    "short_rows": ((3, 2, 5), 1, (1.5, 0.7, 2.0), (1, 0, 2, 0, 0, 2), [(1, 1), (2, 1)]),
+    # 40 x 3 x 7 cells: rows across warp ends, every face clamped
+    "long_rows": ((40, 3, 7), 0, (4.0, 0.3, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)]),
+    # 33 x 2 x 9 cells, no constraint
+    "free": ((33, 2, 9), 0, (1.0, 0.2, 0.9), (0, 0, 0, 0, 0, 0), []),
+    # 64 x 64 x 39 cells: column segments of 4 cells (enough columns for the
+    # launch heuristic), the last one of 3
+    "segments": ((64, 64, 39), 0, (1.0, 1.0, 0.6), (1, 0, 2, 0, 0, 2), [(1, 1), (2, 1)]),
+}
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("mesh", sorted(MESHES))
+def test_tensor_product_heat_vmult(ctx, precision, mesh):
+    rep, nref, hi, bid, dirichlet = MESHES[mesh]
+    for degree in DEGREES[precision]:
+        spec = _spec(degree, rep, nref, hi, bid, dirichlet)
+        m = W.to_lib_mesh(mfgpu, spec)
+        n = W.n_dofs(spec, 1)
+        dt = np.float32 if precision == 32 else np.float64
+        src = W.uniform_vector(n, 11 + degree, dt)
+        constrained = bool(dirichlet)
+        ref = O.heat_vmult(W.to_oracle_mesh(O, spec), nref, 0.1, src.astype(np.float64),
+                           constrained=constrained)
+        op = mfgpu.LaplaceOperator(ctx, m, -1, precision, constrained, delta_t=0.1)
+        d_src = dev(src)
+        d_sf, d_tp = dev(np.zeros_like(src)), dev(np.zeros_like(src))
+        op.set_cell_kernel("line")
+        op.vmult(d_sf, d_src)
+        op.set_cell_kernel("tp")
+        op.vmult(d_tp, d_src)
+        tp, sf = host(d_tp), host(d_sf)
+        assert rel(tp, ref) < TOL[precision], (degree, rel(tp, ref))
+        assert rel(tp, sf) < TOL[precision], (degree, rel(tp, sf))
+        # vmult_add adds
+        op.vmult_add(d_tp, d_src)
+        assert rel(host(d_tp), 2 * ref) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_tensor_product_heat_default_and_host_buffers(ctx, precision):
+    """A 16^3-cell Q2 level takes kernel 4 by default (4096 cells); the
+    overlapped host-buffer vmult (z-slabs of cells) gives the same result."""
+    spec = W.unit_cube_heat(2, 4)
+    m = W.to_lib_mesh(mfgpu, spec)
+    n = W.n_dofs(spec, 1)
+    dt = np.float32 if precision == 32 else np.float64
+    src = W.uniform_vector(n, 5, dt)
+    ref = O.heat_vmult(W.to_oracle_mesh(O, spec), 4, 0.1, src.astype(np.float64))
+    op = mfgpu.LaplaceOperator(ctx, m, -1, precision, True, delta_t=0.1)
+    d = dev(np.zeros_like(src))
+    before = mfgpu.launch_count()
+    op.vmult(d, dev(src))
+    assert mfgpu.launch_count() - before == 1
+    assert rel(host(d), ref) < TOL[precision]
+    if precision == 64:
+        out = np.zeros_like(src)
+        for chunks in (1, 4):
+            op.set_host_chunks(chunks)
+            op.vmult_host(out, src)
+            assert rel(out, ref) < TOL[64], chunks
+
+
+def test_tensor_product_heat_rejects_unsupported(ctx):
+    spec = W.unit_cube_heat(4, 1)
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 32, True, delta_t=0.1)
+    with pytest.raises(mfgpu.MfgpuError):
+        op.set_cell_kernel("tp")
+    spec = W.unit_cube_heat(3, 1)
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    with pytest.raises(mfgpu.MfgpuError):
+        op.set_cell_kernel("tp")
