@@ -333,10 +333,10 @@ extern "C"
   {
     return guarded([&] {
       need(op, "op");
-      if (mode < 0 || mode > 4)
-        throw Error(ERR_ARG,
-                    "cell kernel must be 0 (by grid size), 1 (line), 2 (point), 3 (tensor cores) or 4 (tensor product)");
-      if (mode == 4)
+      if (mode < 0 || mode > 5)
+        throw Error(ERR_ARG, "cell kernel must be 0 (by grid size), 1 (line), 2 (point), 3 (tensor cores), "
+                             "4 (tensor product) or 5 (tensor product, TMA-staged bricks)");
+      if (mode >= 4)
         {
           Operator *o = op->op.get();
           if (!dynamic_cast<HeatOperator *>(o) || o->geom.dim != 3 || o->arith != 0 ||

@@ -28,18 +28,22 @@
 //   * along z, the top node plane of a cell is the bottom plane of the next
 //     cell of the column: its values are carried in registers, and its
 //     results are added into the next cell's before they are written;
-//   * along x, a thread takes the values of its last node column from the
-//     next lane (warp shuffle) and hands the results of that column to it,
-//     so each node column is written by one lane; a warp's last lane and a
-//     row's last cell write their own last column.
+//   * along x, a thread hands the results of its last node column to the
+//     next lane (warp shuffle), so each node column is written by one lane;
+//     a warp's last lane and a row's last cell write their own last column.
 // The remaining shared nodes (the y faces, the warp and column-segment
 // ends) are added with atomics, as in the sum-factorization kernel.
 // Constraints are those of the sum-factorization kernel: constrained
 // source values read as zero, constrained rows get dst += src from the one
 // cell that owns the node (local index < p in every direction, or the last
 // cell along it).
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <tuple>
+#include <vector>
 
 #include "mf_host.h"
 
@@ -48,6 +52,9 @@ namespace mfgpu
   namespace tp
   {
     constexpr int THREADS = 128;
+#ifndef MF_TP_MIN_BLOCKS
+#define MF_TP_MIN_BLOCKS 1
+#endif
 
     // the six 1D matrices, symmetric, scaled as above
     template <int N, typename T>
@@ -137,7 +144,7 @@ namespace mfgpu
     // dst += A src over the cells of z-planes [zc0, zc1) of one level
     // (grid.y = problem of a batch: vectors at offset blockIdx.y * bstride)
     template <int N, typename T, bool CON>
-    __global__ void __launch_bounds__(THREADS)
+    __global__ void __launch_bounds__(THREADS, MF_TP_MIN_BLOCKS)
     heat_tp_kernel(const __grid_constant__ HeatTP<N, T> m, const __grid_constant__ CellGeom<T> g,
                    const int zlen, const int zc0, const int zc1, const T *__restrict__ src,
                    T *__restrict__ dst)
@@ -177,19 +184,16 @@ namespace mfgpu
                (k == 0 && bz0 && cz == 0) || (k == P && bz1 && cz == C2 - 1);
       };
       // node plane k of cell cz into v[b][a] (zero where constrained or
-      // inactive); the last node column comes from lane+1 where it holds it
+      // inactive).  Every lane loads its whole row: the last node column,
+      // which lane+1 loads too, comes from the same L1 line; taking it by
+      // a shuffle would make the prefetch of the next cell wait for its loads.
       auto gather_plane = [&](int k, int cz, bool act, T (&v)[N][N]) {
         const size_t base = col + Nxy * size_t(cz * P + k);
 #pragma unroll
         for (int b = 0; b < N; ++b)
-          {
 #pragma unroll
-            for (int a = 0; a < P; ++a)
-              v[b][a] = (act && !(CON && constrained(a, b, k, cz))) ? __ldg(src + base + Nx * b + a) : T(0);
-            const T right = __shfl_down_sync(FULL, v[b][0], 1);
-            v[b][P]       = rmerge ? right :
-                            (act && !(CON && constrained(P, b, k, cz))) ? __ldg(src + base + Nx * b + P) : T(0);
-          }
+          for (int a = 0; a < N; ++a)
+            v[b][a] = (act && !(CON && constrained(a, b, k, cz))) ? __ldg(src + base + Nx * b + a) : T(0);
       };
       // results of node plane k of cell cz: the last node column goes to
       // lane+1 where it holds it, the first column receives lane-1's
@@ -296,6 +300,307 @@ namespace mfgpu
       scatter_plane(P, czn - 1, active && czn > cz0, carry);
     }
 
+    // -------------------------------------------------------------------
+    // FP32 bricks staged by the tensor memory accelerator.
+    //
+    // A CTA takes bricks of 32 x BY x BZ cells (one cell per thread, x
+    // fastest) in a persistent loop.  The brick's node box, (32p+1) x
+    // (BY p+1) x (BZ p+1) nodes, is loaded row by row (x-rows of the node
+    // grid) by 1D tiled TMA copies into shared memory, double-buffered: the
+    // next brick's rows are in flight while the current brick is computed.
+    // A row of the node grid starts at any float (the row length C0 p + 1 is
+    // odd in general), and a TMA box must start on 16 bytes: each copy starts
+    // at the row's first node rounded down to a multiple of 4 and is ROW
+    // floats long; the cells index the row from its offset.  Each thread
+    // computes its cell from the staged values (the same sweeps as above)
+    // and adds its results into a shared-memory output box (shared atomics);
+    // the box is then added to dst row by row by TMA bulk reductions
+    // (cp.reduce.async.bulk.tensor .add), which the L2 performs atomically,
+    // so no global atomics are issued.  The rounded copies load and add
+    // slack floats of the neighbouring rows: loads are ignored, adds are of
+    // zero.  The tensor maps are 1D over the whole vector (all problems of a
+    // batch), so copies past its end are clipped by the hardware.
+    // Constrained nodes: read as zero by the cells; the node's owning brick
+    // (node index below the brick's upper face in every direction, or on
+    // the domain's last one) writes src into its output box, the others 0.
+    // Every mbarrier wait is bounded: past its limit the CTA sets the error
+    // flag, waits for its copies in flight and returns.
+    // Measured on 64^3 cells (CUDA events, L2 flushed), it is slower than the
+    // register kernel for every brick shape tried (32 x 2 x 2, 32 x 4 x 2,
+    // 32 x 4 x 4): Q1 14.0 against 9.9 us, Q2 40.6 against 26-30 us, Q3
+    // 126 against 80 us; the brick's serial phases (wait, compute, shared
+    // atomics, barrier, reduction) leave the SMs idle where the register
+    // kernel's independent threads overlap.  So it is an opt-in (cell
+    // kernel 5), not the default.
+    // -------------------------------------------------------------------
+    template <int N, int BY, int BZ>
+    struct Brick
+    {
+      static constexpr int P       = N - 1;
+      static constexpr int BX      = 32;
+      static constexpr int THREADS = BX * BY * BZ;
+      static constexpr int RX      = BX * P + 1;                // nodes of a row in the brick
+      static constexpr int RY = BY * P + 1, RZ = BZ * P + 1;    // rows
+      static constexpr int ROWS    = RY * RZ;
+      static constexpr int ROW     = (RX + 3 + 3) / 4 * 4;      // floats per copy: up to 3 of slack before
+      static constexpr int PITCH   = (ROW * 4 + 127) / 128 * 32; // floats per shared row (128-byte rows)
+      static constexpr int BOX     = ROWS * PITCH;
+      // in[2], out, 2 mbarriers, and 128 bytes to align the base
+      static constexpr size_t SMEM = size_t(3 * BOX) * 4 + 64 + 128;
+      static_assert(ROW <= 256, "TMA box too long");
+    };
+
+    __device__ __forceinline__ uint32_t
+    saddr(const void *p)
+    {
+      return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    }
+
+    __device__ __forceinline__ bool
+    mbar_try_wait(uint64_t *bar, unsigned parity)
+    {
+      uint32_t ok;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(ok)
+                   : "r"(saddr(bar)), "r"(parity)
+                   : "memory");
+      return ok != 0;
+    }
+
+    // bounded wait: false after the limit
+    __device__ __forceinline__ bool
+    mbar_wait(uint64_t *bar, unsigned parity)
+    {
+      for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(bar, parity))
+          return true;
+      return false;
+    }
+
+    template <int N, int BY, int BZ, bool CON>
+    __global__ void __launch_bounds__(Brick<N, BY, BZ>::THREADS)
+    heat_tp_tma_kernel(const __grid_constant__ CUtensorMap tsrc, const __grid_constant__ CUtensorMap tdst,
+                       const __grid_constant__ HeatTP<N, float> m, const __grid_constant__ CellGeom<float> g,
+                       const float *__restrict__ srcv, int *err)
+    {
+      using B                = Brick<N, BY, BZ>;
+      constexpr int P        = N - 1;
+      extern __shared__ __align__(128) unsigned char sm_raw[];
+      // TMA rows start on 128 bytes
+      float *sm = reinterpret_cast<float *>(sm_raw + ((128u - (saddr(sm_raw) & 127u)) & 127u));
+      float    *in0  = sm;
+      float    *out  = sm + 2 * B::BOX;
+      uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + 3 * B::BOX);
+      const int C0 = g.C[0], C1 = g.C[1], C2 = g.C[2];
+      const int Nx = g.Nn[0], Ny = g.Nn[1], Nz = g.Nn[2];
+      const int nbx = (C0 + B::BX - 1) / B::BX, nby = (C1 + BY - 1) / BY, nbz = (C2 + BZ - 1) / BZ;
+      const unsigned nbrick = unsigned(nbx) * unsigned(nby) * unsigned(nbz) * g.batch;
+      const int tid = int(threadIdx.x), lane = tid & 31, warp = tid >> 5;
+      const int tx = tid % B::BX, ty = (tid / B::BX) % BY, tz = tid / (B::BX * BY);
+
+      struct Pos
+      {
+        int      x0, y0, z0, ry, rz; // first node, rows in y and z
+        unsigned prob;
+        int      bx, by, bz;
+      };
+      auto pos = [&](unsigned br) {
+        Pos q;
+        q.bx      = int(br % unsigned(nbx));
+        unsigned r = br / unsigned(nbx);
+        q.by      = int(r % unsigned(nby));
+        r /= unsigned(nby);
+        q.bz      = int(r % unsigned(nbz));
+        q.prob    = r / unsigned(nbz);
+        q.x0      = q.bx * B::BX * P;
+        q.y0      = q.by * BY * P;
+        q.z0      = q.bz * BZ * P;
+        q.ry      = min(B::RY, Ny - q.y0);
+        q.rz      = min(B::RZ, Nz - q.z0);
+        return q;
+      };
+      // flat index of the first node of row (j, l) of a brick
+      auto row_flat = [&](const Pos &q, int j, int l) {
+        return size_t(q.prob) * g.n_nodes + size_t(q.x0) +
+               size_t(Nx) * (size_t(q.y0 + j) + size_t(Ny) * size_t(q.z0 + l));
+      };
+      // warp 0 issues the rows of brick q into buffer buf
+      auto issue_loads = [&](const Pos &q, int buf) {
+        if (warp != 0)
+          return;
+        uint64_t *bar = mbar + buf;
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+                       "r"(unsigned(q.ry * q.rz * B::ROW * 4))
+                       : "memory");
+        __syncwarp();
+        float *dstb = in0 + buf * B::BOX;
+        for (int r = lane; r < q.ry * q.rz; r += 32)
+          {
+            const int    j = r % q.ry, l = r / q.ry;
+            const size_t f = row_flat(q, j, l);
+            const int    c = int(f & ~size_t(3));
+            asm volatile("cp.async.bulk.tensor.1d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2}], [%3];" ::"r"(saddr(dstb + (l * B::RY + j) * B::PITCH)),
+                         "l"(&tsrc), "r"(c), "r"(saddr(bar))
+                         : "memory");
+          }
+      };
+
+      if (tid == 0)
+        {
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(mbar + 0)) : "memory");
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(mbar + 1)) : "memory");
+          asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+      __syncthreads();
+      // copies issued into each buffer and waited for (the k-th copy into a
+      // buffer completes its mbarrier's phase k-1, parity (k-1) & 1)
+      unsigned issued[2] = {0u, 0u}, landed[2] = {0u, 0u};
+      unsigned br = blockIdx.x;
+      if (br < nbrick)
+        {
+          issue_loads(pos(br), 0);
+          ++issued[0];
+        }
+      bool failed = false;
+      for (int it = 0; br < nbrick; ++it, br += gridDim.x)
+        {
+          const int  buf = it & 1;
+          const Pos  q   = pos(br);
+          // the previous brick's reductions have read the output box
+          if (warp == 0)
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          __syncthreads();
+          {
+            float4 *o4 = reinterpret_cast<float4 *>(out);
+            for (int i = tid; i < B::BOX / 4; i += B::THREADS)
+              o4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          // the next brick's rows into the other buffer (its cells were
+          // computed before the barrier above)
+          const unsigned brn = br + gridDim.x;
+          if (brn < nbrick)
+            {
+              issue_loads(pos(brn), buf ^ 1);
+              ++issued[buf ^ 1];
+            }
+          if (mbar_wait(mbar + buf, (issued[buf] - 1) & 1u))
+            ++landed[buf];
+          else
+            {
+              failed = true;
+              if (tid == 0)
+                atomicOr(err, 8);
+            }
+          if (__syncthreads_or(failed))
+            {
+              failed = true;
+              break;
+            }
+          const float *inb = in0 + buf * B::BOX;
+          const int    cx = q.bx * B::BX + tx, cy = q.by * BY + ty, cz = q.bz * BZ + tz;
+          const bool   act = cx < C0 && cy < C1 && cz < C2;
+          if (act)
+            {
+              const bool fx0 = CON && cx == 0 && (g.face_mask[0] & 1u);
+              const bool fx1 = CON && cx == C0 - 1 && (g.face_mask[1] & 1u);
+              const bool fy0 = CON && cy == 0 && (g.face_mask[2] & 1u);
+              const bool fy1 = CON && cy == C1 - 1 && (g.face_mask[3] & 1u);
+              const bool fz0 = CON && cz == 0 && (g.face_mask[4] & 1u);
+              const bool fz1 = CON && cz == C2 - 1 && (g.face_mask[5] & 1u);
+              auto con = [&](int a, int b, int k) {
+                return (a == 0 && fx0) || (a == P && fx1) || (b == 0 && fy0) || (b == P && fy1) ||
+                       (k == 0 && fz0) || (k == P && fz1);
+              };
+              // shared index of local node (a, b, k): row (ty p + b, tz p + k),
+              // from the row's offset
+              int rowi[N][N];
+#pragma unroll
+              for (int k = 0; k < N; ++k)
+#pragma unroll
+                for (int b = 0; b < N; ++b)
+                  {
+                    const int j = ty * P + b, l = tz * P + k;
+                    rowi[k][b] = (l * B::RY + j) * B::PITCH + int(row_flat(q, j, l) & 3) + tx * P;
+                  }
+              float x[N][N][N];
+#pragma unroll
+              for (int k = 0; k < N; ++k)
+#pragma unroll
+                for (int b = 0; b < N; ++b)
+#pragma unroll
+                  for (int a = 0; a < N; ++a)
+                    x[k][b][a] = (CON && con(a, b, k)) ? 0.f : inb[rowi[k][b] + a];
+              float y[N][N][N];
+              cell_apply<N, float>(m, x, y);
+#pragma unroll
+              for (int k = 0; k < N; ++k)
+#pragma unroll
+                for (int b = 0; b < N; ++b)
+#pragma unroll
+                  for (int a = 0; a < N; ++a)
+                    if (!(CON && con(a, b, k)))
+                      atomicAdd(out + rowi[k][b] + a, y[k][b][a]);
+            }
+          __syncthreads();
+          if (CON)
+            {
+              // constrained nodes this brick owns: dst += src
+              const int  nx    = min(B::RX, Nx - q.x0);
+              const bool touch = (q.bx == 0 && (g.face_mask[0] & 1u)) || (q.bx == nbx - 1 && (g.face_mask[1] & 1u)) ||
+                                 (q.by == 0 && (g.face_mask[2] & 1u)) || (q.by == nby - 1 && (g.face_mask[3] & 1u)) ||
+                                 (q.bz == 0 && (g.face_mask[4] & 1u)) || (q.bz == nbz - 1 && (g.face_mask[5] & 1u));
+              if (touch)
+                for (int i = tid; i < nx * q.ry * q.rz; i += B::THREADS)
+                  {
+                    const int a = i % nx, r = i / nx, j = r % q.ry, l = r / q.ry;
+                    const int ix = q.x0 + a, iy = q.y0 + j, iz = q.z0 + l;
+                    const bool c = (ix == 0 && (g.face_mask[0] & 1u)) || (ix == Nx - 1 && (g.face_mask[1] & 1u)) ||
+                                   (iy == 0 && (g.face_mask[2] & 1u)) || (iy == Ny - 1 && (g.face_mask[3] & 1u)) ||
+                                   (iz == 0 && (g.face_mask[4] & 1u)) || (iz == Nz - 1 && (g.face_mask[5] & 1u));
+                    const bool own = (a < B::RX - 1 || ix == Nx - 1) && (j < B::RY - 1 || iy == Ny - 1) &&
+                                     (l < B::RZ - 1 || iz == Nz - 1);
+                    if (c && own)
+                      {
+                        const int si = (l * B::RY + j) * B::PITCH + int(row_flat(q, j, l) & 3) + a;
+                        out[si]      = srcv[row_flat(q, j, l) + a];
+                      }
+                  }
+            }
+          // the output box to dst: generic-proxy writes made visible to the
+          // bulk copies, then one reduction per row
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncthreads();
+          if (warp == 0)
+            {
+              for (int r = lane; r < q.ry * q.rz; r += 32)
+                {
+                  const int    j = r % q.ry, l = r / q.ry;
+                  const size_t f = row_flat(q, j, l);
+                  const int    c = int(f & ~size_t(3));
+                  asm volatile("cp.reduce.async.bulk.tensor.1d.global.shared::cta.add.tile.bulk_group"
+                               " [%0, {%1}], [%2];" ::"l"(&tdst),
+                               "r"(c), "r"(saddr(out + (l * B::RY + j) * B::PITCH))
+                               : "memory");
+                }
+              asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+        }
+      if (failed)
+        {
+          // copies still in flight into this CTA's buffers: wait for them
+          // (bounded) before the CTA exits
+          for (int b = 0; b < 2; ++b)
+            if (issued[b] > landed[b])
+              mbar_wait(mbar + b, (issued[b] - 1) & 1u);
+        }
+      if (warp == 0)
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+
     template <int N, typename T>
     HeatTP<N, T>
     make_matrices(const HostBasis &b, const LevelGeom &g, double kdt)
@@ -354,6 +659,105 @@ namespace mfgpu
                                                            static_cast<T *>(a.dst));
       return cudaGetLastError();
     }
+    // cuTensorMapEncodeTiled through the runtime's driver entry point (no
+    // link against libcuda)
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+    EncodeFn
+    encode_fn()
+    {
+      static std::once_flag once;
+      static EncodeFn       fn = nullptr;
+      std::call_once(once, [] {
+        void                           *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+              cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+          fn = reinterpret_cast<EncodeFn>(p);
+      });
+      return fn;
+    }
+
+    // 1D map over n floats at ptr, boxes of `box` floats, zero fill
+    bool
+    encode_rows(CUtensorMap *map, const void *ptr, size_t n, int box)
+    {
+      EncodeFn fn = encode_fn();
+      if (!fn || (reinterpret_cast<uintptr_t>(ptr) & 15u) || n == 0 || n >= (size_t(1) << 32))
+        return false;
+      const cuuint64_t dim[1]    = {cuuint64_t(n)};
+      const cuuint64_t stride[1] = {cuuint64_t(n * 4)}; // unused for rank 1
+      const cuuint32_t bx[1]     = {cuuint32_t(box)};
+      const cuuint32_t es[1]     = {1};
+      return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, const_cast<void *>(ptr), dim, stride, bx, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+
+    // resident CTAs per SM of a kernel and the SM count, per device
+    template <typename K>
+    int
+    resident_ctas(K kernel, int threads, size_t smem, int &sms)
+    {
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess)
+        return 0;
+      static std::mutex                                        mu;
+      static std::vector<std::tuple<const void *, int, int, int>> seen; // kernel, device, ctas, sms
+      std::lock_guard<std::mutex>                              l(mu);
+      for (auto &e : seen)
+        if (std::get<0>(e) == reinterpret_cast<const void *>(kernel) && std::get<1>(e) == dev)
+          {
+            sms = std::get<3>(e);
+            return std::get<2>(e);
+          }
+      int ctas = 0;
+      if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kernel, threads, smem) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+      seen.emplace_back(reinterpret_cast<const void *>(kernel), dev, ctas, sms);
+      return ctas;
+    }
+
+    // the TMA brick kernel over all cells (false: not applicable, nothing
+    // launched)
+    template <int N, int BY, int BZ>
+    bool
+    launch_tma(const HostBasis &b, const LevelGeom &g, const HeatTPArgs &a, cudaStream_t s, cudaError_t &e)
+    {
+      using Bk            = Brick<N, BY, BZ>;
+      const unsigned nb   = unsigned(a.batch > 1 ? a.batch : 1);
+      const size_t   tot  = g.n_nodes * nb;
+      CUtensorMap    ms, md;
+      // row coordinates are 32-bit signed
+      if (!a.err || tot >= (size_t(1) << 31) || !encode_rows(&ms, a.src, tot, Bk::ROW) ||
+          !encode_rows(&md, a.dst, tot, Bk::ROW))
+        return false;
+      auto k   = a.constrained ? heat_tp_tma_kernel<N, BY, BZ, true> : heat_tp_tma_kernel<N, BY, BZ, false>;
+      int  sms = 0;
+      const int ctas = resident_ctas(k, Bk::THREADS, Bk::SMEM, sms);
+      if (ctas <= 0)
+        return false;
+      const HeatTP<N, float> h  = make_matrices<N, float>(b, g, a.kdt);
+      CellGeom<float>        cg = make_cell_geom<float>(g);
+      cg.batch                  = nb;
+      cg.bstride                = nb > 1 ? a.bstride : 0;
+      const size_t bricks = size_t((g.C[0] + Bk::BX - 1) / Bk::BX) * size_t((g.C[1] + BY - 1) / BY) *
+                            size_t((g.C[2] + BZ - 1) / BZ) * nb;
+      const size_t grid = std::min(bricks, size_t(ctas) * size_t(sms));
+      if (grid == 0)
+        {
+          e = cudaSuccess;
+          return true;
+        }
+      k<<<unsigned(grid), Bk::THREADS, Bk::SMEM, s>>>(ms, md, h, cg, static_cast<const float *>(a.src), a.err);
+      e = cudaGetLastError();
+      return true;
+    }
   } // namespace tp
 
   bool
@@ -363,13 +767,14 @@ namespace mfgpu
   }
 
   int
-  heat_tp_zlen(const LevelGeom &g, int zc0, int zc1)
+  heat_tp_zlen(const LevelGeom &g, int zc0, int zc1, int N, int precision)
   {
-    // the longest column segment (at most 4 cells) that keeps 8 warps per
-    // SM of the 152 busy
+    // measured on 64^3 cells: two cells per thread where the next cell's
+    // values are prefetched (FP32 Q1-Q2, FP64 Q1), one otherwise; one as
+    // well where two would leave fewer than 256 threads per SM
     const size_t ncol = size_t(g.C[0]) * size_t(g.C[1]);
     const int    nz   = zc1 - zc0;
-    int          zlen = 4;
+    int          zlen = size_t(N) * N * N * (precision / 8) <= 27 * 4 ? 2 : 1;
     while (zlen > 1 && ncol * size_t((nz + zlen - 1) / zlen) < size_t(152) * 256)
       zlen /= 2;
     return zlen;
@@ -380,6 +785,19 @@ namespace mfgpu
   {
     if (g.dim == 2 || !heat_tp_supported(b.N, precision) || a.zc0 < 0 || a.zc1 > g.C[2] || a.zlen < 1)
       return cudaErrorInvalidValue;
+    // FP32 Q1 and Q2 over all cells, 16-byte aligned vectors, on request:
+    // the TMA brick kernel
+    if (precision == 32 && a.tma && a.zc0 == 0 && a.zc1 == g.C[2] && (a.batch <= 1 || a.bstride == g.n_nodes))
+      {
+        cudaError_t e  = cudaSuccess;
+        bool        ok = false;
+        if (b.N == 2)
+          ok = tp::launch_tma<2, 2, 2>(b, g, a, s, e);
+        else if (b.N == 3)
+          ok = tp::launch_tma<3, 2, 2>(b, g, a, s, e);
+        if (ok)
+          return e;
+      }
     if (precision == 32)
       switch (b.N)
         {

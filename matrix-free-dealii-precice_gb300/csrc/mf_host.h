@@ -291,7 +291,8 @@ namespace mfgpu
     int       scatter     = 0; // 0 atomic adds, 1 parity colours with plain adds (deterministic)
     int       cell_kernel = 0; // 0 by grid size, 1 line-parallel, 2 point-parallel (ApplyArgs::kernel),
                                // 3 element matrix on the tensor cores (FP32 heat, degree <= 5),
-                               // 4 tensor-product form (heat; 0 takes it where supported)
+                               // 4 tensor-product form (heat; 0 takes it where supported), 5 the
+                               // same with FP32 Q1-Q2 bricks staged by TMA
     DevBuf    inv_diag;
     DevBuf    diag;
     bool      diag_ready = false;

@@ -67,9 +67,10 @@ namespace mfgpu
                              const float *src, float *dst, int *err, cudaStream_t s);
 
   // the heat operator in its tensor-product form (1D mass and stiffness
-  // matrices, 7 sweeps per cell), one thread per column segment of zlen
-  // cells, registers only (mf_heat_tp.cu): FP32 N = 2..4, FP64 N = 2..3,
-  // three-dimensional levels; dst += A src over the cells of z-planes
+  // matrices, 7 sweeps per cell; mf_heat_tp.cu): one thread per column
+  // segment of zlen cells, registers only (FP32 N = 2..4, FP64 N = 2..3),
+  // or, on request, for FP32 N = 2..3 over all cells bricks staged in shared
+  // memory by TMA; three-dimensional levels; dst += A src over the cells of z-planes
   // [zc0, zc1), grid.y = problem of a batch
   struct HeatTPArgs
   {
@@ -80,9 +81,14 @@ namespace mfgpu
     void       *dst;
     int         batch   = 1;
     size_t      bstride = 0;
+    // FP32 Q1-Q2 over all cells: the bricks staged by TMA instead of the
+    // register kernel (measured slower; opt-in); err receives the bounded
+    // waits' timeout flag (8)
+    bool        tma = false;
+    int        *err = nullptr;
   };
   bool        heat_tp_supported(int N, int precision);
-  int         heat_tp_zlen(const LevelGeom &g, int zc0, int zc1);
+  int         heat_tp_zlen(const LevelGeom &g, int zc0, int zc1, int N, int precision);
   cudaError_t launch_heat_tp(const HostBasis &b, const LevelGeom &g, int precision, const HeatTPArgs &a,
                              cudaStream_t s);
   // launches of fewer cells than this keep the point-parallel kernel for

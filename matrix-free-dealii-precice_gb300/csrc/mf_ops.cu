@@ -758,30 +758,32 @@ namespace mfgpu
     // the heat operator's tensor-product kernel: by default from
     // TP_MIN_CELLS cells on (below, the point-parallel kernel), over whole
     // z-planes of cells, atomic scatter
-    if (a.kind == 0 && (a.kernel == 0 || a.kernel == 4) && !a.colored && arith == 0 &&
+    if (a.kind == 0 && (a.kernel == 0 || a.kernel == 4 || a.kernel == 5) && !a.colored && arith == 0 &&
         heat_tp_supported(basis.N, precision))
       {
         const size_t layer = size_t(geom.C[0]) * size_t(geom.C[1]);
         const size_t b0 = c1 > c0 ? c0 : 0, b1 = c1 > c0 ? std::min(c1, geom.n_cells) : geom.n_cells;
         if (b0 % layer == 0 && (b1 % layer == 0 || b1 == geom.n_cells) &&
-            (a.kernel == 4 || b1 - b0 >= TP_MIN_CELLS))
+            (a.kernel >= 4 || b1 - b0 >= TP_MIN_CELLS))
           {
             HeatTPArgs t;
             t.kdt         = a.kdt;
             t.constrained = a.constrained;
             t.zc0         = int(b0 / layer);
             t.zc1         = int((b1 + layer - 1) / layer);
-            t.zlen        = heat_tp_zlen(geom, t.zc0, t.zc1);
+            t.zlen        = heat_tp_zlen(geom, t.zc0, t.zc1, basis.N, precision);
             t.src         = src;
             t.dst         = dst;
             t.batch       = a.batch;
             t.bstride     = a.bstride;
+            t.tma         = a.kernel == 5;
+            t.err         = ctx->err.as<int>();
             MF_CK(launch_heat_tp(basis, geom, precision, t, s));
             count_launch();
             return;
           }
       }
-    if (a.kernel == 4)
+    if (a.kernel >= 4)
       a.kernel = 0;
     if (a.kernel == 3)
       {

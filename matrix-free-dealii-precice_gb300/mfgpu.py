@@ -267,9 +267,10 @@ class _Operator:
     def set_cell_kernel(self, mode):
         """0 by grid size, 1 line-parallel, 2 point-parallel, 3 tensor cores
         (FP32 heat operators, element matrix), 4 tensor product (heat
-        operators of low degree, 1D mass and stiffness matrices)."""
+        operators of low degree, 1D mass and stiffness matrices, registers),
+        5 tensor product with FP32 Q1-Q2 bricks staged by TMA."""
         _check(lib().mfgpu_operator_set_cell_kernel(
-            self.h, {"auto": 0, "line": 1, "point": 2, "tensor": 3, "tp": 4}.get(mode, mode)))
+            self.h, {"auto": 0, "line": 1, "point": 2, "tensor": 3, "tp": 4, "tp_tma": 5}.get(mode, mode)))
 
     def set_dense(self, enable=True):
         """Dense copy of a small operator (assembled now; used while the

@@ -75,14 +75,18 @@ def test_tensor_product_heat_vmult(ctx, precision, mesh):
         d_sf, d_tp = dev(np.zeros_like(src)), dev(np.zeros_like(src))
         op.set_cell_kernel("line")
         op.vmult(d_sf, d_src)
-        op.set_cell_kernel("tp")
-        op.vmult(d_tp, d_src)
-        tp, sf = host(d_tp), host(d_sf)
-        assert rel(tp, ref) < TOL[precision], (degree, rel(tp, ref))
-        assert rel(tp, sf) < TOL[precision], (degree, rel(tp, sf))
-        # vmult_add adds
-        op.vmult_add(d_tp, d_src)
-        assert rel(host(d_tp), 2 * ref) < TOL[precision]
+        sf = host(d_sf)
+        # "tp": registers; "tp_tma": FP32 Q1-Q2 bricks staged by TMA,
+        # registers otherwise
+        for mode in ("tp", "tp_tma"):
+            op.set_cell_kernel(mode)
+            op.vmult(d_tp, d_src)
+            tp = host(d_tp)
+            assert rel(tp, ref) < TOL[precision], (mode, degree, rel(tp, ref))
+            assert rel(tp, sf) < TOL[precision], (mode, degree, rel(tp, sf))
+            # vmult_add adds
+            op.vmult_add(d_tp, d_src)
+            assert rel(host(d_tp), 2 * ref) < TOL[precision]
 
 
 @pytest.mark.parametrize("precision", [32, 64])
@@ -118,3 +122,21 @@ def test_tensor_product_heat_rejects_unsupported(ctx):
     op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
     with pytest.raises(mfgpu.MfgpuError):
         op.set_cell_kernel("tp")
+
+
+def test_tensor_product_heat_unaligned_vectors(ctx):
+    """Vectors that do not start on 16 bytes (views at an offset of one
+    float) cannot be staged by TMA: the register kernel serves them."""
+    import torch
+    spec = _spec(2, (40, 3, 7), 0, (4.0, 0.3, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)])
+    n = W.n_dofs(spec, 1)
+    src = W.uniform_vector(n, 21, np.float32)
+    ref = O.heat_vmult(W.to_oracle_mesh(O, spec), 0, 0.1, src.astype(np.float64))
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 32, True, delta_t=0.1)
+    op.set_cell_kernel("tp_tma")
+    big_src = torch.zeros(n + 1, dtype=torch.float32, device="cuda")
+    big_src[1:] = dev(src)
+    big_dst = torch.zeros(n + 1, dtype=torch.float32, device="cuda")
+    op.vmult(big_dst[1:], big_src[1:])
+    assert rel(host(big_dst[1:]), ref) < TOL[32]
+    assert float(big_dst[0]) == 0.0
