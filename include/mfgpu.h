@@ -192,16 +192,17 @@ int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
 int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
 /* cell kernel of vmult: 0 by grid size (default: point-parallel, one
  * thread per quadrature point, below 1024 cells, up to 4096 in native
- * FP64; line-parallel above; heat operators of degree 1..3 in FP32 and
- * 1..2 in native FP64 take kernel 4 from 512 cells on), 1 line-parallel,
+ * FP64; line-parallel above; three-dimensional heat operators in FP32 and
+ * native FP64 take kernel 4 from 512 cells on), 1 line-parallel,
  * 2 point-parallel, 3 tensor cores (three-dimensional FP32 heat
  * operators, degree 1..5: the cells' common element matrix applied to
  * batches of 128 cells by tcgen05.mma in TF32 with a three-term split,
- * FP32 accuracy), 4 tensor product (three-dimensional heat operators,
- * degree 1..3 in FP32, 1..2 in native FP64: the element operator as sums
- * of products of the 1D mass and stiffness matrices, exact for the
- * QGauss(p+1) integral on the level's affine cells, one thread per cell
- * in registers), 5 the tensor product with the cells' nodes staged in
+ * FP32 accuracy), 4 tensor product (three-dimensional heat operators in
+ * FP32 or native FP64: the element operator as sums of products of the 1D
+ * mass and stiffness matrices, exact for the QGauss(p+1) integral on the
+ * level's affine cells, 7 sweeps per cell; one thread per cell in
+ * registers at degree 1..2, (p+1)^2 threads per cell through shared
+ * memory above), 5 the tensor product with the cells' nodes staged in
  * shared memory by TMA row copies and the results added back by TMA bulk
  * reductions (FP32, degree 1..2, 16-byte aligned vectors; measured slower
  * than 4, other cases take 4).  The results agree to round-off. */

@@ -342,7 +342,7 @@ extern "C"
           if (!dynamic_cast<HeatOperator *>(o) || o->geom.dim != 3 || o->arith != 0 ||
               !heat_tp_supported(o->basis.N, o->precision))
             throw Error(ERR_UNSUPPORTED, "the tensor-product cell kernel applies to three-dimensional heat operators "
-                                         "of degree 1..3 (FP32) or 1..2 (native FP64)");
+                                         "in FP32 or native FP64");
         }
       if (mode == 3)
         {

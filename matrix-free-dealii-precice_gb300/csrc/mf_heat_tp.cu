@@ -1,6 +1,7 @@
 // The heat operator (mass + dt k Laplace, LaplaceOperator::do_operation_on_
-// cell, heat_transfer.h:236-250) on box levels in its tensor-product form,
-// one thread per cell, registers only.
+// cell, heat_transfer.h:236-250) on box levels in its tensor-product form:
+// one thread per cell in registers at degrees 1-2, (p+1)^2 threads per cell
+// through shared memory at degrees 3-6.
 //
 // Every cell of a box level is the same affine brick h0 x h1 x h2 and the
 // coefficient is constant (heat_transfer.h:63-71).  The QGauss(p+1) cell
@@ -20,7 +21,7 @@
 // it costs 7 (p+1)^4 multiply-adds per cell, against 12 (p+1)^4 plus the
 // quadrature-point work for evaluate / integrate through the Gauss points.
 //
-// Work split (heat_tp_kernel): thread = a column of `zlen` consecutive cells
+// Degrees 1-2 (heat_tp_kernel): thread = a column of `zlen` consecutive cells
 // along z, threads of a warp consecutive along x.  The (p+1)^3 values of a
 // cell live in registers; all sweeps are register FMAs with the 1D
 // matrices in the kernel's constant bank.  Nodes shared between cells are
@@ -298,6 +299,158 @@ namespace mfgpu
         }
       // the top plane of the segment's last cell
       scatter_plane(P, czn - 1, active && czn > cz0, carry);
+    }
+
+    template <int N, typename T>
+    HeatTP<N, T> make_matrices(const HostBasis &b, const LevelGeom &g, double kdt);
+
+    // -------------------------------------------------------------------
+    // Higher degrees: the same seven sweeps with the cell in shared memory.
+    //
+    // A block takes CPB cells with N^2 threads per cell.  Thread (a, b)
+    // gathers the z-column (a, b) of its cell into registers and applies the
+    // z-matrices there (U = Mz x, V = Kz x), then the cell's lines are swept
+    // through shared memory: thread (a, k) sweeps the y-lines (U <- My U,
+    // V <- Ky U + My V, in place), thread (b, k) the x-lines
+    // (y = Ax U + Mx V, in place), and thread (a, b) reads its z-column of y
+    // back and scatters it (atomics; constrained rows as in the other cell
+    // kernels).  Two arrays of N^3 per cell, three barriers.
+    // -------------------------------------------------------------------
+    template <int N, typename T>
+    __host__ __device__ constexpr int
+    blk_cells()
+    {
+      return N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 3 : 2;
+    }
+
+    template <int N, typename T, bool CON>
+    __global__ void __launch_bounds__(blk_cells<N, T>() * N * N)
+    heat_tp_block_kernel(const __grid_constant__ HeatTP<N, T> m, const __grid_constant__ CellGeom<T> g,
+                         const T *__restrict__ src, T *__restrict__ dst)
+    {
+      constexpr int N2 = N * N, N3 = N * N * N, P = N - 1;
+      constexpr int CPB = blk_cells<N, T>();
+      extern __shared__ __align__(16) unsigned char smraw[];
+      src += size_t(blockIdx.y) * g.bstride;
+      dst += size_t(blockIdx.y) * g.bstride;
+      const int      lc   = int(threadIdx.x) / N2;
+      const int      l    = int(threadIdx.x) - lc * N2;
+      const int      i0   = l % N, i1 = l / N; // (a, b), (a, k) or (b, k) by phase
+      const unsigned cell = g.cell_begin + blockIdx.x * CPB + unsigned(lc);
+      const bool     act  = cell < g.cell_end;
+      const unsigned cc   = act ? cell : g.cell_begin;
+      const int      cx   = int(cc % unsigned(g.C[0]));
+      const int      cyz  = int(cc / unsigned(g.C[0]));
+      const int      cy   = cyz % g.C[1], cz = cyz / g.C[1];
+      T *U = reinterpret_cast<T *>(smraw) + size_t(lc) * 2 * N3; // [k][b][a]
+      T *V = U + N3;
+      const size_t Nx = size_t(g.Nn[0]), Nxy = size_t(g.Nn[0]) * size_t(g.Nn[1]);
+      const int    ix = cx * P + i0, iy = cy * P + i1;
+      const size_t colb = size_t(ix) + Nx * size_t(iy) + Nxy * size_t(cz * P);
+      auto con = [&](int k) {
+        return CON && ((node_mask(g.face_mask, g.Nn, ix, iy, cz * P + k) & 1u) != 0u);
+      };
+      // gather the z-column (a, b) = (i0, i1) and apply the z-matrices
+      {
+        T x[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          x[k] = (act && !con(k)) ? __ldg(src + colb + Nxy * k) : T(0);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+          {
+            U[i * N2 + i1 * N + i0] = dot_row<N, T>(m.Mz, i, x);
+            V[i * N2 + i1 * N + i0] = dot_row<N, T>(m.Kz, i, x);
+          }
+      }
+      __syncthreads();
+      // y-lines (a, k) = (i0, i1): U <- My U, V <- Ky U + My V
+      {
+        T u[N], v[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+          {
+            u[j] = U[i1 * N2 + j * N + i0];
+            v[j] = V[i1 * N2 + j * N + i0];
+          }
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+          {
+            T s = dot_row<N, T>(m.Ky, i, u);
+#pragma unroll
+            for (int j = 0; j < N; ++j)
+              s = fma(m.My[i][j], v[j], s);
+            U[i1 * N2 + i * N + i0] = dot_row<N, T>(m.My, i, u);
+            V[i1 * N2 + i * N + i0] = s;
+          }
+      }
+      __syncthreads();
+      // x-lines (b, k) = (i0, i1): y = Ax U + Mx V, into U
+      {
+        T u[N], v[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+          {
+            u[j] = U[i1 * N2 + i0 * N + j];
+            v[j] = V[i1 * N2 + i0 * N + j];
+          }
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+          {
+            T s = dot_row<N, T>(m.Ax, i, u);
+#pragma unroll
+            for (int j = 0; j < N; ++j)
+              s = fma(m.Mx[i][j], v[j], s);
+            U[i1 * N2 + i0 * N + i] = s;
+          }
+      }
+      __syncthreads();
+      if (!act)
+        return;
+      // scatter the z-column (a, b) = (i0, i1)
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        {
+          T *d = dst + colb + Nxy * k;
+          if (con(k))
+            {
+              const bool owner = (i0 < P || cx == g.C[0] - 1) && (i1 < P || cy == g.C[1] - 1) &&
+                                 (k < P || cz == g.C[2] - 1);
+              if (owner)
+                *d += __ldg(src + colb + Nxy * k);
+            }
+          else
+            atomicAdd(d, U[k * N2 + i1 * N + i0]);
+        }
+    }
+
+    template <int N, typename T>
+    cudaError_t
+    launch_block(const HostBasis &b, const LevelGeom &g, const HeatTPArgs &a, cudaStream_t s)
+    {
+      constexpr int     CPB  = blk_cells<N, T>();
+      const size_t      smem = size_t(CPB) * 2 * N * N * N * sizeof(T);
+      const HeatTP<N, T> h   = make_matrices<N, T>(b, g, a.kdt);
+      CellGeom<T>        cg  = make_cell_geom<T>(g);
+      cg.batch               = unsigned(a.batch > 1 ? a.batch : 1);
+      cg.bstride             = a.batch > 1 ? a.bstride : 0;
+      const size_t layer     = size_t(g.C[0]) * size_t(g.C[1]);
+      cg.cell_begin          = unsigned(size_t(a.zc0) * layer);
+      cg.cell_end            = unsigned(size_t(a.zc1) * layer);
+      const size_t cells     = cg.cell_end - cg.cell_begin;
+      if (cells == 0)
+        return cudaSuccess;
+      const size_t grid = (cells + CPB - 1) / CPB;
+      if (grid > 0x7fffffffu || cg.batch > 65535u || smem > 48 * 1024)
+        return cudaErrorInvalidValue;
+      const dim3 gr(unsigned(grid), cg.batch);
+      if (a.constrained)
+        heat_tp_block_kernel<N, T, true><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const T *>(a.src),
+                                                                       static_cast<T *>(a.dst));
+      else
+        heat_tp_block_kernel<N, T, false><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const T *>(a.src),
+                                                                        static_cast<T *>(a.dst));
+      return cudaGetLastError();
     }
 
     // -------------------------------------------------------------------
@@ -763,7 +916,7 @@ namespace mfgpu
   bool
   heat_tp_supported(int N, int precision)
   {
-    return precision == 32 ? (N >= 2 && N <= 4) : (N >= 2 && N <= 3);
+    return (precision == 32 || precision == 64) && N >= 2 && N <= 7;
   }
 
   int
@@ -798,18 +951,28 @@ namespace mfgpu
         if (ok)
           return e;
       }
+    // one thread per cell in registers at Q1-Q2, the block kernel above
+    // (measured on 64^3 cells: FP32 Q2 31 us in registers, 72 us in blocks;
+    // FP32 Q3 80 against 73 us, FP64 Q2 314 against 510 us)
     if (precision == 32)
       switch (b.N)
         {
           case 2: return tp::launch<2, float>(b, g, a, s);
           case 3: return tp::launch<3, float>(b, g, a, s);
-          case 4: return tp::launch<4, float>(b, g, a, s);
+          case 4: return tp::launch_block<4, float>(b, g, a, s);
+          case 5: return tp::launch_block<5, float>(b, g, a, s);
+          case 6: return tp::launch_block<6, float>(b, g, a, s);
+          case 7: return tp::launch_block<7, float>(b, g, a, s);
         }
     else
       switch (b.N)
         {
           case 2: return tp::launch<2, double>(b, g, a, s);
           case 3: return tp::launch<3, double>(b, g, a, s);
+          case 4: return tp::launch_block<4, double>(b, g, a, s);
+          case 5: return tp::launch_block<5, double>(b, g, a, s);
+          case 6: return tp::launch_block<6, double>(b, g, a, s);
+          case 7: return tp::launch_block<7, double>(b, g, a, s);
         }
     return cudaErrorInvalidValue;
   }

@@ -67,10 +67,11 @@ namespace mfgpu
                              const float *src, float *dst, int *err, cudaStream_t s);
 
   // the heat operator in its tensor-product form (1D mass and stiffness
-  // matrices, 7 sweeps per cell; mf_heat_tp.cu): one thread per column
-  // segment of zlen cells, registers only (FP32 N = 2..4, FP64 N = 2..3),
-  // or, on request, for FP32 N = 2..3 over all cells bricks staged in shared
-  // memory by TMA; three-dimensional levels; dst += A src over the cells of z-planes
+  // matrices, 7 sweeps per cell; mf_heat_tp.cu), N = 2..7, FP32 and FP64:
+  // one thread per column segment of zlen cells in registers (N = 2..3),
+  // N^2 threads per cell through shared memory (N = 4..7), or, on request,
+  // for FP32 N = 2..3 over all cells bricks staged in shared memory by TMA;
+  // three-dimensional levels; dst += A src over the cells of z-planes
   // [zc0, zc1), grid.y = problem of a batch
   struct HeatTPArgs
   {

@@ -3,8 +3,9 @@ operator as sums of products of the 1D mass and stiffness matrices, one
 thread per cell column segment in registers) against the oracle's vmult
 (heat_transfer.h:236-250) and against the sum-factorization kernel.
 
-Tolerances: FP64 1e-12 relative l2 (the operator parity bar), FP32 5e-5 as
-the other FP32 operator tests.  The meshes exercise what the kernel's
+Degrees 1-6: one thread per cell in registers up to FP32 Q3 and FP64 Q2,
+the shared-memory block form above.  Tolerances: FP64 1e-12 relative l2
+(the operator parity bar), FP32 5e-5 as the other FP32 operator tests.  The meshes exercise what the kernel's
 work split depends on: rows of cells shorter and longer than a warp (the
 x-neighbour exchange by shuffles across warp ends), column segments that do
 not divide the z extent (the z-carry of results between the cells of a
@@ -19,7 +20,7 @@ import workloads as W
 
 pytestmark = pytest.mark.gpu
 TOL = {32: 5e-5, 64: 1e-12}
-DEGREES = {32: [1, 2, 3], 64: [1, 2]}
+DEGREES = [1, 2, 3, 4, 5, 6]
 
 
 def rel(a, b):
@@ -61,7 +62,10 @@ MESHES = {
 @pytest.mark.parametrize("mesh", sorted(MESHES))
 def test_tensor_product_heat_vmult(ctx, precision, mesh):
     rep, nref, hi, bid, dirichlet = MESHES[mesh]
-    for degree in DEGREES[precision]:
+    # the 64 x 64 x 39 mesh tests the column segments of the register
+    # kernel (degrees 1-2); the others every degree (registers up to FP32
+    # Q3 and FP64 Q2, the block kernel above)
+    for degree in DEGREES if mesh != "segments" else [1, 2]:
         spec = _spec(degree, rep, nref, hi, bid, dirichlet)
         m = W.to_lib_mesh(mfgpu, spec)
         n = W.n_dofs(spec, 1)
@@ -114,12 +118,16 @@ def test_tensor_product_heat_default_and_host_buffers(ctx, precision):
 
 
 def test_tensor_product_heat_rejects_unsupported(ctx):
-    spec = W.unit_cube_heat(4, 1)
-    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 32, True, delta_t=0.1)
+    """Double-float operators and two-dimensional meshes keep their own
+    kernels."""
+    spec = W.unit_cube_heat(2, 1)
+    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    op.set_fp64_emulation(True)
     with pytest.raises(mfgpu.MfgpuError):
         op.set_cell_kernel("tp")
-    spec = W.unit_cube_heat(3, 1)
-    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
+    m2 = mfgpu.make_mesh(2, 2, (1, 1), (0.0, 0.0), (1.0, 1.0), boundary_id=(1, 0, 0, 0),
+                         dirichlet=[(1, 1)])
+    op = mfgpu.LaplaceOperator(ctx, m2, -1, 32, True, delta_t=0.1)
     with pytest.raises(mfgpu.MfgpuError):
         op.set_cell_kernel("tp")
 
