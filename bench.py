@@ -618,11 +618,11 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
     """Heat operator on the unit cube with 64^3 cells, Q1..Q6: vmult DoF/s
     and achieved GB/s (B_alg = 2 s N_dof + 4 s N_cells) in FP64 (native and
     double-float) and FP32, with the default cell kernel (the tensor-product
-    kernel for FP32 Q1..Q3 and FP64 Q1..Q2, sum factorization through the
-    Gauss points above), the sum-factorization kernel beside it where the
-    default differs (`*_sumfact`), and for FP32 Q1..Q5 the element-matrix
-    product on the tensor cores; FP32-GMG vs FP64-GMG CG to 1e-8 with the
-    seeded Gaussian source."""
+    form: 1D mass and stiffness matrices, 7 sweeps per cell), the
+    sum-factorization kernel through the Gauss points beside it
+    (`*_sumfact`), and for FP32 Q1..Q5 the element-matrix product on the
+    tensor cores; FP32-GMG vs FP64-GMG CG to 1e-8 with the seeded Gaussian
+    source."""
     res = []
     c, w, a = W.gaussian_source(0)
     for deg in range(1, 7):
@@ -634,10 +634,6 @@ def extra_degree_sweep(torch, mfgpu, W, ctx, dev, stream, flush, peak):
         for label, prec, emul in (("fp64", 64, False), ("fp64_sumfact", 64, False), ("fp64_df64", 64, True),
                                   ("fp32", 32, False), ("fp32_sumfact", 32, False), ("fp32_tensor", 32, False)):
             if label == "fp32_tensor" and deg > 5:
-                continue
-            # the sum-factorization kernel beside the default where the
-            # default is the tensor-product kernel (FP32 Q1-Q3, FP64 Q1-Q2)
-            if label.endswith("_sumfact") and deg > (3 if prec == 32 else 2):
                 continue
             dt = torch.float64 if prec == 64 else torch.float32
             op = mfgpu.LaplaceOperator(ctx, mesh, -1, prec, True, delta_t=0.1)
@@ -830,6 +826,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
     span = time.perf_counter() - t0
     max_running, budget = srv.stats()
     reused, built = srv.pool_stats()
+    batched, largest = srv.batch_stats()
     srv.close()
     lat = np.array([r.latency_seconds for r in res])
     errors = sum(1 for r in res if r.status != 0)
@@ -863,6 +860,9 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
             "solves_per_s": n_requests / span, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)), "max_concurrent": max_running,
             "resident_problems": {"reused": reused, "built": built},
+            "batching": {"requests_in_batches": batched, "largest_batch": largest,
+                         "rule": "queued heat requests of the same shape and step count join the one a worker "
+                                 "takes (one operator, V-cycle and CG for all), up to 4"},
             "errors": errors,
             "closed_loop_first100_per_s": {"1_worker": one, f"{workers}_workers": many},
             "baseline_fp64_one_at_a_time": {"solves_per_s": n_requests / bspan,

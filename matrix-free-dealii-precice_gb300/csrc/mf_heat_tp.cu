@@ -314,7 +314,8 @@ namespace mfgpu
     // V <- Ky U + My V, in place), thread (b, k) the x-lines
     // (y = Ax U + Mx V, in place), and thread (a, b) reads its z-column of y
     // back and scatters it (atomics; constrained rows as in the other cell
-    // kernels).  Two arrays of N^3 per cell, three barriers.
+    // kernels).  Two arrays of N^3 per cell, three barriers; the line
+    // products in even-odd form (below).
     // -------------------------------------------------------------------
     template <int N, typename T>
     __host__ __device__ constexpr int
@@ -323,9 +324,105 @@ namespace mfgpu
       return N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 3 : 2;
     }
 
+    // Even-odd form of a symmetric matrix with M[N-1-i][N-1-j] = M[i][j]
+    // (the 1D mass and stiffness matrices: Gauss-Lobatto nodes and Gauss
+    // points are symmetric about the cell centre).  With H = N/2, sums
+    // e_j = v_j + v_{N-1-j} and differences o_j = v_j - v_{N-1-j} (j < H):
+    //   y_i = E e + O o (+ M[i][H] v_H),  y_{N-1-i} = E e - O o (+ ...),
+    //   y_H = sum_j M[H][j] e_j + M[H][H] v_H                  (odd N)
+    // with E_ij = (M_ij + M_i,N-1-j)/2, O_ij = (M_ij - M_i,N-1-j)/2: about
+    // half the products of a plain matrix-vector product.
+    template <int N, typename T>
+    struct EOMat
+    {
+      static constexpr int H = N / 2;
+      T E[H][H], O[H][H];
+      T C[H + 1]; // odd N: M[i][H] for i < H, then M[H][H]
+      T R[H];     // odd N: M[H][j] for j < H
+    };
+
+    template <int N, typename T>
+    struct HeatTPEO
+    {
+      EOMat<N, T> Mx, Ax, My, Ky, Mz, Kz;
+    };
+
+    template <int N, typename T>
+    struct EOSplit
+    {
+      T e[N / 2], o[N / 2], m;
+    };
+
+    template <int N, typename T>
+    __device__ __forceinline__ EOSplit<N, T>
+    eo_split(const T (&v)[N])
+    {
+      EOSplit<N, T> r;
+#pragma unroll
+      for (int j = 0; j < N / 2; ++j)
+        {
+          r.e[j] = v[j] + v[N - 1 - j];
+          r.o[j] = v[j] - v[N - 1 - j];
+        }
+      r.m = (N & 1) ? v[N / 2] : T(0);
+      return r;
+    }
+
+    template <int N, typename T>
+    struct EOAcc
+    {
+      T se[N / 2], so[N / 2], sm;
+    };
+
+    // acc (+)= M v, v given by its split; FIRST: start the sums
+    template <int N, typename T, bool FIRST>
+    __device__ __forceinline__ void
+    eo_acc(EOAcc<N, T> &acc, const EOMat<N, T> &M, const EOSplit<N, T> &v)
+    {
+      constexpr int H = N / 2;
+#pragma unroll
+      for (int i = 0; i < H; ++i)
+        {
+          T se = FIRST ? M.E[i][0] * v.e[0] : fma(M.E[i][0], v.e[0], acc.se[i]);
+          T so = FIRST ? M.O[i][0] * v.o[0] : fma(M.O[i][0], v.o[0], acc.so[i]);
+#pragma unroll
+          for (int j = 1; j < H; ++j)
+            {
+              se = fma(M.E[i][j], v.e[j], se);
+              so = fma(M.O[i][j], v.o[j], so);
+            }
+          if (N & 1)
+            se = fma(M.C[i], v.m, se);
+          acc.se[i] = se;
+          acc.so[i] = so;
+        }
+      if (N & 1)
+        {
+          T sm = FIRST ? M.C[H] * v.m : fma(M.C[H], v.m, acc.sm);
+#pragma unroll
+          for (int j = 0; j < H; ++j)
+            sm = fma(M.R[j], v.e[j], sm);
+          acc.sm = sm;
+        }
+    }
+
+    template <int N, typename T>
+    __device__ __forceinline__ void
+    eo_out(const EOAcc<N, T> &acc, T (&y)[N])
+    {
+#pragma unroll
+      for (int i = 0; i < N / 2; ++i)
+        {
+          y[i]         = acc.se[i] + acc.so[i];
+          y[N - 1 - i] = acc.se[i] - acc.so[i];
+        }
+      if (N & 1)
+        y[N / 2] = acc.sm;
+    }
+
     template <int N, typename T, bool CON>
     __global__ void __launch_bounds__(blk_cells<N, T>() * N * N)
-    heat_tp_block_kernel(const __grid_constant__ HeatTP<N, T> m, const __grid_constant__ CellGeom<T> g,
+    heat_tp_block_kernel(const __grid_constant__ HeatTPEO<N, T> m, const __grid_constant__ CellGeom<T> g,
                          const T *__restrict__ src, T *__restrict__ dst)
     {
       constexpr int N2 = N * N, N3 = N * N * N, P = N - 1;
@@ -356,11 +453,18 @@ namespace mfgpu
 #pragma unroll
         for (int k = 0; k < N; ++k)
           x[k] = (act && !con(k)) ? __ldg(src + colb + Nxy * k) : T(0);
+        const EOSplit<N, T> xs = eo_split<N, T>(x);
+        EOAcc<N, T>         au, av;
+        eo_acc<N, T, true>(au, m.Mz, xs);
+        eo_acc<N, T, true>(av, m.Kz, xs);
+        T u[N], v[N];
+        eo_out<N, T>(au, u);
+        eo_out<N, T>(av, v);
 #pragma unroll
         for (int i = 0; i < N; ++i)
           {
-            U[i * N2 + i1 * N + i0] = dot_row<N, T>(m.Mz, i, x);
-            V[i * N2 + i1 * N + i0] = dot_row<N, T>(m.Kz, i, x);
+            U[i * N2 + i1 * N + i0] = u[i];
+            V[i * N2 + i1 * N + i0] = v[i];
           }
       }
       __syncthreads();
@@ -373,15 +477,18 @@ namespace mfgpu
             u[j] = U[i1 * N2 + j * N + i0];
             v[j] = V[i1 * N2 + j * N + i0];
           }
+        const EOSplit<N, T> us = eo_split<N, T>(u), vs = eo_split<N, T>(v);
+        EOAcc<N, T>         au, av;
+        eo_acc<N, T, true>(au, m.My, us);
+        eo_acc<N, T, true>(av, m.Ky, us);
+        eo_acc<N, T, false>(av, m.My, vs);
+        eo_out<N, T>(au, u);
+        eo_out<N, T>(av, v);
 #pragma unroll
         for (int i = 0; i < N; ++i)
           {
-            T s = dot_row<N, T>(m.Ky, i, u);
-#pragma unroll
-            for (int j = 0; j < N; ++j)
-              s = fma(m.My[i][j], v[j], s);
-            U[i1 * N2 + i * N + i0] = dot_row<N, T>(m.My, i, u);
-            V[i1 * N2 + i * N + i0] = s;
+            U[i1 * N2 + i * N + i0] = u[i];
+            V[i1 * N2 + i * N + i0] = v[i];
           }
       }
       __syncthreads();
@@ -394,15 +501,14 @@ namespace mfgpu
             u[j] = U[i1 * N2 + i0 * N + j];
             v[j] = V[i1 * N2 + i0 * N + j];
           }
+        const EOSplit<N, T> us = eo_split<N, T>(u), vs = eo_split<N, T>(v);
+        EOAcc<N, T>         ay;
+        eo_acc<N, T, true>(ay, m.Ax, us);
+        eo_acc<N, T, false>(ay, m.Mx, vs);
+        eo_out<N, T>(ay, u);
 #pragma unroll
         for (int i = 0; i < N; ++i)
-          {
-            T s = dot_row<N, T>(m.Ax, i, u);
-#pragma unroll
-            for (int j = 0; j < N; ++j)
-              s = fma(m.Mx[i][j], v[j], s);
-            U[i1 * N2 + i0 * N + i] = s;
-          }
+          U[i1 * N2 + i0 * N + i] = u[i];
       }
       __syncthreads();
       if (!act)
@@ -425,12 +531,43 @@ namespace mfgpu
     }
 
     template <int N, typename T>
+    EOMat<N, T>
+    eo_mat(const T (&M)[N][N])
+    {
+      constexpr int H = N / 2;
+      EOMat<N, T>   r{};
+      for (int i = 0; i < H; ++i)
+        for (int j = 0; j < H; ++j)
+          {
+            r.E[i][j] = T((double(M[i][j]) + double(M[i][N - 1 - j])) / 2);
+            r.O[i][j] = T((double(M[i][j]) - double(M[i][N - 1 - j])) / 2);
+          }
+      if (N & 1)
+        {
+          for (int i = 0; i < H; ++i)
+            {
+              r.C[i] = M[i][H];
+              r.R[i] = M[H][i];
+            }
+          r.C[H] = M[H][H];
+        }
+      return r;
+    }
+
+    template <int N, typename T>
     cudaError_t
     launch_block(const HostBasis &b, const LevelGeom &g, const HeatTPArgs &a, cudaStream_t s)
     {
       constexpr int     CPB  = blk_cells<N, T>();
       const size_t      smem = size_t(CPB) * 2 * N * N * N * sizeof(T);
-      const HeatTP<N, T> h   = make_matrices<N, T>(b, g, a.kdt);
+      const HeatTP<N, T> h0  = make_matrices<N, T>(b, g, a.kdt);
+      HeatTPEO<N, T>    h;
+      h.Mx = eo_mat<N, T>(h0.Mx);
+      h.Ax = eo_mat<N, T>(h0.Ax);
+      h.My = eo_mat<N, T>(h0.My);
+      h.Ky = eo_mat<N, T>(h0.Ky);
+      h.Mz = eo_mat<N, T>(h0.Mz);
+      h.Kz = eo_mat<N, T>(h0.Kz);
       CellGeom<T>        cg  = make_cell_geom<T>(g);
       cg.batch               = unsigned(a.batch > 1 ? a.batch : 1);
       cg.bstride             = a.batch > 1 ? a.bstride : 0;
