@@ -918,8 +918,10 @@ KERNEL_CASES = {
     "heat_fp32_q1": ("heat", 1, 6, 32, "native"),  # unit cube 64^3 cells (tensor-product kernel)
     "heat_fp32_q2": ("heat", 2, 6, 32, "native"),
     "heat_fp32_q3": ("heat", 3, 6, 32, "native"),
+    "heat_fp32_q4": ("heat", 4, 6, 32, "native"),
     "heat_fp32_q6": ("heat", 6, 6, 32, "native"),
     "heat_fp64_q2": ("heat", 2, 6, 64, "native"),
+    "heat_fp64_q4": ("heat", 4, 6, 64, "native"),
     "heat_fp32_q2_sumfact": ("heat", 2, 6, 32, "line"),  # sum factorization through the Gauss points
     "heat_fp64_q2_sumfact": ("heat", 2, 6, 64, "line"),
     "heat_fp32_q2_tensor": ("heat", 2, 6, 32, "tensor"),  # element matrix on the tensor cores

@@ -201,11 +201,12 @@ int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
  * FP32 or native FP64: the element operator as sums of products of the 1D
  * mass and stiffness matrices, exact for the QGauss(p+1) integral on the
  * level's affine cells, 7 sweeps per cell; one thread per cell in
- * registers at degree 1..2, (p+1)^2 threads per cell through shared
- * memory above), 5 the tensor product with the cells' nodes staged in
- * shared memory by TMA row copies and the results added back by TMA bulk
- * reductions (FP32, degree 1..2, 16-byte aligned vectors; measured slower
- * than 4, other cases take 4).  The results agree to round-off. */
+ * registers at degree 1 on levels of 16384 cells or more, (p+1)^2
+ * threads per cell through shared memory otherwise), 5 the tensor product
+ * with the cells' nodes staged in shared memory by TMA row copies and the
+ * results added back by TMA bulk reductions (FP32, degree 1..2, 16-byte
+ * aligned vectors; measured slower than 4, other cases take 4).  The
+ * results agree to round-off. */
 int mfgpu_operator_set_cell_kernel(mfgpu_operator *op, int mode);
 /* compute_diagonal (mf_nh_operator.h:1025-1060, heat_transfer.h:205-230) */
 int mfgpu_operator_compute_diagonal(mfgpu_operator *op);

@@ -1,7 +1,7 @@
 // The heat operator (mass + dt k Laplace, LaplaceOperator::do_operation_on_
 // cell, heat_transfer.h:236-250) on box levels in its tensor-product form:
-// one thread per cell in registers at degrees 1-2, (p+1)^2 threads per cell
-// through shared memory at degrees 3-6.
+// one thread per cell in registers at degree 1 on levels of 16384 cells or
+// more, (p+1)^2 threads per cell through shared memory otherwise.
 //
 // Every cell of a box level is the same affine brick h0 x h1 x h2 and the
 // coefficient is constant (heat_transfer.h:63-71).  The QGauss(p+1) cell
@@ -21,7 +21,7 @@
 // it costs 7 (p+1)^4 multiply-adds per cell, against 12 (p+1)^4 plus the
 // quadrature-point work for evaluate / integrate through the Gauss points.
 //
-// Degrees 1-2 (heat_tp_kernel): thread = a column of `zlen` consecutive cells
+// Registers (heat_tp_kernel): thread = a column of `zlen` consecutive cells
 // along z, threads of a warp consecutive along x.  The (p+1)^3 values of a
 // cell live in registers; all sweeps are register FMAs with the 1D
 // matrices in the kernel's constant bank.  Nodes shared between cells are
@@ -321,8 +321,26 @@ namespace mfgpu
     __host__ __device__ constexpr int
     blk_cells()
     {
-      return N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 3 : 2;
+      return N == 2 ? 32 : N == 3 ? 14 : N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 3 : 2;
     }
+
+    // shared layout of a cell: node (a, b, k) at a + N b + SZ k of U, V at
+    // U + N SZ, cells CS apart.  For 4-byte values the plane and cell
+    // padding minimise the shared-memory wavefronts of the four access
+    // patterns (z-column writes, y-lines, x-lines, z-column reads) over the
+    // warps of a block, by exhaustive search over plane padding 0..8 and
+    // cell padding 0..32 with a bank model (wavefronts per warp access,
+    // whole kernel): N = 2 320 -> 104, 3 285 -> 204, 4 544 -> 224,
+    // 5 385 -> 340, 6 534 -> 366, 7 462 -> 427.
+    template <int N, typename T>
+    struct BlkLay
+    {
+      static constexpr int PZ = sizeof(T) == 4 ? (N == 2 ? 2 : N == 3 ? 0 : N == 4 ? 3 : N == 5 ? 0 : 3) : 0;
+      static constexpr int PC =
+        sizeof(T) == 4 ? (N == 2 ? 4 : N == 3 ? 5 : N == 4 ? 24 : N == 5 ? 3 : N == 6 ? 16 : 25) : 0;
+      static constexpr int SZ = N * N + PZ;
+      static constexpr int CS = 2 * N * SZ + PC;
+    };
 
     // Even-odd form of a symmetric matrix with M[N-1-i][N-1-j] = M[i][j]
     // (the 1D mass and stiffness matrices: Gauss-Lobatto nodes and Gauss
@@ -425,7 +443,7 @@ namespace mfgpu
     heat_tp_block_kernel(const __grid_constant__ HeatTPEO<N, T> m, const __grid_constant__ CellGeom<T> g,
                          const T *__restrict__ src, T *__restrict__ dst)
     {
-      constexpr int N2 = N * N, N3 = N * N * N, P = N - 1;
+      constexpr int N2 = N * N, P = N - 1;
       constexpr int CPB = blk_cells<N, T>();
       extern __shared__ __align__(16) unsigned char smraw[];
       src += size_t(blockIdx.y) * g.bstride;
@@ -439,14 +457,19 @@ namespace mfgpu
       const int      cx   = int(cc % unsigned(g.C[0]));
       const int      cyz  = int(cc / unsigned(g.C[0]));
       const int      cy   = cyz % g.C[1], cz = cyz / g.C[1];
-      T *U = reinterpret_cast<T *>(smraw) + size_t(lc) * 2 * N3; // [k][b][a]
-      T *V = U + N3;
+      using L = BlkLay<N, T>;
+      constexpr int SZ = L::SZ;
+      T *U = reinterpret_cast<T *>(smraw) + size_t(lc) * L::CS; // (a, b, k) at a + N b + SZ k
+      T *V = U + N * SZ;
       const size_t Nx = size_t(g.Nn[0]), Nxy = size_t(g.Nn[0]) * size_t(g.Nn[1]);
       const int    ix = cx * P + i0, iy = cy * P + i1;
       const size_t colb = size_t(ix) + Nx * size_t(iy) + Nxy * size_t(cz * P);
-      auto con = [&](int k) {
-        return CON && ((node_mask(g.face_mask, g.Nn, ix, iy, cz * P + k) & 1u) != 0u);
-      };
+      // Dirichlet faces of the z-column (a, b) = (i0, i1), component 0
+      const bool cxy = CON && (((ix == 0) && (g.face_mask[0] & 1u)) || ((ix == g.Nn[0] - 1) && (g.face_mask[1] & 1u)) ||
+                               ((iy == 0) && (g.face_mask[2] & 1u)) || ((iy == g.Nn[1] - 1) && (g.face_mask[3] & 1u)));
+      const bool cz0 = CON && cz == 0 && (g.face_mask[4] & 1u);
+      const bool cz1 = CON && cz == g.C[2] - 1 && (g.face_mask[5] & 1u);
+      auto       con = [&](int k) { return cxy || (k == 0 && cz0) || (k == P && cz1); };
       // gather the z-column (a, b) = (i0, i1) and apply the z-matrices
       {
         T x[N];
@@ -463,8 +486,8 @@ namespace mfgpu
 #pragma unroll
         for (int i = 0; i < N; ++i)
           {
-            U[i * N2 + i1 * N + i0] = u[i];
-            V[i * N2 + i1 * N + i0] = v[i];
+            U[i * SZ + i1 * N + i0] = u[i];
+            V[i * SZ + i1 * N + i0] = v[i];
           }
       }
       __syncthreads();
@@ -474,8 +497,8 @@ namespace mfgpu
 #pragma unroll
         for (int j = 0; j < N; ++j)
           {
-            u[j] = U[i1 * N2 + j * N + i0];
-            v[j] = V[i1 * N2 + j * N + i0];
+            u[j] = U[i1 * SZ + j * N + i0];
+            v[j] = V[i1 * SZ + j * N + i0];
           }
         const EOSplit<N, T> us = eo_split<N, T>(u), vs = eo_split<N, T>(v);
         EOAcc<N, T>         au, av;
@@ -487,8 +510,8 @@ namespace mfgpu
 #pragma unroll
         for (int i = 0; i < N; ++i)
           {
-            U[i1 * N2 + i * N + i0] = u[i];
-            V[i1 * N2 + i * N + i0] = v[i];
+            U[i1 * SZ + i * N + i0] = u[i];
+            V[i1 * SZ + i * N + i0] = v[i];
           }
       }
       __syncthreads();
@@ -498,8 +521,8 @@ namespace mfgpu
 #pragma unroll
         for (int j = 0; j < N; ++j)
           {
-            u[j] = U[i1 * N2 + i0 * N + j];
-            v[j] = V[i1 * N2 + i0 * N + j];
+            u[j] = U[i1 * SZ + i0 * N + j];
+            v[j] = V[i1 * SZ + i0 * N + j];
           }
         const EOSplit<N, T> us = eo_split<N, T>(u), vs = eo_split<N, T>(v);
         EOAcc<N, T>         ay;
@@ -508,7 +531,7 @@ namespace mfgpu
         eo_out<N, T>(ay, u);
 #pragma unroll
         for (int i = 0; i < N; ++i)
-          U[i1 * N2 + i0 * N + i] = u[i];
+          U[i1 * SZ + i0 * N + i] = u[i];
       }
       __syncthreads();
       if (!act)
@@ -526,7 +549,7 @@ namespace mfgpu
                 *d += __ldg(src + colb + Nxy * k);
             }
           else
-            atomicAdd(d, U[k * N2 + i1 * N + i0]);
+            atomicAdd(d, U[k * SZ + i1 * N + i0]);
         }
     }
 
@@ -559,7 +582,7 @@ namespace mfgpu
     launch_block(const HostBasis &b, const LevelGeom &g, const HeatTPArgs &a, cudaStream_t s)
     {
       constexpr int     CPB  = blk_cells<N, T>();
-      const size_t      smem = size_t(CPB) * 2 * N * N * N * sizeof(T);
+      const size_t      smem = size_t(CPB) * BlkLay<N, T>::CS * sizeof(T);
       const HeatTP<N, T> h0  = make_matrices<N, T>(b, g, a.kdt);
       HeatTPEO<N, T>    h;
       h.Mx = eo_mat<N, T>(h0.Mx);
@@ -1088,14 +1111,18 @@ namespace mfgpu
         if (ok)
           return e;
       }
-    // one thread per cell in registers at Q1-Q2, the block kernel above
-    // (measured on 64^3 cells: FP32 Q2 31 us in registers, 72 us in blocks;
-    // FP32 Q3 80 against 73 us, FP64 Q2 314 against 510 us)
+    // one thread per cell in registers at Q1 from 16384 cells on, the block
+    // kernel above otherwise (measured with the padded block layout, CUDA
+    // events, L2 flushed: 64^3 cells Q2 FP32 30.9 us in registers, 29.3 us
+    // in blocks, FP64 314 against 246 us; Q1 FP64 70.3 against 70.0 us;
+    // 16^3 cells FP64 Q2 32 us in registers, 12 us in blocks)
+    const size_t cells = size_t(a.zc1 - a.zc0) * size_t(g.C[0]) * size_t(g.C[1]);
+    const bool   regs  = cells >= 16384;
     if (precision == 32)
       switch (b.N)
         {
-          case 2: return tp::launch<2, float>(b, g, a, s);
-          case 3: return tp::launch<3, float>(b, g, a, s);
+          case 2: return regs ? tp::launch<2, float>(b, g, a, s) : tp::launch_block<2, float>(b, g, a, s);
+          case 3: return tp::launch_block<3, float>(b, g, a, s);
           case 4: return tp::launch_block<4, float>(b, g, a, s);
           case 5: return tp::launch_block<5, float>(b, g, a, s);
           case 6: return tp::launch_block<6, float>(b, g, a, s);
@@ -1104,8 +1131,8 @@ namespace mfgpu
     else
       switch (b.N)
         {
-          case 2: return tp::launch<2, double>(b, g, a, s);
-          case 3: return tp::launch<3, double>(b, g, a, s);
+          case 2: return regs ? tp::launch<2, double>(b, g, a, s) : tp::launch_block<2, double>(b, g, a, s);
+          case 3: return tp::launch_block<3, double>(b, g, a, s);
           case 4: return tp::launch_block<4, double>(b, g, a, s);
           case 5: return tp::launch_block<5, double>(b, g, a, s);
           case 6: return tp::launch_block<6, double>(b, g, a, s);

@@ -68,8 +68,9 @@ namespace mfgpu
 
   // the heat operator in its tensor-product form (1D mass and stiffness
   // matrices, 7 sweeps per cell; mf_heat_tp.cu), N = 2..7, FP32 and FP64:
-  // one thread per column segment of zlen cells in registers (N = 2..3),
-  // N^2 threads per cell through shared memory (N = 4..7), or, on request,
+  // one thread per column segment of zlen cells in registers (N = 2 from
+  // 16384 cells on), N^2 threads per cell through shared memory (otherwise),
+  // or, on request,
   // for FP32 N = 2..3 over all cells bricks staged in shared memory by TMA;
   // three-dimensional levels; dst += A src over the cells of z-planes
   // [zc0, zc1), grid.y = problem of a batch

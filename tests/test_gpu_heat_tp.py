@@ -3,8 +3,8 @@ operator as sums of products of the 1D mass and stiffness matrices, one
 thread per cell column segment in registers) against the oracle's vmult
 (heat_transfer.h:236-250) and against the sum-factorization kernel.
 
-Degrees 1-6: one thread per cell in registers up to FP32 Q3 and FP64 Q2,
-the shared-memory block form above.  Tolerances: FP64 1e-12 relative l2
+Degrees 1-6: one thread per cell in registers at Q1 on levels of 16384
+cells or more, the shared-memory block form otherwise.  Tolerances: FP64 1e-12 relative l2
 (the operator parity bar), FP32 5e-5 as the other FP32 operator tests.  The meshes exercise what the kernel's
 work split depends on: rows of cells shorter and longer than a warp (the
 x-neighbour exchange by shuffles across warp ends), column segments that do
@@ -48,10 +48,11 @@ MESHES = {
     # 6 x 4 x 10 cells: rows shorter than a warp, anisotropic cells, two
     # clamped faces
     "short_rows": ((3, 2, 5), 1, (1.5, 0.7, 2.0), (1, 0, 2, 0, 0, 2), [(1, 1), (2, 1)]),
-    # 40 x 3 x 7 cells: rows across warp ends, every face clamped
-    "long_rows": ((40, 3, 7), 0, (4.0, 0.3, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)]),
-    # 33 x 2 x 9 cells, no constraint
-    "free": ((33, 2, 9), 0, (1.0, 0.2, 0.9), (0, 0, 0, 0, 0, 0), []),
+    # 40 x 30 x 14 cells (16,800: the register kernel at Q1-Q2): rows
+    # across warp ends, every face clamped
+    "long_rows": ((40, 30, 14), 0, (4.0, 3.0, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)]),
+    # 33 x 25 x 20 cells (16,500), no constraint
+    "free": ((33, 25, 20), 0, (1.0, 0.8, 0.9), (0, 0, 0, 0, 0, 0), []),
     # 64 x 64 x 39 cells: column segments of 4 cells (enough columns for the
     # launch heuristic), the last one of 3
     "segments": ((64, 64, 39), 0, (1.0, 1.0, 0.6), (1, 0, 2, 0, 0, 2), [(1, 1), (2, 1)]),
@@ -63,8 +64,7 @@ MESHES = {
 def test_tensor_product_heat_vmult(ctx, precision, mesh):
     rep, nref, hi, bid, dirichlet = MESHES[mesh]
     # the 64 x 64 x 39 mesh tests the column segments of the register
-    # kernel (degrees 1-2); the others every degree (registers up to FP32
-    # Q3 and FP64 Q2, the block kernel above)
+    # kernel (degrees 1-2); the others every degree
     for degree in DEGREES if mesh != "segments" else [1, 2]:
         spec = _spec(degree, rep, nref, hi, bid, dirichlet)
         m = W.to_lib_mesh(mfgpu, spec)
@@ -95,8 +95,9 @@ def test_tensor_product_heat_vmult(ctx, precision, mesh):
 
 @pytest.mark.parametrize("precision", [32, 64])
 def test_tensor_product_heat_default_and_host_buffers(ctx, precision):
-    """A 16^3-cell Q2 level takes kernel 4 by default (4096 cells); the
-    overlapped host-buffer vmult (z-slabs of cells) gives the same result."""
+    """A 16^3-cell Q2 level takes kernel 4 by default (4096 cells, the block
+    form); the overlapped host-buffer vmult (z-slabs of cells) gives the same
+    result."""
     spec = W.unit_cube_heat(2, 4)
     m = W.to_lib_mesh(mfgpu, spec)
     n = W.n_dofs(spec, 1)
@@ -136,7 +137,7 @@ def test_tensor_product_heat_unaligned_vectors(ctx):
     """Vectors that do not start on 16 bytes (views at an offset of one
     float) cannot be staged by TMA: the register kernel serves them."""
     import torch
-    spec = _spec(2, (40, 3, 7), 0, (4.0, 0.3, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)])
+    spec = _spec(2, (40, 30, 14), 0, (4.0, 3.0, 0.7), (1, 1, 1, 1, 1, 1), [(1, 1)])
     n = W.n_dofs(spec, 1)
     src = W.uniform_vector(n, 21, np.float32)
     ref = O.heat_vmult(W.to_oracle_mesh(O, spec), 0, 0.1, src.astype(np.float64))
