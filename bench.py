@@ -838,6 +838,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
     for i in ids:
         srv.wait(i)
     one = 100 / (time.perf_counter() - t0)
+    one_batched = srv.batch_stats()[0]
     srv.close()
     srv = mfgpu.Server(0, workers, 0.8)
     t0 = time.perf_counter()
@@ -845,6 +846,7 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
     for i in ids:
         srv.wait(i)
     many = 100 / (time.perf_counter() - t0)
+    many_batched = srv.batch_stats()[0]
     srv.close()
     # baseline: one at a time, plain FP64 solver
     base_reqs = W.serving_requests(mfgpu, n_requests, seed=seed, mg_precision=64)
@@ -864,7 +866,9 @@ def extra_serving(mfgpu, W, n_requests=300, workers=4, load=0.8, seed=7):
                          "rule": "queued heat requests of the same shape and step count join the one a worker "
                                  "takes (one operator, V-cycle and CG for all), up to 4"},
             "errors": errors,
-            "closed_loop_first100_per_s": {"1_worker": one, f"{workers}_workers": many},
+            "closed_loop_first100_per_s": {"1_worker": one, f"{workers}_workers": many,
+                                           "requests_in_batches": {"1_worker": one_batched,
+                                                                   f"{workers}_workers": many_batched}},
             "baseline_fp64_one_at_a_time": {"solves_per_s": n_requests / bspan,
                                             "service_p50_s": float(np.percentile(brun, 50)),
                                             "service_p99_s": float(np.percentile(brun, 99)),
@@ -923,6 +927,7 @@ KERNEL_CASES = {
     "heat_fp64_q2": ("heat", 2, 6, 64, "native"),
     "heat_fp64_q4": ("heat", 4, 6, 64, "native"),
     "heat_fp32_q2_sumfact": ("heat", 2, 6, 32, "line"),  # sum factorization through the Gauss points
+    "heat_fp32_q6_sumfact": ("heat", 6, 6, 32, "line"),
     "heat_fp64_q2_sumfact": ("heat", 2, 6, 64, "line"),
     "heat_fp32_q2_tensor": ("heat", 2, 6, 32, "tensor"),  # element matrix on the tensor cores
     "heat_fp32_q3_tensor": ("heat", 3, 6, 32, "tensor"),
