@@ -130,7 +130,7 @@ def n_dofs(spec, n_components):
 
 
 def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degrees=(1, 2, 3, 4),
-                     mg_precision=32, tol=1e-8):
+                     mg_precision=32, tol=1e-8, fp64_emulation=None):
     """The serving mix: 60 % heat / 40 % neo-Hookean requests.  Heat: unit
     cube with 8^3..(2^max_heat_ref)^3 cells (uniform random refinement 3..),
     zero Dirichlet on x = 0, a seeded Gaussian source, one backward-Euler
@@ -138,8 +138,10 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
     a seeded traction of magnitude U(50, 150) on x = 8, one Newton-Newmark
     step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG with
     the FP64 operators (fine and coarse level) in double-float arithmetic
-    (mg_precision=32), or the plain FP64 solver (mg_precision=64)."""
+    (mg_precision=32; fp64_emulation=False keeps them in native FP64), or the
+    plain FP64 solver (mg_precision=64)."""
     rng = np.random.Generator(np.random.PCG64(seed))
+    emul = (mg_precision == 32) if fp64_emulation is None else bool(fp64_emulation)
     reqs = []
     for i in range(n):
         r = mfgpu.Request()
@@ -154,7 +156,7 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
             hp.solver = mfgpu.solver_params("gmg", tol=tol, cheb_range=15.0, cheb_eig_its=10,
                                             mg_precision=mg_precision,
                                             coarse_fp64=(mg_precision == 32),
-                                            fp64_emulation=(mg_precision == 32))
+                                            fp64_emulation=emul)
             c, w, a = gaussian_source(int(rng.integers(1 << 30)))
             hp.n_gauss = 8
             for j in range(8):
@@ -173,7 +175,7 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
             sp.caching = b"referential_qp"
             sp.solver = mfgpu.solver_params("gmg", tol=tol, mg_precision=mg_precision,
                                             coarse_fp64=(mg_precision == 32),
-                                            fp64_emulation=(mg_precision == 32))
+                                            fp64_emulation=emul)
             sp.max_newton = 10
             sp.tol_f, sp.tol_f_abs, sp.tol_u, sp.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
             sp.dt, sp.n_steps = 0.01, 1

@@ -25,9 +25,12 @@ def run_all(reqs, workers, max_batch=None):
     return res, max_running
 
 
-def test_results_alone_equal_results_in_the_mix(ctx):
+@pytest.mark.parametrize("emulation", [True, False], ids=["df64_operators", "native_fp64_operators"])
+def test_results_alone_equal_results_in_the_mix(ctx, emulation):
+    """The FP64 operators of the mixed-precision solver in double-float (the
+    serving default) and in native FP64."""
     reqs = W.serving_requests(mfgpu, 12, seed=3, max_heat_ref=4, solid_k=(2, 4),
-                              degrees=(1, 2, 3))
+                              degrees=(1, 2, 3), fp64_emulation=emulation)
     alone, mr1 = run_all(reqs, 1, max_batch=1)
     mix, mr4 = run_all(reqs, 4)
     assert mr1 == 1
