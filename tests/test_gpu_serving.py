@@ -112,11 +112,13 @@ def _heat_request(degree, n_ref, seed, n_steps=1):
     return r
 
 
-@pytest.mark.parametrize("degree,n_ref", [(2, 3), (3, 4)])
+@pytest.mark.parametrize("degree,n_ref", [(2, 3), (3, 4), (1, 5)])
 def test_batched_heat_requests_equal_their_solo_solves(ctx, degree, n_ref):
     """Continuous batching: heat requests of one shape queued behind a busy
     worker are solved together (one operator, V-cycle and CG over all of
-    them); each result equals the request solved alone."""
+    them); each result equals the request solved alone.  The 32^3-cell Q1
+    case runs its finest FP32 level through the register form of the
+    tensor-product heat kernel, the others through the block form."""
     heat = [_heat_request(degree, n_ref, seed) for seed in (31, 32, 33, 34)]
     # a solid request keeps the single worker busy while the heat requests queue
     blocker = next(r for r in W.serving_requests(mfgpu, 30, seed=5, max_heat_ref=3, solid_k=(8,), degrees=(3,))
