@@ -136,12 +136,12 @@ def serving_requests(mfgpu, n, seed=7, max_heat_ref=6, solid_k=(2, 4, 8), degree
     zero Dirichlet on x = 0, a seeded Gaussian source, one backward-Euler
     step.  Solid: cantilever 8k x k x k cells, k in solid_k, clamped at x = 0,
     a seeded traction of magnitude U(50, 150) on x = 8, one Newton-Newmark
-    step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG with
-    the FP64 operators (fine and coarse level) in double-float arithmetic
-    (mg_precision=32; fp64_emulation=False keeps them in native FP64), or the
+    step.  Degree uniform in `degrees`.  FP32-GMG preconditioned FP64 CG
+    with the FP64 operators (fine and coarse level) in native FP64
+    (mg_precision=32; fp64_emulation=True runs them in double-float), or the
     plain FP64 solver (mg_precision=64)."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    emul = (mg_precision == 32) if fp64_emulation is None else bool(fp64_emulation)
+    emul = bool(fp64_emulation) and mg_precision == 32
     reqs = []
     for i in range(n):
         r = mfgpu.Request()

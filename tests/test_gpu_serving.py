@@ -27,8 +27,8 @@ def run_all(reqs, workers, max_batch=None):
 
 @pytest.mark.parametrize("emulation", [True, False], ids=["df64_operators", "native_fp64_operators"])
 def test_results_alone_equal_results_in_the_mix(ctx, emulation):
-    """The FP64 operators of the mixed-precision solver in double-float (the
-    serving default) and in native FP64."""
+    """The FP64 operators of the mixed-precision solver in native FP64 (the
+    serving default) and in double-float."""
     reqs = W.serving_requests(mfgpu, 12, seed=3, max_heat_ref=4, solid_k=(2, 4),
                               degrees=(1, 2, 3), fp64_emulation=emulation)
     alone, mr1 = run_all(reqs, 1, max_batch=1)
@@ -101,7 +101,7 @@ def _heat_request(degree, n_ref, seed, n_steps=1):
     hp.mesh = W.to_lib_mesh(mfgpu, W.unit_cube_heat(degree, n_ref))
     hp.dt, hp.n_steps = 0.1, n_steps
     hp.solver = mfgpu.solver_params("gmg", tol=1e-8, cheb_range=15.0, cheb_eig_its=10, mg_precision=32,
-                                    coarse_fp64=True, fp64_emulation=True)
+                                    coarse_fp64=True)
     c, w, a = W.gaussian_source(seed)
     hp.n_gauss = 8
     for j in range(8):
