@@ -931,6 +931,7 @@ KERNEL_CASES = {
     # name: (operator, degree, refinements, precision, arithmetic)
     "nh_fp64_q4": ("nh", 4, 3, 64, "native"),   # the headline: 64x8x8 cells, 839,619 DoFs
     "nh_df64_q4": ("nh", 4, 3, 64, "df64"),
+    "nh_fp64_q4_line": ("nh", 4, 3, 64, "line"),  # the line-parallel kernel on the headline case
     "nh_fp32_q3": ("nh", 3, 4, 32, "native"),   # finest level of the mixed solve, 2,773,155 DoFs
     "nh_fp32_q3_scalar_ref": ("nh_sr", 3, 4, 32, "native"),
     "heat_fp32_q1": ("heat", 1, 6, 32, "native"),  # unit cube 64^3 cells (tensor-product kernel)
@@ -971,6 +972,8 @@ def run_kernel_case(args):
         op.initialize(u)
         if arith == "df64":
             op.set_fp64_emulation(True)
+        if arith == "line":
+            op.set_cell_kernel("line")
         op.cache()
     else:
         spec = W.unit_cube_heat(deg, nref)
