@@ -192,7 +192,8 @@ int mfgpu_operator_set_host_chunks(mfgpu_operator *op, int n_chunks);
 int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
 /* cell kernel of vmult: 0 by grid size (default: point-parallel, one
  * thread per quadrature point, below 1024 cells, up to 4096 in native
- * FP64; line-parallel above; three-dimensional heat operators in FP32 and
+ * FP64, at every size for the native FP64 referential_qp tangent except
+ * degree 2; line-parallel above; three-dimensional heat operators in FP32 and
  * native FP64 take kernel 4 from 512 cells on), 1 line-parallel,
  * 2 point-parallel, 3 tensor cores (three-dimensional FP32 heat
  * operators, degree 1..5: the cells' common element matrix applied to

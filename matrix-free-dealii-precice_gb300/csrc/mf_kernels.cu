@@ -52,9 +52,15 @@ namespace mfgpu
           return cudaErrorInvalidValue;
         }
       const unsigned n_cells = cg.cell_end - cg.cell_begin;
-      // native FP64 keeps the point-parallel kernel up to 4096 cells (Q4:
-      // 253 against 285 us there, even at 32768)
-      const unsigned point_below = std::is_same<T, double>::value ? 4097u : POINT_CELLS;
+      // native FP64 keeps the point-parallel kernel up to 4096 cells, and the
+      // referential_qp tangent at every size but Q2 (measured, CUDA events,
+      // L2 flushed: 4096 cells Q3 122 against 154 us, Q4 257 / 289, Q5
+      // 498 / 580; 32768 cells Q3 881 / 951, Q4 1995 / 2004, Q6 863 / 873;
+      // Q2 at 32768 cells 384 / 345, where the line kernel's even-odd sweeps
+      // win)
+      const unsigned point_below = !std::is_same<T, double>::value ? POINT_CELLS :
+                                   (Op::prefetch && N != 3)        ? 0xffffffffu :
+                                                                     4097u;
       if (cg.color < 0 && n_cells > 0 && (kernel == 2 || (kernel == 0 && n_cells < point_below)))
         {
           // few cells: one block per cell, one thread per point

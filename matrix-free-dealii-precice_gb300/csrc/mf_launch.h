@@ -98,7 +98,8 @@ namespace mfgpu
   constexpr unsigned TP_MIN_CELLS = 512;
 
   // launches of fewer cells than this take the point-parallel kernel
-  // (native FP64: up to 4096 cells)
+  // (native FP64: up to 4096 cells; the native FP64 referential_qp tangent
+  // at every size but Q2)
   constexpr unsigned POINT_CELLS = 1024;
 
   template <int N, typename T>
