@@ -143,3 +143,95 @@ def test_batched_heat_requests_equal_their_solo_solves(ctx, degree, n_ref):
     # the problems differ: the batch did not hand one result to all
     norms = [b.solution_norm for b in batched]
     assert len(set(norms)) == len(norms)
+
+
+def _oracle_heat(spec, seed, tol):
+    import oracle as O
+    po = O.HeatParams()
+    po.mesh = W.to_oracle_mesh(O, spec)
+    po.dt, po.n_steps, po.tol_rel, po.precond = 0.1, 1, tol, 2
+    po.mg_float = 0
+    c, w, a = W.gaussian_source(seed)
+    po.n_gauss = 8
+    for j in range(8):
+        for d in range(3):
+            po.g_center[j][d] = c[j, d]
+        po.g_width[j] = w[j]
+        po.g_amp[j] = a[j]
+    return O.heat_run(po, return_u=True)
+
+
+def _oracle_solid(spec, traction, tol):
+    import oracle as O
+    po = O.SolidParams()
+    po.mesh = W.to_oracle_mesh(O, spec)
+    po.mat = O.material(0.5e6, 0.4, 1000.0, 0.01, 1)
+    po.caching = O.CACHING["scalar_referential"]
+    po.precond, po.relaxation, po.tol_lin, po.max_it_mult, po.max_newton = 2, 0.65, tol, 1, 10
+    po.tol_f, po.tol_f_abs, po.tol_u, po.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+    po.dt, po.n_steps = 0.01, 1
+    po.body_force[:] = [0.0, 0.0, 0.0]
+    po.traction_id = W.TRACTION_ID
+    po.traction[:] = list(traction)
+    po.watch[:] = [8.0, 0.5, 0.5]
+    po.cheb_degree, po.cheb_range, po.cheb_eig_its, po.coarse_accurate = 5, 20.0, 30, 1
+    po.mg_float = 0
+    return O.solid_run(po)
+
+
+def test_served_results_match_the_oracle(ctx):
+    """Requests served concurrently against the oracle's FP64 solves of the
+    same problems: heat steps (solution norm within 1e-7 relative, CG within
+    +-1) and Newton-Newmark steps (Newton iterations equal, watchpoint within
+    1e-6 relative), FP32-GMG preconditioned FP64 CG to 1e-8 on the server,
+    all-FP64 GMG-CG in the oracle (heat_transfer.h:715-754,
+    mf_elasticity.h:1402-1491)."""
+    import oracle as O
+    tol = 1e-8
+    heat = [(W.unit_cube_heat(1, 4), 41), (W.unit_cube_heat(2, 3), 42)]
+    solid = [(W.cantilever(1, 1), (0.0, -80.0, 0.0)), (W.cantilever(2, 1), (0.0, -120.0, 0.0))]
+    reqs = []
+    for spec, seed in heat:
+        r = mfgpu.Request()
+        r.kind = 0
+        hp = r.heat
+        hp.mesh = W.to_lib_mesh(mfgpu, spec)
+        hp.dt, hp.n_steps = 0.1, 1
+        hp.solver = mfgpu.solver_params("gmg", tol=tol, cheb_range=15.0, cheb_eig_its=10, mg_precision=32,
+                                        coarse_fp64=True)
+        c, w, a = W.gaussian_source(seed)
+        hp.n_gauss = 8
+        for j in range(8):
+            for d in range(3):
+                hp.g_center[j][d] = c[j, d]
+            hp.g_width[j] = w[j]
+            hp.g_amp[j] = a[j]
+        reqs.append(r)
+    for spec, traction in solid:
+        r = mfgpu.Request()
+        r.kind = 1
+        sp = r.solid
+        sp.mesh = W.to_lib_mesh(mfgpu, spec)
+        sp.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+        sp.caching = b"referential_qp"
+        sp.solver = mfgpu.solver_params("gmg", tol=tol, mg_precision=32, coarse_fp64=True)
+        sp.max_newton = 10
+        sp.tol_f, sp.tol_f_abs, sp.tol_u, sp.tol_u_abs = 1e-9, 0.0, 1e-6, 0.0
+        sp.dt, sp.n_steps = 0.01, 1
+        sp.traction_id = W.TRACTION_ID
+        sp.traction[:] = list(traction)
+        sp.watch[:] = [8.0, 0.5, 0.5]
+        reqs.append(r)
+    res, max_running = run_all(reqs, 4)
+    assert max_running > 1
+    for (spec, seed), r in zip(heat, res[:2]):
+        assert r.status == 0, r.message
+        ro, uo = _oracle_heat(spec, seed, tol)
+        assert abs(r.solution_norm - np.linalg.norm(uo)) <= 1e-7 * np.linalg.norm(uo)
+        assert abs(r.cg_iterations - ro.cg_its[0]) <= 1, (r.cg_iterations, ro.cg_its[0])
+    for (spec, traction), r in zip(solid, res[2:]):
+        assert r.status == 0, r.message
+        ro = _oracle_solid(spec, traction, tol)
+        assert r.newton_iterations == ro.newton_its[0]
+        wo = np.array(ro.watch_disp[0][:3])
+        assert np.linalg.norm(np.array(r.watch[:3]) - wo) <= 1e-6 * np.linalg.norm(wo)
