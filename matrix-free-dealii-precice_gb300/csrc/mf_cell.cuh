@@ -921,6 +921,22 @@ namespace mfgpu
     const int      cyz = int(cc / unsigned(g.C[0]));
     const int      cy  = cyz % g.C[1];
     const int      cz  = cyz / g.C[1];
+    // Dirichlet component masks of the z-column (a, b): the x and y faces
+    // once per thread, the z faces per node (node k of the column lies on
+    // z- for k = 0 of the first cell layer, on z+ for k = p of the last)
+    unsigned mxy = 0u, mz0 = 0u, mz1 = 0u;
+    if (CONSTRAINED)
+      {
+        const int ix = cx * g.p + a, iy = cy * g.p + b;
+        mxy = (ix == 0 ? g.face_mask[0] : 0u) | (ix == g.Nn[0] - 1 ? g.face_mask[1] : 0u) |
+              (iy == 0 ? g.face_mask[2] : 0u) | (iy == g.Nn[1] - 1 ? g.face_mask[3] : 0u);
+        mz0 = cz == 0 ? g.face_mask[4] : 0u;
+        mz1 = cz == g.C[2] - 1 ? g.face_mask[5] : 0u;
+      }
+    auto col_mask = [&](int k) { return mxy | (k == 0 ? mz0 : 0u) | (k == N - 1 ? mz1 : 0u); };
+    // node index of the column's node k: colb + k nxy
+    const size_t nxy  = size_t(g.Nn[0]) * size_t(g.Nn[1]);
+    const size_t colb = size_t(cx * g.p + a) + size_t(g.Nn[0]) * size_t(cy * g.p + b) + nxy * size_t(cz * g.p);
 
     // -------- gather + evaluate ------------------------------------------
     // z-column (x=a, y=b) of component c in the storage type; the column of
@@ -932,12 +948,10 @@ namespace mfgpu
           TS val = TS(0);
           if (active)
             {
-              const int ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
-              const size_t node =
-                size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+              const size_t node = colb + size_t(k) * nxy;
               bool skip = false;
               if (CONSTRAINED)
-                skip = (node_mask_g(g, ix, iy, iz) >> c) & 1u;
+                skip = (col_mask(k) >> c) & 1u;
               if constexpr (UNIT)
                 val = (!skip && c == jc && a == ja && b == jb && k == jk) ? TS(1) : TS(0);
               else if (!skip)
@@ -1077,12 +1091,10 @@ namespace mfgpu
 #pragma unroll
             for (int k = 0; k < N; ++k)
               {
-                const int    ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
-                const size_t node =
-                  size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
+                const size_t node = colb + size_t(k) * nxy;
                 if constexpr (UNIT)
                   {
-                    if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
+                    if (CONSTRAINED && ((col_mask(k) >> c) & 1u))
                       continue;
                     const size_t gcol = size_t(jc) * g.n_nodes + size_t(cx * g.p + ja) +
                                         size_t(g.Nn[0]) * (size_t(cy * g.p + jb) +
@@ -1091,7 +1103,7 @@ namespace mfgpu
                               to_storage<TS, T>(col[k]));
                     continue;
                   }
-                if (CONSTRAINED && ((node_mask_g(g, ix, iy, iz) >> c) & 1u))
+                if (CONSTRAINED && ((col_mask(k) >> c) & 1u))
                   {
                     // constrained row: dst += src, written by the one cell
                     // that owns the node (local index < p in every
