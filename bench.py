@@ -678,7 +678,8 @@ def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src,
                          arith="native"):
     """Measurements behind the kernel choices on the headline workload (Q4
     cantilever 64x8x8, 839,619 DoFs), L2 flushed before every application:
-    * scatter: atomic adds vs 8 parity colours with plain adds;
+    * scatter: atomic adds vs 8 parity colours with plain adds (the heat
+      operator with the sum-factorization kernel in both modes);
     * quadrature data: each caching variant of the tangent in native FP64
       (streamed bytes vs recomputation), referential_qp also in FP32, and
       both referential cachings on the FP32 Q3 level of the mixed solve;
@@ -696,6 +697,9 @@ def extra_design_choices(torch, mfgpu, W, ctx, dev, stream, flush, mesh, u, src,
     for prec in (64, 32):
         dt = torch.float64 if prec == 64 else torch.float32
         hop = mfgpu.LaplaceOperator(ctx, hm, -1, prec, True, delta_t=0.1)
+        # both scatter modes with the sum-factorization kernel (the
+        # tensor-product kernel, the default, scatters by atomics only)
+        hop.set_cell_kernel("line")
         hs = torch.rand(hn, dtype=dt, device=dev) * 2 - 1
         hd = torch.zeros_like(hs)
         for mode in ("atomic", "colored"):
