@@ -917,10 +917,10 @@ namespace mfgpu
     T             *XU     = GU + 3 * NC * AS; // 1 scratch array if eval_u
 
     const unsigned cc  = active ? cell : 0u;
-    const int      cx  = int(cc % unsigned(g.C[0]));
-    const int      cyz = int(cc / unsigned(g.C[0]));
-    const int      cy  = cyz % g.C[1];
-    const int      cz  = cyz / g.C[1];
+    const unsigned cyz = g.dC0.div(cc);
+    const int      cx  = int(cc - cyz * unsigned(g.C[0]));
+    const int      cz  = int(g.dC1.div(cyz));
+    const int      cy  = int(cyz) - cz * g.C[1];
     // Dirichlet component masks of the z-column (a, b): the x and y faces
     // once per thread, the z faces per node (node k of the column lies on
     // z- for k = 0 of the first cell layer, on z+ for k = p of the last)
@@ -1176,9 +1176,10 @@ namespace mfgpu
     const int      t    = threadIdx.x;
     const int      a    = t % N, b = (t / N) % N, k = t / N2;
     const unsigned cell = g.cell_begin + blockIdx.x;
-    const int      cx   = int(cell % unsigned(g.C[0]));
-    const int      cyz  = int(cell / unsigned(g.C[0]));
-    const int      cy = cyz % g.C[1], cz = cyz / g.C[1];
+    const unsigned cyz  = g.dC0.div(cell);
+    const int      cx   = int(cell - cyz * unsigned(g.C[0]));
+    const int      cz   = int(g.dC1.div(cyz));
+    const int      cy   = int(cyz) - cz * g.C[1];
     const int      ix = cx * g.p + a, iy = cy * g.p + b, iz = cz * g.p + k;
     const size_t   node = size_t(ix) + size_t(g.Nn[0]) * (size_t(iy) + size_t(g.Nn[1]) * size_t(iz));
     const unsigned mask = CONSTRAINED ? node_mask_g(g, ix, iy, iz) : 0u;

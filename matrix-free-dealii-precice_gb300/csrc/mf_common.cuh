@@ -79,6 +79,43 @@ namespace mfgpu
     EO<N, T, -1> Due;
   };
 
+  // unsigned division by a divisor fixed per level (the cells per row and
+  // per layer), for dividends below 2^31: n / d = (umulhi(n, mul) + n) >>
+  // shift with shift = ceil(log2 d), mul = floor(2^32 (2^shift - d) / d) + 1
+  // (the round-up method of Granlund and Montgomery, "Division by invariant
+  // integers using multiplication", 1994).  Replaces the integer division
+  // sequence that a runtime divisor costs in every cell kernel thread.
+  struct FastDiv
+  {
+    unsigned d, mul, shift;
+    __host__ __device__ __forceinline__ unsigned
+    div(unsigned n) const
+    {
+#ifdef __CUDA_ARCH__
+      return (__umulhi(n, mul) + n) >> shift;
+#else
+      return unsigned(((unsigned long long)(n) * mul >> 32) + n) >> shift;
+#endif
+    }
+    __host__ __device__ __forceinline__ unsigned
+    mod(unsigned n) const
+    {
+      return n - div(n) * d;
+    }
+  };
+
+  inline FastDiv
+  make_fastdiv(unsigned d)
+  {
+    FastDiv f;
+    f.d     = d;
+    f.shift = 0;
+    while ((1ull << f.shift) < d)
+      ++f.shift;
+    f.mul = unsigned(((1ull << 32) * ((1ull << f.shift) - d)) / d + 1);
+    return f;
+  }
+
   // geometry of a level as seen by a cell kernel, in precision T
   template <typename T>
   struct CellGeom
@@ -102,6 +139,8 @@ namespace mfgpu
     // problem blockIdx.y reads src and writes dst at offset blockIdx.y * bstride
     unsigned batch;
     size_t   bstride;
+    // C[0] and C[1] as fast divisors: cell -> (x, y, z)
+    FastDiv  dC0, dC1;
   };
 
   // host-side conversion of a double constant to a compute type
@@ -140,6 +179,8 @@ namespace mfgpu
     c.hc[0] = c.hc[1] = c.hc[2] = 0;
     c.n_nodes    = g.n_nodes;
     c.vol     = conv_host<T>(g.h[0] * g.h[1] * g.h[2]);
+    c.dC0     = make_fastdiv(unsigned(g.C[0]));
+    c.dC1     = make_fastdiv(unsigned(g.C[1]));
     for (int f = 0; f < 6; ++f)
       c.face_mask[f] = g.face_mask[f];
     return c;

@@ -162,10 +162,11 @@ namespace mfgpu
       const unsigned t    = blockIdx.x * THREADS + threadIdx.x;
       const bool     active = t < ncol * nseg;
       const unsigned tt     = active ? t : 0u;
-      const int      cx     = int(tt % unsigned(C0));
-      const int      r      = int(tt / unsigned(C0));
-      const int      cy     = r % C1;
-      const int      cz0    = zc0 + (r / C1) * zlen;
+      const unsigned ru     = g.dC0.div(tt);
+      const int      cx     = int(tt - ru * unsigned(C0));
+      const int      seg    = int(g.dC1.div(ru));
+      const int      cy     = int(ru) - seg * C1;
+      const int      cz0    = zc0 + seg * zlen;
       const int      czn    = min(cz0 + zlen, zc1); // one past the column segment's last cell
       // lane+1 holds cell cx+1 of the same row, lane-1 cell cx-1
       const bool rmerge = active && lane < 31 && cx + 1 < C0;
@@ -454,9 +455,10 @@ namespace mfgpu
       const unsigned cell = g.cell_begin + blockIdx.x * CPB + unsigned(lc);
       const bool     act  = cell < g.cell_end;
       const unsigned cc   = act ? cell : g.cell_begin;
-      const int      cx   = int(cc % unsigned(g.C[0]));
-      const int      cyz  = int(cc / unsigned(g.C[0]));
-      const int      cy   = cyz % g.C[1], cz = cyz / g.C[1];
+      const unsigned cyz  = g.dC0.div(cc);
+      const int      cx   = int(cc - cyz * unsigned(g.C[0]));
+      const int      cz   = int(g.dC1.div(cyz));
+      const int      cy   = int(cyz) - cz * g.C[1];
       using L = BlkLay<N, T>;
       constexpr int SZ = L::SZ;
       T *U = reinterpret_cast<T *>(smraw) + size_t(lc) * L::CS; // (a, b, k) at a + N b + SZ k
