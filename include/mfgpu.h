@@ -194,12 +194,14 @@ int mfgpu_operator_set_dense(mfgpu_operator *op, int enable);
  * thread per quadrature point, below 1024 cells, up to 4096 in native
  * FP64, at every size for the native FP64 referential_qp tangent except
  * degree 2; line-parallel above; three-dimensional heat operators in FP32 and
- * native FP64 take kernel 4 from 512 cells on), 1 line-parallel,
+ * native FP64, and in double-float up to degree 5, take kernel 4 from 512
+ * cells on), 1 line-parallel,
  * 2 point-parallel, 3 tensor cores (three-dimensional FP32 heat
  * operators, degree 1..5: the cells' common element matrix applied to
  * batches of 128 cells by tcgen05.mma in TF32 with a three-term split,
  * FP32 accuracy), 4 tensor product (three-dimensional heat operators in
- * FP32 or native FP64: the element operator as sums of products of the 1D
+ * FP32, native FP64 or double-float, the default for double-float up to
+ * degree 5: the element operator as sums of products of the 1D
  * mass and stiffness matrices, exact for the QGauss(p+1) integral on the
  * level's affine cells, 7 sweeps per cell; one thread per cell in
  * registers at degree 1 on levels of 16384 cells or more, (p+1)^2

@@ -339,10 +339,8 @@ extern "C"
       if (mode >= 4)
         {
           Operator *o = op->op.get();
-          if (!dynamic_cast<HeatOperator *>(o) || o->geom.dim != 3 || o->arith != 0 ||
-              !heat_tp_supported(o->basis.N, o->precision))
-            throw Error(ERR_UNSUPPORTED, "the tensor-product cell kernel applies to three-dimensional heat operators "
-                                         "in FP32 or native FP64");
+          if (!dynamic_cast<HeatOperator *>(o) || o->geom.dim != 3 || !heat_tp_supported(o->basis.N, o->precision))
+            throw Error(ERR_UNSUPPORTED, "the tensor-product cell kernel applies to three-dimensional heat operators");
         }
       if (mode == 3)
         {

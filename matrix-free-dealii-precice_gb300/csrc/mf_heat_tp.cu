@@ -1,7 +1,8 @@
 // The heat operator (mass + dt k Laplace, LaplaceOperator::do_operation_on_
 // cell, heat_transfer.h:236-250) on box levels in its tensor-product form:
 // one thread per cell in registers at degree 1 on levels of 16384 cells or
-// more, (p+1)^2 threads per cell through shared memory otherwise.
+// more, (p+1)^2 threads per cell through shared memory otherwise; the
+// shared-memory form also in double-float arithmetic on FP64 vectors.
 //
 // Every cell of a box level is the same affine brick h0 x h1 x h2 and the
 // coefficient is constant (heat_transfer.h:63-71).  The QGauss(p+1) cell
@@ -75,6 +76,35 @@ namespace mfgpu
       for (int j = 1; j < N; ++j)
         s = fma(M[i][j], v[j], s);
       return s;
+    }
+
+    // multiply-add and zero in the compute type (FP32, FP64 or double-float)
+    __device__ __forceinline__ float
+    tp_fma(float a, float b, float c)
+    {
+      return fmaf(a, b, c);
+    }
+    __device__ __forceinline__ double
+    tp_fma(double a, double b, double c)
+    {
+      return fma(a, b, c);
+    }
+    __device__ __forceinline__ df64
+    tp_fma(df64 a, df64 b, df64 c)
+    {
+      return fma_(a, b, c);
+    }
+    template <typename T>
+    __host__ __device__ __forceinline__ T
+    tp_zero()
+    {
+      return T(0);
+    }
+    template <>
+    __host__ __device__ __forceinline__ df64
+    tp_zero<df64>()
+    {
+      return df64{0.f, 0.f};
     }
 
     // y = A_e x for one cell, x and y indexed [k][b][a] (z, y, x)
@@ -383,7 +413,7 @@ namespace mfgpu
           r.e[j] = v[j] + v[N - 1 - j];
           r.o[j] = v[j] - v[N - 1 - j];
         }
-      r.m = (N & 1) ? v[N / 2] : T(0);
+      r.m = (N & 1) ? v[N / 2] : tp_zero<T>();
       return r;
     }
 
@@ -402,25 +432,25 @@ namespace mfgpu
 #pragma unroll
       for (int i = 0; i < H; ++i)
         {
-          T se = FIRST ? M.E[i][0] * v.e[0] : fma(M.E[i][0], v.e[0], acc.se[i]);
-          T so = FIRST ? M.O[i][0] * v.o[0] : fma(M.O[i][0], v.o[0], acc.so[i]);
+          T se = FIRST ? M.E[i][0] * v.e[0] : tp_fma(M.E[i][0], v.e[0], acc.se[i]);
+          T so = FIRST ? M.O[i][0] * v.o[0] : tp_fma(M.O[i][0], v.o[0], acc.so[i]);
 #pragma unroll
           for (int j = 1; j < H; ++j)
             {
-              se = fma(M.E[i][j], v.e[j], se);
-              so = fma(M.O[i][j], v.o[j], so);
+              se = tp_fma(M.E[i][j], v.e[j], se);
+              so = tp_fma(M.O[i][j], v.o[j], so);
             }
           if (N & 1)
-            se = fma(M.C[i], v.m, se);
+            se = tp_fma(M.C[i], v.m, se);
           acc.se[i] = se;
           acc.so[i] = so;
         }
       if (N & 1)
         {
-          T sm = FIRST ? M.C[H] * v.m : fma(M.C[H], v.m, acc.sm);
+          T sm = FIRST ? M.C[H] * v.m : tp_fma(M.C[H], v.m, acc.sm);
 #pragma unroll
           for (int j = 0; j < H; ++j)
-            sm = fma(M.R[j], v.e[j], sm);
+            sm = tp_fma(M.R[j], v.e[j], sm);
           acc.sm = sm;
         }
     }
@@ -439,10 +469,12 @@ namespace mfgpu
         y[N / 2] = acc.sm;
     }
 
-    template <int N, typename T, bool CON>
+    // TS: storage type of the vectors, T: compute type (TS = double, T =
+    // df64: double-float arithmetic on FP64 vectors)
+    template <int N, typename TS, typename T, bool CON>
     __global__ void __launch_bounds__(blk_cells<N, T>() * N * N)
     heat_tp_block_kernel(const __grid_constant__ HeatTPEO<N, T> m, const __grid_constant__ CellGeom<T> g,
-                         const T *__restrict__ src, T *__restrict__ dst)
+                         const TS *__restrict__ src, TS *__restrict__ dst)
     {
       constexpr int N2 = N * N, P = N - 1;
       constexpr int CPB = blk_cells<N, T>();
@@ -477,7 +509,7 @@ namespace mfgpu
         T x[N];
 #pragma unroll
         for (int k = 0; k < N; ++k)
-          x[k] = (act && !con(k)) ? __ldg(src + colb + Nxy * k) : T(0);
+          x[k] = (act && !con(k)) ? to_compute<T, TS>(__ldg(src + colb + Nxy * k)) : tp_zero<T>();
         const EOSplit<N, T> xs = eo_split<N, T>(x);
         EOAcc<N, T>         au, av;
         eo_acc<N, T, true>(au, m.Mz, xs);
@@ -542,7 +574,7 @@ namespace mfgpu
 #pragma unroll
       for (int k = 0; k < N; ++k)
         {
-          T *d = dst + colb + Nxy * k;
+          TS *d = dst + colb + Nxy * k;
           if (con(k))
             {
               const bool owner = (i0 < P || cx == g.C[0] - 1) && (i1 < P || cy == g.C[1] - 1) &&
@@ -551,48 +583,48 @@ namespace mfgpu
                 *d += __ldg(src + colb + Nxy * k);
             }
           else
-            atomicAdd(d, U[k * SZ + i1 * N + i0]);
+            atomicAdd(d, to_storage<TS, T>(U[k * SZ + i1 * N + i0]));
         }
     }
 
-    template <int N, typename T>
+    template <int N, typename TS, typename T = TS>
     EOMat<N, T>
-    eo_mat(const T (&M)[N][N])
+    eo_mat(const TS (&M)[N][N])
     {
       constexpr int H = N / 2;
       EOMat<N, T>   r{};
       for (int i = 0; i < H; ++i)
         for (int j = 0; j < H; ++j)
           {
-            r.E[i][j] = T((double(M[i][j]) + double(M[i][N - 1 - j])) / 2);
-            r.O[i][j] = T((double(M[i][j]) - double(M[i][N - 1 - j])) / 2);
+            r.E[i][j] = conv_host<T>((double(M[i][j]) + double(M[i][N - 1 - j])) / 2);
+            r.O[i][j] = conv_host<T>((double(M[i][j]) - double(M[i][N - 1 - j])) / 2);
           }
       if (N & 1)
         {
           for (int i = 0; i < H; ++i)
             {
-              r.C[i] = M[i][H];
-              r.R[i] = M[H][i];
+              r.C[i] = conv_host<T>(double(M[i][H]));
+              r.R[i] = conv_host<T>(double(M[H][i]));
             }
-          r.C[H] = M[H][H];
+          r.C[H] = conv_host<T>(double(M[H][H]));
         }
       return r;
     }
 
-    template <int N, typename T>
+    template <int N, typename TS, typename T = TS>
     cudaError_t
     launch_block(const HostBasis &b, const LevelGeom &g, const HeatTPArgs &a, cudaStream_t s)
     {
-      constexpr int     CPB  = blk_cells<N, T>();
-      const size_t      smem = size_t(CPB) * BlkLay<N, T>::CS * sizeof(T);
-      const HeatTP<N, T> h0  = make_matrices<N, T>(b, g, a.kdt);
-      HeatTPEO<N, T>    h;
-      h.Mx = eo_mat<N, T>(h0.Mx);
-      h.Ax = eo_mat<N, T>(h0.Ax);
-      h.My = eo_mat<N, T>(h0.My);
-      h.Ky = eo_mat<N, T>(h0.Ky);
-      h.Mz = eo_mat<N, T>(h0.Mz);
-      h.Kz = eo_mat<N, T>(h0.Kz);
+      constexpr int      CPB  = blk_cells<N, T>();
+      const size_t       smem = size_t(CPB) * BlkLay<N, T>::CS * sizeof(T);
+      const HeatTP<N, TS> h0  = make_matrices<N, TS>(b, g, a.kdt);
+      HeatTPEO<N, T>     h;
+      h.Mx = eo_mat<N, TS, T>(h0.Mx);
+      h.Ax = eo_mat<N, TS, T>(h0.Ax);
+      h.My = eo_mat<N, TS, T>(h0.My);
+      h.Ky = eo_mat<N, TS, T>(h0.Ky);
+      h.Mz = eo_mat<N, TS, T>(h0.Mz);
+      h.Kz = eo_mat<N, TS, T>(h0.Kz);
       CellGeom<T>        cg  = make_cell_geom<T>(g);
       cg.batch               = unsigned(a.batch > 1 ? a.batch : 1);
       cg.bstride             = a.batch > 1 ? a.bstride : 0;
@@ -607,11 +639,11 @@ namespace mfgpu
         return cudaErrorInvalidValue;
       const dim3 gr(unsigned(grid), cg.batch);
       if (a.constrained)
-        heat_tp_block_kernel<N, T, true><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const T *>(a.src),
-                                                                       static_cast<T *>(a.dst));
+        heat_tp_block_kernel<N, TS, T, true><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const TS *>(a.src),
+                                                                           static_cast<TS *>(a.dst));
       else
-        heat_tp_block_kernel<N, T, false><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const T *>(a.src),
-                                                                        static_cast<T *>(a.dst));
+        heat_tp_block_kernel<N, TS, T, false><<<gr, CPB * N * N, smem, s>>>(h, cg, static_cast<const TS *>(a.src),
+                                                                            static_cast<TS *>(a.dst));
       return cudaGetLastError();
     }
 
@@ -1102,7 +1134,7 @@ namespace mfgpu
       return cudaErrorInvalidValue;
     // FP32 Q1 and Q2 over all cells, 16-byte aligned vectors, on request:
     // the TMA brick kernel
-    if (precision == 32 && a.tma && a.zc0 == 0 && a.zc1 == g.C[2] && (a.batch <= 1 || a.bstride == g.n_nodes))
+    if (precision == 32 && a.tma && !a.df64 && a.zc0 == 0 && a.zc1 == g.C[2] && (a.batch <= 1 || a.bstride == g.n_nodes))
       {
         cudaError_t e  = cudaSuccess;
         bool        ok = false;
@@ -1113,6 +1145,17 @@ namespace mfgpu
         if (ok)
           return e;
       }
+    // double-float arithmetic on FP64 vectors: the block kernel
+    if (precision == 64 && a.df64)
+      switch (b.N)
+        {
+          case 2: return tp::launch_block<2, double, df64>(b, g, a, s);
+          case 3: return tp::launch_block<3, double, df64>(b, g, a, s);
+          case 4: return tp::launch_block<4, double, df64>(b, g, a, s);
+          case 5: return tp::launch_block<5, double, df64>(b, g, a, s);
+          case 6: return tp::launch_block<6, double, df64>(b, g, a, s);
+          case 7: return tp::launch_block<7, double, df64>(b, g, a, s);
+        }
     // one thread per cell in registers at Q1 from 16384 cells on, the block
     // kernel above otherwise (measured with the padded block layout, CUDA
     // events, L2 flushed: 64^3 cells Q2 FP32 30.9 us in registers, 29.3 us

@@ -67,7 +67,8 @@ namespace mfgpu
                              const float *src, float *dst, int *err, cudaStream_t s);
 
   // the heat operator in its tensor-product form (1D mass and stiffness
-  // matrices, 7 sweeps per cell; mf_heat_tp.cu), N = 2..7, FP32 and FP64:
+  // matrices, 7 sweeps per cell; mf_heat_tp.cu), N = 2..7, FP32 and FP64
+  // (native, or double-float in the block form):
   // one thread per column segment of zlen cells in registers (N = 2 from
   // 16384 cells on), N^2 threads per cell through shared memory (otherwise),
   // or, on request,
@@ -88,6 +89,8 @@ namespace mfgpu
     // waits' timeout flag (8)
     bool        tma = false;
     int        *err = nullptr;
+    // FP64 vectors in double-float arithmetic (the block kernel)
+    bool        df64 = false;
   };
   bool        heat_tp_supported(int N, int precision);
   int         heat_tp_zlen(const LevelGeom &g, int zc0, int zc1, int N, int precision);

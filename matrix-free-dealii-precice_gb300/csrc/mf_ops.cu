@@ -758,8 +758,10 @@ namespace mfgpu
     // the heat operator's tensor-product kernel: by default from
     // TP_MIN_CELLS cells on (below, the point-parallel kernel), over whole
     // z-planes of cells, atomic scatter
-    if (a.kind == 0 && (a.kernel == 0 || a.kernel == 4 || a.kernel == 5) && !a.colored && arith == 0 &&
-        heat_tp_supported(basis.N, precision))
+    // (double-float from Q1 to Q5: at Q6 the sum-factorization kernel's
+    // double-float form is faster, 22.6 against 19.7 GDoF/s on 64^3 cells)
+    if (a.kind == 0 && (a.kernel == 0 || a.kernel == 4 || a.kernel == 5) && !a.colored &&
+        heat_tp_supported(basis.N, precision) && !(arith == 1 && basis.N == 7 && a.kernel != 4))
       {
         const size_t layer = size_t(geom.C[0]) * size_t(geom.C[1]);
         const size_t b0 = c1 > c0 ? c0 : 0, b1 = c1 > c0 ? std::min(c1, geom.n_cells) : geom.n_cells;
@@ -777,6 +779,7 @@ namespace mfgpu
             t.batch       = a.batch;
             t.bstride     = a.bstride;
             t.tma         = a.kernel == 5;
+            t.df64        = arith == 1;
             t.err         = ctx->err.as<int>();
             MF_CK(launch_heat_tp(basis, geom, precision, t, s));
             count_launch();

@@ -4,7 +4,8 @@ thread per cell column segment in registers) against the oracle's vmult
 (heat_transfer.h:236-250) and against the sum-factorization kernel.
 
 Degrees 1-6: one thread per cell in registers at Q1 on levels of 16384
-cells or more, the shared-memory block form otherwise.  Tolerances: FP64 1e-12 relative l2
+cells or more, the shared-memory block form otherwise (and always in
+double-float).  Tolerances: FP64 1e-12 relative l2
 (the operator parity bar), FP32 5e-5 as the other FP32 operator tests.  The meshes exercise what the kernel's
 work split depends on: rows of cells shorter and longer than a warp (the
 x-neighbour exchange by shuffles across warp ends), column segments that do
@@ -59,9 +60,13 @@ MESHES = {
 }
 
 
-@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("precision", [32, 64, "df64"])
 @pytest.mark.parametrize("mesh", sorted(MESHES))
 def test_tensor_product_heat_vmult(ctx, precision, mesh):
+    """FP32, native FP64 and double-float (FP64 vectors, the block form in
+    float-pair arithmetic: the FP64 bar of 1e-12)."""
+    df64 = precision == "df64"
+    precision = 64 if df64 else precision
     rep, nref, hi, bid, dirichlet = MESHES[mesh]
     # the 64 x 64 x 39 mesh tests the column segments of the register
     # kernel (degrees 1-2); the others every degree
@@ -75,6 +80,8 @@ def test_tensor_product_heat_vmult(ctx, precision, mesh):
         ref = O.heat_vmult(W.to_oracle_mesh(O, spec), nref, 0.1, src.astype(np.float64),
                            constrained=constrained)
         op = mfgpu.LaplaceOperator(ctx, m, -1, precision, constrained, delta_t=0.1)
+        if df64:
+            op.set_fp64_emulation(True)
         d_src = dev(src)
         d_sf, d_tp = dev(np.zeros_like(src)), dev(np.zeros_like(src))
         op.set_cell_kernel("line")
@@ -119,11 +126,10 @@ def test_tensor_product_heat_default_and_host_buffers(ctx, precision):
 
 
 def test_tensor_product_heat_rejects_unsupported(ctx):
-    """Double-float operators and two-dimensional meshes keep their own
+    """Two-dimensional meshes and the neo-Hookean operator keep their own
     kernels."""
-    spec = W.unit_cube_heat(2, 1)
-    op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
-    op.set_fp64_emulation(True)
+    spec = W.cantilever(2, 1, rep=(2, 1, 1), length=(2.0, 1.0, 1.0))
+    op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, "referential_qp")
     with pytest.raises(mfgpu.MfgpuError):
         op.set_cell_kernel("tp")
     m2 = mfgpu.make_mesh(2, 2, (1, 1), (0.0, 0.0), (1.0, 1.0), boundary_id=(1, 0, 0, 0),
