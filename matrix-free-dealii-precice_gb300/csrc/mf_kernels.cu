@@ -58,9 +58,13 @@ namespace mfgpu
       // 498 / 580; 32768 cells Q3 881 / 951, Q4 1995 / 2004, Q6 863 / 873;
       // Q2 at 32768 cells 384 / 345, where the line kernel's even-odd sweeps
       // win)
-      const unsigned point_below = !std::is_same<T, double>::value ? POINT_CELLS :
-                                   (Op::prefetch && N != 3)        ? 0xffffffffu :
-                                                                     4097u;
+      // (the FP32 referential_qp tangent at Q2 up to 4096 cells as well:
+      // 13.0 against 17.0 us there)
+      const unsigned point_below = !std::is_same<T, double>::value ?
+                                     ((std::is_same<T, float>::value && N == 3 && Op::prefetch) ? 4097u :
+                                                                                                 POINT_CELLS) :
+                                   (Op::prefetch && N != 3) ? 0xffffffffu :
+                                                              4097u;
       if (cg.color < 0 && n_cells > 0 && (kernel == 2 || (kernel == 0 && n_cells < point_below)))
         {
           // few cells: one block per cell, one thread per point
