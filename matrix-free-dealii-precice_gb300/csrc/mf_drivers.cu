@@ -34,16 +34,16 @@ namespace mfgpu
 
   static cudaError_t
   dispatch_heat_rhs(int N, const HostBasis &b, const LevelGeom &g, double dt,
-                    const SourceDesc &f, const double *u_old, double *rhs, cudaStream_t s)
+                    const SourceDesc &f, const double *u_old, double *rhs, double *tab, cudaStream_t s)
   {
     switch (N)
       {
-        case 2: return launch_heat_rhs<2>(b, g, dt, f, u_old, rhs, s);
-        case 3: return launch_heat_rhs<3>(b, g, dt, f, u_old, rhs, s);
-        case 4: return launch_heat_rhs<4>(b, g, dt, f, u_old, rhs, s);
-        case 5: return launch_heat_rhs<5>(b, g, dt, f, u_old, rhs, s);
-        case 6: return launch_heat_rhs<6>(b, g, dt, f, u_old, rhs, s);
-        case 7: return launch_heat_rhs<7>(b, g, dt, f, u_old, rhs, s);
+        case 2: return launch_heat_rhs<2>(b, g, dt, f, u_old, rhs, tab, s);
+        case 3: return launch_heat_rhs<3>(b, g, dt, f, u_old, rhs, tab, s);
+        case 4: return launch_heat_rhs<4>(b, g, dt, f, u_old, rhs, tab, s);
+        case 5: return launch_heat_rhs<5>(b, g, dt, f, u_old, rhs, tab, s);
+        case 6: return launch_heat_rhs<6>(b, g, dt, f, u_old, rhs, tab, s);
+        case 7: return launch_heat_rhs<7>(b, g, dt, f, u_old, rhs, tab, s);
       }
     return cudaErrorInvalidValue;
   }
@@ -822,7 +822,13 @@ namespace mfgpu
         if (G.dim == 2)
           MF_CK(launch_heat_rhs2d(basis.N, basis, G, P.dt, srcs[b], sol_old.as<double>() + b * n0, rb, ctx->stream));
         else
-          MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, srcs[b], sol_old.as<double>() + b * n0, rb, ctx->stream));
+          {
+            src_tab.ensure(heat_rhs_table_size(G, basis.N) * sizeof(double));
+            MF_CK(dispatch_heat_rhs(basis.N, basis, G, P.dt, srcs[b], sol_old.as<double>() + b * n0, rb,
+                                    src_tab.as<double>(), ctx->stream));
+            if (srcs[b].n_gauss > 0)
+              count_launch(); // the source table
+          }
         count_launch();
         tol[b] = P.solver.tol * std::sqrt(vec_dot<double>(*ctx, n0, rb, rb));
       }

@@ -127,6 +127,7 @@ namespace mfgpu
     double                                     t       = 0;
     SourceDesc                                 src{};
     DevBuf                                     cg_ws; // vectors of the outer CG, kept across steps
+    DevBuf                                     src_tab; // per-direction factors of the source's Gaussians
     PhaseTimer                                 timer;
     // a batch of nb problems of one shape (mesh, time step, solver) with
     // their own loads: one operator, one multigrid hierarchy and one CG

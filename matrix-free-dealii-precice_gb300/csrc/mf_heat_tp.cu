@@ -1107,6 +1107,94 @@ namespace mfgpu
     }
   } // namespace tp
 
+  namespace tp
+  {
+    // The diagonal of the assembled heat operator on a box level.  The cells
+    // form a Cartesian product, so the assembled operator is the same sum of
+    // Kronecker products as the element operator, of the assembled 1D
+    // matrices: diag = vol [dMz dMy dMx + c0 dMz dMy dKx + c1 dMz dKy dMx +
+    // c2 dKz dMy dMx] with c_d = kdt / h_d^2, where the assembled 1D
+    // diagonal at node i = c p + a is the element diagonal at a for an
+    // interior node (0 < a < p) and the sum of the two elements' end entries
+    // at a vertex.  Rows of constrained nodes are set by the caller.
+    struct HeatDiag
+    {
+      int    N, p, C[3], Nn[3];
+      size_t n_nodes;
+      double m[MAX_N], k[MAX_N]; // element diagonals of M and K on [0,1]
+      double vol, c[3];
+    };
+
+    __device__ __forceinline__ void
+    diag1d(const HeatDiag &d, int i, int dir, double &m, double &k)
+    {
+      const int c = i / d.p, a = i - c * d.p;
+      if (a != 0)
+        {
+          m = d.m[a];
+          k = d.k[a];
+          return;
+        }
+      m = (c > 0 ? d.m[d.p] : 0.0) + (c < d.C[dir] ? d.m[0] : 0.0);
+      k = (c > 0 ? d.k[d.p] : 0.0) + (c < d.C[dir] ? d.k[0] : 0.0);
+    }
+
+    template <typename T>
+    __global__ void
+    heat_diag_kernel(const __grid_constant__ HeatDiag d, T *__restrict__ out)
+    {
+      for (size_t n = size_t(blockIdx.x) * blockDim.x + threadIdx.x; n < d.n_nodes;
+           n += size_t(gridDim.x) * blockDim.x)
+        {
+          const int ix = int(n % size_t(d.Nn[0]));
+          const int iy = int((n / size_t(d.Nn[0])) % size_t(d.Nn[1]));
+          const int iz = int(n / (size_t(d.Nn[0]) * size_t(d.Nn[1])));
+          double    mx, kx, my, ky, mz, kz;
+          diag1d(d, ix, 0, mx, kx);
+          diag1d(d, iy, 1, my, ky);
+          diag1d(d, iz, 2, mz, kz);
+          out[n] = T(d.vol * (mz * my * (mx + d.c[0] * kx) + d.c[1] * mz * ky * mx + d.c[2] * kz * my * mx));
+        }
+    }
+  } // namespace tp
+
+  cudaError_t
+  launch_heat_diag_tp(const HostBasis &b, const LevelGeom &g, int precision, double kdt, void *out, cudaStream_t s)
+  {
+    if (g.dim == 2 || b.N < 2 || b.N > MAX_N || g.p != b.N - 1)
+      return cudaErrorInvalidValue;
+    tp::HeatDiag d{};
+    d.N       = b.N;
+    d.p       = b.N - 1;
+    d.n_nodes = g.n_nodes;
+    for (int dir = 0; dir < 3; ++dir)
+      {
+        d.C[dir]  = g.C[dir];
+        d.Nn[dir] = g.Nn[dir];
+        d.c[dir]  = kdt / (g.h[dir] * g.h[dir]);
+      }
+    d.vol = g.h[0] * g.h[1] * g.h[2];
+    for (int i = 0; i < b.N; ++i)
+      {
+        double m = 0, k = 0;
+        for (int q = 0; q < b.N; ++q)
+          {
+            m += b.w[q] * b.S[q * b.N + i] * b.S[q * b.N + i];
+            k += b.w[q] * b.G[q * b.N + i] * b.G[q * b.N + i];
+          }
+        d.m[i] = m;
+        d.k[i] = k;
+      }
+    const size_t blocks = std::min<size_t>((g.n_nodes + 255) / 256, size_t(152) * 32);
+    if (blocks == 0)
+      return cudaSuccess;
+    if (precision == 32)
+      tp::heat_diag_kernel<float><<<unsigned(blocks), 256, 0, s>>>(d, static_cast<float *>(out));
+    else
+      tp::heat_diag_kernel<double><<<unsigned(blocks), 256, 0, s>>>(d, static_cast<double *>(out));
+    return cudaGetLastError();
+  }
+
   bool
   heat_tp_supported(int N, int precision)
   {

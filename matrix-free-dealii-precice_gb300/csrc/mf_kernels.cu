@@ -1,6 +1,7 @@
 // Instantiation of the cell kernels for one degree.  Compiled once per
 // N = p+1 in {2..7} with -DMF_N=<N>, so the per-degree builds run in
 // parallel.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -319,7 +320,7 @@ namespace mfgpu
   cudaError_t
   launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
                   const SourceDesc &f, const double *u_old, double *rhs,
-                  cudaStream_t s)
+                  double *tab, cudaStream_t s)
   {
     const Shape<N, double>  sh = make_shape<N, double>(b);
     const CellGeom<double>  cg = make_cell_geom<double>(g);
@@ -341,6 +342,23 @@ namespace mfgpu
       }
     for (int i = 0; i < N; ++i)
       sd.xq[i] = b.xq[i];
+    sd.N = N;
+    sd.J = 0;
+    for (int d = 0; d < 3; ++d)
+      {
+        sd.C[d] = g.C[d];
+        sd.J    = std::max(sd.J, g.C[d] * N);
+      }
+    if (sd.n_gauss < 0 || sd.n_gauss > 8 || !tab)
+      return cudaErrorInvalidValue;
+    if (sd.n_gauss > 0)
+      {
+        const int total = sd.n_gauss * 3 * sd.J;
+        heat_source_table_kernel<<<(total + 255) / 256, 256, 0, s>>>(sd, tab);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+          return e;
+      }
     constexpr int  CPB  = cells_per_block<N, 1, double>();
     const size_t   smem = size_t(CPB) * smem_per_cell<N, 1, false>() * sizeof(double);
     const unsigned grid = (cg.n_cells + CPB - 1) / CPB;
@@ -348,7 +366,7 @@ namespace mfgpu
     cudaError_t    e    = prepare(k, smem);
     if (e != cudaSuccess)
       return e;
-    k<<<grid, CPB * N * N, smem, s>>>(sh, cg, sd, dt, u_old, rhs);
+    k<<<grid, CPB * N * N, smem, s>>>(sh, cg, sd, dt, u_old, rhs, tab);
     return cudaGetLastError();
   }
 
@@ -359,7 +377,7 @@ namespace mfgpu
   template cudaError_t launch_diag<MF_N, double>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const void *, void *, cudaStream_t);
   template cudaError_t launch_diag<MF_N, float>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const void *, void *, cudaStream_t);
   template cudaError_t launch_residual<MF_N>(const HostBasis &, const LevelGeom &, int, const NHMatD &, double, const double *, const double *, const double *, double *, cudaStream_t);
-  template cudaError_t launch_heat_rhs<MF_N>(const HostBasis &, const LevelGeom &, double, const SourceDesc &, const double *, double *, cudaStream_t);
+  template cudaError_t launch_heat_rhs<MF_N>(const HostBasis &, const LevelGeom &, double, const SourceDesc &, const double *, double *, double *, cudaStream_t);
   template <int N>
   cudaError_t
   launch_apply_df(const HostBasis &b, const LevelGeom &g, const ApplyArgs &a,

@@ -93,6 +93,11 @@ namespace mfgpu
     bool        df64 = false;
   };
   bool        heat_tp_supported(int N, int precision);
+  // the assembled heat operator's diagonal on a box level from the 1D
+  // element diagonals (out = diag for every node; constrained rows are the
+  // caller's), FP32 or FP64 out
+  cudaError_t launch_heat_diag_tp(const HostBasis &b, const LevelGeom &g, int precision, double kdt, void *out,
+                                  cudaStream_t s);
   int         heat_tp_zlen(const LevelGeom &g, int zc0, int zc1, int N, int precision);
   cudaError_t launch_heat_tp(const HostBasis &b, const LevelGeom &g, int precision, const HeatTPArgs &a,
                              cudaStream_t s);
@@ -147,10 +152,20 @@ namespace mfgpu
     double amp[8];
   };
 
+  // tab: device scratch of heat_rhs_table_size(g, N) doubles (the
+  // per-direction factors of the Gaussians at the quadrature coordinates)
   template <int N>
   cudaError_t launch_heat_rhs(const HostBasis &b, const LevelGeom &g, double dt,
                               const SourceDesc &f, const double *u_old,
-                              double *rhs, cudaStream_t s);
+                              double *rhs, double *tab, cudaStream_t s);
+  inline size_t
+  heat_rhs_table_size(const LevelGeom &g, int N)
+  {
+    int j = 0;
+    for (int d = 0; d < 3; ++d)
+      j = g.C[d] * N > j ? g.C[d] * N : j;
+    return size_t(8) * 3 * size_t(j);
+  }
 
   // two-dimensional kernels (mf_kernels2d.cu); N = p+1, precision 32 / 64
   cudaError_t launch_apply2d(int N, int precision, const HostBasis &b, const LevelGeom &g,

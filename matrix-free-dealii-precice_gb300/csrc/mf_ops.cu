@@ -1185,9 +1185,9 @@ namespace mfgpu
         finish_diagonal();
         return;
       }
-    cudaError_t e = precision == 32 ?
-                      dispatch_diag<float>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream) :
-                      dispatch_diag<double>(basis.N, basis, geom, 0, md, coefficient * delta_t, nullptr, inv_diag.ptr, ctx->stream);
+    // the closed form of the box level's assembled diagonal (one pass over
+    // the nodes instead of a cell loop)
+    cudaError_t e = launch_heat_diag_tp(basis, geom, precision, coefficient * delta_t, inv_diag.ptr, ctx->stream);
     count_launch();
     MF_CK(e);
     // a batch: the problems share the operator, hence the diagonal

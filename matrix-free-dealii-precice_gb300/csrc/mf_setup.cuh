@@ -567,14 +567,44 @@ namespace mfgpu
     double lo[3];
     double h[3];
     double xq[MAX_N];
+    int    C[3];
+    int    N;
+    int    J; // table row length: max_d C[d] N
   };
+
+  // The Gaussians of the source are separable on the level's tensor grid of
+  // quadrature points: exp(-|x - c|^2 / (2 w^2)) is the product of one
+  // factor per direction, each a function of that direction's point
+  // coordinate only.  tab[(3 i + d) J + j] = exp(-(x_j - c_id)^2 / (2 w_i^2))
+  // for the j-th quadrature coordinate along d (cell j / N, point j % N), so
+  // the right-hand side takes three table reads per Gaussian and point
+  // instead of an exponential and a division (the same values to a few
+  // units in the last place).
+  static __global__ void
+  heat_source_table_kernel(const __grid_constant__ SourceDev f, double *__restrict__ tab)
+  {
+    const int total = f.n_gauss * 3 * f.J;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+      {
+        const int j = t % f.J, r = t / f.J, d = r % 3, i = r / 3;
+        double    v = 0.0;
+        if (j < f.C[d] * f.N)
+          {
+            const int    c = j / f.N, q = j - c * f.N;
+            const double x = f.lo[d] + (c + f.xq[q]) * f.h[d] - f.center[i][d];
+            v              = exp(-(x * x) / (2 * f.width[i] * f.width[i]));
+          }
+        tab[t] = v;
+      }
+  }
 
   template <int N>
   __global__ void __launch_bounds__(cells_per_block<N, 1, double>() * N * N)
   heat_rhs_kernel(const __grid_constant__ Shape<N, double> sh,
                   const __grid_constant__ CellGeom<double> g,
                   const __grid_constant__ SourceDev f, double dt,
-                  const double *__restrict__ u_old, double *__restrict__ rhs)
+                  const double *__restrict__ u_old, double *__restrict__ rhs,
+                  const double *__restrict__ tab)
   {
     using T           = double;
     constexpr int N2  = N * N;
@@ -605,21 +635,17 @@ namespace mfgpu
     __syncthreads();
     load_line<N, T, 0>(T1, a, b, x);
     mat_apply<N>(sh.S, x, y);
-    // x-line (qy=a, qz=b): add dt f at the quadrature points, times JxW
-    const double py = f.lo[1] + (cy + f.xq[a]) * f.h[1];
-    const double pz = f.lo[2] + (cz + f.xq[b]) * f.h[2];
+    // x-line (qy=a, qz=b): add dt f at the quadrature points, times JxW;
+    // the Gaussians as products of their per-direction factors
+    double fyz[8];
+    for (int i = 0; i < f.n_gauss; ++i)
+      fyz[i] = f.amp[i] * tab[(3 * i + 1) * f.J + cy * N + a] * tab[(3 * i + 2) * f.J + cz * N + b];
 #pragma unroll
     for (int qx = 0; qx < N; ++qx)
       {
-        const double px = f.lo[0] + (cx + f.xq[qx]) * f.h[0];
-        double       fv = f.constant;
+        double fv = f.constant;
         for (int i = 0; i < f.n_gauss; ++i)
-          {
-            const double dx = px - f.center[i][0], dy = py - f.center[i][1],
-                         dz = pz - f.center[i][2];
-            fv += f.amp[i] * exp(-(dx * dx + dy * dy + dz * dz) /
-                                 (2 * f.width[i] * f.width[i]));
-          }
+          fv += fyz[i] * tab[(3 * i) * f.J + cx * N + qx];
         y[qx] = (y[qx] + dt * fv) * (sh.w[qx] * sh.w[a] * sh.w[b] * g.vol);
       }
     store_line<N, T, 0>(V, a, b, y);
