@@ -812,9 +812,18 @@ namespace mfgpu
                                 ctx->stream));
           ctx->sync();
         }
-    // rhs = -A_unconstrained uD + int (u_old + dt f) v
-    op_u->vmult(rhs.ptr, uD.ptr);
-    vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
+    // rhs = -A_unconstrained uD + int (u_old + dt f) v; without Dirichlet
+    // data (uD = 0, the homogeneous problems) the first term is zero
+    bool any_lift = false;
+    for (int b = 0; b < nb; ++b)
+      any_lift = any_lift || Pb[b].analytic;
+    if (any_lift)
+      {
+        op_u->vmult(rhs.ptr, uD.ptr);
+        vec_axpby<double>(*ctx, n, 0.0, rhs.as<double>(), -1.0, rhs.as<double>());
+      }
+    else
+      MF_CK(cudaMemsetAsync(rhs.ptr, 0, n * sizeof(double), ctx->stream));
     std::vector<double> tol(static_cast<size_t>(nb), 0.0);
     for (int b = 0; b < nb; ++b)
       {
