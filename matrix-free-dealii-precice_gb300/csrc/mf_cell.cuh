@@ -1099,8 +1099,8 @@ namespace mfgpu
                     const size_t gcol = size_t(jc) * g.n_nodes + size_t(cx * g.p + ja) +
                                         size_t(g.Nn[0]) * (size_t(cy * g.p + jb) +
                                                            size_t(g.Nn[1]) * size_t(cz * g.p + jk));
-                    atomicAdd(dst + (size_t(c) * g.n_nodes + node) * (size_t(NC) * g.n_nodes) + gcol,
-                              to_storage<TS, T>(col[k]));
+                    const size_t ld = g.unit_ld ? g.unit_ld : size_t(NC) * g.n_nodes;
+                    atomicAdd(dst + (size_t(c) * g.n_nodes + node) * ld + gcol, to_storage<TS, T>(col[k]));
                     continue;
                   }
                 if (CONSTRAINED && ((col_mask(k) >> c) & 1u))

@@ -141,6 +141,8 @@ namespace mfgpu
     size_t   bstride;
     // C[0] and C[1] as fast divisors: cell -> (x, y, z)
     FastDiv  dC0, dC1;
+    // element-column launches: row stride of the dense matrix (0: NC n_nodes)
+    size_t   unit_ld;
   };
 
   // host-side conversion of a double constant to a compute type
@@ -171,6 +173,7 @@ namespace mfgpu
     c.p       = g.p;
     c.batch   = 1;
     c.bstride = 0;
+    c.unit_ld = 0;
     c.n_cells    = unsigned(g.n_cells);
     c.cell_begin = 0;
     c.cell_end   = unsigned(g.n_cells);

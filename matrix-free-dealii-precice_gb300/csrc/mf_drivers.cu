@@ -418,7 +418,7 @@ namespace mfgpu
         if (mesh.dim == 2)
           k_traction2d<<<unsigned(g.C[1 - nd]), 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
         else
-          k_traction<<<unsigned(g.C[d1] * g.C[d2]), 64, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
+          k_traction<<<unsigned(g.C[d1] * g.C[d2]), 128, 0, ctx->stream>>>(A, u.as<double>(), rhs.as<double>());
         count_launch();
         MF_CK(cudaGetLastError());
       }

@@ -228,11 +228,15 @@ namespace mfgpu
   void cheby_update(Context &c, size_t n, T f1, T f2, bool first, bool zero_ax, const T *b, T *Ax, const T *dinv,
                     T *x, T *xold);
   // constrained rows: op 0 dst=src, 1 dst+=src, 2 dst=0, 3 dst=1, 4 (dst a
-  // dense nc n_nodes square matrix) unit diagonal entry
-  template <typename T> void constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst);
-  // dense row-major n x n operators in precision 32 (float) or 64 (double)
-  void dense_mv(Context &c, int precision, size_t n, const void *A, const void *x, void *y, bool add);
-  void dense_constrained_identity(Context &c, int precision, const LevelGeom &g, int nc, void *A);
+  // dense nc n_nodes square matrix of row stride ld, 0: nc n_nodes) unit
+  // diagonal entry
+  template <typename T>
+  void constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst, size_t ld = 0);
+  // dense row-major n x n operators in precision 32 (float) or 64 (double),
+  // row stride ld = dense_row_stride(n), the entries past column n zero
+  size_t dense_row_stride(size_t n);
+  void   dense_mv(Context &c, int precision, size_t n, const void *A, const void *x, void *y, bool add);
+  void   dense_constrained_identity(Context &c, int precision, const LevelGeom &g, int nc, void *A);
   // one Chebyshev step x_new = x + f1 (x - xo) + f2 dinv (b - A x) (first:
   // x_new = (1 + f1) x + f2 dinv (b - A x)) into xo
   template <typename T>
@@ -322,8 +326,9 @@ namespace mfgpu
     virtual void      compute_diagonal() = 0;
     // Dense copy of a small operator (at most DENSE_MAX_BYTES): the entries
     // of A assembled from element columns (one launch), constrained rows
-    // and columns as the identity.  vmult / vmult_add multiply by it (one
-    // warp per row) while value_state() is what it was at assembly.
+    // and columns as the identity, rows dense_row_stride(m()) apart.  vmult /
+    // vmult_add multiply by it while value_state() is what it was at
+    // assembly.
     static constexpr size_t DENSE_MAX_BYTES = size_t(64) << 20;
     DevBuf                  dense;
     size_t                  dense_key = 0;

@@ -94,6 +94,7 @@ namespace mfgpu
     {
       c.batch   = unsigned(a.batch > 1 ? a.batch : 1);
       c.bstride = a.batch > 1 ? a.bstride : 0;
+      c.unit_ld = a.unit_ld;
       if (a.cell_end > a.cell_begin)
         {
           c.cell_begin = unsigned(a.cell_begin);

@@ -49,6 +49,9 @@ namespace mfgpu
     // n_nodes, zeroed by the caller) and receives the operator's entries of
     // the unconstrained rows and columns; src is not read
     bool        unit = false;
+    // row stride of that matrix in elements (0: m); padded so that every
+    // row starts on a 16-byte boundary
+    size_t      unit_ld = 0;
     // cell kernel: 0 by grid size (point-parallel below POINT_CELLS cells),
     // 1 line-parallel (cell_apply_kernel), 2 point-parallel
     int         kernel = 0;

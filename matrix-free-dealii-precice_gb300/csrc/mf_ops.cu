@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "mf_host.h"
 #include "mf_vec.cuh"
@@ -527,7 +528,7 @@ namespace mfgpu
   }
   template <typename T>
   void
-  constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst)
+  constrained_op(Context &c, const LevelGeom &g, int nc, int op, const T *src, T *dst, size_t ld)
   {
     bool any = false;
     for (int f = 0; f < 6; ++f)
@@ -541,6 +542,7 @@ namespace mfgpu
     for (int f = 0; f < 6; ++f)
       fi.face_mask[f] = g.face_mask[f];
     fi.nc = nc;
+    fi.ld = ld ? ld : size_t(nc) * g.n_nodes;
     size_t maxface = 0;
     for (int d = 0; d < 3; ++d)
       maxface = std::max(maxface, g.n_nodes / size_t(g.Nn[d]));
@@ -550,34 +552,81 @@ namespace mfgpu
     MF_CK(cudaGetLastError());
   }
 
-  static unsigned
-  warp_rows_grid(size_t n)
+  // threads per row of the dense kernels: the largest power of two up to
+  // 256 that keeps n rows within about one full wave (152 SMs x 2048 threads)
+  static int
+  dense_tpr(size_t n)
   {
-    return unsigned((n * 32 + 255) / 256);
+    int tpr = 32;
+    while (tpr < 256 && n * size_t(tpr) * 2 <= size_t(152) * 2048)
+      tpr *= 2;
+    return tpr;
+  }
+
+  size_t
+  dense_row_stride(size_t n)
+  {
+    return (n + 3) / 4 * 4;
+  }
+
+  template <typename T, class Launch>
+  static void
+  dense_launch(size_t n, Launch &&launch)
+  {
+    if (n > size_t(4096))
+      throw Error(ERR_ARG, "dense operator larger than 4096 rows");
+    const int      tpr  = dense_tpr(n);
+    const unsigned grid = unsigned((n * size_t(tpr) + DENSE_THREADS - 1) / DENSE_THREADS);
+    const size_t   smem = dense_row_stride(n) * sizeof(T);
+    switch (tpr)
+      {
+        case 32:
+          launch(std::integral_constant<int, 32>(), grid, smem);
+          break;
+        case 64:
+          launch(std::integral_constant<int, 64>(), grid, smem);
+          break;
+        case 128:
+          launch(std::integral_constant<int, 128>(), grid, smem);
+          break;
+        default:
+          launch(std::integral_constant<int, 256>(), grid, smem);
+          break;
+      }
+  }
+
+  template <typename T>
+  static void
+  dense_mv_t(Context &c, size_t n, const T *A, const T *x, T *y, bool add)
+  {
+    dense_launch<T>(n, [&](auto tpr, unsigned grid, size_t smem) {
+      k_dense_mv<T, decltype(tpr)::value>
+        <<<grid, DENSE_THREADS, smem, c.stream>>>(int(n), int(dense_row_stride(n)), A, x, y, int(add));
+    });
+    count_launch();
+    MF_CK(cudaGetLastError());
   }
 
   void
   dense_mv(Context &c, int precision, size_t n, const void *A, const void *x, void *y, bool add)
   {
     if (precision == 32)
-      k_dense_mv<float><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, static_cast<const float *>(A),
-                                                                 static_cast<const float *>(x),
-                                                                 static_cast<float *>(y), int(add));
+      dense_mv_t<float>(c, n, static_cast<const float *>(A), static_cast<const float *>(x),
+                        static_cast<float *>(y), add);
     else
-      k_dense_mv<double><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, static_cast<const double *>(A),
-                                                                  static_cast<const double *>(x),
-                                                                  static_cast<double *>(y), int(add));
-    count_launch();
-    MF_CK(cudaGetLastError());
+      dense_mv_t<double>(c, n, static_cast<const double *>(A), static_cast<const double *>(x),
+                         static_cast<double *>(y), add);
   }
 
   void
   dense_constrained_identity(Context &c, int precision, const LevelGeom &g, int nc, void *A)
   {
     if (precision == 32)
-      constrained_op<float>(c, g, nc, 4, nullptr, static_cast<float *>(A));
+      constrained_op<float>(c, g, nc, 4, nullptr, static_cast<float *>(A),
+                            dense_row_stride(size_t(nc) * g.n_nodes));
     else
-      constrained_op<double>(c, g, nc, 4, nullptr, static_cast<double *>(A));
+      constrained_op<double>(c, g, nc, 4, nullptr, static_cast<double *>(A),
+                             dense_row_stride(size_t(nc) * g.n_nodes));
   }
 
   template <typename T>
@@ -585,7 +634,11 @@ namespace mfgpu
   cheby_dense_step(Context &c, size_t n, const T *A, T f1, T f2, bool first, const T *b, const T *dinv,
                    const T *x, T *xo)
   {
-    k_cheby_dense<T><<<warp_rows_grid(n), 256, 0, c.stream>>>(n, A, f1, f2, int(first), b, dinv, x, xo);
+    dense_launch<T>(n, [&](auto tpr, unsigned grid, size_t smem) {
+      k_cheby_dense<T, decltype(tpr)::value>
+        <<<grid, DENSE_THREADS, smem, c.stream>>>(int(n), int(dense_row_stride(n)), A, f1, f2, int(first), b, dinv,
+                                                  x, xo);
+    });
     count_launch();
     MF_CK(cudaGetLastError());
   }
@@ -608,7 +661,7 @@ namespace mfgpu
   template void cheby_start<T>(Context &, size_t, T, const T *, const T *, T *, T *);       \
   template void cheby_dense_step<T>(Context &, size_t, const T *, T, T, bool, const T *, const T *, const T *, T *); \
   template void cheby_update<T>(Context &, size_t, T, T, bool, bool, const T *, T *, const T *, T *, T *); \
-  template void constrained_op<T>(Context &, const LevelGeom &, int, int, const T *, T *);
+  template void constrained_op<T>(Context &, const LevelGeom &, int, int, const T *, T *, size_t);
   MF_INST_VEC(float)
   MF_INST_VEC(double)
   template void vec_convert<float, double>(Context &, size_t, const double *, float *);
@@ -809,7 +862,8 @@ namespace mfgpu
   Operator::dense_fits() const
   {
     const size_t n = m();
-    return geom.dim == 3 && constrained && !heat_batch && n > 0 && n <= DENSE_MAX_BYTES / elem_size() / n;
+    return geom.dim == 3 && constrained && !heat_batch && n > 0 &&
+           n <= DENSE_MAX_BYTES / elem_size() / dense_row_stride(n);
   }
 
   void
@@ -820,10 +874,12 @@ namespace mfgpu
                                      std::to_string(DENSE_MAX_BYTES >> 20) + " MiB only");
     const size_t n = m();
     ApplyArgs    a = cell_args();
-    dense.ensure(n * n * elem_size());
+    const size_t ld = dense_row_stride(n);
+    dense.ensure(n * ld * elem_size());
     MF_CK(cudaMemsetAsync(dense.ptr, 0, dense.bytes, ctx->stream));
-    a.dst  = dense.ptr;
-    a.unit = true;
+    a.dst     = dense.ptr;
+    a.unit    = true;
+    a.unit_ld = ld;
     cudaError_t e = precision == 32 ? dispatch_apply<float>(basis.N, basis, geom, a, ctx->stream) :
                     arith == 1      ? dispatch_apply_df(basis.N, basis, geom, a, ctx->stream) :
                                       dispatch_apply<double>(basis.N, basis, geom, a, ctx->stream);

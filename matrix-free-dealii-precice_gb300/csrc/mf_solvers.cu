@@ -221,18 +221,23 @@ namespace mfgpu
     std::vector<double> h;
     MF_CK(cudaMemsetAsync(counter, 0, sizeof(int), c.stream));
     // point-Jacobi preconditioner and an operator that adds: four launches
-    // per iteration (q = A p into the q that the previous direction kernel
-    // zeroed; p.q; x, r, z with |r|^2 and r.z; p and the record)
-    const T *jd = P ? P->jacobi_diagonal() : nullptr;
-    if (jd && A.can_add())
+    // per iteration (q = A p into a zero q; p.q; x, r, z with |r|^2 and
+    // r.z; p and the record).  The direction kernel zeroes q for the next
+    // iteration on small vectors, a memset on large ones
+    // (ZERO_IN_KERNEL_BYTES).
+    const T   *jd     = P ? P->jacobi_diagonal() : nullptr;
+    const bool q_kern = n * sizeof(T) <= ZERO_IN_KERNEL_BYTES;
+    if (jd && A.can_add() && q_kern)
       MF_CK(cudaMemsetAsync(q, 0, n * sizeof(T), c.stream));
     auto iteration = [&]() {
       if (jd && A.can_add())
         {
+          if (!q_kern)
+            MF_CK(cudaMemsetAsync(q, 0, n * sizeof(T), c.stream));
           A.vmult_add(q, p);
           vec_dot_dev<T>(c, n, p, q, S_PQ);
           cg_update_jacobi<T>(c, n, rz, S_PQ, x, p, r, q, jd, z, S_RR, rzn);
-          cg_direction_rec<T>(c, n, rz, rzn, S_PQ, S_RR, z, p, q, rec, counter);
+          cg_direction_rec<T>(c, n, rz, rzn, S_PQ, S_RR, z, p, q_kern ? q : nullptr, rec, counter);
           std::swap(rz, rzn);
           return;
         }

@@ -107,6 +107,42 @@ namespace mfgpu
     return v;
   }
 
+  // block sum of values that only lane 0 of each warp holds
+  __device__ __forceinline__ double
+  block_sum_lane0(double v)
+  {
+    __shared__ double wl[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+      wl[wid] = v;
+    __syncthreads();
+    v = 0;
+    if (wid == 0)
+      {
+        const int nw = (blockDim.x + 31) >> 5;
+        v            = lane < nw ? wl[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          v += __shfl_down_sync(0xffffffffu, v, o);
+      }
+    return v;
+  }
+
+  // num / den of two device scalars, divided by one thread per block and
+  // shared: an FP64 division is a sequence of FP64 instructions, and on a
+  // GPU whose FP64 rate is a small fraction of its FP32 rate, dividing in
+  // every thread of a vector kernel took longer than the vector traffic
+  // (same quotient in every thread; every thread of the block must call it)
+  __device__ __forceinline__ double
+  block_ratio(const double *__restrict__ num, const double *__restrict__ den)
+  {
+    __shared__ double q;
+    if (threadIdx.x == 0)
+      q = *num / *den;
+    __syncthreads();
+    return q;
+  }
+
   // Single-launch reduction: every block stores its partial; the block that
   // finishes last (ticket) sums all partials in a fixed order (the same
   // order for the same partials, so the result is deterministic) into *out and
@@ -199,6 +235,34 @@ namespace mfgpu
     __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
   };
 
+  // block sum of the per-thread accumulators.  For float vectors the warp
+  // part adds the compensated pairs on the FP32 pipe (TwoSum of the high
+  // parts, the low parts and the TwoSum errors added) and one value per
+  // warp goes to FP64, instead of FP64 shuffles and adds in every thread.
+  template <typename T>
+  __device__ __forceinline__ double
+  block_sum_acc(const ProdAcc<T> &a)
+  {
+    return block_sum(a.value());
+  }
+  template <>
+  __device__ __forceinline__ double
+  block_sum_acc<float>(const ProdAcc<float> &a)
+  {
+    float hi = a.hi, lo = a.lo;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        float       s, t;
+        two_sum(hi, h2, s, t);
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(l2, t));
+      }
+    return block_sum_lane0((threadIdx.x & 31u) == 0 ? double(hi) + double(lo) : 0.0);
+  }
+
   template <typename T>
   __global__ void __launch_bounds__(RED_THREADS)
   k_dot(size_t n, const T *__restrict__ x, const T *__restrict__ y,
@@ -208,7 +272,7 @@ namespace mfgpu
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       s.add(x[i], y[i]);
-    finish_partials(block_sum(s.value()), partial, ticket, out);
+    finish_partials(block_sum_acc(s), partial, ticket, out);
   }
 
   // CG update x += alpha p, r -= alpha q with alpha = num/den, and |r|^2
@@ -219,7 +283,7 @@ namespace mfgpu
                  const T *__restrict__ q, double *__restrict__ partial, unsigned *ticket,
                  double *__restrict__ out)
   {
-    const T    alpha = T(*num / *den);
+    const T    alpha = T(block_ratio(num, den));
     ProdAcc<T> s;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
@@ -229,7 +293,7 @@ namespace mfgpu
         r[i]       = rr;
         s.add(rr, rr);
       }
-    finish_partials(block_sum(s.value()), partial, ticket, out);
+    finish_partials(block_sum_acc(s), partial, ticket, out);
   }
 
   // Jacobi-preconditioned CG step: x += alpha p, r -= alpha q (alpha =
@@ -242,7 +306,7 @@ namespace mfgpu
                      double *__restrict__ partial, unsigned *ticket, double *__restrict__ out_rr,
                      double *__restrict__ out_rz)
   {
-    const T    alpha = T(*num / *den);
+    const T    alpha = T(block_ratio(num, den));
     ProdAcc<T> srr, srz;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
@@ -255,9 +319,9 @@ namespace mfgpu
         srr.add(rr, rr);
         srz.add(rr, zz);
       }
-    const double a = block_sum(srr.value());
-    __syncthreads(); // block_sum's shared scratch is reused
-    const double b = block_sum(srz.value());
+    const double a = block_sum_acc(srr);
+    __syncthreads(); // the block sum's shared scratch is reused
+    const double b = block_sum_acc(srz);
     finish_partials2(a, b, partial, ticket, out_rr, out_rz);
   }
 
@@ -270,7 +334,7 @@ namespace mfgpu
                      const T *__restrict__ z, T *__restrict__ p, T *__restrict__ q_zero,
                      double *__restrict__ rec, int *__restrict__ counter)
   {
-    const T beta = T(s[rzn] / s[rz]);
+    const T beta = T(block_ratio(s + rzn, s + rz));
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       {
@@ -294,7 +358,7 @@ namespace mfgpu
                  const double *__restrict__ den, const T *__restrict__ z,
                  T *__restrict__ p)
   {
-    const T beta = T(*num / *den);
+    const T beta = T(block_ratio(num, den));
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       p[i] = z[i] + beta * p[i];
@@ -356,53 +420,124 @@ namespace mfgpu
   // op: 0 dst = src, 1 dst += src, 2 dst = 0, 3 dst = 1
   // ---------------------------------------------------------------------
   // ---------------------------------------------------------------------
-  // Dense row-major n x n operators (small coarse levels): one warp per row
+  // Dense row-major n x n operators (small coarse levels, n <= 4096), rows
+  // ld apart with ld a multiple of 4 (every row starts on a 16-byte
+  // boundary; columns n..ld-1 hold zeros).  TPR threads per row (a power of
+  // two from 32 to 256, chosen so that the grid covers the GPU) in blocks of
+  // DENSE_THREADS.  Each block stages x, zero-padded to ld, in shared
+  // memory; rows and x are read in 16-byte vectors, which keeps several
+  // loads in flight per thread where one element per lane and step left the
+  // warps waiting on L2.  The partial sums of a row are added in a fixed
+  // order, so results do not vary from run to run.
   // ---------------------------------------------------------------------
+  constexpr int DENSE_THREADS = 512;
+
   template <typename T>
-  __device__ __forceinline__ T
-  dense_row_dot(size_t n, const T *__restrict__ row, const T *__restrict__ x, int lane)
+  struct Vec16;
+  template <>
+  struct Vec16<float>
   {
-    T s = T(0);
-    for (size_t j = size_t(lane); j < n; j += 32)
-      s = fma(row[j], x[j], s);
+    using V                 = float4;
+    static constexpr int W = 4;
+  };
+  template <>
+  struct Vec16<double>
+  {
+    using V                 = double2;
+    static constexpr int W = 2;
+  };
+
+  // row r . x, valid in the row's first thread (t == 0); every thread of
+  // the block calls it (it synchronises the block when TPR > 32)
+  template <typename T, int TPR>
+  __device__ __forceinline__ T
+  dense_row_dot(int n, int ld, int r, const T *__restrict__ A, const T *xs, int t, T *red)
+  {
+    using V         = typename Vec16<T>::V;
+    constexpr int W = Vec16<T>::W;
+    T             s0 = T(0), s1 = T(0);
+    if (r < n)
+      {
+        const V  *rv = reinterpret_cast<const V *>(A + size_t(r) * size_t(ld));
+        const V  *xv = reinterpret_cast<const V *>(xs);
+        const int ng = ld / W;
+#pragma unroll 4
+        for (int g = t; g < ng; g += TPR)
+          {
+            const V a = __ldg(rv + g);
+            const V x = xv[g];
+            s0        = fma(a.x, x.x, s0);
+            s1        = fma(a.y, x.y, s1);
+            if constexpr (W == 4)
+              {
+                s0 = fma(a.z, x.z, s0);
+                s1 = fma(a.w, x.w, s1);
+              }
+          }
+      }
+    T s = s0 + s1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
-      s += __shfl_down_sync(0xffffffffu, s, o);
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    if constexpr (TPR > 32)
+      {
+        const int w = int(threadIdx.x) / 32;
+        if ((threadIdx.x & 31u) == 0)
+          red[w] = s;
+        __syncthreads();
+        if (t == 0)
+#pragma unroll
+          for (int k = 1; k < TPR / 32; ++k)
+            s += red[w + k];
+      }
     return s;
   }
 
-  // y = A x (add: y += A x)
   template <typename T>
-  __global__ void
-  k_dense_mv(size_t n, const T *__restrict__ A, const T *__restrict__ x, T *__restrict__ y, int add)
+  __device__ __forceinline__ void
+  dense_stage_x(int n, int ld, const T *__restrict__ x, T *xs)
   {
-    const size_t row  = (blockIdx.x * size_t(blockDim.x) + threadIdx.x) / 32;
-    const int    lane = int(threadIdx.x & 31u);
-    if (row >= n) // whole warps leave together
-      return;
-    const T s = dense_row_dot(n, A + row * n, x, lane);
-    if (lane == 0)
-      y[row] = add ? y[row] + s : s;
+    for (int j = int(threadIdx.x); j < ld; j += DENSE_THREADS)
+      xs[j] = j < n ? x[j] : T(0);
+    __syncthreads();
+  }
+
+  // y = A x (add: y += A x); dynamic shared memory ld * sizeof(T)
+  template <typename T, int TPR>
+  __global__ void __launch_bounds__(DENSE_THREADS)
+  k_dense_mv(int n, int ld, const T *__restrict__ A, const T *__restrict__ x, T *__restrict__ y, int add)
+  {
+    extern __shared__ __align__(16) unsigned char dense_smem[];
+    __shared__ T red[DENSE_THREADS / 32];
+    T           *xs = reinterpret_cast<T *>(dense_smem);
+    dense_stage_x<T>(n, ld, x, xs);
+    const int r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
+    const int t = int(threadIdx.x) % TPR;
+    const T   s = dense_row_dot<T, TPR>(n, ld, r, A, xs, t, red);
+    if (r < n && t == 0)
+      y[r] = add ? y[r] + s : s;
   }
 
   // one Chebyshev step with the dense operator (k_cheby_update with
   // Ax = A x computed in place): xo <- the new iterate; x keeps the
   // current one (the caller swaps the two)
-  template <typename T>
-  __global__ void
-  k_cheby_dense(size_t n, const T *__restrict__ A, T f1, T f2, int first, const T *__restrict__ b,
+  template <typename T, int TPR>
+  __global__ void __launch_bounds__(DENSE_THREADS)
+  k_cheby_dense(int n, int ld, const T *__restrict__ A, T f1, T f2, int first, const T *__restrict__ b,
                 const T *__restrict__ dinv, const T *__restrict__ x, T *__restrict__ xo)
   {
-    const size_t i    = (blockIdx.x * size_t(blockDim.x) + threadIdx.x) / 32;
-    const int    lane = int(threadIdx.x & 31u);
-    if (i >= n)
-      return;
-    const T s = dense_row_dot(n, A + i * n, x, lane);
-    if (lane == 0)
+    extern __shared__ __align__(16) unsigned char dense_smem[];
+    __shared__ T red[DENSE_THREADS / 32];
+    T           *xs = reinterpret_cast<T *>(dense_smem);
+    dense_stage_x<T>(n, ld, x, xs);
+    const int r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
+    const int t = int(threadIdx.x) % TPR;
+    const T   s = dense_row_dot<T, TPR>(n, ld, r, A, xs, t, red);
+    if (r < n && t == 0)
       {
-        const T t  = dinv[i] * (b[i] - s);
-        const T xi = x[i];
-        xo[i]      = first ? (T(1) + f1) * xi + f2 * t : xi + f1 * (xi - xo[i]) + f2 * t;
+        const T tt = dinv[r] * (b[r] - s);
+        const T xi = xs[r];
+        xo[r]      = first ? (T(1) + f1) * xi + f2 * tt : xi + f1 * (xi - xo[r]) + f2 * tt;
       }
   }
 
@@ -412,6 +547,7 @@ namespace mfgpu
     size_t   n_nodes;
     unsigned face_mask[6];
     int      nc;
+    size_t   ld; // op 4: row stride of the dense matrix
   };
 
   template <typename T>
@@ -457,7 +593,7 @@ namespace mfgpu
             else if (op == 3)
               dst[i] = T(1);
             else // dense matrix: unit diagonal entry of row i
-              dst[i * (size_t(fi.nc) * fi.n_nodes + 1)] = T(1);
+              dst[i * fi.ld + i] = T(1);
           }
       }
   }
@@ -516,8 +652,8 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // Boundary traction (mf_elasticity.h:1849-1897): for each cell face on
   // the traction boundary, t0 = t |det F F^{-T} N| at the face Gauss points,
-  // integrated against the face shape functions.  One block per face,
-  // one thread per face quadrature point / face node.
+  // integrated against the face shape functions.  One block per boundary
+  // cell face.
   // ---------------------------------------------------------------------
   struct TractionArgs
   {
@@ -606,90 +742,102 @@ namespace mfgpu
       }
   }
 
-  static __global__ void
+  // 3D: one block per face cell.  The cell's values are staged in shared
+  // memory; along the face normal only two quantities matter, the values on
+  // the face nodes (for the tangential derivatives) and the normal
+  // derivative at the face (Ge, one contraction over the normal index), so
+  // the deformation gradient at a face Gauss point is a tensor-product
+  // interpolation of those two face arrays.
+  static __global__ void __launch_bounds__(128)
   k_traction(const __grid_constant__ TractionArgs A, const double *__restrict__ u,
              double *__restrict__ rhs)
   {
+    __shared__ double uc[3][MAX_N * MAX_N * MAX_N]; // cell values [c][k][j][i]
+    __shared__ double uf[3][MAX_N * MAX_N];          // face-node values [c][i2][i1]
+    __shared__ double un[3][MAX_N * MAX_N];          // face-node normal derivatives
+    __shared__ double Fs[9][MAX_N * MAX_N];          // grad u at the face points [c*3+d][q]
     __shared__ double tq[3][MAX_N * MAX_N];
     const int nd = A.face / 2, side = A.face % 2;
     const int d1 = nd == 0 ? 1 : 0, d2 = nd == 2 ? 1 : 2;
-    const int N  = A.N;
+    const int N = A.N, N2 = N * N, N3 = N2 * N;
     // face cell (c1, c2) in the tangential directions
     const int c1 = blockIdx.x % A.C[d1], c2 = blockIdx.x / A.C[d1];
     int       cc[3];
     cc[nd] = side ? A.C[nd] - 1 : 0;
     cc[d1] = c1;
     cc[d2] = c2;
-    const int ln = side ? N - 1 : 0; // local index of the face in nd
-    for (int t = threadIdx.x; t < N * N; t += blockDim.x)
+    const int    ln  = side ? N - 1 : 0; // local index of the face in nd
+    const size_t Nx  = size_t(A.Nn[0]), Nxy = size_t(A.Nn[0]) * size_t(A.Nn[1]);
+    const size_t org = size_t(cc[0] * A.p) + Nx * size_t(cc[1] * A.p) + Nxy * size_t(cc[2] * A.p);
+    for (int t = threadIdx.x; t < 3 * N3; t += blockDim.x)
+      {
+        const int c = t / N3, l = t - c * N3;
+        const int i = l % N, j = (l / N) % N, k = l / N2;
+        uc[c][l] = u[size_t(c) * A.n_nodes + org + size_t(i) + Nx * size_t(j) + Nxy * size_t(k)];
+      }
+    __syncthreads();
+    int str[3];
+    str[0] = 1;
+    str[1] = N;
+    str[2] = N2;
+    for (int t = threadIdx.x; t < 3 * N2; t += blockDim.x)
+      {
+        const int c = t / N2, l = t - c * N2;
+        const int off = (l % N) * str[d1] + (l / N) * str[d2];
+        double    s   = 0;
+        for (int k = 0; k < N; ++k)
+          s += A.Ge[side][k] * uc[c][off + k * str[nd]];
+        un[c][l] = s;
+        uf[c][l] = uc[c][off + ln * str[nd]];
+      }
+    __syncthreads();
+    // grad u of component c at face point (q1, q2)
+    for (int t = threadIdx.x; t < 3 * N2; t += blockDim.x)
+      {
+        const int c = t / N2, qq = t - c * N2, q1 = qq % N, q2 = qq / N;
+        double    gn = 0, g1 = 0, g2 = 0;
+        for (int i2 = 0; i2 < N; ++i2)
+          {
+            const double s2 = A.S[q2 * N + i2], e2 = A.G[q2 * N + i2];
+            double       rn = 0, r1 = 0, r2 = 0;
+            for (int i1 = 0; i1 < N; ++i1)
+              {
+                const double v = uf[c][i1 + N * i2];
+                rn += A.S[q1 * N + i1] * un[c][i1 + N * i2];
+                r1 += A.G[q1 * N + i1] * v;
+                r2 += A.S[q1 * N + i1] * v;
+              }
+            gn += s2 * rn;
+            g1 += s2 * r1;
+            g2 += e2 * r2;
+          }
+        Fs[c * 3 + nd][qq] = gn / A.h[nd];
+        Fs[c * 3 + d1][qq] = g1 / A.h[d1];
+        Fs[c * 3 + d2][qq] = g2 / A.h[d2];
+      }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N2; t += blockDim.x)
       {
         const int q1 = t % N, q2 = t / N;
-        double    F[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        for (int k = 0; k < N; ++k)
-          for (int j = 0; j < N; ++j)
-            for (int i = 0; i < N; ++i)
-              {
-                int li[3] = {i, j, k};
-                // basis factors per direction: value and derivative
-                double vv[3], dd[3];
-                for (int d = 0; d < 3; ++d)
-                  {
-                    if (d == nd)
-                      {
-                        vv[d] = li[d] == ln ? 1.0 : 0.0;
-                        dd[d] = A.Ge[side][li[d]];
-                      }
-                    else
-                      {
-                        const int q = d == d1 ? q1 : q2;
-                        vv[d]       = A.S[q * N + li[d]];
-                        dd[d]       = A.G[q * N + li[d]];
-                      }
-                  }
-                const double g0 = dd[0] * vv[1] * vv[2] / A.h[0];
-                const double g1 = vv[0] * dd[1] * vv[2] / A.h[1];
-                const double g2 = vv[0] * vv[1] * dd[2] / A.h[2];
-                const size_t node = size_t(cc[0] * A.p + i) +
-                                    size_t(A.Nn[0]) * (size_t(cc[1] * A.p + j) + size_t(A.Nn[1]) * (cc[2] * A.p + k));
-                for (int c = 0; c < 3; ++c)
-                  {
-                    const double uv = u[size_t(c) * A.n_nodes + node];
-                    F[c][0] += g0 * uv;
-                    F[c][1] += g1 * uv;
-                    F[c][2] += g2 * uv;
-                  }
-              }
-        for (int d = 0; d < 3; ++d)
-          F[d][d] += 1.0;
-        const double J = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) -
-                         F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
-                         F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
-        // n* = J F^{-T} N = cofactor(F) N ; cofactor row nd
-        double cof[3][3];
-        cof[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
-        cof[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
-        cof[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
-        cof[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
-        cof[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
-        cof[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
-        cof[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
-        cof[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
-        cof[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
-        (void)J;
-        const double sgn = side ? 1.0 : -1.0;
-        double       ns  = 0;
+        double    F[3][3];
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d)
+            F[c][d] = Fs[c * 3 + d][t] + (c == d ? 1.0 : 0.0);
+        // n* = J F^{-T} N = cofactor(F) N: column nd of the cofactor matrix
+        double cof[3];
+        const int a1 = (nd + 1) % 3, a2 = (nd + 2) % 3;
         for (int i = 0; i < 3; ++i)
           {
-            const double v = cof[i][nd] * sgn; // (J F^{-T})_{i nd} = cof(F)_{i nd}
-            ns += v * v;
+            const int b1 = (i + 1) % 3, b2 = (i + 2) % 3;
+            cof[i] = F[b1][a1] * F[b2][a2] - F[b1][a2] * F[b2][a1];
           }
-        ns              = sqrt(ns);
+        const double ns = sqrt(cof[0] * cof[0] + cof[1] * cof[1] + cof[2] * cof[2]);
         const double jw = A.w[q1] * A.h[d1] * A.w[q2] * A.h[d2];
         for (int c = 0; c < 3; ++c)
           tq[c][t] = A.t[c] * ns * jw;
       }
     __syncthreads();
-    for (int t = threadIdx.x; t < N * N; t += blockDim.x)
+    for (int t = threadIdx.x; t < N2; t += blockDim.x)
       {
         const int i1 = t % N, i2 = t / N;
         int       li[3];
@@ -704,8 +852,7 @@ namespace mfgpu
               for (int c = 0; c < 3; ++c)
                 r[c] += phi * tq[c][q1 + q2 * N];
             }
-        const size_t node = size_t(cc[0] * A.p + li[0]) +
-                            size_t(A.Nn[0]) * (size_t(cc[1] * A.p + li[1]) + size_t(A.Nn[1]) * (cc[2] * A.p + li[2]));
+        const size_t node = org + size_t(li[0]) + Nx * size_t(li[1]) + Nxy * size_t(li[2]);
         for (int c = 0; c < 3; ++c)
           atomicAdd(rhs + size_t(c) * A.n_nodes + node, r[c]);
       }

@@ -570,6 +570,32 @@ def test_dense_copy_matches_matrix_free(ctx, degree, kind, precision, df64, cach
     op.close()
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("rep", [(1, 1, 1), (2, 1, 1), (3, 1, 1)])
+def test_dense_copy_row_splits(ctx, precision, rep):
+    """Dense copies of 1029, 1911 and 2793 rows (Q6 cantilevers of one to
+    three cells) run the dense kernels with 256, 128 and 64 threads per row
+    and rows that start off the 16-byte boundary; each multiplies like the
+    matrix-free operator."""
+    dt = np.float64 if precision == 64 else np.float32
+    tol = 1e-13 if precision == 64 else 2e-6
+    spec = W.cantilever(6, 0, rep=rep, length=(float(rep[0]), 1.0, 1.0))
+    n = W.n_dofs(spec, 3)
+    u1 = W.smooth_displacement(6, 0, spec["rep"], spec["lo"], spec["hi"], seed=2)
+    op = mfgpu.NeoHookOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, precision, "referential_qp")
+    op.set_material(mfgpu.material(0.5e6, 0.4, 1000.0, 0.01))
+    d_u = dev(u1.astype(dt))
+    op.initialize(d_u)
+    op.cache()
+    x = dev(W.uniform_vector(n, 5, dt))
+    mf_x, dn_x = dev(np.zeros(n, dt)), dev(np.zeros(n, dt))
+    op.vmult(mf_x, x)
+    op.set_dense(True)
+    op.vmult(dn_x, x)
+    assert rel(host(dn_x).astype(np.float64), host(mf_x).astype(np.float64)) < tol
+    op.close()
+
+
 def test_dense_copy_rejects_large_operators(ctx):
     spec = W.unit_cube_heat(4, 2)
     op = mfgpu.LaplaceOperator(ctx, W.to_lib_mesh(mfgpu, spec), -1, 64, True, delta_t=0.1)
