@@ -17,6 +17,7 @@ own roofline and e2e figures.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--arith native|df64] [--caching referential_qp|...]
     python bench.py --kernel-case NAME --steps K   # one operator, for ncu
+    python bench.py --solver-case NAME             # one solver workload, for ncu launch lists
 """
 import argparse
 import json
@@ -51,6 +52,9 @@ def parse():
     p.add_argument("--kernel-case", default=None, choices=sorted(KERNEL_CASES),
                    help="apply one operator `--steps` times on its workload and exit (the cases the "
                         "ncu summaries under profiles/ were taken on)")
+    p.add_argument("--solver-case", default=None, choices=sorted(SOLVER_CASES),
+                   help="run one solver workload twice, the second between cudaProfilerStart and "
+                        "cudaProfilerStop (ncu --profile-from-start off), and exit")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -954,6 +958,62 @@ KERNEL_CASES = {
 }
 
 
+SOLVER_CASES = {
+    # the first Newton-Newmark step of the 64x8x8-cell Q4 cantilever (839,619 DoFs)
+    "solid_step_64x8x8_q4": "solid",
+    # the first Newton system of the 128x16x16-cell Q3 cantilever (2,773,155 DoFs) to 1e-8,
+    # FP32 V-cycle, native FP64 fine and coarse operators
+    "mixed_solve_q3": "mixed",
+}
+
+
+def run_solver_case(args):
+    """One solver workload, run twice; the second run is the profiled one."""
+    import torch
+    import build as pkg_build
+    import mfgpu
+    import workloads as W
+    pkg_build.build()
+    dev = torch.device("cuda", 0)
+    ctx = mfgpu.Context(0)
+    kind = SOLVER_CASES[args.solver_case]
+
+    def once():
+        if kind == "solid":
+            s = mfgpu.Solid(ctx, _config1_solid_params(mfgpu, W, 1))
+            r = s.run()
+            s.close()
+            return {"seconds": r.seconds, "newton_its": list(r.newton_its[:1]), "cg_iterations": r.total_cg}
+        spec = W.cantilever(3, 4)
+        n = W.n_dofs(spec, 3)
+        p = mfgpu.SolidParams()
+        p.mesh = W.to_lib_mesh(mfgpu, spec)
+        p.material = mfgpu.material(0.5e6, 0.4, 1000.0, 0.01)
+        p.caching = b"referential_qp"
+        p.solver = mfgpu.solver_params("gmg", tol=1e-8, mg_precision=32, coarse_fp64=True)
+        p.dt, p.n_steps, p.max_newton = 0.01, 1, 10
+        p.traction_id = W.TRACTION_ID
+        p.traction[:] = [0.0, -100.0, 0.0]
+        s = mfgpu.Solid(ctx, p)
+        zero = torch.zeros(n, dtype=torch.float64, device=dev)
+        rhs = torch.zeros_like(zero)
+        du = torch.zeros_like(zero)
+        s.residual(zero, zero, rhs)
+        its, secs = s.linear_solve(zero, rhs, du)
+        s.close()
+        return {"seconds": secs, "cg_iterations": its}
+
+    once()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    out = once()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({"solver_case": args.solver_case, **out}))
+    ctx.close()
+    return 0
+
+
 def run_kernel_case(args):
     """One operator applied `--steps` times on its workload (for ncu)."""
     import torch
@@ -1064,6 +1124,8 @@ def main():
         return run_reference(args)
     if args.kernel_case:
         return run_kernel_case(args)
+    if args.solver_case:
+        return run_solver_case(args)
     rank, world, local = dist_info()
     import torch
     import build as pkg_build

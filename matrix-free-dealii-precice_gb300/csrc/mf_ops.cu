@@ -356,13 +356,19 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // vector kernels
   // ---------------------------------------------------------------------
-  // blocks of a single-launch reduction over n entries: at least 8 entries
-  // per thread, at most RED_BLOCKS (the partials buffer); fixed per n, so a
-  // reduction over the same vector is reproducible
+  // blocks of a single-launch reduction over n entries of type T, at most
+  // RED_BLOCKS (the partials buffer); fixed per n, so a reduction over the
+  // same vector is reproducible.  Each further entry a thread walks to
+  // costs it a memory latency, and each block's FP64 reduction costs FP64
+  // instructions per warp: float vectors take about 2 entries per thread
+  // (their warp sums run on the FP32 pipe), double vectors 8 (measured:
+  // FP32 CG kernels of 2.5k-840k entries faster with 2, the FP64 ones of
+  // 840k slower)
+  template <typename T>
   static inline unsigned
   red_grid(size_t n)
   {
-    const size_t per = size_t(RED_THREADS) * 8;
+    const size_t per = size_t(RED_THREADS) * (sizeof(T) == 4 ? 2 : 8);
     return unsigned(std::max<size_t>(1, std::min<size_t>(RED_BLOCKS, (n + per - 1) / per)));
   }
 
@@ -442,7 +448,7 @@ namespace mfgpu
   void
   vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot)
   {
-    k_dot<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
+    k_dot<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
                                                     c.ticket.as<unsigned>(), scalar_slots(c) + slot);
     count_launch();
     MF_CK(cudaGetLastError());
@@ -463,7 +469,7 @@ namespace mfgpu
             T *r, const T *q, int rr_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update_rr<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+    k_cg_update_rr<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
                                                              c.partial.as<double>(),
                                                              c.ticket.as<unsigned>(), s + rr_slot);
     count_launch();
@@ -475,7 +481,7 @@ namespace mfgpu
                    const T *dinv, T *z, int rr_slot, int rz_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update_jacobi<<<red_grid(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+    k_cg_update_jacobi<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
                                                                  dinv, z, c.partial.as<double>(),
                                                                  c.ticket.as<unsigned>(), s + rr_slot,
                                                                  s + rz_slot);
@@ -577,7 +583,7 @@ namespace mfgpu
       throw Error(ERR_ARG, "dense operator larger than 4096 rows");
     const int      tpr  = dense_tpr(n);
     const unsigned grid = unsigned((n * size_t(tpr) + DENSE_THREADS - 1) / DENSE_THREADS);
-    const size_t   smem = dense_row_stride(n) * sizeof(T);
+    const size_t   smem = 0;
     switch (tpr)
       {
         case 32:

@@ -8,7 +8,7 @@
 
 namespace mfgpu
 {
-  constexpr int RED_BLOCKS  = 608; // 4 x 152 SMs
+  constexpr int RED_BLOCKS  = 1216; // 8 x 152 SMs: 2048 threads on every SM
   constexpr int RED_THREADS = 256;
 
   template <typename T>
@@ -269,6 +269,7 @@ namespace mfgpu
         double *__restrict__ partial, unsigned *ticket, double *__restrict__ out)
   {
     ProdAcc<T> s;
+#pragma unroll 4
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       s.add(x[i], y[i]);
@@ -285,6 +286,7 @@ namespace mfgpu
   {
     const T    alpha = T(block_ratio(num, den));
     ProdAcc<T> s;
+#pragma unroll 4
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       {
@@ -308,6 +310,7 @@ namespace mfgpu
   {
     const T    alpha = T(block_ratio(num, den));
     ProdAcc<T> srr, srz;
+#pragma unroll 4
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x)
       {
@@ -424,11 +427,13 @@ namespace mfgpu
   // ld apart with ld a multiple of 4 (every row starts on a 16-byte
   // boundary; columns n..ld-1 hold zeros).  TPR threads per row (a power of
   // two from 32 to 256, chosen so that the grid covers the GPU) in blocks of
-  // DENSE_THREADS.  Each block stages x, zero-padded to ld, in shared
-  // memory; rows and x are read in 16-byte vectors, which keeps several
-  // loads in flight per thread where one element per lane and step left the
-  // warps waiting on L2.  The partial sums of a row are added in a fixed
-  // order, so results do not vary from run to run.
+  // DENSE_THREADS.  Rows and x are read in 16-byte vectors (x in scalars
+  // when it is not 16-byte aligned), several per thread in flight, where
+  // one element per lane and step left the warps waiting on L2.  The
+  // partial sums of a row are added in a fixed order, so results do not
+  // vary from run to run.  (Staging x in shared memory first, or keeping
+  // only each row's window of nonzero columns, measured slower: a step is
+  // bound by latency, about 4 us per launch in a graph, not by the bytes.)
   // ---------------------------------------------------------------------
   constexpr int DENSE_THREADS = 512;
 
@@ -447,33 +452,59 @@ namespace mfgpu
     static constexpr int W = 2;
   };
 
+  template <typename T, int W>
+  __device__ __forceinline__ void
+  dense_fma(const typename Vec16<T>::V &a, const T *x, T &s0, T &s1)
+  {
+    s0 = fma(a.x, x[0], s0);
+    s1 = fma(a.y, x[1], s1);
+    if constexpr (W == 4)
+      {
+        s0 = fma(a.z, x[2], s0);
+        s1 = fma(a.w, x[3], s1);
+      }
+  }
+
   // row r . x, valid in the row's first thread (t == 0); every thread of
   // the block calls it (it synchronises the block when TPR > 32)
   template <typename T, int TPR>
   __device__ __forceinline__ T
-  dense_row_dot(int n, int ld, int r, const T *__restrict__ A, const T *xs, int t, T *red)
+  dense_row_dot(int n, int ld, int r, const T *__restrict__ A, const T *__restrict__ x, int t, T *red)
   {
     using V         = typename Vec16<T>::V;
     constexpr int W = Vec16<T>::W;
     T             s0 = T(0), s1 = T(0);
     if (r < n)
       {
-        const V  *rv = reinterpret_cast<const V *>(A + size_t(r) * size_t(ld));
-        const V  *xv = reinterpret_cast<const V *>(xs);
-        const int ng = ld / W;
-#pragma unroll 4
-        for (int g = t; g < ng; g += TPR)
+        const T  *row  = A + size_t(r) * size_t(ld);
+        const V  *rv   = reinterpret_cast<const V *>(row);
+        const int full = n / W; // vectors whose W entries of x all exist
+        if ((reinterpret_cast<uintptr_t>(x) & 15u) == 0u)
           {
-            const V a = __ldg(rv + g);
-            const V x = xv[g];
-            s0        = fma(a.x, x.x, s0);
-            s1        = fma(a.y, x.y, s1);
-            if constexpr (W == 4)
+            const V *xv = reinterpret_cast<const V *>(x);
+#pragma unroll 4
+            for (int g = t; g < full; g += TPR)
               {
-                s0 = fma(a.z, x.z, s0);
-                s1 = fma(a.w, x.w, s1);
+                const V a  = __ldg(rv + g);
+                const V xx = __ldg(xv + g);
+                dense_fma<T, W>(a, reinterpret_cast<const T *>(&xx), s0, s1);
               }
           }
+        else
+          {
+#pragma unroll 4
+            for (int g = t; g < full; g += TPR)
+              {
+                const V a = __ldg(rv + g);
+                T       xx[W];
+#pragma unroll
+                for (int k = 0; k < W; ++k)
+                  xx[k] = __ldg(x + g * W + k);
+                dense_fma<T, W>(a, xx, s0, s1);
+              }
+          }
+        for (int j = full * W + t; j < n; j += TPR)
+          s0 = fma(__ldg(row + j), __ldg(x + j), s0);
       }
     T s = s0 + s1;
 #pragma unroll
@@ -493,27 +524,15 @@ namespace mfgpu
     return s;
   }
 
-  template <typename T>
-  __device__ __forceinline__ void
-  dense_stage_x(int n, int ld, const T *__restrict__ x, T *xs)
-  {
-    for (int j = int(threadIdx.x); j < ld; j += DENSE_THREADS)
-      xs[j] = j < n ? x[j] : T(0);
-    __syncthreads();
-  }
-
-  // y = A x (add: y += A x); dynamic shared memory ld * sizeof(T)
+  // y = A x (add: y += A x)
   template <typename T, int TPR>
   __global__ void __launch_bounds__(DENSE_THREADS)
   k_dense_mv(int n, int ld, const T *__restrict__ A, const T *__restrict__ x, T *__restrict__ y, int add)
   {
-    extern __shared__ __align__(16) unsigned char dense_smem[];
     __shared__ T red[DENSE_THREADS / 32];
-    T           *xs = reinterpret_cast<T *>(dense_smem);
-    dense_stage_x<T>(n, ld, x, xs);
-    const int r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
-    const int t = int(threadIdx.x) % TPR;
-    const T   s = dense_row_dot<T, TPR>(n, ld, r, A, xs, t, red);
+    const int    r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
+    const int    t = int(threadIdx.x) % TPR;
+    const T      s = dense_row_dot<T, TPR>(n, ld, r, A, x, t, red);
     if (r < n && t == 0)
       y[r] = add ? y[r] + s : s;
   }
@@ -526,17 +545,14 @@ namespace mfgpu
   k_cheby_dense(int n, int ld, const T *__restrict__ A, T f1, T f2, int first, const T *__restrict__ b,
                 const T *__restrict__ dinv, const T *__restrict__ x, T *__restrict__ xo)
   {
-    extern __shared__ __align__(16) unsigned char dense_smem[];
     __shared__ T red[DENSE_THREADS / 32];
-    T           *xs = reinterpret_cast<T *>(dense_smem);
-    dense_stage_x<T>(n, ld, x, xs);
-    const int r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
-    const int t = int(threadIdx.x) % TPR;
-    const T   s = dense_row_dot<T, TPR>(n, ld, r, A, xs, t, red);
+    const int    r = int(blockIdx.x) * (DENSE_THREADS / TPR) + int(threadIdx.x) / TPR;
+    const int    t = int(threadIdx.x) % TPR;
+    const T      s = dense_row_dot<T, TPR>(n, ld, r, A, x, t, red);
     if (r < n && t == 0)
       {
         const T tt = dinv[r] * (b[r] - s);
-        const T xi = xs[r];
+        const T xi = x[r];
         xo[r]      = first ? (T(1) + f1) * xi + f2 * tt : xi + f1 * (xi - xo[r]) + f2 * tt;
       }
   }
