@@ -356,19 +356,28 @@ namespace mfgpu
   // ---------------------------------------------------------------------
   // vector kernels
   // ---------------------------------------------------------------------
+  static inline unsigned
+  red_threads(size_t n)
+  {
+    return n <= size_t(RED_SHORT) ? unsigned(RED_SHORT_THREADS) : unsigned(RED_THREADS);
+  }
+
   // blocks of a single-launch reduction over n entries of type T, at most
   // RED_BLOCKS (the partials buffer); fixed per n, so a reduction over the
   // same vector is reproducible.  Each further entry a thread walks to
-  // costs it a memory latency, and each block's FP64 reduction costs FP64
-  // instructions per warp: float vectors take about 2 entries per thread
-  // (their warp sums run on the FP32 pipe), double vectors 8 (measured:
-  // FP32 CG kernels of 2.5k-840k entries faster with 2, the FP64 ones of
-  // 840k slower)
+  // costs it a memory latency, and each block's sums cost FP64
+  // instructions: float vectors up to 256k entries take about 2 entries per
+  // thread, longer float vectors and double vectors 8 (measured on the
+  // estimate CG of 14k / 105k / 840k float entries: update 7.5 / 8.4 /
+  // 16.4 us with 2, 10.4 / 10.5 / 14.3 us with 8; FP64 840k slower with 2).
+  // Vectors of at most RED_SHORT entries take one block of RED_SHORT_THREADS.
   template <typename T>
   static inline unsigned
   red_grid(size_t n)
   {
-    const size_t per = size_t(RED_THREADS) * (sizeof(T) == 4 ? 2 : 8);
+    if (n <= size_t(RED_SHORT))
+      return 1u;
+    const size_t per = size_t(RED_THREADS) * (sizeof(T) == 4 && n <= (size_t(1) << 18) ? 2 : 8);
     return unsigned(std::max<size_t>(1, std::min<size_t>(RED_BLOCKS, (n + per - 1) / per)));
   }
 
@@ -448,7 +457,7 @@ namespace mfgpu
   void
   vec_dot_dev(Context &c, size_t n, const T *x, const T *y, int slot)
   {
-    k_dot<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, x, y, c.partial.as<double>(),
+    k_dot<<<red_grid<T>(n), red_threads(n), 0, c.stream>>>(n, x, y, c.partial.as<double>(),
                                                     c.ticket.as<unsigned>(), scalar_slots(c) + slot);
     count_launch();
     MF_CK(cudaGetLastError());
@@ -469,7 +478,7 @@ namespace mfgpu
             T *r, const T *q, int rr_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update_rr<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+    k_cg_update_rr<<<red_grid<T>(n), red_threads(n), 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
                                                              c.partial.as<double>(),
                                                              c.ticket.as<unsigned>(), s + rr_slot);
     count_launch();
@@ -481,7 +490,7 @@ namespace mfgpu
                    const T *dinv, T *z, int rr_slot, int rz_slot)
   {
     double *s = scalar_slots(c);
-    k_cg_update_jacobi<<<red_grid<T>(n), RED_THREADS, 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
+    k_cg_update_jacobi<<<red_grid<T>(n), red_threads(n), 0, c.stream>>>(n, s + num_slot, s + den_slot, x, p, r, q,
                                                                  dinv, z, c.partial.as<double>(),
                                                                  c.ticket.as<unsigned>(), s + rr_slot,
                                                                  s + rz_slot);

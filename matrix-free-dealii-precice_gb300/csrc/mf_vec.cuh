@@ -9,6 +9,11 @@
 namespace mfgpu
 {
   constexpr int RED_BLOCKS  = 1216; // 8 x 152 SMs: 2048 threads on every SM
+  // vectors of at most RED_SHORT entries reduce in one block of
+  // RED_SHORT_THREADS threads: no partials, ticket and fences, whose latency
+  // chain dominated the reductions of coarse levels (a few thousand entries)
+  constexpr int RED_SHORT         = 4096;
+  constexpr int RED_SHORT_THREADS = 1024;
   constexpr int RED_THREADS = 256;
 
   template <typename T>
@@ -151,6 +156,13 @@ namespace mfgpu
   finish_partials(double s, double *__restrict__ partial, unsigned *ticket,
                   double *__restrict__ out)
   {
+    if (gridDim.x == 1)
+      {
+        // one block (short vectors): its sum is the result
+        if (threadIdx.x == 0)
+          *out = s;
+        return;
+      }
     __shared__ bool last;
     if (threadIdx.x == 0)
       {
@@ -178,6 +190,15 @@ namespace mfgpu
   finish_partials2(double s0, double s1, double *__restrict__ partial, unsigned *ticket,
                    double *__restrict__ out0, double *__restrict__ out1)
   {
+    if (gridDim.x == 1)
+      {
+        if (threadIdx.x == 0)
+          {
+            *out0 = s0;
+            *out1 = s1;
+          }
+        return;
+      }
     __shared__ bool last;
     if (threadIdx.x == 0)
       {
@@ -264,7 +285,7 @@ namespace mfgpu
   }
 
   template <typename T>
-  __global__ void __launch_bounds__(RED_THREADS)
+  __global__ void __launch_bounds__(RED_SHORT_THREADS)
   k_dot(size_t n, const T *__restrict__ x, const T *__restrict__ y,
         double *__restrict__ partial, unsigned *ticket, double *__restrict__ out)
   {
@@ -278,7 +299,7 @@ namespace mfgpu
 
   // CG update x += alpha p, r -= alpha q with alpha = num/den, and |r|^2
   template <typename T>
-  __global__ void __launch_bounds__(RED_THREADS)
+  __global__ void __launch_bounds__(RED_SHORT_THREADS)
   k_cg_update_rr(size_t n, const double *__restrict__ num, const double *__restrict__ den,
                  T *__restrict__ x, const T *__restrict__ p, T *__restrict__ r,
                  const T *__restrict__ q, double *__restrict__ partial, unsigned *ticket,
@@ -301,7 +322,7 @@ namespace mfgpu
   // Jacobi-preconditioned CG step: x += alpha p, r -= alpha q (alpha =
   // num/den), z = dinv r, and |r|^2 -> out_rr, r.z -> out_rz
   template <typename T>
-  __global__ void __launch_bounds__(RED_THREADS)
+  __global__ void __launch_bounds__(RED_SHORT_THREADS)
   k_cg_update_jacobi(size_t n, const double *__restrict__ num, const double *__restrict__ den,
                      T *__restrict__ x, const T *__restrict__ p, T *__restrict__ r,
                      const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z,
