@@ -1,7 +1,9 @@
 """The fast division the cell kernels use for cell coordinates (FastDiv in
 csrc/mf_common.cuh: n / d = (umulhi(n, mul) + n) >> shift with per-level
 multipliers) agrees with integer division for every divisor a level can
-have and dividends below 2^31 (cell counts are checked to stay below it).
+have (cell counts per direction and plane, up to 70000) and for random
+large divisors up to 2^31, with dividends below 2^31 (cell counts are
+checked to stay below it).
 Host code compiled by nvcc and run on the CPU; the device path computes the
 same expression with __umulhi."""
 import os
@@ -41,6 +43,34 @@ int main()
       for (int i = 0; i < 64; ++i)
         {
           const unsigned n = unsigned(next() & 0x7fffffffu);
+          if (f.div(n) != n / d || f.mod(n) != n % d)
+            {
+              std::printf("FAIL d=%u n=%u\n", d, n);
+              return 1;
+            }
+          ++checked;
+        }
+    }
+  // large divisors up to 2^31: random ones and the powers of two and
+  // their neighbours
+  for (int t = 0; t < 20000 + 3 * 31; ++t)
+    {
+      unsigned d;
+      if (t < 20000)
+        d = 1u + unsigned(next() % 0x7fffffffull);
+      else
+        {
+          const int k = (t - 20000) % 31, v = (t - 20000) / 31;
+          d = (1u << k) + (v == 0 ? 0u : (v == 1 ? 1u : (k > 0 ? 0xffffffffu : 0u)));
+          if (d == 0u)
+            continue;
+        }
+      const FastDiv f = make_fastdiv(d);
+      for (int i = 0; i < 16; ++i)
+        {
+          const unsigned n = i == 0 ? 0x7fffffffu : (i == 1 ? d - 1 : (i == 2 && d < 0x7fffffffu ? d : unsigned(next() & 0x7fffffffu)));
+          if (n > 0x7fffffffu)
+            continue;
           if (f.div(n) != n / d || f.mod(n) != n % d)
             {
               std::printf("FAIL d=%u n=%u\n", d, n);
