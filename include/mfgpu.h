@@ -290,7 +290,8 @@ typedef struct mfgpu_solver_params
   int    cuda_graphs;     /* replay the V-cycle as a CUDA graph              */
   int    coarse_dense;    /* level-0 operator (three-dimensional, <= 64 MiB)
                              assembled densely after each setup; the coarse
-                             Chebyshev steps multiply by it, one warp per row */
+                             Chebyshev steps multiply by it, one launch
+                             per step */
   int    estimate_condition; /* "Estimate condition number": before each
                                 linear solve of the solid, unpreconditioned
                                 CG (Lanczos) estimates the condition number

@@ -45,9 +45,10 @@ namespace mfgpu
     void       *dst;
     size_t      cell_begin = 0, cell_end = 0; // cell range; empty = all cells
     bool        colored = false; // all cells by parity colour, plain (non-atomic) scatter
-    // element columns: dst is the dense row-major m x m matrix (m = NC
-    // n_nodes, zeroed by the caller) and receives the operator's entries of
-    // the unconstrained rows and columns; src is not read
+    // element columns: dst is the dense row-major matrix of m = NC n_nodes
+    // rows (row stride unit_ld, zeroed by the caller) and receives the
+    // operator's entries of the unconstrained rows and columns; src is not
+    // read
     bool        unit = false;
     // row stride of that matrix in elements (0: m); padded so that every
     // row starts on a 16-byte boundary
