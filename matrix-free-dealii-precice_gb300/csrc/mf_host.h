@@ -427,6 +427,7 @@ namespace mfgpu
     void restrict_add(void *coarse_v, const void *fine_v);      // coarse += P^T fine
     void interpolate(void *coarse_v, const void *fine_v);       // coarse = I fine
   private:
-    void passes(const Band *B, const LevelGeom &from, const LevelGeom &to, const void *in, void *out);
+    void passes(const Band *B, const LevelGeom &from, const LevelGeom &to, const void *in, void *out,
+                bool constrained = false, bool add = false);
   };
 } // namespace mfgpu

@@ -1592,12 +1592,15 @@ namespace mfgpu
 
   // apply the three 1D passes x, y, z: from grid `from` to grid `to`
   void
-  Transfer::passes(const Band *B, const LevelGeom &from, const LevelGeom &to,
-                   const void *in, void *out)
+  Transfer::passes(const Band *B, const LevelGeom &from, const LevelGeom &to, const void *in, void *out,
+                   bool constrained, bool add)
   {
+    // pass 0: in -> tmp1, pass 1: tmp1 -> tmp0, pass 2: tmp0 -> out (in and
+    // out are the caller's vectors, never tmp0 or tmp1).  constrained: pass 0
+    // reads the constrained entries of `from` as 0 and pass 2 leaves those of
+    // `to` 0 (or, adding, untouched).
     int         ext[3] = {from.Nn[0], from.Nn[1], from.Nn[2]};
     const void *cur    = in;
-    void       *bufs[2] = {tmp1.ptr, out};
     for (int d = 0; d < 3; ++d)
       {
         PassDims pd;
@@ -1610,10 +1613,15 @@ namespace mfgpu
         pd.nc         = nc;
         pd.dir        = d;
         pd.width      = B[d].width;
-        // pass 0 -> tmp1, pass 1 -> tmp0 (in == tmp0 for pass 0 is safe:
-        // tmp0 is only read there), pass 2 -> out
-        void *dst = d == 2 ? out : (d == 0 ? tmp1.ptr : tmp0.ptr);
-        (void)bufs;
+        pd.mask_in    = constrained && d == 0;
+        pd.mask_out   = constrained && d == 2;
+        pd.add        = add && d == 2;
+        for (int f = 0; f < 6; ++f)
+          {
+            pd.face_in[f]  = from.face_mask[f];
+            pd.face_out[f] = to.face_mask[f];
+          }
+        void        *dst   = d == 2 ? out : (d == 0 ? tmp1.ptr : tmp0.ptr);
         const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
         if (precision == 32)
           k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
@@ -1628,126 +1636,26 @@ namespace mfgpu
       }
   }
 
+  // The constrained entries of the input read as zero and those of the
+  // result are zero (added: left as they are), as the reference's transfer
+  // with homogeneous boundary values gives; the first and last tensor
+  // passes apply both masks, so a transfer is three launches.
   void
   Transfer::prolongate(void *fine_v, const void *coarse_v)
   {
-    const size_t es = precision == 32 ? 4 : 8;
-    MF_CK(cudaMemcpyAsync(tmp0.ptr, coarse_v, coarse.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (precision == 32)
-      constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp0.as<float>());
-    else
-      constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp0.as<double>());
-    passes(P, coarse, fine, tmp0.ptr, fine_v);
-    if (precision == 32)
-      constrained_op<float>(*ctx, fine, nc, 2, nullptr, (float *)fine_v);
-    else
-      constrained_op<double>(*ctx, fine, nc, 2, nullptr, (double *)fine_v);
+    passes(P, coarse, fine, coarse_v, fine_v, true, false);
   }
 
   void
   Transfer::prolongate_add(void *fine_v, const void *coarse_v)
   {
-    // result of the passes into tmp0 (last pass writes `out`)
-    const size_t es = precision == 32 ? 4 : 8;
-    DevBuf       &out = tmp0;
-    MF_CK(cudaMemcpyAsync(tmp1.ptr, coarse_v, coarse.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (precision == 32)
-      constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp1.as<float>());
-    else
-      constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp1.as<double>());
-    // passes() uses tmp1 and tmp0 as intermediates: run x into a third area
-    // by going through the fine vector itself is not allowed (we add), so
-    // use a dedicated order: x pass tmp1 -> tmp0, y pass tmp0 -> tmp1,
-    // z pass tmp1 -> tmp0
-    int         ext[3] = {coarse.Nn[0], coarse.Nn[1], coarse.Nn[2]};
-    const void *cur    = tmp1.ptr;
-    void       *seq[3] = {tmp0.ptr, tmp1.ptr, tmp0.ptr};
-    for (int d = 0; d < 3; ++d)
-      {
-        PassDims pd;
-        for (int e = 0; e < 3; ++e)
-          {
-            pd.ext_in[e]  = ext[e];
-            pd.ext_out[e] = ext[e];
-          }
-        pd.ext_out[d] = fine.Nn[d];
-        pd.nc         = nc;
-        pd.dir        = d;
-        pd.width      = P[d].width;
-        const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
-        if (precision == 32)
-          k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
-            pd, P[d].col.as<int>(), P[d].val.as<float>(), (const float *)cur, (float *)seq[d]);
-        else
-          k_transfer_pass<double><<<grid_for(total), 256, 0, ctx->stream>>>(
-            pd, P[d].col.as<int>(), P[d].val.as<double>(), (const double *)cur, (double *)seq[d]);
-        count_launch();
-        MF_CK(cudaGetLastError());
-        cur    = seq[d];
-        ext[d] = fine.Nn[d];
-      }
-    const size_t n = fine.n_nodes * nc;
-    if (precision == 32)
-      {
-        constrained_op<float>(*ctx, fine, nc, 2, nullptr, out.as<float>());
-        vec_axpby<float>(*ctx, n, 1.0f, out.as<float>(), 1.0f, (float *)fine_v);
-      }
-    else
-      {
-        constrained_op<double>(*ctx, fine, nc, 2, nullptr, out.as<double>());
-        vec_axpby<double>(*ctx, n, 1.0, out.as<double>(), 1.0, (double *)fine_v);
-      }
+    passes(P, coarse, fine, coarse_v, fine_v, true, true);
   }
 
   void
   Transfer::restrict_add(void *coarse_v, const void *fine_v)
   {
-    const size_t es = precision == 32 ? 4 : 8;
-    MF_CK(cudaMemcpyAsync(tmp0.ptr, fine_v, fine.n_nodes * nc * es, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (precision == 32)
-      constrained_op<float>(*ctx, fine, nc, 2, nullptr, tmp0.as<float>());
-    else
-      constrained_op<double>(*ctx, fine, nc, 2, nullptr, tmp0.as<double>());
-    // x: tmp0 -> tmp1, y: tmp1 -> tmp0 ... the last pass must not overwrite
-    // the input of the add: write it to tmp1 region after tmp0 use
-    int         ext[3] = {fine.Nn[0], fine.Nn[1], fine.Nn[2]};
-    const void *cur    = tmp0.ptr;
-    void       *seq[3] = {tmp1.ptr, tmp0.ptr, tmp1.ptr};
-    for (int d = 0; d < 3; ++d)
-      {
-        PassDims pd;
-        for (int e = 0; e < 3; ++e)
-          {
-            pd.ext_in[e]  = ext[e];
-            pd.ext_out[e] = ext[e];
-          }
-        pd.ext_out[d] = coarse.Nn[d];
-        pd.nc         = nc;
-        pd.dir        = d;
-        pd.width      = R[d].width;
-        const size_t total = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2] * nc;
-        if (precision == 32)
-          k_transfer_pass<float><<<grid_for(total), 256, 0, ctx->stream>>>(
-            pd, R[d].col.as<int>(), R[d].val.as<float>(), (const float *)cur, (float *)seq[d]);
-        else
-          k_transfer_pass<double><<<grid_for(total), 256, 0, ctx->stream>>>(
-            pd, R[d].col.as<int>(), R[d].val.as<double>(), (const double *)cur, (double *)seq[d]);
-        count_launch();
-        MF_CK(cudaGetLastError());
-        cur    = seq[d];
-        ext[d] = coarse.Nn[d];
-      }
-    const size_t n = coarse.n_nodes * nc;
-    if (precision == 32)
-      {
-        constrained_op<float>(*ctx, coarse, nc, 2, nullptr, tmp1.as<float>());
-        vec_axpby<float>(*ctx, n, 1.0f, tmp1.as<float>(), 1.0f, (float *)coarse_v);
-      }
-    else
-      {
-        constrained_op<double>(*ctx, coarse, nc, 2, nullptr, tmp1.as<double>());
-        vec_axpby<double>(*ctx, n, 1.0, tmp1.as<double>(), 1.0, (double *)coarse_v);
-      }
+    passes(R, fine, coarse, fine_v, coarse_v, true, true);
   }
 
   void

@@ -647,7 +647,22 @@ namespace mfgpu
     int nc;
     int dir;
     int width; // entries per row
+    // constrained (homogeneous Dirichlet) entries: input entries on a face
+    // whose mask face_in has the component's bit read as 0 (mask_in), and
+    // such output entries get 0 (mask_out, face_out), as the zeroing of a
+    // copy of the input and of the output did before; add: out += result
+    // (constrained outputs untouched)
+    int      mask_in, mask_out, add;
+    unsigned face_in[6], face_out[6];
   };
+
+  // constrained components at node (i0, i1, i2) of a box of ext nodes
+  __device__ __forceinline__ unsigned
+  pass_node_mask(const unsigned (&f)[6], const int (&ext)[3], int i0, int i1, int i2)
+  {
+    return (i0 == 0 ? f[0] : 0u) | (i0 == ext[0] - 1 ? f[1] : 0u) | (i1 == 0 ? f[2] : 0u) |
+           (i1 == ext[1] - 1 ? f[3] : 0u) | (i2 == 0 ? f[4] : 0u) | (i2 == ext[2] - 1 ? f[5] : 0u);
+  }
 
   template <typename T>
   __global__ void
@@ -658,31 +673,46 @@ namespace mfgpu
     const size_t per_c = size_t(pd.ext_out[0]) * pd.ext_out[1] * pd.ext_out[2];
     const size_t total = per_c * pd.nc;
     const size_t in_c  = size_t(pd.ext_in[0]) * pd.ext_in[1] * pd.ext_in[2];
-    size_t       stride_in = 1;
-    for (int d = 0; d < pd.dir; ++d)
-      stride_in *= pd.ext_in[d];
+    const int    dir   = pd.dir;
+    const size_t stride_in = dir == 0 ? size_t(1) : (dir == 1 ? size_t(pd.ext_in[0]) :
+                                                                size_t(pd.ext_in[0]) * pd.ext_in[1]);
     for (size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x; o < total;
          o += size_t(gridDim.x) * blockDim.x)
       {
         const size_t c  = o / per_c;
         size_t       rm = o - c * per_c;
-        int          idx[3];
-        idx[0] = int(rm % pd.ext_out[0]);
+        const int    i0 = int(rm % pd.ext_out[0]);
         rm /= pd.ext_out[0];
-        idx[1] = int(rm % pd.ext_out[1]);
-        idx[2] = int(rm / pd.ext_out[1]);
-        const int r = idx[pd.dir];
-        idx[pd.dir] = 0;
-        const size_t base = c * in_c + size_t(idx[0]) +
-                            size_t(pd.ext_in[0]) * (size_t(idx[1]) + size_t(pd.ext_in[1]) * idx[2]);
-        T s = T(0);
+        const int  i1  = int(rm % pd.ext_out[1]);
+        const int  i2  = int(rm / pd.ext_out[1]);
+        const int  r   = dir == 0 ? i0 : (dir == 1 ? i1 : i2);
+        const bool con = pd.mask_out && ((pass_node_mask(pd.face_out, pd.ext_out, i0, i1, i2) >> c) & 1u);
+        // input node (j0, j1, j2) = the output node with index cc along dir
+        const int    b0   = dir == 0 ? 0 : i0, b1 = dir == 1 ? 0 : i1, b2 = dir == 2 ? 0 : i2;
+        const size_t base = c * in_c + size_t(b0) + size_t(pd.ext_in[0]) * (size_t(b1) + size_t(pd.ext_in[1]) * b2);
+        T            s    = T(0);
         for (int t = 0; t < pd.width; ++t)
           {
             const int cc = col[r * pd.width + t];
             if (cc >= 0)
-              s += val[r * pd.width + t] * in[base + size_t(cc) * stride_in];
+              {
+                T v = in[base + size_t(cc) * stride_in];
+                if (pd.mask_in &&
+                    ((pass_node_mask(pd.face_in, pd.ext_in, dir == 0 ? cc : i0, dir == 1 ? cc : i1,
+                                     dir == 2 ? cc : i2) >>
+                      c) &
+                     1u))
+                  v = T(0);
+                s += val[r * pd.width + t] * v;
+              }
           }
-        out[o] = s;
+        if (pd.add)
+          {
+            if (!con)
+              out[o] += s;
+          }
+        else
+          out[o] = con ? T(0) : s;
       }
   }
 
