@@ -575,8 +575,9 @@ def test_dense_copy_matches_matrix_free(ctx, degree, kind, precision, df64, cach
 def test_dense_copy_row_splits(ctx, precision, rep):
     """Dense copies of 1029, 1911 and 2793 rows (Q6 cantilevers of one to
     three cells) run the dense kernels with 256, 128 and 64 threads per row
-    and rows that start off the 16-byte boundary; each multiplies like the
-    matrix-free operator."""
+    in FP32 and half as many in FP64, on rows padded to 16-byte boundaries;
+    each multiplies like the matrix-free operator, also on an input vector
+    that is not 16-byte aligned (read in scalars)."""
     dt = np.float64 if precision == 64 else np.float32
     tol = 1e-13 if precision == 64 else 2e-6
     spec = W.cantilever(6, 0, rep=rep, length=(float(rep[0]), 1.0, 1.0))
@@ -593,6 +594,12 @@ def test_dense_copy_row_splits(ctx, precision, rep):
     op.set_dense(True)
     op.vmult(dn_x, x)
     assert rel(host(dn_x).astype(np.float64), host(mf_x).astype(np.float64)) < tol
+    # the same input one element into a larger buffer: not 16-byte aligned
+    xs = dev(np.concatenate([[0.0], W.uniform_vector(n, 5, dt)]).astype(dt))[1:]
+    assert xs.data_ptr() % 16 != 0
+    dn_xs = dev(np.zeros(n, dt))
+    op.vmult(dn_xs, xs)
+    assert rel(host(dn_xs).astype(np.float64), host(mf_x).astype(np.float64)) < tol
     op.close()
 
 
